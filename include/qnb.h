@@ -1,0 +1,256 @@
+/*
+ * qnb.h -- C ABI of the GB300 (sm_103a) nonbonded engine for Q6's qdyn.
+ *
+ * The library replaces the bodies of qdyn's nonbonded routines for the
+ * spherical boundary.  Every entry point below names the Q6 routine it
+ * stands in for (paths relative to the Q6 source tree).  qdyn's MD loop,
+ * topology, FEP and .inp files stay unchanged; its Fortran host calls these
+ * functions through iso_c_binding.
+ *
+ * Conventions
+ *  - All indices are 0-based (the Fortran shim subtracts 1 once, at create).
+ *  - Coordinates x and the gradient d are natom x 3 doubles, atom-major
+ *    (x0,y0,z0,x1,...), i.e. the memory layout of qdyn's TYPE(qr_vec) arrays.
+ *  - d is the GRADIENT dU/dx (as in qdyn), and every call ADDS into d and into
+ *    the energy records, it never overwrites them.
+ *  - Multi-dimensional topology arrays use the Fortran (column-major) layout
+ *    of the qdyn global they mirror; the offset formula is given per field.
+ *  - Charges are the values qdyn holds after prep_sim, i.e. already scaled by
+ *    sqrt(coulomb_constant) (Q6 src/simprep.f90:3714-3721).
+ *  - Every function returns a qnb_status; 0 is success.  The library never
+ *    falls back to a CPU path: without a usable CUDA device, qnb_create fails.
+ *  - A context is used by one host thread at a time; all its work is issued on
+ *    one CUDA stream owned by the context.
+ */
+#ifndef QNB_H
+#define QNB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    QNB_OK = 0,
+    QNB_ERR_ARG = 1,        /* invalid argument or topology                    */
+    QNB_ERR_CUDA = 2,       /* CUDA runtime error (message: qnb_last_error)     */
+    QNB_ERR_CAPACITY = 3,   /* a pair-list row overflowed; rebuilt lists larger */
+    QNB_ERR_STATE = 4,      /* call out of order (e.g. energies before lists)   */
+    QNB_ERR_NOMEM = 5,      /* device allocation failed                          */
+    QNB_ERR_UNSUPPORTED = 6 /* topology feature outside this library's scope     */
+};
+
+/* ---- precision forms ---------------------------------------------------- */
+enum {
+    QNB_PREC_FP64 = 0,  /* plain form: all arithmetic in FP64                     */
+    QNB_PREC_MIXED = 1  /* FP32 pair math, 64-bit fixed-point forces/energies,
+                           FP64 cut-off tests, LRF Taylor and energy reductions   */
+};
+
+/* ---- list kinds for qnb_export_pairs ------------------------------------ */
+enum {
+    QNB_LIST_PP = 0,   /* nbpp: solute-solute atom pairs (i, j)               */
+    QNB_LIST_PW = 1,   /* nbpw: solute atom - solvent atom pairs (i, j)       */
+    QNB_LIST_WW = 2,   /* nbww: solvent-solvent atom pairs (i, j)             */
+    QNB_LIST_QP = 3,   /* nbqp: (Q index iq, solute atom j)                   */
+    QNB_LIST_QW = 4,   /* nbqw: (Q index iq, solvent atom j)                  */
+    QNB_LIST_PP14 = 5  /* subset of nbpp that are 1-4 pairs (LJ code 3)       */
+};
+
+/*
+ * Static model description: a 0-based mirror of the qdyn module globals the
+ * nonbonded path reads (Q6 src/globals.f90, src/topo.f90, src/qatom.f90).
+ * The library copies everything at qnb_create and keeps no host pointer.
+ */
+typedef struct qnb_topology {
+    int32_t natom;        /* nat_pro                                          */
+    int32_t nat_solute;   /* solute atoms come first                          */
+    int32_t nwat;         /* solvent molecules, solv_atom atoms each, after   */
+    int32_t solv_atom;    /*   the solute                                     */
+    int32_t solvent_type; /* 0 = SPC (Q6 SOLVENT_SPC), 1 = 3-atom, 2 = general */
+
+    const double*  crg;   /* [natom] scaled charges                           */
+    const int32_t* iac;   /* [natom] atom type, 0..natyps-1                   */
+    const uint8_t* excl;  /* [natom] excluded (frozen/restrained) atoms       */
+    const uint8_t* heavy; /* [natom] mass >= 4 (Q6 src/topo.f90:885-893)      */
+
+    int32_t natyps;
+    const double*  avdw;  /* [natyps*3], avdw[t*3+k] = iaclib(t+1)%avdw(k+1)  */
+    const double*  bvdw;  /* [natyps*3], same layout                          */
+    const uint8_t* ljcod; /* [natyps*natyps], ljcod[ti*natyps+tj] in {1,2}     */
+    int32_t ivdw_rule;    /* 1 geometric, 2 arithmetic                        */
+    double  el14_scale;
+
+    int32_t ncgp;         /* charge groups: solute groups, then one per       */
+    int32_t ncgp_solute;  /*   solvent molecule                               */
+    const int32_t* cgp_first;   /* [ncgp] first slot in cgpatom               */
+    const int32_t* cgp_last;    /* [ncgp] last slot in cgpatom (inclusive)    */
+    const int32_t* cgp_iswitch; /* [ncgp] switch atom                         */
+    const int32_t* cgpatom;     /* [cgp_last[ncgp-1]+1] atom indices          */
+    int32_t iuse_switch_atom;   /* 1: group cut-off by switch atoms (only
+                                   mode supported; 0 returns UNSUPPORTED)      */
+
+    /* solute exclusions (listex + listexlong) and 1-4 pairs (list14 +
+       list14long) as unordered atom pairs; order inside a pair is free       */
+    int32_t nexcl_pairs;  const int32_t* excl_pairs;  /* [n*2] */
+    int32_t n14_pairs;    const int32_t* pairs14;     /* [n*2] */
+
+    /* Q atoms / FEP states (Q6 src/qatom.f90)                               */
+    int32_t nqat, nstates;
+    const int32_t* iqseq;     /* [nqat] atom index of each Q atom             */
+    const double*  qcrg;      /* [nqat*nstates]  qcrg(iq,s) at iq + nqat*s     */
+    const int32_t* qiac;      /* [nqat*nstates]  Q type, 0-based, same layout  */
+    int32_t nqlib;            /* Q atom types                                 */
+    const double*  qavdw;     /* [nqlib*3]  qavdw(t,k) at t*3 + k             */
+    const double*  qbvdw;     /* [nqlib*3]                                    */
+    int32_t qvdw_flag;        /* Q types redefined in the FEP file            */
+    int32_t qq_use_library_charges;
+    const double*  sc_lookup; /* [nqat*(natyps+nqat)*nstates]
+                                 sc_lookup(iq,t,s) at iq + nqat*(t + (natyps+nqat)*s) */
+    const int8_t*  qconn;     /* [nstates*nat_solute*nqat]
+                                 qconn(s,i,iq) at s + nstates*(i + nat_solute*iq)       */
+    int32_t nel_scale;        /* [el_scale] Q-Q electrostatic scaling          */
+    const int32_t* el_scale_pairs; /* [n*2] Q indices                          */
+    const double*  el_scale;       /* [n*nstates], pair p state s at p*nstates+s */
+    int32_t nqexpnb;               /* [soft_pairs]                               */
+    const int32_t* qexpnb_pairs;   /* [n*2] Q indices                            */
+
+    double xpcent[3];   /* solute centre  (Q-atom list cut-off origin)        */
+    double xwcent[3];   /* solvent centre (radial restraint origin)           */
+    double rexcl_o;     /* exclusion radius                                   */
+} qnb_topology;
+
+typedef struct qnb_options {
+    int32_t precision;   /* QNB_PREC_FP64 or QNB_PREC_MIXED                    */
+    int32_t use_lrf;     /* [MD] lrf on/off                                    */
+    int32_t device;      /* CUDA device ordinal                                */
+    int32_t reserved;
+} qnb_options;
+
+/* NB_ENERGIES-like record for the classical terms (Q6 src/nrgy.f90:31-67). */
+typedef struct qnb_energies {
+    double pp_el, pp_vdw;  /* E%pp  */
+    double pw_el, pw_vdw;  /* E%pw  */
+    double ww_el, ww_vdw;  /* E%ww  */
+    double lrf;            /* E%LRF */
+} qnb_energies;
+
+/* Per-state Q-atom record (part of OQ_ENERGIES, unweighted by lambda). */
+typedef struct qnb_qenergies {
+    double qq_el, qq_vdw;
+    double qp_el, qp_vdw;
+    double qw_el, qw_vdw;
+} qnb_qenergies;
+
+/* Spherical-boundary solvent restraint parameters (Q6 src/simprep.f90:4613-4891). */
+typedef struct qnb_solvent_params {
+    double fk_wsphere;   /* radial restraint force constant                    */
+    double Dwmz, awmz;   /* Morse well depth / width                           */
+    double rwat;         /* target solvent sphere radius                       */
+    double boltz;        /* Boltzmann constant (kcal/mol/K)                    */
+    int32_t wpol_restr;  /* polarisation restraint on/off                      */
+    int32_t nwpolr_shell;/* shells (<= 16)                                     */
+    double fkwpol;       /* polarisation force constant                        */
+    double itdis;        /* pol_update interval in steps                       */
+    double shell_rout[16], shell_dr[16], shell_cstb[16];
+    double theta_corr[16]; /* initial theta_corr per shell (restart file)      */
+} qnb_solvent_params;
+
+typedef struct qnb_context qnb_context;
+
+/* Last error message of the calling thread (static storage). */
+const char* qnb_last_error(void);
+
+/* Library/ABI version, e.g. 0x000100 for 0.1.0. */
+int32_t qnb_version(void);
+
+/* Copies the model, precomputes interaction tables (replaces
+   precompute_interactions, src/simprep.f90:2860-2870, and the static Q lists
+   make_nbqqlist/nbqqlist, src/nonbondene.f90:729-745, 3231-3282). */
+int qnb_create(const qnb_topology* topo, const qnb_options* opt, qnb_context** out);
+
+/* Frees every device and host resource of the context. */
+int qnb_destroy(qnb_context* ctx);
+
+/* EQ(:)%lambda for the nstates FEP states (src/md.f90:974-1004). */
+int qnb_set_lambda(qnb_context* ctx, const double* lambda);
+
+/* Replaces make_pair_lists(Rq,Rcq2,RcLRF2,Rcpp2,Rcpw2,Rcww2)
+   (src/nonbondene.f90:749-837, spherical branch): group centres, pp/pw/ww
+   lists with the LRF Taylor coefficients of groups beyond the cut-offs, and
+   the qp/qw lists (kept after their first build when Rcq2 > rexcl_o^2). */
+int qnb_make_pair_lists(qnb_context* ctx, const double* x, double Rq, double Rcq2,
+                        double RcLRF2, double Rcpp2, double Rcpw2, double Rcww2);
+
+/* Replaces pot_energy_nonbonds(E,EQ,md) (src/potene.f90:320-380, sphere
+   branch): ww/qw (SPC fast path when geometric + SPC), pw, pp, qp and the LRF
+   Taylor term.  With md == 0 only the qw and qp terms run, as in the
+   reference.  EQ has nstates records. */
+int qnb_pot_energy_nonbonds(qnb_context* ctx, const double* x, double* d,
+                            qnb_energies* E, qnb_qenergies* EQ, int32_t md);
+
+/* Replaces the calls nonbond_qq + nonbond_qqp (src/potene.f90:176-177). */
+int qnb_nonbond_qq(qnb_context* ctx, const double* x, double* d, qnb_qenergies* EQ);
+
+/* Solvent boundary set-up (wat_sphere / wat_shells results). */
+int qnb_set_solvent_params(qnb_context* ctx, const qnb_solvent_params* p);
+
+/* Replaces restrain_solvent (src/nonbondene.f90:6466-6544).  Tfree is the
+   temperature of the free degrees of freedom from the integrator. */
+int qnb_restrain_solvent(qnb_context* ctx, const double* x, double* d, double Tfree,
+                         double* E_solvent_radial);
+
+/* Replaces watpol(E,md) (src/nonbondene.f90:6548-6746) at MD step istep. */
+int qnb_watpol(qnb_context* ctx, const double* x, double* d, int32_t istep, int32_t md,
+               double* E_water_pol);
+
+/* Current theta_corr, avtheta, avn_insh per shell (the restart-file state
+   and the numbers watpol prints every itdis steps). */
+int qnb_get_watpol_state(qnb_context* ctx, double* theta_corr, double* avtheta,
+                         double* avn_insh);
+
+/* ---- inspection (parity tests, diagnostics) ----------------------------- */
+
+/* Number of atom pairs in list `kind` as the reference would hold them
+   (nbpp_pair, nbpw_pair, nbww_pair, nbqp_pair, nbqw_pair). */
+int qnb_list_size(qnb_context* ctx, int32_t kind, int64_t* n);
+
+/* Writes the atom pairs of list `kind` (order unspecified) into i/j
+   (capacity cap); *n receives the count.  QNB_ERR_CAPACITY if cap < count. */
+int qnb_export_pairs(qnb_context* ctx, int32_t kind, int32_t* i, int32_t* j,
+                     int64_t cap, int64_t* n);
+
+/* LRF records as 43 doubles per charge group in the order of LRF_TYPE
+   (src/globals.f90:503-509): cgp_cent(3), phi0, phi1(3), phi2(9), phi3(27). */
+int qnb_get_lrf(qnb_context* ctx, double* lrf);
+
+/* ---- device-resident interface (same work, inputs already in HBM) -------- */
+
+/* Device buffers owned by the context: coordinates (natom*3 doubles) and the
+   gradient accumulator (natom*3 doubles).  The *_dev entry points below read
+   x from x_dev and add into d_dev without host copies. */
+int qnb_device_buffers(qnb_context* ctx, double** x_dev, double** d_dev);
+
+/* Stream the context issues its work on (cudaStream_t). */
+int qnb_stream(qnb_context* ctx, void** stream);
+
+int qnb_make_pair_lists_dev(qnb_context* ctx, double Rq, double Rcq2, double RcLRF2,
+                            double Rcpp2, double Rcpw2, double Rcww2);
+
+/* One full nonbonded evaluation on device data: pot_energy_nonbonds(md=1),
+   nonbond_qq/qqp, restrain_solvent and watpol.  Energies are reduced on
+   device; they are copied to E/EQ/Erst (if non-NULL) only when sync != 0.
+   Erst[0] = solvent_radial, Erst[1] = water_pol. */
+int qnb_compute_dev(qnb_context* ctx, double Tfree, int32_t istep, int32_t sync,
+                    qnb_energies* E, qnb_qenergies* EQ, double* Erst);
+
+/* Number of kernel launches the context issued since the last call. */
+int qnb_take_launch_count(qnb_context* ctx, int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QNB_H */

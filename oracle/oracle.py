@@ -1,0 +1,192 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes wrapper of the CPU FP64 oracle.
+
+The oracle (``oracle/qnb_oracle.c``) restates Q6 qdyn's nonbonded path on the
+CPU in strict FP64.  It is the checker for the CUDA engine and the CPU
+baseline of the benchmark; the product package never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "qnb_oracle.c")
+
+# strict IEEE double: no FMA contraction, no fast-math
+CFLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+          "-fno-associative-math", "-Wall", "-Wno-unused-function"]
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        subprocess.check_call(["gcc", *CFLAGS, "-o", LIB, SRC, "-lm"])
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        D = ctypes.c_double
+        I = ctypes.c_int
+        L.orc_create.restype = P
+        L.orc_create.argtypes = [P, I]
+        L.orc_destroy.argtypes = [P]
+        L.orc_set_lambda.argtypes = [P, P]
+        L.orc_make_pair_lists.argtypes = [P, P, D, D, D, D, D, D]
+        L.orc_pot_energy_nonbonds.argtypes = [P, P, P, P, P, I]
+        L.orc_nonbond_qq.argtypes = [P, P, P, P]
+        L.orc_set_solvent_params.argtypes = [P, P]
+        L.orc_restrain_solvent.argtypes = [P, P, P, D, P]
+        L.orc_watpol.argtypes = [P, P, P, I, I, P]
+        L.orc_get_watpol_state.argtypes = [P, P, P, P]
+        L.orc_list_size.restype = ctypes.c_long
+        L.orc_list_size.argtypes = [P, I]
+        L.orc_export_pairs.restype = ctypes.c_long
+        L.orc_export_pairs.argtypes = [P, I, P, P]
+        L.orc_get_lrf.argtypes = [P, P]
+        L.orc_shake.restype = ctypes.c_long
+        L.orc_shake.argtypes = [P, P, I, P, P, P, P, P]
+        L.orc_static_qq_size.restype = ctypes.c_long
+        L.orc_static_qq_size.argtypes = [P, I, I]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Oracle:
+    """Mirror of the reference call sequence on one system."""
+
+    E_FIELDS = ("pp_el", "pp_vdw", "pw_el", "pw_vdw", "ww_el", "ww_vdw", "lrf")
+    Q_FIELDS = ("qq_el", "qq_vdw", "qp_el", "qp_vdw", "qw_el", "qw_vdw")
+
+    def __init__(self, system, use_lrf: bool = True):
+        from q6_gb300.system import TopologyHandle
+        self.s = system
+        self.topo = TopologyHandle(system)
+        self.h = lib().orc_create(self.topo.ptr(), int(use_lrf))
+        self.S = system.nstates
+
+    def close(self):
+        if self.h:
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_lambda(self, lam):
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        lib().orc_set_lambda(self.h, _p(lam))
+
+    def make_pair_lists(self, x, Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        lib().orc_make_pair_lists(self.h, _p(x), Rcq, Rcq ** 2, RcLRF ** 2, Rcpp ** 2,
+                                  Rcpw ** 2, Rcww ** 2)
+
+    def pot_energy_nonbonds(self, x, d=None, md=True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if d is None:
+            d = np.zeros_like(x)
+        E = np.zeros(7)
+        EQ = np.zeros((self.S, 6))
+        lib().orc_pot_energy_nonbonds(self.h, _p(x), _p(d), _p(E), _p(EQ), int(md))
+        return d, dict(zip(self.E_FIELDS, E)), EQ
+
+    def nonbond_qq(self, x, d=None, EQ=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if d is None:
+            d = np.zeros_like(x)
+        if EQ is None:
+            EQ = np.zeros((self.S, 6))
+        lib().orc_nonbond_qq(self.h, _p(x), _p(d), _p(EQ))
+        return d, EQ
+
+    def set_solvent_params(self, p):
+        lib().orc_set_solvent_params(self.h, ctypes.byref(p))
+
+    def restrain_solvent(self, x, d, Tfree):
+        e = np.zeros(1)
+        lib().orc_restrain_solvent(self.h, _p(np.ascontiguousarray(x)), _p(d), Tfree, _p(e))
+        return float(e[0])
+
+    def watpol(self, x, d, istep, md=True):
+        e = np.zeros(1)
+        lib().orc_watpol(self.h, _p(np.ascontiguousarray(x)), _p(d), int(istep), int(md), _p(e))
+        return float(e[0])
+
+    def watpol_state(self):
+        a, b, c = np.zeros(16), np.zeros(16), np.zeros(16)
+        lib().orc_get_watpol_state(self.h, _p(a), _p(b), _p(c))
+        return a, b, c
+
+    def list_size(self, kind):
+        return int(lib().orc_list_size(self.h, kind))
+
+    def export_pairs(self, kind):
+        n = self.list_size(kind)
+        i = np.zeros(max(n, 1), np.int32)
+        j = np.zeros(max(n, 1), np.int32)
+        m = lib().orc_export_pairs(self.h, kind, _p(i), _p(j))
+        return i[:m], j[:m]
+
+    def lrf(self):
+        out = np.zeros((self.s.ncgp, 43))
+        lib().orc_get_lrf(self.h, _p(out))
+        return out
+
+    def evaluate(self, x, lam, cut=None, solvent=None, Tfree=300.0, istep=0, lists=True):
+        """One full nonbonded evaluation in the reference's call order."""
+        cut = cut or {}
+        self.set_lambda(lam)
+        if lists:
+            self.make_pair_lists(x, **cut)
+        d, E, EQ = self.pot_energy_nonbonds(x)
+        d, EQ = self.nonbond_qq(x, d, EQ)
+        erst = [0.0, 0.0]
+        if solvent is not None:
+            erst[0] = self.restrain_solvent(x, d, Tfree)
+            if solvent.wpol_restr:
+                erst[1] = self.watpol(x, d, istep, True)
+        return d, E, EQ, erst
+
+
+def shake(x, molecules, winv):
+    """SHAKE of qdyn's initial_constraint (Q6 src/bondene.f90:1025-1048,
+    1069-1150): ``molecules`` is a list of [(i, j, b0), ...] per molecule in
+    topology bond order; returns the corrected copy of x."""
+    x = np.ascontiguousarray(x, dtype=np.float64).copy()
+    xx = x.copy()
+    starts, ci, cj, d2 = [0], [], [], []
+    for mol in molecules:
+        for i, j, b0 in mol:
+            ci.append(i)
+            cj.append(j)
+            d2.append(b0 * b0)
+        starts.append(len(ci))
+    starts = np.array(starts, np.int32)
+    ci = np.array(ci, np.int32)
+    cj = np.array(cj, np.int32)
+    d2 = np.array(d2, np.float64)
+    winv = np.ascontiguousarray(winv, dtype=np.float64)
+    n = lib().orc_shake(_p(x), _p(xx), len(molecules), _p(starts), _p(ci), _p(cj), _p(d2), _p(winv))
+    if n < 0:
+        raise RuntimeError("shake failure")
+    return x
