@@ -1,0 +1,228 @@
+"""Python host mirror of qdyn's nonbonded call sequence over the C ABI.
+
+``NonbondedEngine`` exposes the reference routines this library replaces with
+the same names and argument meaning (Q6 src/nonbondene.f90, src/potene.f90):
+``make_pair_lists``, ``pot_energy_nonbonds``, ``nonbond_qq``,
+``restrain_solvent`` and ``watpol``.  Gradients are ADDED into the array the
+caller passes, energies are returned per term and per FEP state.
+
+There is no CPU path: without the CUDA library or a CUDA device the
+constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .system import QnbSolventParams, QSystem, TopologyHandle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libqnb.so")
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+LIST_PP, LIST_PW, LIST_WW, LIST_QP, LIST_QW, LIST_PP14 = range(6)
+
+E_FIELDS = ("pp_el", "pp_vdw", "pw_el", "pw_vdw", "ww_el", "ww_vdw", "lrf")
+Q_FIELDS = ("qq_el", "qq_vdw", "qp_el", "qp_vdw", "qw_el", "qw_vdw")
+
+EXPORTED = (
+    "qnb_last_error", "qnb_version", "qnb_create", "qnb_destroy", "qnb_set_lambda",
+    "qnb_make_pair_lists", "qnb_pot_energy_nonbonds", "qnb_nonbond_qq",
+    "qnb_set_solvent_params", "qnb_restrain_solvent", "qnb_watpol", "qnb_get_watpol_state",
+    "qnb_list_size", "qnb_export_pairs", "qnb_get_lrf", "qnb_device_buffers", "qnb_stream",
+    "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_take_launch_count",
+)
+
+
+class QnbError(RuntimeError):
+    pass
+
+
+class QnbOptions(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("use_lrf", ctypes.c_int32),
+                ("device", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libqnb.so (built by ``q6_gb300.build``); raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise QnbError(f"CUDA library {path} not built: run `python -m q6_gb300.build`")
+    L = ctypes.CDLL(path)
+    P, D, I32, I64 = ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_int64
+    L.qnb_last_error.restype = ctypes.c_char_p
+    L.qnb_version.restype = I32
+    sig = {
+        "qnb_create": [P, P, P], "qnb_destroy": [P], "qnb_set_lambda": [P, P],
+        "qnb_make_pair_lists": [P, P, D, D, D, D, D, D],
+        "qnb_make_pair_lists_dev": [P, D, D, D, D, D, D],
+        "qnb_pot_energy_nonbonds": [P, P, P, P, P, I32],
+        "qnb_nonbond_qq": [P, P, P, P], "qnb_set_solvent_params": [P, P],
+        "qnb_restrain_solvent": [P, P, P, D, P], "qnb_watpol": [P, P, P, I32, I32, P],
+        "qnb_get_watpol_state": [P, P, P, P], "qnb_list_size": [P, I32, P],
+        "qnb_export_pairs": [P, I32, P, P, I64, P], "qnb_get_lrf": [P, P],
+        "qnb_device_buffers": [P, P, P], "qnb_stream": [P, P],
+        "qnb_compute_dev": [P, D, I32, I32, P, P, P], "qnb_take_launch_count": [P, P],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class NonbondedEngine:
+    """One qdyn system on one GPU (one CUDA stream)."""
+
+    def __init__(self, system: QSystem, precision: int = PREC_FP64, use_lrf: bool = True,
+                 device: int = 0):
+        self.lib = load_library()
+        self.s = system
+        self.S = system.nstates
+        self.topo = TopologyHandle(system)
+        opt = QnbOptions(precision, int(use_lrf), device, 0)
+        h = ctypes.c_void_p()
+        self._check(self.lib.qnb_create(self.topo.ptr(), ctypes.byref(opt), ctypes.byref(h)))
+        self.h = h
+        self.precision = precision
+
+    def _check(self, rc):
+        if rc != 0:
+            raise QnbError(f"qnb error {rc}: {self.lib.qnb_last_error().decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qnb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- reference routines ---------------------------------------------
+    def set_lambda(self, lam):
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        self._check(self.lib.qnb_set_lambda(self.h, _p(lam)))
+
+    def make_pair_lists(self, x, Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        self._check(self.lib.qnb_make_pair_lists(self.h, _p(x), Rcq, Rcq ** 2, RcLRF ** 2,
+                                                 Rcpp ** 2, Rcpw ** 2, Rcww ** 2))
+
+    def pot_energy_nonbonds(self, x, d=None, md=True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if d is None:
+            d = np.zeros_like(x)
+        E = np.zeros(7)
+        EQ = np.zeros((max(self.S, 1), 6))
+        self._check(self.lib.qnb_pot_energy_nonbonds(self.h, _p(x), _p(d), _p(E), _p(EQ), int(md)))
+        return d, dict(zip(E_FIELDS, E)), EQ[: self.S]
+
+    def nonbond_qq(self, x, d=None, EQ=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if d is None:
+            d = np.zeros_like(x)
+        EQ = np.zeros((max(self.S, 1), 6)) if EQ is None else np.ascontiguousarray(EQ, dtype=np.float64)
+        self._check(self.lib.qnb_nonbond_qq(self.h, _p(x), _p(d), _p(EQ)))
+        return d, EQ[: self.S]
+
+    def set_solvent_params(self, p: QnbSolventParams):
+        self._check(self.lib.qnb_set_solvent_params(self.h, ctypes.byref(p)))
+
+    def restrain_solvent(self, x, d, Tfree):
+        e = np.zeros(1)
+        self._check(self.lib.qnb_restrain_solvent(self.h, _p(np.ascontiguousarray(x)), _p(d), Tfree, _p(e)))
+        return float(e[0])
+
+    def watpol(self, x, d, istep, md=True):
+        e = np.zeros(1)
+        self._check(self.lib.qnb_watpol(self.h, _p(np.ascontiguousarray(x)), _p(d), int(istep), int(md), _p(e)))
+        return float(e[0])
+
+    def watpol_state(self):
+        a, b, c = np.zeros(16), np.zeros(16), np.zeros(16)
+        self._check(self.lib.qnb_get_watpol_state(self.h, _p(a), _p(b), _p(c)))
+        return a, b, c
+
+    # ---- inspection --------------------------------------------------------
+    def list_size(self, kind):
+        n = ctypes.c_int64()
+        self._check(self.lib.qnb_list_size(self.h, kind, ctypes.byref(n)))
+        return int(n.value)
+
+    def export_pairs(self, kind):
+        n = self.list_size(kind)
+        i = np.zeros(max(n, 1), np.int32)
+        j = np.zeros(max(n, 1), np.int32)
+        m = ctypes.c_int64()
+        self._check(self.lib.qnb_export_pairs(self.h, kind, _p(i), _p(j), n, ctypes.byref(m)))
+        return i[:m.value], j[:m.value]
+
+    def lrf(self):
+        out = np.zeros((self.s.ncgp, 43))
+        self._check(self.lib.qnb_get_lrf(self.h, _p(out)))
+        return out
+
+    def launches(self):
+        n = ctypes.c_int64()
+        self._check(self.lib.qnb_take_launch_count(self.h, ctypes.byref(n)))
+        return int(n.value)
+
+    # ---- device-resident interface ------------------------------------------
+    def device_buffers(self):
+        x = ctypes.c_void_p()
+        d = ctypes.c_void_p()
+        self._check(self.lib.qnb_device_buffers(self.h, ctypes.byref(x), ctypes.byref(d)))
+        return x.value, d.value
+
+    def stream(self):
+        st = ctypes.c_void_p()
+        self._check(self.lib.qnb_stream(self.h, ctypes.byref(st)))
+        return st.value
+
+    def make_pair_lists_dev(self, Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0):
+        self._check(self.lib.qnb_make_pair_lists_dev(self.h, Rcq, Rcq ** 2, RcLRF ** 2, Rcpp ** 2,
+                                                     Rcpw ** 2, Rcww ** 2))
+
+    def compute_dev(self, Tfree=300.0, istep=0, sync=True):
+        E = np.zeros(7)
+        EQ = np.zeros((max(self.S, 1), 6))
+        R = np.zeros(2)
+        self._check(self.lib.qnb_compute_dev(self.h, Tfree, int(istep), int(sync), _p(E), _p(EQ), _p(R)))
+        return dict(zip(E_FIELDS, E)), EQ[: self.S], R
+
+    def evaluate(self, x, lam, cut=None, solvent=None, Tfree=300.0, istep=0, lists=True):
+        """One full nonbonded evaluation in the reference's call order."""
+        cut = cut or {}
+        self.set_lambda(lam)
+        if lists:
+            self.make_pair_lists(x, **cut)
+        d, E, EQ = self.pot_energy_nonbonds(x)
+        d, EQ = self.nonbond_qq(x, d, EQ)
+        erst = [0.0, 0.0]
+        if solvent is not None:
+            erst[0] = self.restrain_solvent(x, d, Tfree)
+            if solvent.wpol_restr:
+                erst[1] = self.watpol(x, d, istep, True)
+        return d, E, EQ, erst
