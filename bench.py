@@ -1,0 +1,403 @@
+#!/usr/bin/env python3
+"""Benchmark of the qdyn nonbonded hot path on GB300.
+
+Metric: MD steps/s summed over lambda windows (BASELINE metric), mixed form.
+Workload: 51 lambda windows (lambda = 0, 0.02, ..., 1) of the seeded 25 A,
+2-state sphere (3,000-atom synthetic solute in 3-6-atom charge groups, 12 LJ
+types, 20 Q atoms, SPC water filling the sphere), 10 A cut-offs, Rcq 99,
+LRF on, pair lists rebuilt every 25 steps.  A step is one nonbonded MD step of
+the path: list rebuild (every 25th step), pot_energy_nonbonds (ww, qw, pw,
+pp, qp, LRF Taylor), nonbond_qq/qqp, restrain_solvent and watpol.  Inputs
+(coordinates, topology) are resident in HBM; every timed step is preceded by
+an L2 flush (a 256 MB write) outside its CUDA-event bracket.
+
+--impl reference times the CPU restatement of the reference (oracle/, serial C
+FP64) on all host cores, one process per window as the reference's own
+lambda-window workflow runs, on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NBCYCLE = 25
+CUT = dict(Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
+METRIC = "MD steps/s summed over lambda windows (nonbonded hot path, mixed precision)"
+# algorithmic FP32 flops per unit (FMA = 2, rsqrt/rcp = 1)
+FLOPS = {"pp_atom_pair": 33, "ww_mol_pair": 209, "pw_atom_water": 77}
+
+
+def window_lambdas(n):
+    return [(w / (n - 1) if n > 1 else 0.5) for w in range(n)]
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.p is None:
+            return out
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [ln.split(",") for ln in open(self.f.name).read().strip().splitlines() if ln.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        if sm:
+            out["sm_mhz"] = statistics.median(sm)
+            out["sm_max_mhz"] = float(rows[0][2])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].strip() == "Active" and nm not in out["reasons"]:
+                    out["reasons"].append(nm)
+        out["samples"] = len(rows)
+        return out
+
+
+def make_window_system(seed=2000):
+    from q6_gb300.system import config_window
+    return config_window(seed)
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    from q6_gb300 import build as qbuild
+    from q6_gb300.qnb import KERNEL_CLASSES, PREC_FP64, PREC_MIXED, NonbondedEngine
+    from q6_gb300.system import default_solvent_params, lambdas_for_window
+
+    qbuild.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    s = make_window_system()
+    sp = default_solvent_params(s)
+    nwin = args.windows
+    lams = window_lambdas(nwin)
+    rng = np.random.default_rng(1234 + rank)
+    prec = PREC_MIXED if args.prec == "mixed" else PREC_FP64
+    eng = NonbondedEngine(s, precision=prec, device=local, windows=nwin)
+    eng.set_solvent_params(sp)
+    for w in range(nwin):
+        eng.set_lambda(lambdas_for_window(lams[w], s.nstates), window=w)
+    xs = np.stack([s.x + rng.normal(0.0, 0.01, size=s.x.shape) for _ in range(nwin)])  # distinct frames
+    eng.set_coordinates_dev(xs)
+    eng.make_pair_lists_dev(**CUT)
+    stream = torch.cuda.ExternalStream(eng.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step(istep):
+        if istep % NBCYCLE == 0:
+            eng.make_pair_lists_dev(**CUT)
+        eng.compute_dev(Tfree=300.0, istep=istep, sync=False)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    eng.launches()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    eng.profile(True)
+    total_ms = 0.0
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for k in range(args.steps):
+        istep = args.warmup + k
+        with torch.cuda.stream(stream):
+            flush.zero_()            # L2 flush, outside the timed bracket
+            ev0.record(stream)
+        step(istep)
+        ev1.record(stream)
+        ev1.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ktimes = eng.kernel_times()
+    eng.profile(False)
+    launches = eng.launches()
+    t_local = total_ms
+    if world > 1:
+        t = torch.tensor([t_local], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_local = float(t.item())
+        torch.distributed.barrier()
+    ms_per_step = t_local / args.steps
+    value = world * nwin * args.steps / (t_local / 1e3)
+    counts = {k: eng.list_size(i) for i, k in enumerate(("pp", "pw", "ww", "qp", "qw", "pp14"))}
+
+    # ---- roofline of the dominant kernel class (live CUDA events) ---------
+    step_classes = [c for c in KERNEL_CLASSES if ktimes[c][1] > 0]
+    dom = max(step_classes, key=lambda c: ktimes[c][0])
+    dom_ms, dom_n = ktimes[dom]
+    dom_avg_s = dom_ms / 1e3 / max(dom_n, 1)
+    bytes_per_unit = 4.0   # list streaming: 4 B per atom pair read once per step
+    per_win = {"pp": counts["pp"], "pw": counts["pw"], "ww": counts["ww"],
+               "qp": counts["qp"] * s.nstates, "qw": counts["qw"] * s.nstates}.get(dom)
+    units = per_win * nwin if per_win else None   # one launch covers every window
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    ach = bytes_per_unit * units / dom_avg_s / 1e9 if units else None
+    roof = {"kernel": dom, "bound": "hbm", "achieved": round(ach, 3) if ach else None, "peak": hbm_peak,
+            "unit": "GB/s", "frac": round(ach / hbm_peak, 6) if ach else None, "traffic": read_traffic(dom),
+            "peak_source": peak_src, "units_per_launch": units, "bytes_per_unit": bytes_per_unit,
+            "avg_launch_us": round(dom_avg_s * 1e6, 2)}
+    pair_interactions = counts["pp"] + counts["pw"] + counts["ww"] + (counts["qp"] + counts["qw"]) * s.nstates
+    eng.close()
+
+    e2e = run_e2e(args, s, sp, lams, prec, local)
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 pair math, i64 fixed-point forces, f64 cut-offs/LRF/energies",
+        "data": "synthetic seeded sphere (no dataset)",
+        "config": {"workload": f"{nwin} lambda windows x R25 2-state sphere ({s.natom} atoms, "
+                               f"{s.nwat} SPC, {s.nat_solute}-atom solute, {s.nqat} Q)",
+                   "windows_per_gpu": nwin, "natom": s.natom, "nbcycle": NBCYCLE,
+                   "cutoffs": CUT, "precision": args.prec, "l2": "flushed (256 MB write) before every timed step",
+                   "step": "list rebuild every 25th step + pot_energy_nonbonds + nonbond_qq/qqp + "
+                           "restrain_solvent + watpol (no integrator or bonded terms: outside the path)",
+                   "parallelism": f"replicas: {nwin} windows per GPU in one batched context (each kernel "
+                                  f"launch covers all windows), one GPU per rank"},
+        "pair_interactions_per_step_per_window": pair_interactions,
+        "pair_interactions_per_s": round(pair_interactions * value, 1),
+        "list_sizes_window0": counts,
+        "kernel_ms_total": {k: round(v[0], 4) for k, v in ktimes.items() if v[1]},
+        "roofline": roof,
+        "clocks": clk,
+        "e2e": e2e,
+        "gpu_launches": launches,
+    }
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(s, sp, args)
+        if args.fp64_compare:
+            out["fp64_value"] = fp64_compare(args, s, sp, lams, local)
+            out["mixed_over_fp64"] = round(out["value"] / out["fp64_value"], 3) if out["fp64_value"] else None
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def read_traffic(kernel):
+    """dram bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for ln in open(p):
+        ln = ln.strip()
+        if ln.startswith(kernel + " "):
+            try:
+                return float(ln.split()[1])
+            except ValueError:
+                return None
+    return None
+
+
+def run_e2e(args, s, sp, lams, prec, local):
+    """Same metric through the host-buffer calls a Fortran shim makes, one
+    context per window as one qdyn process per window would hold:
+    make_pair_lists (every 25th step), pot_energy_nonbonds, nonbond_qq,
+    restrain_solvent, watpol; each copies x in and the gradient out."""
+    import numpy as np
+    from q6_gb300.qnb import NonbondedEngine
+    from q6_gb300.system import lambdas_for_window
+    nwin = min(args.windows, 8)
+    steps = max(4, min(args.steps, 50))
+    engs = []
+    for w in range(nwin):
+        e = NonbondedEngine(s, precision=prec, device=local)
+        e.set_solvent_params(sp)
+        e.set_lambda(lambdas_for_window(lams[w], s.nstates))
+        engs.append(e)
+    xs = [s.x.copy() for _ in range(nwin)]
+    ds = [np.zeros_like(s.x) for _ in range(nwin)]
+    for w, e in enumerate(engs):       # warm-up: first list build
+        e.make_pair_lists(xs[w], **CUT)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        for w, eng in enumerate(engs):
+            x, d = xs[w], ds[w]
+            d[:] = 0.0
+            if k % NBCYCLE == 0:
+                eng.make_pair_lists(x, **CUT)
+            d, E, EQ = eng.pot_energy_nonbonds(x, d)
+            d, EQ = eng.nonbond_qq(x, d, EQ)
+            eng.restrain_solvent(x, d, 300.0)
+            eng.watpol(x, d, k)
+    dt = time.perf_counter() - t0
+    for e in engs:
+        e.close()
+    nbytes = s.x.nbytes
+    h2d = nbytes * (4 + 1.0 / NBCYCLE)
+    d2h = nbytes * 4
+    return {"value": round(nwin * steps / dt, 2), "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "windows": nwin, "steps": steps,
+            "path": "qnb_make_pair_lists/qnb_pot_energy_nonbonds/qnb_nonbond_qq/qnb_restrain_solvent/"
+                    "qnb_watpol with host buffers, one context per window"}
+
+
+def fp64_compare(args, s, sp, lams, local):
+    """Plain FP64 form on the same workload (25 steps with one list build)."""
+    import numpy as np
+    import torch
+    from q6_gb300.qnb import PREC_FP64, NonbondedEngine
+    from q6_gb300.system import lambdas_for_window
+    nwin = args.windows
+    e = NonbondedEngine(s, precision=PREC_FP64, device=local, windows=nwin)
+    e.set_solvent_params(sp)
+    for w in range(nwin):
+        e.set_lambda(lambdas_for_window(lams[w], s.nstates), window=w)
+    e.set_coordinates_dev(np.stack([s.x] * nwin))
+    e.make_pair_lists_dev(**CUT)
+    for i in range(3):
+        e.compute_dev(istep=i, sync=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(NBCYCLE):
+        if k % NBCYCLE == 0:
+            e.make_pair_lists_dev(**CUT)
+        e.compute_dev(istep=k, sync=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    e.close()
+    return round(nwin * NBCYCLE / dt, 2)
+
+
+def _oracle_window(payload):
+    """One lambda window of the CPU restatement: `steps` nonbonded steps with a
+    list rebuild every 25th step.  Returns (steps, seconds)."""
+    import pickle
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import Oracle
+    s, sp_bytes, lam, steps = pickle.loads(payload)
+    from q6_gb300.system import QnbSolventParams, lambdas_for_window
+    sp = QnbSolventParams.from_buffer_copy(sp_bytes)
+    o = Oracle(s)
+    o.set_solvent_params(sp)
+    o.set_lambda(lambdas_for_window(lam, s.nstates))
+    t0 = time.perf_counter()
+    for k in range(steps):
+        if k % NBCYCLE == 0:
+            o.make_pair_lists(s.x, **CUT)
+        d, E, EQ = o.pot_energy_nonbonds(s.x)
+        d, EQ = o.nonbond_qq(s.x, d, EQ)
+        o.restrain_solvent(s.x, d, 300.0)
+        o.watpol(s.x, d, k)
+    return steps, time.perf_counter() - t0
+
+
+def cpu_baseline(s, sp, args):
+    """Serial oracle (1 core) on a bounded sample of one window: 2 list builds
+    and 50 steps (about 10-20 s on one core)."""
+    import pickle
+    from oracle import oracle as orc
+    orc.build()
+    steps = 2 * NBCYCLE
+    n, dt = _oracle_window(pickle.dumps((s, bytes(sp), 0.5, steps)))
+    return {"value": round(n / dt, 4), "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": f"1 window x {steps} steps (2 list builds), serial C FP64 restatement, -O2"}
+
+
+def run_reference(args, rank, world):
+    """CPU reference arm: the oracle on all host cores, one process per window."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    import pickle
+    from oracle import oracle as orc
+    from q6_gb300.system import default_solvent_params
+    orc.build()
+    s = make_window_system()
+    sp = default_solvent_params(s)
+    cores = os.cpu_count() or 1
+    nwin = min(args.windows, cores)
+    lams = window_lambdas(args.windows)[:nwin]
+    steps = max(NBCYCLE, min(args.steps, 50))
+    payloads = [pickle.dumps((s, bytes(sp), lam, steps)) for lam in lams]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(nwin) as pool:
+        res = pool.map(_oracle_window, payloads)
+    wall = time.perf_counter() - t0
+    # per-window rates; wall time includes process start-up, so use the
+    # slowest window's own compute time
+    slowest = max(r[1] for r in res)
+    value = sum(r[0] for r in res) / slowest
+    out = {"metric": METRIC, "value": round(value, 4), "unit": "steps/s", "n_gpus": world,
+           "steps": steps, "warmup": 0, "ms_per_step": round(slowest / steps * 1e3, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "impl": "reference",
+           "dtype": "f64", "data": "synthetic seeded sphere (no dataset)",
+           "config": {"workload": f"{nwin} lambda windows x R25 2-state sphere ({s.natom} atoms)",
+                      "windows": nwin, "nbcycle": NBCYCLE, "cutoffs": CUT,
+                      "note": "Q6 qdyn (Fortran) cannot be built on this pool (no gfortran); the "
+                              "serial C restatement in oracle/ runs one process per window"},
+           "cpu_baseline": {"value": round(value, 4), "unit": "steps/s", "cores": nwin, "kind": "port",
+                            "sample": f"{nwin} windows x {steps} steps, one process per window"},
+           "e2e": {"value": round(value, 4), "unit": "steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0},
+           "wall_s": round(wall, 2)}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--windows", type=int, default=51)
+    ap.add_argument("--prec", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-fp64-compare", dest="fp64_compare", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -163,7 +163,7 @@ typedef struct qnb_context qnb_context;
 /* Last error message of the calling thread (static storage). */
 const char* qnb_last_error(void);
 
-/* Library/ABI version, e.g. 0x000100 for 0.1.0. */
+/* Library/ABI version, e.g. 0x000200 for 0.2.0. */
 int32_t qnb_version(void);
 
 /* Copies the model, precomputes interaction tables (replaces
@@ -171,11 +171,27 @@ int32_t qnb_version(void);
    make_nbqqlist/nbqqlist, src/nonbondene.f90:729-745, 3231-3282). */
 int qnb_create(const qnb_topology* topo, const qnb_options* opt, qnb_context** out);
 
+/* A context holding nwin lambda windows (or replicas) of the same topology,
+   each with its own coordinates, lambdas, pair lists, LRF records and
+   accumulators.  The *_dev entry points below process every window in the
+   same kernel launches (grid.y = window).  The host-buffer entry points
+   (qnb_make_pair_lists ... qnb_watpol) act on window 0, which is what one
+   qdyn process per window uses.  No counterpart in the reference, which runs
+   one process per window (tests/exclude_tests/inputs/excl/gen_inps.pl). */
+int qnb_create_batch(const qnb_topology* topo, const qnb_options* opt, int32_t nwin, qnb_context** out);
+
+/* Number of windows of the context. */
+int qnb_window_count(qnb_context* ctx, int32_t* nwin);
+
 /* Frees every device and host resource of the context. */
 int qnb_destroy(qnb_context* ctx);
 
-/* EQ(:)%lambda for the nstates FEP states (src/md.f90:974-1004). */
+/* EQ(:)%lambda for the nstates FEP states (src/md.f90:974-1004), for every
+   window of the context. */
 int qnb_set_lambda(qnb_context* ctx, const double* lambda);
+
+/* The same for window w only. */
+int qnb_set_lambda_window(qnb_context* ctx, int32_t w, const double* lambda);
 
 /* Replaces make_pair_lists(Rq,Rcq2,RcLRF2,Rcpp2,Rcpw2,Rcww2)
    (src/nonbondene.f90:749-837, spherical branch): group centres, pp/pw/ww
@@ -228,10 +244,18 @@ int qnb_get_lrf(qnb_context* ctx, double* lrf);
 
 /* ---- device-resident interface (same work, inputs already in HBM) -------- */
 
-/* Device buffers owned by the context: coordinates (natom*3 doubles) and the
-   gradient accumulator (natom*3 doubles).  The *_dev entry points below read
-   x from x_dev and add into d_dev without host copies. */
+/* Device buffers owned by the context: coordinates and gradient
+   accumulators of all windows, nwin x natom x 3 doubles each, window-major.
+   The *_dev entry points below read x from x_dev and add into d_dev without
+   host copies. */
 int qnb_device_buffers(qnb_context* ctx, double** x_dev, double** d_dev);
+
+/* Copies host coordinates of all windows (nwin x natom x 3) into x_dev. */
+int qnb_upload_coordinates(qnb_context* ctx, const double* x_all);
+
+/* Copies the gradient accumulators of all windows into d_all (nwin x natom
+   x 3); clears them on the device when clear != 0. */
+int qnb_download_gradient(qnb_context* ctx, double* d_all, int32_t clear);
 
 /* Stream the context issues its work on (cudaStream_t). */
 int qnb_stream(qnb_context* ctx, void** stream);
@@ -239,15 +263,32 @@ int qnb_stream(qnb_context* ctx, void** stream);
 int qnb_make_pair_lists_dev(qnb_context* ctx, double Rq, double Rcq2, double RcLRF2,
                             double Rcpp2, double Rcpw2, double Rcww2);
 
-/* One full nonbonded evaluation on device data: pot_energy_nonbonds(md=1),
-   nonbond_qq/qqp, restrain_solvent and watpol.  Energies are reduced on
-   device; they are copied to E/EQ/Erst (if non-NULL) only when sync != 0.
-   Erst[0] = solvent_radial, Erst[1] = water_pol. */
+/* One full nonbonded evaluation of every window on device data:
+   pot_energy_nonbonds(md=1), nonbond_qq/qqp, restrain_solvent and watpol.
+   Energies are reduced on device; they are added to E[nwin], EQ[nwin*nstates]
+   and Erst[nwin*2] (if non-NULL) only when sync != 0.
+   Erst[2w] = solvent_radial, Erst[2w+1] = water_pol of window w. */
 int qnb_compute_dev(qnb_context* ctx, double Tfree, int32_t istep, int32_t sync,
                     qnb_energies* E, qnb_qenergies* EQ, double* Erst);
 
 /* Number of kernel launches the context issued since the last call. */
 int qnb_take_launch_count(qnb_context* ctx, int64_t* n);
+
+/* ---- event profiler (diagnostics; no counterpart in the reference) -------- */
+/* Kernel classes, in the order qnb_kernel_times reports them. */
+enum {
+    QNB_K_WW = 0, QNB_K_QW, QNB_K_PW, QNB_K_PP, QNB_K_QP, QNB_K_LRF_TAYLOR, QNB_K_QQ,
+    QNB_K_RESTRAIN, QNB_K_WATPOL, QNB_K_PACK, QNB_K_APPLY, QNB_K_BUILD, QNB_K_LRF_BUILD,
+    QNB_K_COUNT
+};
+
+/* Brackets every launch of each kernel class with CUDA events on the
+   context's stream while enable != 0. */
+int qnb_profile(qnb_context* ctx, int32_t enable);
+
+/* Total milliseconds and launches per kernel class since the last call
+   (n entries, n <= QNB_K_COUNT); resets the totals. */
+int qnb_kernel_times(qnb_context* ctx, double* ms, int64_t* launches, int32_t n);
 
 #ifdef __cplusplus
 }

@@ -70,7 +70,16 @@ struct qnb_context {
     int natom = 0, nat_solute = 0, nwat = 0, sa = 0, ncgp = 0, ncgp_solute = 0, nqat = 0, S = 0;
     double rexcl_o2 = 0.0;
     DevModel m{};
-    DevState s{};
+    int nwin = 1;
+    std::vector<DevState> st;      // per-window device state (host copy of the pointers)
+    QQEntry* st_qq = nullptr;      // static Q-Q / Q-bonded lists (shared by the windows)
+    int nqq = 0, nqq_qq = 0;
+    DevState* d_states = nullptr;  // the same, on the device
+    double* x_all = nullptr;       // [nwin][natom][3]
+    double* e_all = nullptr;       // [nwin][kNumE] FP64 energy slots
+    unsigned long long* efix_all = nullptr;   // [nwin][kNumE] fixed-point slots
+    int* cnt_all = nullptr;        // [nwin][C_NUM] list counters
+    double* d_all = nullptr;       // [nwin][natom][3]
     int* d_iwhich = nullptr;
     uint8_t* d_qnear = nullptr;
     int* d_wsw = nullptr;
@@ -78,12 +87,25 @@ struct qnb_context {
     double* d_shell_tsum = nullptr;
     std::vector<void*> allocs;
     bool lists_built = false, qp_done = false, qw_done = false;
-    int counts[C_NUM] = {0};
+    std::vector<int> counts;       // [nwin][C_NUM] after the last build
     SolventDev solv{};
     bool have_solv = false;
     int64_t launches = 0;
+    // optional per-kernel-class event timing (qnb_profile)
+    bool profiling = false;
+    struct Pending {
+        int k;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> ev_pool;
+    double prof_ms[K_NUM] = {0};
+    int64_t prof_n[K_NUM] = {0};
     double* h_stage = nullptr;   // pinned staging for x / d (natom*3)
-    double* h_e = nullptr;       // pinned energies (kNumE doubles + kNumE fixed)
+    double* h_e = nullptr;       // pinned energies (nwin x (kNumE doubles + kNumE fixed))
+
+    Launch all() const { return Launch{m, st[0], d_states, nwin, stream}; }
+    Launch one() const { return Launch{m, st[0], d_states, 1, stream}; }   // window 0 only
 
     template <typename T>
     int alloc(T** p, size_t n) {
@@ -109,6 +131,47 @@ struct qnb_context {
 };
 
 namespace {
+
+cudaEvent_t take_event(qnb_context* c) {
+    if (!c->ev_pool.empty()) {
+        cudaEvent_t e = c->ev_pool.back();
+        c->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// runs f (which enqueues kernels on c->stream), bracketed by events when
+// profiling is on
+template <typename F>
+void timed(qnb_context* c, int k, F&& f) {
+    if (!c->profiling) {
+        f();
+        return;
+    }
+    cudaEvent_t a = take_event(c), b = take_event(c);
+    cudaEventRecord(a, c->stream);
+    f();
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({k, a, b});
+}
+
+void collect_profile(qnb_context* c) {
+    if (c->pending.empty()) return;
+    cudaStreamSynchronize(c->stream);
+    for (auto& p : c->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            c->prof_ms[p.k] += ms;
+            c->prof_n[p.k] += 1;
+        }
+        c->ev_pool.push_back(p.a);
+        c->ev_pool.push_back(p.b);
+    }
+    c->pending.clear();
+}
 
 #define TRY(x)                 \
     do {                       \
@@ -239,19 +302,46 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     std::sort(sp.begin(), sp.end(), [](const Sp& x, const Sp& y) {
         return x.i != y.i ? x.i < y.i : (x.j != y.j ? x.j < y.j : x.k < y.k);
     });
-    std::vector<int> spec_off(ns + 1, 0), spec_j;
-    std::vector<uint8_t> spec_kind;
-    for (size_t k = 0; k < sp.size(); ++k) {
-        if (k && sp[k].i == sp[k - 1].i && sp[k].j == sp[k - 1].j) continue;   // keep the excluded entry
-        if (sp[k].i < 0 || sp[k].j >= ns) return fail(QNB_ERR_ARG, "special pair outside the solute");
-        spec_j.push_back(sp[k].j);
-        spec_kind.push_back((uint8_t)sp[k].k);
-        spec_off[sp[k].i + 1]++;
+    // per solute group pair: the special atom pairs, keyed g1*ncgp_solute+g2
+    std::vector<int> slot_of(natom, -1);
+    for (int g = 0; g < t->ncgp_solute; ++g) {
+        if (gslot[g + 1] - gslot[g] > kMaxGroup)
+            return fail(QNB_ERR_UNSUPPORTED, "solute charge group %d has %d atoms (max %d)", g,
+                        gslot[g + 1] - gslot[g], kMaxGroup);
+        for (int a = gslot[g]; a < gslot[g + 1]; ++a) slot_of[gatom[a]] = a - gslot[g];
     }
-    for (int i = 0; i < ns; ++i) spec_off[i + 1] += spec_off[i];
-    TRY(c->upload((int**)&m.spec_off, spec_off));
-    TRY(c->upload((int**)&m.spec_j, spec_j));
-    TRY(c->upload((uint8_t**)&m.spec_kind, spec_kind));
+    struct SG {
+        long long key;
+        int ent;
+    };
+    std::vector<SG> sg;
+    for (size_t k = 0; k < sp.size(); ++k) {
+        if (k && sp[k].i == sp[k - 1].i && sp[k].j == sp[k - 1].j) continue;   // the excluded entry wins
+        if (sp[k].i < 0 || sp[k].j >= ns) return fail(QNB_ERR_ARG, "special pair outside the solute");
+        int i = sp[k].i, j = sp[k].j;   // i < j
+        int gi = iwhich[i], gj = iwhich[j];
+        int si = slot_of[i], sj = slot_of[j];
+        if (gi > gj) {
+            std::swap(gi, gj);
+            std::swap(si, sj);
+        }
+        sg.push_back({(long long)gi * t->ncgp_solute + gj, si | (sj << 8) | (sp[k].k << 16)});
+    }
+    std::stable_sort(sg.begin(), sg.end(), [](const SG& a, const SG& b) { return a.key < b.key; });
+    std::vector<long long> sg_key;
+    std::vector<int> sg_off, sg_ent;
+    for (size_t k = 0; k < sg.size(); ++k) {
+        if (k == 0 || sg[k].key != sg[k - 1].key) {
+            sg_key.push_back(sg[k].key);
+            sg_off.push_back((int)k);
+        }
+        sg_ent.push_back(sg[k].ent);
+    }
+    sg_off.push_back((int)sg.size());
+    m.nsg = (int)sg_key.size();
+    TRY(c->upload((long long**)&m.sg_key, sg_key));
+    TRY(c->upload((int**)&m.sg_off, sg_off));
+    TRY(c->upload((int**)&m.sg_ent, sg_ent));
 
     // LJ tables per code (1..3) and type pair: precompute_set_values_pp's A/B
     std::vector<double2> lj(3 * (size_t)nt * nt);
@@ -472,123 +562,171 @@ int build_model(qnb_context* c, const qnb_topology* t) {
             }
         }
     }
-    c->s.nqq = (int)qq.size();
-    c->s.nqq_qq = nqq_qq;
-    TRY(c->upload(&c->s.qq, qq));
+    c->nqq = (int)qq.size();
+    c->nqq_qq = nqq_qq;
+    TRY(c->upload(&c->st_qq, qq));
+    return QNB_OK;
+}
+
+int upload_states(qnb_context* c) {
+    CU(cudaMemcpyAsync(c->d_states, c->st.data(), sizeof(DevState) * c->nwin, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
     return QNB_OK;
 }
 
 int alloc_state(qnb_context* c) {
-    DevState& s = c->s;
     const DevModel& m = c->m;
-    TRY(c->alloc(&s.x, 3 * (size_t)m.natom));
-    TRY(c->alloc(&s.d, 3 * (size_t)m.natom));
-    TRY(c->alloc(&s.xq, (size_t)m.natom));
-    TRY(c->alloc(&s.fix, 3 * (size_t)m.natom));
-    TRY(c->alloc(&s.e, (size_t)kNumE));
-    TRY(c->alloc(&s.efix, (size_t)kNumE));
-    TRY(c->alloc(&s.lambda, (size_t)std::max(1, m.S)));
-    TRY(c->alloc(&s.lrf, (size_t)std::max(1, m.ncgp) * kLrfLen));
-    TRY(c->alloc(&s.cnt, (size_t)C_NUM));
-    TRY(c->alloc(&s.theta, (size_t)std::max(1, m.nwat)));
-    TRY(c->alloc(&s.shell, (size_t)std::max(1, m.nwat)));
-    TRY(c->alloc(&s.rank, (size_t)std::max(1, m.nwat)));
-    TRY(c->alloc(&s.n_insh, (size_t)kMaxShell));
-    TRY(c->alloc(&s.wstate, (size_t)3 * kMaxShell));
-    TRY(c->alloc(&c->d_shell_tsum, (size_t)kMaxShell));
-    CU(cudaMemset(s.d, 0, sizeof(double) * 3 * m.natom));
-    CU(cudaMemset(s.fix, 0, sizeof(unsigned long long) * 3 * m.natom));
-    CU(cudaMemset(s.cnt, 0, sizeof(int) * C_NUM));
-    CU(cudaMemset(s.wstate, 0, sizeof(double) * 3 * kMaxShell));
-    CU(cudaMemset(s.lrf, 0, sizeof(double) * std::max(1, m.ncgp) * kLrfLen));
-    std::vector<double> lam(std::max(1, m.S), 1.0);
-    CU(cudaMemcpy(s.lambda, lam.data(), lam.size() * sizeof(double), cudaMemcpyHostToDevice));
-    // initial list capacities (grown on overflow)
+    const int W = c->nwin;
+    const size_t n3 = 3 * (size_t)m.natom;
+    c->st.assign(W, DevState{});
+    TRY(c->alloc(&c->x_all, n3 * W));
+    TRY(c->alloc(&c->d_all, n3 * W));
+    TRY(c->alloc(&c->e_all, (size_t)kNumE * W));
+    TRY(c->alloc(&c->efix_all, (size_t)kNumE * W));
+    TRY(c->alloc(&c->cnt_all, (size_t)C_NUM * W));
+    CU(cudaMemset(c->cnt_all, 0, sizeof(int) * C_NUM * W));
+    CU(cudaMemset(c->d_all, 0, sizeof(double) * n3 * W));
     const double rho = 0.04;   // generous water density (molecules / A^3)
     int64_t per_w = (int64_t)(4.0 / 3.0 * M_PI * 1000.0 * rho) + 64;
-    TRY(ensure_cap(c, &s.ww, &s.cap_ww, std::max<int64_t>(1024, (int64_t)m.nwat * per_w / 2)));
-    TRY(ensure_cap(c, &s.pw, &s.cap_pw, std::max<int64_t>(1024, (int64_t)m.nat_solute * per_w)));
-    TRY(ensure_cap(c, &s.pp, &s.cap_pp, std::max<int64_t>(1024, (int64_t)m.nat_solute * 256)));
-    TRY(ensure_cap(c, &s.qp, &s.cap_qp, std::max<int64_t>(1024, (int64_t)m.nat_solute)));
-    TRY(ensure_cap(c, &s.qw, &s.cap_qw, std::max<int64_t>(1024, (int64_t)m.nwat)));
+    std::vector<double> lam(std::max(1, m.S), 1.0);
+    for (int w = 0; w < W; ++w) {
+        DevState& s = c->st[w];
+        s.x = c->x_all + n3 * w;
+        s.d = c->d_all + n3 * w;
+        TRY(c->alloc(&s.xq, (size_t)m.natom));
+        TRY(c->alloc(&s.fix, n3));
+        s.e = c->e_all + (size_t)kNumE * w;
+        s.efix = c->efix_all + (size_t)kNumE * w;
+        TRY(c->alloc(&s.lambda, (size_t)std::max(1, m.S)));
+        TRY(c->alloc(&s.lrf, (size_t)std::max(1, m.ncgp) * kLrfLen));
+        s.cnt = c->cnt_all + (size_t)C_NUM * w;
+        TRY(c->alloc(&s.theta, (size_t)std::max(1, m.nwat)));
+        TRY(c->alloc(&s.shell, (size_t)std::max(1, m.nwat)));
+        TRY(c->alloc(&s.rank, (size_t)std::max(1, m.nwat)));
+        TRY(c->alloc(&s.n_insh, (size_t)kMaxShell));
+        TRY(c->alloc(&s.wstate, (size_t)3 * kMaxShell));
+        TRY(c->alloc(&s.shell_tsum, (size_t)kMaxShell));
+        TRY(c->alloc(&s.shell_list, (size_t)kMaxShell * std::max(1, m.nwat)));
+        CU(cudaMemset(s.fix, 0, sizeof(unsigned long long) * n3));
+        CU(cudaMemset(s.wstate, 0, sizeof(double) * 3 * kMaxShell));
+        CU(cudaMemset(s.lrf, 0, sizeof(double) * std::max(1, m.ncgp) * kLrfLen));
+        CU(cudaMemcpy(s.lambda, lam.data(), lam.size() * sizeof(double), cudaMemcpyHostToDevice));
+        TRY(ensure_cap(c, &s.ww, &s.cap_ww, std::max<int64_t>(1024, (int64_t)m.nwat * per_w / 2)));
+        TRY(ensure_cap(c, &s.pw, &s.cap_pw, std::max<int64_t>(1024, (int64_t)m.nat_solute * per_w)));
+        TRY(ensure_cap(c, &s.pp, &s.cap_pp, std::max<int64_t>(1024, (int64_t)m.nat_solute * 256)));
+        TRY(ensure_cap(c, &s.ppg, &s.cap_ppg, std::max<int64_t>(1024, (int64_t)m.ncgp_solute * 96)));
+        TRY(ensure_cap(c, &s.qp, &s.cap_qp, std::max<int64_t>(1024, (int64_t)m.nat_solute)));
+        TRY(ensure_cap(c, &s.qw, &s.cap_qw, std::max<int64_t>(1024, (int64_t)m.nwat)));
+        s.qq = c->st_qq;
+        s.nqq = c->nqq;
+        s.nqq_qq = c->nqq_qq;
+    }
+    TRY(c->alloc(&c->d_states, (size_t)W));
+    c->counts.assign((size_t)W * C_NUM, 0);
     CU(cudaMallocHost((void**)&c->h_stage, sizeof(double) * std::max(3 * m.natom, 64)));
-    CU(cudaMallocHost((void**)&c->h_e, sizeof(double) * 2 * kNumE));
+    CU(cudaMallocHost((void**)&c->h_e, sizeof(double) * 2 * kNumE * W));
+    return upload_states(c);
+}
+
+int zero_acc(qnb_context* c, int nw) {
+    CU(cudaMemsetAsync(c->e_all, 0, sizeof(double) * kNumE * nw, c->stream));
+    CU(cudaMemsetAsync(c->efix_all, 0, sizeof(unsigned long long) * kNumE * nw, c->stream));
     return QNB_OK;
 }
 
-int zero_acc(qnb_context* c) {
-    CU(cudaMemsetAsync(c->s.e, 0, sizeof(double) * kNumE, c->stream));
-    CU(cudaMemsetAsync(c->s.efix, 0, sizeof(unsigned long long) * kNumE, c->stream));
-    return QNB_OK;
-}
-
-// read energies (FP64 slots + fixed-point slots)
-int read_energies(qnb_context* c, double* out) {
-    CU(cudaMemcpyAsync(c->h_e, c->s.e, sizeof(double) * kNumE, cudaMemcpyDeviceToHost, c->stream));
-    CU(cudaMemcpyAsync(c->h_e + kNumE, c->s.efix, sizeof(double) * kNumE, cudaMemcpyDeviceToHost, c->stream));
+// energies of the first nw windows: out[w*kNumE + k] (FP64 slots + fixed-point slots)
+int read_energies(qnb_context* c, int nw, double* out) {
+    CU(cudaMemcpyAsync(c->h_e, c->e_all, sizeof(double) * kNumE * nw, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(c->h_e + (size_t)kNumE * c->nwin, c->efix_all, sizeof(double) * kNumE * nw,
+                       cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
-    const long long* fx = (const long long*)(c->h_e + kNumE);
-    for (int k = 0; k < kNumE; ++k) out[k] = c->h_e[k] + (double)fx[k] * (1.0 / kFix);
+    const long long* fx = (const long long*)(c->h_e + (size_t)kNumE * c->nwin);
+    for (int k = 0; k < kNumE * nw; ++k) out[k] = c->h_e[k] + (double)fx[k] * (1.0 / kFix);
     return QNB_OK;
 }
 
 int stage_x(qnb_context* c, const double* x) {
     size_t n = 3 * (size_t)c->natom;
     memcpy(c->h_stage, x, n * sizeof(double));
-    CU(cudaMemcpyAsync(c->s.x, c->h_stage, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->st[0].x, c->h_stage, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     return QNB_OK;
 }
 
-// device gradient -> add into the caller's d, then clear the device gradient
+// window 0's device gradient -> added into the caller's d; device gradient cleared
 int unstage_d(qnb_context* c, double* d) {
     size_t n = 3 * (size_t)c->natom;
     if (c->mixed) {
-        launch_apply_fixed(c->m, c->s, c->stream);
+        launch_apply_fixed(c->one());
         c->launches++;
         TRY(check_launch());
     }
-    CU(cudaMemcpyAsync(c->h_stage, c->s.d, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    CU(cudaMemsetAsync(c->s.d, 0, n * sizeof(double), c->stream));
+    CU(cudaMemcpyAsync(c->h_stage, c->st[0].d, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemsetAsync(c->st[0].d, 0, n * sizeof(double), c->stream));
     CU(cudaStreamSynchronize(c->stream));
     for (size_t k = 0; k < n; ++k) d[k] += c->h_stage[k];
     return QNB_OK;
 }
 
-int build_lists(qnb_context* c, const Cut& cut) {
-    DevState& s = c->s;
-    const DevModel& m = c->m;
+// grows the lists of every window to at least the sizes the last build counted
+int grow_lists(qnb_context* c, bool* grew, bool* do_qp, bool* do_qw) {
+    *grew = false;
+    int64_t need[C_NUM] = {0};
+    for (int w = 0; w < c->nwin; ++w)
+        for (int k = 0; k < C_NUM; ++k) need[k] = std::max<int64_t>(need[k], c->counts[w * C_NUM + k]);
+    DevState& s0 = c->st[0];
+    struct G {
+        int k;
+        int64_t cap;
+    } gs[] = {{C_WW, s0.cap_ww}, {C_PW, s0.cap_pw}, {C_PP, s0.cap_pp}, {C_PPG, s0.cap_ppg},
+              {C_QP, s0.cap_qp}, {C_QW, s0.cap_qw}};
+    for (auto& g : gs) {
+        if (need[g.k] <= g.cap) continue;
+        int64_t n = need[g.k] * 5 / 4 + 1024;
+        for (int w = 0; w < c->nwin; ++w) {
+            DevState& s = c->st[w];
+            switch (g.k) {
+                case C_WW: TRY(ensure_cap(c, &s.ww, &s.cap_ww, n)); break;
+                case C_PW: TRY(ensure_cap(c, &s.pw, &s.cap_pw, n)); break;
+                case C_PP: TRY(ensure_cap(c, &s.pp, &s.cap_pp, n)); break;
+                case C_PPG: TRY(ensure_cap(c, &s.ppg, &s.cap_ppg, n)); break;
+                case C_QP: TRY(ensure_cap(c, &s.qp, &s.cap_qp, n)); *do_qp = true; break;
+                case C_QW: TRY(ensure_cap(c, &s.qw, &s.cap_qw, n)); *do_qw = true; break;
+            }
+        }
+        *grew = true;
+    }
+    if (*grew) TRY(upload_states(c));
+    return QNB_OK;
+}
+
+int build_lists(qnb_context* c, const Cut& cut, int nw) {
+    Launch L = nw == 1 ? c->one() : c->all();
     bool do_qp = !(c->qp_done && cut.rcq2 > c->rexcl_o2);   // src/nonbondene.f90:3678
     bool do_qw = !(c->qw_done && cut.rcq2 > c->rexcl_o2);   // src/nonbondene.f90:3889
     for (int attempt = 0; attempt < 4; ++attempt) {
-        CU(cudaMemsetAsync(s.cnt + C_WW, 0, sizeof(int) * 3, c->stream));   // WW, PW, PP
-        CU(cudaMemsetAsync(s.cnt + C_PP14, 0, sizeof(int), c->stream));
-        if (do_qp) CU(cudaMemsetAsync(s.cnt + C_QP, 0, sizeof(int), c->stream));
-        if (do_qw) CU(cudaMemsetAsync(s.cnt + C_QW, 0, sizeof(int), c->stream));
+        unsigned keep = (do_qp ? 0u : 1u << C_QP) | (do_qw ? 0u : 1u << C_QW);
+        launch_reset_counts(L, keep);
+        timed(c, K_BUILD, [&] {
+            launch_pack(L);
+            if (c->use_lrf) launch_group_centres(L);
+            launch_build_pp(L, cut);
+            launch_build_pw(L, cut);
+            if (do_qp) launch_build_qp(L, c->d_qnear, cut.rcq2);
+            launch_build_ww(L, cut);
+            if (do_qw) launch_build_qw(L, cut);
+        });
+        c->launches += 7 + (c->use_lrf ? 1 : 0);
         if (c->use_lrf) {
-            launch_group_centres(m, s, c->stream);
-            c->launches++;
-        }
-        launch_build_pp(m, s, cut, c->stream);
-        launch_build_pw(m, s, cut, c->stream);
-        if (do_qp) launch_build_qp_impl(m, s, c->d_qnear, cut.rcq2, c->stream);
-        launch_build_ww(m, s, cut, c->stream);
-        if (do_qw) launch_build_qw(m, s, cut, c->stream);
-        c->launches += 5;
-        if (c->use_lrf) {
-            launch_lrf_accumulate(m, s, cut, c->mixed, c->stream);
+            timed(c, K_LRF_BUILD, [&] { launch_lrf_accumulate(L, cut, c->mixed); });
             c->launches++;
         }
         TRY(check_launch());
-        CU(cudaMemcpyAsync(c->counts, s.cnt, sizeof(int) * C_NUM, cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaMemcpyAsync(c->counts.data(), c->cnt_all, sizeof(int) * C_NUM * nw, cudaMemcpyDeviceToHost,
+                           c->stream));
         CU(cudaStreamSynchronize(c->stream));
-        bool grow = false;
-        auto need = [&](int64_t n, int64_t cap) { return n > cap; };
-        if (need(c->counts[C_WW], s.cap_ww)) { TRY(ensure_cap(c, &s.ww, &s.cap_ww, c->counts[C_WW] * 5 / 4 + 1024)); grow = true; }
-        if (need(c->counts[C_PW], s.cap_pw)) { TRY(ensure_cap(c, &s.pw, &s.cap_pw, c->counts[C_PW] * 5 / 4 + 1024)); grow = true; }
-        if (need(c->counts[C_PP], s.cap_pp)) { TRY(ensure_cap(c, &s.pp, &s.cap_pp, c->counts[C_PP] * 5 / 4 + 1024)); grow = true; }
-        if (need(c->counts[C_QP], s.cap_qp)) { TRY(ensure_cap(c, &s.qp, &s.cap_qp, c->counts[C_QP] + 1024)); grow = true; do_qp = true; }
-        if (need(c->counts[C_QW], s.cap_qw)) { TRY(ensure_cap(c, &s.qw, &s.cap_qw, c->counts[C_QW] + 1024)); grow = true; do_qw = true; }
-        if (!grow) {
+        bool grew = false;
+        TRY(grow_lists(c, &grew, &do_qp, &do_qw));
+        if (!grew) {
             if (do_qp) c->qp_done = true;
             if (do_qw) c->qw_done = true;
             c->lists_built = true;
@@ -598,16 +736,24 @@ int build_lists(qnb_context* c, const Cut& cut) {
     return fail(QNB_ERR_CAPACITY, "pair lists kept overflowing");
 }
 
-int compute_nonbond(qnb_context* c, int md) {
+int compute_nonbond(qnb_context* c, int md, int nw) {
     if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built");
-    int nl = 0;
-    if (c->mixed) {
-        launch_pack_mixed(c->m, c->s, c->stream);
+    Launch L = nw == 1 ? c->one() : c->all();
+    int mx = c->mixed, nl = 0;
+    if (mx) {
+        timed(c, K_PACK, [&] { launch_pack(L); });
         ++nl;
     }
-    launch_nonbond(c->m, c->s, c->mixed, md, c->stream, &nl);
+    // call order of pot_energy_nonbonds, src/potene.f90:340-379
+    if (c->m.natom > c->m.nat_solute) {
+        if (md) timed(c, K_WW, [&] { launch_ww(L, mx); }), ++nl;
+        timed(c, K_QW, [&] { launch_qw(L, mx); }), ++nl;
+        if (md) timed(c, K_PW, [&] { launch_pw(L, mx); }), ++nl;
+    }
+    if (md) timed(c, K_PP, [&] { launch_pp(L, mx); }), ++nl;
+    timed(c, K_QP, [&] { launch_qp(L, mx); }), ++nl;
     if (c->use_lrf && md) {
-        launch_lrf_taylor_impl(c->m, c->s, c->d_iwhich, c->mixed, c->stream);
+        timed(c, K_LRF_TAYLOR, [&] { launch_lrf_taylor(L, c->d_iwhich, mx); });
         ++nl;
     }
     c->launches += nl;
@@ -637,13 +783,14 @@ void add_energies(const double* e, qnb_energies* E, qnb_qenergies* EQ, int S) {
 
 int64_t list_pairs(const qnb_context* c, int kind) {
     int64_t sa = c->sa;
+    const int* cnt = c->counts.data();   // window 0
     switch (kind) {
-        case QNB_LIST_PP: return c->counts[C_PP];
-        case QNB_LIST_PP14: return c->counts[C_PP14];
-        case QNB_LIST_PW: return (int64_t)c->counts[C_PW] * sa;
-        case QNB_LIST_WW: return (int64_t)c->counts[C_WW] * sa * sa;
-        case QNB_LIST_QP: return (int64_t)c->counts[C_QP] * c->nqat;
-        case QNB_LIST_QW: return (int64_t)c->counts[C_QW] * c->nqat * sa;
+        case QNB_LIST_PP: return cnt[C_PP];
+        case QNB_LIST_PP14: return cnt[C_PP14];
+        case QNB_LIST_PW: return (int64_t)cnt[C_PW] * sa;
+        case QNB_LIST_WW: return (int64_t)cnt[C_WW] * sa * sa;
+        case QNB_LIST_QP: return (int64_t)cnt[C_QP] * c->nqat;
+        case QNB_LIST_QW: return (int64_t)cnt[C_QW] * c->nqat * sa;
     }
     return -1;
 }
@@ -657,11 +804,12 @@ extern "C" {
 
 const char* qnb_last_error(void) { return g_err.c_str(); }
 
-int32_t qnb_version(void) { return 0x000100; }
+int32_t qnb_version(void) { return 0x000200; }
 
-int qnb_create(const qnb_topology* t, const qnb_options* opt, qnb_context** out) {
+int qnb_create_batch(const qnb_topology* t, const qnb_options* opt, int32_t nwin, qnb_context** out) {
     if (!t || !opt || !out) return fail(QNB_ERR_ARG, "null argument");
     *out = nullptr;
+    if (nwin < 1 || nwin > 65535) return fail(QNB_ERR_ARG, "nwin must be 1..65535");
     if (t->natom <= 0 || t->nat_solute < 0 || t->nat_solute > t->natom || t->nwat < 0)
         return fail(QNB_ERR_ARG, "bad atom counts");
     if (t->natom != t->nat_solute + t->nwat * t->solv_atom) return fail(QNB_ERR_ARG, "natom != nat_solute + nwat*solv_atom");
@@ -680,6 +828,7 @@ int qnb_create(const qnb_topology* t, const qnb_options* opt, qnb_context** out)
     c->device = opt->device;
     c->mixed = opt->precision == QNB_PREC_MIXED;
     c->use_lrf = opt->use_lrf ? 1 : 0;
+    c->nwin = nwin;
     c->natom = t->natom;
     c->nat_solute = t->nat_solute;
     c->nwat = t->nwat;
@@ -701,11 +850,20 @@ int qnb_create(const qnb_topology* t, const qnb_options* opt, qnb_context** out)
     return QNB_OK;
 }
 
+int qnb_create(const qnb_topology* t, const qnb_options* opt, qnb_context** out) {
+    return qnb_create_batch(t, opt, 1, out);
+}
+
 int qnb_destroy(qnb_context* c) {
     if (!c) return QNB_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (void* p : c->allocs) cudaFree(p);
+    for (auto& p : c->pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto e : c->ev_pool) cudaEventDestroy(e);
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->h_e) cudaFreeHost(c->h_e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -713,13 +871,26 @@ int qnb_destroy(qnb_context* c) {
     return QNB_OK;
 }
 
-int qnb_set_lambda(qnb_context* c, const double* lambda) {
+int qnb_window_count(qnb_context* c, int32_t* n) {
+    if (!c || !n) return fail(QNB_ERR_ARG, "null argument");
+    *n = c->nwin;
+    return QNB_OK;
+}
+
+int qnb_set_lambda_window(qnb_context* c, int32_t w, const double* lambda) {
     if (!c || (!lambda && c->S > 0)) return fail(QNB_ERR_ARG, "null argument");
+    if (w < 0 || w >= c->nwin) return fail(QNB_ERR_ARG, "window %d of %d", w, c->nwin);
     if (c->S == 0) return QNB_OK;
     CU(cudaSetDevice(c->device));
     memcpy(c->h_stage, lambda, sizeof(double) * c->S);
-    CU(cudaMemcpyAsync(c->s.lambda, c->h_stage, sizeof(double) * c->S, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->st[w].lambda, c->h_stage, sizeof(double) * c->S, cudaMemcpyHostToDevice, c->stream));
     CU(cudaStreamSynchronize(c->stream));
+    return QNB_OK;
+}
+
+int qnb_set_lambda(qnb_context* c, const double* lambda) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    for (int w = 0; w < c->nwin; ++w) TRY(qnb_set_lambda_window(c, w, lambda));
     return QNB_OK;
 }
 
@@ -729,15 +900,17 @@ int qnb_make_pair_lists_dev(qnb_context* c, double Rq, double Rcq2, double RcLRF
     if (!c) return fail(QNB_ERR_ARG, "null context");
     CU(cudaSetDevice(c->device));
     Cut cut{Rcq2, RcLRF2, Rcpp2, Rcpw2, Rcww2};
-    return build_lists(c, cut);
+    return build_lists(c, cut, c->nwin);
 }
 
 int qnb_make_pair_lists(qnb_context* c, const double* x, double Rq, double Rcq2, double RcLRF2, double Rcpp2,
                         double Rcpw2, double Rcww2) {
+    (void)Rq;
     if (!c || !x) return fail(QNB_ERR_ARG, "null argument");
     CU(cudaSetDevice(c->device));
     TRY(stage_x(c, x));
-    return qnb_make_pair_lists_dev(c, Rq, Rcq2, RcLRF2, Rcpp2, Rcpw2, Rcww2);
+    Cut cut{Rcq2, RcLRF2, Rcpp2, Rcpw2, Rcww2};
+    return build_lists(c, cut, 1);
 }
 
 int qnb_pot_energy_nonbonds(qnb_context* c, const double* x, double* d, qnb_energies* E, qnb_qenergies* EQ,
@@ -745,12 +918,12 @@ int qnb_pot_energy_nonbonds(qnb_context* c, const double* x, double* d, qnb_ener
     if (!c || !x || !d) return fail(QNB_ERR_ARG, "null argument");
     CU(cudaSetDevice(c->device));
     TRY(stage_x(c, x));
-    TRY(zero_acc(c));
-    TRY(compute_nonbond(c, md));
+    TRY(zero_acc(c, 1));
+    TRY(compute_nonbond(c, md, 1));
     TRY(unstage_d(c, d));
-    double e[kNumE];
-    TRY(read_energies(c, e));
-    add_energies(e, E, EQ, c->S);
+    std::vector<double> e(kNumE);
+    TRY(read_energies(c, 1, e.data()));
+    add_energies(e.data(), E, EQ, c->S);
     return QNB_OK;
 }
 
@@ -758,14 +931,14 @@ int qnb_nonbond_qq(qnb_context* c, const double* x, double* d, qnb_qenergies* EQ
     if (!c || !x || !d) return fail(QNB_ERR_ARG, "null argument");
     CU(cudaSetDevice(c->device));
     TRY(stage_x(c, x));
-    TRY(zero_acc(c));
-    launch_nonbond_qq(c->m, c->s, c->mixed, c->stream);
+    TRY(zero_acc(c, 1));
+    launch_nonbond_qq(c->one(), c->mixed);
     c->launches++;
     TRY(check_launch());
     TRY(unstage_d(c, d));
-    double e[kNumE];
-    TRY(read_energies(c, e));
-    add_energies(e, nullptr, EQ, c->S);
+    std::vector<double> e(kNumE);
+    TRY(read_energies(c, 1, e.data()));
+    add_energies(e.data(), nullptr, EQ, c->S);
     return QNB_OK;
 }
 
@@ -773,6 +946,7 @@ int qnb_set_solvent_params(qnb_context* c, const qnb_solvent_params* p) {
     if (!c || !p) return fail(QNB_ERR_ARG, "null argument");
     if (p->wpol_restr && (p->nwpolr_shell < 1 || p->nwpolr_shell > kMaxShell))
         return fail(QNB_ERR_ARG, "nwpolr_shell must be 1..%d", kMaxShell);
+    if (p->wpol_restr && !(p->itdis >= 1.0)) return fail(QNB_ERR_ARG, "itdis must be >= 1");
     CU(cudaSetDevice(c->device));
     SolventDev& s = c->solv;
     s.fk_wsphere = p->fk_wsphere;
@@ -791,7 +965,8 @@ int qnb_set_solvent_params(qnb_context* c, const qnb_solvent_params* p) {
     }
     double ws[3 * kMaxShell] = {0};
     for (int k = 0; k < kMaxShell; ++k) ws[k] = p->theta_corr[k];
-    CU(cudaMemcpyAsync(c->s.wstate, ws, sizeof(ws), cudaMemcpyHostToDevice, c->stream));
+    for (int w = 0; w < c->nwin; ++w)
+        CU(cudaMemcpyAsync(c->st[w].wstate, ws, sizeof(ws), cudaMemcpyHostToDevice, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     c->have_solv = true;
     return QNB_OK;
@@ -802,13 +977,13 @@ int qnb_restrain_solvent(qnb_context* c, const double* x, double* d, double Tfre
     if (!c->have_solv) return fail(QNB_ERR_STATE, "solvent parameters not set");
     CU(cudaSetDevice(c->device));
     TRY(stage_x(c, x));
-    TRY(zero_acc(c));
-    launch_restrain_solvent_impl(c->m, c->s, c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv, c->stream);
+    TRY(zero_acc(c, 1));
+    launch_restrain_solvent(c->one(), c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv);
     c->launches++;
     TRY(check_launch());
     TRY(unstage_d(c, d));
-    double e[kNumE];
-    TRY(read_energies(c, e));
+    std::vector<double> e(kNumE);
+    TRY(read_energies(c, 1, e.data()));
     *E += e[E_RST_RAD];
     return QNB_OK;
 }
@@ -818,14 +993,12 @@ int qnb_watpol(qnb_context* c, const double* x, double* d, int32_t istep, int32_
     if (!c->have_solv) return fail(QNB_ERR_STATE, "solvent parameters not set");
     CU(cudaSetDevice(c->device));
     TRY(stage_x(c, x));
-    TRY(zero_acc(c));
-    int nl = 0;
-    launch_watpol_impl(c->m, c->s, c->solv, istep, md, c->mixed, c->d_shell_tsum, c->stream, &nl);
-    c->launches += nl;
+    TRY(zero_acc(c, 1));
+    c->launches += launch_watpol(c->one(), c->solv, istep, md, c->mixed);
     TRY(check_launch());
     TRY(unstage_d(c, d));
-    double e[kNumE];
-    TRY(read_energies(c, e));
+    std::vector<double> e(kNumE);
+    TRY(read_energies(c, 1, e.data()));
     *E += e[E_RST_POL];
     return QNB_OK;
 }
@@ -834,7 +1007,7 @@ int qnb_get_watpol_state(qnb_context* c, double* theta_corr, double* avtheta, do
     if (!c) return fail(QNB_ERR_ARG, "null context");
     CU(cudaSetDevice(c->device));
     double ws[3 * kMaxShell];
-    CU(cudaMemcpyAsync(ws, c->s.wstate, sizeof(ws), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(ws, c->st[0].wstate, sizeof(ws), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     for (int k = 0; k < kMaxShell; ++k) {
         if (theta_corr) theta_corr[k] = ws[k];
@@ -866,7 +1039,7 @@ int qnb_export_pairs(qnb_context* c, int32_t kind, int32_t* i, int32_t* j, int64
     CU(cudaMalloc(&dj, cnt * sizeof(int32_t)));
     CU(cudaMalloc(&dc, sizeof(int)));
     CU(cudaMemsetAsync(dc, 0, sizeof(int), c->stream));
-    launch_export_pairs(c->m, c->s, kind, di, dj, cnt, dc, c->stream);
+    launch_export_pairs(c->all(), 0, kind, di, dj, cnt, dc);
     int rc = check_launch();
     if (!rc) {
         cudaMemcpyAsync(i, di, cnt * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
@@ -882,15 +1055,34 @@ int qnb_export_pairs(qnb_context* c, int32_t kind, int32_t* i, int32_t* j, int64
 int qnb_get_lrf(qnb_context* c, double* lrf) {
     if (!c || !lrf) return fail(QNB_ERR_ARG, "null argument");
     CU(cudaSetDevice(c->device));
-    CU(cudaMemcpyAsync(lrf, c->s.lrf, sizeof(double) * kLrfLen * c->ncgp, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(lrf, c->st[0].lrf, sizeof(double) * kLrfLen * c->ncgp, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     return QNB_OK;
 }
 
 int qnb_device_buffers(qnb_context* c, double** x_dev, double** d_dev) {
     if (!c) return fail(QNB_ERR_ARG, "null context");
-    if (x_dev) *x_dev = c->s.x;
-    if (d_dev) *d_dev = c->s.d;
+    if (x_dev) *x_dev = c->x_all;
+    if (d_dev) *d_dev = c->d_all;
+    return QNB_OK;
+}
+
+int qnb_upload_coordinates(qnb_context* c, const double* x_all) {
+    if (!c || !x_all) return fail(QNB_ERR_ARG, "null argument");
+    CU(cudaSetDevice(c->device));
+    CU(cudaMemcpyAsync(c->x_all, x_all, sizeof(double) * 3 * (size_t)c->natom * c->nwin, cudaMemcpyHostToDevice,
+                       c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return QNB_OK;
+}
+
+int qnb_download_gradient(qnb_context* c, double* d_all, int32_t clear) {
+    if (!c || !d_all) return fail(QNB_ERR_ARG, "null argument");
+    CU(cudaSetDevice(c->device));
+    size_t n = 3 * (size_t)c->natom * c->nwin;
+    CU(cudaMemcpyAsync(d_all, c->d_all, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (clear) CU(cudaMemsetAsync(c->d_all, 0, sizeof(double) * n, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
     return QNB_OK;
 }
 
@@ -904,30 +1096,54 @@ int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, q
                     double* Erst) {
     if (!c) return fail(QNB_ERR_ARG, "null context");
     CU(cudaSetDevice(c->device));
-    TRY(zero_acc(c));
-    TRY(compute_nonbond(c, 1));
-    launch_nonbond_qq(c->m, c->s, c->mixed, c->stream);
+    Launch L = c->all();
+    TRY(zero_acc(c, c->nwin));
+    TRY(compute_nonbond(c, 1, c->nwin));
+    timed(c, K_QQ, [&] { launch_nonbond_qq(L, c->mixed); });
     c->launches++;
     if (c->have_solv) {
-        launch_restrain_solvent_impl(c->m, c->s, c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv, c->stream);
+        timed(c, K_RESTRAIN, [&] { launch_restrain_solvent(L, c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv); });
         c->launches++;
         int nl = 0;
-        launch_watpol_impl(c->m, c->s, c->solv, istep, 1, c->mixed, c->d_shell_tsum, c->stream, &nl);
+        timed(c, K_WATPOL, [&] { nl = launch_watpol(L, c->solv, istep, 1, c->mixed); });
         c->launches += nl;
     }
     if (c->mixed) {
-        launch_apply_fixed(c->m, c->s, c->stream);
+        timed(c, K_APPLY, [&] { launch_apply_fixed(L); });
         c->launches++;
     }
     TRY(check_launch());
     if (sync) {
-        double e[kNumE];
-        TRY(read_energies(c, e));
-        add_energies(e, E, EQ, c->S);
-        if (Erst) {
-            Erst[0] += e[E_RST_RAD];
-            Erst[1] += e[E_RST_POL];
+        std::vector<double> e((size_t)kNumE * c->nwin);
+        TRY(read_energies(c, c->nwin, e.data()));
+        for (int w = 0; w < c->nwin; ++w) {
+            add_energies(e.data() + (size_t)w * kNumE, E ? E + w : nullptr, EQ ? EQ + (size_t)w * c->S : nullptr, c->S);
+            if (Erst) {
+                Erst[2 * w] += e[(size_t)w * kNumE + E_RST_RAD];
+                Erst[2 * w + 1] += e[(size_t)w * kNumE + E_RST_POL];
+            }
         }
+    }
+    return QNB_OK;
+}
+
+int qnb_profile(qnb_context* c, int32_t enable) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    collect_profile(c);
+    c->profiling = enable != 0;
+    return QNB_OK;
+}
+
+int qnb_kernel_times(qnb_context* c, double* ms, int64_t* launches, int32_t n) {
+    if (!c || !ms || !launches) return fail(QNB_ERR_ARG, "null argument");
+    CU(cudaSetDevice(c->device));
+    collect_profile(c);
+    for (int k = 0; k < n && k < K_NUM; ++k) {
+        ms[k] = c->prof_ms[k];
+        launches[k] = c->prof_n[k];
+        c->prof_ms[k] = 0.0;
+        c->prof_n[k] = 0;
     }
     return QNB_OK;
 }

@@ -24,8 +24,10 @@ enum {
 __host__ __device__ constexpr int eq_slot(int s, int k) { return E_Q0 + 6 * s + k; }
 constexpr int kNumE = E_Q0 + 6 * kMaxStates;
 
-// list counters / status words
-enum { C_WW = 0, C_PW, C_PP, C_QP, C_QW, C_PP14, C_NUM };
+// list counters (entries at list granularity, plus reference atom-pair counts)
+enum { C_WW = 0, C_PW, C_PP, C_QP, C_QW, C_PP14, C_PPG, C_NUM };
+
+constexpr int kMaxGroup = 16;   // atoms per solute charge group handled on device
 
 struct alignas(32) QPar {   // one (pair type, state) parameter set: A, B, elec, soft-core alpha
     double A, B, el, sc;
@@ -47,9 +49,14 @@ struct DevModel {
     const int* gslot;           // [ncgp+1] offsets into gatom
     const int* gatom;           // group member atoms
     const int* gsw;             // [ncgp] switch atoms
-    const int* spec_off;        // [nat_solute+1] special partners of i (j > i)
-    const int* spec_j;
-    const uint8_t* spec_kind;   // 1 excluded, 3 1-4
+    // solute group pairs holding excluded or 1-4 atom pairs: sorted keys
+    // g1*ncgp_solute+g2 (g1 <= g2), each with a run of entries
+    // (slot in g1) | (slot in g2) << 8 | kind << 16, kind 1 excluded / 3 1-4;
+    // inside one group the slots are ordered by atom index
+    int nsg;
+    const long long* sg_key;
+    const int* sg_off;          // [nsg+1]
+    const int* sg_ent;
     const double2* lj;          // [3][natyps][natyps] (A,B) per LJ code 1..3
     const float2* ljf;
     const uint8_t* ljcod;       // [natyps][natyps]
@@ -66,6 +73,8 @@ struct DevModel {
     const QParF* qw_tabf;
     double xpcent[3], xwcent[3];
     double rexcl_o2;
+    // FP32 copies are stored relative to xpcent, which bounds their magnitude
+    // by the sphere size (FP32 cut-off prefilter and mixed-form pair math)
 };
 
 struct QQEntry {   // static Q-Q / Q-bonded-P pair of one state
@@ -87,6 +96,7 @@ struct DevState {
     int2* ww; int64_t cap_ww;      // water pairs (iw, jw), iw < jw
     int2* pw; int64_t cap_pw;      // (solute atom, water)
     int2* pp; int64_t cap_pp;      // (i, j | code << 28)
+    int2* ppg; int64_t cap_ppg;    // listed solute group pairs (g1 <= g2)
     int* qp;  int64_t cap_qp;      // solute atoms interacting with all Q atoms
     int* qw;  int64_t cap_qw;      // waters interacting with all Q atoms
     QQEntry* qq; int nqq;          // static qq + qqp entries (all states)
@@ -96,7 +106,9 @@ struct DevState {
     int* shell;          // [nwat] shell or -1
     int* rank;           // [nwat]
     int* n_insh;         // [kMaxShell]
+    int* shell_list;     // [kMaxShell][nwat] waters per shell
     double* wstate;      // [3*kMaxShell]: theta_corr, avtheta, avn_insh
+    double* shell_tsum;  // [kMaxShell] per-step sum of theta per shell
 };
 
 // ---- launch wrappers (qnb_kernels.cu) ---------------------------------------
@@ -104,31 +116,50 @@ struct Cut {
     double rcq2, rlrf2, rcpp2, rcpw2, rcww2;
 };
 
-void launch_group_centres(const DevModel& m, DevState& s, cudaStream_t st);
-void launch_build_ww(const DevModel& m, DevState& s, const Cut& c, cudaStream_t st);
-void launch_build_pw(const DevModel& m, DevState& s, const Cut& c, cudaStream_t st);
-void launch_build_pp(const DevModel& m, DevState& s, const Cut& c, cudaStream_t st);
-void launch_build_qp_impl(const DevModel& m, DevState& s, const uint8_t* qnear, double rcq2, cudaStream_t st);
-void launch_build_qw(const DevModel& m, DevState& s, const Cut& c, cudaStream_t st);
-void launch_lrf_accumulate(const DevModel& m, DevState& s, const Cut& c, int mixed, cudaStream_t st);
+// Every launch covers all nwin windows of a context (grid.y = window); s0 is
+// window 0's host-side state (capacities are equal across windows) and ds the
+// device array of all windows' states.
+struct Launch {
+    const DevModel& m;
+    const DevState& s0;
+    const DevState* ds;
+    int nwin;
+    cudaStream_t st;
+};
 
-void launch_pack_mixed(const DevModel& m, DevState& s, cudaStream_t st);
-void launch_nonbond(const DevModel& m, DevState& s, int mixed, int md, cudaStream_t st, int* nlaunch);
-void launch_nonbond_qq(const DevModel& m, DevState& s, int mixed, cudaStream_t st);
-void launch_lrf_taylor_impl(const DevModel& m, DevState& s, const int* iwhich, int mixed, cudaStream_t st);
-void launch_apply_fixed(const DevModel& m, DevState& s, cudaStream_t st);
+void launch_pack(const Launch& L);
+void launch_reset_counts(const Launch& L, unsigned keep_mask);
+void launch_group_centres(const Launch& L);
+void launch_build_ww(const Launch& L, const Cut& c);
+void launch_build_pw(const Launch& L, const Cut& c);
+void launch_build_pp(const Launch& L, const Cut& c);
+void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2);
+void launch_build_qw(const Launch& L, const Cut& c);
+void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed);
+
+void launch_ww(const Launch& L, int mixed);
+void launch_qw(const Launch& L, int mixed);
+void launch_pw(const Launch& L, int mixed);
+void launch_pp(const Launch& L, int mixed);
+void launch_qp(const Launch& L, int mixed);
+void launch_nonbond_qq(const Launch& L, int mixed);
+void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed);
+void launch_apply_fixed(const Launch& L);
+
+// kernel classes timed by the optional event profiler
+enum { K_WW = 0, K_QW, K_PW, K_PP, K_QP, K_LRF_TAYLOR, K_QQ, K_RESTRAIN, K_WATPOL, K_PACK, K_APPLY,
+       K_BUILD, K_LRF_BUILD, K_NUM };
 
 struct SolventDev {
     double fk_wsphere, Dwmz, awmz, rwat, boltz, fkwpol, itdis;
     int wpol, nshell;
     double rout[kMaxShell], dr[kMaxShell], cstb[kMaxShell];
 };
-void launch_restrain_solvent_impl(const DevModel& m, DevState& s, const SolventDev& p, double Tfree, int mixed,
-                                  const int* wsw, const uint8_t* heavy_solv, cudaStream_t st);
-void launch_watpol_impl(const DevModel& m, DevState& s, const SolventDev& p, int istep, int md, int mixed,
-                        double* shell_tsum, cudaStream_t st, int* nlaunch);
+void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
+                             const uint8_t* heavy_solv);
+int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int mixed);
 
-void launch_export_pairs(const DevModel& m, const DevState& s, int kind, int32_t* di, int32_t* dj,
-                         int64_t cap, int* dcount, cudaStream_t st);
+void launch_export_pairs(const Launch& L, int win, int kind, int32_t* di, int32_t* dj, int64_t cap,
+                         int* dcount);
 
 }  // namespace qnb

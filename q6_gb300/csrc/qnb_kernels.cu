@@ -152,7 +152,9 @@ struct ESum<true> {
 // =============================================================================
 
 // cgp_centers, src/nonbondene.f90:43-78: zero the LRF record and set the centre
-__global__ void k_group_centres(DevModel m, const double* __restrict__ x, double* __restrict__ lrf) {
+__global__ void k_group_centres(DevModel m, const DevState* __restrict__ states) {
+    const double* __restrict__ x = states[blockIdx.y].x;
+    double* __restrict__ lrf = states[blockIdx.y].lrf;
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= m.ncgp) return;
     double cx = 0.0, cy = 0.0, cz = 0.0;
@@ -171,36 +173,76 @@ __global__ void k_group_centres(DevModel m, const double* __restrict__ x, double
     for (int k = 3; k < kLrfLen; ++k) L[k] = 0.0;
 }
 
+// FP32 coordinates relative to xpcent, charge in w (cut-off prefilter and
+// mixed-form pair math)
+__global__ void k_pack(DevModel m, const DevState* __restrict__ states) {
+    const double* __restrict__ x = states[blockIdx.y].x;
+    float4* __restrict__ xq = states[blockIdx.y].xq;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m.natom) return;
+    xq[i] = make_float4((float)(x[3 * i] - m.xpcent[0]), (float)(x[3 * i + 1] - m.xpcent[1]),
+                        (float)(x[3 * i + 2] - m.xpcent[2]), (float)m.crg[i]);
+}
+
+__device__ __forceinline__ float r2_f(float4 a, float4 b) {
+    float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// Exact cut-off decision r2 <= rc2.  The FP32 distance of centred
+// coordinates (|x| within the sphere, relative error far below 1e-5 of r2)
+// decides away from the boundary; within 2e-4 of it the FP64 distance in the
+// reference's operation order decides, so the outcome is the FP64 one.
+__device__ __forceinline__ bool within(float r2f, double rc2, const double* __restrict__ x, int a, int b) {
+    float c = (float)rc2;
+    if (r2f < c * 0.9998f) return true;
+    if (r2f > c * 1.0002f) return false;
+    return dist2_exact(x[3 * a], x[3 * a + 1], x[3 * a + 2], x[3 * b], x[3 * b + 1], x[3 * b + 2]) <= rc2;
+}
+
 // nbwwlist(_lrf) pair selection, src/nonbondene.f90:4274-4395: water pairs
 // with O-O r2 <= Rcww2, neither O excluded.  Each unordered pair is kept once
-// (iw < jw), the same set as the reference's parity rule.
-__global__ void k_build_ww(DevModel m, const double* __restrict__ x, int2* __restrict__ out,
-                           int64_t cap, int* __restrict__ cnt, double rc2) {
+// (iw < jw), the same set as the reference's parity rule.  A warp owns rows
+// r and nwat-1-r so every warp scans about nwat candidates.
+__global__ void k_build_ww(DevModel m, const DevState* __restrict__ states, double rc2) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const float4* __restrict__ xq = s.xq;
+    int2* __restrict__ out = s.ww;
+    int64_t cap = s.cap_ww;
+    int* cnt = s.cnt + C_WW;
     int lane = threadIdx.x & 31;
-    for (int iw = warp_id_global(); iw < m.nwat; iw += warps_total()) {
-        int io = m.nat_solute + m.sa * iw;
-        if (m.excl[io]) continue;
-        double xi = x[3 * io], yi = x[3 * io + 1], zi = x[3 * io + 2];
-        for (int j0 = iw + 1; j0 < m.nwat; j0 += kWarp) {
-            int jw = j0 + lane;
-            bool ok = false;
-            if (jw < m.nwat) {
-                int jo = m.nat_solute + m.sa * jw;
-                if (!m.excl[jo]) {
-                    double r2 = dist2_exact(xi, yi, zi, x[3 * jo], x[3 * jo + 1], x[3 * jo + 2]);
-                    ok = (r2 <= rc2);
+    int half = (m.nwat + 1) / 2;
+    for (int w = warp_id_global(); w < half; w += warps_total()) {
+        for (int pass = 0; pass < 2; ++pass) {
+            int iw = pass == 0 ? w : m.nwat - 1 - w;
+            if (pass == 1 && iw == w) break;
+            int io = m.nat_solute + m.sa * iw;
+            if (m.excl[io]) continue;
+            float4 xi = xq[io];
+            for (int j0 = iw + 1; j0 < m.nwat; j0 += kWarp) {
+                int jw = j0 + lane;
+                bool ok = false;
+                if (jw < m.nwat) {
+                    int jo = m.nat_solute + m.sa * jw;
+                    if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), rc2, x, io, jo);
                 }
+                int pos = warp_append(cnt, ok ? 1 : 0);
+                if (ok && pos < cap) out[pos] = make_int2(iw, jw);
             }
-            int pos = warp_append(cnt, ok ? 1 : 0);
-            if (ok && pos < cap) out[pos] = make_int2(iw, jw);
         }
     }
 }
 
 // nbpwlist(_lrf), src/nonbondene.f90:2842-2955: solute group switch atom to
 // water O within Rcpw; every non-Q atom of the group pairs with the molecule.
-__global__ void k_build_pw(DevModel m, const double* __restrict__ x, int2* __restrict__ out,
-                           int64_t cap, int* __restrict__ cnt, double rc2) {
+__global__ void k_build_pw(DevModel m, const DevState* __restrict__ states, double rc2) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const float4* __restrict__ xq = s.xq;
+    int2* __restrict__ out = s.pw;
+    int64_t cap = s.cap_pw;
+    int* cnt = s.cnt + C_PW;
     int lane = threadIdx.x & 31;
     for (int ig = warp_id_global(); ig < m.ncgp_solute; ig += warps_total()) {
         int is = m.gsw[ig];
@@ -209,16 +251,13 @@ __global__ void k_build_pw(DevModel m, const double* __restrict__ x, int2* __res
         int nq = 0;
         for (int a = a0; a < a1; ++a) nq += (m.iqatom[m.gatom[a]] < 0);
         if (nq == 0) continue;
-        double xi = x[3 * is], yi = x[3 * is + 1], zi = x[3 * is + 2];
+        float4 xi = xq[is];
         for (int j0 = 0; j0 < m.nwat; j0 += kWarp) {
             int jw = j0 + lane;
             bool ok = false;
             if (jw < m.nwat) {
                 int jo = m.nat_solute + m.sa * jw;
-                if (!m.excl[jo]) {
-                    double r2 = dist2_exact(xi, yi, zi, x[3 * jo], x[3 * jo + 1], x[3 * jo + 2]);
-                    ok = (r2 <= rc2);
-                }
+                if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), rc2, x, is, jo);
             }
             int pos = warp_append(cnt, ok ? nq : 0);
             if (ok) {
@@ -233,74 +272,117 @@ __global__ void k_build_pw(DevModel m, const double* __restrict__ x, int2* __res
     }
 }
 
-// classification of one solute atom pair as pp_int_comp does it
-// (src/simprep.f90:2992-3053): 0 = excluded, 3 = 1-4, else ljcod
-__device__ __forceinline__ int pp_code(const DevModel& m, int i, int j) {
-    int lo = i < j ? i : j, hi = i < j ? j : i;
-    for (int k = m.spec_off[lo]; k < m.spec_off[lo + 1]; ++k)
-        if (m.spec_j[k] == hi) return m.spec_kind[k] == 1 ? 0 : 3;
-    return m.ljcod[m.iac[i] * m.natyps + m.iac[j]];
+// special (excluded / 1-4) status of one atom pair of a solute group pair
+__device__ __forceinline__ int sg_find(const DevModel& m, long long key) {
+    int lo = 0, hi = m.nsg - 1;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        long long k = m.sg_key[mid];
+        if (k == key) return mid;
+        if (k < key) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return -1;
+}
+__device__ __forceinline__ int sg_kind(const DevModel& m, int sgi, int sa, int sb) {
+    if (sgi < 0) return 0;
+    int want = sa | (sb << 8);
+    for (int k = m.sg_off[sgi]; k < m.sg_off[sgi + 1]; ++k) {
+        int e = m.sg_ent[k];
+        if ((e & 0xffff) == want) return e >> 16;
+    }
+    return 0;
 }
 
-// is the pair in the reference's list (pp_map != 0 and precomp%set)?
-// precompute_set_values_pp, src/simprep.f90:3321-3350
-__device__ __forceinline__ int pp_accept(const DevModel& m, int i, int j) {
-    if (m.iqatom[i] >= 0 || m.iqatom[j] >= 0) return 0;
-    int code = pp_code(m, i, j);
-    if (code == 0) return 0;
+// reference list membership and LJ code of atom pair (i, j) of a solute group
+// pair: pp_int_comp + precompute_set_values_pp, src/simprep.f90:2952-3065,
+// 3321-3350 (0 = not listed, 3 = 1-4, else ljcod)
+__device__ __forceinline__ int pp_accept(const DevModel& m, int i, int j, int kind) {
+    if (kind == 1) return 0;
+    int code = kind == 3 ? 3 : m.ljcod[m.iac[i] * m.natyps + m.iac[j]];
     int ti = m.iac[i], tj = m.iac[j];
     bool set = m.ljset[((code - 1) * m.natyps + ti) * m.natyps + tj] ||
                fabs(__dmul_rn(m.crg[i], m.crg[j])) > 1.0e-10;
     return set ? code : 0;
 }
 
-// nbpplist(_lrf), src/nonbondene.f90:1777-1908: solute group pairs whose
-// switch atoms are within Rcpp, expanded to the accepted atom pairs.
-__global__ void k_build_pp(DevModel m, const double* __restrict__ x, int2* __restrict__ out,
-                           int64_t cap, int* __restrict__ cnt, int* __restrict__ cnt14, double rc2) {
+// nbpplist(_lrf) group selection, src/nonbondene.f90:1777-1908: solute group
+// pairs whose switch atoms are within Rcpp (g1 <= g2; a group with itself is
+// always listed).  Rows are paired like k_build_ww for balance.
+__global__ void k_build_pp_groups(DevModel m, const DevState* __restrict__ states, double rc2) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const float4* __restrict__ xq = s.xq;
+    int2* __restrict__ out = s.ppg;
+    int64_t cap = s.cap_ppg;
+    int* cnt = s.cnt + C_PPG;
     int lane = threadIdx.x & 31;
-    for (int ig = warp_id_global(); ig < m.ncgp_solute; ig += warps_total()) {
-        int is = m.gsw[ig];
-        if (m.excl[is]) continue;
-        int a0 = m.gslot[ig], a1 = m.gslot[ig + 1];
-        double xi = x[3 * is], yi = x[3 * is + 1], zi = x[3 * is + 2];
-        for (int j0 = ig; j0 < m.ncgp_solute; j0 += kWarp) {
-            int jg = j0 + lane;
-            bool ok = false;
-            if (jg < m.ncgp_solute) {
-                int js = m.gsw[jg];
-                if (!m.excl[js]) {
-                    double r2 = (jg == ig) ? 0.0
-                                           : dist2_exact(xi, yi, zi, x[3 * js], x[3 * js + 1], x[3 * js + 2]);
-                    ok = (r2 <= rc2);
+    int G = m.ncgp_solute, half = (G + 1) / 2;
+    for (int w = warp_id_global(); w < half; w += warps_total()) {
+        for (int pass = 0; pass < 2; ++pass) {
+            int g1 = pass == 0 ? w : G - 1 - w;
+            if (pass == 1 && g1 == w) break;
+            int s1 = m.gsw[g1];
+            if (m.excl[s1]) continue;
+            float4 x1 = xq[s1];
+            for (int j0 = g1; j0 < G; j0 += kWarp) {
+                int g2 = j0 + lane;
+                bool ok = false;
+                if (g2 < G) {
+                    int s2 = m.gsw[g2];
+                    if (!m.excl[s2]) ok = (g2 == g1) || within(r2_f(x1, xq[s2]), rc2, x, s1, s2);
                 }
+                int pos = warp_append(cnt, ok ? 1 : 0);
+                if (ok && pos < cap) out[pos] = make_int2(g1, g2);
             }
-            int n = 0, n14 = 0;
-            int b0 = 0, b1 = 0;
-            if (ok) {
-                b0 = m.gslot[jg];
-                b1 = m.gslot[jg + 1];
-                for (int a = a0; a < a1; ++a)
-                    for (int b = b0; b < b1; ++b) {
-                        int i = m.gatom[a], j = m.gatom[b];
-                        if (jg == ig && i >= j) continue;
-                        int c = pp_accept(m, i, j);
-                        n += (c != 0);
-                        n14 += (c == 3);
+        }
+    }
+}
+
+// expands listed solute group pairs into the reference's atom pairs
+// (i, j | code << 28); one thread per group pair
+__global__ void k_expand_pp(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
+    const int2* __restrict__ groups = s.ppg;
+    const int* ngroups = s.cnt + C_PPG;
+    int64_t gcap = s.cap_ppg;
+    int2* __restrict__ out = s.pp;
+    int64_t cap = s.cap_pp;
+    int* cnt = s.cnt + C_PP;
+    int* cnt14 = s.cnt + C_PP14;
+    int n = min((int64_t)*ngroups, gcap);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        int2 g = groups[p];
+        int a0 = m.gslot[g.x], a1 = m.gslot[g.x + 1], b0 = m.gslot[g.y], b1 = m.gslot[g.y + 1];
+        int sgi = m.nsg ? sg_find(m, (long long)g.x * m.ncgp_solute + g.y) : -1;
+        int na = 0, n14 = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+            int pos = 0;
+            if (pass == 1) {
+                if (na == 0) break;
+                pos = atomicAdd(cnt, na);
+                if (n14) atomicAdd(cnt14, n14);
+            }
+            for (int a = a0; a < a1; ++a) {
+                int i = m.gatom[a];
+                if (m.iqatom[i] >= 0) continue;
+                for (int b = b0; b < b1; ++b) {
+                    int j = m.gatom[b];
+                    if (m.iqatom[j] >= 0) continue;
+                    int sa = a - a0, sb = b - b0;
+                    if (g.x == g.y) {
+                        if (i >= j) continue;
                     }
-            }
-            int pos = warp_append(cnt, n);
-            if (__any_sync(kFull, n14 > 0)) warp_append(cnt14, n14);
-            if (n > 0) {
-                for (int a = a0; a < a1; ++a)
-                    for (int b = b0; b < b1; ++b) {
-                        int i = m.gatom[a], j = m.gatom[b];
-                        if (jg == ig && i >= j) continue;
-                        int c = pp_accept(m, i, j);
-                        if (c == 0) continue;
-                        if (pos < cap) out[pos] = make_int2(i, j | (c << 28));
+                    int code = pp_accept(m, i, j, sg_kind(m, sgi, sa, sb));
+                    if (!code) continue;
+                    if (pass == 0) {
+                        ++na;
+                        n14 += (code == 3);
+                    } else {
+                        if (pos < cap) out[pos] = make_int2(i, j | (code << 28));
                         ++pos;
                     }
+                }
             }
         }
     }
@@ -308,8 +390,13 @@ __global__ void k_build_pp(DevModel m, const double* __restrict__ x, int2* __res
 
 // nbqplist, src/nonbondene.f90:3647-3742: solute groups whose switch atom is
 // within Rcq of the solute centre; atoms not bonded/angled to any Q atom.
-__global__ void k_build_qp(DevModel m, const double* __restrict__ x, const uint8_t* __restrict__ qnear,
-                           int* __restrict__ out, int64_t cap, int* __restrict__ cnt, double rcq2) {
+__global__ void k_build_qp(DevModel m, const DevState* __restrict__ states, const uint8_t* __restrict__ qnear,
+                           double rcq2) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    int* __restrict__ out = s.qp;
+    int64_t cap = s.cap_qp;
+    int* cnt = s.cnt + C_QP;
     int ig = blockIdx.x * blockDim.x + threadIdx.x;
     if (ig >= m.ncgp_solute) return;
     int is = m.gsw[ig];
@@ -325,8 +412,12 @@ __global__ void k_build_qp(DevModel m, const double* __restrict__ x, const uint8
 }
 
 // nbqwlist, src/nonbondene.f90:3862-3944: waters with O within Rcq of xpcent
-__global__ void k_build_qw(DevModel m, const double* __restrict__ x, int* __restrict__ out, int64_t cap,
-                           int* __restrict__ cnt, double rcq2) {
+__global__ void k_build_qw(DevModel m, const DevState* __restrict__ states, double rcq2) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    int* __restrict__ out = s.qw;
+    int64_t cap = s.cap_qw;
+    int* cnt = s.cnt + C_QW;
     int iw = blockIdx.x * blockDim.x + threadIdx.x;
     if (iw >= m.nwat) return;
     int io = m.nat_solute + m.sa * iw;
@@ -352,8 +443,16 @@ __device__ __forceinline__ int group_dist_atom(const DevModel& m, int g) {
 template <typename T>
 __device__ __forceinline__ void lrf_terms(T dx, T dy, T dz, T q, T* acc) {
     T r2 = dx * dx + dy * dy + dz * dz;
-    T f0 = q / (r2 * sqrt(r2));
-    T f1 = T(3) * f0 / r2;
+    T f0, f1;
+    if constexpr (std::is_same<T, float>::value) {
+        float ri = rsqrtf(r2);
+        float ri2 = ri * ri;
+        f0 = q * ri * ri2;
+        f1 = 3.0f * f0 * ri2;
+    } else {
+        f0 = q / (r2 * sqrt(r2));
+        f1 = T(3) * f0 / r2;
+    }
     T f2 = -f1 / r2;
     T d[3] = {dx, dy, dz};
     acc[0] += f0 * r2;
@@ -393,9 +492,22 @@ __device__ __forceinline__ void lrf_terms(T dx, T dy, T dz, T q, T* acc) {
     P[24] -= u0; P[25] -= u1; P[26] -= T(3) * u2;
 }
 
+// LRF classification of a group pair: true when rc2 < r2 <= rlrf2 in FP64
+__device__ __forceinline__ bool lrf_pair(float r2f, double rc2, double rlrf2, const double* __restrict__ x, int a,
+                                         int b) {
+    float c1 = (float)rc2, c2 = (float)rlrf2;
+    if (r2f > c1 * 1.0002f && r2f < c2 * 0.9998f) return true;
+    if (r2f < c1 * 0.9998f || r2f > c2 * 1.0002f) return false;
+    double r2 = dist2_exact(x[3 * a], x[3 * a + 1], x[3 * a + 2], x[3 * b], x[3 * b + 1], x[3 * b + 2]);
+    return r2 > rc2 && r2 <= rlrf2;
+}
+
 template <bool MIX>
-__global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const double* __restrict__ x,
-                                                         double* __restrict__ lrf, Cut c) {
+__global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const DevState* __restrict__ states, Cut c) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const float4* __restrict__ xq = s.xq;
+    double* __restrict__ lrf = s.lrf;
     typedef typename std::conditional<MIX, float, double>::type T;
     int lane = threadIdx.x & 31;
     for (int g2 = warp_id_global(); g2 < m.ncgp; g2 += warps_total()) {
@@ -404,7 +516,8 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const double
         bool sol2 = g2 < m.ncgp_solute;
         double* L = lrf + (size_t)g2 * kLrfLen;
         double cx = L[0], cy = L[1], cz = L[2];
-        double xs = x[3 * s2], ys = x[3 * s2 + 1], zs = x[3 * s2 + 2];
+        float4 x2 = xq[s2];
+        float cxf = (float)(cx - m.xpcent[0]), cyf = (float)(cy - m.xpcent[1]), czf = (float)(cz - m.xpcent[2]);
         T acc[40];
 #pragma unroll
         for (int k = 0; k < 40; ++k) acc[k] = T(0);
@@ -414,13 +527,16 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const double
             if (m.excl[s1]) continue;
             bool sol1 = g1 < m.ncgp_solute;
             double rc2 = (sol1 && sol2) ? c.rcpp2 : ((sol1 || sol2) ? c.rcpw2 : c.rcww2);
-            double r2 = dist2_exact(xs, ys, zs, x[3 * s1], x[3 * s1 + 1], x[3 * s1 + 2]);
-            if (r2 <= rc2 || r2 > c.rlrf2) continue;
+            if (!lrf_pair(r2_f(x2, xq[s1]), rc2, c.rlrf2, x, s2, s1)) continue;
             for (int a = m.gslot[g1]; a < m.gslot[g1 + 1]; ++a) {
                 int i = m.gatom[a];
                 if (m.iqatom[i] >= 0) continue;
-                T dx = T(x[3 * i] - cx), dy = T(x[3 * i + 1] - cy), dz = T(x[3 * i + 2] - cz);
-                lrf_terms<T>(dx, dy, dz, T(m.crg[i]), acc);
+                if constexpr (MIX) {
+                    float4 xi = xq[i];
+                    lrf_terms<float>(xi.x - cxf, xi.y - cyf, xi.z - czf, xi.w, acc);
+                } else {
+                    lrf_terms<double>(x[3 * i] - cx, x[3 * i + 1] - cy, x[3 * i + 2] - cz, m.crg[i], acc);
+                }
             }
         }
 #pragma unroll
@@ -435,11 +551,6 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const double
 // Force / energy kernels
 // =============================================================================
 
-__global__ void k_pack_mixed(DevModel m, const double* __restrict__ x, float4* __restrict__ xq) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m.natom) return;
-    xq[i] = make_float4((float)x[3 * i], (float)x[3 * i + 1], (float)x[3 * i + 2], (float)m.crg[i]);
-}
 
 // one plain pair (nbe, src/nonbonded.f90:45-75); returns dv, vec via refs
 struct PairD {
@@ -492,7 +603,8 @@ __device__ __forceinline__ PairF nbe_f(float4 a, float4 b, float A, float B, flo
 
 // nonbond_ww_spc / nonbond_ww, src/nonbondene.f90:5886-5975, 5509-5573
 template <bool MIX, bool SPC>
-__global__ void __launch_bounds__(256) k_ww(DevModel m, DevState s) {
+__global__ void __launch_bounds__(256) k_ww(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> eel, evdw;
     int n = min((int64_t)s.cnt[C_WW], s.cap_ww);
@@ -542,7 +654,8 @@ __global__ void __launch_bounds__(256) k_ww(DevModel m, DevState s) {
 
 // nonbond_pw, src/nonbondene.f90:4856-4916 (pw_precomp, src/simprep.f90:3354-3386)
 template <bool MIX>
-__global__ void __launch_bounds__(256) k_pw(DevModel m, DevState s) {
+__global__ void __launch_bounds__(256) k_pw(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> eel, evdw;
     int n = min((int64_t)s.cnt[C_PW], s.cap_pw);
@@ -586,7 +699,8 @@ __global__ void __launch_bounds__(256) k_pw(DevModel m, DevState s) {
 
 // nonbond_pp, src/nonbondene.f90:4694-4760 (pp_precomp values)
 template <bool MIX>
-__global__ void __launch_bounds__(256) k_pp(DevModel m, DevState s) {
+__global__ void __launch_bounds__(256) k_pp(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> eel, evdw;
     int n = min((int64_t)s.cnt[C_PP], s.cap_pp);
@@ -620,35 +734,9 @@ __global__ void __launch_bounds__(256) k_pp(DevModel m, DevState s) {
     evdw.flush(acc, E_PP_VDW);
 }
 
-// Q-atom x environment.  One thread per environment atom (qp) or molecule
-// (qw) loops over the Q atoms; the Q-atom gradients are summed per block in
-// shared memory and added once per block.
-template <bool MIX>
-struct QShared;
-template <>
-struct QShared<false> {
-    double* g;
-    __device__ __forceinline__ void add(int iq, double gx, double gy, double gz) {
-        atomicAdd(g + 3 * iq, gx);
-        atomicAdd(g + 3 * iq + 1, gy);
-        atomicAdd(g + 3 * iq + 2, gz);
-    }
-};
-template <>
-struct QShared<true> {
-    unsigned long long* g;
-    __device__ __forceinline__ void add(int iq, float gx, float gy, float gz) {
-        atomicAdd(g + 3 * iq, to_fix(gx));
-        atomicAdd(g + 3 * iq + 1, to_fix(gy));
-        atomicAdd(g + 3 * iq + 2, to_fix(gz));
-    }
-};
-
 // nbe_qx soft-core pair for one state, src/nonbonded.f90:200-222
-__device__ __forceinline__ void nbe_qx_d(double r2, double r, double r6inv_hc_, double A, double B,
-                                         double el, double sc, double lam, double& vel, double& vdw,
-                                         double& dv) {
-    double r6_hc = r6inv_hc_;          // = 1 / dist%r6 = |r|^6
+__device__ __forceinline__ void nbe_qx_d(double r2, double r, double r6_hc, double A, double B, double el,
+                                         double sc, double lam, double& vel, double& vdw, double& dv) {
     double r6 = 1.0 / (r6_hc + sc);
     double r12 = r6 * r6;
     vel = el * r;
@@ -656,9 +744,9 @@ __device__ __forceinline__ void nbe_qx_d(double r2, double r, double r6inv_hc_, 
     vdw = va - vb;
     dv = r2 * (-vel - (12.0 * va - 6.0 * vb) * r6 * r6_hc) * lam;
 }
-__device__ __forceinline__ void nbe_qx_f(float r2, float r, float r6_hc, float A, float B, float el,
-                                         float sc, float lam, float& vel, float& vdw, float& dv) {
-    float r6 = 1.0f / (r6_hc + sc);
+__device__ __forceinline__ void nbe_qx_f(float r2, float r, float r6_hc, float A, float B, float el, float sc,
+                                         float lam, float& vel, float& vdw, float& dv) {
+    float r6 = __frcp_rn(r6_hc + sc);
     float r12 = r6 * r6;
     vel = el * r;
     float va = A * r12, vb = B * r6;
@@ -667,26 +755,62 @@ __device__ __forceinline__ void nbe_qx_f(float r2, float r, float r6_hc, float A
 }
 
 constexpr int kMaxQ = 64;
+constexpr int kQBlock = 256;   // threads per block of the Q kernels
 
-// nonbond_qw_spc / nonbond_qw, src/nonbondene.f90:5658-5767, 5339-5418
-template <bool MIX, bool SPC>
-__global__ void __launch_bounds__(256) k_qw(DevModel m, DevState s) {
+// Q-atom gradients: every lane keeps its Q atoms' sums in registers; at the
+// end the warps of a block combine them in shared memory and the block adds
+// them once (fixed point in the mixed form).
+template <bool MIX>
+__device__ __forceinline__ void flush_q_grad(const DevModel& m, const DevState& s, const float (&gqf)[2][3],
+                                             const double (&gqd)[2][3]) {
     typedef typename std::conditional<MIX, unsigned long long, double>::type GT;
-    __shared__ GT gq[3 * kMaxQ];
-    for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) gq[k] = GT(0);
+    __shared__ GT red[3 * kMaxQ];
+    for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) red[k] = GT(0);
     __syncthreads();
-    QShared<MIX> qs{gq};
+    int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < kMaxQ / 32; ++k) {
+        int iq = k * 32 + lane;
+        if (iq >= m.nqat) break;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if constexpr (MIX) atomicAdd(&red[3 * iq + c], to_fix(gqf[k][c]));
+            else atomicAdd(&red[3 * iq + c], gqd[k][c]);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) {
+        int i = m.iqseq[k / 3];
+        if constexpr (MIX) atomicAdd(s.fix + 3 * i + k % 3, (unsigned long long)red[k]);
+        else atomicAdd(s.d + 3 * i + k % 3, (double)red[k]);
+    }
+}
+
+// nonbond_qw_spc / nonbond_qw, src/nonbondene.f90:5658-5767, 5339-5418:
+// one warp per listed water molecule, lane = Q atom.
+template <bool MIX, bool SPC>
+__global__ void __launch_bounds__(kQBlock) k_qw(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> eel[kMaxStates], evdw[kMaxStates];
+    float gqf[2][3] = {};
+    double gqd[2][3] = {};
+    int lane = threadIdx.x & 31;
     int n = min((int64_t)s.cnt[C_QW], s.cap_qw);
     int sa = m.sa, S = m.S;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    for (int p = warp_id_global(); p < n; p += warps_total()) {
         int j0 = m.nat_solute + sa * s.qw[p];
-        for (int iq = 0; iq < m.nqat; ++iq) {
-            int i = m.iqseq[iq];
-            for (int a = 0; a < sa; ++a) {
-                int j = j0 + a;
-                bool lj = !SPC || a == 0;
+        for (int a = 0; a < sa; ++a) {
+            int j = j0 + a;
+            bool lj = !SPC || a == 0;
+            float gjf[3] = {0, 0, 0};
+            double gjd[3] = {0, 0, 0};
+#pragma unroll
+            for (int k = 0; k < kMaxQ / 32; ++k) {
+                int iq = k * 32 + lane;
+                if (iq >= m.nqat) break;
+                int i = m.iqseq[iq];
+                const QPar* P = m.qw_tab + (iq * sa + a) * S;
                 if constexpr (!MIX) {
                     double tx = s.x[3 * j] - s.x[3 * i], ty = s.x[3 * j + 1] - s.x[3 * i + 1],
                            tz = s.x[3 * j + 2] - s.x[3 * i + 2];
@@ -694,10 +818,9 @@ __global__ void __launch_bounds__(256) k_qw(DevModel m, DevState s) {
                     double r = sqrt(r2);
                     double dvs = 0.0;
                     if (lj) {
-                        double r6 = r2 * r2 * r2;
-                        double r6hc = 1.0 / r6;
+                        double r6hc = 1.0 / (r2 * r2 * r2);
                         for (int st = 0; st < S; ++st) {
-                            QPar q = m.qw_tab[(iq * sa + a) * S + st];
+                            QPar q = P[st];
                             double vel, vdw, dv;
                             nbe_qx_d(r2, r, r6hc, q.A, q.B, q.el, q.sc, s.lambda[st], vel, vdw, dv);
                             dvs += dv;
@@ -706,25 +829,24 @@ __global__ void __launch_bounds__(256) k_qw(DevModel m, DevState s) {
                         }
                     } else {   // nbe_qspc, src/nonbonded.f90:226-243
                         for (int st = 0; st < S; ++st) {
-                            QPar q = m.qw_tab[(iq * sa + a) * S + st];
-                            double vel = q.el * r;
+                            double vel = P[st].el * r;
                             dvs += -r2 * vel * s.lambda[st];
                             eel[st].add(vel);
                         }
                     }
-                    qs.add(iq, -tx * dvs, -ty * dvs, -tz * dvs);
-                    acc.grad(j, tx * dvs, ty * dvs, tz * dvs);
+                    gqd[k][0] -= tx * dvs; gqd[k][1] -= ty * dvs; gqd[k][2] -= tz * dvs;
+                    gjd[0] += tx * dvs; gjd[1] += ty * dvs; gjd[2] += tz * dvs;
                 } else {
+                    const QParF* F = m.qw_tabf + (iq * sa + a) * S;
                     float4 xi = s.xq[i], xj = s.xq[j];
                     float tx = xj.x - xi.x, ty = xj.y - xi.y, tz = xj.z - xi.z;
                     float ri = rsqrtf(tx * tx + ty * ty + tz * tz);
                     float r2 = ri * ri;
                     float dvs = 0.0f;
                     if (lj) {
-                        float r6 = r2 * r2 * r2;
-                        float r6hc = 1.0f / r6;
+                        float r6hc = __frcp_rn(r2 * r2 * r2);
                         for (int st = 0; st < S; ++st) {
-                            QParF q = m.qw_tabf[(iq * sa + a) * S + st];
+                            QParF q = F[st];
                             float vel, vdw, dv;
                             nbe_qx_f(r2, ri, r6hc, q.A, q.B, q.el, q.sc, (float)s.lambda[st], vel, vdw, dv);
                             dvs += dv;
@@ -733,15 +855,27 @@ __global__ void __launch_bounds__(256) k_qw(DevModel m, DevState s) {
                         }
                     } else {
                         for (int st = 0; st < S; ++st) {
-                            QParF q = m.qw_tabf[(iq * sa + a) * S + st];
-                            float vel = q.el * ri;
+                            float vel = F[st].el * ri;
                             dvs += -r2 * vel * (float)s.lambda[st];
                             eel[st].add(vel);
                         }
                     }
-                    qs.add(iq, -tx * dvs, -ty * dvs, -tz * dvs);
-                    acc.grad(j, tx * dvs, ty * dvs, tz * dvs);
+                    gqf[k][0] -= tx * dvs; gqf[k][1] -= ty * dvs; gqf[k][2] -= tz * dvs;
+                    gjf[0] += tx * dvs; gjf[1] += ty * dvs; gjf[2] += tz * dvs;
                 }
+            }
+            // molecule atom gradient: sum over the warp's Q atoms
+            if constexpr (MIX) {
+                unsigned long long v0 = warp_sum(to_fix(gjf[0])), v1 = warp_sum(to_fix(gjf[1])),
+                                   v2 = warp_sum(to_fix(gjf[2]));
+                if (lane == 0) {
+                    atomicAdd(s.fix + 3 * j, v0);
+                    atomicAdd(s.fix + 3 * j + 1, v1);
+                    atomicAdd(s.fix + 3 * j + 2, v2);
+                }
+            } else {
+                double v0 = warp_sum(gjd[0]), v1 = warp_sum(gjd[1]), v2 = warp_sum(gjd[2]);
+                if (lane == 0) acc.grad(j, v0, v1, v2);
             }
         }
     }
@@ -749,29 +883,29 @@ __global__ void __launch_bounds__(256) k_qw(DevModel m, DevState s) {
         eel[st].flush(acc, eq_slot(st, 4));
         evdw[st].flush(acc, eq_slot(st, 5));
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) {
-        int i = m.iqseq[k / 3];
-        if constexpr (MIX) atomicAdd(s.fix + 3 * i + k % 3, (unsigned long long)gq[k]);
-        else atomicAdd(s.d + 3 * i + k % 3, (double)gq[k]);
-    }
+    flush_q_grad<MIX>(m, s, gqf, gqd);
 }
 
-// nonbond_qp, src/nonbondene.f90:5157-5230 (qp_precomp, src/simprep.f90:3112-3148)
+// nonbond_qp, src/nonbondene.f90:5157-5230 (qp_precomp, src/simprep.f90:3112-3148):
+// one warp per listed solute atom, lane = Q atom.
 template <bool MIX>
-__global__ void __launch_bounds__(256) k_qp(DevModel m, DevState s) {
-    typedef typename std::conditional<MIX, unsigned long long, double>::type GT;
-    __shared__ GT gq[3 * kMaxQ];
-    for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) gq[k] = GT(0);
-    __syncthreads();
-    QShared<MIX> qs{gq};
+__global__ void __launch_bounds__(kQBlock) k_qp(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> eel[kMaxStates], evdw[kMaxStates];
+    float gqf[2][3] = {};
+    double gqd[2][3] = {};
+    int lane = threadIdx.x & 31;
     int n = min((int64_t)s.cnt[C_QP], s.cap_qp);
     int S = m.S;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    for (int p = warp_id_global(); p < n; p += warps_total()) {
         int j = s.qp[p];
-        for (int iq = 0; iq < m.nqat; ++iq) {
+        float gjf[3] = {0, 0, 0};
+        double gjd[3] = {0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < kMaxQ / 32; ++k) {
+            int iq = k * 32 + lane;
+            if (iq >= m.nqat) break;
             int i = m.iqseq[iq];
             size_t t0 = ((size_t)j * m.nqat + iq) * S;
             if constexpr (!MIX) {
@@ -779,8 +913,7 @@ __global__ void __launch_bounds__(256) k_qp(DevModel m, DevState s) {
                        tz = s.x[3 * j + 2] - s.x[3 * i + 2];
                 double r2 = 1.0 / (tx * tx + ty * ty + tz * tz);
                 double r = sqrt(r2);
-                double r6 = r2 * r2 * r2;
-                double r6hc = 1.0 / r6;
+                double r6hc = 1.0 / (r2 * r2 * r2);
                 double dvs = 0.0;
                 for (int st = 0; st < S; ++st) {
                     QPar q = m.qp_tab[t0 + st];
@@ -790,15 +923,14 @@ __global__ void __launch_bounds__(256) k_qp(DevModel m, DevState s) {
                     eel[st].add(vel);
                     evdw[st].add(vdw);
                 }
-                qs.add(iq, -tx * dvs, -ty * dvs, -tz * dvs);
-                acc.grad(j, tx * dvs, ty * dvs, tz * dvs);
+                gqd[k][0] -= tx * dvs; gqd[k][1] -= ty * dvs; gqd[k][2] -= tz * dvs;
+                gjd[0] += tx * dvs; gjd[1] += ty * dvs; gjd[2] += tz * dvs;
             } else {
                 float4 xi = s.xq[i], xj = s.xq[j];
                 float tx = xj.x - xi.x, ty = xj.y - xi.y, tz = xj.z - xi.z;
                 float ri = rsqrtf(tx * tx + ty * ty + tz * tz);
                 float r2 = ri * ri;
-                float r6 = r2 * r2 * r2;
-                float r6hc = 1.0f / r6;
+                float r6hc = __frcp_rn(r2 * r2 * r2);
                 float dvs = 0.0f;
                 for (int st = 0; st < S; ++st) {
                     QParF q = m.qp_tabf[t0 + st];
@@ -808,27 +940,35 @@ __global__ void __launch_bounds__(256) k_qp(DevModel m, DevState s) {
                     eel[st].add(vel);
                     evdw[st].add(vdw);
                 }
-                qs.add(iq, -tx * dvs, -ty * dvs, -tz * dvs);
-                acc.grad(j, tx * dvs, ty * dvs, tz * dvs);
+                gqf[k][0] -= tx * dvs; gqf[k][1] -= ty * dvs; gqf[k][2] -= tz * dvs;
+                gjf[0] += tx * dvs; gjf[1] += ty * dvs; gjf[2] += tz * dvs;
             }
+        }
+        if constexpr (MIX) {
+            unsigned long long v0 = warp_sum(to_fix(gjf[0])), v1 = warp_sum(to_fix(gjf[1])),
+                               v2 = warp_sum(to_fix(gjf[2]));
+            if (lane == 0) {
+                atomicAdd(s.fix + 3 * j, v0);
+                atomicAdd(s.fix + 3 * j + 1, v1);
+                atomicAdd(s.fix + 3 * j + 2, v2);
+            }
+        } else {
+            double v0 = warp_sum(gjd[0]), v1 = warp_sum(gjd[1]), v2 = warp_sum(gjd[2]);
+            if (lane == 0) acc.grad(j, v0, v1, v2);
         }
     }
     for (int st = 0; st < S; ++st) {
         eel[st].flush(acc, eq_slot(st, 2));
         evdw[st].flush(acc, eq_slot(st, 3));
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) {
-        int i = m.iqseq[k / 3];
-        if constexpr (MIX) atomicAdd(s.fix + 3 * i + k % 3, (unsigned long long)gq[k]);
-        else atomicAdd(s.d + 3 * i + k % 3, (double)gq[k]);
-    }
+    flush_q_grad<MIX>(m, s, gqf, gqd);
 }
 
 // nonbond_qq + nonbond_qqp (static lists), src/nonbondene.f90:5013-5153,
 // pair kernel nbe_qq, src/nonbonded.f90:111-150.  Always FP64: few pairs.
 template <bool MIX>
-__global__ void k_qq(DevModel m, DevState s) {
+__global__ void k_qq(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= s.nqq) return;
@@ -868,7 +1008,8 @@ __global__ void k_qq(DevModel m, DevState s) {
 
 // lrf_taylor, src/nonbondene.f90:507-571 (FP64 in both forms)
 template <bool MIX>
-__global__ void __launch_bounds__(256) k_lrf_taylor(DevModel m, DevState s, const int* __restrict__ iwhich) {
+__global__ void __launch_bounds__(256) k_lrf_taylor(DevModel m, const DevState* __restrict__ states, const int* __restrict__ iwhich) {
+    const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> elrf;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.natom; i += gridDim.x * blockDim.x) {
@@ -901,7 +1042,9 @@ __global__ void __launch_bounds__(256) k_lrf_taylor(DevModel m, DevState s, cons
 }
 
 // mixed form: add the fixed-point gradient into d and clear it
-__global__ void k_apply_fixed(int n, unsigned long long* __restrict__ fix, double* __restrict__ d) {
+__global__ void k_apply_fixed(int n, const DevState* __restrict__ states) {
+    unsigned long long* __restrict__ fix = states[blockIdx.y].fix;
+    double* __restrict__ d = states[blockIdx.y].d;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         long long v = (long long)fix[k];
         if (v != 0) {
@@ -917,8 +1060,9 @@ __global__ void k_apply_fixed(int n, unsigned long long* __restrict__ fix, doubl
 
 // restrain_solvent, src/nonbondene.f90:6466-6544
 template <bool MIX>
-__global__ void k_restrain_solvent(DevModel m, DevState s, SolventDev p, double shift,
+__global__ void k_restrain_solvent(DevModel m, const DevState* __restrict__ states, SolventDev p, double shift,
                                    const int* __restrict__ wsw, const uint8_t* __restrict__ heavy_solv) {
+    const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> er;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < m.nwat; w += gridDim.x * blockDim.x) {
@@ -990,7 +1134,8 @@ __device__ __forceinline__ void water_vectors(const DevModel& m, const double* x
     rcx /= rc; rcy /= rc; rcz /= rc;
 }
 
-__global__ void k_watpol_theta(DevModel m, DevState s, SolventDev p) {
+__global__ void k_watpol_theta(DevModel m, const DevState* __restrict__ states, SolventDev p) {
+    const DevState& s = states[blockIdx.y];
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= m.nwat) return;
     s.shell[w] = -1;
@@ -1009,29 +1154,54 @@ __global__ void k_watpol_theta(DevModel m, DevState s, SolventDev p) {
             if (rc <= p.rout[is]) break;
         if (is < 0) is = 0;
         s.shell[w] = is;
-        atomicAdd(s.n_insh + is, 1);
+        int k = atomicAdd(s.n_insh + is, 1);
+        s.shell_list[(size_t)is * m.nwat + k] = w;
     }
 }
 
 // stable selection order of src/nonbondene.f90:6612-6628: rank = number of
 // waters of the same shell with smaller theta, ties broken by water index
-__global__ void k_watpol_rank(DevModel m, DevState s) {
-    int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= m.nwat) return;
-    int sh = s.shell[w];
-    if (sh < 0) return;
-    double t = s.theta[w];
-    int r = 0;
-    for (int v = 0; v < m.nwat; ++v) {
-        if (s.shell[v] != sh) continue;
-        double tv = s.theta[v];
-        r += (tv < t) || (tv == t && v < w);
+// (the reference scans the shell in water order and keeps the first minimum).
+// One block per shell; the shell's thetas are staged in shared memory.
+__global__ void __launch_bounds__(256) k_watpol_rank(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
+    // theta >= 0, so the bit patterns of the doubles order like the values;
+    // integer compares keep the sort off the (narrow) FP64 pipe
+    __shared__ long long th[1024];
+    __shared__ int ww[1024];
+    int sh = blockIdx.x;
+    int n = s.n_insh[sh];
+    const int* L = s.shell_list + (size_t)sh * m.nwat;
+    for (int base = 0; base < n; base += 1024) {
+        int cn = min(1024, n - base);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cn; k += blockDim.x) {
+            ww[k] = L[base + k];
+            th[k] = __double_as_longlong(s.theta[ww[k]]);
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            int w = L[k];
+            long long t = __double_as_longlong(s.theta[w]);
+            int r = 0;
+            for (int v = 0; v < cn; ++v) r += (th[v] < t) || (th[v] == t && ww[v] < w);
+            if (base == 0) s.rank[w] = r;
+            else s.rank[w] += r;
+        }
     }
-    s.rank[w] = r;
+}
+
+__global__ void k_watpol_reset(const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.x];
+    if (threadIdx.x < kMaxShell) {
+        s.n_insh[threadIdx.x] = 0;
+        s.shell_tsum[threadIdx.x] = 0.0;
+    }
 }
 
 // theta_corr update every itdis steps, src/nonbondene.f90:6630-6645
-__global__ void k_watpol_update(SolventDev p, double* wstate) {
+__global__ void k_watpol_update(SolventDev p, const DevState* __restrict__ states) {
+    double* wstate = states[blockIdx.y].wstate;
     int is = threadIdx.x;
     if (is >= p.nshell) return;
     double* tc = wstate;
@@ -1046,7 +1216,8 @@ __global__ void k_watpol_update(SolventDev p, double* wstate) {
 
 // energy and gradient, src/nonbondene.f90:6646-6742
 template <bool MIX>
-__global__ void k_watpol_force(DevModel m, DevState s, SolventDev p, double* __restrict__ shell_tsum) {
+__global__ void k_watpol_force(DevModel m, const DevState* __restrict__ states, SolventDev p) {
+    const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> ep;
     const double pi = 3.14159265358979323846;
@@ -1061,7 +1232,7 @@ __global__ void k_watpol_force(DevModel m, DevState s, SolventDev p, double* __r
         if (t0 < 0.0) t0 = 0.0;
         if (t0 > pi) t0 = pi;
         double th = s.theta[w];
-        atomicAdd(shell_tsum + sh, th);
+        atomicAdd(s.shell_tsum + sh, th);
         double dth = th - t0 + s.wstate[sh];
         ep.add(0.5 * p.fkwpol * dth * dth);
         double dv = p.fkwpol * dth;
@@ -1088,20 +1259,22 @@ __global__ void k_watpol_force(DevModel m, DevState s, SolventDev p, double* __r
 }
 
 // running averages (md only), src/nonbondene.f90:6738-6741
-__global__ void k_watpol_average(SolventDev p, DevState s, const double* shell_tsum) {
+__global__ void k_watpol_average(SolventDev p, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
     int is = threadIdx.x;
     if (is >= p.nshell) return;
     int n = s.n_insh[is];
     if (n == 0) return;
-    s.wstate[kMaxShell + is] += shell_tsum[is] / (double)n;
+    s.wstate[kMaxShell + is] += s.shell_tsum[is] / (double)n;
     s.wstate[2 * kMaxShell + is] += (double)n;
 }
 
 // =============================================================================
 // list export (parity tests): expand to the reference's atom pairs
 // =============================================================================
-__global__ void k_export(DevModel m, DevState s, int kind, int32_t* __restrict__ oi, int32_t* __restrict__ oj,
-                         int64_t cap, int* __restrict__ ocount) {
+__global__ void k_export(DevModel m, const DevState* __restrict__ states, int win, int kind,
+                         int32_t* __restrict__ oi, int32_t* __restrict__ oj, int64_t cap, int* __restrict__ ocount) {
+    const DevState& s = states[win];
     int sa = m.sa;
     int n = 0, mult = 1;
     switch (kind) {
@@ -1164,127 +1337,141 @@ int blocks_for(int64_t n, int bs, int per_sm) {
     if (b > lim) b = lim;
     return (int)(b < 1 ? 1 : b);
 }
+
+// grid for per-window work `work` (items) in blocks of bs: at most per_sm
+// resident blocks per SM over all windows
+dim3 grid_for(int64_t work, int bs, int per_sm, int nwin) {
+    int64_t b = (work + bs - 1) / bs;
+    int64_t lim = ((int64_t)sms() * per_sm + nwin - 1) / nwin;
+    if (b > lim) b = lim;
+    if (b < 1) b = 1;
+    return dim3((unsigned)b, (unsigned)nwin);
+}
+
 }  // namespace
 
-void launch_group_centres(const DevModel& m, DevState& s, cudaStream_t st) {
-    k_group_centres<<<(m.ncgp + 127) / 128, 128, 0, st>>>(m, s.x, s.lrf);
-}
-void launch_build_ww(const DevModel& m, DevState& s, const Cut& c, cudaStream_t st) {
-    if (m.nwat == 0) return;
-    k_build_ww<<<blocks_for((int64_t)m.nwat * 32, 256, 8), 256, 0, st>>>(m, s.x, s.ww, s.cap_ww, s.cnt + C_WW,
-                                                                          c.rcww2);
-}
-void launch_build_pw(const DevModel& m, DevState& s, const Cut& c, cudaStream_t st) {
-    if (m.nwat == 0 || m.ncgp_solute == 0) return;
-    k_build_pw<<<blocks_for((int64_t)m.ncgp_solute * 32, 256, 8), 256, 0, st>>>(m, s.x, s.pw, s.cap_pw,
-                                                                                 s.cnt + C_PW, c.rcpw2);
-}
-void launch_build_pp(const DevModel& m, DevState& s, const Cut& c, cudaStream_t st) {
-    if (m.ncgp_solute == 0) return;
-    k_build_pp<<<blocks_for((int64_t)m.ncgp_solute * 32, 256, 8), 256, 0, st>>>(
-        m, s.x, s.pp, s.cap_pp, s.cnt + C_PP, s.cnt + C_PP14, c.rcpp2);
-}
-void launch_build_qw(const DevModel& m, DevState& s, const Cut& c, cudaStream_t st) {
-    if (m.nwat == 0 || m.nqat == 0) return;
-    k_build_qw<<<(m.nwat + 255) / 256, 256, 0, st>>>(m, s.x, s.qw, s.cap_qw, s.cnt + C_QW, c.rcq2);
-}
-void launch_build_qp_impl(const DevModel& m, DevState& s, const uint8_t* qnear, double rcq2, cudaStream_t st) {
-    if (m.ncgp_solute == 0 || m.nqat == 0) return;
-    k_build_qp<<<(m.ncgp_solute + 127) / 128, 128, 0, st>>>(m, s.x, qnear, s.qp, s.cap_qp, s.cnt + C_QP, rcq2);
-}
-void launch_lrf_accumulate(const DevModel& m, DevState& s, const Cut& c, int mixed, cudaStream_t st) {
-    int b = blocks_for((int64_t)m.ncgp * 32, 128, 16);
-    if (mixed) k_lrf_accumulate<true><<<b, 128, 0, st>>>(m, s.x, s.lrf, c);
-    else k_lrf_accumulate<false><<<b, 128, 0, st>>>(m, s.x, s.lrf, c);
-}
-void launch_pack_mixed(const DevModel& m, DevState& s, cudaStream_t st) {
-    k_pack_mixed<<<(m.natom + 255) / 256, 256, 0, st>>>(m, s.x, s.xq);
+__global__ void k_reset_counts(const DevState* __restrict__ states, unsigned keep) {
+    int k = threadIdx.x;
+    if (k < C_NUM && !((keep >> k) & 1u)) states[blockIdx.x].cnt[k] = 0;
 }
 
-void launch_nonbond(const DevModel& m, DevState& s, int mixed, int md, cudaStream_t st, int* nl) {
-    const int bs = 256;
-    int bw = blocks_for(s.cap_ww, bs, 8), bp = blocks_for(s.cap_pw, bs, 8), bpp = blocks_for(s.cap_pp, bs, 8);
-    int bq = blocks_for(s.cap_qw, bs, 4), bqp = blocks_for(s.cap_qp, bs, 4);
-    bool spc = m.spc != 0;
-    if (m.natom > m.nat_solute) {
-        if (md) {
-            if (mixed) { if (spc) k_ww<true, true><<<bw, bs, 0, st>>>(m, s); else k_ww<true, false><<<bw, bs, 0, st>>>(m, s); }
-            else { if (spc) k_ww<false, true><<<bw, bs, 0, st>>>(m, s); else k_ww<false, false><<<bw, bs, 0, st>>>(m, s); }
-            ++*nl;
-        }
-        if (m.nqat > 0) {
-            if (mixed) { if (spc) k_qw<true, true><<<bq, bs, 0, st>>>(m, s); else k_qw<true, false><<<bq, bs, 0, st>>>(m, s); }
-            else { if (spc) k_qw<false, true><<<bq, bs, 0, st>>>(m, s); else k_qw<false, false><<<bq, bs, 0, st>>>(m, s); }
-            ++*nl;
-        }
-        if (md && m.ncgp_solute > 0) {
-            if (mixed) k_pw<true><<<bp, bs, 0, st>>>(m, s); else k_pw<false><<<bp, bs, 0, st>>>(m, s);
-            ++*nl;
-        }
-    }
-    if (md && m.ncgp_solute > 0) {
-        if (mixed) k_pp<true><<<bpp, bs, 0, st>>>(m, s); else k_pp<false><<<bpp, bs, 0, st>>>(m, s);
-        ++*nl;
-    }
-    if (m.nqat > 0 && m.nat_solute > 0) {
-        if (mixed) k_qp<true><<<bqp, bs, 0, st>>>(m, s); else k_qp<false><<<bqp, bs, 0, st>>>(m, s);
-        ++*nl;
-    }
+void launch_reset_counts(const Launch& L, unsigned keep_mask) {
+    k_reset_counts<<<L.nwin, 32, 0, L.st>>>(L.ds, keep_mask);
 }
 
-void launch_nonbond_qq(const DevModel& m, DevState& s, int mixed, cudaStream_t st) {
-    if (s.nqq == 0) return;
-    int b = (s.nqq + 127) / 128;
-    if (mixed) k_qq<true><<<b, 128, 0, st>>>(m, s); else k_qq<false><<<b, 128, 0, st>>>(m, s);
+void launch_pack(const Launch& L) {
+    k_pack<<<dim3((L.m.natom + 255) / 256, L.nwin), 256, 0, L.st>>>(L.m, L.ds);
+}
+void launch_group_centres(const Launch& L) {
+    k_group_centres<<<dim3((L.m.ncgp + 63) / 64, L.nwin), 64, 0, L.st>>>(L.m, L.ds);
+}
+void launch_build_ww(const Launch& L, const Cut& c) {
+    if (L.m.nwat == 0) return;
+    int half = (L.m.nwat + 1) / 2;
+    k_build_ww<<<grid_for((int64_t)half * 32, 256, 8, L.nwin), 256, 0, L.st>>>(L.m, L.ds, c.rcww2);
+}
+void launch_build_pw(const Launch& L, const Cut& c) {
+    if (L.m.nwat == 0 || L.m.ncgp_solute == 0) return;
+    k_build_pw<<<grid_for((int64_t)L.m.ncgp_solute * 32, 256, 8, L.nwin), 256, 0, L.st>>>(L.m, L.ds, c.rcpw2);
+}
+void launch_build_pp(const Launch& L, const Cut& c) {
+    if (L.m.ncgp_solute == 0) return;
+    int half = (L.m.ncgp_solute + 1) / 2;
+    k_build_pp_groups<<<grid_for((int64_t)half * 32, 256, 8, L.nwin), 256, 0, L.st>>>(L.m, L.ds, c.rcpp2);
+    k_expand_pp<<<grid_for(L.s0.cap_ppg, 128, 8, L.nwin), 128, 0, L.st>>>(L.m, L.ds);
+}
+void launch_build_qw(const Launch& L, const Cut& c) {
+    if (L.m.nwat == 0 || L.m.nqat == 0) return;
+    k_build_qw<<<dim3((L.m.nwat + 255) / 256, L.nwin), 256, 0, L.st>>>(L.m, L.ds, c.rcq2);
+}
+void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2) {
+    if (L.m.ncgp_solute == 0 || L.m.nqat == 0) return;
+    k_build_qp<<<dim3((L.m.ncgp_solute + 127) / 128, L.nwin), 128, 0, L.st>>>(L.m, L.ds, qnear, rcq2);
+}
+void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed) {
+    dim3 g = grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin);
+    if (mixed) k_lrf_accumulate<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+    else k_lrf_accumulate<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
 }
 
-void launch_lrf_taylor_impl(const DevModel& m, DevState& s, const int* iwhich, int mixed, cudaStream_t st) {
-    int b = blocks_for(m.natom, 256, 4);
-    if (mixed) k_lrf_taylor<true><<<b, 256, 0, st>>>(m, s, iwhich);
-    else k_lrf_taylor<false><<<b, 256, 0, st>>>(m, s, iwhich);
+void launch_ww(const Launch& L, int mixed) {
+    if (L.m.nwat == 0) return;
+    dim3 g = grid_for(L.s0.cap_ww, 256, 8, L.nwin);
+    bool spc = L.m.spc != 0;
+    if (mixed) { if (spc) k_ww<true, true><<<g, 256, 0, L.st>>>(L.m, L.ds); else k_ww<true, false><<<g, 256, 0, L.st>>>(L.m, L.ds); }
+    else { if (spc) k_ww<false, true><<<g, 256, 0, L.st>>>(L.m, L.ds); else k_ww<false, false><<<g, 256, 0, L.st>>>(L.m, L.ds); }
 }
-
-void launch_apply_fixed(const DevModel& m, DevState& s, cudaStream_t st) {
-    int n = 3 * m.natom;
-    k_apply_fixed<<<blocks_for(n, 256, 4), 256, 0, st>>>(n, s.fix, s.d);
+void launch_qw(const Launch& L, int mixed) {
+    if (L.m.nwat == 0 || L.m.nqat == 0) return;
+    dim3 g = grid_for(L.s0.cap_qw * 32, kQBlock, 8, L.nwin);
+    bool spc = L.m.spc != 0;
+    if (mixed) { if (spc) k_qw<true, true><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); else k_qw<true, false><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); }
+    else { if (spc) k_qw<false, true><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); else k_qw<false, false><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); }
 }
-
-void launch_restrain_solvent_impl(const DevModel& m, DevState& s, const SolventDev& p, double Tfree, int mixed,
-                                  const int* wsw, const uint8_t* heavy_solv, cudaStream_t st) {
-    if (m.nwat == 0) return;
+void launch_pw(const Launch& L, int mixed) {
+    if (L.m.nwat == 0 || L.m.ncgp_solute == 0) return;
+    dim3 g = grid_for(L.s0.cap_pw, 256, 8, L.nwin);
+    if (mixed) k_pw<true><<<g, 256, 0, L.st>>>(L.m, L.ds); else k_pw<false><<<g, 256, 0, L.st>>>(L.m, L.ds);
+}
+void launch_pp(const Launch& L, int mixed) {
+    if (L.m.ncgp_solute == 0) return;
+    dim3 g = grid_for(L.s0.cap_pp, 256, 8, L.nwin);
+    if (mixed) k_pp<true><<<g, 256, 0, L.st>>>(L.m, L.ds); else k_pp<false><<<g, 256, 0, L.st>>>(L.m, L.ds);
+}
+void launch_qp(const Launch& L, int mixed) {
+    if (L.m.nqat == 0 || L.m.nat_solute == 0) return;
+    dim3 g = grid_for(L.s0.cap_qp * 32, kQBlock, 8, L.nwin);
+    if (mixed) k_qp<true><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); else k_qp<false><<<g, kQBlock, 0, L.st>>>(L.m, L.ds);
+}
+void launch_nonbond_qq(const Launch& L, int mixed) {
+    if (L.s0.nqq == 0) return;
+    dim3 g((L.s0.nqq + 31) / 32, L.nwin);   // FP64 work: small blocks spread it over the SMs
+    if (mixed) k_qq<true><<<g, 32, 0, L.st>>>(L.m, L.ds); else k_qq<false><<<g, 32, 0, L.st>>>(L.m, L.ds);
+}
+void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed) {
+    dim3 g = grid_for(L.m.natom, 64, 16, L.nwin);
+    if (mixed) k_lrf_taylor<true><<<g, 64, 0, L.st>>>(L.m, L.ds, iwhich);
+    else k_lrf_taylor<false><<<g, 64, 0, L.st>>>(L.m, L.ds, iwhich);
+}
+void launch_apply_fixed(const Launch& L) {
+    int n = 3 * L.m.natom;
+    k_apply_fixed<<<grid_for(n, 256, 4, L.nwin), 256, 0, L.st>>>(n, L.ds);
+}
+void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
+                             const uint8_t* heavy_solv) {
+    if (L.m.nwat == 0) return;
     double shift = (p.fk_wsphere != 0.0) ? sqrt(p.boltz * Tfree / p.fk_wsphere) : 0.0;
-    int b = blocks_for(m.nwat, 256, 4);
-    if (mixed) k_restrain_solvent<true><<<b, 256, 0, st>>>(m, s, p, shift, wsw, heavy_solv);
-    else k_restrain_solvent<false><<<b, 256, 0, st>>>(m, s, p, shift, wsw, heavy_solv);
+    dim3 g = grid_for(L.m.nwat, 32, 16, L.nwin);
+    if (mixed) k_restrain_solvent<true><<<g, 32, 0, L.st>>>(L.m, L.ds, p, shift, wsw, heavy_solv);
+    else k_restrain_solvent<false><<<g, 32, 0, L.st>>>(L.m, L.ds, p, shift, wsw, heavy_solv);
 }
-
-void launch_watpol_impl(const DevModel& m, DevState& s, const SolventDev& p, int istep, int md, int mixed,
-                        double* shell_tsum, cudaStream_t st, int* nl) {
-    if (m.nwat == 0 || !p.wpol || p.nshell <= 0) return;
-    int bw = (m.nwat + 255) / 256;
+// returns the number of launches
+int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int mixed) {
+    if (L.m.nwat == 0 || !p.wpol || p.nshell <= 0) return 0;
+    int nl = 0;
+    dim3 gw((L.m.nwat + 31) / 32, L.nwin);   // FP64 math per water: 32-thread blocks
     if (md) {
-        cudaMemsetAsync(s.n_insh, 0, sizeof(int) * kMaxShell, st);
-        k_watpol_theta<<<bw, 256, 0, st>>>(m, s, p);
-        k_watpol_rank<<<bw, 256, 0, st>>>(m, s);
-        *nl += 2;
+        k_watpol_reset<<<L.nwin, kMaxShell, 0, L.st>>>(L.ds);
+        k_watpol_theta<<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+        k_watpol_rank<<<dim3(p.nshell, L.nwin), 256, 0, L.st>>>(L.m, L.ds);
+        nl += 3;
     }
     if (istep > 0 && md && (istep % (int)llround(p.itdis)) == 0) {
-        k_watpol_update<<<1, kMaxShell, 0, st>>>(p, s.wstate);
-        ++*nl;
+        k_watpol_update<<<dim3(1, L.nwin), kMaxShell, 0, L.st>>>(p, L.ds);
+        ++nl;
     }
-    cudaMemsetAsync(shell_tsum, 0, sizeof(double) * kMaxShell, st);
-    if (mixed) k_watpol_force<true><<<bw, 256, 0, st>>>(m, s, p, shell_tsum);
-    else k_watpol_force<false><<<bw, 256, 0, st>>>(m, s, p, shell_tsum);
-    ++*nl;
+    if (mixed) k_watpol_force<true><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+    else k_watpol_force<false><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+    ++nl;
     if (md) {
-        k_watpol_average<<<1, kMaxShell, 0, st>>>(p, s, shell_tsum);
-        ++*nl;
+        k_watpol_average<<<dim3(1, L.nwin), kMaxShell, 0, L.st>>>(p, L.ds);
+        ++nl;
     }
+    return nl;
 }
 
-void launch_export_pairs(const DevModel& m, const DevState& s, int kind, int32_t* di, int32_t* dj, int64_t cap,
-                         int* dcount, cudaStream_t st) {
-    k_export<<<blocks_for(1 << 20, 256, 8), 256, 0, st>>>(m, s, kind, di, dj, cap, dcount);
+void launch_export_pairs(const Launch& L, int win, int kind, int32_t* di, int32_t* dj, int64_t cap, int* dcount) {
+    k_export<<<blocks_for(1 << 20, 256, 8), 256, 0, L.st>>>(L.m, L.ds, win, kind, di, dj, cap, dcount);
 }
 
 }  // namespace qnb

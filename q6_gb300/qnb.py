@@ -34,7 +34,11 @@ EXPORTED = (
     "qnb_set_solvent_params", "qnb_restrain_solvent", "qnb_watpol", "qnb_get_watpol_state",
     "qnb_list_size", "qnb_export_pairs", "qnb_get_lrf", "qnb_device_buffers", "qnb_stream",
     "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_take_launch_count",
+    "qnb_profile", "qnb_kernel_times", "qnb_create_batch", "qnb_window_count",
+    "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
 )
+KERNEL_CLASSES = ("ww", "qw", "pw", "pp", "qp", "lrf_taylor", "qq", "restrain", "watpol", "pack",
+                  "apply", "build", "lrf_build")
 
 
 class QnbError(RuntimeError):
@@ -71,6 +75,10 @@ def load_library(path: str = LIB_PATH):
         "qnb_export_pairs": [P, I32, P, P, I64, P], "qnb_get_lrf": [P, P],
         "qnb_device_buffers": [P, P, P], "qnb_stream": [P, P],
         "qnb_compute_dev": [P, D, I32, I32, P, P, P], "qnb_take_launch_count": [P, P],
+        "qnb_profile": [P, I32], "qnb_kernel_times": [P, P, P, I32],
+        "qnb_create_batch": [P, P, I32, P], "qnb_window_count": [P, P],
+        "qnb_set_lambda_window": [P, I32, P], "qnb_upload_coordinates": [P, P],
+        "qnb_download_gradient": [P, P, I32],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -88,14 +96,15 @@ class NonbondedEngine:
     """One qdyn system on one GPU (one CUDA stream)."""
 
     def __init__(self, system: QSystem, precision: int = PREC_FP64, use_lrf: bool = True,
-                 device: int = 0):
+                 device: int = 0, windows: int = 1):
         self.lib = load_library()
         self.s = system
         self.S = system.nstates
+        self.nwin = int(windows)
         self.topo = TopologyHandle(system)
         opt = QnbOptions(precision, int(use_lrf), device, 0)
         h = ctypes.c_void_p()
-        self._check(self.lib.qnb_create(self.topo.ptr(), ctypes.byref(opt), ctypes.byref(h)))
+        self._check(self.lib.qnb_create_batch(self.topo.ptr(), ctypes.byref(opt), self.nwin, ctypes.byref(h)))
         self.h = h
         self.precision = precision
 
@@ -121,9 +130,12 @@ class NonbondedEngine:
         self.close()
 
     # ---- reference routines ---------------------------------------------
-    def set_lambda(self, lam):
+    def set_lambda(self, lam, window=None):
         lam = np.ascontiguousarray(lam, dtype=np.float64)
-        self._check(self.lib.qnb_set_lambda(self.h, _p(lam)))
+        if window is None:
+            self._check(self.lib.qnb_set_lambda(self.h, _p(lam)))
+        else:
+            self._check(self.lib.qnb_set_lambda_window(self.h, int(window), _p(lam)))
 
     def make_pair_lists(self, x, Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0):
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -189,6 +201,16 @@ class NonbondedEngine:
         self._check(self.lib.qnb_take_launch_count(self.h, ctypes.byref(n)))
         return int(n.value)
 
+    def profile(self, enable=True):
+        self._check(self.lib.qnb_profile(self.h, int(enable)))
+
+    def kernel_times(self):
+        n = len(KERNEL_CLASSES)
+        ms = np.zeros(n)
+        cnt = np.zeros(n, np.int64)
+        self._check(self.lib.qnb_kernel_times(self.h, _p(ms), _p(cnt), n))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(KERNEL_CLASSES)}
+
     # ---- device-resident interface ------------------------------------------
     def device_buffers(self):
         x = ctypes.c_void_p()
@@ -206,11 +228,25 @@ class NonbondedEngine:
                                                      Rcpw ** 2, Rcww ** 2))
 
     def compute_dev(self, Tfree=300.0, istep=0, sync=True):
-        E = np.zeros(7)
-        EQ = np.zeros((max(self.S, 1), 6))
-        R = np.zeros(2)
+        """All windows; returns per-window energies (lists) when sync."""
+        W = self.nwin
+        E = np.zeros((W, 7))
+        EQ = np.zeros((W, max(self.S, 1), 6))
+        R = np.zeros((W, 2))
         self._check(self.lib.qnb_compute_dev(self.h, Tfree, int(istep), int(sync), _p(E), _p(EQ), _p(R)))
-        return dict(zip(E_FIELDS, E)), EQ[: self.S], R
+        return [dict(zip(E_FIELDS, e)) for e in E], EQ[:, : self.S], R
+
+    def set_coordinates_dev(self, x_all):
+        """Copies coordinates of all windows (nwin x natom x 3) into HBM."""
+        xa = np.ascontiguousarray(x_all, dtype=np.float64)
+        assert xa.size == self.nwin * self.s.natom * 3
+        self._check(self.lib.qnb_upload_coordinates(self.h, _p(xa)))
+
+    def gradient_dev(self, clear=True):
+        """Gradient accumulators of all windows (nwin x natom x 3)."""
+        out = np.zeros((self.nwin, self.s.natom, 3))
+        self._check(self.lib.qnb_download_gradient(self.h, _p(out), int(clear)))
+        return out
 
     def evaluate(self, x, lam, cut=None, solvent=None, Tfree=300.0, istep=0, lists=True):
         """One full nonbonded evaluation in the reference's call order."""

