@@ -87,6 +87,10 @@ struct qnb_context {
     double* d_shell_tsum = nullptr;
     std::vector<void*> allocs;
     bool lists_built = false, qp_done = false, qw_done = false;
+    bool diag_valid = false;       // mixed form: half lists for inspection built from x_build
+    Cut last_cut{};
+    int maxg = 1;                  // largest solute charge group
+    DevState* d_diag = nullptr;    // scratch device state for inspection builds
     std::vector<int> counts;       // [nwin][C_NUM] after the last build
     SolventDev solv{};
     bool have_solv = false;
@@ -309,6 +313,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
             return fail(QNB_ERR_UNSUPPORTED, "solute charge group %d has %d atoms (max %d)", g,
                         gslot[g + 1] - gslot[g], kMaxGroup);
         for (int a = gslot[g]; a < gslot[g + 1]; ++a) slot_of[gatom[a]] = a - gslot[g];
+        c->maxg = std::max(c->maxg, gslot[g + 1] - gslot[g]);
     }
     struct SG {
         long long key;
@@ -360,6 +365,14 @@ int build_model(qnb_context* c, const qnb_topology* t) {
             }
     for (auto v : ljcod)
         if (v < 1 || v > 2) return fail(QNB_ERR_ARG, "ljcod entries must be 1 or 2");
+    std::vector<float4> ljpair((size_t)nt * nt);
+    for (int a = 0; a < nt; ++a)
+        for (int b = 0; b < nt; ++b) {
+            int code = t->ljcod[a * nt + b];
+            float2 p1 = ljf[((size_t)(code - 1) * nt + a) * nt + b], p3 = ljf[((size_t)2 * nt + a) * nt + b];
+            ljpair[(size_t)a * nt + b] = make_float4(p1.x, p1.y, p3.x, p3.y);
+        }
+    TRY(c->upload((float4**)&m.ljpair, ljpair));
     TRY(c->upload((double2**)&m.lj, lj));
     TRY(c->upload((float2**)&m.ljf, ljf));
     TRY(c->upload((uint8_t**)&m.ljset, ljset));
@@ -617,11 +630,27 @@ int alloc_state(qnb_context* c) {
         TRY(ensure_cap(c, &s.ppg, &s.cap_ppg, std::max<int64_t>(1024, (int64_t)m.ncgp_solute * 96)));
         TRY(ensure_cap(c, &s.qp, &s.cap_qp, std::max<int64_t>(1024, (int64_t)m.nat_solute)));
         TRY(ensure_cap(c, &s.qw, &s.cap_qw, std::max<int64_t>(1024, (int64_t)m.nwat)));
+        if (c->mixed) {
+            s.cap_gp = 1024;
+            s.cap_gw = 256;
+            s.cap_rww = 256;
+            s.cap_wg = 192;
+            TRY(c->alloc(&s.row_gp, (size_t)std::max(1, m.ncgp_solute) * s.cap_gp));
+            TRY(c->alloc(&s.row_gw, (size_t)std::max(1, m.ncgp_solute) * s.cap_gw));
+            TRY(c->alloc(&s.row_ww, (size_t)std::max(1, m.nwat) * s.cap_rww));
+            TRY(c->alloc(&s.row_wg, (size_t)std::max(1, m.nwat) * s.cap_wg));
+            TRY(c->alloc(&s.cnt_gp, (size_t)std::max(1, m.ncgp_solute)));
+            TRY(c->alloc(&s.cnt_gw, (size_t)std::max(1, m.ncgp_solute)));
+            TRY(c->alloc(&s.cnt_ww, (size_t)std::max(1, m.nwat)));
+            TRY(c->alloc(&s.cnt_wg, (size_t)std::max(1, m.nwat)));
+            TRY(c->alloc(&s.x_build, n3));
+        }
         s.qq = c->st_qq;
         s.nqq = c->nqq;
         s.nqq_qq = c->nqq_qq;
     }
     TRY(c->alloc(&c->d_states, (size_t)W));
+    TRY(c->alloc(&c->d_diag, (size_t)1));
     c->counts.assign((size_t)W * C_NUM, 0);
     CU(cudaMallocHost((void**)&c->h_stage, sizeof(double) * std::max(3 * m.natom, 64)));
     CU(cudaMallocHost((void**)&c->h_e, sizeof(double) * 2 * kNumE * W));
@@ -695,6 +724,36 @@ int grow_lists(qnb_context* c, bool* grew, bool* do_qp, bool* do_qw) {
         }
         *grew = true;
     }
+    if (c->mixed) {
+        struct R {
+            int k;
+            int* cap;
+            int** row;
+            int nrows;
+        };
+        for (int w = 0; w < c->nwin; ++w) {
+            DevState& s = c->st[w];
+            if (need[C_RGP] > s.cap_gp) {
+                int cap = (int)(need[C_RGP] + need[C_RGP] / 4 + 32);
+                c->release(s.row_gp);
+                s.row_gp = nullptr;
+                TRY(c->alloc(&s.row_gp, (size_t)std::max(1, c->ncgp_solute) * cap));
+                s.cap_gp = cap;
+                *grew = true;
+            }
+            R rs[] = {{C_RGW, &s.cap_gw, &s.row_gw, c->ncgp_solute},
+                      {C_RWW, &s.cap_rww, &s.row_ww, c->nwat}, {C_RWG, &s.cap_wg, &s.row_wg, c->nwat}};
+            for (auto& r : rs) {
+                if (need[r.k] <= *r.cap) continue;
+                int cap = (int)(need[r.k] + need[r.k] / 4 + 32);
+                c->release(*r.row);
+                *r.row = nullptr;
+                TRY(c->alloc(r.row, (size_t)std::max(1, r.nrows) * cap));
+                *r.cap = cap;
+                *grew = true;
+            }
+        }
+    }
     if (*grew) TRY(upload_states(c));
     return QNB_OK;
 }
@@ -704,15 +763,19 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
     bool do_qp = !(c->qp_done && cut.rcq2 > c->rexcl_o2);   // src/nonbondene.f90:3678
     bool do_qw = !(c->qw_done && cut.rcq2 > c->rexcl_o2);   // src/nonbondene.f90:3889
     for (int attempt = 0; attempt < 4; ++attempt) {
-        unsigned keep = (do_qp ? 0u : 1u << C_QP) | (do_qw ? 0u : 1u << C_QW);
+        unsigned keep = (do_qp ? 0u : 1u << C_QP) | (do_qw ? 0u : 1u << C_QW);   // everything else restarts
         launch_reset_counts(L, keep);
         timed(c, K_BUILD, [&] {
             launch_pack(L);
             if (c->use_lrf) launch_group_centres(L);
-            launch_build_pp(L, cut);
-            launch_build_pw(L, cut);
+            if (c->mixed) {
+                launch_build_rows(L, cut);
+            } else {
+                launch_build_pp(L, cut);
+                launch_build_pw(L, cut);
+                launch_build_ww(L, cut);
+            }
             if (do_qp) launch_build_qp(L, c->d_qnear, cut.rcq2);
-            launch_build_ww(L, cut);
             if (do_qw) launch_build_qw(L, cut);
         });
         c->launches += 7 + (c->use_lrf ? 1 : 0);
@@ -730,6 +793,12 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
             if (do_qp) c->qp_done = true;
             if (do_qw) c->qw_done = true;
             c->lists_built = true;
+            if (c->mixed) {   // keep window 0's build coordinates for list inspection
+                CU(cudaMemcpyAsync(c->st[0].x_build, c->st[0].x, sizeof(double) * 3 * c->natom,
+                                   cudaMemcpyDeviceToDevice, c->stream));
+                c->diag_valid = false;
+                c->last_cut = cut;
+            }
             return QNB_OK;
         }
     }
@@ -745,12 +814,22 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
         ++nl;
     }
     // call order of pot_energy_nonbonds, src/potene.f90:340-379
-    if (c->m.natom > c->m.nat_solute) {
-        if (md) timed(c, K_WW, [&] { launch_ww(L, mx); }), ++nl;
-        timed(c, K_QW, [&] { launch_qw(L, mx); }), ++nl;
-        if (md) timed(c, K_PW, [&] { launch_pw(L, mx); }), ++nl;
+    if (mx) {
+        // gather rows: water rows carry ww + the water side of pw, solute
+        // group rows pp + the solute side of pw
+        if (c->m.natom > c->m.nat_solute) {
+            if (md) timed(c, K_WW, [&] { launch_rows_water(L); }), ++nl;
+            timed(c, K_QW, [&] { launch_qw(L, mx); }), ++nl;
+        }
+        if (md) timed(c, K_PP, [&] { launch_rows_solute(L, c->maxg); }), ++nl;
+    } else {
+        if (c->m.natom > c->m.nat_solute) {
+            if (md) timed(c, K_WW, [&] { launch_ww(L, mx); }), ++nl;
+            timed(c, K_QW, [&] { launch_qw(L, mx); }), ++nl;
+            if (md) timed(c, K_PW, [&] { launch_pw(L, mx); }), ++nl;
+        }
+        if (md) timed(c, K_PP, [&] { launch_pp(L, mx); }), ++nl;
     }
-    if (md) timed(c, K_PP, [&] { launch_pp(L, mx); }), ++nl;
     timed(c, K_QP, [&] { launch_qp(L, mx); }), ++nl;
     if (c->use_lrf && md) {
         timed(c, K_LRF_TAYLOR, [&] { launch_lrf_taylor(L, c->d_iwhich, mx); });
@@ -779,6 +858,35 @@ void add_energies(const double* e, qnb_energies* E, qnb_qenergies* EQ, int S) {
             EQ[s].qw_el += e[eq_slot(s, 4)];
             EQ[s].qw_vdw += e[eq_slot(s, 5)];
         }
+}
+
+// mixed form: the inspection entry points report the reference's atom-pair
+// lists; they are built on demand from window 0's build coordinates with the
+// same exact selection as the rows
+int ensure_half_lists(qnb_context* c) {
+    if (!c->mixed || c->diag_valid || !c->lists_built) return QNB_OK;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        DevState tmp = c->st[0];
+        tmp.x = c->st[0].x_build;
+        CU(cudaMemcpyAsync(c->d_diag, &tmp, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
+        Launch L{c->m, tmp, c->d_diag, 1, c->stream};
+        unsigned keep = ~((1u << C_WW) | (1u << C_PW) | (1u << C_PP) | (1u << C_PP14) | (1u << C_PPG));
+        launch_reset_counts(L, keep);
+        launch_pack(L);
+        launch_build_pp(L, c->last_cut);
+        launch_build_pw(L, c->last_cut);
+        launch_build_ww(L, c->last_cut);
+        TRY(check_launch());
+        CU(cudaMemcpyAsync(c->counts.data(), c->cnt_all, sizeof(int) * C_NUM, cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaStreamSynchronize(c->stream));
+        bool grew = false, dq = false, dw = false;
+        TRY(grow_lists(c, &grew, &dq, &dw));
+        if (!grew) {
+            c->diag_valid = true;
+            return QNB_OK;
+        }
+    }
+    return fail(QNB_ERR_CAPACITY, "inspection lists kept overflowing");
 }
 
 int64_t list_pairs(const qnb_context* c, int kind) {
@@ -1019,6 +1127,8 @@ int qnb_get_watpol_state(qnb_context* c, double* theta_corr, double* avtheta, do
 
 int qnb_list_size(qnb_context* c, int32_t kind, int64_t* n) {
     if (!c || !n) return fail(QNB_ERR_ARG, "null argument");
+    CU(cudaSetDevice(c->device));
+    TRY(ensure_half_lists(c));
     int64_t v = list_pairs(c, kind);
     if (v < 0) return fail(QNB_ERR_ARG, "list kind %d", kind);
     *n = v;
@@ -1027,6 +1137,8 @@ int qnb_list_size(qnb_context* c, int32_t kind, int64_t* n) {
 
 int qnb_export_pairs(qnb_context* c, int32_t kind, int32_t* i, int32_t* j, int64_t cap, int64_t* n) {
     if (!c || !n) return fail(QNB_ERR_ARG, "null argument");
+    CU(cudaSetDevice(c->device));
+    TRY(ensure_half_lists(c));
     int64_t cnt = list_pairs(c, kind);
     if (cnt < 0) return fail(QNB_ERR_ARG, "list kind %d", kind);
     *n = cnt;

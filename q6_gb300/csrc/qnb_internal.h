@@ -25,9 +25,12 @@ __host__ __device__ constexpr int eq_slot(int s, int k) { return E_Q0 + 6 * s + 
 constexpr int kNumE = E_Q0 + 6 * kMaxStates;
 
 // list counters (entries at list granularity, plus reference atom-pair counts)
-enum { C_WW = 0, C_PW, C_PP, C_QP, C_QW, C_PP14, C_PPG, C_NUM };
+enum { C_WW = 0, C_PW, C_PP, C_QP, C_QW, C_PP14, C_PPG,
+       C_RGP, C_RGW, C_RWW, C_RWG,   // longest row seen (mixed-form row lists)
+       C_NUM };
 
-constexpr int kMaxGroup = 16;   // atoms per solute charge group handled on device
+constexpr int kMaxGroup = 15;   // atoms per solute charge group handled on device
+constexpr int kMaxTypesShared = 32;   // type-pair table staged in shared memory up to this many types
 
 struct alignas(32) QPar {   // one (pair type, state) parameter set: A, B, elec, soft-core alpha
     double A, B, el, sc;
@@ -59,6 +62,7 @@ struct DevModel {
     const int* sg_ent;
     const double2* lj;          // [3][natyps][natyps] (A,B) per LJ code 1..3
     const float2* ljf;
+    const float4* ljpair;       // [natyps][natyps]: (A,B) of ljcod code, (A,B) of code 3
     const uint8_t* ljcod;       // [natyps][natyps]
     const uint8_t* ljset;       // [3][natyps][natyps]: |A| or |B| > QREAL_EPS
     int wtype[kMaxSolv];        // solvent template (first molecule) atom types
@@ -99,6 +103,13 @@ struct DevState {
     int2* ppg; int64_t cap_ppg;    // listed solute group pairs (g1 <= g2)
     int* qp;  int64_t cap_qp;      // solute atoms interacting with all Q atoms
     int* qw;  int64_t cap_qw;      // waters interacting with all Q atoms
+    // mixed form: gather rows (ELL, fixed capacity per row); row r of list X
+    // holds partners at X[r*cap_X .. r*cap_X + cnt_X[r])
+    uint2* row_gp; int* cnt_gp; int cap_gp; // solute group -> solute atoms: {j | flags, 2-bit kind per row atom}
+    int* row_gw; int* cnt_gw; int cap_gw;   // solute group -> waters
+    int* row_ww; int* cnt_ww; int cap_rww;  // water -> waters
+    int* row_wg; int* cnt_wg; int cap_wg;   // water -> solute groups
+    double* x_build;                        // coordinates of the last list build
     QQEntry* qq; int nqq;          // static qq + qqp entries (all states)
     int nqq_qq;                    // first nqq_qq entries are Q-Q (EQ%qq), rest Q-P (EQ%qp)
     // water polarisation
@@ -137,6 +148,9 @@ void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2);
 void launch_build_qw(const Launch& L, const Cut& c);
 void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed);
 
+void launch_build_rows(const Launch& L, const Cut& c);
+void launch_rows_solute(const Launch& L, int maxg);
+void launch_rows_water(const Launch& L);
 void launch_ww(const Launch& L, int mixed);
 void launch_qw(const Launch& L, int mixed);
 void launch_pw(const Launch& L, int mixed);

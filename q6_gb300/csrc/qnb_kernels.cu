@@ -1318,6 +1318,345 @@ __global__ void k_export(DevModel m, const DevState* __restrict__ states, int wi
 }
 
 // =============================================================================
+// Mixed form: gather rows.  Every solute charge group and every water owns a
+// row of partners; a warp walks one row and accumulates the gradient of the
+// row's own atoms only, so each pair is evaluated once from each side (twice
+// in FP32) and no per-pair atomics are needed.  Energies are counted once.
+// =============================================================================
+
+// appends this lane's candidate to row `row` (one warp owns the row)
+__device__ __forceinline__ int row_append(int* __restrict__ row, int cap, int count, bool ok, int value) {
+    unsigned b = __ballot_sync(kFull, ok);
+    int lane = threadIdx.x & 31;
+    if (ok) {
+        int pos = count + __popc(b & ((1u << lane) - 1u));
+        if (pos < cap) row[pos] = value;
+    }
+    return count + __popc(b);
+}
+
+// nbpplist/nbpwlist/nbwwlist selections (src/nonbondene.f90:1777-1908,
+// 2842-2955, 4274-4395) stored from both sides.  Rows 0..ncgp_solute-1 are
+// solute groups, the next nwat rows waters; one warp per row.
+__global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cut c) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const float4* __restrict__ xq = s.xq;
+    int nrows = m.ncgp_solute + m.nwat;
+    int lane = threadIdx.x & 31;
+    for (int r = warp_id_global(); r < nrows; r += warps_total()) {
+        if (r < m.ncgp_solute) {
+            int g = r, is = m.gsw[g];
+            int npp = 0, npw = 0;
+            if (!m.excl[is]) {
+                float4 xi = xq[is];
+                int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
+                uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
+                for (int j0 = 0; j0 < m.ncgp_solute; j0 += kWarp) {
+                    int g2 = j0 + lane;
+                    bool ok = false;
+                    int b0 = 0, n2 = 0, nq = 0;
+                    if (g2 < m.ncgp_solute) {
+                        int s2 = m.gsw[g2];
+                        if (!m.excl[s2]) ok = (g2 == g) || within(r2_f(xi, xq[s2]), c.rcpp2, x, is, s2);
+                        if (ok) {
+                            b0 = m.gslot[g2];
+                            n2 = m.gslot[g2 + 1] - b0;
+                            for (int b = 0; b < n2; ++b) nq += (m.iqatom[m.gatom[b0 + b]] < 0);
+                        }
+                    }
+                    // row-local offsets: inclusive warp scan of the emitted counts
+                    int incl = nq;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        int v = __shfl_up_sync(kFull, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    int total = __shfl_sync(kFull, incl, 31);
+                    if (nq > 0) {
+                        int pos = npp + incl - nq;
+                        bool lower = g <= g2;
+                        int sgi = m.nsg ? sg_find(m, lower ? (long long)g * m.ncgp_solute + g2
+                                                           : (long long)g2 * m.ncgp_solute + g) : -1;
+                        unsigned flags = (g < g2 ? 1u : 0u) | (g == g2 ? 2u : 0u);
+                        for (int b = 0; b < n2; ++b) {
+                            int j = m.gatom[b0 + b];
+                            if (m.iqatom[j] >= 0) continue;
+                            unsigned mask = 0;
+                            for (int a = 0; a < n1; ++a) {
+                                int i = m.gatom[a0 + a];
+                                int kind = 0;
+                                if (i == j) kind = 1;
+                                else if (sgi >= 0) {
+                                    if (g == g2) kind = i < j ? sg_kind(m, sgi, a, b) : sg_kind(m, sgi, b, a);
+                                    else kind = lower ? sg_kind(m, sgi, a, b) : sg_kind(m, sgi, b, a);
+                                }
+                                mask |= (unsigned)kind << (2 * a);
+                            }
+                            if (pos < s.cap_gp) rp[pos] = make_uint2((unsigned)j | (flags << 28), mask);
+                            ++pos;
+                        }
+                    }
+                    npp += total;
+                }
+                int* rw = s.row_gw + (size_t)g * s.cap_gw;
+                for (int j0 = 0; j0 < m.nwat; j0 += kWarp) {
+                    int jw = j0 + lane;
+                    bool ok = false;
+                    if (jw < m.nwat) {
+                        int jo = m.nat_solute + m.sa * jw;
+                        if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), c.rcpw2, x, is, jo);
+                    }
+                    npw = row_append(rw, s.cap_gw, npw, ok, jw);
+                }
+            }
+            if (lane == 0) {
+                s.cnt_gp[g] = min(npp, s.cap_gp);
+                s.cnt_gw[g] = min(npw, s.cap_gw);
+                atomicMax(s.cnt + C_RGP, npp);
+                atomicMax(s.cnt + C_RGW, npw);
+            }
+        } else {
+            int w = r - m.ncgp_solute, io = m.nat_solute + m.sa * w;
+            int nww = 0, nwg = 0;
+            if (!m.excl[io]) {
+                float4 xi = xq[io];
+                int* rw = s.row_ww + (size_t)w * s.cap_rww;
+                for (int j0 = 0; j0 < m.nwat; j0 += kWarp) {
+                    int jw = j0 + lane;
+                    bool ok = false;
+                    if (jw < m.nwat && jw != w) {
+                        int jo = m.nat_solute + m.sa * jw;
+                        if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), c.rcww2, x, io, jo);
+                    }
+                    nww = row_append(rw, s.cap_rww, nww, ok, jw);
+                }
+                int* rg = s.row_wg + (size_t)w * s.cap_wg;
+                for (int j0 = 0; j0 < m.ncgp_solute; j0 += kWarp) {
+                    int g = j0 + lane;
+                    bool ok = false;
+                    if (g < m.ncgp_solute) {
+                        int s2 = m.gsw[g];
+                        // the same test as from the group side: r2(switch atom, O)
+                        if (!m.excl[s2]) ok = within(r2_f(xq[s2], xi), c.rcpw2, x, s2, io);
+                    }
+                    nwg = row_append(rg, s.cap_wg, nwg, ok, g);
+                }
+            }
+            if (lane == 0) {
+                s.cnt_ww[w] = min(nww, s.cap_rww);
+                s.cnt_wg[w] = min(nwg, s.cap_wg);
+                atomicMax(s.cnt + C_RWW, nww);
+                atomicMax(s.cnt + C_RWG, nwg);
+            }
+        }
+    }
+}
+
+// FP32 pair (nbe / nbe_spc): adds the gradient on atom i to g, returns energies
+__device__ __forceinline__ void pair_f(float4 a, float4 b, float A, float B, float el, bool lj, float& gx,
+                                      float& gy, float& gz, float& vel, float& vdw) {
+    PairF q = nbe_f(a, b, A, B, el, lj);
+    gx -= q.tx * q.dv;
+    gy -= q.ty * q.dv;
+    gz -= q.tz * q.dv;
+    vel = q.vel;
+    vdw = q.vdw;
+}
+
+// type-pair LJ parameters (code ljcod: A,B; code 3: A,B) staged in shared
+// memory when the type table is small
+struct TypeTab {
+    const float4* t;
+    int nt;
+    __device__ __forceinline__ float4 operator()(int a, int b) const { return t[a * nt + b]; }
+};
+__device__ __forceinline__ TypeTab stage_types(const DevModel& m, float4* sh) {
+    if (m.natyps <= kMaxTypesShared) {
+        for (int k = threadIdx.x; k < m.natyps * m.natyps; k += blockDim.x) sh[k] = m.ljpair[k];
+        __syncthreads();
+        return TypeTab{sh, m.natyps};
+    }
+    return TypeTab{m.ljpair, m.natyps};
+}
+
+// solute group rows: pp (partner atoms with exclusion / 1-4 kinds) and pw
+// (partner waters): gradient of the group's own atoms
+template <int MAXG>
+__global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState* __restrict__ states) {
+    __shared__ float4 sh_lj[kMaxTypesShared * kMaxTypesShared];
+    const DevState& s = states[blockIdx.y];
+    TypeTab lj = stage_types(m, sh_lj);
+    Acc<true> acc = make_acc<true>(s);
+    ESum<true> epel, epvdw, ewel, ewvdw;
+    const float4* __restrict__ xq = s.xq;
+    const float el14 = (float)m.el14;
+    int lane = threadIdx.x & 31;
+    for (int g = warp_id_global(); g < m.ncgp_solute; g += warps_total()) {
+        int npp = s.cnt_gp[g], npw = s.cnt_gw[g];
+        if (npp == 0 && npw == 0) continue;
+        int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
+        int ia[MAXG], ta[MAXG];
+        float4 xa[MAXG];
+        bool qa[MAXG];
+        float f[MAXG][3];
+#pragma unroll
+        for (int a = 0; a < MAXG; ++a) {
+            f[a][0] = f[a][1] = f[a][2] = 0.f;
+            if (a < n1) {
+                ia[a] = m.gatom[a0 + a];
+                ta[a] = m.iac[ia[a]];
+                xa[a] = xq[ia[a]];
+                qa[a] = m.iqatom[ia[a]] >= 0;
+            } else {
+                ia[a] = 0x7fffffff;
+                ta[a] = 0;
+                xa[a] = make_float4(0, 0, 0, 0);
+                qa[a] = true;
+            }
+        }
+        // ---- solute partner atoms (nonbond_pp, src/nonbondene.f90:4694-4760)
+        const uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
+        for (int k = lane; k < npp; k += kWarp) {
+            uint2 e = rp[k];
+            int j = (int)(e.x & 0x0fffffffu);
+            bool lowerg = (e.x >> 28) & 1u, sameg = (e.x >> 29) & 1u;
+            float4 xb = xq[j];
+            int tj = m.iac[j];
+#pragma unroll
+            for (int a = 0; a < MAXG; ++a) {
+                if (qa[a]) continue;
+                unsigned kind = (e.y >> (2 * a)) & 3u;
+                if (kind == 1u) continue;
+                float4 p = lj(ta[a], tj);
+                bool is14 = kind == 3u;
+                float A = is14 ? p.z : p.x, B = is14 ? p.w : p.y;
+                float el = xa[a].w * xb.w;
+                if (is14) el *= el14;
+                float vel, vdw;
+                pair_f(xa[a], xb, A, B, el, true, f[a][0], f[a][1], f[a][2], vel, vdw);
+                if (lowerg || (sameg && ia[a] < j)) {   // each pair's energy once
+                    epel.add(vel);
+                    epvdw.add(vdw);
+                }
+            }
+        }
+        // ---- water partners (nonbond_pw, src/nonbondene.f90:4856-4916); energy counted here
+        const int* rw = s.row_gw + (size_t)g * s.cap_gw;
+        for (int k = lane; k < npw; k += kWarp) {
+            int j0 = m.nat_solute + m.sa * rw[k];
+            for (int b = 0; b < m.sa; ++b) {
+                float4 xb = xq[j0 + b];
+                int tw = m.wtype[b];
+#pragma unroll
+                for (int a = 0; a < MAXG; ++a) {
+                    if (qa[a]) continue;
+                    float4 p = lj(ta[a], tw);
+                    float vel, vdw;
+                    pair_f(xa[a], xb, p.x, p.y, xa[a].w * m.wcrgf[b], true, f[a][0], f[a][1], f[a][2], vel, vdw);
+                    ewel.add(vel);
+                    ewvdw.add(vdw);
+                }
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < MAXG; ++a) {
+            if (a >= n1) break;   // warp-uniform
+            unsigned long long v0 = warp_sum(to_fix(f[a][0])), v1 = warp_sum(to_fix(f[a][1])),
+                               v2 = warp_sum(to_fix(f[a][2]));
+            if (lane == 0 && !qa[a]) {
+                atomicAdd(s.fix + 3 * ia[a], v0);
+                atomicAdd(s.fix + 3 * ia[a] + 1, v1);
+                atomicAdd(s.fix + 3 * ia[a] + 2, v2);
+            }
+        }
+    }
+    epel.flush(acc, E_PP_EL);
+    epvdw.flush(acc, E_PP_VDW);
+    ewel.flush(acc, E_PW_EL);
+    ewvdw.flush(acc, E_PW_VDW);
+}
+
+// water rows: ww (waters, SPC fast path as nonbond_ww_spc) and wp (solute
+// groups) gradient of the water's atoms
+template <bool SPC>
+__global__ void __launch_bounds__(128) k_rows_water(DevModel m, const DevState* __restrict__ states) {
+    __shared__ float4 sh_lj[kMaxTypesShared * kMaxTypesShared];
+    const DevState& s = states[blockIdx.y];
+    TypeTab lj = stage_types(m, sh_lj);
+    Acc<true> acc = make_acc<true>(s);
+    ESum<true> eel, evdw;
+    const float4* __restrict__ xq = s.xq;
+    int lane = threadIdx.x & 31;
+    const int sa = m.sa;
+    for (int w = warp_id_global(); w < m.nwat; w += warps_total()) {
+        int nww = s.cnt_ww[w], nwg = s.cnt_wg[w];
+        if (nww == 0 && nwg == 0) continue;
+        int i0 = m.nat_solute + sa * w;
+        float4 xa[kMaxSolv];
+        float f[kMaxSolv][3];
+#pragma unroll
+        for (int a = 0; a < kMaxSolv; ++a) {
+            f[a][0] = f[a][1] = f[a][2] = 0.f;
+            xa[a] = a < sa ? xq[i0 + a] : make_float4(0, 0, 0, 0);
+        }
+        const int* rw = s.row_ww + (size_t)w * s.cap_rww;
+        for (int k = lane; k < nww; k += kWarp) {
+            int w2 = rw[k];
+            int j0 = m.nat_solute + sa * w2;
+            bool count = w < w2;
+#pragma unroll
+            for (int b = 0; b < kMaxSolv; ++b) {
+                if (b >= sa) break;
+                float4 xb = xq[j0 + b];
+#pragma unroll
+                for (int a = 0; a < kMaxSolv; ++a) {
+                    if (a >= sa) break;
+                    int kk = a * kMaxSolv + b;
+                    bool lj = !SPC || (a == 0 && b == 0);
+                    float vel, vdw;
+                    pair_f(xa[a], xb, m.wwAf[kk], m.wwBf[kk], m.wwEf[kk], lj, f[a][0], f[a][1], f[a][2], vel, vdw);
+                    if (count) {
+                        eel.add(vel);
+                        if (lj) evdw.add(vdw);
+                    }
+                }
+            }
+        }
+        const int* rg = s.row_wg + (size_t)w * s.cap_wg;
+        for (int k = lane; k < nwg; k += kWarp) {
+            int g = rg[k];
+            for (int bb = m.gslot[g]; bb < m.gslot[g + 1]; ++bb) {
+                int j = m.gatom[bb];
+                if (m.iqatom[j] >= 0) continue;
+                float4 xb = xq[j];
+                int tj = m.iac[j];
+#pragma unroll
+                for (int a = 0; a < kMaxSolv; ++a) {
+                    if (a >= sa) break;
+                    float4 p = lj(tj, m.wtype[a]);
+                    float vel, vdw;
+                    pair_f(xa[a], xb, p.x, p.y, xb.w * m.wcrgf[a], true, f[a][0], f[a][1], f[a][2], vel, vdw);
+                }
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < kMaxSolv; ++a) {
+            if (a >= sa) break;
+            unsigned long long v0 = warp_sum(to_fix(f[a][0])), v1 = warp_sum(to_fix(f[a][1])),
+                               v2 = warp_sum(to_fix(f[a][2]));
+            if (lane == 0) {
+                atomicAdd(s.fix + 3 * (i0 + a), v0);
+                atomicAdd(s.fix + 3 * (i0 + a) + 1, v1);
+                atomicAdd(s.fix + 3 * (i0 + a) + 2, v2);
+            }
+        }
+    }
+    eel.flush(acc, E_WW_EL);
+    evdw.flush(acc, E_WW_VDW);
+}
+
+// =============================================================================
 // launch wrappers
 // =============================================================================
 namespace {
@@ -1394,6 +1733,24 @@ void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed) {
     else k_lrf_accumulate<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
 }
 
+void launch_build_rows(const Launch& L, const Cut& c) {
+    int nrows = L.m.ncgp_solute + L.m.nwat;
+    if (nrows == 0) return;
+    k_build_rows<<<grid_for((int64_t)nrows * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c);
+}
+void launch_rows_solute(const Launch& L, int maxg) {
+    if (L.m.ncgp_solute == 0) return;
+    dim3 g = grid_for((int64_t)L.m.ncgp_solute * 32, 128, 16, L.nwin);
+    if (maxg <= 4) k_rows_solute<4><<<g, 128, 0, L.st>>>(L.m, L.ds);
+    else if (maxg <= 8) k_rows_solute<8><<<g, 128, 0, L.st>>>(L.m, L.ds);
+    else k_rows_solute<16><<<g, 128, 0, L.st>>>(L.m, L.ds);
+}
+void launch_rows_water(const Launch& L) {
+    if (L.m.nwat == 0) return;
+    dim3 g = grid_for((int64_t)L.m.nwat * 32, 128, 16, L.nwin);
+    if (L.m.spc) k_rows_water<true><<<g, 128, 0, L.st>>>(L.m, L.ds);
+    else k_rows_water<false><<<g, 128, 0, L.st>>>(L.m, L.ds);
+}
 void launch_ww(const Launch& L, int mixed) {
     if (L.m.nwat == 0) return;
     dim3 g = grid_for(L.s0.cap_ww, 256, 8, L.nwin);
