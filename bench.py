@@ -185,7 +185,7 @@ def run_ours(args, rank, world, local):
     pair_interactions = counts["pp"] + counts["pw"] + counts["ww"] + (counts["qp"] + counts["qw"]) * s.nstates
     eng.close()
 
-    e2e = run_e2e(args, s, sp, lams, prec, local)
+    e2e = run_e2e(args, s, sp, lams, prec, local) if args.e2e else None
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
@@ -210,7 +210,8 @@ def run_ours(args, rank, world, local):
         "gpu_launches": launches,
     }
     if rank == 0:
-        out["cpu_baseline"] = cpu_baseline(s, sp, args)
+        if args.cpu:
+            out["cpu_baseline"] = cpu_baseline(s, sp, args)
         if args.fp64_compare:
             out["fp64_value"] = fp64_compare(args, s, sp, lams, local)
             out["mixed_over_fp64"] = round(out["value"] / out["fp64_value"], 3) if out["fp64_value"] else None
@@ -389,6 +390,10 @@ def main():
     ap.add_argument("--windows", type=int, default=51)
     ap.add_argument("--prec", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-fp64-compare", dest="fp64_compare", action="store_false")
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false",
+                    help="skip the host-buffer arm (profiling runs)")
+    ap.add_argument("--no-cpu-baseline", dest="cpu", action="store_false",
+                    help="skip the CPU oracle sample (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

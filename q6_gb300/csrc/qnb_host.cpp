@@ -81,6 +81,7 @@ struct qnb_context {
     int* cnt_all = nullptr;        // [nwin][C_NUM] list counters
     double* d_all = nullptr;       // [nwin][natom][3]
     int* d_iwhich = nullptr;
+    int* d_lrf_src = nullptr;      // per atom: LRF source distance atom | solute flag << 30, or -1
     uint8_t* d_qnear = nullptr;
     int* d_wsw = nullptr;
     uint8_t* d_heavy_solv = nullptr;
@@ -287,6 +288,17 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     TRY(c->upload((int**)&m.gatom, gatom));
     TRY(c->upload((int**)&m.gsw, gsw));
     TRY(c->upload(&c->d_iwhich, iwhich));
+    // lrf_update sources: non-Q atoms of groups whose distance atom is not
+    // excluded (src/nonbondene.f90:658-660 and the list builders' excl skips)
+    std::vector<int> lrf_src(natom, -1);
+    for (int i = 0; i < natom; ++i) {
+        if (iqatom[i] >= 0) continue;
+        int g = iwhich[i];
+        int d = g < t->ncgp_solute ? t->cgp_iswitch[g] : ns + sa * (g - t->ncgp_solute);
+        if (t->excl[d]) continue;
+        lrf_src[i] = d | ((g < t->ncgp_solute ? 1 : 0) << 30);
+    }
+    TRY(c->upload(&c->d_lrf_src, lrf_src));
     TRY(c->upload(&c->d_wsw, wsw));
 
     // special solute pairs: excluded (listex + listexlong) and 1-4 (list14 +
@@ -780,7 +792,7 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
         });
         c->launches += 7 + (c->use_lrf ? 1 : 0);
         if (c->use_lrf) {
-            timed(c, K_LRF_BUILD, [&] { launch_lrf_accumulate(L, cut, c->mixed); });
+            timed(c, K_LRF_BUILD, [&] { launch_lrf_accumulate(L, cut, c->mixed, c->d_lrf_src); });
             c->launches++;
         }
         TRY(check_launch());

@@ -146,7 +146,7 @@ void launch_build_pw(const Launch& L, const Cut& c);
 void launch_build_pp(const Launch& L, const Cut& c);
 void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2);
 void launch_build_qw(const Launch& L, const Cut& c);
-void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed);
+void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src);
 
 void launch_build_rows(const Launch& L, const Cut& c);
 void launch_rows_solute(const Launch& L, int maxg);

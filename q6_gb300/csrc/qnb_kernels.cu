@@ -440,56 +440,94 @@ __device__ __forceinline__ int group_dist_atom(const DevModel& m, int g) {
     return g < m.ncgp_solute ? m.gsw[g] : m.nat_solute + m.sa * (g - m.ncgp_solute);
 }
 
+// lrf_update's sums (src/nonbondene.f90:628-725) regrouped by symmetry: per
+// source atom (dr from the target centre, charge q)
+//   m[0]      phi0 += f0 r2
+//   m[1..3]   phi1 -= dr f0
+//   m[4..9]   S2(ab)  += f1 dr_a dr_b        (a <= b; phi2(a)_b = S2(ab) - [a==b] F0)
+//   m[10]     F0      += f0
+//   m[11..20] S3(abc) += 5 f2 dr_a dr_b dr_c (a <= b <= c)
+//   m[21..23] U(c)    += f2 r2 dr_c
+// with f0 = q/r^3, f1 = 3 f0/r^2, f2 = -f1/r^2.  lrf_expand rebuilds the 40
+// reference coefficients, including its diagonal corrections of phi3.
+constexpr int kLrfMom = 24;
 template <typename T>
-__device__ __forceinline__ void lrf_terms(T dx, T dy, T dz, T q, T* acc) {
+__device__ __forceinline__ void lrf_terms(T dx, T dy, T dz, T q, T* m) {
     T r2 = dx * dx + dy * dy + dz * dz;
-    T f0, f1;
+    T ri2, f0;
     if constexpr (std::is_same<T, float>::value) {
         float ri = rsqrtf(r2);
-        float ri2 = ri * ri;
+        ri2 = ri * ri;
         f0 = q * ri * ri2;
-        f1 = 3.0f * f0 * ri2;
     } else {
+        ri2 = 1.0 / r2;
         f0 = q / (r2 * sqrt(r2));
-        f1 = T(3) * f0 / r2;
     }
-    T f2 = -f1 / r2;
-    T d[3] = {dx, dy, dz};
-    acc[0] += f0 * r2;
-    acc[1] -= dx * f0;
-    acc[2] -= dy * f0;
-    acc[3] -= dz * f0;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        T t = d[a] * f1;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) acc[4 + 3 * a + c] += d[c] * t;
-    }
-    acc[4 + 0] -= f0;
-    acc[4 + 4] -= f0;
-    acc[4 + 8] -= f0;
-    T f25 = T(5) * f2;
-#pragma unroll
+    T f1 = T(3) * f0 * ri2;
+    T f2 = -f1 * ri2;
+    m[0] += f0 * r2;
+    m[1] -= dx * f0;
+    m[2] -= dy * f0;
+    m[3] -= dz * f0;
+    T ax = dx * f1, ay = dy * f1, az = dz * f1;
+    m[4] += ax * dx; m[5] += ax * dy; m[6] += ax * dz;
+    m[7] += ay * dy; m[8] += ay * dz; m[9] += az * dz;
+    m[10] += f0;
+    T g = T(5) * f2;
+    T gxx = g * dx * dx, gyy = g * dy * dy, gzz = g * dz * dz, gxy = g * dx * dy, gxz = g * dx * dz,
+      gyz = g * dy * dz;
+    m[11] += gxx * dx;   // xxx
+    m[12] += gxx * dy;   // xxy
+    m[13] += gxx * dz;   // xxz
+    m[14] += gyy * dx;   // xyy
+    m[15] += gxy * dz;   // xyz
+    m[16] += gzz * dx;   // xzz
+    m[17] += gyy * dy;   // yyy
+    m[18] += gyy * dz;   // yyz
+    m[19] += gzz * dy;   // yzz
+    m[20] += gzz * dz;   // zzz
+    T h = f2 * r2;
+    m[21] += h * dx;
+    m[22] += h * dy;
+    m[23] += h * dz;
+}
+
+// 40 reference coefficients (phi0, phi1(3), phi2(3x3), phi3(9x3)) from the moments
+__device__ __forceinline__ void lrf_expand(const double* m, double* L) {
+    // S3 index of the sorted triple (a<=b<=c)
+    auto s3 = [&](int a, int b, int c) -> double {
+        int t;
+        if (a > b) { t = a; a = b; b = t; }
+        if (b > c) { t = b; b = c; c = t; }
+        if (a > b) { t = a; a = b; b = t; }
+        const int idx[3][3][3] = {{{11, 12, 13}, {12, 14, 15}, {13, 15, 16}},
+                                  {{12, 14, 15}, {14, 17, 18}, {15, 18, 19}},
+                                  {{13, 15, 16}, {15, 18, 19}, {16, 19, 20}}};
+        return m[idx[a][b][c]];
+    };
+    const int i2[3][3] = {{4, 5, 6}, {5, 7, 8}, {6, 8, 9}};
+    L[0] = m[0];
+    L[1] = m[1];
+    L[2] = m[2];
+    L[3] = m[3];
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) L[4 + 3 * a + c] = m[i2[a][c]] - (a == c ? m[10] : 0.0);
     for (int n = 0; n < 3; ++n)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            T tk = d[n] * d[j] * f25;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) acc[13 + 3 * (j + 3 * n) + c] += tk * d[c];
-        }
-    T u0 = dx * r2 * f2, u1 = dy * r2 * f2, u2 = dz * r2 * f2;
-    T* P = acc + 13;   // P[3*m + c] = phi3(m+1) component c
-    P[0] -= T(3) * u0; P[1] -= u1; P[2] -= u2;
-    P[3] -= u1; P[4] -= u0;
-    P[6] -= u2;
-    P[8] -= u0;
-    P[9] -= u1; P[10] -= u0;
-    P[12] -= u0; P[13] -= T(3) * u1; P[14] -= u2;
-    P[16] -= u2; P[17] -= u1;
-    P[18] -= u2;
-    P[20] -= u0;
-    P[22] -= u2; P[23] -= u1;
-    P[24] -= u0; P[25] -= u1; P[26] -= T(3) * u2;
+        for (int j = 0; j < 3; ++j)
+            for (int c = 0; c < 3; ++c) L[13 + 3 * (j + 3 * n) + c] = s3(n, j, c);
+    const double* U = m + 21;
+    double* P = L + 13;
+    P[0] -= 3.0 * U[0]; P[1] -= U[1]; P[2] -= U[2];
+    P[3] -= U[1]; P[4] -= U[0];
+    P[6] -= U[2];
+    P[8] -= U[0];
+    P[9] -= U[1]; P[10] -= U[0];
+    P[12] -= U[0]; P[13] -= 3.0 * U[1]; P[14] -= U[2];
+    P[16] -= U[2]; P[17] -= U[1];
+    P[18] -= U[2];
+    P[20] -= U[0];
+    P[22] -= U[2]; P[23] -= U[1];
+    P[24] -= U[0]; P[25] -= U[1]; P[26] -= 3.0 * U[2];
 }
 
 // LRF classification of a group pair: true when rc2 < r2 <= rlrf2 in FP64
@@ -502,13 +540,18 @@ __device__ __forceinline__ bool lrf_pair(float r2f, double rc2, double rlrf2, co
     return r2 > rc2 && r2 <= rlrf2;
 }
 
+// One warp per target group g2 sums the far-field contributions of every
+// non-Q atom whose group is classified "LRF" against g2 (lanes stride over the
+// atoms, so loads are coalesced); the 40 coefficients are then reduced across
+// the warp.  Mixed form: FP32 terms (rsqrt on the SFU); FP64 form: FP64 terms.
 template <bool MIX>
-__global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const DevState* __restrict__ states, Cut c) {
+__global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const DevState* __restrict__ states, Cut c,
+                                                         const int* __restrict__ lrf_src) {
+    typedef typename std::conditional<MIX, float, double>::type T;
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
     const float4* __restrict__ xq = s.xq;
     double* __restrict__ lrf = s.lrf;
-    typedef typename std::conditional<MIX, float, double>::type T;
     int lane = threadIdx.x & 31;
     for (int g2 = warp_id_global(); g2 < m.ncgp; g2 += warps_total()) {
         int s2 = group_dist_atom(m, g2);
@@ -518,32 +561,33 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const DevSta
         double cx = L[0], cy = L[1], cz = L[2];
         float4 x2 = xq[s2];
         float cxf = (float)(cx - m.xpcent[0]), cyf = (float)(cy - m.xpcent[1]), czf = (float)(cz - m.xpcent[2]);
-        T acc[40];
+        const double rc_s = sol2 ? c.rcpp2 : c.rcpw2, rc_w = sol2 ? c.rcpw2 : c.rcww2;
+        T mom[kLrfMom];
 #pragma unroll
-        for (int k = 0; k < 40; ++k) acc[k] = T(0);
-        for (int g1 = lane; g1 < m.ncgp; g1 += kWarp) {
-            if (g1 == g2) continue;
-            int s1 = group_dist_atom(m, g1);
-            if (m.excl[s1]) continue;
-            bool sol1 = g1 < m.ncgp_solute;
-            double rc2 = (sol1 && sol2) ? c.rcpp2 : ((sol1 || sol2) ? c.rcpw2 : c.rcww2);
+        for (int k = 0; k < kLrfMom; ++k) mom[k] = T(0);
+        for (int i = lane; i < m.natom; i += kWarp) {
+            int src = lrf_src[i];   // distance atom of i's group | solute flag << 30, -1 if never a source
+            if (src < 0) continue;
+            int s1 = src & 0x3fffffff;
+            if (s1 == s2) continue;   // same group
+            double rc2 = (src >> 30) ? rc_s : rc_w;
             if (!lrf_pair(r2_f(x2, xq[s1]), rc2, c.rlrf2, x, s2, s1)) continue;
-            for (int a = m.gslot[g1]; a < m.gslot[g1 + 1]; ++a) {
-                int i = m.gatom[a];
-                if (m.iqatom[i] >= 0) continue;
-                if constexpr (MIX) {
-                    float4 xi = xq[i];
-                    lrf_terms<float>(xi.x - cxf, xi.y - cyf, xi.z - czf, xi.w, acc);
-                } else {
-                    lrf_terms<double>(x[3 * i] - cx, x[3 * i + 1] - cy, x[3 * i + 2] - cz, m.crg[i], acc);
-                }
+            if constexpr (MIX) {
+                float4 xi = xq[i];
+                lrf_terms<float>(xi.x - cxf, xi.y - cyf, xi.z - czf, xi.w, mom);
+            } else {
+                lrf_terms<double>(x[3 * i] - cx, x[3 * i + 1] - cy, x[3 * i + 2] - cz, m.crg[i], mom);
             }
         }
+        double tot[kLrfMom];
 #pragma unroll
-        for (int k = 0; k < 40; ++k) {
-            double v = warp_sum((double)acc[k]);
-            if (lane == 0) L[3 + k] = v;
+        for (int k = 0; k < kLrfMom; ++k) {
+            T v = mom[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+            tot[k] = (double)v;
         }
+        if (lane == 0) lrf_expand(tot, L + 3);
     }
 }
 
@@ -746,7 +790,7 @@ __device__ __forceinline__ void nbe_qx_d(double r2, double r, double r6_hc, doub
 }
 __device__ __forceinline__ void nbe_qx_f(float r2, float r, float r6_hc, float A, float B, float el, float sc,
                                          float lam, float& vel, float& vdw, float& dv) {
-    float r6 = __frcp_rn(r6_hc + sc);
+    float r6 = __fdividef(1.0f, r6_hc + sc);
     float r12 = r6 * r6;
     vel = el * r;
     float va = A * r12, vb = B * r6;
@@ -786,180 +830,159 @@ __device__ __forceinline__ void flush_q_grad(const DevModel& m, const DevState& 
     }
 }
 
-// nonbond_qw_spc / nonbond_qw, src/nonbondene.f90:5658-5767, 5339-5418:
-// one warp per listed water molecule, lane = Q atom.
-template <bool MIX, bool SPC>
-__global__ void __launch_bounds__(kQBlock) k_qw(DevModel m, const DevState* __restrict__ states) {
+// Per-lane Q-atom x environment-atom interaction for all states (soft-core
+// LJ + Coulomb when lj, Coulomb only otherwise): returns the lambda-weighted
+// dv sum over states and adds the per-state energies to pel/pvdw.
+template <bool MIX, int SMAX>
+struct QPairT;
+template <int SMAX>
+struct QPairT<false, SMAX> {
+    __device__ __forceinline__ static double run(const QPar* P, const double* lam, int S, bool lj, double r2, double r,
+                                                 double* pel, double* pvdw) {
+        double dvs = 0.0;
+        if (lj) {
+            double r6hc = 1.0 / (r2 * r2 * r2);
+#pragma unroll
+            for (int st = 0; st < SMAX; ++st) {
+                if (st >= S) break;
+                QPar q = P[st];
+                double vel, vdw, dv;
+                nbe_qx_d(r2, r, r6hc, q.A, q.B, q.el, q.sc, lam[st], vel, vdw, dv);
+                dvs += dv;
+                pel[st] += vel;
+                pvdw[st] += vdw;
+            }
+        } else {   // nbe_qspc, src/nonbonded.f90:226-243
+#pragma unroll
+            for (int st = 0; st < SMAX; ++st) {
+                if (st >= S) break;
+                double vel = P[st].el * r;
+                dvs += -r2 * vel * lam[st];
+                pel[st] += vel;
+            }
+        }
+        return dvs;
+    }
+};
+template <int SMAX>
+struct QPairT<true, SMAX> {
+    __device__ __forceinline__ static float run(const QParF* P, const float* lam, int S, bool lj, float r2, float r,
+                                                float* pel, float* pvdw) {
+        float dvs = 0.0f;
+        if (lj) {
+            float r6hc = __fdividef(1.0f, r2 * r2 * r2);
+#pragma unroll
+            for (int st = 0; st < SMAX; ++st) {
+                if (st >= S) break;
+                QParF q = P[st];
+                float vel, vdw, dv;
+                nbe_qx_f(r2, r, r6hc, q.A, q.B, q.el, q.sc, lam[st], vel, vdw, dv);
+                dvs += dv;
+                pel[st] += vel;
+                pvdw[st] += vdw;
+            }
+        } else {
+#pragma unroll
+            for (int st = 0; st < SMAX; ++st) {
+                if (st >= S) break;
+                float vel = P[st].el * r;
+                dvs += -r2 * vel * lam[st];
+                pel[st] += vel;
+            }
+        }
+        return dvs;
+    }
+};
+
+// nonbond_qw_spc / nonbond_qw (src/nonbondene.f90:5658-5767, 5339-5418) and
+// nonbond_qp (src/nonbondene.f90:5157-5230): one warp per listed environment
+// unit (a water molecule, or one solute atom), lane = Q atom.  The unit's
+// per-state energies are summed in registers and converted once per unit.
+template <bool MIX, bool SPC, bool WATER, int SMAX>
+__global__ void __launch_bounds__(kQBlock) k_qenv(DevModel m, const DevState* __restrict__ states) {
+    typedef typename std::conditional<MIX, float, double>::type T;
     const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
-    ESum<MIX> eel[kMaxStates], evdw[kMaxStates];
+    ESum<MIX> eel[SMAX], evdw[SMAX];
     float gqf[2][3] = {};
     double gqd[2][3] = {};
+    T lam[SMAX];
+#pragma unroll
+    for (int st = 0; st < SMAX; ++st) lam[st] = st < m.S ? (T)s.lambda[st] : T(0);
     int lane = threadIdx.x & 31;
-    int n = min((int64_t)s.cnt[C_QW], s.cap_qw);
-    int sa = m.sa, S = m.S;
+    int n = WATER ? min((int64_t)s.cnt[C_QW], s.cap_qw) : min((int64_t)s.cnt[C_QP], s.cap_qp);
+    int S = m.S;
+    const int na = WATER ? m.sa : 1;
     for (int p = warp_id_global(); p < n; p += warps_total()) {
-        int j0 = m.nat_solute + sa * s.qw[p];
-        for (int a = 0; a < sa; ++a) {
+        int j0 = WATER ? m.nat_solute + m.sa * s.qw[p] : s.qp[p];
+        T pel[SMAX], pvdw[SMAX];
+#pragma unroll
+        for (int st = 0; st < SMAX; ++st) pel[st] = pvdw[st] = T(0);
+        for (int a = 0; a < na; ++a) {
             int j = j0 + a;
-            bool lj = !SPC || a == 0;
-            float gjf[3] = {0, 0, 0};
-            double gjd[3] = {0, 0, 0};
+            bool lj = !WATER || !SPC || a == 0;
+            T gj[3] = {T(0), T(0), T(0)};
 #pragma unroll
             for (int k = 0; k < kMaxQ / 32; ++k) {
                 int iq = k * 32 + lane;
                 if (iq >= m.nqat) break;
                 int i = m.iqseq[iq];
-                const QPar* P = m.qw_tab + (iq * sa + a) * S;
-                if constexpr (!MIX) {
-                    double tx = s.x[3 * j] - s.x[3 * i], ty = s.x[3 * j + 1] - s.x[3 * i + 1],
-                           tz = s.x[3 * j + 2] - s.x[3 * i + 2];
-                    double r2 = 1.0 / (tx * tx + ty * ty + tz * tz);
-                    double r = sqrt(r2);
-                    double dvs = 0.0;
-                    if (lj) {
-                        double r6hc = 1.0 / (r2 * r2 * r2);
-                        for (int st = 0; st < S; ++st) {
-                            QPar q = P[st];
-                            double vel, vdw, dv;
-                            nbe_qx_d(r2, r, r6hc, q.A, q.B, q.el, q.sc, s.lambda[st], vel, vdw, dv);
-                            dvs += dv;
-                            eel[st].add(vel);
-                            evdw[st].add(vdw);
-                        }
-                    } else {   // nbe_qspc, src/nonbonded.f90:226-243
-                        for (int st = 0; st < S; ++st) {
-                            double vel = P[st].el * r;
-                            dvs += -r2 * vel * s.lambda[st];
-                            eel[st].add(vel);
-                        }
-                    }
-                    gqd[k][0] -= tx * dvs; gqd[k][1] -= ty * dvs; gqd[k][2] -= tz * dvs;
-                    gjd[0] += tx * dvs; gjd[1] += ty * dvs; gjd[2] += tz * dvs;
-                } else {
-                    const QParF* F = m.qw_tabf + (iq * sa + a) * S;
+                T tx, ty, tz, r2, r;
+                if constexpr (MIX) {
                     float4 xi = s.xq[i], xj = s.xq[j];
-                    float tx = xj.x - xi.x, ty = xj.y - xi.y, tz = xj.z - xi.z;
-                    float ri = rsqrtf(tx * tx + ty * ty + tz * tz);
-                    float r2 = ri * ri;
-                    float dvs = 0.0f;
-                    if (lj) {
-                        float r6hc = __frcp_rn(r2 * r2 * r2);
-                        for (int st = 0; st < S; ++st) {
-                            QParF q = F[st];
-                            float vel, vdw, dv;
-                            nbe_qx_f(r2, ri, r6hc, q.A, q.B, q.el, q.sc, (float)s.lambda[st], vel, vdw, dv);
-                            dvs += dv;
-                            eel[st].add(vel);
-                            evdw[st].add(vdw);
-                        }
-                    } else {
-                        for (int st = 0; st < S; ++st) {
-                            float vel = F[st].el * ri;
-                            dvs += -r2 * vel * (float)s.lambda[st];
-                            eel[st].add(vel);
-                        }
-                    }
-                    gqf[k][0] -= tx * dvs; gqf[k][1] -= ty * dvs; gqf[k][2] -= tz * dvs;
-                    gjf[0] += tx * dvs; gjf[1] += ty * dvs; gjf[2] += tz * dvs;
+                    tx = xj.x - xi.x;
+                    ty = xj.y - xi.y;
+                    tz = xj.z - xi.z;
+                    r = rsqrtf(tx * tx + ty * ty + tz * tz);
+                    r2 = r * r;
+                } else {
+                    tx = s.x[3 * j] - s.x[3 * i];
+                    ty = s.x[3 * j + 1] - s.x[3 * i + 1];
+                    tz = s.x[3 * j + 2] - s.x[3 * i + 2];
+                    r2 = 1.0 / (tx * tx + ty * ty + tz * tz);
+                    r = sqrt(r2);
                 }
+                T dvs;
+                if constexpr (MIX) {
+                    const QParF* P = WATER ? m.qw_tabf + (iq * m.sa + a) * S : m.qp_tabf + ((size_t)j * m.nqat + iq) * S;
+                    dvs = QPairT<true, SMAX>::run(P, lam, S, lj, r2, r, pel, pvdw);
+                    gqf[k][0] -= tx * dvs; gqf[k][1] -= ty * dvs; gqf[k][2] -= tz * dvs;
+                } else {
+                    const QPar* P = WATER ? m.qw_tab + (iq * m.sa + a) * S : m.qp_tab + ((size_t)j * m.nqat + iq) * S;
+                    dvs = QPairT<false, SMAX>::run(P, lam, S, lj, r2, r, pel, pvdw);
+                    gqd[k][0] -= tx * dvs; gqd[k][1] -= ty * dvs; gqd[k][2] -= tz * dvs;
+                }
+                gj[0] += tx * dvs;
+                gj[1] += ty * dvs;
+                gj[2] += tz * dvs;
             }
-            // molecule atom gradient: sum over the warp's Q atoms
+            // environment atom gradient: sum over the warp's Q atoms
             if constexpr (MIX) {
-                unsigned long long v0 = warp_sum(to_fix(gjf[0])), v1 = warp_sum(to_fix(gjf[1])),
-                                   v2 = warp_sum(to_fix(gjf[2]));
+                unsigned long long v0 = warp_sum(to_fix(gj[0])), v1 = warp_sum(to_fix(gj[1])),
+                                   v2 = warp_sum(to_fix(gj[2]));
                 if (lane == 0) {
                     atomicAdd(s.fix + 3 * j, v0);
                     atomicAdd(s.fix + 3 * j + 1, v1);
                     atomicAdd(s.fix + 3 * j + 2, v2);
                 }
             } else {
-                double v0 = warp_sum(gjd[0]), v1 = warp_sum(gjd[1]), v2 = warp_sum(gjd[2]);
+                double v0 = warp_sum(gj[0]), v1 = warp_sum(gj[1]), v2 = warp_sum(gj[2]);
                 if (lane == 0) acc.grad(j, v0, v1, v2);
             }
         }
-    }
-    for (int st = 0; st < S; ++st) {
-        eel[st].flush(acc, eq_slot(st, 4));
-        evdw[st].flush(acc, eq_slot(st, 5));
-    }
-    flush_q_grad<MIX>(m, s, gqf, gqd);
-}
-
-// nonbond_qp, src/nonbondene.f90:5157-5230 (qp_precomp, src/simprep.f90:3112-3148):
-// one warp per listed solute atom, lane = Q atom.
-template <bool MIX>
-__global__ void __launch_bounds__(kQBlock) k_qp(DevModel m, const DevState* __restrict__ states) {
-    const DevState& s = states[blockIdx.y];
-    Acc<MIX> acc = make_acc<MIX>(s);
-    ESum<MIX> eel[kMaxStates], evdw[kMaxStates];
-    float gqf[2][3] = {};
-    double gqd[2][3] = {};
-    int lane = threadIdx.x & 31;
-    int n = min((int64_t)s.cnt[C_QP], s.cap_qp);
-    int S = m.S;
-    for (int p = warp_id_global(); p < n; p += warps_total()) {
-        int j = s.qp[p];
-        float gjf[3] = {0, 0, 0};
-        double gjd[3] = {0, 0, 0};
 #pragma unroll
-        for (int k = 0; k < kMaxQ / 32; ++k) {
-            int iq = k * 32 + lane;
-            if (iq >= m.nqat) break;
-            int i = m.iqseq[iq];
-            size_t t0 = ((size_t)j * m.nqat + iq) * S;
-            if constexpr (!MIX) {
-                double tx = s.x[3 * j] - s.x[3 * i], ty = s.x[3 * j + 1] - s.x[3 * i + 1],
-                       tz = s.x[3 * j + 2] - s.x[3 * i + 2];
-                double r2 = 1.0 / (tx * tx + ty * ty + tz * tz);
-                double r = sqrt(r2);
-                double r6hc = 1.0 / (r2 * r2 * r2);
-                double dvs = 0.0;
-                for (int st = 0; st < S; ++st) {
-                    QPar q = m.qp_tab[t0 + st];
-                    double vel, vdw, dv;
-                    nbe_qx_d(r2, r, r6hc, q.A, q.B, q.el, q.sc, s.lambda[st], vel, vdw, dv);
-                    dvs += dv;
-                    eel[st].add(vel);
-                    evdw[st].add(vdw);
-                }
-                gqd[k][0] -= tx * dvs; gqd[k][1] -= ty * dvs; gqd[k][2] -= tz * dvs;
-                gjd[0] += tx * dvs; gjd[1] += ty * dvs; gjd[2] += tz * dvs;
-            } else {
-                float4 xi = s.xq[i], xj = s.xq[j];
-                float tx = xj.x - xi.x, ty = xj.y - xi.y, tz = xj.z - xi.z;
-                float ri = rsqrtf(tx * tx + ty * ty + tz * tz);
-                float r2 = ri * ri;
-                float r6hc = __frcp_rn(r2 * r2 * r2);
-                float dvs = 0.0f;
-                for (int st = 0; st < S; ++st) {
-                    QParF q = m.qp_tabf[t0 + st];
-                    float vel, vdw, dv;
-                    nbe_qx_f(r2, ri, r6hc, q.A, q.B, q.el, q.sc, (float)s.lambda[st], vel, vdw, dv);
-                    dvs += dv;
-                    eel[st].add(vel);
-                    evdw[st].add(vdw);
-                }
-                gqf[k][0] -= tx * dvs; gqf[k][1] -= ty * dvs; gqf[k][2] -= tz * dvs;
-                gjf[0] += tx * dvs; gjf[1] += ty * dvs; gjf[2] += tz * dvs;
-            }
-        }
-        if constexpr (MIX) {
-            unsigned long long v0 = warp_sum(to_fix(gjf[0])), v1 = warp_sum(to_fix(gjf[1])),
-                               v2 = warp_sum(to_fix(gjf[2]));
-            if (lane == 0) {
-                atomicAdd(s.fix + 3 * j, v0);
-                atomicAdd(s.fix + 3 * j + 1, v1);
-                atomicAdd(s.fix + 3 * j + 2, v2);
-            }
-        } else {
-            double v0 = warp_sum(gjd[0]), v1 = warp_sum(gjd[1]), v2 = warp_sum(gjd[2]);
-            if (lane == 0) acc.grad(j, v0, v1, v2);
+        for (int st = 0; st < SMAX; ++st) {
+            if (st >= S) break;
+            eel[st].add(pel[st]);
+            evdw[st].add(pvdw[st]);
         }
     }
-    for (int st = 0; st < S; ++st) {
-        eel[st].flush(acc, eq_slot(st, 2));
-        evdw[st].flush(acc, eq_slot(st, 3));
+    const int kel = WATER ? 4 : 2;
+#pragma unroll
+    for (int st = 0; st < SMAX; ++st) {
+        if (st >= S) break;
+        eel[st].flush(acc, eq_slot(st, kel));
+        evdw[st].flush(acc, eq_slot(st, kel + 1));
     }
     flush_q_grad<MIX>(m, s, gqf, gqd);
 }
@@ -1515,6 +1538,9 @@ __global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState*
                 qa[a] = true;
             }
         }
+        // per-row FP32 energy sums of this lane, converted to fixed point once
+        // per row (row contents do not depend on the grid, so neither do they)
+        float rpel = 0.f, rpvdw = 0.f, rwel = 0.f, rwvdw = 0.f;
         // ---- solute partner atoms (nonbond_pp, src/nonbondene.f90:4694-4760)
         const uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
         for (int k = lane; k < npp; k += kWarp) {
@@ -1523,6 +1549,7 @@ __global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState*
             bool lowerg = (e.x >> 28) & 1u, sameg = (e.x >> 29) & 1u;
             float4 xb = xq[j];
             int tj = m.iac[j];
+            float pel = 0.f, pvdw = 0.f;   // this entry's energies, converted once
 #pragma unroll
             for (int a = 0; a < MAXG; ++a) {
                 if (qa[a]) continue;
@@ -1536,15 +1563,18 @@ __global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState*
                 float vel, vdw;
                 pair_f(xa[a], xb, A, B, el, true, f[a][0], f[a][1], f[a][2], vel, vdw);
                 if (lowerg || (sameg && ia[a] < j)) {   // each pair's energy once
-                    epel.add(vel);
-                    epvdw.add(vdw);
+                    pel += vel;
+                    pvdw += vdw;
                 }
             }
+            rpel += pel;
+            rpvdw += pvdw;
         }
         // ---- water partners (nonbond_pw, src/nonbondene.f90:4856-4916); energy counted here
         const int* rw = s.row_gw + (size_t)g * s.cap_gw;
         for (int k = lane; k < npw; k += kWarp) {
             int j0 = m.nat_solute + m.sa * rw[k];
+            float pel = 0.f, pvdw = 0.f;
             for (int b = 0; b < m.sa; ++b) {
                 float4 xb = xq[j0 + b];
                 int tw = m.wtype[b];
@@ -1554,11 +1584,17 @@ __global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState*
                     float4 p = lj(ta[a], tw);
                     float vel, vdw;
                     pair_f(xa[a], xb, p.x, p.y, xa[a].w * m.wcrgf[b], true, f[a][0], f[a][1], f[a][2], vel, vdw);
-                    ewel.add(vel);
-                    ewvdw.add(vdw);
+                    pel += vel;
+                    pvdw += vdw;
                 }
             }
+            rwel += pel;
+            rwvdw += pvdw;
         }
+        epel.add(rpel);
+        epvdw.add(rpvdw);
+        ewel.add(rwel);
+        ewvdw.add(rwvdw);
 #pragma unroll
         for (int a = 0; a < MAXG; ++a) {
             if (a >= n1) break;   // warp-uniform
@@ -1600,11 +1636,12 @@ __global__ void __launch_bounds__(128) k_rows_water(DevModel m, const DevState* 
             f[a][0] = f[a][1] = f[a][2] = 0.f;
             xa[a] = a < sa ? xq[i0 + a] : make_float4(0, 0, 0, 0);
         }
+        float rel = 0.f, rvdw = 0.f;
         const int* rw = s.row_ww + (size_t)w * s.cap_rww;
         for (int k = lane; k < nww; k += kWarp) {
             int w2 = rw[k];
             int j0 = m.nat_solute + sa * w2;
-            bool count = w < w2;
+            float pel = 0.f, pvdw = 0.f;
 #pragma unroll
             for (int b = 0; b < kMaxSolv; ++b) {
                 if (b >= sa) break;
@@ -1616,13 +1653,17 @@ __global__ void __launch_bounds__(128) k_rows_water(DevModel m, const DevState* 
                     bool lj = !SPC || (a == 0 && b == 0);
                     float vel, vdw;
                     pair_f(xa[a], xb, m.wwAf[kk], m.wwBf[kk], m.wwEf[kk], lj, f[a][0], f[a][1], f[a][2], vel, vdw);
-                    if (count) {
-                        eel.add(vel);
-                        if (lj) evdw.add(vdw);
-                    }
+                    pel += vel;
+                    if (lj) pvdw += vdw;
                 }
             }
+            if (w < w2) {   // each molecule pair's energy once
+                rel += pel;
+                rvdw += pvdw;
+            }
         }
+        eel.add(rel);
+        evdw.add(rvdw);
         const int* rg = s.row_wg + (size_t)w * s.cap_wg;
         for (int k = lane; k < nwg; k += kWarp) {
             int g = rg[k];
@@ -1727,10 +1768,10 @@ void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2) {
     if (L.m.ncgp_solute == 0 || L.m.nqat == 0) return;
     k_build_qp<<<dim3((L.m.ncgp_solute + 127) / 128, L.nwin), 128, 0, L.st>>>(L.m, L.ds, qnear, rcq2);
 }
-void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed) {
+void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src) {
     dim3 g = grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin);
-    if (mixed) k_lrf_accumulate<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
-    else k_lrf_accumulate<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+    if (mixed) k_lrf_accumulate<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
+    else k_lrf_accumulate<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
 }
 
 void launch_build_rows(const Launch& L, const Cut& c) {
@@ -1742,6 +1783,7 @@ void launch_rows_solute(const Launch& L, int maxg) {
     if (L.m.ncgp_solute == 0) return;
     dim3 g = grid_for((int64_t)L.m.ncgp_solute * 32, 128, 16, L.nwin);
     if (maxg <= 4) k_rows_solute<4><<<g, 128, 0, L.st>>>(L.m, L.ds);
+    else if (maxg <= 6) k_rows_solute<6><<<g, 128, 0, L.st>>>(L.m, L.ds);
     else if (maxg <= 8) k_rows_solute<8><<<g, 128, 0, L.st>>>(L.m, L.ds);
     else k_rows_solute<16><<<g, 128, 0, L.st>>>(L.m, L.ds);
 }
@@ -1758,12 +1800,23 @@ void launch_ww(const Launch& L, int mixed) {
     if (mixed) { if (spc) k_ww<true, true><<<g, 256, 0, L.st>>>(L.m, L.ds); else k_ww<true, false><<<g, 256, 0, L.st>>>(L.m, L.ds); }
     else { if (spc) k_ww<false, true><<<g, 256, 0, L.st>>>(L.m, L.ds); else k_ww<false, false><<<g, 256, 0, L.st>>>(L.m, L.ds); }
 }
+template <bool WATER>
+void launch_qenv(const Launch& L, int mixed, dim3 g) {
+    bool spc = L.m.spc != 0;
+    bool s4 = L.m.S <= 4;
+#define QL(MIX, SPC, SM) k_qenv<MIX, SPC, WATER, SM><<<g, kQBlock, 0, L.st>>>(L.m, L.ds)
+    if (mixed) {
+        if (spc) { if (s4) QL(true, true, 4); else QL(true, true, kMaxStates); }
+        else { if (s4) QL(true, false, 4); else QL(true, false, kMaxStates); }
+    } else {
+        if (spc) { if (s4) QL(false, true, 4); else QL(false, true, kMaxStates); }
+        else { if (s4) QL(false, false, 4); else QL(false, false, kMaxStates); }
+    }
+#undef QL
+}
 void launch_qw(const Launch& L, int mixed) {
     if (L.m.nwat == 0 || L.m.nqat == 0) return;
-    dim3 g = grid_for(L.s0.cap_qw * 32, kQBlock, 8, L.nwin);
-    bool spc = L.m.spc != 0;
-    if (mixed) { if (spc) k_qw<true, true><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); else k_qw<true, false><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); }
-    else { if (spc) k_qw<false, true><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); else k_qw<false, false><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); }
+    launch_qenv<true>(L, mixed, grid_for(L.s0.cap_qw * 32, kQBlock, 8, L.nwin));
 }
 void launch_pw(const Launch& L, int mixed) {
     if (L.m.nwat == 0 || L.m.ncgp_solute == 0) return;
@@ -1777,8 +1830,7 @@ void launch_pp(const Launch& L, int mixed) {
 }
 void launch_qp(const Launch& L, int mixed) {
     if (L.m.nqat == 0 || L.m.nat_solute == 0) return;
-    dim3 g = grid_for(L.s0.cap_qp * 32, kQBlock, 8, L.nwin);
-    if (mixed) k_qp<true><<<g, kQBlock, 0, L.st>>>(L.m, L.ds); else k_qp<false><<<g, kQBlock, 0, L.st>>>(L.m, L.ds);
+    launch_qenv<false>(L, mixed, grid_for(L.s0.cap_qp * 32, kQBlock, 8, L.nwin));
 }
 void launch_nonbond_qq(const Launch& L, int mixed) {
     if (L.s0.nqq == 0) return;
