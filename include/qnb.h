@@ -290,6 +290,37 @@ int qnb_profile(qnb_context* ctx, int32_t enable);
    (n entries, n <= QNB_K_COUNT); resets the totals. */
 int qnb_kernel_times(qnb_context* ctx, double* ms, int64_t* launches, int32_t n);
 
+/* ---- allocation-free entry point (no counterpart in the reference) ------- */
+
+/* Water-water SPC energies and gradient without any device allocation, for
+   callers that may not call cudaMalloc: a host that gives this library a
+   fixed memory budget, work recorded into a CUDA graph, or a process whose
+   own allocator owns the device.  It is the FP64 nbwwlist + nonbond_ww_spc
+   computation: water pairs whose O atoms lie within rc2 (neither O excluded)
+   each contribute LJ + Coulomb for O-O and Coulomb for the other eight atom
+   pairs.
+   Inputs and outputs are the caller's device buffers:
+     x_dev    natom x 3 coordinates; waters are 3 atoms each, starting at
+              atom first_water_atom (O, H, H);
+     excl_dev optional excluded-atom flags (u8 per atom), or NULL;
+     q_oxygen, q_hydrogen  scaled charges; A_oo, B_oo the O-O LJ A and B;
+     d_dev    gradient, natom x 3, ADDED into;
+     e_dev    2 doubles, el and vdW, ADDED into;
+     stream   a cudaStream_t, or NULL for the legacy default stream.
+   Scratch: a file-scope device array that holds 1,048,576 water pairs
+   (8 MiB). Every GPU that loads the library keeps it until the process
+   exits. More than 65,536 waters, or more pairs within the cut-off than the
+   array holds, returns QNB_ERR_CAPACITY (message in qnb_last_error).  All
+   calls on a device share the array: each call clears its counter first,
+   and calls that overlap on the GPU (different streams or threads) race.
+   The first call on a device looks up the array's device address
+   (cudaGetSymbolAddress) with that device current; make that first call
+   before any stream capture.  The call waits on `stream` once, after the
+   pair selection, to check the pair count. */
+int qnb_ww_spc_noalloc(const double* x_dev, const uint8_t* excl_dev, int32_t first_water_atom, int32_t nwat,
+                       double q_oxygen, double q_hydrogen, double A_oo, double B_oo, double rc2,
+                       double* d_dev, double* e_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

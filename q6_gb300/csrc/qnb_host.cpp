@@ -61,6 +61,11 @@ void combine(int rule, double ai, double aj, double bi, double bj, double* A, do
 
 }  // namespace
 
+int qnb::set_error(int code, const char* msg) {
+    g_err = msg;
+    return code;
+}
+
 struct qnb_context {
     int device = 0;
     cudaStream_t stream = nullptr;

@@ -176,4 +176,7 @@ int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int m
 void launch_export_pairs(const Launch& L, int win, int kind, int32_t* di, int32_t* dj, int64_t cap,
                          int* dcount);
 
+// records msg as the calling thread's qnb_last_error text; returns code
+int set_error(int code, const char* msg);
+
 }  // namespace qnb

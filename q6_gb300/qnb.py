@@ -36,6 +36,7 @@ EXPORTED = (
     "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_take_launch_count",
     "qnb_profile", "qnb_kernel_times", "qnb_create_batch", "qnb_window_count",
     "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
+    "qnb_ww_spc_noalloc",
 )
 KERNEL_CLASSES = ("ww", "qw", "pw", "pp", "qp", "lrf_taylor", "qq", "restrain", "watpol", "pack",
                   "apply", "build", "lrf_build")
@@ -79,6 +80,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_create_batch": [P, P, I32, P], "qnb_window_count": [P, P],
         "qnb_set_lambda_window": [P, I32, P], "qnb_upload_coordinates": [P, P],
         "qnb_download_gradient": [P, P, I32],
+        "qnb_ww_spc_noalloc": [P, P, I32, I32, D, D, D, D, D, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
