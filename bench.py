@@ -167,8 +167,19 @@ def run_ours(args, rank, world, local):
     dom_ms, dom_n = ktimes[dom]
     dom_avg_s = dom_ms / 1e3 / max(dom_n, 1)
     bytes_per_unit = 4.0   # list streaming: 4 B per atom pair read once per step
-    per_win = {"pp": counts["pp"], "pw": counts["pw"], "ww": counts["ww"],
-               "qp": counts["qp"] * s.nstates, "qw": counts["qw"] * s.nstates}.get(dom)
+    if args.prec == "mixed":
+        # gather rows: the solute-row class evaluates pp and the solute side of
+        # pw, the water-row class ww and the water side of pw
+        per_win = {"pp": counts["pp"] + counts["pw"], "ww": counts["ww"] + counts["pw"],
+                   "qp": counts["qp"] * s.nstates, "qw": counts["qw"] * s.nstates}.get(dom)
+        flops_win = {"pp": 33 * counts["pp"] + 77 * counts["pw"] // 3,
+                     "ww": 209 * counts["ww"] // 9 + 77 * counts["pw"] // 3,
+                     "qp": (22 + 17 * s.nstates) * counts["qp"],
+                     "qw": ((22 + 17 * s.nstates) + 2 * (19 + 5 * s.nstates)) * counts["qw"] // 3}.get(dom)
+    else:
+        per_win = {"pp": counts["pp"], "pw": counts["pw"], "ww": counts["ww"],
+                   "qp": counts["qp"] * s.nstates, "qw": counts["qw"] * s.nstates}.get(dom)
+        flops_win = None
     units = per_win * nwin if per_win else None   # one launch covers every window
     peaks = {}
     try:
@@ -182,8 +193,19 @@ def run_ours(args, rank, world, local):
             "unit": "GB/s", "frac": round(ach / hbm_peak, 6) if ach else None, "traffic": read_traffic(dom),
             "peak_source": peak_src, "units_per_launch": units, "bytes_per_unit": bytes_per_unit,
             "avg_launch_us": round(dom_avg_s * 1e6, 2)}
+    fp32_peak = sgemm_fp32_peak(torch)
+    roof_fp32 = None
+    if flops_win:
+        fl = flops_win * nwin / dom_avg_s / 1e12
+        roof_fp32 = {"kernel": dom, "bound": "fp32", "achieved": round(fl, 3), "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": round(fl / fp32_peak, 4) if fp32_peak else None,
+                     "peak_source": "measured here: cuBLAS SGEMM 8192^3 with TF32 off (FP32 CUDA cores)",
+                     "flops_per_launch": flops_win * nwin,
+                     "flops_per_unit": "33 per LJ+Coulomb atom pair, 77 per solute atom x SPC water, "
+                                       "209 per SPC water pair, 22+17S per Q pair with LJ, 19+5S Coulomb-only"}
     pair_interactions = counts["pp"] + counts["pw"] + counts["ww"] + (counts["qp"] + counts["qw"]) * s.nstates
     eng.close()
+    dg = dg_check(s, sp, lams, local, nwin) if args.dg else None
 
     e2e = run_e2e(args, s, sp, lams, prec, local) if args.e2e else None
     out = {
@@ -205,9 +227,11 @@ def run_ours(args, rank, world, local):
         "list_sizes_window0": counts,
         "kernel_ms_total": {k: round(v[0], 4) for k, v in ktimes.items() if v[1]},
         "roofline": roof,
+        "roofline_fp32": roof_fp32,
         "clocks": clk,
         "e2e": e2e,
         "gpu_launches": launches,
+        "dg_check": dg,
     }
     if rank == 0:
         if args.cpu:
@@ -218,6 +242,62 @@ def run_ours(args, rank, world, local):
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def sgemm_fp32_peak(torch):
+    """FP32 CUDA-core throughput of this GPU: best of 5 cuBLAS SGEMMs
+    (8192^3, TF32 disabled), TFLOP/s."""
+    try:
+        prev = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = False
+        n = 8192
+        a = torch.randn(n, n, device="cuda")
+        b = torch.randn(n, n, device="cuda")
+        best = 1e9
+        for _ in range(6):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        torch.backends.cuda.matmul.allow_tf32 = prev
+        del a, b
+        return round(2.0 * n ** 3 / (best / 1e3) / 1e12, 2)
+    except Exception:
+        return None
+
+
+def dg_check(s, sp, lams, local, nwin, frames=4):
+    """Per-window dG (Qfep exponential averaging) of the mixed form against
+    the FP64 form on identical frames: `frames` perturbed copies (0.05 A) of
+    each window's coordinates."""
+    import numpy as np
+    from q6_gb300.fep import BOLTZ, qfep_dg, state_energies, window_increments
+    from q6_gb300.qnb import PREC_FP64, PREC_MIXED, NonbondedEngine
+    from q6_gb300.system import lambdas_for_window
+    rng = np.random.default_rng(99)
+    lam = np.array([lambdas_for_window(l, s.nstates) for l in lams])
+    fr = np.stack([np.stack([s.x + rng.normal(0, 0.05, s.x.shape) for _ in range(frames)]) for _ in range(nwin)])
+    out = {}
+    for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+        v = np.zeros((nwin, frames, s.nstates))
+        with NonbondedEngine(s, precision=prec, device=local, windows=nwin) as e:
+            e.set_solvent_params(sp)
+            for w in range(nwin):
+                e.set_lambda(lam[w], window=w)
+            for k in range(frames):
+                e.set_coordinates_dev(fr[:, k])
+                e.make_pair_lists_dev(**CUT)
+                _, EQ, _ = e.compute_dev(sync=True)
+                v[:, k, :] = state_energies(EQ)
+        out[name] = window_increments(qfep_dg(v, lam, BOLTZ * 300.0)[2])
+    err = np.abs(out["mixed"] - out["fp64"])
+    return {"windows": nwin, "frames_per_window": frames, "max_abs_err_kcal": round(float(err.max()), 6),
+            "mean_abs_err_kcal": round(float(err.mean()), 6), "tolerance_kcal": 0.02,
+            "total_dG_fp64": round(float(out["fp64"].sum()), 4), "total_dG_mixed": round(float(out["mixed"].sum()), 4),
+            "frames": "seeded 0.05 A perturbations of the window coordinates (no MD trajectory)"}
 
 
 def read_traffic(kernel):
@@ -394,6 +474,8 @@ def main():
                     help="skip the host-buffer arm (profiling runs)")
     ap.add_argument("--no-cpu-baseline", dest="cpu", action="store_false",
                     help="skip the CPU oracle sample (profiling runs)")
+    ap.add_argument("--no-dg", dest="dg", action="store_false",
+                    help="skip the mixed-vs-FP64 dG check")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -271,6 +271,20 @@ int qnb_make_pair_lists_dev(qnb_context* ctx, double Rq, double Rcq2, double RcL
 int qnb_compute_dev(qnb_context* ctx, double Tfree, int32_t istep, int32_t sync,
                     qnb_energies* E, qnb_qenergies* EQ, double* Erst);
 
+/* Adjoint of the Q-atom energies (no counterpart in the reference; for
+   force-field and EVB parameter fitting).  For every window w, Q atom iq and
+   state s, at the current device coordinates and lists:
+     dq[w*nqat*nstates + iq + nqat*s] = dE_s/d qcrg(iq,s)   (scaled charge)
+     dA[...]                          = dE_s/d qA(iq,s)
+     dB[...]                          = dE_s/d qB(iq,s)
+   E_s is the state's unweighted Q-atom nonbonded energy (qq + qp + qw).  qA,
+   qB are the Q atom's code-1 LJ factors (A_pair = qA * a_j, B_pair = qB * b_j;
+   qavdw(qiac(iq,s),1) with Q atom types, iaclib(iac)%avdw(1) otherwise);
+   1-4 and soft pairs use other factors and do not contribute to dA/dB.  The
+   gradient of the gap E2-E1 is dE2/dp(.,2) - dE1/dp(.,1).  Pair terms are
+   recomputed from the lists; geometric rule only (QNB_ERR_UNSUPPORTED else). */
+int qnb_q_adjoint_dev(qnb_context* ctx, double* dq, double* dA, double* dB);
+
 /* Number of kernel launches the context issued since the last call. */
 int qnb_take_launch_count(qnb_context* ctx, int64_t* n);
 

@@ -470,6 +470,29 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                 }
             }
         }
+    // adjoint factors of qp pairs: charge factor crg_j (x el14 for 1-4) and
+    // the environment LJ factors when the Q side uses its code-1 factor
+    m.adj_ok = t->ivdw_rule == 1 ? 1 : 0;
+    auto q_side_code1 = [&](int vdw) { return t->qvdw_flag ? (vdw == 1 || vdw == 2) : (vdw == 1); };
+    std::vector<double4_16a> qp_adj(qp_tab.size());
+    if (nq > 0)
+        for (int ig = 0; ig < ns; ++ig) {
+            if (qnear[ig]) continue;
+            for (int jq = 0; jq < nq; ++jq) {
+                int vdw = t->ljcod[t->iac[ig] * nt + t->iac[t->iqseq[jq]]];
+                for (int s2 = 0; s2 < S; ++s2) {
+                    if (QC(s2, ig, jq) == 4) vdw = 3;
+                    double4_16a f;
+                    f.x = t->qq_use_library_charges ? 0.0 : t->crg[ig] * (vdw == 3 ? t->el14_scale : 1.0);
+                    bool lj1 = q_side_code1(vdw);
+                    f.y = lj1 ? t->avdw[t->iac[ig] * 3 + vdw - 1] : 0.0;
+                    f.z = lj1 ? t->bvdw[t->iac[ig] * 3 + vdw - 1] : 0.0;
+                    f.w = 0.0;
+                    qp_adj[((size_t)ig * nq + jq) * S + s2] = f;
+                }
+            }
+        }
+    TRY(c->upload((double4_16a**)&m.qp_adj, qp_adj));
     std::vector<QParF> qp_tabf(qp_tab.size());
     for (size_t k = 0; k < qp_tab.size(); ++k)
         qp_tabf[k] = QParF{(float)qp_tab[k].A, (float)qp_tab[k].B, (float)qp_tab[k].el, (float)qp_tab[k].sc};
@@ -495,6 +518,23 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                     qw_tab[((size_t)iq * sa + a) * S + s] = p;
                 }
             }
+    std::vector<double4_16a> qw_adj(qw_tab.size());
+    if (nq > 0 && t->nwat > 0)
+        for (int iq = 0; iq < nq; ++iq)
+            for (int a = 0; a < sa; ++a) {
+                int tw = t->iac[ns + a];
+                int vdw = t->ljcod[tw * nt + t->iac[t->iqseq[iq]]];
+                for (int s2 = 0; s2 < S; ++s2) {
+                    double4_16a f;
+                    f.x = t->qq_use_library_charges ? 0.0 : t->crg[ns + a];
+                    bool lj1 = q_side_code1(vdw);
+                    f.y = lj1 ? t->avdw[tw * 3 + vdw - 1] : 0.0;
+                    f.z = lj1 ? t->bvdw[tw * 3 + vdw - 1] : 0.0;
+                    f.w = 0.0;
+                    qw_adj[((size_t)iq * sa + a) * S + s2] = f;
+                }
+            }
+    TRY(c->upload((double4_16a**)&m.qw_adj, qw_adj));
     std::vector<QParF> qw_tabf(qw_tab.size());
     for (size_t k = 0; k < qw_tab.size(); ++k)
         qw_tabf[k] = QParF{(float)qw_tab[k].A, (float)qw_tab[k].B, (float)qw_tab[k].el, (float)qw_tab[k].sc};
@@ -504,6 +544,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     // static lists: qq_int_comp + nbqqlist (src/simprep.f90:3152-3268,
     // src/nonbondene.f90:3231-3282)
     std::vector<QQEntry> qq;
+    std::vector<QQAdj> qadj;
     for (int iq = 0; iq + 1 < nq; ++iq) {
         int ia = t->iqseq[iq];
         for (int jq = iq + 1; jq < nq; ++jq) {
@@ -570,6 +611,18 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                 if (vdw == 3) el = el * t->el14_scale;
                 if (!set) continue;
                 qq.push_back(QQEntry{ia, ja, s, (vdw == 2 && t->qvdw_flag) ? 1 : 0, A, B, el, sc});
+                {
+                    double f14 = vdw == 3 ? t->el14_scale : 1.0;
+                    bool lib = t->qq_use_library_charges != 0;
+                    bool lj1 = vdw == 1;
+                    double fa_i = t->qvdw_flag ? t->qavdw[ti * 3] : t->avdw[t->iac[ia] * 3];
+                    double fa_j = t->qvdw_flag ? t->qavdw[tj * 3] : t->avdw[t->iac[ja] * 3];
+                    double fb_i = t->qvdw_flag ? t->qbvdw[ti * 3] : t->bvdw[t->iac[ia] * 3];
+                    double fb_j = t->qvdw_flag ? t->qbvdw[tj * 3] : t->bvdw[t->iac[ja] * 3];
+                    qadj.push_back(QQAdj{iq, jq, s, 0, lib ? 0.0 : QCRG(jq, s) * els * f14,
+                                         lib ? 0.0 : QCRG(iq, s) * els * f14, lj1 ? fa_j : 0.0, lj1 ? fa_i : 0.0,
+                                         lj1 ? fb_j : 0.0, lj1 ? fb_i : 0.0});
+                }
             }
         }
     }
@@ -589,12 +642,20 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                 QPar p = qp_values(iq, ja, s, vdw, &set);
                 if (!set) continue;
                 qq.push_back(QQEntry{ia, ja, s, 0, p.A, p.B, p.el, p.sc});
+                {
+                    bool lj1 = q_side_code1(vdw);
+                    qadj.push_back(QQAdj{iq, -1, s, 0,
+                                         t->qq_use_library_charges ? 0.0 : t->crg[ja] * (vdw == 3 ? t->el14_scale : 1.0),
+                                         0.0, lj1 ? t->avdw[t->iac[ja] * 3 + vdw - 1] : 0.0, 0.0,
+                                         lj1 ? t->bvdw[t->iac[ja] * 3 + vdw - 1] : 0.0, 0.0});
+                }
             }
         }
     }
     c->nqq = (int)qq.size();
     c->nqq_qq = nqq_qq;
     TRY(c->upload(&c->st_qq, qq));
+    TRY(c->upload((QQAdj**)&m.qq_adj, qadj));
     return QNB_OK;
 }
 
@@ -636,6 +697,7 @@ int alloc_state(qnb_context* c) {
         TRY(c->alloc(&s.n_insh, (size_t)kMaxShell));
         TRY(c->alloc(&s.wstate, (size_t)3 * kMaxShell));
         TRY(c->alloc(&s.shell_tsum, (size_t)kMaxShell));
+        TRY(c->alloc(&s.adj, (size_t)3 * std::max(1, m.nqat * m.S)));
         TRY(c->alloc(&s.shell_list, (size_t)kMaxShell * std::max(1, m.nwat)));
         CU(cudaMemset(s.fix, 0, sizeof(unsigned long long) * n3));
         CU(cudaMemset(s.wstate, 0, sizeof(double) * 3 * kMaxShell));
@@ -1252,6 +1314,29 @@ int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, q
                 Erst[2 * w + 1] += e[(size_t)w * kNumE + E_RST_POL];
             }
         }
+    }
+    return QNB_OK;
+}
+
+int qnb_q_adjoint_dev(qnb_context* c, double* dq, double* dA, double* dB) {
+    if (!c || !dq || !dA || !dB) return fail(QNB_ERR_ARG, "null argument");
+    if (!c->m.adj_ok) return fail(QNB_ERR_UNSUPPORTED, "parameter gradients need the geometric combination rule");
+    if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built");
+    CU(cudaSetDevice(c->device));
+    const size_t n = (size_t)c->nqat * c->S;
+    if (n == 0) return QNB_OK;
+    for (int w = 0; w < c->nwin; ++w) CU(cudaMemsetAsync(c->st[w].adj, 0, sizeof(double) * 3 * n, c->stream));
+    if (c->mixed) launch_pack(c->all());
+    launch_q_adjoint(c->all(), c->mixed);
+    c->launches += 3;
+    TRY(check_launch());
+    std::vector<double> h(3 * n);
+    for (int w = 0; w < c->nwin; ++w) {
+        CU(cudaMemcpyAsync(h.data(), c->st[w].adj, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaStreamSynchronize(c->stream));
+        memcpy(dq + w * n, h.data(), sizeof(double) * n);
+        memcpy(dA + w * n, h.data() + n, sizeof(double) * n);
+        memcpy(dB + w * n, h.data() + 2 * n, sizeof(double) * n);
     }
     return QNB_OK;
 }

@@ -39,6 +39,15 @@ struct alignas(16) QParF {
     float A, B, el, sc;
 };
 
+// Adjoint factors of a static Q pair: d(el)/d(qcrg), d(A)/d(qA), d(B)/d(qB)
+// for Q atom iq (c_i, a_i, b_i) and, for Q-Q pairs, for jq (c_j, a_j, b_j);
+// jq = -1 for a Q-bonded solute partner.  a/b are zero for pairs whose Q-side
+// LJ factor is not the code-1 factor (1-4 pairs, soft pairs).
+struct QQAdj {
+    int iq, jq, s, pad;
+    double ci, cj, ai, aj, bi, bj;
+};
+
 // Static model on the device.  Passed by value to kernels.
 struct DevModel {
     int natom, nat_solute, nwat, sa, ncgp, ncgp_solute, natyps, nqat, S;
@@ -75,6 +84,11 @@ struct DevModel {
     const QParF* qp_tabf;
     const QPar* qw_tab;         // [nqat][sa][S]
     const QParF* qw_tabf;
+    // adjoint factors (c, a, b, unused) with the layouts of qp_tab / qw_tab
+    const double4_16a* qp_adj;
+    const double4_16a* qw_adj;
+    const QQAdj* qq_adj;        // parallel to the static Q-Q / Q-bonded list
+    int adj_ok;                 // geometric rule: parameter gradients available
     double xpcent[3], xwcent[3];
     double rexcl_o2;
     // FP32 copies are stored relative to xpcent, which bounds their magnitude
@@ -85,6 +99,7 @@ struct QQEntry {   // static Q-Q / Q-bonded-P pair of one state
     int i, j, s, soft;      // atom indices (not Q indices), state, exp-repulsion flag
     double A, B, el, sc;
 };
+
 
 // Per-context device state of the lists, coordinates and accumulators.
 struct DevState {
@@ -111,6 +126,7 @@ struct DevState {
     int* row_wg; int* cnt_wg; int cap_wg;   // water -> solute groups
     double* x_build;                        // coordinates of the last list build
     QQEntry* qq; int nqq;          // static qq + qqp entries (all states)
+    double* adj;                   // [3][nqat*S] dE_s/dqcrg, dE_s/dqA, dE_s/dqB of this window
     int nqq_qq;                    // first nqq_qq entries are Q-Q (EQ%qq), rest Q-P (EQ%qp)
     // water polarisation
     double* theta;       // [nwat]
@@ -172,6 +188,8 @@ struct SolventDev {
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv);
 int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int mixed);
+
+void launch_q_adjoint(const Launch& L, int mixed);
 
 void launch_export_pairs(const Launch& L, int win, int kind, int32_t* di, int32_t* dj, int64_t cap,
                          int* dcount);

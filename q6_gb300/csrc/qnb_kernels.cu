@@ -987,6 +987,115 @@ __global__ void __launch_bounds__(kQBlock) k_qenv(DevModel m, const DevState* __
     flush_q_grad<MIX>(m, s, gqf, gqd);
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of the Q-atom energies with respect to the Q parameters: for every
+// Q atom iq and state s, dE_s/dqcrg(iq,s), dE_s/dqA(iq,s) and dE_s/dqB(iq,s),
+// where qA/qB are the Q atom's code-1 LJ factors (A_pair = qA * a_j,
+// B_pair = qB * b_j, geometric rule).  The pair terms are recomputed from the
+// lists: E_s = sum el/r + A/(r^6+alpha)^2 - B/(r^6+alpha) (nbe_qx,
+// src/nonbonded.f90:200-222), so
+//   dE/dqcrg += c_j / r,  dE/dqA += a_j / (r^6+alpha)^2,  dE/dqB -= b_j / (r^6+alpha).
+// One warp per environment unit, lane = Q atom, sums in FP64 registers.
+// ---------------------------------------------------------------------------
+template <bool MIX, bool SPC, bool WATER, int SMAX>
+__global__ void __launch_bounds__(kQBlock) k_qadj_env(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
+    double aq[2][SMAX] = {}, aa[2][SMAX] = {}, ab[2][SMAX] = {};
+    int lane = threadIdx.x & 31;
+    int n = WATER ? min((int64_t)s.cnt[C_QW], s.cap_qw) : min((int64_t)s.cnt[C_QP], s.cap_qp);
+    const int S = m.S, na = WATER ? m.sa : 1;
+    for (int p = warp_id_global(); p < n; p += warps_total()) {
+        int j0 = WATER ? m.nat_solute + m.sa * s.qw[p] : s.qp[p];
+        for (int a = 0; a < na; ++a) {
+            int j = j0 + a;
+            bool lj = !WATER || !SPC || a == 0;
+#pragma unroll
+            for (int k = 0; k < kMaxQ / 32; ++k) {
+                int iq = k * 32 + lane;
+                if (iq >= m.nqat) break;
+                int i = m.iqseq[iq];
+                double r, r6;
+                if constexpr (MIX) {
+                    float4 xi = s.xq[i], xj = s.xq[j];
+                    float tx = xj.x - xi.x, ty = xj.y - xi.y, tz = xj.z - xi.z;
+                    float d2 = tx * tx + ty * ty + tz * tz;
+                    r = (double)rsqrtf(d2);
+                    r6 = (double)(d2 * d2 * d2);
+                } else {
+                    double tx = s.x[3 * j] - s.x[3 * i], ty = s.x[3 * j + 1] - s.x[3 * i + 1],
+                           tz = s.x[3 * j + 2] - s.x[3 * i + 2];
+                    double d2 = tx * tx + ty * ty + tz * tz;
+                    r = 1.0 / sqrt(d2);
+                    r6 = d2 * d2 * d2;
+                }
+                size_t t0 = WATER ? (size_t)(iq * m.sa + a) * S : ((size_t)j * m.nqat + iq) * S;
+                const double4_16a* F = (WATER ? m.qw_adj : m.qp_adj) + t0;
+                const QPar* P = (WATER ? m.qw_tab : m.qp_tab) + t0;
+#pragma unroll
+                for (int st = 0; st < SMAX; ++st) {
+                    if (st >= S) break;
+                    double4_16a f = F[st];
+                    aq[k][st] += f.x * r;
+                    if (lj) {
+                        double u = 1.0 / (r6 + P[st].sc);
+                        aa[k][st] += f.y * u * u;
+                        ab[k][st] -= f.z * u;
+                    }
+                }
+            }
+        }
+    }
+    // block sums in shared memory, one atomic per value and block
+    __shared__ double red[3 * kMaxQ * kMaxStates];
+    for (int k = threadIdx.x; k < 3 * m.nqat * S; k += blockDim.x) red[k] = 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kMaxQ / 32; ++k) {
+        int iq = k * 32 + lane;
+        if (iq >= m.nqat) break;
+#pragma unroll
+        for (int st = 0; st < SMAX; ++st) {
+            if (st >= S) break;
+            int o = iq + m.nqat * st;
+            atomicAdd(&red[o], aq[k][st]);
+            atomicAdd(&red[m.nqat * S + o], aa[k][st]);
+            atomicAdd(&red[2 * m.nqat * S + o], ab[k][st]);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * m.nqat * S; k += blockDim.x)
+        if (red[k] != 0.0) atomicAdd(s.adj + k, red[k]);
+}
+
+// static Q-Q and Q-bonded pairs (nbqq / nbqqp lists)
+__global__ void k_qadj_qq(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= s.nqq) return;
+    QQEntry e = s.qq[p];
+    QQAdj f = m.qq_adj[p];
+    double tx = s.x[3 * e.j] - s.x[3 * e.i], ty = s.x[3 * e.j + 1] - s.x[3 * e.i + 1],
+           tz = s.x[3 * e.j + 2] - s.x[3 * e.i + 2];
+    double d2 = tx * tx + ty * ty + tz * tz;
+    double r = 1.0 / sqrt(d2), r6 = d2 * d2 * d2;
+    double u = 1.0 / (r6 + e.sc);
+    int nqs = m.nqat * m.S;
+    int oi = f.iq + m.nqat * f.s;
+    atomicAdd(s.adj + oi, f.ci * r);
+    if (!e.soft) {
+        atomicAdd(s.adj + nqs + oi, f.ai * u * u);
+        atomicAdd(s.adj + 2 * nqs + oi, -f.bi * u);
+    }
+    if (f.jq >= 0) {
+        int oj = f.jq + m.nqat * f.s;
+        atomicAdd(s.adj + oj, f.cj * r);
+        if (!e.soft) {
+            atomicAdd(s.adj + nqs + oj, f.aj * u * u);
+            atomicAdd(s.adj + 2 * nqs + oj, -f.bj * u);
+        }
+    }
+}
+
 // nonbond_qq + nonbond_qqp (static lists), src/nonbondene.f90:5013-5153,
 // pair kernel nbe_qq, src/nonbonded.f90:111-150.  Always FP64: few pairs.
 template <bool MIX>
@@ -1877,6 +1986,26 @@ int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int m
         ++nl;
     }
     return nl;
+}
+
+void launch_q_adjoint(const Launch& L, int mixed) {
+    if (L.m.nqat == 0) return;
+    bool spc = L.m.spc != 0, s4 = L.m.S <= 4;
+#define QA(MIX, SPC, W, SM) k_qadj_env<MIX, SPC, W, SM><<<g, kQBlock, 0, L.st>>>(L.m, L.ds)
+    if (L.m.nwat > 0) {
+        dim3 g = grid_for(L.s0.cap_qw * 32, kQBlock, 8, L.nwin);
+        if (mixed) { if (spc) { if (s4) QA(true, true, true, 4); else QA(true, true, true, kMaxStates); }
+                     else { if (s4) QA(true, false, true, 4); else QA(true, false, true, kMaxStates); } }
+        else { if (spc) { if (s4) QA(false, true, true, 4); else QA(false, true, true, kMaxStates); }
+               else { if (s4) QA(false, false, true, 4); else QA(false, false, true, kMaxStates); } }
+    }
+    if (L.m.nat_solute > 0) {
+        dim3 g = grid_for(L.s0.cap_qp * 32, kQBlock, 8, L.nwin);
+        if (mixed) { if (s4) QA(true, true, false, 4); else QA(true, true, false, kMaxStates); }
+        else { if (s4) QA(false, true, false, 4); else QA(false, true, false, kMaxStates); }
+    }
+#undef QA
+    if (L.s0.nqq > 0) k_qadj_qq<<<dim3((L.s0.nqq + 63) / 64, L.nwin), 64, 0, L.st>>>(L.m, L.ds);
 }
 
 void launch_export_pairs(const Launch& L, int win, int kind, int32_t* di, int32_t* dj, int64_t cap, int* dcount) {

@@ -36,7 +36,7 @@ EXPORTED = (
     "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_take_launch_count",
     "qnb_profile", "qnb_kernel_times", "qnb_create_batch", "qnb_window_count",
     "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
-    "qnb_ww_spc_noalloc",
+    "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev",
 )
 KERNEL_CLASSES = ("ww", "qw", "pw", "pp", "qp", "lrf_taylor", "qq", "restrain", "watpol", "pack",
                   "apply", "build", "lrf_build")
@@ -81,6 +81,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_set_lambda_window": [P, I32, P], "qnb_upload_coordinates": [P, P],
         "qnb_download_gradient": [P, P, I32],
         "qnb_ww_spc_noalloc": [P, P, I32, I32, D, D, D, D, D, P, P, P],
+        "qnb_q_adjoint_dev": [P, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -237,6 +238,14 @@ class NonbondedEngine:
         R = np.zeros((W, 2))
         self._check(self.lib.qnb_compute_dev(self.h, Tfree, int(istep), int(sync), _p(E), _p(EQ), _p(R)))
         return [dict(zip(E_FIELDS, e)) for e in E], EQ[:, : self.S], R
+
+    def q_adjoint_dev(self):
+        """dE_s/dqcrg, dE_s/dqA, dE_s/dqB per window: arrays [nwin][nqat][nstates]."""
+        n = self.nwin * self.s.nqat * self.S
+        dq, dA, dB = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._check(self.lib.qnb_q_adjoint_dev(self.h, _p(dq), _p(dA), _p(dB)))
+        shp = (self.nwin, self.S, self.s.nqat)
+        return tuple(a.reshape(shp).transpose(0, 2, 1).copy() for a in (dq, dA, dB))
 
     def set_coordinates_dev(self, x_all):
         """Copies coordinates of all windows (nwin x natom x 3) into HBM."""
