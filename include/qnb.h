@@ -89,8 +89,8 @@ typedef struct qnb_topology {
     const int32_t* cgp_last;    /* [ncgp] last slot in cgpatom (inclusive)    */
     const int32_t* cgp_iswitch; /* [ncgp] switch atom                         */
     const int32_t* cgpatom;     /* [cgp_last[ncgp-1]+1] atom indices          */
-    int32_t iuse_switch_atom;   /* 1: group cut-off by switch atoms (only
-                                   mode supported; 0 returns UNSUPPORTED)      */
+    int32_t iuse_switch_atom;   /* 1: group cut-off by switch atoms; 0: by
+                                   any atom pair (nbpplis2/nbpwlis2/nbqplis2) */
 
     /* solute exclusions (listex + listexlong) and 1-4 pairs (list14 +
        list14long) as unordered atom pairs; order inside a pair is free       */

@@ -63,6 +63,7 @@ typedef struct orc {
     int nel; int* elp; double* elv; int nqexp; int* qexp;
     double xpcent[3], xwcent[3], rexcl_o;
     int use_lrf;
+    int any_atom;       /* iuse_switch_atom == 0: the *lis2* group tests   */
     /* solvent (first molecule) parameters: chg_solv, aLJ_solv, bLJ_solv */
     double chg_solv[16], aLJ[16][3], bLJ[16][3];
     pre_t ww_pre[16][16];
@@ -306,6 +307,7 @@ orc* orc_create(const qnb_topology* t, int use_lrf) {
     for (int k = 0; k < 3; ++k) { o->xpcent[k] = t->xpcent[k]; o->xwcent[k] = t->xwcent[k]; }
     o->rexcl_o = t->rexcl_o;
     o->use_lrf = use_lrf;
+    o->any_atom = t->iuse_switch_atom == 0;
     for (int s = 0; s < o->S; ++s) o->lambda[s] = 1.0;
 
     /* solvent parameters from the first solvent molecule, src/simprep.f90:3616-3621 */
@@ -532,7 +534,43 @@ static inline int parity_skip(int a, int b) {
     return (a > b && ((a + b) % 2) == 0) || (a < b && ((a + b) % 2) == 1);
 }
 
-/* nbpplist(_lrf), src/nonbondene.f90:1520-1639, 1777-1908 */
+/* Group-pair cut-off test.  Switch-atom mode (nbpplist_lrf,
+   src/nonbondene.f90:1861): r2 of the two switch atoms.  Any-atom mode
+   (nbpplis2_lrf, src/nonbondene.f90:1451-1468): inside as soon as one atom
+   pair (all atoms, Q and excluded ones too) is within the cut-off; r2 is then
+   the last pair examined, which for an outside pair is (last atom of ig, last
+   atom of jg) -- the value the reference's LRF test reads. */
+static int pp_inside(const orc* o, const double* x, int ig, int jg, double rcut2, double* r2) {
+    if (!o->any_atom) {
+        *r2 = qdist4(X(x, o->csw[ig]), X(x, o->csw[jg]));
+        return *r2 <= rcut2;
+    }
+    *r2 = 1.0;
+    for (int ia = o->cfirst[ig]; ia <= o->clast[ig]; ++ia)
+        for (int jb = o->cfirst[jg]; jb <= o->clast[jg]; ++jb) {
+            *r2 = qdist4(X(x, o->cgpatom[ia]), X(x, o->cgpatom[jb]));
+            if (*r2 <= rcut2) return 1;
+        }
+    return 0;
+}
+
+/* Solute group to water (first atom ja) test: switch atom (nbpwlist_lrf,
+   src/nonbondene.f90:2915) or any atom of the group (nbpwlis2_lrf,
+   src/nonbondene.f90:2565-2577, r2 of the last atom when outside). */
+static int pw_inside(const orc* o, const double* x, int ig, int ja, double rcut2, double* r2) {
+    if (!o->any_atom) {
+        *r2 = qdist4(X(x, o->csw[ig]), X(x, ja));
+        return *r2 <= rcut2;
+    }
+    *r2 = 1.0;
+    for (int ia = o->cfirst[ig]; ia <= o->clast[ig]; ++ia) {
+        *r2 = qdist4(X(x, o->cgpatom[ia]), X(x, ja));
+        if (*r2 <= rcut2) return 1;
+    }
+    return 0;
+}
+
+/* nbpplist(_lrf), src/nonbondene.f90:1520-1639, 1777-1908; nbpplis2(_lrf) 950-1086, 1369-1516 */
 static void nbpplist(orc* o, const double* x, double rcut2, double rlrf2) {
     o->nbpp.n = 0; o->nbpp14.n = 0;
     for (int ig = 0; ig < o->ncgp_solute; ++ig) {
@@ -542,8 +580,8 @@ static void nbpplist(orc* o, const double* x, double rcut2, double rlrf2) {
             if (parity_skip(ig, jg)) continue;
             int ja = o->csw[jg];
             if (o->excl[ja]) continue;
-            double r2 = qdist4(X(x, is), X(x, ja));
-            if (r2 <= rcut2) {
+            double r2;
+            if (pp_inside(o, x, ig, jg, rcut2, &r2)) {
                 for (int ia = o->cfirst[ig]; ia <= o->clast[ig]; ++ia) {
                     int i = o->cgpatom[ia];
                     if (o->iqatom[i] != 0) continue;
@@ -568,7 +606,7 @@ static void nbpplist(orc* o, const double* x, double rcut2, double rlrf2) {
     }
 }
 
-/* nbpwlist(_lrf), src/nonbondene.f90:2622-2725, 2842-2955 */
+/* nbpwlist(_lrf), src/nonbondene.f90:2622-2725, 2842-2955; nbpwlis2(_lrf) 2137-2242, 2493-2618 */
 static void nbpwlist(orc* o, const double* x, double rcut2, double rlrf2) {
     o->nbpw.n = 0;
     for (int ig = 0; ig < o->ncgp_solute; ++ig) {
@@ -578,8 +616,8 @@ static void nbpwlist(orc* o, const double* x, double rcut2, double rlrf2) {
             int ja = o->nat_solute + o->solv_atom * jw;
             int jg = o->iwhich[ja];
             if (o->excl[ja]) continue;
-            double r2 = qdist4(X(x, is), X(x, ja));
-            if (r2 <= rcut2) {
+            double r2;
+            if (pw_inside(o, x, ig, ja, rcut2, &r2)) {
                 for (int ia = o->cfirst[ig]; ia <= o->clast[ig]; ++ia) {
                     int i = o->cgpatom[ia];
                     if (o->iqatom[i] != 0) continue;
@@ -627,7 +665,7 @@ static void nbwwlist(orc* o, const double* x, double rcut2, double rlrf2) {
     }
 }
 
-/* nbqplist, src/nonbondene.f90:3647-3742 */
+/* nbqplist, src/nonbondene.f90:3647-3742; nbqplis2 3408-3519 */
 static void nbqplist(orc* o, const double* x, double rcq2) {
     if (o->qp_done && rcq2 > o->rexcl_o * o->rexcl_o) return;
     if (o->nqat == 0) return;
@@ -636,8 +674,14 @@ static void nbqplist(orc* o, const double* x, double rcq2) {
     for (int ig = 0; ig < o->ncgp_solute; ++ig) {
         int ia = o->csw[ig];
         if (o->excl[ia]) continue;
-        double r2 = qdist4(X(x, ia), xp);
-        if (r2 > rcq2) continue;
+        int inside = 0;
+        if (o->any_atom) {   /* nbqplis2, src/nonbondene.f90:3477-3487 */
+            for (int a = o->cfirst[ig]; a <= o->clast[ig] && !inside; ++a)
+                inside = qdist4(X(x, o->cgpatom[a]), xp) <= rcq2;
+        } else {
+            inside = qdist4(X(x, ia), xp) <= rcq2;
+        }
+        if (!inside) continue;
         for (int a = o->cfirst[ig]; a <= o->clast[ig]; ++a) {
             int i = o->cgpatom[a];
             if (any_qconn_le3(o, i)) continue;

@@ -222,6 +222,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     m.S = S;
     m.el14 = t->el14_scale;
     m.use_lrf = c->use_lrf;
+    m.any_atom = t->iuse_switch_atom == 0;   // nbpplis2/nbpwlis2/nbqplis2 group tests
     m.spc = (t->ivdw_rule == 1 && t->solvent_type == 0) ? 1 : 0;   // src/potene.f90:347-349
     for (int k = 0; k < 3; ++k) {
         m.xpcent[k] = t->xpcent[k];
@@ -332,6 +333,8 @@ int build_model(qnb_context* c, const qnb_topology* t) {
         for (int a = gslot[g]; a < gslot[g + 1]; ++a) slot_of[gatom[a]] = a - gslot[g];
         c->maxg = std::max(c->maxg, gslot[g + 1] - gslot[g]);
     }
+    // must agree with k_rows_solute's template choice (MAXG <= 8)
+    m.type_in_entry = (c->maxg <= 8 && t->natyps <= 0xffff) ? 1 : 0;
     struct SG {
         long long key;
         int ent;
@@ -422,6 +425,15 @@ int build_model(qnb_context* c, const qnb_topology* t) {
             }
     }
     TRY(c->upload(&c->d_heavy_solv, heavy_solv));
+    // solvent atoms without LJ against every type (SPC hydrogens): their
+    // solute pairs reduce to the Coulomb term exactly
+    m.wlj_mask = 0;
+    if (t->nwat > 0)
+        for (int a = 0; a < sa; ++a)
+            for (int b = 0; b < nt; ++b) {
+                float4 p = ljpair[(size_t)b * nt + m.wtype[a]];
+                if (p.x != 0.f || p.y != 0.f) m.wlj_mask |= 1u << a;
+            }
 
     // ---- Q atoms -------------------------------------------------------------
     auto QC = [&](int s, int i, int iq) { return (int)t->qconn[s + S * (i + ns * iq)]; };
@@ -1003,7 +1015,7 @@ int qnb_create_batch(const qnb_topology* t, const qnb_options* opt, int32_t nwin
     if (t->nstates < 0 || t->nstates > kMaxStates) return fail(QNB_ERR_UNSUPPORTED, "nstates %d > %d", t->nstates, kMaxStates);
     if (t->nqat > 64) return fail(QNB_ERR_UNSUPPORTED, "nqat %d > 64", t->nqat);
     if (t->nqat > 0 && t->nstates < 1) return fail(QNB_ERR_ARG, "Q atoms need nstates >= 1");
-    if (t->iuse_switch_atom != 1) return fail(QNB_ERR_UNSUPPORTED, "any-atom charge-group cut-off (switch atoms off)");
+    if (t->iuse_switch_atom != 0 && t->iuse_switch_atom != 1) return fail(QNB_ERR_ARG, "iuse_switch_atom must be 0 or 1");
     if (t->natom >= (1 << 28)) return fail(QNB_ERR_UNSUPPORTED, "natom >= 2^28");
     if (opt->precision != QNB_PREC_FP64 && opt->precision != QNB_PREC_MIXED) return fail(QNB_ERR_ARG, "precision");
     int ndev = 0;

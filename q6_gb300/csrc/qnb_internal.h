@@ -53,6 +53,8 @@ struct DevModel {
     int natom, nat_solute, nwat, sa, ncgp, ncgp_solute, natyps, nqat, S;
     int spc;           // SPC fast path for ww / qw (geometric rule + SPC solvent)
     int use_lrf;
+    int any_atom;      // 1: a group pair is inside when any atom pair is (switch atoms off)
+    int type_in_entry; // solute row entries carry the partner's LJ type (groups of <= 8 atoms)
     double el14;
     const int* iac;
     const double* crg;
@@ -75,6 +77,7 @@ struct DevModel {
     const uint8_t* ljcod;       // [natyps][natyps]
     const uint8_t* ljset;       // [3][natyps][natyps]: |A| or |B| > QREAL_EPS
     int wtype[kMaxSolv];        // solvent template (first molecule) atom types
+    unsigned wlj_mask;          // bit a: template atom a has LJ parameters with some solute type
     double wcrg[kMaxSolv];      // and charges
     float wcrgf[kMaxSolv];
     double wwA[kMaxSolv * kMaxSolv], wwB[kMaxSolv * kMaxSolv], wwE[kMaxSolv * kMaxSolv];  // ww_precomp

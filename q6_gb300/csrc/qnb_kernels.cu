@@ -115,6 +115,11 @@ __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
     return v;
 }
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+    return v;
+}
 __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
@@ -200,6 +205,48 @@ __device__ __forceinline__ bool within(float r2f, double rc2, const double* __re
     return dist2_exact(x[3 * a], x[3 * a + 1], x[3 * a + 2], x[3 * b], x[3 * b + 1], x[3 * b + 2]) <= rc2;
 }
 
+// Any-atom group tests (iuse_switch_atom = 0): nbpplis2(_lrf) and
+// nbpwlis2(_lrf), src/nonbondene.f90:1451-1468, 2565-2577.  A solute group
+// pair is inside when any of its atom pairs (Q and excluded atoms included)
+// is within the cut-off; a group and a water when any atom of the group is
+// within the cut-off of the water's first atom.
+__device__ __forceinline__ bool gg_inside_any(const DevModel& m, const double* __restrict__ x,
+                                              const float4* __restrict__ xq, int g1, int g2, double rc2) {
+    int b0 = m.gslot[g2], b1 = m.gslot[g2 + 1];
+    for (int a = m.gslot[g1]; a < m.gslot[g1 + 1]; ++a) {
+        int i = m.gatom[a];
+        float4 xi = xq[i];
+        for (int b = b0; b < b1; ++b) {
+            int j = m.gatom[b];
+            if (within(r2_f(xi, xq[j]), rc2, x, i, j)) return true;
+        }
+    }
+    return false;
+}
+__device__ __forceinline__ bool gw_inside_any(const DevModel& m, const double* __restrict__ x,
+                                              const float4* __restrict__ xq, int g, int o, double rc2) {
+    float4 xo = xq[o];
+    for (int a = m.gslot[g]; a < m.gslot[g + 1]; ++a) {
+        int i = m.gatom[a];
+        if (within(r2_f(xq[i], xo), rc2, x, i, o)) return true;
+    }
+    return false;
+}
+// solute group pair g1 != g2 inside the cut-off, in either mode
+__device__ __forceinline__ bool gg_inside(const DevModel& m, const double* __restrict__ x,
+                                          const float4* __restrict__ xq, int g1, int g2, double rc2) {
+    if (m.any_atom) return gg_inside_any(m, x, xq, g1, g2, rc2);
+    int s1 = m.gsw[g1], s2 = m.gsw[g2];
+    return within(r2_f(xq[s1], xq[s2]), rc2, x, s1, s2);
+}
+// solute group g and the water whose first atom is o, in either mode
+__device__ __forceinline__ bool gw_inside(const DevModel& m, const double* __restrict__ x,
+                                          const float4* __restrict__ xq, int g, int o, double rc2) {
+    if (m.any_atom) return gw_inside_any(m, x, xq, g, o, rc2);
+    int s = m.gsw[g];
+    return within(r2_f(xq[s], xq[o]), rc2, x, s, o);
+}
+
 // nbwwlist(_lrf) pair selection, src/nonbondene.f90:4274-4395: water pairs
 // with O-O r2 <= Rcww2, neither O excluded.  Each unordered pair is kept once
 // (iw < jw), the same set as the reference's parity rule.  A warp owns rows
@@ -235,7 +282,8 @@ __global__ void k_build_ww(DevModel m, const DevState* __restrict__ states, doub
 }
 
 // nbpwlist(_lrf), src/nonbondene.f90:2842-2955: solute group switch atom to
-// water O within Rcpw; every non-Q atom of the group pairs with the molecule.
+// water O within Rcpw (nbpwlis2(_lrf), 2137-2242, 2493-2618: any atom of the
+// group); every non-Q atom of the group pairs with the molecule.
 __global__ void k_build_pw(DevModel m, const DevState* __restrict__ states, double rc2) {
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
@@ -251,13 +299,12 @@ __global__ void k_build_pw(DevModel m, const DevState* __restrict__ states, doub
         int nq = 0;
         for (int a = a0; a < a1; ++a) nq += (m.iqatom[m.gatom[a]] < 0);
         if (nq == 0) continue;
-        float4 xi = xq[is];
         for (int j0 = 0; j0 < m.nwat; j0 += kWarp) {
             int jw = j0 + lane;
             bool ok = false;
             if (jw < m.nwat) {
                 int jo = m.nat_solute + m.sa * jw;
-                if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), rc2, x, is, jo);
+                if (!m.excl[jo]) ok = gw_inside(m, x, xq, ig, jo, rc2);
             }
             int pos = warp_append(cnt, ok ? nq : 0);
             if (ok) {
@@ -307,7 +354,8 @@ __device__ __forceinline__ int pp_accept(const DevModel& m, int i, int j, int ki
 }
 
 // nbpplist(_lrf) group selection, src/nonbondene.f90:1777-1908: solute group
-// pairs whose switch atoms are within Rcpp (g1 <= g2; a group with itself is
+// pairs whose switch atoms are within Rcpp, or any atom pairs for
+// nbpplis2(_lrf), 950-1086, 1369-1516 (g1 <= g2; a group with itself is
 // always listed).  Rows are paired like k_build_ww for balance.
 __global__ void k_build_pp_groups(DevModel m, const DevState* __restrict__ states, double rc2) {
     const DevState& s = states[blockIdx.y];
@@ -324,13 +372,12 @@ __global__ void k_build_pp_groups(DevModel m, const DevState* __restrict__ state
             if (pass == 1 && g1 == w) break;
             int s1 = m.gsw[g1];
             if (m.excl[s1]) continue;
-            float4 x1 = xq[s1];
             for (int j0 = g1; j0 < G; j0 += kWarp) {
                 int g2 = j0 + lane;
                 bool ok = false;
                 if (g2 < G) {
                     int s2 = m.gsw[g2];
-                    if (!m.excl[s2]) ok = (g2 == g1) || within(r2_f(x1, xq[s2]), rc2, x, s1, s2);
+                    if (!m.excl[s2]) ok = (g2 == g1) || gg_inside(m, x, xq, g1, g2, rc2);
                 }
                 int pos = warp_append(cnt, ok ? 1 : 0);
                 if (ok && pos < cap) out[pos] = make_int2(g1, g2);
@@ -401,8 +448,16 @@ __global__ void k_build_qp(DevModel m, const DevState* __restrict__ states, cons
     if (ig >= m.ncgp_solute) return;
     int is = m.gsw[ig];
     if (m.excl[is]) return;
-    double r2 = dist2_exact(x[3 * is], x[3 * is + 1], x[3 * is + 2], m.xpcent[0], m.xpcent[1], m.xpcent[2]);
-    if (r2 > rcq2) return;
+    bool inside = false;
+    if (m.any_atom) {   // nbqplis2, src/nonbondene.f90:3477-3487
+        for (int a = m.gslot[ig]; a < m.gslot[ig + 1] && !inside; ++a) {
+            int i = m.gatom[a];
+            inside = dist2_exact(x[3 * i], x[3 * i + 1], x[3 * i + 2], m.xpcent[0], m.xpcent[1], m.xpcent[2]) <= rcq2;
+        }
+    } else {
+        inside = dist2_exact(x[3 * is], x[3 * is + 1], x[3 * is + 2], m.xpcent[0], m.xpcent[1], m.xpcent[2]) <= rcq2;
+    }
+    if (!inside) return;
     for (int a = m.gslot[ig]; a < m.gslot[ig + 1]; ++a) {
         int i = m.gatom[a];
         if (qnear[i]) continue;
@@ -577,6 +632,75 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const DevSta
                 lrf_terms<float>(xi.x - cxf, xi.y - cyf, xi.z - czf, xi.w, mom);
             } else {
                 lrf_terms<double>(x[3 * i] - cx, x[3 * i + 1] - cy, x[3 * i + 2] - cz, m.crg[i], mom);
+            }
+        }
+        double tot[kLrfMom];
+#pragma unroll
+        for (int k = 0; k < kLrfMom; ++k) {
+            T v = mom[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+            tot[k] = (double)v;
+        }
+        if (lane == 0) lrf_expand(tot, L + 3);
+    }
+}
+
+// Any-atom mode (nbpplis2_lrf / nbpwlis2_lrf, src/nonbondene.f90:1369-1516,
+// 2493-2618): a pair of groups that involves a solute group is "LRF" when no
+// atom pair is inside the cut-off and the r2 of the last atom pair examined,
+// (last atom of one group, last atom of the other; a water's first atom), is
+// within RcLRF.  Water pairs keep the O-O test.  One warp per target group g2;
+// lanes stride over the source groups, so each group pair is classified once.
+__device__ __forceinline__ int group_last_atom(const DevModel& m, int g) {
+    return g < m.ncgp_solute ? m.gatom[m.gslot[g + 1] - 1] : m.nat_solute + m.sa * (g - m.ncgp_solute);
+}
+template <bool MIX>
+__global__ void __launch_bounds__(128) k_lrf_accumulate_any(DevModel m, const DevState* __restrict__ states, Cut c) {
+    typedef typename std::conditional<MIX, float, double>::type T;
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const float4* __restrict__ xq = s.xq;
+    double* __restrict__ lrf = s.lrf;
+    int lane = threadIdx.x & 31;
+    for (int g2 = warp_id_global(); g2 < m.ncgp; g2 += warps_total()) {
+        int s2 = group_dist_atom(m, g2);
+        if (m.excl[s2]) continue;
+        bool sol2 = g2 < m.ncgp_solute;
+        int l2 = group_last_atom(m, g2);
+        double* L = lrf + (size_t)g2 * kLrfLen;
+        double cx = L[0], cy = L[1], cz = L[2];
+        float cxf = (float)(cx - m.xpcent[0]), cyf = (float)(cy - m.xpcent[1]), czf = (float)(cz - m.xpcent[2]);
+        T mom[kLrfMom];
+#pragma unroll
+        for (int k = 0; k < kLrfMom; ++k) mom[k] = T(0);
+        for (int g1 = lane; g1 < m.ncgp; g1 += kWarp) {
+            if (g1 == g2) continue;
+            int s1 = group_dist_atom(m, g1);
+            if (m.excl[s1]) continue;
+            bool sol1 = g1 < m.ncgp_solute;
+            bool far;
+            if (sol1 && sol2) {
+                far = !gg_inside_any(m, x, xq, g1, g2, c.rcpp2);
+            } else if (sol1 || sol2) {
+                far = !gw_inside_any(m, x, xq, sol1 ? g1 : g2, sol1 ? s2 : s1, c.rcpw2);
+            } else {
+                far = lrf_pair(r2_f(xq[s2], xq[s1]), c.rcww2, c.rlrf2, x, s2, s1);
+            }
+            if (far && (sol1 || sol2)) {
+                int l1 = group_last_atom(m, g1);
+                far = within(r2_f(xq[l1], xq[l2]), c.rlrf2, x, l1, l2);
+            }
+            if (!far) continue;
+            for (int a = m.gslot[g1]; a < m.gslot[g1 + 1]; ++a) {
+                int i = m.gatom[a];
+                if (m.iqatom[i] >= 0) continue;
+                if constexpr (MIX) {
+                    float4 xi = xq[i];
+                    lrf_terms<float>(xi.x - cxf, xi.y - cyf, xi.z - czf, xi.w, mom);
+                } else {
+                    lrf_terms<double>(x[3 * i] - cx, x[3 * i + 1] - cy, x[3 * i + 2] - cz, m.crg[i], mom);
+                }
             }
         }
         double tot[kLrfMom];
@@ -1481,7 +1605,6 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
             int g = r, is = m.gsw[g];
             int npp = 0, npw = 0;
             if (!m.excl[is]) {
-                float4 xi = xq[is];
                 int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
                 uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
                 for (int j0 = 0; j0 < m.ncgp_solute; j0 += kWarp) {
@@ -1490,7 +1613,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                     int b0 = 0, n2 = 0, nq = 0;
                     if (g2 < m.ncgp_solute) {
                         int s2 = m.gsw[g2];
-                        if (!m.excl[s2]) ok = (g2 == g) || within(r2_f(xi, xq[s2]), c.rcpp2, x, is, s2);
+                        if (!m.excl[s2]) ok = (g2 == g) || gg_inside(m, x, xq, g, g2, c.rcpp2);
                         if (ok) {
                             b0 = m.gslot[g2];
                             n2 = m.gslot[g2 + 1] - b0;
@@ -1525,6 +1648,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                                 }
                                 mask |= (unsigned)kind << (2 * a);
                             }
+                            if (m.type_in_entry) mask |= (unsigned)m.iac[j] << 16;
                             if (pos < s.cap_gp) rp[pos] = make_uint2((unsigned)j | (flags << 28), mask);
                             ++pos;
                         }
@@ -1537,7 +1661,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                     bool ok = false;
                     if (jw < m.nwat) {
                         int jo = m.nat_solute + m.sa * jw;
-                        if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), c.rcpw2, x, is, jo);
+                        if (!m.excl[jo]) ok = gw_inside(m, x, xq, g, jo, c.rcpw2);
                     }
                     npw = row_append(rw, s.cap_gw, npw, ok, jw);
                 }
@@ -1569,8 +1693,8 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                     bool ok = false;
                     if (g < m.ncgp_solute) {
                         int s2 = m.gsw[g];
-                        // the same test as from the group side: r2(switch atom, O)
-                        if (!m.excl[s2]) ok = within(r2_f(xq[s2], xi), c.rcpw2, x, s2, io);
+                        // the same test as from the group side
+                        if (!m.excl[s2]) ok = gw_inside(m, x, xq, g, io, c.rcpw2);
                     }
                     nwg = row_append(rg, s.cap_wg, nwg, ok, g);
                 }
@@ -1613,10 +1737,26 @@ __device__ __forceinline__ TypeTab stage_types(const DevModel& m, float4* sh) {
 }
 
 // solute group rows: pp (partner atoms with exclusion / 1-4 kinds) and pw
-// (partner waters): gradient of the group's own atoms
+// (partner waters): gradient of the group's own atoms.  Every solute pair sits
+// in the rows of both of its atoms (a pair inside one group twice in that
+// group's row) and both evaluations give the same FP32 energy, so the row sums
+// of all pp energies are halved instead of testing which side counts a pair.
+// Groups of at most 8 atoms carry the partner's LJ type in entry bits 16..31.
+//
+// Resident 128-thread blocks per SM asked of the register allocator: the
+// kernel waits mostly on its gathers, so occupancy pays more than the few
+// spilled registers (6 blocks = 80 registers for groups of up to 6 atoms).
+#ifndef QNB_ROWS_MIN_BLOCKS
+#define QNB_ROWS_MIN_BLOCKS 0   // 0: the per-size default below
+#endif
 template <int MAXG>
-__global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState* __restrict__ states) {
+constexpr int rows_min_blocks() {
+    return QNB_ROWS_MIN_BLOCKS ? QNB_ROWS_MIN_BLOCKS : (MAXG <= 6 ? 6 : (MAXG <= 8 ? 4 : 1));
+}
+template <int MAXG>
+__global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(DevModel m, const DevState* __restrict__ states) {
     __shared__ float4 sh_lj[kMaxTypesShared * kMaxTypesShared];
+    constexpr bool kTypeInEntry = MAXG <= 8;
     const DevState& s = states[blockIdx.y];
     TypeTab lj = stage_types(m, sh_lj);
     Acc<true> acc = make_acc<true>(s);
@@ -1628,7 +1768,7 @@ __global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState*
         int npp = s.cnt_gp[g], npw = s.cnt_gw[g];
         if (npp == 0 && npw == 0) continue;
         int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
-        int ia[MAXG], ta[MAXG];
+        int ta[MAXG];
         float4 xa[MAXG];
         bool qa[MAXG];
         float f[MAXG][3];
@@ -1636,12 +1776,11 @@ __global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState*
         for (int a = 0; a < MAXG; ++a) {
             f[a][0] = f[a][1] = f[a][2] = 0.f;
             if (a < n1) {
-                ia[a] = m.gatom[a0 + a];
-                ta[a] = m.iac[ia[a]];
-                xa[a] = xq[ia[a]];
-                qa[a] = m.iqatom[ia[a]] >= 0;
+                int i = m.gatom[a0 + a];
+                ta[a] = m.iac[i];
+                xa[a] = xq[i];
+                qa[a] = m.iqatom[i] >= 0;
             } else {
-                ia[a] = 0x7fffffff;
                 ta[a] = 0;
                 xa[a] = make_float4(0, 0, 0, 0);
                 qa[a] = true;
@@ -1655,10 +1794,8 @@ __global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState*
         for (int k = lane; k < npp; k += kWarp) {
             uint2 e = rp[k];
             int j = (int)(e.x & 0x0fffffffu);
-            bool lowerg = (e.x >> 28) & 1u, sameg = (e.x >> 29) & 1u;
             float4 xb = xq[j];
-            int tj = m.iac[j];
-            float pel = 0.f, pvdw = 0.f;   // this entry's energies, converted once
+            int tj = kTypeInEntry ? (int)(e.y >> 16) : m.iac[j];
 #pragma unroll
             for (int a = 0; a < MAXG; ++a) {
                 if (qa[a]) continue;
@@ -1671,48 +1808,52 @@ __global__ void __launch_bounds__(128) k_rows_solute(DevModel m, const DevState*
                 if (is14) el *= el14;
                 float vel, vdw;
                 pair_f(xa[a], xb, A, B, el, true, f[a][0], f[a][1], f[a][2], vel, vdw);
-                if (lowerg || (sameg && ia[a] < j)) {   // each pair's energy once
-                    pel += vel;
-                    pvdw += vdw;
-                }
+                rpel += vel;
+                rpvdw += vdw;
             }
-            rpel += pel;
-            rpvdw += pvdw;
         }
         // ---- water partners (nonbond_pw, src/nonbondene.f90:4856-4916); energy counted here
         const int* rw = s.row_gw + (size_t)g * s.cap_gw;
         for (int k = lane; k < npw; k += kWarp) {
             int j0 = m.nat_solute + m.sa * rw[k];
-            float pel = 0.f, pvdw = 0.f;
             for (int b = 0; b < m.sa; ++b) {
                 float4 xb = xq[j0 + b];
                 int tw = m.wtype[b];
+                if ((m.wlj_mask >> b) & 1u) {
 #pragma unroll
-                for (int a = 0; a < MAXG; ++a) {
-                    if (qa[a]) continue;
-                    float4 p = lj(ta[a], tw);
-                    float vel, vdw;
-                    pair_f(xa[a], xb, p.x, p.y, xa[a].w * m.wcrgf[b], true, f[a][0], f[a][1], f[a][2], vel, vdw);
-                    pel += vel;
-                    pvdw += vdw;
+                    for (int a = 0; a < MAXG; ++a) {
+                        if (qa[a]) continue;
+                        float4 p = lj(ta[a], tw);
+                        float vel, vdw;
+                        pair_f(xa[a], xb, p.x, p.y, xa[a].w * m.wcrgf[b], true, f[a][0], f[a][1], f[a][2], vel, vdw);
+                        rwel += vel;
+                        rwvdw += vdw;
+                    }
+                } else {   // A = B = 0 with every solute type: the Coulomb term alone, bit for bit
+#pragma unroll
+                    for (int a = 0; a < MAXG; ++a) {
+                        if (qa[a]) continue;
+                        float vel, vdw;
+                        pair_f(xa[a], xb, 0.f, 0.f, xa[a].w * m.wcrgf[b], false, f[a][0], f[a][1], f[a][2], vel, vdw);
+                        rwel += vel;
+                    }
                 }
             }
-            rwel += pel;
-            rwvdw += pvdw;
         }
-        epel.add(rpel);
-        epvdw.add(rpvdw);
+        epel.add(0.5f * rpel);
+        epvdw.add(0.5f * rpvdw);
         ewel.add(rwel);
         ewvdw.add(rwvdw);
+        // gradient: FP32 warp sums in a fixed order, one conversion per atom
 #pragma unroll
         for (int a = 0; a < MAXG; ++a) {
             if (a >= n1) break;   // warp-uniform
-            unsigned long long v0 = warp_sum(to_fix(f[a][0])), v1 = warp_sum(to_fix(f[a][1])),
-                               v2 = warp_sum(to_fix(f[a][2]));
+            float v0 = warp_sum(f[a][0]), v1 = warp_sum(f[a][1]), v2 = warp_sum(f[a][2]);
             if (lane == 0 && !qa[a]) {
-                atomicAdd(s.fix + 3 * ia[a], v0);
-                atomicAdd(s.fix + 3 * ia[a] + 1, v1);
-                atomicAdd(s.fix + 3 * ia[a] + 2, v2);
+                int i = m.gatom[a0 + a];
+                atomicAdd(s.fix + 3 * i, to_fix(v0));
+                atomicAdd(s.fix + 3 * i + 1, to_fix(v1));
+                atomicAdd(s.fix + 3 * i + 2, to_fix(v2));
             }
         }
     }
@@ -1784,21 +1925,21 @@ __global__ void __launch_bounds__(128) k_rows_water(DevModel m, const DevState* 
 #pragma unroll
                 for (int a = 0; a < kMaxSolv; ++a) {
                     if (a >= sa) break;
-                    float4 p = lj(tj, m.wtype[a]);
+                    bool ljw = (m.wlj_mask >> a) & 1u;
+                    float4 p = ljw ? lj(tj, m.wtype[a]) : make_float4(0.f, 0.f, 0.f, 0.f);
                     float vel, vdw;
-                    pair_f(xa[a], xb, p.x, p.y, xb.w * m.wcrgf[a], true, f[a][0], f[a][1], f[a][2], vel, vdw);
+                    pair_f(xa[a], xb, p.x, p.y, xb.w * m.wcrgf[a], ljw, f[a][0], f[a][1], f[a][2], vel, vdw);
                 }
             }
         }
 #pragma unroll
         for (int a = 0; a < kMaxSolv; ++a) {
             if (a >= sa) break;
-            unsigned long long v0 = warp_sum(to_fix(f[a][0])), v1 = warp_sum(to_fix(f[a][1])),
-                               v2 = warp_sum(to_fix(f[a][2]));
+            float v0 = warp_sum(f[a][0]), v1 = warp_sum(f[a][1]), v2 = warp_sum(f[a][2]);
             if (lane == 0) {
-                atomicAdd(s.fix + 3 * (i0 + a), v0);
-                atomicAdd(s.fix + 3 * (i0 + a) + 1, v1);
-                atomicAdd(s.fix + 3 * (i0 + a) + 2, v2);
+                atomicAdd(s.fix + 3 * (i0 + a), to_fix(v0));
+                atomicAdd(s.fix + 3 * (i0 + a) + 1, to_fix(v1));
+                atomicAdd(s.fix + 3 * (i0 + a) + 2, to_fix(v2));
             }
         }
     }
@@ -1879,6 +2020,11 @@ void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2) {
 }
 void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src) {
     dim3 g = grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin);
+    if (L.m.any_atom) {
+        if (mixed) k_lrf_accumulate_any<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+        else k_lrf_accumulate_any<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+        return;
+    }
     if (mixed) k_lrf_accumulate<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
     else k_lrf_accumulate<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
 }
