@@ -704,6 +704,7 @@ int alloc_state(qnb_context* c) {
         TRY(c->alloc(&s.lrf, (size_t)std::max(1, m.ncgp) * kLrfLen));
         s.cnt = c->cnt_all + (size_t)C_NUM * w;
         TRY(c->alloc(&s.theta, (size_t)std::max(1, m.nwat)));
+        TRY(c->alloc(&s.wvec, (size_t)8 * std::max(1, m.nwat)));
         TRY(c->alloc(&s.shell, (size_t)std::max(1, m.nwat)));
         TRY(c->alloc(&s.rank, (size_t)std::max(1, m.nwat)));
         TRY(c->alloc(&s.n_insh, (size_t)kMaxShell));

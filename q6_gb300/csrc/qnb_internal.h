@@ -133,6 +133,7 @@ struct DevState {
     int nqq_qq;                    // first nqq_qq entries are Q-Q (EQ%qq), rest Q-P (EQ%qp)
     // water polarisation
     double* theta;       // [nwat]
+    double* wvec;        // [nwat][8] unit dipole / radial vectors and lengths of the last md call
     int* shell;          // [nwat] shell or -1
     int* rank;           // [nwat]
     int* n_insh;         // [kMaxShell]

@@ -197,12 +197,21 @@ __device__ __forceinline__ float r2_f(float4 a, float4 b) {
 // Exact cut-off decision r2 <= rc2.  The FP32 distance of centred
 // coordinates (|x| within the sphere, relative error far below 1e-5 of r2)
 // decides away from the boundary; within 2e-4 of it the FP64 distance in the
-// reference's operation order decides, so the outcome is the FP64 one.
-__device__ __forceinline__ bool within(float r2f, double rc2, const double* __restrict__ x, int a, int b) {
-    float c = (float)rc2;
-    if (r2f < c * 0.9998f) return true;
-    if (r2f > c * 1.0002f) return false;
-    return dist2_exact(x[3 * a], x[3 * a + 1], x[3 * a + 2], x[3 * b], x[3 * b + 1], x[3 * b + 2]) <= rc2;
+// reference's operation order decides, so the outcome is the FP64 one.  The
+// FP32 band is built once per kernel: a double-to-float conversion per test
+// would execute on the FP64 pipe.
+struct Band {
+    float lo, hi;   // r2f < lo: inside; r2f > hi: outside
+    double c;       // the FP64 threshold
+};
+__device__ __forceinline__ Band band(double c) {
+    float f = (float)c;
+    return Band{f * 0.9998f, f * 1.0002f, c};
+}
+__device__ __forceinline__ bool within(float r2f, const Band& rc, const double* __restrict__ x, int a, int b) {
+    if (r2f < rc.lo) return true;
+    if (r2f > rc.hi) return false;
+    return dist2_exact(x[3 * a], x[3 * a + 1], x[3 * a + 2], x[3 * b], x[3 * b + 1], x[3 * b + 2]) <= rc.c;
 }
 
 // Any-atom group tests (iuse_switch_atom = 0): nbpplis2(_lrf) and
@@ -211,7 +220,7 @@ __device__ __forceinline__ bool within(float r2f, double rc2, const double* __re
 // is within the cut-off; a group and a water when any atom of the group is
 // within the cut-off of the water's first atom.
 __device__ __forceinline__ bool gg_inside_any(const DevModel& m, const double* __restrict__ x,
-                                              const float4* __restrict__ xq, int g1, int g2, double rc2) {
+                                              const float4* __restrict__ xq, int g1, int g2, const Band& rc2) {
     int b0 = m.gslot[g2], b1 = m.gslot[g2 + 1];
     for (int a = m.gslot[g1]; a < m.gslot[g1 + 1]; ++a) {
         int i = m.gatom[a];
@@ -224,7 +233,7 @@ __device__ __forceinline__ bool gg_inside_any(const DevModel& m, const double* _
     return false;
 }
 __device__ __forceinline__ bool gw_inside_any(const DevModel& m, const double* __restrict__ x,
-                                              const float4* __restrict__ xq, int g, int o, double rc2) {
+                                              const float4* __restrict__ xq, int g, int o, const Band& rc2) {
     float4 xo = xq[o];
     for (int a = m.gslot[g]; a < m.gslot[g + 1]; ++a) {
         int i = m.gatom[a];
@@ -234,14 +243,14 @@ __device__ __forceinline__ bool gw_inside_any(const DevModel& m, const double* _
 }
 // solute group pair g1 != g2 inside the cut-off, in either mode
 __device__ __forceinline__ bool gg_inside(const DevModel& m, const double* __restrict__ x,
-                                          const float4* __restrict__ xq, int g1, int g2, double rc2) {
+                                          const float4* __restrict__ xq, int g1, int g2, const Band& rc2) {
     if (m.any_atom) return gg_inside_any(m, x, xq, g1, g2, rc2);
     int s1 = m.gsw[g1], s2 = m.gsw[g2];
     return within(r2_f(xq[s1], xq[s2]), rc2, x, s1, s2);
 }
 // solute group g and the water whose first atom is o, in either mode
 __device__ __forceinline__ bool gw_inside(const DevModel& m, const double* __restrict__ x,
-                                          const float4* __restrict__ xq, int g, int o, double rc2) {
+                                          const float4* __restrict__ xq, int g, int o, const Band& rc2) {
     if (m.any_atom) return gw_inside_any(m, x, xq, g, o, rc2);
     int s = m.gsw[g];
     return within(r2_f(xq[s], xq[o]), rc2, x, s, o);
@@ -251,7 +260,8 @@ __device__ __forceinline__ bool gw_inside(const DevModel& m, const double* __res
 // with O-O r2 <= Rcww2, neither O excluded.  Each unordered pair is kept once
 // (iw < jw), the same set as the reference's parity rule.  A warp owns rows
 // r and nwat-1-r so every warp scans about nwat candidates.
-__global__ void k_build_ww(DevModel m, const DevState* __restrict__ states, double rc2) {
+__global__ void k_build_ww(DevModel m, const DevState* __restrict__ states, double rc2d) {
+    const Band rc2 = band(rc2d);
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
     const float4* __restrict__ xq = s.xq;
@@ -284,7 +294,8 @@ __global__ void k_build_ww(DevModel m, const DevState* __restrict__ states, doub
 // nbpwlist(_lrf), src/nonbondene.f90:2842-2955: solute group switch atom to
 // water O within Rcpw (nbpwlis2(_lrf), 2137-2242, 2493-2618: any atom of the
 // group); every non-Q atom of the group pairs with the molecule.
-__global__ void k_build_pw(DevModel m, const DevState* __restrict__ states, double rc2) {
+__global__ void k_build_pw(DevModel m, const DevState* __restrict__ states, double rc2d) {
+    const Band rc2 = band(rc2d);
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
     const float4* __restrict__ xq = s.xq;
@@ -357,7 +368,8 @@ __device__ __forceinline__ int pp_accept(const DevModel& m, int i, int j, int ki
 // pairs whose switch atoms are within Rcpp, or any atom pairs for
 // nbpplis2(_lrf), 950-1086, 1369-1516 (g1 <= g2; a group with itself is
 // always listed).  Rows are paired like k_build_ww for balance.
-__global__ void k_build_pp_groups(DevModel m, const DevState* __restrict__ states, double rc2) {
+__global__ void k_build_pp_groups(DevModel m, const DevState* __restrict__ states, double rc2d) {
+    const Band rc2 = band(rc2d);
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
     const float4* __restrict__ xq = s.xq;
@@ -435,53 +447,99 @@ __global__ void k_expand_pp(DevModel m, const DevState* __restrict__ states) {
     }
 }
 
+// Exclusive prefix sum of v over the block (blockDim.x a multiple of 32, at
+// most 1024); *total receives the block sum.  Used for ordered appends.
+__device__ __forceinline__ int block_excl_scan(int v, int* total) {
+    __shared__ int wsum[32];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    __syncthreads();   // wsum reuse across calls
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < nw ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(kFull, w, o);
+            if (lane >= o) w += t;
+        }
+        if (lane < nw) wsum[lane] = w;   // inclusive over warps
+    }
+    __syncthreads();
+    *total = wsum[nw - 1];
+    return (warp ? wsum[warp - 1] : 0) + incl - v;
+}
+
 // nbqplist, src/nonbondene.f90:3647-3742: solute groups whose switch atom is
-// within Rcq of the solute centre; atoms not bonded/angled to any Q atom.
-__global__ void k_build_qp(DevModel m, const DevState* __restrict__ states, const uint8_t* __restrict__ qnear,
-                           double rcq2) {
+// within Rcq of the solute centre (nbqplis2, 3408-3519: any atom of the
+// group); atoms not bonded/angled to any Q atom.  One block per window
+// appends in group order, so the list order is deterministic.
+__global__ void __launch_bounds__(1024) k_build_qp(DevModel m, const DevState* __restrict__ states,
+                                                   const uint8_t* __restrict__ qnear, double rcq2) {
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
     int* __restrict__ out = s.qp;
-    int64_t cap = s.cap_qp;
-    int* cnt = s.cnt + C_QP;
-    int ig = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ig >= m.ncgp_solute) return;
-    int is = m.gsw[ig];
-    if (m.excl[is]) return;
-    bool inside = false;
-    if (m.any_atom) {   // nbqplis2, src/nonbondene.f90:3477-3487
-        for (int a = m.gslot[ig]; a < m.gslot[ig + 1] && !inside; ++a) {
-            int i = m.gatom[a];
-            inside = dist2_exact(x[3 * i], x[3 * i + 1], x[3 * i + 2], m.xpcent[0], m.xpcent[1], m.xpcent[2]) <= rcq2;
+    const int64_t cap = s.cap_qp;
+    int base = 0;
+    for (int g0 = 0; g0 < m.ncgp_solute; g0 += blockDim.x) {
+        int ig = g0 + threadIdx.x, na = 0;
+        if (ig < m.ncgp_solute && !m.excl[m.gsw[ig]]) {
+            bool inside = false;
+            if (m.any_atom) {   // nbqplis2, src/nonbondene.f90:3477-3487
+                for (int a = m.gslot[ig]; a < m.gslot[ig + 1] && !inside; ++a) {
+                    int i = m.gatom[a];
+                    inside = dist2_exact(x[3 * i], x[3 * i + 1], x[3 * i + 2], m.xpcent[0], m.xpcent[1],
+                                         m.xpcent[2]) <= rcq2;
+                }
+            } else {
+                int is = m.gsw[ig];
+                inside = dist2_exact(x[3 * is], x[3 * is + 1], x[3 * is + 2], m.xpcent[0], m.xpcent[1],
+                                     m.xpcent[2]) <= rcq2;
+            }
+            if (inside)
+                for (int a = m.gslot[ig]; a < m.gslot[ig + 1]; ++a) na += !qnear[m.gatom[a]];
         }
-    } else {
-        inside = dist2_exact(x[3 * is], x[3 * is + 1], x[3 * is + 2], m.xpcent[0], m.xpcent[1], m.xpcent[2]) <= rcq2;
+        int tot;
+        int pos = base + block_excl_scan(na, &tot);
+        if (na)
+            for (int a = m.gslot[ig]; a < m.gslot[ig + 1]; ++a) {
+                int i = m.gatom[a];
+                if (qnear[i]) continue;
+                if (pos < cap) out[pos] = i;
+                ++pos;
+            }
+        base += tot;
     }
-    if (!inside) return;
-    for (int a = m.gslot[ig]; a < m.gslot[ig + 1]; ++a) {
-        int i = m.gatom[a];
-        if (qnear[i]) continue;
-        int pos = atomicAdd(cnt, 1);
-        if (pos < cap) out[pos] = i;
-    }
+    if (threadIdx.x == 0) s.cnt[C_QP] = base;
 }
 
-// nbqwlist, src/nonbondene.f90:3862-3944: waters with O within Rcq of xpcent
-__global__ void k_build_qw(DevModel m, const DevState* __restrict__ states, double rcq2) {
+// nbqwlist, src/nonbondene.f90:3862-3944: waters with O within Rcq of xpcent,
+// appended in water order by one block per window
+__global__ void __launch_bounds__(1024) k_build_qw(DevModel m, const DevState* __restrict__ states, double rcq2) {
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
     int* __restrict__ out = s.qw;
-    int64_t cap = s.cap_qw;
-    int* cnt = s.cnt + C_QW;
-    int iw = blockIdx.x * blockDim.x + threadIdx.x;
-    if (iw >= m.nwat) return;
-    int io = m.nat_solute + m.sa * iw;
-    if (m.excl[io]) return;
-    double r2 = dist2_exact(x[3 * io], x[3 * io + 1], x[3 * io + 2], m.xpcent[0], m.xpcent[1], m.xpcent[2]);
-    if (r2 <= rcq2) {
-        int pos = atomicAdd(cnt, 1);
-        if (pos < cap) out[pos] = iw;
+    const int64_t cap = s.cap_qw;
+    int base = 0;
+    for (int w0 = 0; w0 < m.nwat; w0 += blockDim.x) {
+        int iw = w0 + threadIdx.x;
+        bool ok = false;
+        if (iw < m.nwat) {
+            int io = m.nat_solute + m.sa * iw;
+            ok = !m.excl[io] && dist2_exact(x[3 * io], x[3 * io + 1], x[3 * io + 2], m.xpcent[0], m.xpcent[1],
+                                            m.xpcent[2]) <= rcq2;
+        }
+        int tot;
+        int pos = base + block_excl_scan(ok ? 1 : 0, &tot);
+        if (ok && pos < cap) out[pos] = iw;
+        base += tot;
     }
+    if (threadIdx.x == 0) s.cnt[C_QW] = base;
 }
 
 // -----------------------------------------------------------------------------
@@ -586,13 +644,12 @@ __device__ __forceinline__ void lrf_expand(const double* m, double* L) {
 }
 
 // LRF classification of a group pair: true when rc2 < r2 <= rlrf2 in FP64
-__device__ __forceinline__ bool lrf_pair(float r2f, double rc2, double rlrf2, const double* __restrict__ x, int a,
-                                         int b) {
-    float c1 = (float)rc2, c2 = (float)rlrf2;
-    if (r2f > c1 * 1.0002f && r2f < c2 * 0.9998f) return true;
-    if (r2f < c1 * 0.9998f || r2f > c2 * 1.0002f) return false;
+__device__ __forceinline__ bool lrf_pair(float r2f, const Band& rc, const Band& rl, const double* __restrict__ x,
+                                         int a, int b) {
+    if (r2f > rc.hi && r2f < rl.lo) return true;
+    if (r2f < rc.lo || r2f > rl.hi) return false;
     double r2 = dist2_exact(x[3 * a], x[3 * a + 1], x[3 * a + 2], x[3 * b], x[3 * b + 1], x[3 * b + 2]);
-    return r2 > rc2 && r2 <= rlrf2;
+    return r2 > rc.c && r2 <= rl.c;
 }
 
 // One warp per target group g2 sums the far-field contributions of every
@@ -602,6 +659,7 @@ __device__ __forceinline__ bool lrf_pair(float r2f, double rc2, double rlrf2, co
 template <bool MIX>
 __global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const DevState* __restrict__ states, Cut c,
                                                          const int* __restrict__ lrf_src) {
+    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
     typedef typename std::conditional<MIX, float, double>::type T;
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
@@ -616,7 +674,7 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const DevSta
         double cx = L[0], cy = L[1], cz = L[2];
         float4 x2 = xq[s2];
         float cxf = (float)(cx - m.xpcent[0]), cyf = (float)(cy - m.xpcent[1]), czf = (float)(cz - m.xpcent[2]);
-        const double rc_s = sol2 ? c.rcpp2 : c.rcpw2, rc_w = sol2 ? c.rcpw2 : c.rcww2;
+        const Band rc_s = sol2 ? bpp : bpw, rc_w = sol2 ? bpw : bww;
         T mom[kLrfMom];
 #pragma unroll
         for (int k = 0; k < kLrfMom; ++k) mom[k] = T(0);
@@ -625,8 +683,8 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const DevSta
             if (src < 0) continue;
             int s1 = src & 0x3fffffff;
             if (s1 == s2) continue;   // same group
-            double rc2 = (src >> 30) ? rc_s : rc_w;
-            if (!lrf_pair(r2_f(x2, xq[s1]), rc2, c.rlrf2, x, s2, s1)) continue;
+            const Band& rc2 = (src >> 30) ? rc_s : rc_w;
+            if (!lrf_pair(r2_f(x2, xq[s1]), rc2, blrf, x, s2, s1)) continue;
             if constexpr (MIX) {
                 float4 xi = xq[i];
                 lrf_terms<float>(xi.x - cxf, xi.y - cyf, xi.z - czf, xi.w, mom);
@@ -657,6 +715,7 @@ __device__ __forceinline__ int group_last_atom(const DevModel& m, int g) {
 }
 template <bool MIX>
 __global__ void __launch_bounds__(128) k_lrf_accumulate_any(DevModel m, const DevState* __restrict__ states, Cut c) {
+    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
     typedef typename std::conditional<MIX, float, double>::type T;
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
@@ -681,15 +740,15 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate_any(DevModel m, const De
             bool sol1 = g1 < m.ncgp_solute;
             bool far;
             if (sol1 && sol2) {
-                far = !gg_inside_any(m, x, xq, g1, g2, c.rcpp2);
+                far = !gg_inside_any(m, x, xq, g1, g2, bpp);
             } else if (sol1 || sol2) {
-                far = !gw_inside_any(m, x, xq, sol1 ? g1 : g2, sol1 ? s2 : s1, c.rcpw2);
+                far = !gw_inside_any(m, x, xq, sol1 ? g1 : g2, sol1 ? s2 : s1, bpw);
             } else {
-                far = lrf_pair(r2_f(xq[s2], xq[s1]), c.rcww2, c.rlrf2, x, s2, s1);
+                far = lrf_pair(r2_f(xq[s2], xq[s1]), bww, blrf, x, s2, s1);
             }
             if (far && (sol1 || sol2)) {
                 int l1 = group_last_atom(m, g1);
-                far = within(r2_f(xq[l1], xq[l2]), c.rlrf2, x, l1, l2);
+                far = within(r2_f(xq[l1], xq[l2]), blrf, x, l1, l2);
             }
             if (!far) continue;
             for (int a = m.gslot[g1]; a < m.gslot[g1 + 1]; ++a) {
@@ -1020,8 +1079,12 @@ struct QPairT<true, SMAX> {
 
 // nonbond_qw_spc / nonbond_qw (src/nonbondene.f90:5658-5767, 5339-5418) and
 // nonbond_qp (src/nonbondene.f90:5157-5230): one warp per listed environment
-// unit (a water molecule, or one solute atom), lane = Q atom.  The unit's
-// per-state energies are summed in registers and converted once per unit.
+// unit (a water molecule, or one solute atom), lane = Q atom.  A warp takes
+// fixed chunks of kQChunk consecutive units; the per-state energies of a
+// chunk are summed in registers and converted once per chunk, so the fixed-
+// point totals do not depend on the grid.  An environment atom's gradient is
+// summed over the Q atoms in FP32 in a fixed shuffle order, then converted.
+constexpr int kQChunk = 8;
 template <bool MIX, bool SPC, bool WATER, int SMAX>
 __global__ void __launch_bounds__(kQBlock) k_qenv(DevModel m, const DevState* __restrict__ states) {
     typedef typename std::conditional<MIX, float, double>::type T;
@@ -1037,11 +1100,14 @@ __global__ void __launch_bounds__(kQBlock) k_qenv(DevModel m, const DevState* __
     int n = WATER ? min((int64_t)s.cnt[C_QW], s.cap_qw) : min((int64_t)s.cnt[C_QP], s.cap_qp);
     int S = m.S;
     const int na = WATER ? m.sa : 1;
-    for (int p = warp_id_global(); p < n; p += warps_total()) {
-        int j0 = WATER ? m.nat_solute + m.sa * s.qw[p] : s.qp[p];
-        T pel[SMAX], pvdw[SMAX];
+    const int nchunk = (n + kQChunk - 1) / kQChunk;
+    for (int ch = warp_id_global(); ch < nchunk; ch += warps_total()) {
+      T pel[SMAX], pvdw[SMAX];
 #pragma unroll
-        for (int st = 0; st < SMAX; ++st) pel[st] = pvdw[st] = T(0);
+      for (int st = 0; st < SMAX; ++st) pel[st] = pvdw[st] = T(0);
+      const int pend = min(n, (ch + 1) * kQChunk);
+      for (int p = ch * kQChunk; p < pend; ++p) {
+        int j0 = WATER ? m.nat_solute + m.sa * s.qw[p] : s.qp[p];
         for (int a = 0; a < na; ++a) {
             int j = j0 + a;
             bool lj = !WATER || !SPC || a == 0;
@@ -1081,25 +1147,16 @@ __global__ void __launch_bounds__(kQBlock) k_qenv(DevModel m, const DevState* __
                 gj[2] += tz * dvs;
             }
             // environment atom gradient: sum over the warp's Q atoms
-            if constexpr (MIX) {
-                unsigned long long v0 = warp_sum(to_fix(gj[0])), v1 = warp_sum(to_fix(gj[1])),
-                                   v2 = warp_sum(to_fix(gj[2]));
-                if (lane == 0) {
-                    atomicAdd(s.fix + 3 * j, v0);
-                    atomicAdd(s.fix + 3 * j + 1, v1);
-                    atomicAdd(s.fix + 3 * j + 2, v2);
-                }
-            } else {
-                double v0 = warp_sum(gj[0]), v1 = warp_sum(gj[1]), v2 = warp_sum(gj[2]);
-                if (lane == 0) acc.grad(j, v0, v1, v2);
-            }
+            T v0 = warp_sum(gj[0]), v1 = warp_sum(gj[1]), v2 = warp_sum(gj[2]);
+            if (lane == 0) acc.grad(j, v0, v1, v2);
         }
+      }
 #pragma unroll
-        for (int st = 0; st < SMAX; ++st) {
-            if (st >= S) break;
-            eel[st].add(pel[st]);
-            evdw[st].add(pvdw[st]);
-        }
+      for (int st = 0; st < SMAX; ++st) {
+          if (st >= S) break;
+          eel[st].add(pel[st]);
+          evdw[st].add(pvdw[st]);
+      }
     }
     const int kel = WATER ? 4 : 2;
 #pragma unroll
@@ -1403,6 +1460,9 @@ __global__ void k_watpol_theta(DevModel m, const DevState* __restrict__ states, 
     double scp = rmx * rcx + rmy * rcy + rmz * rcz;
     scp = fmin(1.0, fmax(-1.0, scp));
     s.theta[w] = acos(scp);
+    double* v = s.wvec + 8 * (size_t)w;   // reused by k_watpol_force in the same call
+    v[0] = rmx; v[1] = rmy; v[2] = rmz; v[3] = rm;
+    v[4] = rcx; v[5] = rcy; v[6] = rcz; v[7] = rc;
     int N = p.nshell;
     if (rc > p.rout[N - 1] - p.dr[N - 1]) {
         int is;
@@ -1418,16 +1478,18 @@ __global__ void k_watpol_theta(DevModel m, const DevState* __restrict__ states, 
 // stable selection order of src/nonbondene.f90:6612-6628: rank = number of
 // waters of the same shell with smaller theta, ties broken by water index
 // (the reference scans the shell in water order and keeps the first minimum).
-// One block per shell; the shell's thetas are staged in shared memory.
-__global__ void __launch_bounds__(256) k_watpol_rank(DevModel m, const DevState* __restrict__ states) {
+// One block per shell; the shell's thetas are staged in shared memory and one
+// warp ranks one water at a time, its lanes splitting the comparisons.
+constexpr int kRankBlock = 512;
+__global__ void __launch_bounds__(kRankBlock) k_watpol_rank(DevModel m, const DevState* __restrict__ states) {
     const DevState& s = states[blockIdx.y];
     // theta >= 0, so the bit patterns of the doubles order like the values;
     // integer compares keep the sort off the (narrow) FP64 pipe
     __shared__ long long th[1024];
     __shared__ int ww[1024];
-    int sh = blockIdx.x;
-    int n = s.n_insh[sh];
+    const int sh = blockIdx.x, n = s.n_insh[sh];
     const int* L = s.shell_list + (size_t)sh * m.nwat;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int base = 0; base < n; base += 1024) {
         int cn = min(1024, n - base);
         __syncthreads();
@@ -1436,13 +1498,23 @@ __global__ void __launch_bounds__(256) k_watpol_rank(DevModel m, const DevState*
             th[k] = __double_as_longlong(s.theta[ww[k]]);
         }
         __syncthreads();
-        for (int k = threadIdx.x; k < n; k += blockDim.x) {
-            int w = L[k];
-            long long t = __double_as_longlong(s.theta[w]);
+        for (int k = warp; k < n; k += nw) {
+            int w;
+            long long t;
+            if (k >= base && k < base + cn) {
+                w = ww[k - base];
+                t = th[k - base];
+            } else {
+                w = L[k];
+                t = __double_as_longlong(s.theta[w]);
+            }
             int r = 0;
-            for (int v = 0; v < cn; ++v) r += (th[v] < t) || (th[v] == t && ww[v] < w);
-            if (base == 0) s.rank[w] = r;
-            else s.rank[w] += r;
+            for (int v = lane; v < cn; v += kWarp) r += (th[v] < t) || (th[v] == t && ww[v] < w);
+            r = __reduce_add_sync(kFull, r);
+            if (lane == 0) {
+                if (base == 0) s.rank[w] = r;
+                else s.rank[w] += r;
+            }
         }
     }
 }
@@ -1470,8 +1542,10 @@ __global__ void k_watpol_update(SolventDev p, const DevState* __restrict__ state
     an[is] = 0.0;
 }
 
-// energy and gradient, src/nonbondene.f90:6646-6742
-template <bool MIX>
+// energy and gradient, src/nonbondene.f90:6646-6742.  STORED: the vectors and
+// theta of this call's k_watpol_theta are current (md); otherwise they are
+// recomputed from the coordinates, as the reference does in every call.
+template <bool MIX, bool STORED>
 __global__ void k_watpol_force(DevModel m, const DevState* __restrict__ states, SolventDev p) {
     const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
@@ -1492,11 +1566,18 @@ __global__ void k_watpol_force(DevModel m, const DevState* __restrict__ states, 
         double dth = th - t0 + s.wstate[sh];
         ep.add(0.5 * p.fkwpol * dth * dth);
         double dv = p.fkwpol * dth;
-        double rmx, rmy, rmz, rm, rcx, rcy, rcz, rc;
-        water_vectors(m, s.x, w, rmx, rmy, rmz, rm, rcx, rcy, rcz, rc);
+        double rmx, rmy, rmz, rm, rcx, rcy, rcz, rc, f0;
+        if constexpr (STORED) {
+            const double* v = s.wvec + 8 * (size_t)w;
+            rmx = v[0]; rmy = v[1]; rmz = v[2]; rm = v[3];
+            rcx = v[4]; rcy = v[5]; rcz = v[6]; rc = v[7];
+        } else {
+            water_vectors(m, s.x, w, rmx, rmy, rmz, rm, rcx, rcy, rcz, rc);
+        }
         double scp = rmx * rcx + rmy * rcy + rmz * rcz;
         scp = fmin(1.0, fmax(-1.0, scp));
-        double f0 = sin(acos(scp));
+        // theta = acos(scp) of this same scp when STORED
+        f0 = STORED ? sin(th) : sin(acos(scp));
         if (fabs(f0) < 1.0e-10) f0 = 1.0e-10;
         f0 = dv * (-1.0 / f0);
         double f1x = (rcx - rmx * scp) * -2.0 / rm, f1y = (rcy - rmy * scp) * -2.0 / rm,
@@ -1595,6 +1676,7 @@ __device__ __forceinline__ int row_append(int* __restrict__ row, int cap, int co
 // 2842-2955, 4274-4395) stored from both sides.  Rows 0..ncgp_solute-1 are
 // solute groups, the next nwat rows waters; one warp per row.
 __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cut c) {
+    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
     const float4* __restrict__ xq = s.xq;
@@ -1613,7 +1695,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                     int b0 = 0, n2 = 0, nq = 0;
                     if (g2 < m.ncgp_solute) {
                         int s2 = m.gsw[g2];
-                        if (!m.excl[s2]) ok = (g2 == g) || gg_inside(m, x, xq, g, g2, c.rcpp2);
+                        if (!m.excl[s2]) ok = (g2 == g) || gg_inside(m, x, xq, g, g2, bpp);
                         if (ok) {
                             b0 = m.gslot[g2];
                             n2 = m.gslot[g2 + 1] - b0;
@@ -1661,7 +1743,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                     bool ok = false;
                     if (jw < m.nwat) {
                         int jo = m.nat_solute + m.sa * jw;
-                        if (!m.excl[jo]) ok = gw_inside(m, x, xq, g, jo, c.rcpw2);
+                        if (!m.excl[jo]) ok = gw_inside(m, x, xq, g, jo, bpw);
                     }
                     npw = row_append(rw, s.cap_gw, npw, ok, jw);
                 }
@@ -1683,7 +1765,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                     bool ok = false;
                     if (jw < m.nwat && jw != w) {
                         int jo = m.nat_solute + m.sa * jw;
-                        if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), c.rcww2, x, io, jo);
+                        if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), bww, x, io, jo);
                     }
                     nww = row_append(rw, s.cap_rww, nww, ok, jw);
                 }
@@ -1694,7 +1776,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                     if (g < m.ncgp_solute) {
                         int s2 = m.gsw[g];
                         // the same test as from the group side
-                        if (!m.excl[s2]) ok = gw_inside(m, x, xq, g, io, c.rcpw2);
+                        if (!m.excl[s2]) ok = gw_inside(m, x, xq, g, io, bpw);
                     }
                     nwg = row_append(rg, s.cap_wg, nwg, ok, g);
                 }
@@ -2012,11 +2094,11 @@ void launch_build_pp(const Launch& L, const Cut& c) {
 }
 void launch_build_qw(const Launch& L, const Cut& c) {
     if (L.m.nwat == 0 || L.m.nqat == 0) return;
-    k_build_qw<<<dim3((L.m.nwat + 255) / 256, L.nwin), 256, 0, L.st>>>(L.m, L.ds, c.rcq2);
+    k_build_qw<<<dim3(1, L.nwin), 1024, 0, L.st>>>(L.m, L.ds, c.rcq2);
 }
 void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2) {
     if (L.m.ncgp_solute == 0 || L.m.nqat == 0) return;
-    k_build_qp<<<dim3((L.m.ncgp_solute + 127) / 128, L.nwin), 128, 0, L.st>>>(L.m, L.ds, qnear, rcq2);
+    k_build_qp<<<dim3(1, L.nwin), 1024, 0, L.st>>>(L.m, L.ds, qnear, rcq2);
 }
 void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src) {
     dim3 g = grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin);
@@ -2117,15 +2199,20 @@ int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int m
     if (md) {
         k_watpol_reset<<<L.nwin, kMaxShell, 0, L.st>>>(L.ds);
         k_watpol_theta<<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
-        k_watpol_rank<<<dim3(p.nshell, L.nwin), 256, 0, L.st>>>(L.m, L.ds);
+        k_watpol_rank<<<dim3(p.nshell, L.nwin), kRankBlock, 0, L.st>>>(L.m, L.ds);
         nl += 3;
     }
     if (istep > 0 && md && (istep % (int)llround(p.itdis)) == 0) {
         k_watpol_update<<<dim3(1, L.nwin), kMaxShell, 0, L.st>>>(p, L.ds);
         ++nl;
     }
-    if (mixed) k_watpol_force<true><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
-    else k_watpol_force<false><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+    if (md) {
+        if (mixed) k_watpol_force<true, true><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+        else k_watpol_force<false, true><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+    } else {
+        if (mixed) k_watpol_force<true, false><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+        else k_watpol_force<false, false><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+    }
     ++nl;
     if (md) {
         k_watpol_average<<<dim3(1, L.nwin), kMaxShell, 0, L.st>>>(p, L.ds);
