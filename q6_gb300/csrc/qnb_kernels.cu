@@ -57,11 +57,33 @@ __device__ __forceinline__ int warp_append(int* counter, int n) {
 }
 
 // ---- accumulation back-ends -------------------------------------------------
+// v * 2^32 rounded to the nearest integer (ties to even) as a 64-bit two's
+// complement value.  The float form uses the hardware conversion: measured,
+// its issue cost in the FP32 kernels is below that of an integer rebuild.
 __device__ __forceinline__ unsigned long long to_fix(float v) {
     return (unsigned long long)__float2ll_rn(v * kFixF);
 }
+// The double form is built from the IEEE-754 fields with integer
+// instructions, saturated like cvt.rni.s64.f64 (NaN gives 0): GB300 executes
+// DMUL and double-to-int64 conversions on its FP64 pipe (1/64 of the FP32
+// rate), which the FP64 kernels of the mixed form (LRF Taylor, Q-Q, solvent
+// restraints) already keep busy.
 __device__ __forceinline__ unsigned long long to_fixd(double v) {
-    return (unsigned long long)__double2ll_rn(v * kFix);
+    unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    int e = (int)((u >> 52) & 0x7ffull);
+    unsigned long long m = (u & 0xfffffffffffffull) | 0x10000000000000ull;
+    int sh = e - 1043;                    // v * 2^32 = m * 2^(e - 1023 - 52 + 32)
+    int ls = min(max(sh, 0), 10);
+    int k = min(max(-sh, 0), 63);
+    unsigned long long q = m >> k;
+    unsigned long long rem = m & ((1ull << k) - 1ull), half = (1ull << k) >> 1;
+    q += (unsigned long long)((k > 0) & ((rem > half) | ((rem == half) & (q & 1ull))));
+    unsigned long long r = sh >= 0 ? (m << ls) : q;
+    if (e == 0) r = 0ull;
+    bool sat = sh > 10;
+    if (sat) r = (e == 2047 && (u & 0xfffffffffffffull)) ? 0ull : 0x7fffffffffffffffull;
+    unsigned long long neg = (sat && r) ? 0x8000000000000000ull : 0ull - r;
+    return (u >> 63) ? neg : r;
 }
 
 template <bool MIX>
@@ -653,11 +675,95 @@ __device__ __forceinline__ bool lrf_pair(float r2f, const Band& rc, const Band& 
 }
 
 // One warp per target group g2 sums the far-field contributions of every
-// non-Q atom whose group is classified "LRF" against g2 (lanes stride over the
-// atoms, so loads are coalesced); the 40 coefficients are then reduced across
-// the warp.  Mixed form: FP32 terms (rsqrt on the SFU); FP64 form: FP64 terms.
+// non-Q atom whose group is classified "LRF" against g2; the 40 coefficients
+// are then reduced across the warp.  The warps of a block take consecutive
+// targets and stream the source atoms through shared memory together: each
+// atom (position, charge, its group's distance atom) is loaded from global
+// memory once per block instead of once per target.  Mixed form: FP32 terms
+// (rsqrt on the SFU); FP64 form: FP64 terms.
+constexpr int kLrfBlock = 256;
 template <bool MIX>
-__global__ void __launch_bounds__(128) k_lrf_accumulate(DevModel m, const DevState* __restrict__ states, Cut c,
+__global__ void __launch_bounds__(kLrfBlock) k_lrf_accumulate(DevModel m, const DevState* __restrict__ states, Cut c,
+                                                              const int* __restrict__ lrf_src) {
+    typedef typename std::conditional<MIX, float, double>::type T;
+    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
+    __shared__ float4 s_xs[kLrfBlock];                  // distance atom of the source's group
+    __shared__ int s_src[kLrfBlock];                    // lrf_src entry (-1: not a source)
+    __shared__ T s_xi[4 * kLrfBlock];                   // source x, y, z (centred in FP32), charge
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const float4* __restrict__ xq = s.xq;
+    double* __restrict__ lrf = s.lrf;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kLrfBlock / 32;
+    for (int gbase = blockIdx.x * nw; gbase < m.ncgp; gbase += gridDim.x * nw) {   // block-uniform
+        const int g2 = gbase + warp;
+        int s2 = 0;
+        bool act = g2 < m.ncgp;
+        if (act) {
+            s2 = group_dist_atom(m, g2);
+            act = !m.excl[s2];
+        }
+        const bool sol2 = act && g2 < m.ncgp_solute;
+        const Band rc_s = sol2 ? bpp : bpw, rc_w = sol2 ? bpw : bww;
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        float4 x2 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (act) {
+            const double* L = lrf + (size_t)g2 * kLrfLen;
+            cx = L[0]; cy = L[1]; cz = L[2];
+            x2 = xq[s2];
+        }
+        const T ccx = MIX ? T(cx - m.xpcent[0]) : T(cx), ccy = MIX ? T(cy - m.xpcent[1]) : T(cy),
+                ccz = MIX ? T(cz - m.xpcent[2]) : T(cz);
+        T mom[kLrfMom];
+#pragma unroll
+        for (int k = 0; k < kLrfMom; ++k) mom[k] = T(0);
+        for (int i0 = 0; i0 < m.natom; i0 += kLrfBlock) {
+            __syncthreads();
+            {
+                int i = i0 + threadIdx.x, t = threadIdx.x;
+                int src = i < m.natom ? lrf_src[i] : -1;
+                s_src[t] = src;
+                if (src >= 0) {
+                    s_xs[t] = xq[src & 0x3fffffff];
+                    if constexpr (MIX) {
+                        float4 xi = xq[i];
+                        s_xi[4 * t] = xi.x; s_xi[4 * t + 1] = xi.y; s_xi[4 * t + 2] = xi.z; s_xi[4 * t + 3] = xi.w;
+                    } else {
+                        s_xi[4 * t] = x[3 * i]; s_xi[4 * t + 1] = x[3 * i + 1]; s_xi[4 * t + 2] = x[3 * i + 2];
+                        s_xi[4 * t + 3] = m.crg[i];
+                    }
+                }
+            }
+            __syncthreads();
+            if (!act) continue;
+            const int n = min(kLrfBlock, m.natom - i0);
+            for (int k = lane; k < n; k += kWarp) {
+                int src = s_src[k];   // distance atom of i's group | solute flag << 30
+                if (src < 0) continue;
+                int s1 = src & 0x3fffffff;
+                if (s1 == s2) continue;   // same group
+                const Band& rc2 = (src >> 30) ? rc_s : rc_w;
+                if (!lrf_pair(r2_f(x2, s_xs[k]), rc2, blrf, x, s2, s1)) continue;
+                lrf_terms<T>(s_xi[4 * k] - ccx, s_xi[4 * k + 1] - ccy, s_xi[4 * k + 2] - ccz, s_xi[4 * k + 3], mom);
+            }
+        }
+        if (!act) continue;
+        double tot[kLrfMom];
+#pragma unroll
+        for (int k = 0; k < kLrfMom; ++k) {
+            T v = mom[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+            tot[k] = (double)v;
+        }
+        if (lane == 0) lrf_expand(tot, lrf + (size_t)g2 * kLrfLen + 3);
+    }
+}
+
+// Unstaged variant: one warp per target group reads the source atoms straight
+// from global memory (lanes stride over the atoms, so loads are coalesced).
+template <bool MIX>
+__global__ void __launch_bounds__(128) k_lrf_accumulate_direct(DevModel m, const DevState* __restrict__ states, Cut c,
                                                          const int* __restrict__ lrf_src) {
     const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
     typedef typename std::conditional<MIX, float, double>::type T;
@@ -2101,14 +2207,21 @@ void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2) {
     k_build_qp<<<dim3(1, L.nwin), 1024, 0, L.st>>>(L.m, L.ds, qnear, rcq2);
 }
 void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src) {
-    dim3 g = grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin);
     if (L.m.any_atom) {
+        dim3 g = grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin);
         if (mixed) k_lrf_accumulate_any<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
         else k_lrf_accumulate_any<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
         return;
     }
-    if (mixed) k_lrf_accumulate<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
-    else k_lrf_accumulate<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
+// FP64 form: the unstaged kernel measured faster (its FP64 terms, not the
+// loads, bound it, and the staged block holds more registers)
+#ifndef QNB_LRF_FP64_STAGED
+#define QNB_LRF_FP64_STAGED 0
+#endif
+    dim3 g = grid_for((int64_t)L.m.ncgp * 32, kLrfBlock, 3, L.nwin);
+    if (mixed) k_lrf_accumulate<true><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
+    else if (QNB_LRF_FP64_STAGED) k_lrf_accumulate<false><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
+    else k_lrf_accumulate_direct<false><<<grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
 }
 
 void launch_build_rows(const Launch& L, const Cut& c) {
