@@ -826,7 +826,7 @@ int grow_lists(qnb_context* c, bool* grew, bool* do_qp, bool* do_qw) {
         for (int w = 0; w < c->nwin; ++w) {
             DevState& s = c->st[w];
             if (need[C_RGP] > s.cap_gp) {
-                int cap = (int)(need[C_RGP] + need[C_RGP] / 4 + 32);
+                int cap = ((int)(need[C_RGP] + need[C_RGP] / 4 + 32) + 3) & ~3;   // 16-byte row starts
                 c->release(s.row_gp);
                 s.row_gp = nullptr;
                 TRY(c->alloc(&s.row_gp, (size_t)std::max(1, c->ncgp_solute) * cap));
@@ -837,7 +837,7 @@ int grow_lists(qnb_context* c, bool* grew, bool* do_qp, bool* do_qw) {
                       {C_RWW, &s.cap_rww, &s.row_ww, c->nwat}, {C_RWG, &s.cap_wg, &s.row_wg, c->nwat}};
             for (auto& r : rs) {
                 if (need[r.k] <= *r.cap) continue;
-                int cap = (int)(need[r.k] + need[r.k] / 4 + 32);
+                int cap = ((int)(need[r.k] + need[r.k] / 4 + 32) + 3) & ~3;   // 16-byte row starts
                 c->release(*r.row);
                 *r.row = nullptr;
                 TRY(c->alloc(r.row, (size_t)std::max(1, r.nrows) * cap));

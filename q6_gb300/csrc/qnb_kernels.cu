@@ -1924,6 +1924,21 @@ __device__ __forceinline__ TypeTab stage_types(const DevModel& m, float4* sh) {
     return TypeTab{m.ljpair, m.natyps};
 }
 
+// Asynchronous global-to-shared copies of row entries (16 bytes per lane,
+// L2 only): a warp fetches the next chunk of its row while it evaluates the
+// current one, so the DRAM latency of the streamed rows is paid once per
+// chunk instead of once per loop iteration.  Row capacities are multiples of
+// 4 entries, so every row starts on a 16-byte boundary and a chunk rounded up
+// to whole 16-byte units stays inside its row.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+constexpr int kRowChunk = 128;   // entries per prefetched chunk
+
 // solute group rows: pp (partner atoms with exclusion / 1-4 kinds) and pw
 // (partner waters): gradient of the group's own atoms.  Every solute pair sits
 // in the rows of both of its atoms (a pair inside one group twice in that
@@ -1944,8 +1959,11 @@ constexpr int rows_min_blocks() {
 template <int MAXG>
 __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(DevModel m, const DevState* __restrict__ states) {
     __shared__ float4 sh_lj[kMaxTypesShared * kMaxTypesShared];
+    __shared__ __align__(16) uint2 sh_pp[4][2][kRowChunk];   // per warp: double-buffered pp entries
+    __shared__ __align__(16) int sh_pw[4][kRowChunk];        // per warp: first chunk of pw entries
     constexpr bool kTypeInEntry = MAXG <= 8;
     const DevState& s = states[blockIdx.y];
+    const int wib = threadIdx.x >> 5;
     TypeTab lj = stage_types(m, sh_lj);
     Acc<true> acc = make_acc<true>(s);
     ESum<true> epel, epvdw, ewel, ewvdw;
@@ -1979,8 +1997,28 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
         float rpel = 0.f, rpvdw = 0.f, rwel = 0.f, rwvdw = 0.f;
         // ---- solute partner atoms (nonbond_pp, src/nonbondene.f90:4694-4760)
         const uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
-        for (int k = lane; k < npp; k += kWarp) {
-            uint2 e = rp[k];
+        const int* rw = s.row_gw + (size_t)g * s.cap_gw;
+        const int nchunk = (npp + kRowChunk - 1) / kRowChunk;
+        auto fetch_pp = [&](int ch) {
+            int e0 = ch * kRowChunk, units = (min(kRowChunk, npp - e0) + 1) >> 1;
+            for (int u = lane; u < units; u += kWarp) cp_async16(&sh_pp[wib][ch & 1][2 * u], rp + e0 + 2 * u);
+        };
+        if (nchunk > 0) fetch_pp(0);
+        for (int u = lane; u < (min(kRowChunk, npw) + 3) >> 2; u += kWarp) cp_async16(&sh_pw[wib][4 * u], rw + 4 * u);
+        cp_async_commit();
+        for (int ch = 0; ch < nchunk; ++ch) {
+          if (ch + 1 < nchunk) {
+              fetch_pp(ch + 1);
+              cp_async_commit();
+              cp_async_wait<1>();
+          } else {
+              cp_async_wait<0>();
+          }
+          __syncwarp();
+          const uint2* buf = sh_pp[wib][ch & 1];
+          const int n = min(kRowChunk, npp - ch * kRowChunk);
+          for (int k = lane; k < n; k += kWarp) {
+            uint2 e = buf[k];
             int j = (int)(e.x & 0x0fffffffu);
             float4 xb = xq[j];
             int tj = kTypeInEntry ? (int)(e.y >> 16) : m.iac[j];
@@ -1999,11 +2037,16 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
                 rpel += vel;
                 rpvdw += vdw;
             }
+          }
+          __syncwarp();   // this buffer is refilled two chunks later
+        }
+        if (nchunk == 0) {
+            cp_async_wait<0>();
+            __syncwarp();
         }
         // ---- water partners (nonbond_pw, src/nonbondene.f90:4856-4916); energy counted here
-        const int* rw = s.row_gw + (size_t)g * s.cap_gw;
         for (int k = lane; k < npw; k += kWarp) {
-            int j0 = m.nat_solute + m.sa * rw[k];
+            int j0 = m.nat_solute + m.sa * (k < kRowChunk ? sh_pw[wib][k] : rw[k]);
             for (int b = 0; b < m.sa; ++b) {
                 float4 xb = xq[j0 + b];
                 int tw = m.wtype[b];
@@ -2028,6 +2071,7 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
                 }
             }
         }
+        __syncwarp();   // sh_pw is refilled by the next row
         epel.add(0.5f * rpel);
         epvdw.add(0.5f * rpvdw);
         ewel.add(rwel);
@@ -2054,9 +2098,12 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
 // water rows: ww (waters, SPC fast path as nonbond_ww_spc) and wp (solute
 // groups) gradient of the water's atoms
 template <bool SPC>
-__global__ void __launch_bounds__(128) k_rows_water(DevModel m, const DevState* __restrict__ states) {
+__global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevState* __restrict__ states) {
     __shared__ float4 sh_lj[kMaxTypesShared * kMaxTypesShared];
+    __shared__ __align__(16) int sh_ww[4][2][kRowChunk];   // per warp: double-buffered ww entries
+    __shared__ __align__(16) int sh_wg[4][kRowChunk];      // per warp: first chunk of wp entries
     const DevState& s = states[blockIdx.y];
+    const int wib = threadIdx.x >> 5;
     TypeTab lj = stage_types(m, sh_lj);
     Acc<true> acc = make_acc<true>(s);
     ESum<true> eel, evdw;
@@ -2076,8 +2123,28 @@ __global__ void __launch_bounds__(128) k_rows_water(DevModel m, const DevState* 
         }
         float rel = 0.f, rvdw = 0.f;
         const int* rw = s.row_ww + (size_t)w * s.cap_rww;
-        for (int k = lane; k < nww; k += kWarp) {
-            int w2 = rw[k];
+        const int* rg = s.row_wg + (size_t)w * s.cap_wg;
+        const int nchunk = (nww + kRowChunk - 1) / kRowChunk;
+        auto fetch_ww = [&](int ch) {
+            int e0 = ch * kRowChunk, units = (min(kRowChunk, nww - e0) + 3) >> 2;
+            for (int u = lane; u < units; u += kWarp) cp_async16(&sh_ww[wib][ch & 1][4 * u], rw + e0 + 4 * u);
+        };
+        if (nchunk > 0) fetch_ww(0);
+        for (int u = lane; u < (min(kRowChunk, nwg) + 3) >> 2; u += kWarp) cp_async16(&sh_wg[wib][4 * u], rg + 4 * u);
+        cp_async_commit();
+        for (int ch = 0; ch < nchunk; ++ch) {
+          if (ch + 1 < nchunk) {
+              fetch_ww(ch + 1);
+              cp_async_commit();
+              cp_async_wait<1>();
+          } else {
+              cp_async_wait<0>();
+          }
+          __syncwarp();
+          const int* buf = sh_ww[wib][ch & 1];
+          const int n = min(kRowChunk, nww - ch * kRowChunk);
+          for (int k = lane; k < n; k += kWarp) {
+            int w2 = buf[k];
             int j0 = m.nat_solute + sa * w2;
             float pel = 0.f, pvdw = 0.f;
 #pragma unroll
@@ -2099,12 +2166,17 @@ __global__ void __launch_bounds__(128) k_rows_water(DevModel m, const DevState* 
                 rel += pel;
                 rvdw += pvdw;
             }
+          }
+          __syncwarp();   // this buffer is refilled two chunks later
+        }
+        if (nchunk == 0) {
+            cp_async_wait<0>();
+            __syncwarp();
         }
         eel.add(rel);
         evdw.add(rvdw);
-        const int* rg = s.row_wg + (size_t)w * s.cap_wg;
         for (int k = lane; k < nwg; k += kWarp) {
-            int g = rg[k];
+            int g = k < kRowChunk ? sh_wg[wib][k] : rg[k];
             for (int bb = m.gslot[g]; bb < m.gslot[g + 1]; ++bb) {
                 int j = m.gatom[bb];
                 if (m.iqatom[j] >= 0) continue;
@@ -2120,6 +2192,7 @@ __global__ void __launch_bounds__(128) k_rows_water(DevModel m, const DevState* 
                 }
             }
         }
+        __syncwarp();   // sh_wg is refilled by the next row
 #pragma unroll
         for (int a = 0; a < kMaxSolv; ++a) {
             if (a >= sa) break;
