@@ -96,6 +96,7 @@ struct qnb_context {
     bool diag_valid = false;       // mixed form: half lists for inspection built from x_build
     Cut last_cut{};
     int maxg = 1;                  // largest solute charge group
+    bool rows_pending = false;     // mixed form: frow not yet added into d
     DevState* d_diag = nullptr;    // scratch device state for inspection builds
     std::vector<int> counts;       // [nwin][C_NUM] after the last build
     SolventDev solv{};
@@ -697,6 +698,9 @@ int alloc_state(qnb_context* c) {
         s.x = c->x_all + n3 * w;
         s.d = c->d_all + n3 * w;
         TRY(c->alloc(&s.xq, (size_t)m.natom));
+        TRY(c->alloc(&s.frow, (size_t)3 * m.natom));
+        CU(cudaMemset(s.frow, 0, sizeof(float) * 3 * m.natom));   // atoms outside every row stay 0
+        TRY(c->alloc(&s.erow, (size_t)std::max(1, m.ncgp_solute + m.nwat)));
         TRY(c->alloc(&s.fix, n3));
         s.e = c->e_all + (size_t)kNumE * w;
         s.efix = c->efix_all + (size_t)kNumE * w;
@@ -777,7 +781,8 @@ int stage_x(qnb_context* c, const double* x) {
 int unstage_d(qnb_context* c, double* d) {
     size_t n = 3 * (size_t)c->natom;
     if (c->mixed) {
-        launch_apply_fixed(c->one());
+        launch_apply_fixed(c->one(), c->rows_pending ? 1 : 0);
+        c->rows_pending = false;
         c->launches++;
         TRY(check_launch());
     }
@@ -913,7 +918,14 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
             if (md) timed(c, K_WW, [&] { launch_rows_water(L); }), ++nl;
             timed(c, K_QW, [&] { launch_qw(L, mx); }), ++nl;
         }
-        if (md) timed(c, K_PP, [&] { launch_rows_solute(L, c->maxg); }), ++nl;
+        if (md) {
+            timed(c, K_PP, [&] {
+                launch_rows_solute(L, c->maxg);
+                launch_row_sums(L);
+            });
+            nl += 2;
+            c->rows_pending = true;   // frow holds this evaluation's row gradients
+        }
     } else {
         if (c->m.natom > c->m.nat_solute) {
             if (md) timed(c, K_WW, [&] { launch_ww(L, mx); }), ++nl;
@@ -1313,7 +1325,8 @@ int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, q
         c->launches += nl;
     }
     if (c->mixed) {
-        timed(c, K_APPLY, [&] { launch_apply_fixed(L); });
+        timed(c, K_APPLY, [&] { launch_apply_fixed(L, c->rows_pending ? 1 : 0); });
+        c->rows_pending = false;
         c->launches++;
     }
     TRY(check_launch());

@@ -109,6 +109,8 @@ struct DevState {
     double* x;           // [natom*3] coordinates (FP64, as qdyn holds them)
     double* d;           // [natom*3] gradient accumulator (FP64 mode target)
     float4* xq;          // [natom] FP32 (x,y,z,charge) for the mixed form
+    float* frow;         // [natom*3] mixed form: row-kernel gradient of each atom's own row (FP32)
+    float4* erow;        // [ncgp_solute+nwat] mixed form: row energies (pp el, vdw, pw el, vdw | ww el, vdw)
     unsigned long long* fix;   // [natom*3] fixed-point gradient (mixed form)
     double* e;           // [kNumE] FP64 energies
     unsigned long long* efix;  // [kNumE] fixed-point energies (mixed form)
@@ -178,7 +180,8 @@ void launch_pp(const Launch& L, int mixed);
 void launch_qp(const Launch& L, int mixed);
 void launch_nonbond_qq(const Launch& L, int mixed);
 void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed);
-void launch_apply_fixed(const Launch& L);
+void launch_apply_fixed(const Launch& L, int rows);
+void launch_row_sums(const Launch& L);
 
 // kernel classes timed by the optional event profiler
 enum { K_WW = 0, K_QW, K_PW, K_PP, K_QP, K_LRF_TAYLOR, K_QQ, K_RESTRAIN, K_WATPOL, K_PACK, K_APPLY,

@@ -1461,15 +1461,53 @@ __global__ void __launch_bounds__(256) k_lrf_taylor(DevModel m, const DevState* 
 }
 
 // mixed form: add the fixed-point gradient into d and clear it
-__global__ void k_apply_fixed(int n, const DevState* __restrict__ states) {
+// d += fixed-point gradient (cleared for the next evaluation), plus the rows'
+// FP32 gradient when the row kernels ran in this evaluation: they rewrite
+// every atom of every row each time, and atoms outside all rows stay 0
+__global__ void k_apply_fixed(int n, const DevState* __restrict__ states, int rows) {
     unsigned long long* __restrict__ fix = states[blockIdx.y].fix;
+    const float* __restrict__ frow = states[blockIdx.y].frow;
     double* __restrict__ d = states[blockIdx.y].d;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         long long v = (long long)fix[k];
-        if (v != 0) {
-            d[k] += (double)v * (1.0 / kFix);
-            fix[k] = 0ull;
+        double add = (double)v * (1.0 / kFix);
+        if (rows) add += (double)frow[k];
+        if (add != 0.0) d[k] += add;
+        if (v != 0) fix[k] = 0ull;
+    }
+}
+
+// Row energies of the mixed form summed in row order in FP64 (one block per
+// window, fixed reduction tree): the pp/pw/ww energy slots.
+__global__ void __launch_bounds__(256) k_row_sums(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.x];
+    __shared__ double red[6][256];
+    double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const int nrows = m.ncgp_solute + m.nwat;
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+        float4 e = s.erow[r];
+        if (r < m.ncgp_solute) {
+            a[0] += e.x; a[1] += e.y; a[2] += e.z; a[3] += e.w;
+        } else {
+            a[4] += e.x; a[5] += e.y;
         }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = a[k];
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {   // the only writer of these slots in the mixed form
+        s.e[E_PP_EL] += red[0][0];
+        s.e[E_PP_VDW] += red[1][0];
+        s.e[E_PW_EL] += red[2][0];
+        s.e[E_PW_VDW] += red[3][0];
+        s.e[E_WW_EL] += red[4][0];
+        s.e[E_WW_VDW] += red[5][0];
     }
 }
 
@@ -1965,14 +2003,11 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
     const DevState& s = states[blockIdx.y];
     const int wib = threadIdx.x >> 5;
     TypeTab lj = stage_types(m, sh_lj);
-    Acc<true> acc = make_acc<true>(s);
-    ESum<true> epel, epvdw, ewel, ewvdw;
     const float4* __restrict__ xq = s.xq;
     const float el14 = (float)m.el14;
     int lane = threadIdx.x & 31;
     for (int g = warp_id_global(); g < m.ncgp_solute; g += warps_total()) {
-        int npp = s.cnt_gp[g], npw = s.cnt_gw[g];
-        if (npp == 0 && npw == 0) continue;
+        int npp = s.cnt_gp[g], npw = s.cnt_gw[g];   // an empty row still writes its zeros
         int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
         int ta[MAXG];
         float4 xa[MAXG];
@@ -2072,27 +2107,24 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
             }
         }
         __syncwarp();   // sh_pw is refilled by the next row
-        epel.add(0.5f * rpel);
-        epvdw.add(0.5f * rpvdw);
-        ewel.add(rwel);
-        ewvdw.add(rwvdw);
-        // gradient: FP32 warp sums in a fixed order, one conversion per atom
+        // The row owns its atoms' pp and pw gradient and its energies: FP32
+        // warp sums in a fixed shuffle order, stored without atomics or
+        // conversions (k_apply_fixed and k_row_sums add them in FP64)
+        float e0 = warp_sum(0.5f * rpel), e1 = warp_sum(0.5f * rpvdw), e2 = warp_sum(rwel), e3 = warp_sum(rwvdw);
+        if (lane == 0) s.erow[g] = make_float4(e0, e1, e2, e3);
 #pragma unroll
         for (int a = 0; a < MAXG; ++a) {
             if (a >= n1) break;   // warp-uniform
             float v0 = warp_sum(f[a][0]), v1 = warp_sum(f[a][1]), v2 = warp_sum(f[a][2]);
-            if (lane == 0 && !qa[a]) {
+            if (lane == 0) {
                 int i = m.gatom[a0 + a];
-                atomicAdd(s.fix + 3 * i, to_fix(v0));
-                atomicAdd(s.fix + 3 * i + 1, to_fix(v1));
-                atomicAdd(s.fix + 3 * i + 2, to_fix(v2));
+                float* fr = s.frow + 3 * i;
+                fr[0] = qa[a] ? 0.f : v0;
+                fr[1] = qa[a] ? 0.f : v1;
+                fr[2] = qa[a] ? 0.f : v2;
             }
         }
     }
-    epel.flush(acc, E_PP_EL);
-    epvdw.flush(acc, E_PP_VDW);
-    ewel.flush(acc, E_PW_EL);
-    ewvdw.flush(acc, E_PW_VDW);
 }
 
 // water rows: ww (waters, SPC fast path as nonbond_ww_spc) and wp (solute
@@ -2105,14 +2137,11 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
     const DevState& s = states[blockIdx.y];
     const int wib = threadIdx.x >> 5;
     TypeTab lj = stage_types(m, sh_lj);
-    Acc<true> acc = make_acc<true>(s);
-    ESum<true> eel, evdw;
     const float4* __restrict__ xq = s.xq;
     int lane = threadIdx.x & 31;
     const int sa = m.sa;
     for (int w = warp_id_global(); w < m.nwat; w += warps_total()) {
-        int nww = s.cnt_ww[w], nwg = s.cnt_wg[w];
-        if (nww == 0 && nwg == 0) continue;
+        int nww = s.cnt_ww[w], nwg = s.cnt_wg[w];   // an empty row still writes its zeros
         int i0 = m.nat_solute + sa * w;
         float4 xa[kMaxSolv];
         float f[kMaxSolv][3];
@@ -2173,8 +2202,6 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
             cp_async_wait<0>();
             __syncwarp();
         }
-        eel.add(rel);
-        evdw.add(rvdw);
         for (int k = lane; k < nwg; k += kWarp) {
             int g = k < kRowChunk ? sh_wg[wib][k] : rg[k];
             for (int bb = m.gslot[g]; bb < m.gslot[g + 1]; ++bb) {
@@ -2193,19 +2220,21 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
             }
         }
         __syncwarp();   // sh_wg is refilled by the next row
+        // row gradient and energies stored as in k_rows_solute
+        float e0 = warp_sum(rel), e1 = warp_sum(rvdw);
+        if (lane == 0) s.erow[m.ncgp_solute + w] = make_float4(e0, e1, 0.f, 0.f);
 #pragma unroll
         for (int a = 0; a < kMaxSolv; ++a) {
             if (a >= sa) break;
             float v0 = warp_sum(f[a][0]), v1 = warp_sum(f[a][1]), v2 = warp_sum(f[a][2]);
             if (lane == 0) {
-                atomicAdd(s.fix + 3 * (i0 + a), to_fix(v0));
-                atomicAdd(s.fix + 3 * (i0 + a) + 1, to_fix(v1));
-                atomicAdd(s.fix + 3 * (i0 + a) + 2, to_fix(v2));
+                float* fr = s.frow + 3 * (i0 + a);
+                fr[0] = v0;
+                fr[1] = v1;
+                fr[2] = v2;
             }
         }
     }
-    eel.flush(acc, E_WW_EL);
-    evdw.flush(acc, E_WW_VDW);
 }
 
 // =============================================================================
@@ -2365,9 +2394,13 @@ void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed) {
     if (mixed) k_lrf_taylor<true><<<g, 64, 0, L.st>>>(L.m, L.ds, iwhich);
     else k_lrf_taylor<false><<<g, 64, 0, L.st>>>(L.m, L.ds, iwhich);
 }
-void launch_apply_fixed(const Launch& L) {
+void launch_apply_fixed(const Launch& L, int rows) {
     int n = 3 * L.m.natom;
-    k_apply_fixed<<<grid_for(n, 256, 4, L.nwin), 256, 0, L.st>>>(n, L.ds);
+    k_apply_fixed<<<grid_for(n, 256, 16, L.nwin), 256, 0, L.st>>>(n, L.ds, rows);
+}
+void launch_row_sums(const Launch& L) {
+    if (L.m.ncgp_solute + L.m.nwat == 0) return;
+    k_row_sums<<<L.nwin, 256, 0, L.st>>>(L.m, L.ds);
 }
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv) {
