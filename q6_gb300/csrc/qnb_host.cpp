@@ -97,6 +97,7 @@ struct qnb_context {
     Cut last_cut{};
     int maxg = 1;                  // largest solute charge group
     bool rows_pending = false;     // mixed form: frow not yet added into d
+    bool qenv_pending = false;     // mixed form: fq not yet added into d
     DevState* d_diag = nullptr;    // scratch device state for inspection builds
     std::vector<int> counts;       // [nwin][C_NUM] after the last build
     SolventDev solv{};
@@ -700,6 +701,8 @@ int alloc_state(qnb_context* c) {
         TRY(c->alloc(&s.xq, (size_t)m.natom));
         TRY(c->alloc(&s.frow, (size_t)3 * m.natom));
         CU(cudaMemset(s.frow, 0, sizeof(float) * 3 * m.natom));   // atoms outside every row stay 0
+        TRY(c->alloc(&s.fq, (size_t)3 * m.natom));
+        CU(cudaMemset(s.fq, 0, sizeof(float) * 3 * m.natom));     // atoms outside the Q lists stay 0
         TRY(c->alloc(&s.erow, (size_t)std::max(1, m.ncgp_solute + m.nwat)));
         TRY(c->alloc(&s.fix, n3));
         s.e = c->e_all + (size_t)kNumE * w;
@@ -781,8 +784,8 @@ int stage_x(qnb_context* c, const double* x) {
 int unstage_d(qnb_context* c, double* d) {
     size_t n = 3 * (size_t)c->natom;
     if (c->mixed) {
-        launch_apply_fixed(c->one(), c->rows_pending ? 1 : 0);
-        c->rows_pending = false;
+        launch_apply_fixed(c->one(), c->rows_pending ? 1 : 0, c->qenv_pending ? 1 : 0);
+        c->rows_pending = c->qenv_pending = false;
         c->launches++;
         TRY(check_launch());
     }
@@ -862,20 +865,22 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
     for (int attempt = 0; attempt < 4; ++attempt) {
         unsigned keep = (do_qp ? 0u : 1u << C_QP) | (do_qw ? 0u : 1u << C_QW);   // everything else restarts
         launch_reset_counts(L, keep);
+        int nl = 2;   // reset + pack
         timed(c, K_BUILD, [&] {
             launch_pack(L);
-            if (c->use_lrf) launch_group_centres(L);
+            if (c->use_lrf) launch_group_centres(L), ++nl;
             if (c->mixed) {
-                launch_build_rows(L, cut);
+                launch_build_rows(L, cut), ++nl;
             } else {
-                launch_build_pp(L, cut);
-                launch_build_pw(L, cut);
-                launch_build_ww(L, cut);
+                launch_build_pp(L, cut), nl += 2;
+                launch_build_pw(L, cut), ++nl;
+                launch_build_ww(L, cut), ++nl;
             }
-            if (do_qp) launch_build_qp(L, c->d_qnear, cut.rcq2);
-            if (do_qw) launch_build_qw(L, cut);
+            if (do_qp) launch_build_qp(L, c->d_qnear, cut.rcq2), ++nl;
+            if (do_qw) launch_build_qw(L, cut), ++nl;
+            if (c->mixed && (do_qp || do_qw)) launch_clear_fq(L), ++nl;   // atoms may leave the Q lists
         });
-        c->launches += 7 + (c->use_lrf ? 1 : 0);
+        c->launches += nl + (c->use_lrf ? 1 : 0);
         if (c->use_lrf) {
             timed(c, K_LRF_BUILD, [&] { launch_lrf_accumulate(L, cut, c->mixed, c->d_lrf_src); });
             c->launches++;
@@ -935,6 +940,7 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
         if (md) timed(c, K_PP, [&] { launch_pp(L, mx); }), ++nl;
     }
     timed(c, K_QP, [&] { launch_qp(L, mx); }), ++nl;
+    if (mx) c->qenv_pending = true;   // fq holds this evaluation's Q-environment gradients
     if (c->use_lrf && md) {
         timed(c, K_LRF_TAYLOR, [&] { launch_lrf_taylor(L, c->d_iwhich, mx); });
         ++nl;
@@ -1325,8 +1331,8 @@ int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, q
         c->launches += nl;
     }
     if (c->mixed) {
-        timed(c, K_APPLY, [&] { launch_apply_fixed(L, c->rows_pending ? 1 : 0); });
-        c->rows_pending = false;
+        timed(c, K_APPLY, [&] { launch_apply_fixed(L, c->rows_pending ? 1 : 0, c->qenv_pending ? 1 : 0); });
+        c->rows_pending = c->qenv_pending = false;
         c->launches++;
     }
     TRY(check_launch());

@@ -111,6 +111,7 @@ struct DevState {
     float4* xq;          // [natom] FP32 (x,y,z,charge) for the mixed form
     float* frow;         // [natom*3] mixed form: row-kernel gradient of each atom's own row (FP32)
     float4* erow;        // [ncgp_solute+nwat] mixed form: row energies (pp el, vdw, pw el, vdw | ww el, vdw)
+    float* fq;           // [natom*3] mixed form: Q-environment gradient of each listed qp atom / qw water
     unsigned long long* fix;   // [natom*3] fixed-point gradient (mixed form)
     double* e;           // [kNumE] FP64 energies
     unsigned long long* efix;  // [kNumE] fixed-point energies (mixed form)
@@ -180,7 +181,8 @@ void launch_pp(const Launch& L, int mixed);
 void launch_qp(const Launch& L, int mixed);
 void launch_nonbond_qq(const Launch& L, int mixed);
 void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed);
-void launch_apply_fixed(const Launch& L, int rows);
+void launch_apply_fixed(const Launch& L, int rows, int qenv);
+void launch_clear_fq(const Launch& L);
 void launch_row_sums(const Launch& L);
 
 // kernel classes timed by the optional event profiler

@@ -1252,9 +1252,19 @@ __global__ void __launch_bounds__(kQBlock) k_qenv(DevModel m, const DevState* __
                 gj[1] += ty * dvs;
                 gj[2] += tz * dvs;
             }
-            // environment atom gradient: sum over the warp's Q atoms
+            // environment atom gradient: sum over the warp's Q atoms.  Each
+            // atom is in one unit of the list, so the mixed form stores its
+            // FP32 sum (k_apply_fixed adds it) instead of a converted atomic
             T v0 = warp_sum(gj[0]), v1 = warp_sum(gj[1]), v2 = warp_sum(gj[2]);
-            if (lane == 0) acc.grad(j, v0, v1, v2);
+            if (lane == 0) {
+                if constexpr (MIX) {
+                    s.fq[3 * j] = v0;
+                    s.fq[3 * j + 1] = v1;
+                    s.fq[3 * j + 2] = v2;
+                } else {
+                    acc.grad(j, v0, v1, v2);
+                }
+            }
         }
       }
 #pragma unroll
@@ -1462,16 +1472,19 @@ __global__ void __launch_bounds__(256) k_lrf_taylor(DevModel m, const DevState* 
 
 // mixed form: add the fixed-point gradient into d and clear it
 // d += fixed-point gradient (cleared for the next evaluation), plus the rows'
-// FP32 gradient when the row kernels ran in this evaluation: they rewrite
-// every atom of every row each time, and atoms outside all rows stay 0
-__global__ void k_apply_fixed(int n, const DevState* __restrict__ states, int rows) {
+// and the Q-environment FP32 gradients when those kernels ran in this
+// evaluation: they rewrite every atom they own each time, and atoms they do
+// not own stay 0 (fq is cleared when the Q lists are rebuilt)
+__global__ void k_apply_fixed(int n, const DevState* __restrict__ states, int rows, int qenv) {
     unsigned long long* __restrict__ fix = states[blockIdx.y].fix;
     const float* __restrict__ frow = states[blockIdx.y].frow;
+    const float* __restrict__ fq = states[blockIdx.y].fq;
     double* __restrict__ d = states[blockIdx.y].d;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         long long v = (long long)fix[k];
         double add = (double)v * (1.0 / kFix);
         if (rows) add += (double)frow[k];
+        if (qenv) add += (double)fq[k];
         if (add != 0.0) d[k] += add;
         if (v != 0) fix[k] = 0ull;
     }
@@ -2394,9 +2407,17 @@ void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed) {
     if (mixed) k_lrf_taylor<true><<<g, 64, 0, L.st>>>(L.m, L.ds, iwhich);
     else k_lrf_taylor<false><<<g, 64, 0, L.st>>>(L.m, L.ds, iwhich);
 }
-void launch_apply_fixed(const Launch& L, int rows) {
+void launch_apply_fixed(const Launch& L, int rows, int qenv) {
     int n = 3 * L.m.natom;
-    k_apply_fixed<<<grid_for(n, 256, 16, L.nwin), 256, 0, L.st>>>(n, L.ds, rows);
+    k_apply_fixed<<<grid_for(n, 256, 16, L.nwin), 256, 0, L.st>>>(n, L.ds, rows, qenv);
+}
+__global__ void k_clear_fq(int n, const DevState* __restrict__ states) {
+    float* __restrict__ fq = states[blockIdx.y].fq;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) fq[k] = 0.f;
+}
+void launch_clear_fq(const Launch& L) {
+    int n = 3 * L.m.natom;
+    k_clear_fq<<<grid_for(n, 256, 4, L.nwin), 256, 0, L.st>>>(n, L.ds);
 }
 void launch_row_sums(const Launch& L) {
     if (L.m.ncgp_solute + L.m.nwat == 0) return;
