@@ -1960,7 +1960,9 @@ __device__ __forceinline__ void pair_f(float4 a, float4 b, float A, float B, flo
 }
 
 // type-pair LJ parameters (code ljcod: A,B; code 3: A,B) staged in shared
-// memory when the type table is small
+// memory when the type table is small; the kernels take it as dynamic shared
+// memory of exactly natyps^2 entries, leaving the rest of the SM's 256 KB to
+// the L1 cache that serves the partner gathers
 struct TypeTab {
     const float4* t;
     int nt;
@@ -2009,7 +2011,7 @@ constexpr int rows_min_blocks() {
 }
 template <int MAXG>
 __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(DevModel m, const DevState* __restrict__ states) {
-    __shared__ float4 sh_lj[kMaxTypesShared * kMaxTypesShared];
+    extern __shared__ float4 sh_lj[];   // natyps^2 type-pair table (dynamic: only its real size)
     __shared__ __align__(16) uint2 sh_pp[4][2][kRowChunk];   // per warp: double-buffered pp entries
     __shared__ __align__(16) int sh_pw[4][kRowChunk];        // per warp: first chunk of pw entries
     constexpr bool kTypeInEntry = MAXG <= 8;
@@ -2070,10 +2072,11 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
             int j = (int)(e.x & 0x0fffffffu);
             float4 xb = xq[j];
             int tj = kTypeInEntry ? (int)(e.y >> 16) : m.iac[j];
+            const unsigned kinds = kTypeInEntry ? (e.y & 0xffffu) : e.y;
 #pragma unroll
             for (int a = 0; a < MAXG; ++a) {
                 if (qa[a]) continue;
-                unsigned kind = (e.y >> (2 * a)) & 3u;
+                unsigned kind = (kinds >> (2 * a)) & 3u;
                 if (kind == 1u) continue;
                 float4 p = lj(ta[a], tj);
                 bool is14 = kind == 3u;
@@ -2144,7 +2147,7 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
 // groups) gradient of the water's atoms
 template <bool SPC>
 __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevState* __restrict__ states) {
-    __shared__ float4 sh_lj[kMaxTypesShared * kMaxTypesShared];
+    extern __shared__ float4 sh_lj[];   // natyps^2 type-pair table (dynamic: only its real size)
     __shared__ __align__(16) int sh_ww[4][2][kRowChunk];   // per warp: double-buffered ww entries
     __shared__ __align__(16) int sh_wg[4][kRowChunk];      // per warp: first chunk of wp entries
     const DevState& s = states[blockIdx.y];
@@ -2344,19 +2347,24 @@ void launch_build_rows(const Launch& L, const Cut& c) {
     if (nrows == 0) return;
     k_build_rows<<<grid_for((int64_t)nrows * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c);
 }
+int lj_smem(const DevModel& m) {
+    return m.natyps <= kMaxTypesShared ? (int)(m.natyps * m.natyps * sizeof(float4)) : 0;
+}
 void launch_rows_solute(const Launch& L, int maxg) {
     if (L.m.ncgp_solute == 0) return;
     dim3 g = grid_for((int64_t)L.m.ncgp_solute * 32, 128, 16, L.nwin);
-    if (maxg <= 4) k_rows_solute<4><<<g, 128, 0, L.st>>>(L.m, L.ds);
-    else if (maxg <= 6) k_rows_solute<6><<<g, 128, 0, L.st>>>(L.m, L.ds);
-    else if (maxg <= 8) k_rows_solute<8><<<g, 128, 0, L.st>>>(L.m, L.ds);
-    else k_rows_solute<16><<<g, 128, 0, L.st>>>(L.m, L.ds);
+    int sm = lj_smem(L.m);
+    if (maxg <= 4) k_rows_solute<4><<<g, 128, sm, L.st>>>(L.m, L.ds);
+    else if (maxg <= 6) k_rows_solute<6><<<g, 128, sm, L.st>>>(L.m, L.ds);
+    else if (maxg <= 8) k_rows_solute<8><<<g, 128, sm, L.st>>>(L.m, L.ds);
+    else k_rows_solute<16><<<g, 128, sm, L.st>>>(L.m, L.ds);
 }
 void launch_rows_water(const Launch& L) {
     if (L.m.nwat == 0) return;
     dim3 g = grid_for((int64_t)L.m.nwat * 32, 128, 16, L.nwin);
-    if (L.m.spc) k_rows_water<true><<<g, 128, 0, L.st>>>(L.m, L.ds);
-    else k_rows_water<false><<<g, 128, 0, L.st>>>(L.m, L.ds);
+    int sm = lj_smem(L.m);
+    if (L.m.spc) k_rows_water<true><<<g, 128, sm, L.st>>>(L.m, L.ds);
+    else k_rows_water<false><<<g, 128, sm, L.st>>>(L.m, L.ds);
 }
 void launch_ww(const Launch& L, int mixed) {
     if (L.m.nwat == 0) return;
