@@ -223,6 +223,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     m.nqat = nq;
     m.S = S;
     m.el14 = t->el14_scale;
+    m.el14f = (float)m.el14;
     m.use_lrf = c->use_lrf;
     m.any_atom = t->iuse_switch_atom == 0;   // nbpplis2/nbpwlis2/nbqplis2 group tests
     m.spc = (t->ivdw_rule == 1 && t->solvent_type == 0) ? 1 : 0;   // src/potene.f90:347-349

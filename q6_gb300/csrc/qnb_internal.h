@@ -56,6 +56,7 @@ struct DevModel {
     int any_atom;      // 1: a group pair is inside when any atom pair is (switch atoms off)
     int type_in_entry; // solute row entries carry the partner's LJ type (groups of <= 8 atoms)
     double el14;
+    float el14f;       // el14 rounded to FP32 once, for the FP32 pair kernels
     const int* iac;
     const double* crg;
     const int* iqatom;          // -1 or Q index

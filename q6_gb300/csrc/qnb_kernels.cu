@@ -1055,7 +1055,7 @@ __global__ void __launch_bounds__(256) k_pp(DevModel m, const DevState* __restri
             float2 ab = m.ljf[t];
             float4 xi = s.xq[i], xj = s.xq[j];
             float el = xi.w * xj.w;
-            if (code == 3) el *= (float)m.el14;
+            if (code == 3) el *= m.el14f;
             PairF q = nbe_f(xi, xj, ab.x, ab.y, el, true);
             acc.grad(i, -q.tx * q.dv, -q.ty * q.dv, -q.tz * q.dv);
             acc.grad(j, q.tx * q.dv, q.ty * q.dv, q.tz * q.dv);
@@ -2019,7 +2019,10 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
     const int wib = threadIdx.x >> 5;
     TypeTab lj = stage_types(m, sh_lj);
     const float4* __restrict__ xq = s.xq;
-    const float el14 = (float)m.el14;
+    // m.el14f, not (float)m.el14: under register pressure the compiler may
+    // rematerialise a double-to-float conversion of the parameter inside the
+    // pair loop, and that conversion runs on the narrow FP64 pipe
+    const float el14 = m.el14f;
     int lane = threadIdx.x & 31;
     for (int g = warp_id_global(); g < m.ncgp_solute; g += warps_total()) {
         int npp = s.cnt_gp[g], npw = s.cnt_gw[g];   // an empty row still writes its zeros
