@@ -316,46 +316,88 @@ def read_traffic(kernel):
 
 
 def run_e2e(args, s, sp, lams, prec, local):
-    """Same metric through the host-buffer calls a Fortran shim makes, one
-    context per window as one qdyn process per window would hold:
-    make_pair_lists (every 25th step), pot_energy_nonbonds, nonbond_qq,
-    restrain_solvent, watpol; each copies x in and the gradient out."""
+    """Same metric end to end through the public C ABI with host buffers.
+
+    Batched path (the headline): one context holds every window, as a driver
+    running all lambda windows in one process would; each step copies all
+    windows' coordinates in from pinned host memory (qnb_upload_coordinates),
+    rebuilds the lists every 25th step, evaluates (qnb_compute_dev, energies
+    read back) and copies all gradients out to pinned memory
+    (qnb_download_gradient).
+
+    Drop-in path (reported beside it): one context per window, as one qdyn
+    process per window holds, through the calls the Fortran shim makes
+    (make_pair_lists, pot_energy_nonbonds, nonbond_qq, restrain_solvent,
+    watpol), each copying x in and the gradient out."""
     import numpy as np
+    import torch
     from q6_gb300.qnb import NonbondedEngine
     from q6_gb300.system import lambdas_for_window
-    nwin = min(args.windows, 8)
+    nwin = args.windows
     steps = max(4, min(args.steps, 50))
-    engs = []
+    eng = NonbondedEngine(s, precision=prec, device=local, windows=nwin)
+    eng.set_solvent_params(sp)
     for w in range(nwin):
+        eng.set_lambda(lambdas_for_window(lams[w], s.nstates), window=w)
+    shape = (nwin, s.natom, 3)
+    x_pin = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    d_pin = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    rng = np.random.default_rng(77)
+    x_pin[:] = np.stack([s.x + rng.normal(0.0, 0.01, size=s.x.shape) for _ in range(nwin)])
+
+    def step(k):
+        eng.set_coordinates_dev(x_pin)                    # H2D, all windows
+        if k % NBCYCLE == 0:
+            eng.make_pair_lists_dev(**CUT)
+        eng.compute_dev(Tfree=300.0, istep=k, sync=True)  # energies D2H
+        eng.gradient_dev(out=d_pin)                       # gradients D2H
+
+    for k in range(3):
+        step(k)
+    t0 = time.perf_counter()
+    for k in range(3, 3 + steps):
+        step(k)
+    dt = time.perf_counter() - t0
+    eng.close()
+    nbytes = s.x.nbytes * nwin
+    ebytes = nwin * (7 + 6 * s.nstates + 2) * 8   # E, EQ and restraint records
+    out = {"value": round(nwin * steps / dt, 2), "unit": "steps/s", "h2d_bytes_per_step": int(nbytes),
+           "d2h_bytes_per_step": int(nbytes + ebytes), "windows": nwin, "steps": steps,
+           "path": "qnb_upload_coordinates (pinned) + qnb_make_pair_lists_dev every 25th step + "
+                   "qnb_compute_dev(sync) + qnb_download_gradient (pinned), one context holding all windows"}
+
+    # drop-in path: one single-window context per window
+    nw1 = min(nwin, 8)
+    engs = []
+    for w in range(nw1):
         e = NonbondedEngine(s, precision=prec, device=local)
         e.set_solvent_params(sp)
         e.set_lambda(lambdas_for_window(lams[w], s.nstates))
         engs.append(e)
-    xs = [s.x.copy() for _ in range(nwin)]
-    ds = [np.zeros_like(s.x) for _ in range(nwin)]
-    for w, e in enumerate(engs):       # warm-up: first list build
+    xs = [s.x.copy() for _ in range(nw1)]
+    ds = [np.zeros_like(s.x) for _ in range(nw1)]
+    for w, e in enumerate(engs):
         e.make_pair_lists(xs[w], **CUT)
     t0 = time.perf_counter()
     for k in range(steps):
-        for w, eng in enumerate(engs):
+        for w, e1 in enumerate(engs):
             x, d = xs[w], ds[w]
             d[:] = 0.0
             if k % NBCYCLE == 0:
-                eng.make_pair_lists(x, **CUT)
-            d, E, EQ = eng.pot_energy_nonbonds(x, d)
-            d, EQ = eng.nonbond_qq(x, d, EQ)
-            eng.restrain_solvent(x, d, 300.0)
-            eng.watpol(x, d, k)
-    dt = time.perf_counter() - t0
-    for e in engs:
-        e.close()
-    nbytes = s.x.nbytes
-    h2d = nbytes * (4 + 1.0 / NBCYCLE)
-    d2h = nbytes * 4
-    return {"value": round(nwin * steps / dt, 2), "unit": "steps/s", "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "windows": nwin, "steps": steps,
-            "path": "qnb_make_pair_lists/qnb_pot_energy_nonbonds/qnb_nonbond_qq/qnb_restrain_solvent/"
-                    "qnb_watpol with host buffers, one context per window"}
+                e1.make_pair_lists(x, **CUT)
+            d, E, EQ = e1.pot_energy_nonbonds(x, d)
+            d, EQ = e1.nonbond_qq(x, d, EQ)
+            e1.restrain_solvent(x, d, 300.0)
+            e1.watpol(x, d, k)
+    dt1 = time.perf_counter() - t0
+    for e1 in engs:
+        e1.close()
+    out["drop_in"] = {"value": round(nw1 * steps / dt1, 2), "unit": "steps/s", "windows": nw1,
+                      "h2d_bytes_per_step": int(s.x.nbytes * (4 + 1.0 / NBCYCLE)),
+                      "d2h_bytes_per_step": int(s.x.nbytes * 4),
+                      "path": "qnb_make_pair_lists/qnb_pot_energy_nonbonds/qnb_nonbond_qq/qnb_restrain_solvent/"
+                              "qnb_watpol with host buffers, one context per window, windows in sequence"}
+    return out
 
 
 def fp64_compare(args, s, sp, lams, local):
@@ -386,25 +428,32 @@ def fp64_compare(args, s, sp, lams, local):
 
 
 def _oracle_window(payload):
-    """One lambda window of the CPU restatement: `steps` nonbonded steps with a
-    list rebuild every 25th step.  Returns (steps, seconds)."""
+    """One lambda window of the CPU restatement: `warmup` untimed steps, then
+    `steps` timed nonbonded steps, with a list rebuild every 25th step.
+    Returns (steps, seconds)."""
     import pickle
     sys.path.insert(0, ROOT)
     from oracle.oracle import Oracle
-    s, sp_bytes, lam, steps = pickle.loads(payload)
+    s, sp_bytes, lam, steps, warmup = pickle.loads(payload)
     from q6_gb300.system import QnbSolventParams, lambdas_for_window
     sp = QnbSolventParams.from_buffer_copy(sp_bytes)
     o = Oracle(s)
     o.set_solvent_params(sp)
     o.set_lambda(lambdas_for_window(lam, s.nstates))
-    t0 = time.perf_counter()
-    for k in range(steps):
+
+    def step(k):
         if k % NBCYCLE == 0:
             o.make_pair_lists(s.x, **CUT)
         d, E, EQ = o.pot_energy_nonbonds(s.x)
         d, EQ = o.nonbond_qq(s.x, d, EQ)
         o.restrain_solvent(s.x, d, 300.0)
         o.watpol(s.x, d, k)
+
+    for k in range(warmup):
+        step(k)
+    t0 = time.perf_counter()
+    for k in range(warmup, warmup + steps):
+        step(k)
     return steps, time.perf_counter() - t0
 
 
@@ -414,10 +463,11 @@ def cpu_baseline(s, sp, args):
     import pickle
     from oracle import oracle as orc
     orc.build()
-    steps = 2 * NBCYCLE
-    n, dt = _oracle_window(pickle.dumps((s, bytes(sp), 0.5, steps)))
+    steps, warmup = 2 * NBCYCLE, 3
+    n, dt = _oracle_window(pickle.dumps((s, bytes(sp), 0.5, steps, warmup)))
     return {"value": round(n / dt, 4), "unit": "steps/s", "cores": 1, "kind": "port",
-            "sample": f"1 window x {steps} steps (2 list builds), serial C FP64 restatement, -O2"}
+            "sample": f"1 window x {steps} timed steps after {warmup} warm-up steps (2 list builds), "
+                      "serial C FP64 restatement, -O2"}
 
 
 def run_reference(args, rank, world):
@@ -432,29 +482,36 @@ def run_reference(args, rank, world):
     s = make_window_system()
     sp = default_solvent_params(s)
     cores = os.cpu_count() or 1
-    nwin = min(args.windows, cores)
-    lams = window_lambdas(args.windows)[:nwin]
-    steps = max(NBCYCLE, min(args.steps, 50))
-    payloads = [pickle.dumps((s, bytes(sp), lam, steps)) for lam in lams]
+    nwin = args.windows                      # the same windows as the GPU arm
+    lams = window_lambdas(nwin)
+    # --steps timed steps per window after --warmup untimed ones (an oracle
+    # step takes about 30 ms on one core, so K = 100 stays a few seconds)
+    steps, warmup = args.steps, args.warmup
+    payloads = [pickle.dumps((s, bytes(sp), lam, steps, warmup)) for lam in lams]
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
-    with ctx.Pool(nwin) as pool:
-        res = pool.map(_oracle_window, payloads)
+    nproc = min(nwin, cores)
+    with ctx.Pool(nproc) as pool:
+        res = pool.map(_oracle_window, payloads, chunksize=1)
     wall = time.perf_counter() - t0
-    # per-window rates; wall time includes process start-up, so use the
-    # slowest window's own compute time
-    slowest = max(r[1] for r in res)
-    value = sum(r[0] for r in res) / slowest
+    # throughput of the host's cores: all windows' timed steps over their
+    # compute time spread evenly across the processes (process start-up and
+    # the untimed warm-up steps are left out)
+    busy = sum(r[1] for r in res) / nproc
+    slowest = busy
+    value = sum(r[0] for r in res) / busy
     out = {"metric": METRIC, "value": round(value, 4), "unit": "steps/s", "n_gpus": world,
-           "steps": steps, "warmup": 0, "ms_per_step": round(slowest / steps * 1e3, 3),
+           "steps": steps, "warmup": warmup, "ms_per_step": round(slowest / steps * 1e3, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "impl": "reference",
            "dtype": "f64", "data": "synthetic seeded sphere (no dataset)",
            "config": {"workload": f"{nwin} lambda windows x R25 2-state sphere ({s.natom} atoms)",
                       "windows": nwin, "nbcycle": NBCYCLE, "cutoffs": CUT,
                       "note": "Q6 qdyn (Fortran) cannot be built on this pool (no gfortran); the "
-                              "serial C restatement in oracle/ runs one process per window"},
-           "cpu_baseline": {"value": round(value, 4), "unit": "steps/s", "cores": nwin, "kind": "port",
-                            "sample": f"{nwin} windows x {steps} steps, one process per window"},
+                              "serial C restatement in oracle/ runs each window in its own process, "
+                              "as qdyn runs one process per window, on all host cores"},
+           "cpu_baseline": {"value": round(value, 4), "unit": "steps/s", "cores": nproc, "kind": "port",
+                            "sample": f"{nwin} windows x {steps} timed steps after {warmup} warm-up steps, "
+                                      f"on {nproc} processes"},
            "e2e": {"value": round(value, 4), "unit": "steps/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0},
            "wall_s": round(wall, 2)}

@@ -253,9 +253,12 @@ class NonbondedEngine:
         assert xa.size == self.nwin * self.s.natom * 3
         self._check(self.lib.qnb_upload_coordinates(self.h, _p(xa)))
 
-    def gradient_dev(self, clear=True):
-        """Gradient accumulators of all windows (nwin x natom x 3)."""
-        out = np.zeros((self.nwin, self.s.natom, 3))
+    def gradient_dev(self, clear=True, out=None):
+        """Gradient accumulators of all windows (nwin x natom x 3), into `out`
+        (a C-contiguous float64 array, e.g. a view of pinned memory) if given."""
+        if out is None:
+            out = np.zeros((self.nwin, self.s.natom, 3))
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.nwin * self.s.natom * 3
         self._check(self.lib.qnb_download_gradient(self.h, _p(out), int(clear)))
         return out
 
