@@ -253,18 +253,40 @@ def _rand_rot(rng):
 
 
 def _grow_tree(rng, n, rmax, bond=1.5, clash=2.0, max_deg=4):
+    """Random tree of `n` atoms with `bond` bonds inside radius `rmax`, no two
+    atoms closer than `clash`.  Compact growth: of a few random open atoms,
+    the one nearest the centre is extended, so the solute fills a core and
+    water the outer shell.  Atoms are then numbered in depth-first order from
+    the root, so runs of consecutive atoms are bonded neighbourhoods (charge
+    groups cut from them are spatially compact, as in real topologies)."""
+    if n == 0:
+        return np.zeros((0, 3)), np.zeros((0, 2), dtype=np.int64)
     pos = np.zeros((n, 3))
     parent = -np.ones(n, dtype=np.int64)
     deg = np.zeros(n, dtype=np.int64)
     fails = np.zeros(n, dtype=np.int64)
+    cells: dict = {}
+
+    def cell(c):
+        return (int(math.floor(c[0] / clash)), int(math.floor(c[1] / clash)), int(math.floor(c[2] / clash)))
+
+    def clashes(c, skip):
+        cx, cy, cz = cell(c)
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    for j in cells.get((cx + dx, cy + dy, cz + dz), ()):
+                        if j != skip and np.sum((pos[j] - c) ** 2) < clash * clash:
+                            return True
+        return False
+
+    cells.setdefault(cell(pos[0]), []).append(0)
     k = 1
     tries = 0
     while k < n:
         tries += 1
         if tries > 200 * n:
             raise RuntimeError("solute growth failed: sphere too small")
-        # compact growth: of a few random open atoms, extend the one nearest
-        # the centre, so the solute fills a core and water the outer shell
         cand = rng.integers(0, k, size=6)
         cand = cand[deg[cand] < max_deg]
         if cand.size == 0:
@@ -276,19 +298,56 @@ def _grow_tree(rng, n, rmax, bond=1.5, clash=2.0, max_deg=4):
         v = rng.normal(size=3)
         v /= np.linalg.norm(v)
         c = pos[p] + bond * v
-        if np.linalg.norm(c) > rmax:
-            continue
-        dd = np.linalg.norm(pos[:k] - c, axis=1)
-        dd[p] = 99.0
-        if np.any(dd < clash):
+        if np.linalg.norm(c) > rmax or clashes(c, p):
             continue
         pos[k] = c
+        cells.setdefault(cell(c), []).append(k)
         parent[k] = p
         deg[p] += 1
         deg[k] = 1
         k += 1
-    bonds = np.array([(parent[i], i) for i in range(1, n)], dtype=np.int64).reshape(-1, 2)
+    # depth-first numbering from the root (children in creation order)
+    children = [[] for _ in range(n)]
+    for i in range(1, n):
+        children[parent[i]].append(i)
+    order, stack = [], [0]
+    while stack:
+        i = stack.pop()
+        order.append(i)
+        stack.extend(reversed(children[i]))
+    new_of = np.empty(n, dtype=np.int64)
+    new_of[np.array(order)] = np.arange(n)
+    pos = pos[np.array(order)]
+    bonds = np.array([(new_of[parent[i]], new_of[i]) for i in range(1, n)], dtype=np.int64).reshape(-1, 2)
     return pos, bonds
+
+
+def _compact_groups(rng, pos, sizes_range, reach=4.0):
+    """Charge groups of spatially adjacent atoms: walk the atoms in order and
+    give each unassigned atom a group of a drawn size (sizes_range), filled
+    with its nearest unassigned atoms within `reach`.  Returns the atom order
+    with groups consecutive, and the group sizes."""
+    n = len(pos)
+    cells: dict = {}
+    key = lambda c: (int(math.floor(c[0] / reach)), int(math.floor(c[1] / reach)), int(math.floor(c[2] / reach)))
+    for i in range(n):
+        cells.setdefault(key(pos[i]), []).append(i)
+    taken = np.zeros(n, dtype=bool)
+    order, sizes = [], []
+    for a in range(n):
+        if taken[a]:
+            continue
+        g = int(rng.integers(sizes_range[0], sizes_range[1] + 1))
+        cx, cy, cz = key(pos[a])
+        near = [j for dx in (-1, 0, 1) for dy in (-1, 0, 1) for dz in (-1, 0, 1)
+                for j in cells.get((cx + dx, cy + dy, cz + dz), ()) if j != a and not taken[j]]
+        near = [j for j in near if np.sum((pos[j] - pos[a]) ** 2) <= reach * reach]
+        near.sort(key=lambda j: (float(np.sum((pos[j] - pos[a]) ** 2)), j))
+        members = [a] + near[:g - 1]
+        taken[members] = True
+        order.extend(members)
+        sizes.append(len(members))
+    return np.array(order, dtype=np.int64), sizes
 
 
 def _graph_dist(n, bonds, maxd=3):
@@ -343,16 +402,13 @@ def make_system(R: float = 15.0, n_solute: int = 20, group_sizes=(3, 5), ntypes:
 
     # ---- solute -----------------------------------------------------------
     pos, bonds = _grow_tree(rng, n_solute, rmax=max(R - 2.0, 3.0))
+    # charge groups of adjacent atoms, numbered consecutively
+    order, sizes = _compact_groups(rng, pos, group_sizes) if n_solute else (np.zeros(0, np.int64), [])
+    new_of = np.empty(n_solute, dtype=np.int64)
+    new_of[order] = np.arange(n_solute)
+    pos = pos[order]
+    bonds = np.sort(new_of[bonds], axis=1) if len(bonds) else bonds
     iac_s = rng.integers(0, ntypes, size=n_solute)
-    sizes = []
-    left = n_solute
-    while left > 0:
-        g = int(rng.integers(group_sizes[0], group_sizes[1] + 1))
-        g = min(g, left)
-        if left - g in (1, 2) and left > group_sizes[1]:
-            g = left - group_sizes[0]
-        sizes.append(g)
-        left -= g
     crg_s = np.zeros(n_solute)
     cgp_first, cgp_last, cgp_sw = [], [], []
     k = 0
