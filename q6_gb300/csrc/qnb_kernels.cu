@@ -58,10 +58,30 @@ __device__ __forceinline__ int warp_append(int* counter, int n) {
 
 // ---- accumulation back-ends -------------------------------------------------
 // v * 2^32 rounded to the nearest integer (ties to even) as a 64-bit two's
-// complement value.  The float form uses the hardware conversion: measured,
-// its issue cost in the FP32 kernels is below that of an integer rebuild.
+// complement value.  to_fix uses the hardware conversion, which executes on
+// the FP64 pipe; to_fix_alu builds the same value from the IEEE-754 fields
+// with integer instructions (saturated like cvt.rni.s64.f32, NaN gives 0),
+// for kernels whose FP64 pipe is the bottleneck.  Which one pays is measured
+// per kernel.
 __device__ __forceinline__ unsigned long long to_fix(float v) {
     return (unsigned long long)__float2ll_rn(v * kFixF);
+}
+__device__ __forceinline__ unsigned long long to_fix_alu(float v) {
+    unsigned u = __float_as_uint(v);
+    int e = (int)((u >> 23) & 0xffu);
+    unsigned m = (u & 0x7fffffu) | 0x800000u;
+    int sh = e - 118;                     // v * 2^32 = m * 2^(e - 127 - 23 + 32)
+    int ls = min(max(sh, 0), 39);
+    int k = min(max(-sh, 0), 31);
+    unsigned q = m >> k;
+    unsigned rem = m & ((1u << k) - 1u), half = (1u << k) >> 1;
+    q += (unsigned)((k > 0) & ((rem > half) | ((rem == half) & (q & 1u))));
+    unsigned long long r = sh >= 0 ? ((unsigned long long)m << ls) : (unsigned long long)q;
+    if (e == 0) r = 0ull;                 // zero and subnormals: |v * 2^32| < 2^-94
+    bool sat = sh > 39;                   // |v| >= 2^31, infinities, NaN
+    if (sat) r = (e == 255 && (u & 0x7fffffu)) ? 0ull : 0x7fffffffffffffffull;
+    unsigned long long neg = (sat && r) ? 0x8000000000000000ull : 0ull - r;
+    return (u >> 31) ? neg : r;
 }
 // The double form is built from the IEEE-754 fields with integer
 // instructions, saturated like cvt.rni.s64.f64 (NaN gives 0): GB300 executes
@@ -165,6 +185,7 @@ template <>
 struct ESum<true> {
     unsigned long long v = 0ull;
     __device__ __forceinline__ void add(float x) { v += to_fix(x); }
+    __device__ __forceinline__ void add_alu(float x) { v += to_fix_alu(x); }
     __device__ __forceinline__ void add(double x) { v += to_fixd(x); }
     __device__ __forceinline__ void flush(const Acc<true>& a, int slot) {
         unsigned long long t = warp_sum(v);
@@ -1094,8 +1115,8 @@ constexpr int kQBlock = 256;   // threads per block of the Q kernels
 // end the warps of a block combine them in shared memory and the block adds
 // them once (fixed point in the mixed form).
 template <bool MIX>
-__device__ __forceinline__ void flush_q_grad(const DevModel& m, const DevState& s, const float (&gqf)[2][3],
-                                             const double (&gqd)[2][3]) {
+__device__ __forceinline__ void flush_q_grad(const DevModel& m, const DevState& s,
+                                             const unsigned long long (&gqx)[2][3], const double (&gqd)[2][3]) {
     typedef typename std::conditional<MIX, unsigned long long, double>::type GT;
     __shared__ GT red[3 * kMaxQ];
     for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) red[k] = GT(0);
@@ -1107,7 +1128,7 @@ __device__ __forceinline__ void flush_q_grad(const DevModel& m, const DevState& 
         if (iq >= m.nqat) break;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            if constexpr (MIX) atomicAdd(&red[3 * iq + c], to_fix(gqf[k][c]));
+            if constexpr (MIX) atomicAdd(&red[3 * iq + c], gqx[k][c]);
             else atomicAdd(&red[3 * iq + c], gqd[k][c]);
         }
     }
@@ -1190,14 +1211,18 @@ struct QPairT<true, SMAX> {
 // chunk are summed in registers and converted once per chunk, so the fixed-
 // point totals do not depend on the grid.  An environment atom's gradient is
 // summed over the Q atoms in FP32 in a fixed shuffle order, then converted.
-constexpr int kQChunk = 8;
+#ifndef QNB_Q_CHUNK
+#define QNB_Q_CHUNK 8
+#endif
+constexpr int kQChunk = QNB_Q_CHUNK;
 template <bool MIX, bool SPC, bool WATER, int SMAX>
-__global__ void __launch_bounds__(kQBlock) k_qenv(DevModel m, const DevState* __restrict__ states) {
+__global__ void __launch_bounds__(kQBlock, 3) k_qenv(DevModel m, const DevState* __restrict__ states) {
     typedef typename std::conditional<MIX, float, double>::type T;
     const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> eel[SMAX], evdw[SMAX];
-    float gqf[2][3] = {};
+    float gqf[2][3] = {};              // this chunk's Q-atom gradient (mixed form)
+    unsigned long long gqx[2][3] = {}; // converted once per chunk: the sum over chunks is exact
     double gqd[2][3] = {};
     T lam[SMAX];
 #pragma unroll
@@ -1270,8 +1295,24 @@ __global__ void __launch_bounds__(kQBlock) k_qenv(DevModel m, const DevState* __
 #pragma unroll
       for (int st = 0; st < SMAX; ++st) {
           if (st >= S) break;
-          eel[st].add(pel[st]);
-          evdw[st].add(pvdw[st]);
+          if constexpr (MIX) {
+              eel[st].add_alu(pel[st]);
+              evdw[st].add_alu(pvdw[st]);
+          } else {
+              eel[st].add(pel[st]);
+              evdw[st].add(pvdw[st]);
+          }
+      }
+      if constexpr (MIX) {
+#pragma unroll
+          for (int k = 0; k < kMaxQ / 32; ++k) {
+              if (k * 32 >= m.nqat) break;   // warp-uniform
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                  gqx[k][c] += to_fix_alu(gqf[k][c]);
+                  gqf[k][c] = 0.f;
+              }
+          }
       }
     }
     const int kel = WATER ? 4 : 2;
@@ -1281,7 +1322,7 @@ __global__ void __launch_bounds__(kQBlock) k_qenv(DevModel m, const DevState* __
         eel[st].flush(acc, eq_slot(st, kel));
         evdw[st].flush(acc, eq_slot(st, kel + 1));
     }
-    flush_q_grad<MIX>(m, s, gqf, gqd);
+    flush_q_grad<MIX>(m, s, gqx, gqd);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,176 @@
+"""The benchmark configurations at full size on the GPU.
+
+1  R15 droplet, 20-atom solute, 6 Q atoms, 2 states (FP64, the oracle's size)
+2  R25 sphere, 3,000-atom solute, 20 Q atoms, 2 states (the metric's system)
+3  51 lambda windows of config 1 in one batched context, and 16 replicas with
+   radii drawn from 18-30 A
+4  config 1 with a 40-atom solute, 30 Q atoms in 4 states, log-normal Q LJ
+5  R40 sphere, 8,000-atom solute, 40 Q atoms in 4 states, 12 A cut-offs, 16
+   windows batched
+
+Bars: the FP64 form against the CPU oracle within 1e-6 kcal/mol per energy
+term (1e-9 relative for terms above 1,000 kcal/mol: the FP64 form sums with
+atomics, so its rounding follows the schedule) and 1e-6 relative per gradient
+component; the mixed form within 1e-3 relative; batched windows bit-equal to
+single-window contexts; list sizes equal."""
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle
+from q6_gb300.qnb import LIST_PP, LIST_PW, LIST_QP, LIST_QW, LIST_WW, PREC_FP64, PREC_MIXED, NonbondedEngine
+from q6_gb300.system import (config_adjoint, config_large, config_small, config_window, default_solvent_params,
+                             lambdas_for_window, make_system)
+
+pytestmark = pytest.mark.gpu
+
+CUT10 = dict(Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
+CUT12 = dict(Rcq=99.0, RcLRF=99.0, Rcpp=12.0, Rcpw=12.0, Rcww=12.0)
+
+
+def fp64_bar(e):
+    return 1e-6 * max(1.0, abs(e) / 1e3)
+
+
+def grad_ok(d, d0, rel):
+    scale = np.maximum(np.abs(d0), np.median(np.abs(d0)))
+    return bool(np.all(np.abs(d - d0) <= rel * scale + 1e-9))
+
+
+def check_vs_oracle(s, cut, lam):
+    sp = default_solvent_params(s)
+    o = Oracle(s)
+    o.set_solvent_params(sp)
+    d0, E0, EQ0, R0 = o.evaluate(s.x, lam, cut=cut, solvent=sp)
+    o.make_pair_lists(s.x, **cut)
+    for prec, tol, gtol in ((PREC_FP64, 1e-6, 1e-6), (PREC_MIXED, 1e-3, 2e-3)):
+        with NonbondedEngine(s, precision=prec) as eng:
+            eng.set_solvent_params(sp)
+            d, E, EQ, R = eng.evaluate(s.x, lam, cut=cut, solvent=sp)
+            for kind in (LIST_PP, LIST_PW, LIST_WW, LIST_QP, LIST_QW):
+                assert eng.list_size(kind) == o.list_size(kind), (prec, kind)
+        for k in E0:
+            bar = fp64_bar(E0[k]) if prec == PREC_FP64 else tol * max(1.0, abs(E0[k]))
+            assert abs(E[k] - E0[k]) <= bar, (prec, k, E[k], E0[k])
+        qbar = tol if prec == PREC_FP64 else tol * np.maximum(1.0, np.abs(EQ0))
+        assert np.all(np.abs(EQ - EQ0) <= qbar), (prec, EQ, EQ0)
+        assert grad_ok(d, d0, gtol), prec
+
+
+def test_config1_droplet():
+    check_vs_oracle(config_small(), CUT10, [0.5, 0.5])
+
+
+def test_config2_r25_sphere():
+    check_vs_oracle(config_window(), CUT10, [0.5, 0.5])
+
+
+def test_config4_four_state_evb():
+    check_vs_oracle(config_adjoint(), CUT10, [0.4, 0.3, 0.2, 0.1])
+
+
+def batched_vs_single(s, cut, lams, check_windows, prec=PREC_MIXED):
+    W = len(lams)
+    sp = default_solvent_params(s)
+    rng = np.random.default_rng(17)
+    xs = np.stack([s.x + rng.normal(0.0, 0.02, s.x.shape) for _ in range(W)])
+    with NonbondedEngine(s, precision=prec, windows=W) as b:
+        b.set_solvent_params(sp)
+        for w in range(W):
+            b.set_lambda(lams[w], window=w)
+        b.set_coordinates_dev(xs)
+        b.make_pair_lists_dev(**cut)
+        E, EQ, R = b.compute_dev(Tfree=300.0, istep=0, sync=True)
+        D = b.gradient_dev()
+    for w in check_windows:
+        with NonbondedEngine(s, precision=prec) as e:
+            e.set_solvent_params(sp)
+            e.set_lambda(lams[w])
+            e.set_coordinates_dev(xs[w][None])
+            e.make_pair_lists_dev(**cut)
+            E1, EQ1, R1 = e.compute_dev(Tfree=300.0, istep=0, sync=True)
+            D1 = e.gradient_dev()
+        for k in E1[0]:
+            assert E[w][k] == E1[0][k], (w, k)
+        assert np.array_equal(EQ[w], EQ1[0]) and np.array_equal(R[w], R1[0]), w
+        assert np.array_equal(D[w], D1[0]), w
+    return xs, E, EQ, D
+
+
+def test_config3_51_windows_batched():
+    s = config_small()
+    lams = [lambdas_for_window(l, s.nstates) for l in np.linspace(0.0, 1.0, 51)]
+    batched_vs_single(s, CUT10, lams, check_windows=(0, 25, 50))
+
+
+def test_config3_uneven_replicas():
+    """16 replicas, radii uniform in 18-30 A: each its own context; the mixed
+    form within 1e-3 of the FP64 form, and 3 of them (smallest, median,
+    largest) FP64 against the oracle."""
+    rng = np.random.default_rng(3016)
+    radii = np.sort(rng.uniform(18.0, 30.0, 16))
+    for r_i, R in enumerate(radii):
+        s = make_system(R=float(R), n_solute=20, group_sizes=(3, 5), ntypes=6, nq=6, nstates=2,
+                        seed=3100 + r_i)
+        sp = default_solvent_params(s)
+        out = {}
+        for prec in (PREC_FP64, PREC_MIXED):
+            with NonbondedEngine(s, precision=prec) as eng:
+                eng.set_solvent_params(sp)
+                out[prec] = eng.evaluate(s.x, [0.5, 0.5], cut=CUT10, solvent=sp)
+        d64, E64, EQ64, _ = out[PREC_FP64]
+        dmx, Emx, EQmx, _ = out[PREC_MIXED]
+        for k in E64:
+            assert abs(Emx[k] - E64[k]) <= 1e-3 * max(1.0, abs(E64[k])), (R, k)
+        assert np.allclose(EQmx, EQ64, rtol=1e-3, atol=1e-3), R
+        assert grad_ok(dmx, d64, 2e-3), R
+        if r_i in (0, 8, 15):
+            o = Oracle(s)
+            o.set_solvent_params(sp)
+            d0, E0, EQ0, _ = o.evaluate(s.x, [0.5, 0.5], cut=CUT10, solvent=sp)
+            for k in E0:
+                assert abs(E64[k] - E0[k]) <= fp64_bar(E0[k]), (R, k, E64[k], E0[k])
+            assert np.all(np.abs(EQ64 - EQ0) <= 1e-6), R
+            assert grad_ok(d64, d0, 1e-6), R
+
+
+@pytest.fixture(scope="module")
+def large():
+    return config_large()
+
+
+def test_config5_large_fp64_vs_oracle(large):
+    s = large
+    lam = [0.25, 0.25, 0.25, 0.25]
+    sp = default_solvent_params(s)
+    o = Oracle(s)
+    o.set_solvent_params(sp)
+    d0, E0, EQ0, R0 = o.evaluate(s.x, lam, cut=CUT12, solvent=sp)
+    with NonbondedEngine(s, precision=PREC_FP64) as eng:
+        eng.set_solvent_params(sp)
+        d, E, EQ, R = eng.evaluate(s.x, lam, cut=CUT12, solvent=sp)
+    for k in E0:
+        assert abs(E[k] - E0[k]) <= fp64_bar(E0[k]), (k, E[k], E0[k])
+    assert np.all(np.abs(EQ - EQ0) <= 1e-6), (EQ, EQ0)
+    assert grad_ok(d, d0, 1e-6)
+
+
+def test_config5_large_16_windows(large):
+    """16 batched windows: window 3 and 12 bit-equal to single contexts, and
+    every window's mixed energies within 1e-3 of the FP64 form's."""
+    s = large
+    lams = [lambdas_for_window(l, s.nstates) for l in np.linspace(0.0, 1.0, 16)]
+    xs, E, EQ, D = batched_vs_single(s, CUT12, lams, check_windows=(3, 12))
+    sp = default_solvent_params(s)
+    with NonbondedEngine(s, precision=PREC_FP64, windows=16) as b:
+        b.set_solvent_params(sp)
+        for w in range(16):
+            b.set_lambda(lams[w], window=w)
+        b.set_coordinates_dev(xs)
+        b.make_pair_lists_dev(**CUT12)
+        E64, EQ64, _ = b.compute_dev(Tfree=300.0, istep=0, sync=True)
+        D64 = b.gradient_dev()
+    for w in range(16):
+        for k in E64[w]:
+            assert abs(E[w][k] - E64[w][k]) <= 1e-3 * max(1.0, abs(E64[w][k])), (w, k)
+        assert np.allclose(EQ[w], EQ64[w], rtol=1e-3, atol=1e-3), w
+        assert grad_ok(D[w], D64[w], 2e-3), w

@@ -58,3 +58,35 @@ def test_gradient_matches_finite_differences():
             xm = s.x.copy(); xm[i, c] -= h
             fd = (energy(xp)[0] - energy(xm)[0]) / (2 * h)
             assert abs(fd - d0[i, c]) <= 1e-4 * max(1.0, abs(fd)), (i, c, fd, d0[i, c])
+
+
+def test_lrf_energy_approximates_far_field_coulomb():
+    """The LRF Taylor energy (lrf_update + lrf_taylor) approximates the exact
+    Coulomb energy of the pairs it replaces: non-Q atoms of group pairs beyond
+    the cut-off.  An independent numpy sum over those pairs pins the oracle's
+    far-pair classification and expansion; the expansion is truncated after
+    the third order in |x_i - centre| / r (groups of up to 3 A radius, sources
+    beyond 10 A), so the bar is 5 %."""
+    s = make_system(R=15.0, n_solute=60, group_sizes=(3, 5), ntypes=6, nq=6, nstates=2, seed=71)
+    o = Oracle(s)
+    o.make_pair_lists(s.x)
+    _, E, _ = o.pot_energy_nonbonds(s.x)
+    ns = s.ncgp_solute
+    groups = [s.cgpatom[s.cgp_first[g]:s.cgp_last[g] + 1] for g in range(s.ncgp)]
+    dist = np.array([s.cgp_iswitch[g] if g < ns else groups[g][0] for g in range(s.ncgp)])
+    gid = np.zeros(s.natom, dtype=int)
+    for g, atoms in enumerate(groups):
+        gid[atoms] = g
+    q = s.crg.copy()
+    q[s.iqseq] = 0.0
+    d2 = ((s.x[dist][:, None, :] - s.x[dist][None, :, :]) ** 2).sum(-1)
+    far_g = (d2 > 100.0) & ~s.excl[dist][:, None].astype(bool) & ~s.excl[dist][None, :].astype(bool)
+    e = 0.0
+    for i in range(s.natom):
+        if q[i] == 0.0 or s.excl[dist[gid[i]]]:
+            continue
+        far = far_g[gid[i]][gid]
+        r = np.sqrt(((s.x - s.x[i]) ** 2).sum(1))
+        e += q[i] * np.sum(q[far] / r[far])
+    e *= 0.5
+    assert abs(E["lrf"] - e) <= 0.05 * abs(e), (E["lrf"], e)
