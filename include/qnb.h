@@ -163,7 +163,7 @@ typedef struct qnb_context qnb_context;
 /* Last error message of the calling thread (static storage). */
 const char* qnb_last_error(void);
 
-/* Library/ABI version, e.g. 0x000200 for 0.2.0. */
+/* Library/ABI version, e.g. 0x000300 for 0.3.0. */
 int32_t qnb_version(void);
 
 /* Copies the model, precomputes interaction tables (replaces
@@ -271,6 +271,33 @@ int qnb_make_pair_lists_dev(qnb_context* ctx, double Rq, double Rcq2, double RcL
 int qnb_compute_dev(qnb_context* ctx, double Tfree, int32_t istep, int32_t sync,
                     qnb_energies* E, qnb_qenergies* EQ, double* Erst);
 
+/* Energies of the last qnb_compute_dev / qnb_group_compute evaluation of all
+   windows, added into E[nwin], EQ[nwin*nstates], Erst[nwin*2] (waits for
+   the context's stream). */
+int qnb_get_energies_dev(qnb_context* ctx, qnb_energies* E, qnb_qenergies* EQ, double* Erst);
+
+/* qnb_compute_dev replays its kernel sequence from a CUDA graph (default on;
+   0 launches kernel by kernel).  A graph is captured on first use and again
+   whenever list capacities, solvent parameters or Tfree change; the steps
+   that update watpol's theta_corr use a second graph.  With qnb_profile on,
+   the graph also records the per-class timing events; call
+   qnb_profile_collect after each evaluation has finished (otherwise the
+   next qnb_compute_dev waits for it before replaying). */
+int qnb_set_graphs(qnb_context* ctx, int32_t enable);
+int qnb_profile_collect(qnb_context* ctx);
+
+/* A group of contexts (systems of different sizes, e.g. replicas of uneven
+   sphere radii, on one device) evaluated as ONE CUDA graph launch: each
+   context's kernel sequence is an independent branch of the graph, so the
+   systems run concurrently.  qnb_group_compute is qnb_compute_dev(sync = 0)
+   for every member; read energies with qnb_get_energies_dev and gradients
+   with qnb_download_gradient.  Members must outlive the group; profiling
+   must be off.  No counterpart in the reference (one process per window). */
+typedef struct qnb_group qnb_group;
+int qnb_group_create(qnb_context** ctxs, int32_t n, qnb_group** group);
+int qnb_group_compute(qnb_group* group, double Tfree, int32_t istep);
+int qnb_group_destroy(qnb_group* group);
+
 /* Adjoint of the Q-atom energies (no counterpart in the reference; for
    force-field and EVB parameter fitting).  For every window w, Q atom iq and
    state s, at the current device coordinates and lists:
@@ -299,6 +326,9 @@ enum {
 /* Brackets every launch of each kernel class with CUDA events on the
    context's stream while enable != 0. */
 int qnb_profile(qnb_context* ctx, int32_t enable);
+/* Profiling of the kernel classes whose bits (1 << QNB_K_*) are set only;
+   0 turns profiling off.  Fewer events, less perturbation of the timing. */
+int qnb_profile_classes(qnb_context* ctx, uint32_t mask);
 
 /* Total milliseconds and launches per kernel class since the last call
    (n entries, n <= QNB_K_COUNT); resets the totals. */

@@ -97,6 +97,26 @@ struct qnb_context {
     Cut last_cut{};
     int maxg = 1;                  // largest solute charge group
     bool rows_pending = false;     // mixed form: frow not yet added into d
+    // CUDA-graph replay of qnb_compute_dev: one instantiated graph per
+    // variant (watpol theta_corr update step or not), valid while its key
+    // (launch-geometry epoch, Tfree) matches
+    bool use_graphs = true;
+    uint64_t epoch = 1;            // bumped whenever launch parameters change
+    struct Pending {
+        int k;
+        cudaEvent_t a, b;
+        bool owned;    // the events belong to a captured graph (not pooled)
+    };
+    struct GraphSlot {
+        cudaGraphExec_t exec = nullptr;
+        uint64_t key_epoch = 0;
+        double key_tfree = 0.0;
+        unsigned key_mask = 0;
+        int64_t nlaunch = 0;
+        std::vector<Pending> prof;   // profiled graphs: the event pairs their nodes record
+    } gslot[2][2];                   // [watpol update step][profiled]
+    bool capturing = false;          // timed() is recording into a graph capture
+    std::vector<Pending> cap_pending;
     bool qenv_pending = false;     // mixed form: fq not yet added into d
     DevState* d_diag = nullptr;    // scratch device state for inspection builds
     std::vector<int> counts;       // [nwin][C_NUM] after the last build
@@ -105,10 +125,7 @@ struct qnb_context {
     int64_t launches = 0;
     // optional per-kernel-class event timing (qnb_profile)
     bool profiling = false;
-    struct Pending {
-        int k;
-        cudaEvent_t a, b;
-    };
+    unsigned prof_mask = ~0u;      // kernel classes bracketed with events while profiling
     std::vector<Pending> pending;
     std::vector<cudaEvent_t> ev_pool;
     double prof_ms[K_NUM] = {0};
@@ -159,15 +176,19 @@ cudaEvent_t take_event(qnb_context* c) {
 // profiling is on
 template <typename F>
 void timed(qnb_context* c, int k, F&& f) {
-    if (!c->profiling) {
+    if (!c->profiling || !((c->prof_mask >> k) & 1u)) {
         f();
         return;
     }
     cudaEvent_t a = take_event(c), b = take_event(c);
-    cudaEventRecord(a, c->stream);
+    // inside a capture, an external record becomes an event-record node that
+    // records the event on every replay (a plain record only orders streams)
+    const unsigned fl = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    cudaEventRecordWithFlags(a, c->stream, fl);
     f();
-    cudaEventRecord(b, c->stream);
-    c->pending.push_back({k, a, b});
+    cudaEventRecordWithFlags(b, c->stream, fl);
+    if (c->capturing) c->cap_pending.push_back({k, a, b, true});
+    else c->pending.push_back({k, a, b, false});
 }
 
 void collect_profile(qnb_context* c) {
@@ -178,9 +199,13 @@ void collect_profile(qnb_context* c) {
         if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
             c->prof_ms[p.k] += ms;
             c->prof_n[p.k] += 1;
+        } else {
+            cudaGetLastError();   // a missing time must not surface as a later launch error
         }
-        c->ev_pool.push_back(p.a);
-        c->ev_pool.push_back(p.b);
+        if (!p.owned) {
+            c->ev_pool.push_back(p.a);
+            c->ev_pool.push_back(p.b);
+        }
     }
     c->pending.clear();
 }
@@ -675,6 +700,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
 }
 
 int upload_states(qnb_context* c) {
+    ++c->epoch;   // capacities / buffers may have changed: captured graphs are stale
     CU(cudaMemcpyAsync(c->d_states, c->st.data(), sizeof(DevState) * c->nwin, cudaMemcpyHostToDevice, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     return QNB_OK;
@@ -718,6 +744,7 @@ int alloc_state(qnb_context* c) {
         TRY(c->alloc(&s.n_insh, (size_t)kMaxShell));
         TRY(c->alloc(&s.wstate, (size_t)3 * kMaxShell));
         TRY(c->alloc(&s.shell_tsum, (size_t)kMaxShell));
+        TRY(c->alloc(&s.theta_sorted, (size_t)kMaxShell * std::max(1, m.nwat)));
         TRY(c->alloc(&s.adj, (size_t)3 * std::max(1, m.nqat * m.S)));
         TRY(c->alloc(&s.shell_list, (size_t)kMaxShell * std::max(1, m.nwat)));
         CU(cudaMemset(s.fix, 0, sizeof(unsigned long long) * n3));
@@ -1023,7 +1050,7 @@ extern "C" {
 
 const char* qnb_last_error(void) { return g_err.c_str(); }
 
-int32_t qnb_version(void) { return 0x000200; }
+int32_t qnb_version(void) { return 0x000300; }
 
 int qnb_create_batch(const qnb_topology* t, const qnb_options* opt, int32_t nwin, qnb_context** out) {
     if (!t || !opt || !out) return fail(QNB_ERR_ARG, "null argument");
@@ -1078,11 +1105,20 @@ int qnb_destroy(qnb_context* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (void* p : c->allocs) cudaFree(p);
-    for (auto& p : c->pending) {
-        cudaEventDestroy(p.a);
-        cudaEventDestroy(p.b);
-    }
+    for (auto& p : c->pending)
+        if (!p.owned) {
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+        }
     for (auto e : c->ev_pool) cudaEventDestroy(e);
+    for (auto& row : c->gslot)
+        for (auto& g : row) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            for (auto& p : g.prof) {
+                cudaEventDestroy(p.a);
+                cudaEventDestroy(p.b);
+            }
+        }
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->h_e) cudaFreeHost(c->h_e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1188,6 +1224,7 @@ int qnb_set_solvent_params(qnb_context* c, const qnb_solvent_params* p) {
         CU(cudaMemcpyAsync(c->st[w].wstate, ws, sizeof(ws), cudaMemcpyHostToDevice, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     c->have_solv = true;
+    ++c->epoch;   // SolventDev is passed by value: captured graphs are stale
     return QNB_OK;
 }
 
@@ -1315,10 +1352,14 @@ int qnb_stream(qnb_context* c, void** stream) {
     return QNB_OK;
 }
 
-int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, qnb_energies* E, qnb_qenergies* EQ,
-                    double* Erst) {
-    if (!c) return fail(QNB_ERR_ARG, "null context");
-    CU(cudaSetDevice(c->device));
+}  // extern "C"
+
+namespace {
+
+// One evaluation of every window (accumulators zeroed, pot_energy_nonbonds,
+// nonbond_qq/qqp, restrain_solvent, watpol, gradient applied), enqueued on
+// c->stream without any host synchronisation, so it can be captured.
+int enqueue_compute(qnb_context* c, double Tfree, int istep) {
     Launch L = c->all();
     TRY(zero_acc(c, c->nwin));
     TRY(compute_nonbond(c, 1, c->nwin));
@@ -1336,18 +1377,233 @@ int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, q
         c->rows_pending = c->qenv_pending = false;
         c->launches++;
     }
-    TRY(check_launch());
-    if (sync) {
-        std::vector<double> e((size_t)kNumE * c->nwin);
-        TRY(read_energies(c, c->nwin, e.data()));
-        for (int w = 0; w < c->nwin; ++w) {
-            add_energies(e.data() + (size_t)w * kNumE, E ? E + w : nullptr, EQ ? EQ + (size_t)w * c->S : nullptr, c->S);
-            if (Erst) {
-                Erst[2 * w] += e[(size_t)w * kNumE + E_RST_RAD];
-                Erst[2 * w + 1] += e[(size_t)w * kNumE + E_RST_POL];
+    return check_launch();
+}
+
+// whether this step runs watpol's theta_corr update (src/nonbondene.f90:6630)
+bool watpol_update_step(const qnb_context* c, int istep) {
+    return c->have_solv && c->solv.wpol && c->solv.nshell > 0 && istep > 0 &&
+           (istep % (int)llround(c->solv.itdis)) == 0;
+}
+
+// Captures f (which enqueues on `st`) into an instantiated graph.
+template <typename F>
+int capture_graph(cudaStream_t st, cudaGraphExec_t* exec, F&& f) {
+    *exec = nullptr;
+    CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = f();
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(QNB_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        *exec = nullptr;
+        return fail(QNB_ERR_CUDA, "graph instantiation: %s", cudaGetErrorString(e));
+    }
+    return QNB_OK;
+}
+
+// enqueue_compute through a cached CUDA graph: one launch per step instead
+// of one per kernel.  A graph is captured per variant (watpol update step or
+// not; profiled or not) and re-captured when the launch geometry (list
+// capacities, solvent parameters) or Tfree changed.  A profiled graph holds
+// event-record nodes around each kernel class; after every replay its event
+// pairs are queued for collect_profile, which must run (qnb_profile_collect)
+// before the next replay re-records them -- run_compute collects first if the
+// caller did not.
+int run_compute(qnb_context* c, double Tfree, int istep) {
+    if (!c->use_graphs) return enqueue_compute(c, Tfree, istep);
+    const int prof = c->profiling ? 1 : 0;
+    auto& g = c->gslot[watpol_update_step(c, istep) ? 1 : 0][prof];
+    for (auto& p : c->pending)
+        if (p.owned) {   // an earlier replay's times were not collected yet
+            collect_profile(c);
+            break;
+        }
+    const unsigned mask = prof ? c->prof_mask : 0u;
+    if (!g.exec || g.key_epoch != c->epoch || g.key_tfree != Tfree || g.key_mask != mask) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        for (auto& p : g.prof) {
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+        }
+        g.prof.clear();
+        int64_t l0 = c->launches;
+        c->capturing = true;
+        c->cap_pending.clear();
+        int rc = capture_graph(c->stream, &g.exec, [&] { return enqueue_compute(c, Tfree, istep); });
+        c->capturing = false;
+        g.prof.swap(c->cap_pending);
+        if (rc) {
+            for (auto& p : g.prof) {
+                cudaEventDestroy(p.a);
+                cudaEventDestroy(p.b);
             }
+            g.prof.clear();
+            return rc;
+        }
+        g.key_epoch = c->epoch;
+        g.key_tfree = Tfree;
+        g.key_mask = mask;
+        g.nlaunch = c->launches - l0;
+        c->launches = l0;   // counted when the graph runs
+    }
+    CU(cudaGraphLaunch(g.exec, c->stream));
+    c->launches += g.nlaunch;
+    if (prof) c->pending.insert(c->pending.end(), g.prof.begin(), g.prof.end());
+    return QNB_OK;
+}
+
+int energies_out(qnb_context* c, qnb_energies* E, qnb_qenergies* EQ, double* Erst) {
+    std::vector<double> e((size_t)kNumE * c->nwin);
+    TRY(read_energies(c, c->nwin, e.data()));
+    for (int w = 0; w < c->nwin; ++w) {
+        add_energies(e.data() + (size_t)w * kNumE, E ? E + w : nullptr, EQ ? EQ + (size_t)w * c->S : nullptr, c->S);
+        if (Erst) {
+            Erst[2 * w] += e[(size_t)w * kNumE + E_RST_RAD];
+            Erst[2 * w + 1] += e[(size_t)w * kNumE + E_RST_POL];
         }
     }
+    return QNB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, qnb_energies* E, qnb_qenergies* EQ,
+                    double* Erst) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built");
+    TRY(run_compute(c, Tfree, istep));
+    if (sync) TRY(energies_out(c, E, EQ, Erst));
+    return QNB_OK;
+}
+
+int qnb_get_energies_dev(qnb_context* c, qnb_energies* E, qnb_qenergies* EQ, double* Erst) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    return energies_out(c, E, EQ, Erst);
+}
+
+int qnb_set_graphs(qnb_context* c, int32_t enable) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    c->use_graphs = enable != 0;
+    return QNB_OK;
+}
+
+}  // extern "C"
+
+// ---- groups: several contexts (uneven systems) in one graph launch ---------
+struct qnb_group {
+    std::vector<qnb_context*> ctx;
+    cudaEvent_t fork = nullptr, done = nullptr;
+    std::vector<cudaEvent_t> join;
+    struct Slot {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<uint64_t> epochs;
+        std::vector<char> update;
+        double tfree = 0.0;
+        int64_t nlaunch = 0;
+    };
+    std::vector<Slot> slots;   // one per distinct pattern of watpol update steps seen
+};
+
+extern "C" {
+
+int qnb_group_create(qnb_context** ctxs, int32_t n, qnb_group** out) {
+    if (!ctxs || !out || n < 1) return fail(QNB_ERR_ARG, "null argument or empty group");
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!ctxs[i]) return fail(QNB_ERR_ARG, "null context %d", i);
+        if (ctxs[i]->device != ctxs[0]->device) return fail(QNB_ERR_ARG, "group contexts on different devices");
+        for (int j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) return fail(QNB_ERR_ARG, "context %d repeated in the group", i);
+    }
+    CU(cudaSetDevice(ctxs[0]->device));
+    qnb_group* g = new qnb_group();
+    g->ctx.assign(ctxs, ctxs + n);
+    g->join.assign(n, nullptr);
+    cudaError_t e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming);
+    for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&g->join[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        qnb_group_destroy(g);
+        return fail(QNB_ERR_CUDA, "group events: %s", cudaGetErrorString(e));
+    }
+    *out = g;
+    return QNB_OK;
+}
+
+int qnb_group_destroy(qnb_group* g) {
+    if (!g) return QNB_OK;
+    for (auto& s : g->slots)
+        if (s.exec) cudaGraphExecDestroy(s.exec);
+    if (g->fork) cudaEventDestroy(g->fork);
+    if (g->done) cudaEventDestroy(g->done);
+    for (auto e : g->join)
+        if (e) cudaEventDestroy(e);
+    delete g;
+    return QNB_OK;
+}
+
+// One evaluation of every window of every context of the group, as one CUDA
+// graph launch on the first context's stream: the contexts' kernel
+// sequences are independent branches of the graph, so systems of different
+// sizes run concurrently.  The other contexts' streams wait for the graph.
+int qnb_group_compute(qnb_group* g, double Tfree, int32_t istep) {
+    if (!g) return fail(QNB_ERR_ARG, "null group");
+    const int n = (int)g->ctx.size();
+    qnb_context* c0 = g->ctx[0];
+    CU(cudaSetDevice(c0->device));
+    std::vector<uint64_t> epochs(n);
+    std::vector<char> update(n);
+    for (int i = 0; i < n; ++i) {
+        if (!g->ctx[i]->lists_built) return fail(QNB_ERR_STATE, "pair lists of group context %d not built", i);
+        if (g->ctx[i]->profiling) return fail(QNB_ERR_STATE, "profiling is on for group context %d", i);
+        epochs[i] = g->ctx[i]->epoch;
+        update[i] = watpol_update_step(g->ctx[i], istep) ? 1 : 0;
+    }
+    qnb_group::Slot* slot = nullptr;
+    for (auto& s : g->slots)
+        if (s.update == update) slot = &s;
+    if (!slot) {
+        g->slots.emplace_back();
+        slot = &g->slots.back();
+        slot->update = update;
+    }
+    if (!slot->exec || slot->epochs != epochs || slot->tfree != Tfree) {
+        if (slot->exec) cudaGraphExecDestroy(slot->exec);
+        std::vector<int64_t> l0(n);
+        for (int i = 0; i < n; ++i) l0[i] = g->ctx[i]->launches;
+        TRY(capture_graph(c0->stream, &slot->exec, [&]() -> int {
+            CU(cudaEventRecord(g->fork, c0->stream));
+            for (int i = 1; i < n; ++i) CU(cudaStreamWaitEvent(g->ctx[i]->stream, g->fork, 0));
+            for (int i = 0; i < n; ++i) TRY(enqueue_compute(g->ctx[i], Tfree, istep));
+            for (int i = 1; i < n; ++i) {
+                CU(cudaEventRecord(g->join[i], g->ctx[i]->stream));
+                CU(cudaStreamWaitEvent(c0->stream, g->join[i], 0));
+            }
+            return QNB_OK;
+        }));
+        slot->epochs = epochs;
+        slot->tfree = Tfree;
+        slot->nlaunch = 0;
+        for (int i = 0; i < n; ++i) {
+            slot->nlaunch += g->ctx[i]->launches - l0[i];
+            g->ctx[i]->launches = l0[i];
+        }
+    }
+    CU(cudaGraphLaunch(slot->exec, c0->stream));
+    c0->launches += slot->nlaunch;
+    CU(cudaEventRecord(g->done, c0->stream));
+    for (int i = 1; i < n; ++i) CU(cudaStreamWaitEvent(g->ctx[i]->stream, g->done, 0));
     return QNB_OK;
 }
 
@@ -1379,9 +1635,24 @@ int qnb_profile(qnb_context* c, int32_t enable) {
     CU(cudaSetDevice(c->device));
     collect_profile(c);
     c->profiling = enable != 0;
+    c->prof_mask = ~0u;
+    return QNB_OK;
+}
+int qnb_profile_classes(qnb_context* c, uint32_t mask) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    collect_profile(c);
+    c->profiling = mask != 0;
+    c->prof_mask = mask;
     return QNB_OK;
 }
 
+int qnb_profile_collect(qnb_context* c) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    collect_profile(c);
+    return QNB_OK;
+}
 int qnb_kernel_times(qnb_context* c, double* ms, int64_t* launches, int32_t n) {
     if (!c || !ms || !launches) return fail(QNB_ERR_ARG, "null argument");
     CU(cudaSetDevice(c->device));

@@ -143,7 +143,8 @@ struct DevState {
     int* n_insh;         // [kMaxShell]
     int* shell_list;     // [kMaxShell][nwat] waters per shell
     double* wstate;      // [3*kMaxShell]: theta_corr, avtheta, avn_insh
-    double* shell_tsum;  // [kMaxShell] per-step sum of theta per shell
+    double* shell_tsum;  // [kMaxShell] per-step sum of theta per shell (in sorted order)
+    double* theta_sorted;   // [kMaxShell][nwat] the shell's thetas by rank
 };
 
 // ---- launch wrappers (qnb_kernels.cu) ---------------------------------------

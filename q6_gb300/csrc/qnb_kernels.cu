@@ -1715,6 +1715,22 @@ __global__ void __launch_bounds__(kRankBlock) k_watpol_rank(DevModel m, const De
             }
         }
     }
+    // the shell's theta sum (src/nonbondene.f90:6652-6666) over the thetas
+    // scattered to their ranks, by one warp in a fixed order: deterministic
+    // whatever order the shell list was filled in (FP64 atomics were not)
+    __syncthreads();
+    double* sorted = s.theta_sorted + (size_t)sh * m.nwat;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        int w = L[k];
+        sorted[s.rank[w]] = s.theta[w];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        double t = 0.0;
+        for (int k = lane; k < n; k += kWarp) t += sorted[k];
+        t = warp_sum(t);
+        if (lane == 0) s.shell_tsum[sh] = t;
+    }
 }
 
 __global__ void k_watpol_reset(const DevState* __restrict__ states) {
@@ -1760,7 +1776,6 @@ __global__ void k_watpol_force(DevModel m, const DevState* __restrict__ states, 
         if (t0 < 0.0) t0 = 0.0;
         if (t0 > pi) t0 = pi;
         double th = s.theta[w];
-        atomicAdd(s.shell_tsum + sh, th);
         double dth = th - t0 + s.wstate[sh];
         ep.add(0.5 * p.fkwpol * dth * dth);
         double dv = p.fkwpol * dth;

@@ -36,7 +36,9 @@ EXPORTED = (
     "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_take_launch_count",
     "qnb_profile", "qnb_kernel_times", "qnb_create_batch", "qnb_window_count",
     "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
-    "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev",
+    "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev", "qnb_get_energies_dev", "qnb_set_graphs",
+    "qnb_group_create", "qnb_group_compute", "qnb_group_destroy", "qnb_profile_collect",
+    "qnb_profile_classes",
 )
 KERNEL_CLASSES = ("ww", "qw", "pw", "pp", "qp", "lrf_taylor", "qq", "restrain", "watpol", "pack",
                   "apply", "build", "lrf_build")
@@ -82,6 +84,9 @@ def load_library(path: str = LIB_PATH):
         "qnb_download_gradient": [P, P, I32],
         "qnb_ww_spc_noalloc": [P, P, I32, I32, D, D, D, D, D, P, P, P],
         "qnb_q_adjoint_dev": [P, P, P, P],
+        "qnb_get_energies_dev": [P, P, P, P], "qnb_set_graphs": [P, I32],
+        "qnb_group_create": [P, I32, P], "qnb_group_compute": [P, D, I32], "qnb_group_destroy": [P],
+        "qnb_profile_collect": [P], "qnb_profile_classes": [P, ctypes.c_uint32],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -239,6 +244,31 @@ class NonbondedEngine:
         self._check(self.lib.qnb_compute_dev(self.h, Tfree, int(istep), int(sync), _p(E), _p(EQ), _p(R)))
         return [dict(zip(E_FIELDS, e)) for e in E], EQ[:, : self.S], R
 
+    def energies_dev(self):
+        """Energies of the last evaluation of every window (waits for it):
+        per-window dicts, EQ [nwin][nstates][6], restraints [nwin][2]."""
+        W = self.nwin
+        E = np.zeros((W, 7))
+        EQ = np.zeros((W, max(self.S, 1), 6))
+        R = np.zeros((W, 2))
+        self._check(self.lib.qnb_get_energies_dev(self.h, _p(E), _p(EQ), _p(R)))
+        return [dict(zip(E_FIELDS, e)) for e in E], EQ[:, : self.S], R
+
+    def profile_classes(self, names):
+        """Profile only the named kernel classes (KERNEL_CLASSES); [] stops."""
+        mask = 0
+        for n in names:
+            mask |= 1 << KERNEL_CLASSES.index(n)
+        self._check(self.lib.qnb_profile_classes(self.h, mask))
+
+    def profile_collect(self):
+        """Reads the per-class timing events of finished evaluations."""
+        self._check(self.lib.qnb_profile_collect(self.h))
+
+    def set_graphs(self, enable: bool):
+        """CUDA-graph replay of compute_dev (on by default)."""
+        self._check(self.lib.qnb_set_graphs(self.h, int(bool(enable))))
+
     def q_adjoint_dev(self):
         """dE_s/dqcrg, dE_s/dqA, dE_s/dqB per window: arrays [nwin][nqat][nstates]."""
         n = self.nwin * self.s.nqat * self.S
@@ -276,3 +306,34 @@ class NonbondedEngine:
             if solvent.wpol_restr:
                 erst[1] = self.watpol(x, d, istep, True)
         return d, E, EQ, erst
+
+
+class Group:
+    """Several engines (systems of different sizes on one GPU) evaluated as one
+    CUDA graph launch per step (qnb_group_*)."""
+
+    def __init__(self, engines):
+        self.lib = load_library()
+        self.engines = list(engines)
+        arr = (ctypes.c_void_p * len(self.engines))(*[e.h.value for e in self.engines])
+        h = ctypes.c_void_p()
+        rc = self.lib.qnb_group_create(arr, len(self.engines), ctypes.byref(h))
+        if rc != 0:
+            raise QnbError(f"qnb error {rc}: {self.lib.qnb_last_error().decode()}")
+        self.h = h
+
+    def compute(self, Tfree=300.0, istep=0):
+        rc = self.lib.qnb_group_compute(self.h, Tfree, int(istep))
+        if rc != 0:
+            raise QnbError(f"qnb error {rc}: {self.lib.qnb_last_error().decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qnb_group_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

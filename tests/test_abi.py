@@ -25,7 +25,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared():
         assert hasattr(lib, name), name
     lib.qnb_version.restype = ctypes.c_int32
-    assert lib.qnb_version() == 0x000200
+    assert lib.qnb_version() == 0x000300
 
 
 def test_struct_layouts_match_header():
