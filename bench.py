@@ -261,6 +261,8 @@ def run_ours(args, rank, world, local):
     if rank == 0:
         if args.cpu:
             out["cpu_baseline"] = cpu_baseline(s, sp, args)
+        if args.replicas:
+            out["replica_group"] = replica_group(args, local)
         if args.fp64_compare:
             out["fp64_value"] = fp64_compare(args, s, sp, lams, local)
             out["mixed_over_fp64"] = round(out["value"] / out["fp64_value"], 3) if out["fp64_value"] else None
@@ -425,6 +427,58 @@ def run_e2e(args, s, sp, lams, prec, local):
     return out
 
 
+def replica_group(args, local):
+    """Config 3 as one CUDA graph launch per step (qnb_group_compute): the
+    51-window context of the R15 system plus 16 single-window replicas with
+    radii drawn uniformly from 18-30 A.  Window-steps/s summed over all 67
+    windows, L2 flushed before every timed step."""
+    import numpy as np
+    import torch
+    from q6_gb300.qnb import PREC_MIXED, Group, NonbondedEngine
+    from q6_gb300.system import config_small, default_solvent_params, lambdas_for_window, make_system
+    rng = np.random.default_rng(3016)
+    radii = np.sort(rng.uniform(18.0, 30.0, 16))
+    systems = [config_small()] + [make_system(R=float(R), n_solute=20, group_sizes=(3, 5), ntypes=6, nq=6,
+                                              nstates=2, seed=3100 + i) for i, R in enumerate(radii)]
+    nwin = [51] + [1] * 16
+    engs = []
+    for s, W in zip(systems, nwin):
+        e = NonbondedEngine(s, precision=PREC_MIXED, device=local, windows=W)
+        e.set_solvent_params(default_solvent_params(s))
+        for w in range(W):
+            e.set_lambda(lambdas_for_window(w / 50.0 if W == 51 else 0.5, s.nstates), window=w)
+        e.set_coordinates_dev(np.stack([s.x] * W))
+        e.make_pair_lists_dev(**CUT)
+        engs.append(e)
+    grp = Group(engs)
+    stream = torch.cuda.ExternalStream(engs[0].stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    steps = max(10, min(args.steps, 100))
+    for k in range(3):
+        grp.compute(Tfree=300.0, istep=k + 1)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    tot = 0.0
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev0.record(stream)
+        grp.compute(Tfree=300.0, istep=k + 4)
+        ev1.record(stream)
+        ev1.synchronize()
+        tot += ev0.elapsed_time(ev1)
+    grp.close()
+    wins = sum(nwin)
+    for e in engs:
+        e.close()
+    return {"value": round(wins * steps / (tot / 1e3), 1), "unit": "window-steps/s", "ms_per_step": round(tot / steps, 4),
+            "windows": wins, "systems": len(systems), "atoms": int(sum(s.natom * w for s, w in zip(systems, nwin))),
+            "radii": [15.0] + [round(float(r), 2) for r in radii], "steps": steps,
+            "what": "evaluation step (no list rebuild) of 51 windows of the R15 system + 16 replicas of uneven radii, "
+                    "one CUDA graph launch per step"}
+
+
 def fp64_compare(args, s, sp, lams, local):
     """Plain FP64 form on the same workload (25 steps with one list build)."""
     import numpy as np
@@ -556,6 +610,8 @@ def main():
                     help="skip the host-buffer arm (profiling runs)")
     ap.add_argument("--no-cpu-baseline", dest="cpu", action="store_false",
                     help="skip the CPU oracle sample (profiling runs)")
+    ap.add_argument("--no-replicas", dest="replicas", action="store_false",
+                    help="skip the 51-window + 16-replica graph group")
     ap.add_argument("--no-dg", dest="dg", action="store_false",
                     help="skip the mixed-vs-FP64 dG check")
     args = ap.parse_args()

@@ -174,3 +174,46 @@ def test_config5_large_16_windows(large):
             assert abs(E[w][k] - E64[w][k]) <= 1e-3 * max(1.0, abs(E64[w][k])), (w, k)
         assert np.allclose(EQ[w], EQ64[w], rtol=1e-3, atol=1e-3), w
         assert grad_ok(D[w], D64[w], 2e-3), w
+
+
+def test_config3_one_graph_launch_for_windows_and_replicas():
+    """Config 3 as one CUDA graph launch per step: the 51-window context of
+    the config-1 system plus 16 single-window replicas of uneven radii; every
+    context's energies and gradients bit-equal to its own qnb_compute_dev."""
+    from q6_gb300.qnb import Group
+    base = config_small()
+    rng = np.random.default_rng(3016)
+    radii = np.sort(rng.uniform(18.0, 30.0, 16))
+    systems = [base] + [make_system(R=float(R), n_solute=20, group_sizes=(3, 5), ntypes=6, nq=6, nstates=2,
+                                    seed=3100 + i) for i, R in enumerate(radii)]
+    nwin = [51] + [1] * 16
+    lam51 = [lambdas_for_window(l, 2) for l in np.linspace(0.0, 1.0, 51)]
+    res = {}
+    for grouped in (False, True):
+        engs = []
+        for s, W in zip(systems, nwin):
+            e = NonbondedEngine(s, precision=PREC_MIXED, windows=W)
+            e.set_solvent_params(default_solvent_params(s))
+            for w in range(W):
+                e.set_lambda(lam51[w] if W == 51 else [0.5, 0.5], window=w)
+            e.set_coordinates_dev(np.stack([s.x] * W))
+            e.make_pair_lists_dev(**CUT10)
+            engs.append(e)
+        grp = Group(engs) if grouped else None
+        out = []
+        for k in range(2):
+            if grouped:
+                grp.compute(Tfree=300.0, istep=k)
+            else:
+                for e in engs:
+                    e.compute_dev(Tfree=300.0, istep=k, sync=False)
+            out.append([(e.energies_dev(), e.gradient_dev()) for e in engs])
+        if grp:
+            grp.close()
+        for e in engs:
+            e.close()
+        res[grouped] = out
+    for step_a, step_b in zip(res[False], res[True]):
+        for ((Ea, EQa, Ra), Da), ((Eb, EQb, Rb), Db) in zip(step_a, step_b):
+            assert all(a == b for a, b in zip(Ea, Eb))
+            assert np.array_equal(EQa, EQb) and np.array_equal(Ra, Rb) and np.array_equal(Da, Db)
