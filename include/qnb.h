@@ -271,6 +271,16 @@ int qnb_make_pair_lists_dev(qnb_context* ctx, double Rq, double Rcq2, double RcL
 int qnb_compute_dev(qnb_context* ctx, double Tfree, int32_t istep, int32_t sync,
                     qnb_energies* E, qnb_qenergies* EQ, double* Erst);
 
+/* nonbond_solvent_internal (src/nonbondene.f90:6082-6154): intra-molecular
+   solvent pairs, replaces the nonbnd_solv_int list that
+   prep_sim_precompute_solvent (src/simprep.f90:4003-4125) builds when the
+   solvent has torsions.  ij[2k], ij[2k+1]: 0-based atom offsets inside a
+   solvent molecule; A, B, el: the pair's vdWA, vdWB, elec.  Every molecule's
+   pairs are evaluated in pot_energy_nonbonds (md) into E.ww.  n = 0 removes
+   the list (the default). */
+int qnb_set_solvent_internal(qnb_context* ctx, int32_t n, const int32_t* ij, const double* A, const double* B,
+                             const double* el);
+
 /* Energies of the last qnb_compute_dev / qnb_group_compute evaluation of all
    windows, added into E[nwin], EQ[nwin*nstates], Erst[nwin*2] (waits for
    the context's stream). */

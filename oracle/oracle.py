@@ -48,6 +48,7 @@ def lib():
         L.orc_pot_energy_nonbonds.argtypes = [P, P, P, P, P, I]
         L.orc_nonbond_qq.argtypes = [P, P, P, P]
         L.orc_set_solvent_params.argtypes = [P, P]
+        L.orc_set_solvent_internal.argtypes = [P, ctypes.c_int, P, P, P, P]
         L.orc_restrain_solvent.argtypes = [P, P, P, D, P]
         L.orc_watpol.argtypes = [P, P, P, I, I, P]
         L.orc_get_watpol_state.argtypes = [P, P, P, P]
@@ -121,6 +122,13 @@ class Oracle:
 
     def set_solvent_params(self, p):
         lib().orc_set_solvent_params(self.h, ctypes.byref(p))
+
+    def set_solvent_internal(self, pairs, A, B, el):
+        """nonbnd_solv_int: (i, j) offsets inside a solvent molecule with their
+        A, B, elec (applied to every molecule when md)."""
+        ij = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        a, b, e = (np.ascontiguousarray(np.asarray(v, dtype=np.float64)) for v in (A, B, el))
+        lib().orc_set_solvent_internal(self.h, len(a), _p(ij), _p(a), _p(b), _p(e))
 
     def restrain_solvent(self, x, d, Tfree):
         e = np.zeros(1)

@@ -63,7 +63,9 @@ typedef struct orc {
     int nel; int* elp; double* elv; int nqexp; int* qexp;
     double xpcent[3], xwcent[3], rexcl_o;
     int use_lrf;
-    int any_atom;       /* iuse_switch_atom == 0: the *lis2* group tests   */
+    int any_atom;
+    /* nonbnd_solv_int: intra-molecular solvent pairs (offsets in a molecule) */
+    int nsi; int *si_i, *si_j; double *si_A, *si_B, *si_el;       /* iuse_switch_atom == 0: the *lis2* group tests   */
     /* solvent (first molecule) parameters: chg_solv, aLJ_solv, bLJ_solv */
     double chg_solv[16], aLJ[16][3], bLJ[16][3];
     pre_t ww_pre[16][16];
@@ -448,6 +450,7 @@ void orc_destroy(orc* o) {
     if (!o) return;
     free(o->crg); free(o->iac); free(o->excl); free(o->heavy); free(o->avdw); free(o->bvdw);
     free(o->ljcod); free(o->cfirst); free(o->clast); free(o->csw); free(o->cgpatom); free(o->iwhich);
+    free(o->si_i); free(o->si_j); free(o->si_A); free(o->si_B); free(o->si_el);
     free(o->exkeys); free(o->k14); free(o->iqseq); free(o->iqatom); free(o->qcrg); free(o->qiac);
     free(o->qavdw); free(o->qbvdw); free(o->sc); free(o->qconn); free(o->elp); free(o->elv); free(o->qexp);
     free(o->pw_pre); free(o->qp_pre); free(o->qw_pre);
@@ -745,6 +748,38 @@ static eret nbe(const double* x, int i, int j, double A, double B, double el) {
     r.vec = t;
     return r;
 }
+/* nonbond_solvent_internal, src/nonbondene.f90:6082-6154: the listed pairs
+   inside every solvent molecule (q_dist2), with the reference's grouping of
+   dv = r2*(-Vel) + r2*(-12 Va + 6 Vb) */
+static void nonbond_solvent_internal(const orc* o, const double* x, double* d, double* el, double* vdw) {
+    for (int iw = 0; iw < o->nwat; ++iw) {
+        int is = o->nat_solute + o->solv_atom * iw;
+        for (int ip = 0; ip < o->nsi; ++ip) {
+            int ia = is + o->si_i[ip], ib = is + o->si_j[ip];
+            v3 t = vsub(X(x, ib), X(x, ia));
+            double r2 = 1.0 / vsq(t);
+            double r = sqrt(r2);
+            double r6 = r2 * r2 * r2;
+            double r12 = r6 * r6;
+            double Vel = o->si_el[ip] * r, Va = o->si_A[ip] * r12, Vb = o->si_B[ip] * r6;
+            double dv = r2 * (-Vel) + r2 * (-12.0 * Va + 6.0 * Vb);
+            *el += Vel;
+            *vdw += Va - Vb;
+            d[3 * ia] -= t.x * dv; d[3 * ia + 1] -= t.y * dv; d[3 * ia + 2] -= t.z * dv;
+            d[3 * ib] += t.x * dv; d[3 * ib + 1] += t.y * dv; d[3 * ib + 2] += t.z * dv;
+        }
+    }
+}
+
+void orc_set_solvent_internal(orc* o, int n, const int32_t* ij, const double* A, const double* B,
+                              const double* el) {
+    free(o->si_i); free(o->si_j); free(o->si_A); free(o->si_B); free(o->si_el);
+    o->nsi = n;
+    o->si_i = (int*)calloc(n ? n : 1, sizeof(int)); o->si_j = (int*)calloc(n ? n : 1, sizeof(int));
+    o->si_A = dup_d(A, n); o->si_B = dup_d(B, n); o->si_el = dup_d(el, n);
+    for (int k = 0; k < n; ++k) { o->si_i[k] = ij[2 * k]; o->si_j[k] = ij[2 * k + 1]; }
+}
+
 /* nbe_spc, src/nonbonded.f90:247-267 (q_dist, src/math.f90:214-224) */
 static eret nbe_spc(const double* x, int i, int j, double el) {
     eret r;
@@ -961,6 +996,8 @@ int orc_pot_energy_nonbonds(orc* o, const double* x, double* d, qnb_energies* E,
             nonbond_qw(o, x, d, EQ);
             if (md) nonbond_list(&o->nbww, x, d, &E->ww_el, &E->ww_vdw);
         }
+        /* src/potene.f90:361-366: only when the solvent has torsions */
+        if (md && o->nsi > 0) nonbond_solvent_internal(o, x, d, &E->ww_el, &E->ww_vdw);
         if (md) nonbond_list(&o->nbpw, x, d, &E->pw_el, &E->pw_vdw);
     }
     if (md) nonbond_list(&o->nbpp, x, d, &E->pp_el, &E->pp_vdw);

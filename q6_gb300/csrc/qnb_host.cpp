@@ -118,6 +118,9 @@ struct qnb_context {
     bool capturing = false;          // timed() is recording into a graph capture
     std::vector<Pending> cap_pending;
     bool qenv_pending = false;     // mixed form: fq not yet added into d
+    int nsi = 0;                   // nonbnd_solv_int pairs (solvents with torsions)
+    int2* d_si = nullptr;
+    double* d_sip = nullptr;       // [nsi][A, B, el]
     DevState* d_diag = nullptr;    // scratch device state for inspection builds
     std::vector<int> counts;       // [nwin][C_NUM] after the last build
     SolventDev solv{};
@@ -950,6 +953,8 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
         if (c->m.natom > c->m.nat_solute) {
             if (md) timed(c, K_WW, [&] { launch_rows_water(L); }), ++nl;
             timed(c, K_QW, [&] { launch_qw(L, mx); }), ++nl;
+            // src/potene.f90:361-366
+            if (md && c->nsi) timed(c, K_WW, [&] { launch_solvent_internal(L, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
         }
         if (md) {
             timed(c, K_PP, [&] {
@@ -963,6 +968,7 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
         if (c->m.natom > c->m.nat_solute) {
             if (md) timed(c, K_WW, [&] { launch_ww(L, mx); }), ++nl;
             timed(c, K_QW, [&] { launch_qw(L, mx); }), ++nl;
+            if (md && c->nsi) timed(c, K_WW, [&] { launch_solvent_internal(L, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
             if (md) timed(c, K_PW, [&] { launch_pw(L, mx); }), ++nl;
         }
         if (md) timed(c, K_PP, [&] { launch_pp(L, mx); }), ++nl;
@@ -1483,6 +1489,34 @@ int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, q
     if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built");
     TRY(run_compute(c, Tfree, istep));
     if (sync) TRY(energies_out(c, E, EQ, Erst));
+    return QNB_OK;
+}
+
+int qnb_set_solvent_internal(qnb_context* c, int32_t n, const int32_t* ij, const double* A, const double* B,
+                             const double* el) {
+    if (!c || n < 0 || (n > 0 && (!ij || !A || !B || !el))) return fail(QNB_ERR_ARG, "null argument");
+    for (int k = 0; k < n; ++k)
+        if (ij[2 * k] < 0 || ij[2 * k] >= c->m.sa || ij[2 * k + 1] < 0 || ij[2 * k + 1] >= c->m.sa ||
+            ij[2 * k] == ij[2 * k + 1])
+            return fail(QNB_ERR_ARG, "solvent pair %d: atoms must be distinct offsets 0..%d", k, c->m.sa - 1);
+    CU(cudaSetDevice(c->device));
+    if (c->d_si) c->release(c->d_si), c->d_si = nullptr;
+    if (c->d_sip) c->release(c->d_sip), c->d_sip = nullptr;
+    c->nsi = 0;
+    if (n > 0) {
+        std::vector<int2> v(n);
+        std::vector<double> p(3 * (size_t)n);
+        for (int k = 0; k < n; ++k) {
+            v[k] = make_int2(ij[2 * k], ij[2 * k + 1]);
+            p[3 * k] = A[k];
+            p[3 * k + 1] = B[k];
+            p[3 * k + 2] = el[k];
+        }
+        TRY(c->upload(&c->d_si, v));
+        TRY(c->upload(&c->d_sip, p));
+        c->nsi = n;
+    }
+    ++c->epoch;   // a launch more (or less) per step
     return QNB_OK;
 }
 

@@ -186,6 +186,7 @@ void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed);
 void launch_apply_fixed(const Launch& L, int rows, int qenv);
 void launch_clear_fq(const Launch& L);
 void launch_row_sums(const Launch& L);
+void launch_solvent_internal(const Launch& L, const int2* ij, const double* par, int n, int mixed);
 
 // kernel classes timed by the optional event profiler
 enum { K_WW = 0, K_QW, K_PW, K_PP, K_QP, K_LRF_TAYLOR, K_QQ, K_RESTRAIN, K_WATPOL, K_PACK, K_APPLY,

@@ -2004,6 +2004,44 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
     }
 }
 
+// nonbond_solvent_internal, src/nonbondene.f90:6082-6154: the listed pairs
+// (offsets in a molecule, nonbnd_solv_int) inside every solvent molecule, for
+// solvents with torsions; q_dist2 and the reference's grouping of dv.  FP64
+// in both forms (a few pairs per molecule); the mixed form accumulates in
+// fixed point.
+template <bool MIX>
+__global__ void k_solvent_internal(DevModel m, const DevState* __restrict__ states, const int2* __restrict__ ij,
+                                   const double* __restrict__ par, int n) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    Acc<MIX> acc = make_acc<MIX>(s);
+    ESum<MIX> eel, evdw;
+    for (int iw = blockIdx.x * blockDim.x + threadIdx.x; iw < m.nwat; iw += gridDim.x * blockDim.x) {
+        int is = m.nat_solute + m.sa * iw;
+        for (int ip = 0; ip < n; ++ip) {
+            int ia = is + ij[ip].x, ib = is + ij[ip].y;
+            double tx = x[3 * ib] - x[3 * ia], ty = x[3 * ib + 1] - x[3 * ia + 1], tz = x[3 * ib + 2] - x[3 * ia + 2];
+            double r2 = 1.0 / (tx * tx + ty * ty + tz * tz);
+            double r = sqrt(r2);
+            double r6 = r2 * r2 * r2;
+            double r12 = r6 * r6;
+            double vel = par[3 * ip + 2] * r, va = par[3 * ip] * r12, vb = par[3 * ip + 1] * r6;
+            double dv = r2 * (-vel) + r2 * (-12.0 * va + 6.0 * vb);
+            eel.add(vel);
+            evdw.add(va - vb);
+            if constexpr (MIX) {
+                acc.gradd(ia, -tx * dv, -ty * dv, -tz * dv);
+                acc.gradd(ib, tx * dv, ty * dv, tz * dv);
+            } else {
+                acc.grad(ia, -tx * dv, -ty * dv, -tz * dv);
+                acc.grad(ib, tx * dv, ty * dv, tz * dv);
+            }
+        }
+    }
+    eel.flush(acc, E_WW_EL);
+    evdw.flush(acc, E_WW_VDW);
+}
+
 // FP32 pair (nbe / nbe_spc): adds the gradient on atom i to g, returns energies
 __device__ __forceinline__ void pair_f(float4 a, float4 b, float A, float B, float el, bool lj, float& gx,
                                       float& gy, float& gz, float& vel, float& vdw) {
@@ -2417,6 +2455,12 @@ void launch_rows_solute(const Launch& L, int maxg) {
     else if (maxg <= 6) k_rows_solute<6><<<g, 128, sm, L.st>>>(L.m, L.ds);
     else if (maxg <= 8) k_rows_solute<8><<<g, 128, sm, L.st>>>(L.m, L.ds);
     else k_rows_solute<16><<<g, 128, sm, L.st>>>(L.m, L.ds);
+}
+void launch_solvent_internal(const Launch& L, const int2* ij, const double* par, int n, int mixed) {
+    if (L.m.nwat == 0 || n == 0) return;
+    dim3 g = grid_for(L.m.nwat, 64, 8, L.nwin);   // FP64 work: small blocks over all SMs
+    if (mixed) k_solvent_internal<true><<<g, 64, 0, L.st>>>(L.m, L.ds, ij, par, n);
+    else k_solvent_internal<false><<<g, 64, 0, L.st>>>(L.m, L.ds, ij, par, n);
 }
 void launch_rows_water(const Launch& L) {
     if (L.m.nwat == 0) return;

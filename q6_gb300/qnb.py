@@ -38,7 +38,7 @@ EXPORTED = (
     "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
     "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev", "qnb_get_energies_dev", "qnb_set_graphs",
     "qnb_group_create", "qnb_group_compute", "qnb_group_destroy", "qnb_profile_collect",
-    "qnb_profile_classes",
+    "qnb_profile_classes", "qnb_set_solvent_internal",
 )
 KERNEL_CLASSES = ("ww", "qw", "pw", "pp", "qp", "lrf_taylor", "qq", "restrain", "watpol", "pack",
                   "apply", "build", "lrf_build")
@@ -87,6 +87,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_get_energies_dev": [P, P, P, P], "qnb_set_graphs": [P, I32],
         "qnb_group_create": [P, I32, P], "qnb_group_compute": [P, D, I32], "qnb_group_destroy": [P],
         "qnb_profile_collect": [P], "qnb_profile_classes": [P, ctypes.c_uint32],
+        "qnb_set_solvent_internal": [P, I32, P, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -253,6 +254,13 @@ class NonbondedEngine:
         R = np.zeros((W, 2))
         self._check(self.lib.qnb_get_energies_dev(self.h, _p(E), _p(EQ), _p(R)))
         return [dict(zip(E_FIELDS, e)) for e in E], EQ[:, : self.S], R
+
+    def set_solvent_internal(self, pairs, A, B, el):
+        """nonbnd_solv_int: (i, j) offsets inside a solvent molecule with their
+        vdWA, vdWB, elec; evaluated for every molecule in pot_energy_nonbonds."""
+        ij = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        a, b, e = (np.ascontiguousarray(np.asarray(v, dtype=np.float64)) for v in (A, B, el))
+        self._check(self.lib.qnb_set_solvent_internal(self.h, len(a), _p(ij), _p(a), _p(b), _p(e)))
 
     def profile_classes(self, names):
         """Profile only the named kernel classes (KERNEL_CLASSES); [] stops."""
