@@ -281,6 +281,23 @@ int qnb_compute_dev(qnb_context* ctx, double Tfree, int32_t istep, int32_t sync,
 int qnb_set_solvent_internal(qnb_context* ctx, int32_t n, const int32_t* ij, const double* A, const double* B,
                              const double* el);
 
+/* Launch-geometry autotuner (no counterpart in the reference).  Times, with
+   CUDA events over `reps` evaluations of the current lists and coordinates,
+   the candidate blocks-per-SM of each per-step kernel class and of the list
+   build, one parameter at a time, and keeps the fastest.  Results are
+   independent of these choices.  The Q chunk (units per fixed-point
+   conversion of the Q energies, default 8) is kept: it sets the grouping of
+   FP32 partial sums, so changing it with qnb_set_tuning changes the Q
+   energies at the FP32 rounding level (deterministically).  Needs built lists;
+   restores the watpol running averages and clears the gradient
+   accumulators.  values (may be NULL) receives the QNB_TUNE_COUNT choices:
+   solute rows, water rows, qp, qw (blocks per SM), Q chunk (units), LRF
+   Taylor, LRF accumulation, row build (blocks per SM). */
+enum { QNB_TUNE_COUNT = 8 };
+int qnb_autotune(qnb_context* ctx, int32_t reps, int32_t* values);
+int qnb_get_tuning(qnb_context* ctx, int32_t* values);
+int qnb_set_tuning(qnb_context* ctx, const int32_t* values);
+
 /* Energies of the last qnb_compute_dev / qnb_group_compute evaluation of all
    windows, added into E[nwin], EQ[nwin*nstates], Erst[nwin*2] (waits for
    the context's stream). */

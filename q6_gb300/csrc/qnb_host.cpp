@@ -95,6 +95,7 @@ struct qnb_context {
     bool lists_built = false, qp_done = false, qw_done = false;
     bool diag_valid = false;       // mixed form: half lists for inspection built from x_build
     Cut last_cut{};
+    int last_build_nw = 1;
     int maxg = 1;                  // largest solute charge group
     bool rows_pending = false;     // mixed form: frow not yet added into d
     // CUDA-graph replay of qnb_compute_dev: one instantiated graph per
@@ -136,8 +137,9 @@ struct qnb_context {
     double* h_stage = nullptr;   // pinned staging for x / d (natom*3)
     double* h_e = nullptr;       // pinned energies (nwin x (kNumE doubles + kNumE fixed))
 
-    Launch all() const { return Launch{m, st[0], d_states, nwin, stream}; }
-    Launch one() const { return Launch{m, st[0], d_states, 1, stream}; }   // window 0 only
+    Tune tune = kTuneDefault;
+    Launch all() const { return Launch{m, st[0], d_states, nwin, stream, tune}; }
+    Launch one() const { return Launch{m, st[0], d_states, 1, stream, tune}; }   // window 0 only
 
     template <typename T>
     int alloc(T** p, size_t n) {
@@ -926,11 +928,12 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
             if (do_qp) c->qp_done = true;
             if (do_qw) c->qw_done = true;
             c->lists_built = true;
+            c->last_cut = cut;
+            c->last_build_nw = nw;
             if (c->mixed) {   // keep window 0's build coordinates for list inspection
                 CU(cudaMemcpyAsync(c->st[0].x_build, c->st[0].x, sizeof(double) * 3 * c->natom,
                                    cudaMemcpyDeviceToDevice, c->stream));
                 c->diag_valid = false;
-                c->last_cut = cut;
             }
             return QNB_OK;
         }
@@ -1013,7 +1016,7 @@ int ensure_half_lists(qnb_context* c) {
         DevState tmp = c->st[0];
         tmp.x = c->st[0].x_build;
         CU(cudaMemcpyAsync(c->d_diag, &tmp, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
-        Launch L{c->m, tmp, c->d_diag, 1, c->stream};
+        Launch L{c->m, tmp, c->d_diag, 1, c->stream, c->tune};
         unsigned keep = ~((1u << C_WW) | (1u << C_PW) | (1u << C_PP) | (1u << C_PP14) | (1u << C_PPG));
         launch_reset_counts(L, keep);
         launch_pack(L);
@@ -1517,6 +1520,117 @@ int qnb_set_solvent_internal(qnb_context* c, int32_t n, const int32_t* ij, const
         c->nsi = n;
     }
     ++c->epoch;   // a launch more (or less) per step
+    return QNB_OK;
+}
+
+int qnb_get_tuning(qnb_context* c, int32_t* values) {
+    if (!c || !values) return fail(QNB_ERR_ARG, "null argument");
+    for (int k = 0; k < T_NUM; ++k) values[k] = c->tune.v[k];
+    return QNB_OK;
+}
+
+int qnb_set_tuning(qnb_context* c, const int32_t* values) {
+    if (!c || !values) return fail(QNB_ERR_ARG, "null argument");
+    for (int k = 0; k < T_NUM; ++k)
+        if (values[k] < 1 || values[k] > 256) return fail(QNB_ERR_ARG, "tuning value %d out of 1..256", k);
+    for (int k = 0; k < T_NUM; ++k) c->tune.v[k] = values[k];
+    ++c->epoch;   // new launch geometry: captured graphs are stale
+    return QNB_OK;
+}
+
+// Autotuner: coordinate search over the launch geometry of the per-step
+// kernels (blocks per SM of the solute rows, water rows, qp, qw and LRF
+// Taylor kernels) and of the list build (row build, LRF accumulation), each
+// candidate timed with CUDA events over `reps` evaluations (or builds) of the
+// current lists and coordinates after one untimed run.  Results do not
+// depend on these choices (the mixed form is bit-identical for every one).
+// The Q-kernel chunk size is not searched: it sets the grouping of the Q
+// energies' FP32 partial sums (qnb_set_tuning can still change it).  The
+// watpol running averages are restored afterwards; the gradient accumulators
+// are cleared.
+int qnb_autotune(qnb_context* c, int32_t reps, int32_t* values) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built");
+    if (reps < 1) reps = 1;
+    CU(cudaSetDevice(c->device));
+    const size_t wsn = 3 * kMaxShell;
+    std::vector<double> ws(wsn * c->nwin);
+    for (int w = 0; w < c->nwin; ++w)
+        CU(cudaMemcpyAsync(ws.data() + wsn * w, c->st[w].wstate, sizeof(double) * wsn, cudaMemcpyDeviceToHost,
+                           c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    collect_profile(c);
+    const bool prof0 = c->profiling, graphs0 = c->use_graphs;
+    const unsigned mask0 = c->prof_mask;
+    double ms0[K_NUM];
+    int64_t n0[K_NUM];
+    for (int k = 0; k < K_NUM; ++k) ms0[k] = c->prof_ms[k], n0[k] = c->prof_n[k];
+    c->use_graphs = false;
+    const int nw = c->last_build_nw;
+    auto run = [&](bool build, unsigned mask, int count) -> int {
+        c->profiling = true;
+        c->prof_mask = mask;
+        for (int r = 0; r < count; ++r) {
+            if (build) TRY(build_lists(c, c->last_cut, nw));
+            else TRY(enqueue_compute(c, 300.0, 1));
+        }
+        collect_profile(c);
+        return QNB_OK;
+    };
+    auto measure = [&](bool build, unsigned mask, double* ms) -> int {
+        TRY(run(build, mask, 1));   // untimed: first launch of this geometry
+        for (int k = 0; k < K_NUM; ++k) c->prof_ms[k] = 0.0, c->prof_n[k] = 0;
+        TRY(run(build, mask, reps));
+        double t = 0.0;
+        for (int k = 0; k < K_NUM; ++k)
+            if ((mask >> k) & 1u) t += c->prof_ms[k];
+        *ms = t;
+        return QNB_OK;
+    };
+    struct Plan {
+        int t;
+        std::vector<int> vals;
+        unsigned mask;
+        bool build;
+    };
+    const unsigned B = 1u;
+    std::vector<Plan> plan = {
+        {T_ROWS_SOLUTE, {3, 4, 6, 8, 12, 16, 24}, B << K_PP, false},
+        {T_ROWS_WATER, {4, 6, 8, 12, 16, 24}, B << K_WW, false},
+        {T_QP, {2, 3, 4, 6, 8, 12}, B << K_QP, false},
+        {T_QW, {2, 3, 4, 6, 8, 12}, B << K_QW, false},
+        {T_TAYLOR, {4, 8, 16, 24, 32}, B << K_LRF_TAYLOR, false},
+    };
+    if (c->mixed) plan.push_back({T_BUILD, {4, 8, 16, 24, 32}, B << K_BUILD, true});
+    if (c->mixed && c->use_lrf) plan.push_back({T_LRF, {1, 2, 3, 4, 6}, B << K_LRF_BUILD, true});
+    int rc = QNB_OK;
+    for (auto& p : plan) {
+        int best = c->tune.v[p.t];
+        double best_ms = 1e30;
+        for (int v : p.vals) {
+            c->tune.v[p.t] = v;
+            double ms = 0.0;
+            rc = measure(p.build, p.mask, &ms);
+            if (rc) break;
+            if (ms < best_ms) best_ms = ms, best = v;
+        }
+        c->tune.v[p.t] = best;
+        if (rc) break;
+    }
+    // restore: profiling state, totals, watpol averages; clear the gradients
+    c->profiling = prof0;
+    c->prof_mask = mask0;
+    c->use_graphs = graphs0;
+    for (int k = 0; k < K_NUM; ++k) c->prof_ms[k] = ms0[k], c->prof_n[k] = n0[k];
+    for (int w = 0; w < c->nwin; ++w)
+        CU(cudaMemcpyAsync(c->st[w].wstate, ws.data() + wsn * w, sizeof(double) * wsn, cudaMemcpyHostToDevice,
+                           c->stream));
+    CU(cudaMemsetAsync(c->d_all, 0, sizeof(double) * 3 * (size_t)c->natom * c->nwin, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    ++c->epoch;
+    if (rc) return rc;
+    if (values)
+        for (int k = 0; k < T_NUM; ++k) values[k] = c->tune.v[k];
     return QNB_OK;
 }
 

@@ -155,12 +155,21 @@ struct Cut {
 // Every launch covers all nwin windows of a context (grid.y = window); s0 is
 // window 0's host-side state (capacities are equal across windows) and ds the
 // device array of all windows' states.
+// Launch geometry chosen by the autotuner (qnb_autotune): blocks per SM of
+// the per-step kernels and of the list build, and the Q-kernel chunk size
+enum TuneParam { T_ROWS_SOLUTE, T_ROWS_WATER, T_QP, T_QW, T_QCHUNK, T_TAYLOR, T_LRF, T_BUILD, T_NUM };
+struct Tune {
+    int v[T_NUM];
+};
+constexpr Tune kTuneDefault = {{16, 16, 8, 8, 8, 16, 3, 16}};
+
 struct Launch {
     const DevModel& m;
     const DevState& s0;
     const DevState* ds;
     int nwin;
     cudaStream_t st;
+    const Tune& tu;
 };
 
 void launch_pack(const Launch& L);

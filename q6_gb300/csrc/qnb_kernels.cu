@@ -1207,16 +1207,13 @@ struct QPairT<true, SMAX> {
 // nonbond_qw_spc / nonbond_qw (src/nonbondene.f90:5658-5767, 5339-5418) and
 // nonbond_qp (src/nonbondene.f90:5157-5230): one warp per listed environment
 // unit (a water molecule, or one solute atom), lane = Q atom.  A warp takes
-// fixed chunks of kQChunk consecutive units; the per-state energies of a
+// fixed chunks of qchunk consecutive units (autotuned); the per-state energies of a
 // chunk are summed in registers and converted once per chunk, so the fixed-
 // point totals do not depend on the grid.  An environment atom's gradient is
 // summed over the Q atoms in FP32 in a fixed shuffle order, then converted.
-#ifndef QNB_Q_CHUNK
-#define QNB_Q_CHUNK 8
-#endif
-constexpr int kQChunk = QNB_Q_CHUNK;
+
 template <bool MIX, bool SPC, bool WATER, int SMAX>
-__global__ void __launch_bounds__(kQBlock, 3) k_qenv(DevModel m, const DevState* __restrict__ states) {
+__global__ void __launch_bounds__(kQBlock, 3) k_qenv(DevModel m, const DevState* __restrict__ states, int qchunk) {
     typedef typename std::conditional<MIX, float, double>::type T;
     const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
@@ -1231,13 +1228,13 @@ __global__ void __launch_bounds__(kQBlock, 3) k_qenv(DevModel m, const DevState*
     int n = WATER ? min((int64_t)s.cnt[C_QW], s.cap_qw) : min((int64_t)s.cnt[C_QP], s.cap_qp);
     int S = m.S;
     const int na = WATER ? m.sa : 1;
-    const int nchunk = (n + kQChunk - 1) / kQChunk;
+    const int nchunk = (n + qchunk - 1) / qchunk;
     for (int ch = warp_id_global(); ch < nchunk; ch += warps_total()) {
       T pel[SMAX], pvdw[SMAX];
 #pragma unroll
       for (int st = 0; st < SMAX; ++st) pel[st] = pvdw[st] = T(0);
-      const int pend = min(n, (ch + 1) * kQChunk);
-      for (int p = ch * kQChunk; p < pend; ++p) {
+      const int pend = min(n, (ch + 1) * qchunk);
+      for (int p = ch * qchunk; p < pend; ++p) {
         int j0 = WATER ? m.nat_solute + m.sa * s.qw[p] : s.qp[p];
         for (int a = 0; a < na; ++a) {
             int j = j0 + a;
@@ -2433,7 +2430,7 @@ void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* 
 #ifndef QNB_LRF_FP64_STAGED
 #define QNB_LRF_FP64_STAGED 0
 #endif
-    dim3 g = grid_for((int64_t)L.m.ncgp * 32, kLrfBlock, 3, L.nwin);
+    dim3 g = grid_for((int64_t)L.m.ncgp * 32, kLrfBlock, L.tu.v[T_LRF], L.nwin);
     if (mixed) k_lrf_accumulate<true><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
     else if (QNB_LRF_FP64_STAGED) k_lrf_accumulate<false><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
     else k_lrf_accumulate_direct<false><<<grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
@@ -2442,14 +2439,14 @@ void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* 
 void launch_build_rows(const Launch& L, const Cut& c) {
     int nrows = L.m.ncgp_solute + L.m.nwat;
     if (nrows == 0) return;
-    k_build_rows<<<grid_for((int64_t)nrows * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c);
+    k_build_rows<<<grid_for((int64_t)nrows * 32, 128, L.tu.v[T_BUILD], L.nwin), 128, 0, L.st>>>(L.m, L.ds, c);
 }
 int lj_smem(const DevModel& m) {
     return m.natyps <= kMaxTypesShared ? (int)(m.natyps * m.natyps * sizeof(float4)) : 0;
 }
 void launch_rows_solute(const Launch& L, int maxg) {
     if (L.m.ncgp_solute == 0) return;
-    dim3 g = grid_for((int64_t)L.m.ncgp_solute * 32, 128, 16, L.nwin);
+    dim3 g = grid_for((int64_t)L.m.ncgp_solute * 32, 128, L.tu.v[T_ROWS_SOLUTE], L.nwin);
     int sm = lj_smem(L.m);
     if (maxg <= 4) k_rows_solute<4><<<g, 128, sm, L.st>>>(L.m, L.ds);
     else if (maxg <= 6) k_rows_solute<6><<<g, 128, sm, L.st>>>(L.m, L.ds);
@@ -2464,7 +2461,7 @@ void launch_solvent_internal(const Launch& L, const int2* ij, const double* par,
 }
 void launch_rows_water(const Launch& L) {
     if (L.m.nwat == 0) return;
-    dim3 g = grid_for((int64_t)L.m.nwat * 32, 128, 16, L.nwin);
+    dim3 g = grid_for((int64_t)L.m.nwat * 32, 128, L.tu.v[T_ROWS_WATER], L.nwin);
     int sm = lj_smem(L.m);
     if (L.m.spc) k_rows_water<true><<<g, 128, sm, L.st>>>(L.m, L.ds);
     else k_rows_water<false><<<g, 128, sm, L.st>>>(L.m, L.ds);
@@ -2480,7 +2477,7 @@ template <bool WATER>
 void launch_qenv(const Launch& L, int mixed, dim3 g) {
     bool spc = L.m.spc != 0;
     bool s4 = L.m.S <= 4;
-#define QL(MIX, SPC, SM) k_qenv<MIX, SPC, WATER, SM><<<g, kQBlock, 0, L.st>>>(L.m, L.ds)
+#define QL(MIX, SPC, SM) k_qenv<MIX, SPC, WATER, SM><<<g, kQBlock, 0, L.st>>>(L.m, L.ds, L.tu.v[T_QCHUNK])
     if (mixed) {
         if (spc) { if (s4) QL(true, true, 4); else QL(true, true, kMaxStates); }
         else { if (s4) QL(true, false, 4); else QL(true, false, kMaxStates); }
@@ -2492,7 +2489,7 @@ void launch_qenv(const Launch& L, int mixed, dim3 g) {
 }
 void launch_qw(const Launch& L, int mixed) {
     if (L.m.nwat == 0 || L.m.nqat == 0) return;
-    launch_qenv<true>(L, mixed, grid_for(L.s0.cap_qw * 32, kQBlock, 8, L.nwin));
+    launch_qenv<true>(L, mixed, grid_for(L.s0.cap_qw * 32, kQBlock, L.tu.v[T_QW], L.nwin));
 }
 void launch_pw(const Launch& L, int mixed) {
     if (L.m.nwat == 0 || L.m.ncgp_solute == 0) return;
@@ -2506,7 +2503,7 @@ void launch_pp(const Launch& L, int mixed) {
 }
 void launch_qp(const Launch& L, int mixed) {
     if (L.m.nqat == 0 || L.m.nat_solute == 0) return;
-    launch_qenv<false>(L, mixed, grid_for(L.s0.cap_qp * 32, kQBlock, 8, L.nwin));
+    launch_qenv<false>(L, mixed, grid_for(L.s0.cap_qp * 32, kQBlock, L.tu.v[T_QP], L.nwin));
 }
 void launch_nonbond_qq(const Launch& L, int mixed) {
     if (L.s0.nqq == 0) return;
@@ -2514,7 +2511,7 @@ void launch_nonbond_qq(const Launch& L, int mixed) {
     if (mixed) k_qq<true><<<g, 32, 0, L.st>>>(L.m, L.ds); else k_qq<false><<<g, 32, 0, L.st>>>(L.m, L.ds);
 }
 void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed) {
-    dim3 g = grid_for(L.m.natom, 64, 16, L.nwin);
+    dim3 g = grid_for(L.m.natom, 64, L.tu.v[T_TAYLOR], L.nwin);
     if (mixed) k_lrf_taylor<true><<<g, 64, 0, L.st>>>(L.m, L.ds, iwhich);
     else k_lrf_taylor<false><<<g, 64, 0, L.st>>>(L.m, L.ds, iwhich);
 }

@@ -38,8 +38,10 @@ EXPORTED = (
     "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
     "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev", "qnb_get_energies_dev", "qnb_set_graphs",
     "qnb_group_create", "qnb_group_compute", "qnb_group_destroy", "qnb_profile_collect",
-    "qnb_profile_classes", "qnb_set_solvent_internal",
+    "qnb_profile_classes", "qnb_set_solvent_internal", "qnb_autotune", "qnb_get_tuning", "qnb_set_tuning",
 )
+TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
+              "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
 KERNEL_CLASSES = ("ww", "qw", "pw", "pp", "qp", "lrf_taylor", "qq", "restrain", "watpol", "pack",
                   "apply", "build", "lrf_build")
 
@@ -88,6 +90,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_group_create": [P, I32, P], "qnb_group_compute": [P, D, I32], "qnb_group_destroy": [P],
         "qnb_profile_collect": [P], "qnb_profile_classes": [P, ctypes.c_uint32],
         "qnb_set_solvent_internal": [P, I32, P, P, P, P],
+        "qnb_autotune": [P, I32, P], "qnb_get_tuning": [P, P], "qnb_set_tuning": [P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -261,6 +264,22 @@ class NonbondedEngine:
         ij = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
         a, b, e = (np.ascontiguousarray(np.asarray(v, dtype=np.float64)) for v in (A, B, el))
         self._check(self.lib.qnb_set_solvent_internal(self.h, len(a), _p(ij), _p(a), _p(b), _p(e)))
+
+    def autotune(self, reps=3):
+        """Times the launch-geometry candidates on the current lists; returns
+        the chosen values by name (qnb_autotune)."""
+        v = np.zeros(len(TUNE_NAMES), dtype=np.int32)
+        self._check(self.lib.qnb_autotune(self.h, int(reps), _p(v)))
+        return dict(zip(TUNE_NAMES, v.tolist()))
+
+    def tuning(self):
+        v = np.zeros(len(TUNE_NAMES), dtype=np.int32)
+        self._check(self.lib.qnb_get_tuning(self.h, _p(v)))
+        return dict(zip(TUNE_NAMES, v.tolist()))
+
+    def set_tuning(self, values):
+        v = np.array([values[n] for n in TUNE_NAMES], dtype=np.int32)
+        self._check(self.lib.qnb_set_tuning(self.h, _p(v)))
 
     def profile_classes(self, names):
         """Profile only the named kernel classes (KERNEL_CLASSES); [] stops."""
