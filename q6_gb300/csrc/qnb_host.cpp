@@ -1595,14 +1595,14 @@ int qnb_autotune(qnb_context* c, int32_t reps, int32_t* values) {
     };
     const unsigned B = 1u;
     std::vector<Plan> plan = {
-        {T_ROWS_SOLUTE, {3, 4, 6, 8, 12, 16, 24}, B << K_PP, false},
-        {T_ROWS_WATER, {4, 6, 8, 12, 16, 24}, B << K_WW, false},
-        {T_QP, {2, 3, 4, 6, 8, 12}, B << K_QP, false},
-        {T_QW, {2, 3, 4, 6, 8, 12}, B << K_QW, false},
-        {T_TAYLOR, {4, 8, 16, 24, 32}, B << K_LRF_TAYLOR, false},
+        {T_ROWS_SOLUTE, {4, 6, 8, 12, 16, 24, 32, 48}, B << K_PP, false},
+        {T_ROWS_WATER, {4, 8, 12, 16, 24, 32, 48}, B << K_WW, false},
+        {T_QP, {2, 3, 4, 6, 8, 12, 16}, B << K_QP, false},
+        {T_QW, {2, 3, 4, 6, 8, 12, 16}, B << K_QW, false},
+        {T_TAYLOR, {8, 16, 24, 32, 48, 64}, B << K_LRF_TAYLOR, false},
     };
-    if (c->mixed) plan.push_back({T_BUILD, {4, 8, 16, 24, 32}, B << K_BUILD, true});
-    if (c->mixed && c->use_lrf) plan.push_back({T_LRF, {1, 2, 3, 4, 6}, B << K_LRF_BUILD, true});
+    if (c->mixed) plan.push_back({T_BUILD, {8, 16, 24, 32, 48, 64}, B << K_BUILD, true});
+    if (c->mixed && c->use_lrf) plan.push_back({T_LRF, {2, 3, 4, 6, 8, 12}, B << K_LRF_BUILD, true});
     int rc = QNB_OK;
     for (auto& p : plan) {
         int best = c->tune.v[p.t];

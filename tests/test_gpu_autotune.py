@@ -27,7 +27,7 @@ def test_autotune_keeps_results(prec):
         default = e.tuning()
         chosen = e.autotune(reps=2)
         assert set(chosen) == set(TUNE_NAMES)
-        assert all(1 <= v <= 32 for v in chosen.values())
+        assert all(1 <= v <= 64 for v in chosen.values())
         assert e.tuning() == chosen
         ws1 = e.watpol_state()
         for a, b in zip(ws0, ws1):
