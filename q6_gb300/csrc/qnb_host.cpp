@@ -260,6 +260,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     for (int k = 0; k < 3; ++k) {
         m.xpcent[k] = t->xpcent[k];
         m.xwcent[k] = t->xwcent[k];
+        m.wcoff[k] = (float)(t->xpcent[k] - t->xwcent[k]);
     }
     m.rexcl_o2 = t->rexcl_o * t->rexcl_o;
     c->rexcl_o2 = m.rexcl_o2;
@@ -743,6 +744,7 @@ int alloc_state(qnb_context* c) {
         TRY(c->alloc(&s.lrf, (size_t)std::max(1, m.ncgp) * kLrfLen));
         s.cnt = c->cnt_all + (size_t)C_NUM * w;
         TRY(c->alloc(&s.theta, (size_t)std::max(1, m.nwat)));
+        TRY(c->alloc(&s.rkey, (size_t)std::max(1, m.nwat)));
         TRY(c->alloc(&s.wvec, (size_t)8 * std::max(1, m.nwat)));
         TRY(c->alloc(&s.shell, (size_t)std::max(1, m.nwat)));
         TRY(c->alloc(&s.rank, (size_t)std::max(1, m.nwat)));
@@ -1226,7 +1228,12 @@ int qnb_set_solvent_params(qnb_context* c, const qnb_solvent_params* p) {
         s.rout[k] = p->shell_rout[k];
         s.dr[k] = p->shell_dr[k];
         s.cstb[k] = p->shell_cstb[k];
+        s.cstbf[k] = (float)p->shell_cstb[k];
     }
+    s.fk_wspheref = (float)s.fk_wsphere;
+    s.Dwmzf = (float)s.Dwmz;
+    s.awmzf = (float)s.awmz;
+    s.fkwpolf = (float)s.fkwpol;
     double ws[3 * kMaxShell] = {0};
     for (int k = 0; k < kMaxShell; ++k) ws[k] = p->theta_corr[k];
     for (int w = 0; w < c->nwin; ++w)
@@ -1243,6 +1250,7 @@ int qnb_restrain_solvent(qnb_context* c, const double* x, double* d, double Tfre
     CU(cudaSetDevice(c->device));
     TRY(stage_x(c, x));
     TRY(zero_acc(c, 1));
+    if (c->mixed) launch_pack(c->one()), c->launches++;   // the mixed kernels read the FP32 copy
     launch_restrain_solvent(c->one(), c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv);
     c->launches++;
     TRY(check_launch());
@@ -1259,6 +1267,7 @@ int qnb_watpol(qnb_context* c, const double* x, double* d, int32_t istep, int32_
     CU(cudaSetDevice(c->device));
     TRY(stage_x(c, x));
     TRY(zero_acc(c, 1));
+    if (c->mixed) launch_pack(c->one()), c->launches++;   // the mixed kernels read the FP32 copy
     c->launches += launch_watpol(c->one(), c->solv, istep, md, c->mixed);
     TRY(check_launch());
     TRY(unstage_d(c, d));

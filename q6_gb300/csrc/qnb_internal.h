@@ -94,6 +94,7 @@ struct DevModel {
     const QQAdj* qq_adj;        // parallel to the static Q-Q / Q-bonded list
     int adj_ok;                 // geometric rule: parameter gradients available
     double xpcent[3], xwcent[3];
+    float wcoff[3];             // xpcent - xwcent in FP32: packed (xpcent-centred) coordinates to xwcent-centred
     double rexcl_o2;
     // FP32 copies are stored relative to xpcent, which bounds their magnitude
     // by the sphere size (FP32 cut-off prefilter and mixed-form pair math)
@@ -137,6 +138,7 @@ struct DevState {
     int nqq_qq;                    // first nqq_qq entries are Q-Q (EQ%qq), rest Q-P (EQ%qp)
     // water polarisation
     double* theta;       // [nwat]
+    double* rkey;        // [nwat] selection-sort key (theta; 1 - cos theta in the mixed form)
     double* wvec;        // [nwat][8] unit dipole / radial vectors and lengths of the last md call
     int* shell;          // [nwat] shell or -1
     int* rank;           // [nwat]
@@ -205,6 +207,8 @@ struct SolventDev {
     double fk_wsphere, Dwmz, awmz, rwat, boltz, fkwpol, itdis;
     int wpol, nshell;
     double rout[kMaxShell], dr[kMaxShell], cstb[kMaxShell];
+    // FP32 copies for the mixed form's restraint kernels
+    float fk_wspheref, Dwmzf, awmzf, fkwpolf, cstbf[kMaxShell];
 };
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv);

@@ -130,6 +130,11 @@ struct Acc<true> {
         atomicAdd(f + 3 * i + 1, to_fix(gy));
         atomicAdd(f + 3 * i + 2, to_fix(gz));
     }
+    __device__ __forceinline__ void grad_alu(int i, float gx, float gy, float gz) const {
+        atomicAdd(f + 3 * i, to_fix_alu(gx));
+        atomicAdd(f + 3 * i + 1, to_fix_alu(gy));
+        atomicAdd(f + 3 * i + 2, to_fix_alu(gz));
+    }
     __device__ __forceinline__ void gradd(int i, double gx, double gy, double gz) const {
         atomicAdd(f + 3 * i, to_fixd(gx));
         atomicAdd(f + 3 * i + 1, to_fixd(gy));
@@ -1573,6 +1578,7 @@ __global__ void k_restrain_solvent(DevModel m, const DevState* __restrict__ stat
     const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> er;
+    const float r0f = (float)(p.rwat - shift);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < m.nwat; w += gridDim.x * blockDim.x) {
         int isw = wsw[w];
         if (m.excl[isw]) continue;
@@ -1586,6 +1592,27 @@ __global__ void k_restrain_solvent(DevModel m, const DevState* __restrict__ stat
                 if (!heavy_solv[is]) continue;
                 idist = first;
                 i = first + is;
+            }
+            if constexpr (MIX) {   // FP32 arithmetic; the two branches meet with equal value and slope at db = 0
+                float4 xa = s.xq[idist];
+                float ux = xa.x + m.wcoff[0], uy = xa.y + m.wcoff[1], uz = xa.z + m.wcoff[2];
+                float bf = sqrtf(ux * ux + uy * uy + uz * uz);
+                float dbf = bf - r0f;
+                float ef, dvf;
+                if (dbf > 0.f) {
+                    ef = 0.5f * p.fk_wspheref * (dbf * dbf) - p.Dwmzf;
+                    dvf = p.fk_wspheref * dbf / bf;
+                } else if (bf > 0.f) {
+                    float fexp = expf(p.awmzf * dbf);
+                    ef = p.Dwmzf * (fexp * fexp - 2.f * fexp);
+                    dvf = -2.f * p.Dwmzf * p.awmzf * (fexp - fexp * fexp) / bf;
+                } else {
+                    ef = 0.f;
+                    dvf = 0.f;
+                }
+                acc.grad_alu(i, ux * dvf, uy * dvf, uz * dvf);
+                er.add_alu(ef);
+                continue;
             }
             double vx = s.x[3 * idist] - m.xwcent[0], vy = s.x[3 * idist + 1] - m.xwcent[1],
                    vz = s.x[3 * idist + 2] - m.xwcent[2];
@@ -1642,28 +1669,96 @@ __device__ __forceinline__ void water_vectors(const DevModel& m, const double* x
     rcx /= rc; rcy /= rc; rcz /= rc;
 }
 
+// SPC water vectors in FP32 from the packed (xpcent-centred) coordinates:
+// dipole direction H1 + H2 - 2 O and radial vector O - xwcent, with lengths
+__device__ __forceinline__ void water_vectors_f(const DevModel& m, const float4* __restrict__ xq, int w, float& rmx,
+                                                float& rmy, float& rmz, float& rm, float& rcx, float& rcy,
+                                                float& rcz, float& rc) {
+    int i = m.nat_solute + 3 * w;
+    float4 o = xq[i], h1 = xq[i + 1], h2 = xq[i + 2];
+    float ux = h1.x + h2.x - 2.f * o.x, uy = h1.y + h2.y - 2.f * o.y, uz = h1.z + h2.z - 2.f * o.z;
+    rcx = o.x + m.wcoff[0];
+    rcy = o.y + m.wcoff[1];
+    rcz = o.z + m.wcoff[2];
+    rm = sqrtf(ux * ux + uy * uy + uz * uz);
+    rmx = ux / rm; rmy = uy / rm; rmz = uz / rm;
+    rc = sqrtf(rcx * rcx + rcy * rcy + rcz * rcz);
+    rcx /= rc; rcy /= rc; rcz /= rc;
+}
+
+// Shell of a water from its radial distance rc: the outer shells beyond
+// rout[N-1] - dr[N-1] (src/nonbondene.f90:6590-6606).  `rcd` is exact FP64.
+__device__ __forceinline__ int watpol_shell(const SolventDev& p, double rcd) {
+    int N = p.nshell;
+    if (!(rcd > p.rout[N - 1] - p.dr[N - 1])) return -1;
+    int is;
+    for (is = N - 1; is >= 1; --is)
+        if (rcd <= p.rout[is]) break;
+    return is < 0 ? 0 : is;
+}
+
+// Mixed form (SPC): the selection order is decided in FP64, on the key
+// 1 - cos(theta) from FP64 dot products (one square root and one division
+// instead of the reference's six divisions and an arc cosine; it orders like
+// theta), because swapping two waters' targets changes their forces by
+// fkwpol * dtheta0.  Theta and the unit vectors for the energy and forces
+// are FP32 from the same FP64 differences, and the shell of every water is
+// decided exactly: the FP32 distance decides away from the shell radii, the
+// FP64 distance within 2e-4 of one.
+template <bool MIX>
 __global__ void k_watpol_theta(DevModel m, const DevState* __restrict__ states, SolventDev p) {
     const DevState& s = states[blockIdx.y];
     int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= m.nwat) return;
     s.shell[w] = -1;
     s.theta[w] = 0.0;
+    s.rkey[w] = 0.0;
     int i = m.nat_solute + m.sa * w;
     if (m.excl[i]) return;
-    double rmx, rmy, rmz, rm, rcx, rcy, rcz, rc;
-    water_vectors(m, s.x, w, rmx, rmy, rmz, rm, rcx, rcy, rcz, rc);
-    double scp = rmx * rcx + rmy * rcy + rmz * rcz;
-    scp = fmin(1.0, fmax(-1.0, scp));
-    s.theta[w] = acos(scp);
     double* v = s.wvec + 8 * (size_t)w;   // reused by k_watpol_force in the same call
-    v[0] = rmx; v[1] = rmy; v[2] = rmz; v[3] = rm;
-    v[4] = rcx; v[5] = rcy; v[6] = rcz; v[7] = rc;
-    int N = p.nshell;
-    if (rc > p.rout[N - 1] - p.dr[N - 1]) {
-        int is;
-        for (is = N - 1; is >= 1; --is)
-            if (rc <= p.rout[is]) break;
-        if (is < 0) is = 0;
+    double rcd;
+    if (MIX && m.sa == 3) {
+        const double* x = s.x;
+        double ux = x[3 * (i + 1)] + x[3 * (i + 2)] - 2.0 * x[3 * i];
+        double uy = x[3 * (i + 1) + 1] + x[3 * (i + 2) + 1] - 2.0 * x[3 * i + 1];
+        double uz = x[3 * (i + 1) + 2] + x[3 * (i + 2) + 2] - 2.0 * x[3 * i + 2];
+        double qx = x[3 * i] - m.xwcent[0], qy = x[3 * i + 1] - m.xwcent[1], qz = x[3 * i + 2] - m.xwcent[2];
+        double uu = ux * ux + uy * uy + uz * uz, rr = qx * qx + qy * qy + qz * qz, ur = ux * qx + uy * qy + uz * qz;
+        double scp64 = fmin(1.0, fmax(-1.0, ur / sqrt(uu * rr)));
+        s.rkey[w] = 1.0 - scp64;
+        float rm = sqrtf((float)uu), rc = sqrtf((float)rr);
+        float rmx = (float)ux / rm, rmy = (float)uy / rm, rmz = (float)uz / rm;
+        float rcx = (float)qx / rc, rcy = (float)qy / rc, rcz = (float)qz / rc;
+        s.theta[w] = (double)acosf((float)scp64);
+        v[0] = rmx; v[1] = rmy; v[2] = rmz; v[3] = rm;
+        v[4] = rcx; v[5] = rcy; v[6] = rcz; v[7] = rc;
+        bool near = false;
+        for (int k = 0; k < p.nshell; ++k) {
+            float t = (float)p.rout[k];
+            near |= fabsf(rc - t) <= 2e-4f * t;
+        }
+        {
+            float t = (float)(p.rout[p.nshell - 1] - p.dr[p.nshell - 1]);
+            near |= fabsf(rc - t) <= 2e-4f * t;
+        }
+        if (near) {   // the reference's FP64 distance
+            rcd = sqrt(rr);
+        } else {
+            rcd = (double)rc;
+        }
+    } else {
+        double rmx, rmy, rmz, rm, rcx, rcy, rcz, rc;
+        water_vectors(m, s.x, w, rmx, rmy, rmz, rm, rcx, rcy, rcz, rc);
+        double scp = rmx * rcx + rmy * rcy + rmz * rcz;
+        scp = fmin(1.0, fmax(-1.0, scp));
+        s.theta[w] = acos(scp);
+        s.rkey[w] = s.theta[w];
+        v[0] = rmx; v[1] = rmy; v[2] = rmz; v[3] = rm;
+        v[4] = rcx; v[5] = rcy; v[6] = rcz; v[7] = rc;
+        rcd = rc;
+    }
+    int is = watpol_shell(p, rcd);
+    if (is >= 0) {
         s.shell[w] = is;
         int k = atomicAdd(s.n_insh + is, 1);
         s.shell_list[(size_t)is * m.nwat + k] = w;
@@ -1678,7 +1773,8 @@ __global__ void k_watpol_theta(DevModel m, const DevState* __restrict__ states, 
 constexpr int kRankBlock = 512;
 __global__ void __launch_bounds__(kRankBlock) k_watpol_rank(DevModel m, const DevState* __restrict__ states) {
     const DevState& s = states[blockIdx.y];
-    // theta >= 0, so the bit patterns of the doubles order like the values;
+    // the keys (theta, or 1 - cos theta in the mixed form) are >= 0, so the
+    // bit patterns of the doubles order like the values;
     // integer compares keep the sort off the (narrow) FP64 pipe
     __shared__ long long th[1024];
     __shared__ int ww[1024];
@@ -1690,7 +1786,7 @@ __global__ void __launch_bounds__(kRankBlock) k_watpol_rank(DevModel m, const De
         __syncthreads();
         for (int k = threadIdx.x; k < cn; k += blockDim.x) {
             ww[k] = L[base + k];
-            th[k] = __double_as_longlong(s.theta[ww[k]]);
+            th[k] = __double_as_longlong(s.rkey[ww[k]]);
         }
         __syncthreads();
         for (int k = warp; k < n; k += nw) {
@@ -1701,7 +1797,7 @@ __global__ void __launch_bounds__(kRankBlock) k_watpol_rank(DevModel m, const De
                 t = th[k - base];
             } else {
                 w = L[k];
-                t = __double_as_longlong(s.theta[w]);
+                t = __double_as_longlong(s.rkey[w]);
             }
             int r = 0;
             for (int v = lane; v < cn; v += kWarp) r += (th[v] < t) || (th[v] == t && ww[v] < w);
@@ -1767,6 +1863,38 @@ __global__ void k_watpol_force(DevModel m, const DevState* __restrict__ states, 
         if (sh < 0) continue;
         int n = s.n_insh[sh];
         int il = s.rank[w] + 1;
+        if constexpr (MIX) {
+            if (m.sa == 3) {   // FP32 arithmetic (the theta kernel's FP32 vectors when STORED)
+                const float pif = 3.14159265f;
+                float arg = 1.f + (1.f - 2.f * (float)il) / (float)n;
+                float t0 = acosf(arg);
+                t0 = t0 - 3.f * sinf(t0) * p.cstbf[sh] / 2.f;
+                t0 = fminf(fmaxf(t0, 0.f), pif);
+                float th = (float)s.theta[w];
+                float dth = th - t0 + (float)s.wstate[sh];
+                ep.add_alu(0.5f * p.fkwpolf * dth * dth);
+                float dv = p.fkwpolf * dth;
+                float rmx, rmy, rmz, rm, rcx, rcy, rcz, rc;
+                if constexpr (STORED) {
+                    const double* v = s.wvec + 8 * (size_t)w;
+                    rmx = (float)v[0]; rmy = (float)v[1]; rmz = (float)v[2]; rm = (float)v[3];
+                    rcx = (float)v[4]; rcy = (float)v[5]; rcz = (float)v[6]; rc = (float)v[7];
+                } else {
+                    water_vectors_f(m, s.xq, w, rmx, rmy, rmz, rm, rcx, rcy, rcz, rc);
+                }
+                float scp = fminf(1.f, fmaxf(-1.f, rmx * rcx + rmy * rcy + rmz * rcz));
+                float f0 = STORED ? sinf(th) : sinf(acosf(scp));
+                if (fabsf(f0) < 1.0e-10f) f0 = 1.0e-10f;
+                f0 = dv * (-1.f / f0);
+                float f3x = (rcx - rmx * scp) / rm, f3y = (rcy - rmy * scp) / rm, f3z = (rcz - rmz * scp) / rm;
+                float f2x = (rmx - rcx * scp) / rc, f2y = (rmy - rcy * scp) / rc, f2z = (rmz - rcz * scp) / rc;
+                int i = m.nat_solute + 3 * w;
+                acc.grad_alu(i, (-2.f * f3x + f2x) * f0, (-2.f * f3y + f2y) * f0, (-2.f * f3z + f2z) * f0);
+                acc.grad_alu(i + 1, f3x * f0, f3y * f0, f3z * f0);
+                acc.grad_alu(i + 2, f3x * f0, f3y * f0, f3z * f0);
+                continue;
+            }
+        }
         double arg = 1.0 + (1.0 - 2.0 * (double)il) / (double)n;
         double t0 = acos(arg);
         t0 = t0 - 3.0 * sin(t0) * p.cstb[sh] / 2.0;
@@ -2546,7 +2674,8 @@ int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int m
     dim3 gw((L.m.nwat + 31) / 32, L.nwin);   // FP64 math per water: 32-thread blocks
     if (md) {
         k_watpol_reset<<<L.nwin, kMaxShell, 0, L.st>>>(L.ds);
-        k_watpol_theta<<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+        if (mixed) k_watpol_theta<true><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
+        else k_watpol_theta<false><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
         k_watpol_rank<<<dim3(p.nshell, L.nwin), kRankBlock, 0, L.st>>>(L.m, L.ds);
         nl += 3;
     }
