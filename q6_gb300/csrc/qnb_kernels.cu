@@ -2318,6 +2318,25 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
             __syncwarp();
         }
         // ---- water partners (nonbond_pw, src/nonbondene.f90:4856-4916); energy counted here
+        if (m.sa == 3 && m.wlj_mask == 1u) {   // SPC: O with LJ, two LJ-free H; the molecule loaded at once
+          const float qo = m.wcrgf[0], qh1 = m.wcrgf[1], qh2 = m.wcrgf[2];
+          const int to = m.wtype[0];
+          for (int k = lane; k < npw; k += kWarp) {
+            int j0 = m.nat_solute + 3 * (k < kRowChunk ? sh_pw[wib][k] : rw[k]);
+            float4 xo = xq[j0], xh1 = xq[j0 + 1], xh2 = xq[j0 + 2];
+#pragma unroll
+            for (int a = 0; a < MAXG; ++a) {
+                if (qa[a]) continue;
+                float4 p = lj(ta[a], to);
+                float v1, d1, v2, d2, v3, d3;
+                pair_f(xa[a], xo, p.x, p.y, xa[a].w * qo, true, f[a][0], f[a][1], f[a][2], v1, d1);
+                pair_f(xa[a], xh1, 0.f, 0.f, xa[a].w * qh1, false, f[a][0], f[a][1], f[a][2], v2, d2);
+                pair_f(xa[a], xh2, 0.f, 0.f, xa[a].w * qh2, false, f[a][0], f[a][1], f[a][2], v3, d3);
+                rwel += v1 + v2 + v3;
+                rwvdw += d1;
+            }
+          }
+        } else {
         for (int k = lane; k < npw; k += kWarp) {
             int j0 = m.nat_solute + m.sa * (k < kRowChunk ? sh_pw[wib][k] : rw[k]);
             for (int b = 0; b < m.sa; ++b) {
@@ -2343,6 +2362,7 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
                     }
                 }
             }
+        }
         }
         __syncwarp();   // sh_pw is refilled by the next row
         // The row owns its atoms' pp and pw gradient and its energies: FP32
