@@ -544,6 +544,14 @@ int build_model(qnb_context* c, const qnb_topology* t) {
         qp_tabf[k] = QParF{(float)qp_tab[k].A, (float)qp_tab[k].B, (float)qp_tab[k].el, (float)qp_tab[k].sc};
     TRY(c->upload((QPar**)&m.qp_tab, qp_tab));
     TRY(c->upload((QParF**)&m.qp_tabf, qp_tabf));
+    // the same FP32 table ordered [Q atom][solute atom][state]: lanes that
+    // take consecutive solute atoms read consecutive entries
+    std::vector<QParF> qp_tabft(qp_tabf.size());
+    for (int jq = 0; jq < nq; ++jq)
+        for (int ig = 0; ig < ns; ++ig)
+            for (int s2 = 0; s2 < S; ++s2)
+                qp_tabft[((size_t)jq * ns + ig) * S + s2] = qp_tabf[((size_t)ig * nq + jq) * S + s2];
+    TRY(c->upload((QParF**)&m.qp_tabft, qp_tabft));
 
     // qw_int_comp + precompute_set_values_qw, src/simprep.f90:3272-3292, 3517-3558
     std::vector<QPar> qw_tab((size_t)std::max(nq, 1) * std::max(sa, 1) * std::max(S, 1));

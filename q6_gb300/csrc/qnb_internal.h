@@ -86,6 +86,7 @@ struct DevModel {
     const int* iqseq;           // [nqat]
     const QPar* qp_tab;         // [nat_solute][nqat][S]
     const QParF* qp_tabf;
+    const QParF* qp_tabft;      // [nqat][nat_solute][S] (the transposed Q kernel's order)
     const QPar* qw_tab;         // [nqat][sa][S]
     const QParF* qw_tabf;
     // adjoint factors (c, a, b, unused) with the layouts of qp_tab / qw_tab

@@ -1337,6 +1337,102 @@ __global__ void __launch_bounds__(kQBlock, 3) k_qenv(DevModel m, const DevState*
 //   dE/dqcrg += c_j / r,  dE/dqA += a_j / (r^6+alpha)^2,  dE/dqB -= b_j / (r^6+alpha).
 // One warp per environment unit, lane = Q atom, sums in FP64 registers.
 // ---------------------------------------------------------------------------
+// Mixed form, transposed: lane = environment unit (a listed solute atom or
+// water), each warp taking a fixed chunk of 32 consecutive units, and a loop
+// over the Q atoms with their coordinates in shared memory.  An environment
+// atom's gradient stays in its lane (stored once, no reduction); a Q atom's
+// gradient is a fixed-order warp sum per Q atom and chunk, added to the
+// block's fixed-point total; each unit's per-state energies are converted
+// once.  The sums do not depend on the grid.  qw's parameters are the same
+// for all lanes (broadcast); qp's come from the [Q atom][solute atom] table,
+// so lanes holding consecutive solute atoms read consecutive entries.
+template <bool SPC, bool WATER, int SMAX>
+__global__ void __launch_bounds__(kQBlock) k_qenv_lanes(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
+    __shared__ unsigned long long red[3 * kMaxQ];
+    __shared__ float4 sq[kMaxQ];
+    for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) red[k] = 0ull;
+    for (int k = threadIdx.x; k < m.nqat; k += blockDim.x) sq[k] = s.xq[m.iqseq[k]];
+    __syncthreads();
+    Acc<true> acc = make_acc<true>(s);
+    ESum<true> eel[SMAX], evdw[SMAX];
+    float lam[SMAX];
+#pragma unroll
+    for (int st = 0; st < SMAX; ++st) lam[st] = st < m.S ? (float)s.lambda[st] : 0.f;
+    const int lane = threadIdx.x & 31, S = m.S, nq = m.nqat;
+    const int n = WATER ? min((int64_t)s.cnt[C_QW], s.cap_qw) : min((int64_t)s.cnt[C_QP], s.cap_qp);
+    constexpr int NA = WATER ? kMaxSolv : 1;
+    const int na = WATER ? m.sa : 1;
+    for (int c0 = warp_id_global() * kWarp; c0 < n; c0 += warps_total() * kWarp) {
+        const int p = c0 + lane;
+        const bool act = p < n;
+        const int j0 = act ? (WATER ? m.nat_solute + m.sa * s.qw[p] : s.qp[p]) : 0;
+        float4 xj[NA];
+        float gj[NA][3];
+#pragma unroll
+        for (int a = 0; a < NA; ++a) {
+            gj[a][0] = gj[a][1] = gj[a][2] = 0.f;
+            xj[a] = (act && a < na) ? s.xq[j0 + a] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        float pel[SMAX], pvdw[SMAX];
+#pragma unroll
+        for (int st = 0; st < SMAX; ++st) pel[st] = pvdw[st] = 0.f;
+        for (int iq = 0; iq < nq; ++iq) {
+            const float4 xi = sq[iq];
+            float gx = 0.f, gy = 0.f, gz = 0.f;
+            if (act) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) {
+                    if (a >= na) break;
+                    const bool lj = !WATER || !SPC || a == 0;
+                    float tx = xj[a].x - xi.x, ty = xj[a].y - xi.y, tz = xj[a].z - xi.z;
+                    float r = rsqrtf(tx * tx + ty * ty + tz * tz), r2 = r * r;
+                    const QParF* P = WATER ? m.qw_tabf + (iq * m.sa + a) * S
+                                           : m.qp_tabft + ((size_t)iq * m.nat_solute + j0) * S;
+                    float dvs = QPairT<true, SMAX>::run(P, lam, S, lj, r2, r, pel, pvdw);
+                    gx -= tx * dvs; gy -= ty * dvs; gz -= tz * dvs;
+                    gj[a][0] += tx * dvs; gj[a][1] += ty * dvs; gj[a][2] += tz * dvs;
+                }
+            }
+            gx = warp_sum(gx);
+            gy = warp_sum(gy);
+            gz = warp_sum(gz);
+            if (lane == 0) {
+                atomicAdd(&red[3 * iq], to_fix_alu(gx));
+                atomicAdd(&red[3 * iq + 1], to_fix_alu(gy));
+                atomicAdd(&red[3 * iq + 2], to_fix_alu(gz));
+            }
+        }
+        if (act) {
+#pragma unroll
+            for (int a = 0; a < NA; ++a) {
+                if (a >= na) break;
+                s.fq[3 * (j0 + a)] = gj[a][0];
+                s.fq[3 * (j0 + a) + 1] = gj[a][1];
+                s.fq[3 * (j0 + a) + 2] = gj[a][2];
+            }
+#pragma unroll
+            for (int st = 0; st < SMAX; ++st) {
+                if (st >= S) break;
+                eel[st].add_alu(pel[st]);
+                evdw[st].add_alu(pvdw[st]);
+            }
+        }
+    }
+    const int kel = WATER ? 4 : 2;
+#pragma unroll
+    for (int st = 0; st < SMAX; ++st) {
+        if (st >= S) break;
+        eel[st].flush(acc, eq_slot(st, kel));
+        evdw[st].flush(acc, eq_slot(st, kel + 1));
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * nq; k += blockDim.x) {
+        unsigned long long v = red[k];
+        if (v) atomicAdd(s.fix + 3 * m.iqseq[k / 3] + k % 3, v);
+    }
+}
+
 template <bool MIX, bool SPC, bool WATER, int SMAX>
 __global__ void __launch_bounds__(kQBlock) k_qadj_env(DevModel m, const DevState* __restrict__ states) {
     const DevState& s = states[blockIdx.y];
@@ -2621,12 +2717,19 @@ void launch_ww(const Launch& L, int mixed) {
     if (mixed) { if (spc) k_ww<true, true><<<g, 256, 0, L.st>>>(L.m, L.ds); else k_ww<true, false><<<g, 256, 0, L.st>>>(L.m, L.ds); }
     else { if (spc) k_ww<false, true><<<g, 256, 0, L.st>>>(L.m, L.ds); else k_ww<false, false><<<g, 256, 0, L.st>>>(L.m, L.ds); }
 }
+#ifndef QNB_Q_LANES
+#define QNB_Q_LANES 1   // mixed form: k_qenv_lanes (1) or k_qenv (0)
+#endif
 template <bool WATER>
 void launch_qenv(const Launch& L, int mixed, dim3 g) {
     bool spc = L.m.spc != 0;
     bool s4 = L.m.S <= 4;
 #define QL(MIX, SPC, SM) k_qenv<MIX, SPC, WATER, SM><<<g, kQBlock, 0, L.st>>>(L.m, L.ds, L.tu.v[T_QCHUNK])
-    if (mixed) {
+#define QT(SPC, SM) k_qenv_lanes<SPC, WATER, SM><<<g, kQBlock, 0, L.st>>>(L.m, L.ds)
+    if (mixed && QNB_Q_LANES) {
+        if (spc) { if (s4) QT(true, 4); else QT(true, kMaxStates); }
+        else { if (s4) QT(false, 4); else QT(false, kMaxStates); }
+    } else if (mixed) {
         if (spc) { if (s4) QL(true, true, 4); else QL(true, true, kMaxStates); }
         else { if (s4) QL(true, false, 4); else QL(true, false, kMaxStates); }
     } else {
@@ -2634,6 +2737,7 @@ void launch_qenv(const Launch& L, int mixed, dim3 g) {
         else { if (s4) QL(false, false, 4); else QL(false, false, kMaxStates); }
     }
 #undef QL
+#undef QT
 }
 void launch_qw(const Launch& L, int mixed) {
     if (L.m.nwat == 0 || L.m.nqat == 0) return;
