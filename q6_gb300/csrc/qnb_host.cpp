@@ -69,6 +69,8 @@ int qnb::set_error(int code, const char* msg) {
 struct qnb_context {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;   // list build: the LRF accumulation runs beside the row build
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int mixed = 0;
     int use_lrf = 1;
     // host copies of the model pieces the host logic needs
@@ -180,7 +182,7 @@ cudaEvent_t take_event(qnb_context* c) {
 // runs f (which enqueues kernels on c->stream), bracketed by events when
 // profiling is on
 template <typename F>
-void timed(qnb_context* c, int k, F&& f) {
+void timed_on(qnb_context* c, cudaStream_t st, int k, F&& f) {
     if (!c->profiling || !((c->prof_mask >> k) & 1u)) {
         f();
         return;
@@ -189,11 +191,15 @@ void timed(qnb_context* c, int k, F&& f) {
     // inside a capture, an external record becomes an event-record node that
     // records the event on every replay (a plain record only orders streams)
     const unsigned fl = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-    cudaEventRecordWithFlags(a, c->stream, fl);
+    cudaEventRecordWithFlags(a, st, fl);
     f();
-    cudaEventRecordWithFlags(b, c->stream, fl);
+    cudaEventRecordWithFlags(b, st, fl);
     if (c->capturing) c->cap_pending.push_back({k, a, b, true});
     else c->pending.push_back({k, a, b, false});
+}
+template <typename F>
+void timed(qnb_context* c, int k, F&& f) {
+    timed_on(c, c->stream, k, f);
 }
 
 void collect_profile(qnb_context* c) {
@@ -912,6 +918,17 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
         timed(c, K_BUILD, [&] {
             launch_pack(L);
             if (c->use_lrf) launch_group_centres(L), ++nl;
+        });
+        // the LRF accumulation (needs the packed coordinates and the group
+        // centres only) runs on the second stream beside the list builds
+        if (c->use_lrf) {
+            CU(cudaEventRecord(c->ev_fork, c->stream));
+            CU(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
+            Launch L2{L.m, L.s0, L.ds, L.nwin, c->stream2, L.tu};
+            timed_on(c, c->stream2, K_LRF_BUILD, [&] { launch_lrf_accumulate(L2, cut, c->mixed, c->d_lrf_src); });
+            CU(cudaEventRecord(c->ev_join, c->stream2));
+        }
+        timed(c, K_BUILD, [&] {
             if (c->mixed) {
                 launch_build_rows(L, cut), ++nl;
             } else {
@@ -924,10 +941,7 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
             if (c->mixed && (do_qp || do_qw)) launch_clear_fq(L), ++nl;   // atoms may leave the Q lists
         });
         c->launches += nl + (c->use_lrf ? 1 : 0);
-        if (c->use_lrf) {
-            timed(c, K_LRF_BUILD, [&] { launch_lrf_accumulate(L, cut, c->mixed, c->d_lrf_src); });
-            c->launches++;
-        }
+        if (c->use_lrf) CU(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
         TRY(check_launch());
         CU(cudaMemcpyAsync(c->counts.data(), c->cnt_all, sizeof(int) * C_NUM * nw, cudaMemcpyDeviceToHost,
                            c->stream));
@@ -1103,7 +1117,10 @@ int qnb_create_batch(const qnb_topology* t, const qnb_options* opt, int32_t nwin
     c->nqat = t->nqat;
     c->S = t->nstates;
     int rc = QNB_OK;
-    if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
         rc = fail(QNB_ERR_CUDA, "stream creation failed");
     if (!rc) rc = build_model(c, t);
     if (!rc) rc = alloc_state(c);
@@ -1140,6 +1157,9 @@ int qnb_destroy(qnb_context* c) {
         }
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->h_e) cudaFreeHost(c->h_e);
+    if (c->stream2) cudaStreamSynchronize(c->stream2), cudaStreamDestroy(c->stream2);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return QNB_OK;
