@@ -1534,12 +1534,22 @@ __global__ void k_qadj_qq(DevModel m, const DevState* __restrict__ states) {
 
 // nonbond_qq + nonbond_qqp (static lists), src/nonbondene.f90:5013-5153,
 // pair kernel nbe_qq, src/nonbonded.f90:111-150.  Always FP64: few pairs.
+// Every pair touches a Q atom and one of a few energy slots, so the Q atoms'
+// gradients and the energies are summed in shared memory per block (fixed
+// point in the mixed form) and added once per block: global atomics on those
+// few addresses serialise.
 template <bool MIX>
-__global__ void k_qq(DevModel m, const DevState* __restrict__ states) {
+__global__ void __launch_bounds__(256) k_qq(DevModel m, const DevState* __restrict__ states) {
+    typedef typename std::conditional<MIX, unsigned long long, double>::type GT;
+    __shared__ GT red[3 * kMaxQ];
+    __shared__ GT rede[kNumE];
     const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
+    for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) red[k] = GT(0);
+    for (int k = threadIdx.x; k < kNumE; k += blockDim.x) rede[k] = GT(0);
+    __syncthreads();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= s.nqq) return;
+    if (p < s.nqq) {
     QQEntry e = s.qq[p];
     double tx = s.x[3 * e.j] - s.x[3 * e.i], ty = s.x[3 * e.j + 1] - s.x[3 * e.i + 1],
            tz = s.x[3 * e.j + 2] - s.x[3 * e.i + 2];
@@ -1561,16 +1571,45 @@ __global__ void k_qq(DevModel m, const DevState* __restrict__ states) {
         dv = r2 * (-vel - (12.0 * va - 6.0 * vb) * r6 * r6_hc) * lam;
     }
     int kel = p < s.nqq_qq ? 0 : 2;
+    const double g[2][3] = {{-tx * dv, -ty * dv, -tz * dv}, {tx * dv, ty * dv, tz * dv}};
+    const int at[2] = {e.i, e.j};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        int iq = m.iqatom[at[h]];
+        if (iq >= 0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if constexpr (MIX) atomicAdd(&red[3 * iq + c], to_fixd(g[h][c]));
+                else atomicAdd(&red[3 * iq + c], g[h][c]);
+            }
+        } else {
+            if constexpr (MIX) acc.gradd(at[h], g[h][0], g[h][1], g[h][2]);
+            else acc.grad(at[h], g[h][0], g[h][1], g[h][2]);
+        }
+    }
     if constexpr (!MIX) {
-        acc.grad(e.i, -tx * dv, -ty * dv, -tz * dv);
-        acc.grad(e.j, tx * dv, ty * dv, tz * dv);
-        acc.energy(eq_slot(e.s, kel), vel);
-        acc.energy(eq_slot(e.s, kel + 1), va - vb);
+        atomicAdd(&rede[eq_slot(e.s, kel)], vel);
+        atomicAdd(&rede[eq_slot(e.s, kel + 1)], va - vb);
     } else {
-        acc.gradd(e.i, -tx * dv, -ty * dv, -tz * dv);
-        acc.gradd(e.j, tx * dv, ty * dv, tz * dv);
-        acc.energy_fix(eq_slot(e.s, kel), to_fixd(vel));
-        acc.energy_fix(eq_slot(e.s, kel + 1), to_fixd(va - vb));
+        atomicAdd(&rede[eq_slot(e.s, kel)], to_fixd(vel));
+        atomicAdd(&rede[eq_slot(e.s, kel + 1)], to_fixd(va - vb));
+    }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kNumE; k += blockDim.x) {
+        GT v = rede[k];
+        if (v != GT(0)) {
+            if constexpr (MIX) acc.energy_fix(k, v);
+            else acc.energy(k, v);
+        }
+    }
+    for (int k = threadIdx.x; k < 3 * m.nqat; k += blockDim.x) {
+        GT v = red[k];
+        if (v != GT(0)) {
+            int i = m.iqseq[k / 3];
+            if constexpr (MIX) atomicAdd(s.fix + 3 * i + k % 3, v);
+            else atomicAdd(s.d + 3 * i + k % 3, v);
+        }
     }
 }
 
@@ -1629,11 +1668,13 @@ __global__ void k_apply_fixed(int n, const DevState* __restrict__ states, int ro
     }
 }
 
-// Row energies of the mixed form summed in row order in FP64 (one block per
-// window, fixed reduction tree): the pp/pw/ww energy slots.
-__global__ void __launch_bounds__(256) k_row_sums(DevModel m, const DevState* __restrict__ states) {
+// Row energies of the mixed form summed in FP64 (one block per window, a
+// fixed reduction tree): the pp/pw/ww energy slots.
+constexpr int kRowSumBlock = 512;
+__global__ void __launch_bounds__(kRowSumBlock) k_row_sums(DevModel m, const DevState* __restrict__ states) {
     const DevState& s = states[blockIdx.x];
-    __shared__ double red[6][256];
+    __shared__ double red[kRowSumBlock / 32][6];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     const int nrows = m.ncgp_solute + m.nwat;
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
@@ -1645,21 +1686,25 @@ __global__ void __launch_bounds__(256) k_row_sums(DevModel m, const DevState* __
         }
     }
 #pragma unroll
-    for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = a[k];
-    __syncthreads();
-    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-        if (threadIdx.x < h)
+    for (int k = 0; k < 6; ++k) a[k] = warp_sum(a[k]);
+    if (lane == 0)
 #pragma unroll
-            for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {   // the only writer of these slots in the mixed form
-        s.e[E_PP_EL] += red[0][0];
-        s.e[E_PP_VDW] += red[1][0];
-        s.e[E_PW_EL] += red[2][0];
-        s.e[E_PW_VDW] += red[3][0];
-        s.e[E_WW_EL] += red[4][0];
-        s.e[E_WW_VDW] += red[5][0];
+        for (int k = 0; k < 6; ++k) red[warp][k] = a[k];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            double v = lane < kRowSumBlock / 32 ? red[lane][k] : 0.0;
+            a[k] = warp_sum(v);
+        }
+        if (lane == 0) {   // the only writer of these slots in the mixed form
+            s.e[E_PP_EL] += a[0];
+            s.e[E_PP_VDW] += a[1];
+            s.e[E_PW_EL] += a[2];
+            s.e[E_PW_VDW] += a[3];
+            s.e[E_WW_EL] += a[4];
+            s.e[E_WW_VDW] += a[5];
+        }
     }
 }
 
@@ -1862,11 +1907,13 @@ __global__ void k_watpol_theta(DevModel m, const DevState* __restrict__ states, 
 }
 
 // stable selection order of src/nonbondene.f90:6612-6628: rank = number of
-// waters of the same shell with smaller theta, ties broken by water index
+// waters of the same shell with a smaller key, ties broken by water index
 // (the reference scans the shell in water order and keeps the first minimum).
-// One block per shell; the shell's thetas are staged in shared memory and one
-// warp ranks one water at a time, its lanes splitting the comparisons.
-constexpr int kRankBlock = 512;
+// kRankParts blocks per shell: each stages the whole shell's keys in shared
+// memory and ranks its share of the waters, one warp per water with the
+// lanes splitting the comparisons.
+constexpr int kRankBlock = 256;
+constexpr int kRankParts = 4;
 __global__ void __launch_bounds__(kRankBlock) k_watpol_rank(DevModel m, const DevState* __restrict__ states) {
     const DevState& s = states[blockIdx.y];
     // the keys (theta, or 1 - cos theta in the mixed form) are >= 0, so the
@@ -1874,7 +1921,7 @@ __global__ void __launch_bounds__(kRankBlock) k_watpol_rank(DevModel m, const De
     // integer compares keep the sort off the (narrow) FP64 pipe
     __shared__ long long th[1024];
     __shared__ int ww[1024];
-    const int sh = blockIdx.x, n = s.n_insh[sh];
+    const int sh = blockIdx.x / kRankParts, part = blockIdx.x % kRankParts, n = s.n_insh[sh];
     const int* L = s.shell_list + (size_t)sh * m.nwat;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int base = 0; base < n; base += 1024) {
@@ -1885,7 +1932,7 @@ __global__ void __launch_bounds__(kRankBlock) k_watpol_rank(DevModel m, const De
             th[k] = __double_as_longlong(s.rkey[ww[k]]);
         }
         __syncthreads();
-        for (int k = warp; k < n; k += nw) {
+        for (int k = part * nw + warp; k < n; k += kRankParts * nw) {
             int w;
             long long t;
             if (k >= base && k < base + cn) {
@@ -1903,22 +1950,6 @@ __global__ void __launch_bounds__(kRankBlock) k_watpol_rank(DevModel m, const De
                 else s.rank[w] += r;
             }
         }
-    }
-    // the shell's theta sum (src/nonbondene.f90:6652-6666) over the thetas
-    // scattered to their ranks, by one warp in a fixed order: deterministic
-    // whatever order the shell list was filled in (FP64 atomics were not)
-    __syncthreads();
-    double* sorted = s.theta_sorted + (size_t)sh * m.nwat;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        int w = L[k];
-        sorted[s.rank[w]] = s.theta[w];
-    }
-    __syncthreads();
-    if (warp == 0) {
-        double t = 0.0;
-        for (int k = lane; k < n; k += kWarp) t += sorted[k];
-        t = warp_sum(t);
-        if (lane == 0) s.shell_tsum[sh] = t;
     }
 }
 
@@ -2030,14 +2061,34 @@ __global__ void k_watpol_force(DevModel m, const DevState* __restrict__ states, 
 }
 
 // running averages (md only), src/nonbondene.f90:6738-6741
-__global__ void k_watpol_average(SolventDev p, const DevState* __restrict__ states) {
+// running averages (md only), src/nonbondene.f90:6738-6741.  The shell's
+// theta sum (6652-6666) is taken over the thetas placed at their ranks, by one
+// warp per shell in a fixed order: deterministic whatever order the shell
+// list was filled in.
+__global__ void __launch_bounds__(512) k_watpol_average(DevModel m, SolventDev p, const DevState* __restrict__ states) {
     const DevState& s = states[blockIdx.y];
-    int is = threadIdx.x;
-    if (is >= p.nshell) return;
-    int n = s.n_insh[is];
-    if (n == 0) return;
-    s.wstate[kMaxShell + is] += s.shell_tsum[is] / (double)n;
-    s.wstate[2 * kMaxShell + is] += (double)n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int sh = 0; sh < p.nshell; ++sh) {
+        const int n = s.n_insh[sh];
+        const int* L = s.shell_list + (size_t)sh * m.nwat;
+        double* sorted = s.theta_sorted + (size_t)sh * m.nwat;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            int w = L[k];
+            sorted[s.rank[w]] = s.theta[w];
+        }
+    }
+    __syncthreads();
+    for (int sh = warp; sh < p.nshell; sh += nw) {
+        const int n = s.n_insh[sh];
+        const double* sorted = s.theta_sorted + (size_t)sh * m.nwat;
+        double t = 0.0;
+        for (int k = lane; k < n; k += kWarp) t += sorted[k];
+        t = warp_sum(t);
+        if (lane == 0 && n > 0) {
+            s.wstate[kMaxShell + sh] += t / (double)n;
+            s.wstate[2 * kMaxShell + sh] += (double)n;
+        }
+    }
 }
 
 // =============================================================================
@@ -2759,8 +2810,8 @@ void launch_qp(const Launch& L, int mixed) {
 }
 void launch_nonbond_qq(const Launch& L, int mixed) {
     if (L.s0.nqq == 0) return;
-    dim3 g((L.s0.nqq + 31) / 32, L.nwin);   // FP64 work: small blocks spread it over the SMs
-    if (mixed) k_qq<true><<<g, 32, 0, L.st>>>(L.m, L.ds); else k_qq<false><<<g, 32, 0, L.st>>>(L.m, L.ds);
+    dim3 g((L.s0.nqq + 255) / 256, L.nwin);
+    if (mixed) k_qq<true><<<g, 256, 0, L.st>>>(L.m, L.ds); else k_qq<false><<<g, 256, 0, L.st>>>(L.m, L.ds);
 }
 void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed) {
     dim3 g = grid_for(L.m.natom, 64, L.tu.v[T_TAYLOR], L.nwin);
@@ -2781,7 +2832,7 @@ void launch_clear_fq(const Launch& L) {
 }
 void launch_row_sums(const Launch& L) {
     if (L.m.ncgp_solute + L.m.nwat == 0) return;
-    k_row_sums<<<L.nwin, 256, 0, L.st>>>(L.m, L.ds);
+    k_row_sums<<<L.nwin, kRowSumBlock, 0, L.st>>>(L.m, L.ds);
 }
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv) {
@@ -2800,7 +2851,7 @@ int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int m
         k_watpol_reset<<<L.nwin, kMaxShell, 0, L.st>>>(L.ds);
         if (mixed) k_watpol_theta<true><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
         else k_watpol_theta<false><<<gw, 32, 0, L.st>>>(L.m, L.ds, p);
-        k_watpol_rank<<<dim3(p.nshell, L.nwin), kRankBlock, 0, L.st>>>(L.m, L.ds);
+        k_watpol_rank<<<dim3(p.nshell * kRankParts, L.nwin), kRankBlock, 0, L.st>>>(L.m, L.ds);
         nl += 3;
     }
     if (istep > 0 && md && (istep % (int)llround(p.itdis)) == 0) {
@@ -2816,7 +2867,7 @@ int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int m
     }
     ++nl;
     if (md) {
-        k_watpol_average<<<dim3(1, L.nwin), kMaxShell, 0, L.st>>>(p, L.ds);
+        k_watpol_average<<<dim3(1, L.nwin), 512, 0, L.st>>>(L.m, p, L.ds);
         ++nl;
     }
     return nl;
