@@ -80,6 +80,8 @@ struct qnb_context {
     int nwin = 1;
     std::vector<DevState> st;      // per-window device state (host copy of the pointers)
     QQEntry* st_qq = nullptr;      // static Q-Q / Q-bonded lists (shared by the windows)
+    float4* st_qqf = nullptr;      // their (A, B, el, sc) in FP32 for the mixed form
+    float* lambdaf_all = nullptr;  // [W][kMaxStates] lambda in FP32
     int nqq = 0, nqq_qq = 0;
     DevState* d_states = nullptr;  // the same, on the device
     double* x_all = nullptr;       // [nwin][natom][3]
@@ -715,6 +717,10 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     c->nqq = (int)qq.size();
     c->nqq_qq = nqq_qq;
     TRY(c->upload(&c->st_qq, qq));
+    std::vector<float4> qqf(qq.size());
+    for (size_t k = 0; k < qq.size(); ++k)
+        qqf[k] = make_float4((float)qq[k].A, (float)qq[k].B, (float)qq[k].el, (float)qq[k].sc);
+    TRY(c->upload(&c->st_qqf, qqf));
     TRY(c->upload((QQAdj**)&m.qq_adj, qadj));
     return QNB_OK;
 }
@@ -741,6 +747,8 @@ int alloc_state(qnb_context* c) {
     const double rho = 0.04;   // generous water density (molecules / A^3)
     int64_t per_w = (int64_t)(4.0 / 3.0 * M_PI * 1000.0 * rho) + 64;
     std::vector<double> lam(std::max(1, m.S), 1.0);
+    std::vector<float> lamf((size_t)kMaxStates * W, 1.0f);
+    TRY(c->upload(&c->lambdaf_all, lamf));
     for (int w = 0; w < W; ++w) {
         DevState& s = c->st[w];
         s.x = c->x_all + n3 * w;
@@ -794,6 +802,8 @@ int alloc_state(qnb_context* c) {
             TRY(c->alloc(&s.x_build, n3));
         }
         s.qq = c->st_qq;
+        s.qqf = c->st_qqf;
+        s.lambdaf = c->lambdaf_all + (size_t)kMaxStates * w;
         s.nqq = c->nqq;
         s.nqq_qq = c->nqq_qq;
     }
@@ -1177,7 +1187,11 @@ int qnb_set_lambda_window(qnb_context* c, int32_t w, const double* lambda) {
     if (c->S == 0) return QNB_OK;
     CU(cudaSetDevice(c->device));
     memcpy(c->h_stage, lambda, sizeof(double) * c->S);
+    float* lf = reinterpret_cast<float*>(c->h_stage + c->S);   // staging holds >= 64 doubles, S <= kMaxStates
+    for (int k = 0; k < c->S; ++k) lf[k] = (float)lambda[k];
     CU(cudaMemcpyAsync(c->st[w].lambda, c->h_stage, sizeof(double) * c->S, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->lambdaf_all + (size_t)kMaxStates * w, lf, sizeof(float) * c->S, cudaMemcpyHostToDevice,
+                       c->stream));
     CU(cudaStreamSynchronize(c->stream));
     return QNB_OK;
 }

@@ -135,6 +135,8 @@ struct DevState {
     int* row_wg; int* cnt_wg; int cap_wg;   // water -> solute groups
     double* x_build;                        // coordinates of the last list build
     QQEntry* qq; int nqq;          // static qq + qqp entries (all states)
+    const float4* qqf;   // the entries' (A, B, el, sc) in FP32 (mixed form)
+    const float* lambdaf;   // [S] lambda in FP32 (mixed form)
     double* adj;                   // [3][nqat*S] dE_s/dqcrg, dE_s/dqA, dE_s/dqB of this window
     int nqq_qq;                    // first nqq_qq entries are Q-Q (EQ%qq), rest Q-P (EQ%qp)
     // water polarisation

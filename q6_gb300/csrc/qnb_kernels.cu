@@ -1533,8 +1533,10 @@ __global__ void k_qadj_qq(DevModel m, const DevState* __restrict__ states) {
 }
 
 // nonbond_qq + nonbond_qqp (static lists), src/nonbondene.f90:5013-5153,
-// pair kernel nbe_qq, src/nonbonded.f90:111-150.  Always FP64: few pairs.
-// Every pair touches a Q atom and one of a few energy slots, so the Q atoms'
+// pair kernel nbe_qq, src/nonbonded.f90:111-150.  The FP64 form computes in
+// FP64; the mixed form in FP32 like the other pair kernels (the FP64 pipe runs
+// at 1/64 of the FP32 rate), with the entries' parameters and lambda kept in
+// FP32 copies.  Every pair touches a Q atom and one of a few energy slots, so the Q atoms'
 // gradients and the energies are summed in shared memory per block (fixed
 // point in the mixed form) and added once per block: global atomics on those
 // few addresses serialise.
@@ -1551,48 +1553,74 @@ __global__ void __launch_bounds__(256) k_qq(DevModel m, const DevState* __restri
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < s.nqq) {
     QQEntry e = s.qq[p];
-    double tx = s.x[3 * e.j] - s.x[3 * e.i], ty = s.x[3 * e.j + 1] - s.x[3 * e.i + 1],
-           tz = s.x[3 * e.j + 2] - s.x[3 * e.i + 2];
-    double r2 = 1.0 / (tx * tx + ty * ty + tz * tz);
-    double r = sqrt(r2);
-    double r6d = r2 * r2 * r2;
-    double r6_hc = 1.0 / r6d;
-    double r6 = 1.0 / (r6_hc + e.sc);
-    double r12 = r6 * r6;
-    double lam = s.lambda[e.s];
-    double vel = e.el * r, va, vb, dv;
-    if (e.soft) {
-        vb = 0.0;
-        va = e.A * exp(-e.B / r);
-        dv = r2 * (-vel - e.B * va / r) * lam;
-    } else {
-        va = e.A * r12;
-        vb = e.B * r6;
-        dv = r2 * (-vel - (12.0 * va - 6.0 * vb) * r6 * r6_hc) * lam;
-    }
-    int kel = p < s.nqq_qq ? 0 : 2;
-    const double g[2][3] = {{-tx * dv, -ty * dv, -tz * dv}, {tx * dv, ty * dv, tz * dv}};
+    const int kel = p < s.nqq_qq ? 0 : 2;
     const int at[2] = {e.i, e.j};
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        int iq = m.iqatom[at[h]];
-        if (iq >= 0) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                if constexpr (MIX) atomicAdd(&red[3 * iq + c], to_fixd(g[h][c]));
-                else atomicAdd(&red[3 * iq + c], g[h][c]);
-            }
+    if constexpr (MIX) {   // FP32 pair arithmetic, fixed-point sums
+        const float4 pf = s.qqf[p];   // A, B, el, sc
+        float4 xi = s.xq[e.i], xj = s.xq[e.j];
+        float tx = xj.x - xi.x, ty = xj.y - xi.y, tz = xj.z - xi.z;
+        float d2 = tx * tx + ty * ty + tz * tz;
+        float r = rsqrtf(d2), r2 = r * r;   // r = 1/distance as in nbe_qq
+        float r6_hc = __fdividef(1.0f, r2 * r2 * r2);
+        float r6 = __fdividef(1.0f, r6_hc + pf.w);
+        float lam = s.lambdaf[e.s];
+        float vel = pf.z * r, va, vb, dv;
+        if (e.soft) {
+            vb = 0.0f;
+            float dist = d2 * r;
+            va = pf.x * expf(-pf.y * dist);
+            dv = r2 * (-vel - pf.y * va * dist) * lam;
         } else {
-            if constexpr (MIX) acc.gradd(at[h], g[h][0], g[h][1], g[h][2]);
-            else acc.grad(at[h], g[h][0], g[h][1], g[h][2]);
+            va = pf.x * r6 * r6;
+            vb = pf.y * r6;
+            dv = r2 * (-vel - (12.0f * va - 6.0f * vb) * r6 * r6_hc) * lam;
         }
-    }
-    if constexpr (!MIX) {
+        const float g[2][3] = {{-tx * dv, -ty * dv, -tz * dv}, {tx * dv, ty * dv, tz * dv}};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            int iq = m.iqatom[at[h]];
+            if (iq >= 0) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) atomicAdd(&red[3 * iq + c], to_fix_alu(g[h][c]));
+            } else {
+                acc.grad(at[h], g[h][0], g[h][1], g[h][2]);
+            }
+        }
+        atomicAdd(&rede[eq_slot(e.s, kel)], to_fix_alu(vel));
+        atomicAdd(&rede[eq_slot(e.s, kel + 1)], to_fix_alu(va - vb));
+    } else {
+        double tx = s.x[3 * e.j] - s.x[3 * e.i], ty = s.x[3 * e.j + 1] - s.x[3 * e.i + 1],
+               tz = s.x[3 * e.j + 2] - s.x[3 * e.i + 2];
+        double r2 = 1.0 / (tx * tx + ty * ty + tz * tz);
+        double r = sqrt(r2);
+        double r6d = r2 * r2 * r2;
+        double r6_hc = 1.0 / r6d;
+        double r6 = 1.0 / (r6_hc + e.sc);
+        double r12 = r6 * r6;
+        double lam = s.lambda[e.s];
+        double vel = e.el * r, va, vb, dv;
+        if (e.soft) {
+            vb = 0.0;
+            va = e.A * exp(-e.B / r);
+            dv = r2 * (-vel - e.B * va / r) * lam;
+        } else {
+            va = e.A * r12;
+            vb = e.B * r6;
+            dv = r2 * (-vel - (12.0 * va - 6.0 * vb) * r6 * r6_hc) * lam;
+        }
+        const double g[2][3] = {{-tx * dv, -ty * dv, -tz * dv}, {tx * dv, ty * dv, tz * dv}};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            int iq = m.iqatom[at[h]];
+            if (iq >= 0) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) atomicAdd(&red[3 * iq + c], g[h][c]);
+            } else {
+                acc.grad(at[h], g[h][0], g[h][1], g[h][2]);
+            }
+        }
         atomicAdd(&rede[eq_slot(e.s, kel)], vel);
         atomicAdd(&rede[eq_slot(e.s, kel + 1)], va - vb);
-    } else {
-        atomicAdd(&rede[eq_slot(e.s, kel)], to_fixd(vel));
-        atomicAdd(&rede[eq_slot(e.s, kel + 1)], to_fixd(va - vb));
     }
     }
     __syncthreads();
