@@ -306,17 +306,22 @@ def sgemm_fp32_peak(torch):
 def dg_check(s, sp, lams, local, nwin, frames=4):
     """Per-window dG (Qfep exponential averaging) of the mixed form against
     the FP64 form on identical frames: `frames` perturbed copies (0.05 A) of
-    each window's coordinates."""
+    each window's coordinates.  Every window's per-state energies go through
+    an energy file in qdyn's layout, and dG comes from the Qfep summary of
+    those files."""
     import numpy as np
-    from q6_gb300.fep import BOLTZ, qfep_dg, state_energies, window_increments
+    from q6_gb300.enefile import EnergyFileWriter, qfep_files
+    from q6_gb300.fep import BOLTZ, window_increments
     from q6_gb300.qnb import PREC_FP64, PREC_MIXED, NonbondedEngine
     from q6_gb300.system import lambdas_for_window
     rng = np.random.default_rng(99)
     lam = np.array([lambdas_for_window(l, s.nstates) for l in lams])
     fr = np.stack([np.stack([s.x + rng.normal(0, 0.05, s.x.shape) for _ in range(frames)]) for _ in range(nwin)])
     out = {}
+    tmp = tempfile.mkdtemp(prefix="qnb_dg_")
     for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
-        v = np.zeros((nwin, frames, s.nstates))
+        paths = [os.path.join(tmp, "%s_%03d.en" % (name, w)) for w in range(nwin)]
+        files = [EnergyFileWriter(p, s.nstates) for p in paths]
         with NonbondedEngine(s, precision=prec, device=local, windows=nwin) as e:
             e.set_solvent_params(sp)
             for w in range(nwin):
@@ -325,13 +330,20 @@ def dg_check(s, sp, lams, local, nwin, frames=4):
                 e.set_coordinates_dev(fr[:, k])
                 e.make_pair_lists_dev(**CUT)
                 _, EQ, _ = e.compute_dev(sync=True)
-                v[:, k, :] = state_energies(EQ)
-        out[name] = window_increments(qfep_dg(v, lam, BOLTZ * 300.0)[2])
+                for w in range(nwin):
+                    files[w].write_step(lam[w], EQ[w])
+        for f in files:
+            f.close()
+        out[name] = window_increments(qfep_files(paths, s.nstates, rt=BOLTZ * 300.0)[3])
+        for p in paths:
+            os.remove(p)
+    os.rmdir(tmp)
     err = np.abs(out["mixed"] - out["fp64"])
     return {"windows": nwin, "frames_per_window": frames, "max_abs_err_kcal": round(float(err.max()), 6),
             "mean_abs_err_kcal": round(float(err.mean()), 6), "tolerance_kcal": 0.02,
             "total_dG_fp64": round(float(out["fp64"].sum()), 4), "total_dG_mixed": round(float(out["mixed"].sum()), 4),
-            "frames": "seeded 0.05 A perturbations of the window coordinates (no MD trajectory)"}
+            "frames": "seeded 0.05 A perturbations of the window coordinates (no MD trajectory)",
+            "path": "per-window energy files in qdyn's put_ene layout -> Qfep FEP summary"}
 
 
 def read_traffic(kernel):
