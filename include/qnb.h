@@ -39,7 +39,8 @@ enum {
     QNB_ERR_CAPACITY = 3,   /* a pair-list row overflowed; rebuilt lists larger */
     QNB_ERR_STATE = 4,      /* call out of order (e.g. energies before lists)   */
     QNB_ERR_NOMEM = 5,      /* device allocation failed                          */
-    QNB_ERR_UNSUPPORTED = 6 /* topology feature outside this library's scope     */
+    QNB_ERR_UNSUPPORTED = 6, /* topology feature outside this library's scope    */
+    QNB_ERR_CONSTRAINT = 7  /* SHAKE did not converge in 1000 iterations          */
 };
 
 /* ---- precision forms ---------------------------------------------------- */
@@ -360,6 +361,72 @@ int qnb_profile_classes(qnb_context* ctx, uint32_t mask);
 /* Total milliseconds and launches per kernel class since the last call
    (n entries, n <= QNB_K_COUNT); resets the totals. */
 int qnb_kernel_times(qnb_context* ctx, double* ms, int64_t* launches, int32_t n);
+
+/* ---- device-resident MD step (FP64) ----------------------------------------
+   qdyn's leap-frog step for the spherical boundary with the Berendsen
+   thermostat (md_run, src/md.f90:1687-1812), every window of the context on
+   the device, no host round trip per step:
+     every nbcycle steps  make_pair_lists (qnb_make_pair_lists_dev);
+     pot_energy           d = 0, then the evaluation of qnb_compute_dev, with
+                          restrain_solvent's Tfree taken on the device from the
+                          window's last temperature() (src/md.f90:1379-1447);
+     newvel_ber           per temperature group g (src/md.f90:1451-1466):
+                          v = (v - d winv dt) sfact_g, xx = x, x = x + v dt;
+     constraint           SHAKE (src/bondene.f90:1069-1150), then
+                          v = (x - xx) / dt for every atom;
+     temperature          Ekin, Temp, Tfree and the Berendsen factors
+                          sfact_g = sqrt(1 + dt/tau_T (Temp0/Tfree_g - 1)).
+   Bonded terms are outside this library: the step integrates the nonbonded,
+   Q-Q and solvent-boundary forces (constrain the solute's bonds, or add the
+   bonded gradient through the caller's own kernels on qnb_stream between
+   steps).  Units as qdyn: masses in amu, time in fs (converted with qdyn's
+   0.020462 per fs, src/md.f90:207 and 231), velocities in A per internal
+   time unit. */
+enum { QNB_MAX_TGROUPS = 4 };
+typedef struct qnb_md_params {
+    double stepsize;          /* time step (fs)                                  */
+    double temp0;             /* Berendsen target temperature (K)               */
+    double tau_t;             /* bath_coupling relaxation time (fs)             */
+    double ndegf, ndegfree;   /* degrees of freedom: all atoms and non-excluded
+                                 atoms (src/simprep.f90:2439-2440)              */
+    int32_t ntgroups;         /* temperature coupling groups, 1..QNB_MAX_TGROUPS */
+    int32_t nbcycle;          /* pair-list update interval (steps)              */
+    int32_t tg_first[QNB_MAX_TGROUPS], tg_last[QNB_MAX_TGROUPS];   /* 0-based,
+                                 inclusive atom range of each group             */
+    double tg_ndegf[QNB_MAX_TGROUPS], tg_ndegfree[QNB_MAX_TGROUPS];
+    double rq, rcq, rclrf, rcpp, rcpw, rcww;   /* cut-offs of the rebuilds (A)   */
+} qnb_md_params;
+
+/* Per window and step of qnb_md_run: the step's energies (as qnb_compute_dev
+   reports them) and, after the step's temperature(), Ekin (E%kinetic), Temp,
+   Tfree and the SHAKE iterations summed over the constrained molecules. */
+typedef struct qnb_md_record {
+    qnb_energies E;
+    double solvent_radial, water_pol;
+    double ekin, temp, tfree, shake_iterations;
+} qnb_md_record;
+
+/* mass[natom] (amu); the constraints of molecule m are
+   con_ij[2k], con_ij[2k+1] (0-based atoms) at distance con_dist[k] (A) for
+   k in [mol_first[m], mol_first[m+1]), m < nmol.  Velocities start at 0. */
+int qnb_md_init(qnb_context* ctx, const qnb_md_params* p, const double* mass, int32_t nmol,
+                const int32_t* mol_first, const int32_t* con_ij, const double* con_dist);
+int qnb_md_set_velocities(qnb_context* ctx, int32_t window, const double* v);
+/* x and/or v (natom x 3, either may be NULL) of one window. */
+int qnb_md_get_state(qnb_context* ctx, int32_t window, double* x, double* v);
+/* qdyn's start of dynamics on every window's device coordinates and
+   velocities: initial_constraint (src/bondene.f90:1025-1048), then, if
+   stop_cm != 0, stop_cm_translation (src/simprep.f90:4496-4518), then
+   temperature() for Tfree and the thermostat factors of the first step.
+   Required after qnb_md_init and after every qnb_md_set_velocities or
+   coordinate upload before qnb_md_run. */
+int qnb_md_prepare(qnb_context* ctx, int32_t stop_cm);
+/* nsteps steps of every window starting at step number istep0 (lists are
+   rebuilt where istep % nbcycle == 0, watpol updates by istep).  rec (may be
+   NULL): [nsteps][nwin] records; EQ (may be NULL): [nsteps][nwin][nstates].
+   QNB_ERR_CONSTRAINT if SHAKE failed in any window (the coordinates are then
+   those of the failed step). */
+int qnb_md_run(qnb_context* ctx, int32_t nsteps, int32_t istep0, qnb_md_record* rec, qnb_qenergies* EQ);
 
 /* ---- allocation-free entry point (no counterpart in the reference) ------- */
 

@@ -59,6 +59,10 @@ def lib():
         L.orc_get_lrf.argtypes = [P, P]
         L.orc_shake.restype = ctypes.c_long
         L.orc_shake.argtypes = [P, P, I, P, P, P, P, P]
+        L.orc_md_newvel.argtypes = [I, P, P, P, P, P, D, I, P, P, P]
+        L.orc_md_velocity.argtypes = [I, P, P, P, D]
+        L.orc_md_stop_cm.argtypes = [I, P, P]
+        L.orc_md_temperature.argtypes = [I, P, P, P, I, P, P, P, P, D, D, D, D, D, D, P, P]
         L.orc_static_qq_size.restype = ctypes.c_long
         L.orc_static_qq_size.argtypes = [P, I, I]
         _lib = L
@@ -198,3 +202,89 @@ def shake(x, molecules, winv):
     if n < 0:
         raise RuntimeError("shake failure")
     return x
+
+
+class OracleMD:
+    """qdyn's MD step on the CPU (test infrastructure): the oracle's
+    nonbonded evaluation plus newvel_ber, SHAKE, v = (x - xx)/dt and
+    temperature() with the Berendsen factors, in md_run's order
+    (src/md.f90:1687-1812).  ``p`` is a q6_gb300.md.QnbMdParams, ``cons`` the
+    matching Constraints, ``sp`` the solvent parameters (or None)."""
+
+    BOLTZ = 0.001986
+    MAGIC = 0.020462
+
+    def __init__(self, oracle: Oracle, p, cons, sp=None, lam=None):
+        self.o, self.p, self.cons, self.sp = oracle, p, cons, sp
+        s = oracle.s
+        self.n = s.natom
+        self.mass = np.ascontiguousarray(s.mass[s.iac], dtype=np.float64)
+        self.winv = 1.0 / self.mass
+        self.excl = np.ascontiguousarray(s.excl, dtype=np.uint8)
+        self.ntg = p.ntgroups
+        self.first = np.array(p.tg_first[:self.ntg], np.int32)
+        self.last = np.array(p.tg_last[:self.ntg], np.int32)
+        self.tg_ndegf = np.array(p.tg_ndegf[:self.ntg], np.float64)
+        self.tg_ndegfree = np.array(p.tg_ndegfree[:self.ntg], np.float64)
+        self.dt = self.MAGIC * p.stepsize
+        self.tau = self.MAGIC * p.tau_t
+        self.sfact = np.zeros(self.ntg)
+        self.ci = np.ascontiguousarray(cons.ij[:, 0], dtype=np.int32)
+        self.cj = np.ascontiguousarray(cons.ij[:, 1], dtype=np.int32)
+        self.d2 = np.ascontiguousarray(cons.dist * cons.dist)
+        self.nmol = len(cons.mol_first) - 1
+        if lam is not None:
+            oracle.set_lambda(lam)
+        self.tfree = 0.0
+
+    def _shake(self, x, ref):
+        n = lib().orc_shake(_p(x), _p(ref), self.nmol, _p(self.cons.mol_first), _p(self.ci), _p(self.cj),
+                            _p(self.d2), _p(self.winv))
+        if n < 0:
+            raise RuntimeError("shake failure")
+        return n
+
+    def temperature(self, v):
+        out = np.zeros(3 + 3 * self.ntg)
+        lib().orc_md_temperature(self.n, _p(v), _p(self.mass), _p(self.excl), self.ntg, _p(self.first),
+                                 _p(self.last), _p(self.tg_ndegf), _p(self.tg_ndegfree), self.p.ndegf,
+                                 self.p.ndegfree, self.p.temp0, self.dt, self.tau, self.BOLTZ, _p(self.sfact),
+                                 _p(out))
+        self.tfree = out[2]
+        return out
+
+    def prepare(self, x, v, stop_cm=True):
+        """initial_constraint, stop_cm_translation, temperature()."""
+        x = np.ascontiguousarray(x, dtype=np.float64).copy()
+        v = np.ascontiguousarray(v, dtype=np.float64).copy()
+        xx = x.copy()
+        self._shake(x, xx)
+        xx = x - v * self.dt
+        self._shake(xx, x)
+        lib().orc_md_velocity(self.n, _p(x), _p(xx), _p(v), self.dt)
+        if stop_cm:
+            lib().orc_md_stop_cm(self.n, _p(v), _p(self.mass))
+        self.temperature(v)
+        return x, v
+
+    def step(self, x, v, istep, cut):
+        o = self.o
+        if istep % self.p.nbcycle == 0:
+            o.make_pair_lists(x, **cut)
+        d = np.zeros_like(x)
+        d, E, EQ = o.pot_energy_nonbonds(x, d)
+        d, EQ = o.nonbond_qq(x, d, EQ)
+        erst = [0.0, 0.0]
+        if self.sp is not None:
+            erst[0] = o.restrain_solvent(x, d, self.tfree)
+            if self.sp.wpol_restr:
+                erst[1] = o.watpol(x, d, istep, True)
+        xx = np.zeros_like(x)
+        lib().orc_md_newvel(self.n, _p(x), _p(xx), _p(v), _p(d), _p(self.winv), self.dt, self.ntg,
+                            _p(self.first), _p(self.last), _p(self.sfact))
+        iters = 0
+        if self.nmol > 0:
+            iters = self._shake(x, xx)
+            lib().orc_md_velocity(self.n, _p(x), _p(xx), _p(v), self.dt)
+        t = self.temperature(v)
+        return dict(E=E, EQ=EQ, erst=erst, ekin=t[0], temp=t[1], tfree=t[2], shake_iterations=iters)

@@ -1300,3 +1300,74 @@ long orc_shake(double* x, const double* xx, int nmol, const int32_t* mol_start, 
     free(ready);
     return total;
 }
+
+/* ---- MD step pieces (strict FP64, the reference's evaluation order) ------
+   newvel_ber src/md.f90:1451-1466; v = (x - xx)/dt src/md.f90:1787-1789;
+   temperature src/md.f90:1379-1447; stop_cm_translation
+   src/simprep.f90:4496-4518.  SHAKE is orc_shake above. */
+static int md_group(int i, int ntg, const int32_t* first, const int32_t* last) {
+    for (int g = 0; g < ntg; ++g)
+        if (i >= first[g] && i <= last[g]) return g;
+    return -1;
+}
+
+void orc_md_newvel(int natom, double* x, double* xx, double* v, const double* d, const double* winv, double dt,
+                   int ntg, const int32_t* first, const int32_t* last, const double* sfact) {
+    for (int g = 0; g < ntg; ++g)
+        for (int i = first[g]; i <= last[g]; ++i)
+            for (int c = 0; c < 3; ++c) {
+                int k = 3 * i + c;
+                v[k] = (v[k] - d[k] * winv[i] * dt) * sfact[g];
+                xx[k] = x[k];
+                x[k] = x[k] + v[k] * dt;
+            }
+    (void)natom;
+}
+
+void orc_md_velocity(int natom, const double* x, const double* xx, double* v, double dt) {
+    for (int k = 0; k < 3 * natom; ++k) v[k] = (x[k] - xx[k]) / dt;
+}
+
+void orc_md_stop_cm(int natom, double* v, const double* mass) {
+    double tot = 0.0, vcm[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < natom; ++i) {
+        tot = tot + mass[i];
+        for (int c = 0; c < 3; ++c) vcm[c] = vcm[c] + v[3 * i + c] * mass[i];
+    }
+    for (int c = 0; c < 3; ++c) vcm[c] = vcm[c] / tot;
+    for (int i = 0; i < natom; ++i)
+        for (int c = 0; c < 3; ++c) v[3 * i + c] = v[3 * i + c] - vcm[c];
+}
+
+/* out: ekin, temp, tfree, then per group temp, tfree, texcl; sfact updated */
+void orc_md_temperature(int natom, const double* v, const double* mass, const uint8_t* excl, int ntg,
+                        const int32_t* first, const int32_t* last, const double* tg_ndegf,
+                        const double* tg_ndegfree, double ndegf, double ndegfree, double temp0, double dt,
+                        double tau, double boltz, double* sfact, double* out) {
+    double gt[8] = {0}, gf[8] = {0}, gx[8] = {0};
+    for (int g = 0; g < ntg; ++g)
+        for (int i = first[g]; i <= last[g]; ++i) {
+            double sq = v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2];
+            double ek = 0.5 * mass[i] * sq;
+            gt[g] = gt[g] + ek;
+            if (!excl[i]) gf[g] = gf[g] + ek;
+            else gx[g] = gx[g] + ek;
+        }
+    double tfree = 0.0, temp = 0.0;
+    for (int g = 0; g < ntg; ++g) tfree = tfree + gf[g];
+    for (int g = 0; g < ntg; ++g) temp = temp + gt[g];
+    out[0] = temp;
+    out[1] = 2.0 * temp / boltz / ndegf;
+    out[2] = 2.0 * tfree / boltz / ndegfree;
+    for (int g = 0; g < ntg; ++g) {
+        double tt = 2.0 * gt[g] / boltz / tg_ndegf[g];
+        double tf = 2.0 * gf[g] / boltz / tg_ndegfree[g];
+        double tx = tg_ndegf[g] != tg_ndegfree[g] ? 2.0 * gx[g] / boltz / (tg_ndegf[g] - tg_ndegfree[g]) : gx[g];
+        out[3 + 3 * g] = tt;
+        out[4 + 3 * g] = tf;
+        out[5 + 3 * g] = tx;
+        if (tf != 0.0) sfact[g] = temp0 / tf - 1.0;
+        sfact[g] = sqrt(1.0 + dt / tau * sfact[g]);
+    }
+    (void)natom;
+}

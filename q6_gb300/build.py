@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libqnb.so")
-SOURCES = ["qnb_kernels.cu", "qnb_host.cpp", "qnb_noalloc.cu"]
+SOURCES = ["qnb_kernels.cu", "qnb_host.cpp", "qnb_noalloc.cu", "qmd_kernels.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-diag-suppress", "177"]

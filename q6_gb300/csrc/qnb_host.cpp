@@ -141,6 +141,15 @@ struct qnb_context {
     double* h_stage = nullptr;   // pinned staging for x / d (natom*3)
     double* h_e = nullptr;       // pinned energies (nwin x (kNumE doubles + kNumE fixed))
 
+    // device-resident MD (qnb_md_*)
+    bool md_ready = false;         // qnb_md_init done
+    bool md_prepared = false;      // qnb_md_prepare done since the last state change
+    qnb_md_params mdp{};
+    MdDev md{};
+    double* md_rec = nullptr;      // [md_rec_steps][nwin][kMdRec] step records
+    int md_rec_steps = 0;
+    double* h_md_rec = nullptr;    // pinned copy of one chunk of records
+
     Tune tune = kTuneDefault;
     Launch all() const { return Launch{m, st[0], d_states, nwin, stream, tune}; }
     Launch one() const { return Launch{m, st[0], d_states, 1, stream, tune}; }   // window 0 only
@@ -1167,6 +1176,7 @@ int qnb_destroy(qnb_context* c) {
         }
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->h_e) cudaFreeHost(c->h_e);
+    if (c->h_md_rec) cudaFreeHost(c->h_md_rec);
     if (c->stream2) cudaStreamSynchronize(c->stream2), cudaStreamDestroy(c->stream2);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
@@ -1869,6 +1879,231 @@ int qnb_take_launch_count(qnb_context* c, int64_t* n) {
     if (!c || !n) return fail(QNB_ERR_ARG, "null argument");
     *n = c->launches;
     c->launches = 0;
+    return QNB_OK;
+}
+
+}  // extern "C"
+
+// =============================================================================
+// Device-resident MD step (qnb_md_*)
+// =============================================================================
+namespace {
+
+constexpr double kMagicStepConv = 0.020462;   // fs -> internal time, src/globals.f90:47
+constexpr double kBoltz = 0.001986;           // src/globals.f90:46
+constexpr int kMdChunk = 256;                 // steps recorded on the device between read-backs
+
+int md_check(qnb_context* c) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    if (!c->md_ready) return fail(QNB_ERR_STATE, "qnb_md_init not called");
+    return QNB_OK;
+}
+
+// windows whose SHAKE failed since the flags were cleared
+int md_fail_check(qnb_context* c) {
+    std::vector<int> f(c->nwin);
+    CU(cudaMemcpyAsync(f.data(), c->md.fail, sizeof(int) * c->nwin, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    for (int w = 0; w < c->nwin; ++w)
+        if (f[w]) return fail(QNB_ERR_CONSTRAINT, "SHAKE failed in window %d, molecule %d", w, f[w] - 1);
+    return QNB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qnb_md_init(qnb_context* c, const qnb_md_params* p, const double* mass, int32_t nmol, const int32_t* mol_first,
+                const int32_t* con_ij, const double* con_dist) {
+    if (!c || !p || !mass || nmol < 0 || (nmol > 0 && (!mol_first || !con_ij || !con_dist)))
+        return fail(QNB_ERR_ARG, "null argument");
+    if (c->md_ready) return fail(QNB_ERR_STATE, "qnb_md_init already called on this context");
+    const int n = c->natom;
+    if (!(p->stepsize > 0.0) || !(p->temp0 > 0.0) || !(p->tau_t >= p->stepsize))
+        return fail(QNB_ERR_ARG, "stepsize > 0, temp0 > 0 and tau_t >= stepsize required");
+    if (p->ntgroups < 1 || p->ntgroups > kMaxTg) return fail(QNB_ERR_ARG, "ntgroups %d not in 1..%d", p->ntgroups, kMaxTg);
+    if (p->nbcycle < 1) return fail(QNB_ERR_ARG, "nbcycle %d < 1", p->nbcycle);
+    if (!(p->ndegf > 0.0) || !(p->ndegfree > 0.0)) return fail(QNB_ERR_ARG, "degrees of freedom must be positive");
+    for (int g = 0; g < p->ntgroups; ++g) {
+        if (p->tg_first[g] < 0 || p->tg_last[g] >= n || p->tg_first[g] > p->tg_last[g])
+            return fail(QNB_ERR_ARG, "temperature group %d: bad atom range", g);
+        if (!(p->tg_ndegf[g] > 0.0) || !(p->tg_ndegfree[g] > 0.0))
+            return fail(QNB_ERR_ARG, "temperature group %d: degrees of freedom must be positive", g);
+        for (int h = 0; h < g; ++h)
+            if (p->tg_first[g] <= p->tg_last[h] && p->tg_first[h] <= p->tg_last[g])
+                return fail(QNB_ERR_ARG, "temperature groups %d and %d overlap", h, g);
+    }
+    for (int i = 0; i < n; ++i)
+        if (!(mass[i] > 0.0)) return fail(QNB_ERR_ARG, "mass of atom %d not positive", i);
+    int ncons = 0;
+    if (nmol > 0) {
+        if (mol_first[0] != 0) return fail(QNB_ERR_ARG, "mol_first[0] must be 0");
+        for (int m = 0; m < nmol; ++m)
+            if (mol_first[m + 1] < mol_first[m]) return fail(QNB_ERR_ARG, "mol_first not ascending at %d", m);
+        ncons = mol_first[nmol];
+        for (int k = 0; k < ncons; ++k) {
+            int i = con_ij[2 * k], j = con_ij[2 * k + 1];
+            if (i < 0 || i >= n || j < 0 || j >= n || i == j || !(con_dist[k] > 0.0))
+                return fail(QNB_ERR_ARG, "constraint %d: bad atoms or distance", k);
+        }
+    }
+    CU(cudaSetDevice(c->device));
+    MdDev& md = c->md;
+    md = MdDev{};
+    md.natom = n;
+    md.ntg = p->ntgroups;
+    md.nmol = nmol;
+    md.ncons = ncons;
+    for (int g = 0; g < kMaxTg; ++g) {
+        bool on = g < p->ntgroups;
+        md.tg_first[g] = on ? p->tg_first[g] : 1;
+        md.tg_last[g] = on ? p->tg_last[g] : 0;
+        md.tg_ndegf[g] = on ? p->tg_ndegf[g] : 1.0;
+        md.tg_ndegfree[g] = on ? p->tg_ndegfree[g] : 1.0;
+    }
+    md.ndegf = p->ndegf;
+    md.ndegfree = p->ndegfree;
+    md.dt = kMagicStepConv * p->stepsize;
+    md.tau = kMagicStepConv * p->tau_t;
+    md.temp0 = p->temp0;
+    md.boltz = kBoltz;
+    std::vector<double> m(mass, mass + n), wi(n);
+    for (int i = 0; i < n; ++i) wi[i] = 1.0 / m[i];
+    TRY(c->upload((double**)&md.mass, m));
+    TRY(c->upload((double**)&md.winv, wi));
+    std::vector<int> mf(nmol + 1, 0);
+    std::vector<int2> con(ncons);
+    std::vector<double> d2(ncons);
+    for (int k = 0; k <= nmol && nmol > 0; ++k) mf[k] = mol_first[k];
+    for (int k = 0; k < ncons; ++k) {
+        con[k] = make_int2(con_ij[2 * k], con_ij[2 * k + 1]);
+        d2[k] = con_dist[k] * con_dist[k];
+    }
+    TRY(c->upload((int**)&md.mol_first, mf));
+    TRY(c->upload((int2**)&md.con, con));
+    TRY(c->upload((double**)&md.dist2, d2));
+    const size_t n3 = 3 * (size_t)n;
+    TRY(c->alloc(&md.ready, (size_t)std::max(1, ncons) * c->nwin));
+    TRY(c->alloc(&md.v, n3 * c->nwin));
+    TRY(c->alloc(&md.xx, n3 * c->nwin));
+    TRY(c->alloc(&md.win, (size_t)c->nwin));
+    TRY(c->alloc(&md.fail, (size_t)c->nwin));
+    CU(cudaMemset(md.v, 0, sizeof(double) * n3 * c->nwin));
+    CU(cudaMemset(md.xx, 0, sizeof(double) * n3 * c->nwin));
+    CU(cudaMemset(md.win, 0, sizeof(MdWin) * c->nwin));
+    CU(cudaMemset(md.fail, 0, sizeof(int) * c->nwin));
+    TRY(c->alloc(&c->md_rec, (size_t)kMdChunk * c->nwin * kMdRec));
+    c->md_rec_steps = kMdChunk;
+    CU(cudaMallocHost((void**)&c->h_md_rec, sizeof(double) * kMdChunk * c->nwin * kMdRec));
+    // restrain_solvent of an MD step reads the window's Tfree on the device
+    for (int w = 0; w < c->nwin; ++w) c->st[w].md_tfree = &md.win[w].tfree;
+    TRY(upload_states(c));
+    c->mdp = *p;
+    c->md_ready = true;
+    c->md_prepared = false;
+    return QNB_OK;
+}
+
+int qnb_md_set_velocities(qnb_context* c, int32_t w, const double* v) {
+    TRY(md_check(c));
+    if (!v || w < 0 || w >= c->nwin) return fail(QNB_ERR_ARG, "bad window or null velocities");
+    CU(cudaSetDevice(c->device));
+    size_t n3 = 3 * (size_t)c->natom;
+    CU(cudaMemcpy(c->md.v + n3 * w, v, sizeof(double) * n3, cudaMemcpyHostToDevice));
+    c->md_prepared = false;
+    return QNB_OK;
+}
+
+int qnb_md_get_state(qnb_context* c, int32_t w, double* x, double* v) {
+    TRY(md_check(c));
+    if (w < 0 || w >= c->nwin) return fail(QNB_ERR_ARG, "window %d of %d", w, c->nwin);
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    size_t n3 = 3 * (size_t)c->natom;
+    if (x) CU(cudaMemcpy(x, c->st[w].x, sizeof(double) * n3, cudaMemcpyDeviceToHost));
+    if (v) CU(cudaMemcpy(v, c->md.v + n3 * w, sizeof(double) * n3, cudaMemcpyDeviceToHost));
+    return QNB_OK;
+}
+
+int qnb_md_prepare(qnb_context* c, int32_t stop_cm) {
+    TRY(md_check(c));
+    CU(cudaSetDevice(c->device));
+    Launch L = c->all();
+    CU(cudaMemsetAsync(c->md.fail, 0, sizeof(int) * c->nwin, c->stream));
+    // initial_constraint: xx = x, SHAKE x; xx = x - v dt, SHAKE xx against x; v = (x - xx)/dt
+    launch_md_copy_x(L, c->md, 1);
+    launch_md_shake(L, c->md, 0);
+    launch_md_copy_x(L, c->md, 2);
+    launch_md_shake(L, c->md, 1);
+    launch_md_velocity(L, c->md);
+    if (stop_cm) launch_md_stop_cm(L, c->md);
+    launch_md_temperature(L, c->md, c->m.excl);
+    c->launches += 6 + (stop_cm ? 1 : 0) + 1;
+    TRY(check_launch());
+    TRY(md_fail_check(c));
+    c->md_prepared = true;
+    return QNB_OK;
+}
+
+int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* rec, qnb_qenergies* EQ) {
+    TRY(md_check(c));
+    if (nsteps < 0 || istep0 < 0) return fail(QNB_ERR_ARG, "nsteps and istep0 must be >= 0");
+    if (!c->md_prepared) return fail(QNB_ERR_STATE, "qnb_md_prepare not called since the last state change");
+    CU(cudaSetDevice(c->device));
+    const qnb_md_params& p = c->mdp;
+    const int W = c->nwin;
+    CU(cudaMemsetAsync(c->md.fail, 0, sizeof(int) * W, c->stream));
+    for (int k0 = 0; k0 < nsteps; k0 += kMdChunk) {
+        const int nk = std::min(kMdChunk, nsteps - k0);
+        for (int k = 0; k < nk; ++k) {
+            const int istep = istep0 + k0 + k;
+            if (istep % p.nbcycle == 0 || !c->lists_built) {
+                if (k0 + k > 0) TRY(md_fail_check(c));   // no list build on coordinates of a failed SHAKE
+                Cut cut{p.rcq * p.rcq, p.rclrf * p.rclrf, p.rcpp * p.rcpp, p.rcpw * p.rcpw, p.rcww * p.rcww};
+                TRY(build_lists(c, cut, W));
+            }
+            Launch L = c->all();
+            launch_md_clear_d(L, c->md);
+            c->launches++;
+            TRY(run_compute(c, -1.0, istep));   // Tfree < 0: restrain_solvent reads it on the device
+            launch_md_newvel(L, c->md);
+            launch_md_shake(L, c->md, 0);
+            if (c->md.nmol > 0) launch_md_velocity(L, c->md);
+            launch_md_temperature(L, c->md, c->m.excl);
+            launch_md_record(L, c->md, c->e_all, c->efix_all, c->md_rec + (size_t)k * W * kMdRec);
+            c->launches += 4 + (c->md.nmol > 0 ? 1 : 0);
+            TRY(check_launch());
+        }
+        if (rec || EQ) {
+            CU(cudaMemcpyAsync(c->h_md_rec, c->md_rec, sizeof(double) * nk * W * kMdRec, cudaMemcpyDeviceToHost,
+                               c->stream));
+            CU(cudaStreamSynchronize(c->stream));
+            for (int k = 0; k < nk; ++k)
+                for (int w = 0; w < W; ++w) {
+                    const double* r = c->h_md_rec + ((size_t)k * W + w) * kMdRec;
+                    const long long* fx = reinterpret_cast<const long long*>(r + kNumE);
+                    double e[kNumE];
+                    for (int q = 0; q < kNumE; ++q) e[q] = r[q] + (double)fx[q] * (1.0 / kFix);
+                    size_t idx = (size_t)(k0 + k) * W + w;
+                    if (rec) {
+                        qnb_md_record& o = rec[idx];
+                        o = qnb_md_record{};
+                        add_energies(e, &o.E, nullptr, c->S);
+                        o.solvent_radial = e[E_RST_RAD];
+                        o.water_pol = e[E_RST_POL];
+                        o.ekin = r[2 * kNumE];
+                        o.temp = r[2 * kNumE + 1];
+                        o.tfree = r[2 * kNumE + 2];
+                        o.shake_iterations = r[2 * kNumE + 3];
+                    }
+                    if (EQ) {
+                        for (int s = 0; s < c->S; ++s) EQ[idx * c->S + s] = qnb_qenergies{};
+                        add_energies(e, nullptr, EQ + idx * c->S, c->S);
+                    }
+                }
+        }
+        TRY(md_fail_check(c));
+    }
     return QNB_OK;
 }
 

@@ -110,6 +110,7 @@ struct QQEntry {   // static Q-Q / Q-bonded-P pair of one state
 // Per-context device state of the lists, coordinates and accumulators.
 struct DevState {
     double* x;           // [natom*3] coordinates (FP64, as qdyn holds them)
+    const double* md_tfree;   // Tfree of the window's last MD temperature() (null before qnb_md_init)
     double* d;           // [natom*3] gradient accumulator (FP64 mode target)
     float4* xq;          // [natom] FP32 (x,y,z,charge) for the mixed form
     float* frow;         // [natom*3] mixed form: row-kernel gradient of each atom's own row (FP32)
@@ -213,6 +214,7 @@ struct SolventDev {
     // FP32 copies for the mixed form's restraint kernels
     float fk_wspheref, Dwmzf, awmzf, fkwpolf, cstbf[kMaxShell];
 };
+// Tfree < 0: every window's Tfree is read on the device (DevState::md_tfree)
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv);
 int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int mixed);
@@ -221,6 +223,46 @@ void launch_q_adjoint(const Launch& L, int mixed);
 
 void launch_export_pairs(const Launch& L, int win, int kind, int32_t* di, int32_t* dj, int64_t cap,
                          int* dcount);
+
+// ---- device-resident MD step (FP64) ----------------------------------------
+constexpr int kMaxTg = 4;          // temperature coupling groups
+constexpr int kShakeMaxIter = 1000;   // CONST_MAX_ITER, src/globals.f90:520
+struct MdWin {                     // per window, device
+    double sfact[kMaxTg];          // Berendsen factors of the next newvel
+    double temp, tfree, ekin;      // last temperature()
+    double tg_temp[kMaxTg], tg_tfree[kMaxTg], tg_texcl[kMaxTg];
+    unsigned long long shake_iters;   // SHAKE iterations of the last step, summed over molecules
+};
+struct MdDev {
+    int natom, ntg, nmol;
+    int tg_first[kMaxTg], tg_last[kMaxTg];
+    double tg_ndegf[kMaxTg], tg_ndegfree[kMaxTg], ndegf, ndegfree;
+    double dt, tau, temp0, boltz;
+    const double* winv;            // [natom] 1/mass
+    const double* mass;            // [natom]
+    const int* mol_first;          // [nmol+1]
+    const int2* con;               // [ncons] atom pairs
+    const double* dist2;           // [ncons] squared constraint distances
+    uint8_t* ready;                // [nwin][ncons] SHAKE scratch
+    int ncons;
+    double* v;                     // [nwin][natom*3]
+    double* xx;                    // [nwin][natom*3] positions before newvel
+    MdWin* win;                    // [nwin]
+    int* fail;                     // [nwin] 1 + a molecule whose SHAKE failed, 0 if none (sticky)
+};
+// a record of one window and step: FP64 energy slots, fixed-point slots, then
+// ekin, temp, tfree, SHAKE iterations
+constexpr int kMdRec = 2 * kNumE + 4;
+void launch_md_newvel(const Launch& L, const MdDev& md);
+// mode 0: constrain x against xx (the step); 1: constrain xx against x
+void launch_md_shake(const Launch& L, const MdDev& md, int mode);
+void launch_md_velocity(const Launch& L, const MdDev& md);
+void launch_md_copy_x(const Launch& L, const MdDev& md, int to_xx);   // xx = x (1) or the x - v dt of initial_constraint (2)
+void launch_md_temperature(const Launch& L, const MdDev& md, const uint8_t* excl);
+void launch_md_stop_cm(const Launch& L, const MdDev& md);
+void launch_md_record(const Launch& L, const MdDev& md, const double* e_all, const unsigned long long* efix_all,
+                      double* rec);
+void launch_md_clear_d(const Launch& L, const MdDev& md);   // d = 0, SHAKE count = 0
 
 // records msg as the calling thread's qnb_last_error text; returns code
 int set_error(int code, const char* msg);

@@ -1743,8 +1743,10 @@ __global__ void __launch_bounds__(kRowSumBlock) k_row_sums(DevModel m, const Dev
 // restrain_solvent, src/nonbondene.f90:6466-6544
 template <bool MIX>
 __global__ void k_restrain_solvent(DevModel m, const DevState* __restrict__ states, SolventDev p, double shift,
-                                   const int* __restrict__ wsw, const uint8_t* __restrict__ heavy_solv) {
+                                   const int* __restrict__ wsw, const uint8_t* __restrict__ heavy_solv, int tdev) {
     const DevState& s = states[blockIdx.y];
+    if (tdev)   // the window's Tfree from its last MD temperature(), as the host computes the shift
+        shift = (p.fk_wsphere != 0.0) ? sqrt(p.boltz * *s.md_tfree / p.fk_wsphere) : 0.0;
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> er;
     const float r0f = (float)(p.rwat - shift);
@@ -2865,10 +2867,11 @@ void launch_row_sums(const Launch& L) {
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv) {
     if (L.m.nwat == 0) return;
-    double shift = (p.fk_wsphere != 0.0) ? sqrt(p.boltz * Tfree / p.fk_wsphere) : 0.0;
+    const int tdev = Tfree < 0.0;
+    double shift = (!tdev && p.fk_wsphere != 0.0) ? sqrt(p.boltz * Tfree / p.fk_wsphere) : 0.0;
     dim3 g = grid_for(L.m.nwat, 32, 16, L.nwin);
-    if (mixed) k_restrain_solvent<true><<<g, 32, 0, L.st>>>(L.m, L.ds, p, shift, wsw, heavy_solv);
-    else k_restrain_solvent<false><<<g, 32, 0, L.st>>>(L.m, L.ds, p, shift, wsw, heavy_solv);
+    if (mixed) k_restrain_solvent<true><<<g, 32, 0, L.st>>>(L.m, L.ds, p, shift, wsw, heavy_solv, tdev);
+    else k_restrain_solvent<false><<<g, 32, 0, L.st>>>(L.m, L.ds, p, shift, wsw, heavy_solv, tdev);
 }
 // returns the number of launches
 int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int mixed) {

@@ -39,6 +39,7 @@ EXPORTED = (
     "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev", "qnb_get_energies_dev", "qnb_set_graphs",
     "qnb_group_create", "qnb_group_compute", "qnb_group_destroy", "qnb_profile_collect",
     "qnb_profile_classes", "qnb_set_solvent_internal", "qnb_autotune", "qnb_get_tuning", "qnb_set_tuning",
+    "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -91,6 +92,8 @@ def load_library(path: str = LIB_PATH):
         "qnb_profile_collect": [P], "qnb_profile_classes": [P, ctypes.c_uint32],
         "qnb_set_solvent_internal": [P, I32, P, P, P, P],
         "qnb_autotune": [P, I32, P], "qnb_get_tuning": [P, P], "qnb_set_tuning": [P, P],
+        "qnb_md_init": [P, P, P, I32, P, P, P], "qnb_md_set_velocities": [P, I32, P],
+        "qnb_md_get_state": [P, I32, P, P], "qnb_md_prepare": [P, I32], "qnb_md_run": [P, I32, I32, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -280,6 +283,52 @@ class NonbondedEngine:
     def set_tuning(self, values):
         v = np.array([values[n] for n in TUNE_NAMES], dtype=np.int32)
         self._check(self.lib.qnb_set_tuning(self.h, _p(v)))
+
+    # ---- device-resident MD step (qnb_md_*) -----------------------------
+    def md_init(self, setup=None):
+        """qnb_md_init from an MdSetup (q6_gb300.md): constraints, degrees of
+        freedom and temperature groups as qdyn derives them for this system."""
+        from .md import MdSetup, build_constraints, md_params
+        setup = setup or MdSetup()
+        cons = build_constraints(self.s, setup)
+        self.md_setup, self.md_constraints = setup, cons
+        self.md_p = md_params(self.s, setup, cons)
+        mass = np.ascontiguousarray(self.s.mass[self.s.iac], dtype=np.float64)
+        ij = np.ascontiguousarray(cons.ij, dtype=np.int32)
+        dist = np.ascontiguousarray(cons.dist)
+        self._check(self.lib.qnb_md_init(self.h, ctypes.byref(self.md_p), _p(mass), len(cons.mol_first) - 1,
+                                         _p(cons.mol_first), _p(ij), _p(dist)))
+
+    def md_set_velocities(self, v, window=None):
+        """v: [natom, 3] for one window (or every window if window is None),
+        or [nwin, natom, 3]."""
+        v = np.asarray(v, dtype=np.float64)
+        wins = range(self.nwin) if window is None else [window]
+        for k, w in enumerate(wins):
+            vw = np.ascontiguousarray(v[k] if v.ndim == 3 else v)
+            self._check(self.lib.qnb_md_set_velocities(self.h, int(w), _p(vw)))
+
+    def md_state(self, window=0):
+        x = np.zeros((self.s.natom, 3))
+        v = np.zeros((self.s.natom, 3))
+        self._check(self.lib.qnb_md_get_state(self.h, int(window), _p(x), _p(v)))
+        return x, v
+
+    def md_prepare(self, stop_cm=True):
+        self._check(self.lib.qnb_md_prepare(self.h, int(bool(stop_cm))))
+
+    def md_run(self, nsteps, istep0=0, records=True):
+        """nsteps MD steps of every window.  Returns (rec [nsteps][nwin]
+        structured as q6_gb300.md.MD_RECORD, EQ [nsteps][nwin][nstates][6])
+        or (None, None) without records."""
+        from .md import MD_RECORD
+        if not records:
+            self._check(self.lib.qnb_md_run(self.h, int(nsteps), int(istep0), None, None))
+            return None, None
+        rec = np.zeros((nsteps, self.nwin), MD_RECORD)
+        EQ = np.zeros((nsteps, self.nwin, max(self.S, 1), 6))
+        self._check(self.lib.qnb_md_run(self.h, int(nsteps), int(istep0), _p(rec), _p(EQ)))
+        return rec, EQ[:, :, : self.S]
 
     def profile_classes(self, names):
         """Profile only the named kernel classes (KERNEL_CLASSES); [] stops."""

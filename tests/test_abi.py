@@ -5,6 +5,7 @@ import os
 import re
 
 from q6_gb300 import build as qbuild
+from q6_gb300.md import MD_RECORD, QnbMdParams
 from q6_gb300.qnb import EXPORTED, QnbOptions
 from q6_gb300.system import QnbSolventParams, QnbTopology
 
@@ -46,6 +47,35 @@ def test_struct_layouts_match_header():
     assert nfields("qnb_topology") == len(QnbTopology._fields_)
     assert nfields("qnb_solvent_params") == len(QnbSolventParams._fields_)
     assert nfields("qnb_options") == len(QnbOptions._fields_)
+    assert nfields("qnb_md_params") == len(QnbMdParams._fields_)
+
+
+def test_md_struct_offsets_match_c_compiler(tmp_path):
+    """sizeof / offsetof of the MD structs from gcc against the ctypes and
+    numpy mirrors."""
+    import shutil
+    import subprocess
+    import pytest
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    names = [f[0] for f in QnbMdParams._fields_]
+    rec = list(MD_RECORD.names)
+    src = ['#include <stdio.h>', '#include <stddef.h>', '#include "qnb.h"', "int main(void) {",
+           'printf("%zu\\n", sizeof(qnb_md_params));']
+    src += ['printf("%%zu\\n", offsetof(qnb_md_params, %s));' % n for n in names]
+    src += ['printf("%zu\\n", sizeof(qnb_md_record));', 'printf("%zu\\n", offsetof(qnb_md_record, E));']
+    src += ['printf("%%zu\\n", offsetof(qnb_md_record, %s));' % n for n in rec[1:]]
+    src += ["return 0; }"]
+    c = tmp_path / "lay.c"
+    c.write_text("\n".join(src))
+    exe = tmp_path / "lay"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)])
+    out = [int(v) for v in subprocess.check_output([str(exe)]).split()]
+    assert out[0] == ctypes.sizeof(QnbMdParams)
+    assert out[1:1 + len(names)] == [getattr(QnbMdParams, n).offset for n in names]
+    k = 1 + len(names)
+    assert out[k] == MD_RECORD.itemsize
+    assert out[k + 1:] == [MD_RECORD.fields[n][1] for n in rec]
 
 
 def test_create_fails_loudly_without_gpu_or_bad_args():
