@@ -348,6 +348,7 @@ int qnb_take_launch_count(qnb_context* ctx, int64_t* n);
 enum {
     QNB_K_WW = 0, QNB_K_QW, QNB_K_PW, QNB_K_PP, QNB_K_QP, QNB_K_LRF_TAYLOR, QNB_K_QQ,
     QNB_K_RESTRAIN, QNB_K_WATPOL, QNB_K_PACK, QNB_K_APPLY, QNB_K_BUILD, QNB_K_LRF_BUILD,
+    QNB_K_BONDED, QNB_K_MD,
     QNB_K_COUNT
 };
 
@@ -361,6 +362,54 @@ int qnb_profile_classes(qnb_context* ctx, uint32_t mask);
 /* Total milliseconds and launches per kernel class since the last call
    (n entries, n <= QNB_K_COUNT); resets the totals. */
 int qnb_kernel_times(qnb_context* ctx, double* ms, int64_t* launches, int32_t n);
+
+/* ---- bonded terms (FP64) -----------------------------------------------------
+   pot_energy_bonds (src/potene.f90:258-317) and the Q-atom bonded terms of
+   pot_energy (src/potene.f90:180-189), evaluated inside qnb_compute_dev and
+   qnb_md_run once set:
+     bond       0.5 fk (r - b0)^2                       src/bondene.f90:182-245
+     angle      0.5 fk (theta - theta0)^2               src/bondene.f90:41-113
+     Urey-Bradley (urey_bradley != 0) ureyfk (r13 - r0)^2 on the same angles
+     torsion    fk (1 + cos(rmult phi - delta)) / paths src/bondene.f90:689-762
+     improper   imp_type 1: 0.5 fk wrap(phi - phi0)^2;  src/bondene.f90:247-317
+                imp_type 2: fk (1 + cos(2 phi - phi0))  src/bondene.f90:319-385
+     Q bond     Dmz (e^2 - 2e) + 0.5 fk db^2, e = exp(-amz db)   src/bondene.f90:506-553
+     Q angle / torsion / improper as above per state (Q torsions without the
+     paths divisor), energies unweighted per state, gradient weighted by
+     lambda_s                                           src/bondene.f90:387-448, 555-688
+   Lists are 0-based atoms and library codes; a code < 0 skips the term (the
+   topology entries qdyn removes: redefined in the FEP file, or constrained by
+   SHAKE, src/simprep.f90:1050-1135, 2330-2345, 4395-4491).  Entries [0,
+   n*_solute) count as solute (E%p), the rest as solvent (E%w).  Angles in
+   radians; torsion libraries hold 1/paths.  Q terms hold one code per state
+   (q*_code[term * nstates + s]).  Couplings of Q angles, torsions and
+   impropers to Morse bonds are not supported. */
+typedef struct qnb_bonded {
+    int32_t nbonds, nbonds_solute;     const int32_t* bonds;      /* [3n] i j code    */
+    int32_t nbondlib;                  const double* bondlib;     /* [2n] fk b0       */
+    int32_t nangles, nangles_solute;   const int32_t* angles;     /* [4n] i j k code  */
+    int32_t nanglib;                   const double* anglib;      /* [4n] fk theta0 ureyfk ureyr0 */
+    int32_t ntors, ntors_solute;       const int32_t* torsions;   /* [5n] i j k l code */
+    int32_t ntorlib;                   const double* torlib;      /* [4n] fk rmult delta 1/paths */
+    int32_t nimps, nimps_solute;       const int32_t* impropers;  /* [5n] i j k l code */
+    int32_t nimplib;                   const double* implib;      /* [2n] fk phi0     */
+    int32_t imp_type;                  /* 1 harmonic, 2 periodic                   */
+    int32_t urey_bradley;              /* CHARMM force fields: Urey-Bradley on     */
+    int32_t nqbonds;    const int32_t* qbonds;    const int32_t* qbond_code;   /* [2n], [n*S] */
+    int32_t nqbondlib;  const double* qbondlib;   /* [4n] Dmz amz r0 fk          */
+    int32_t nqangles;   const int32_t* qangles;   const int32_t* qangle_code;  /* [3n], [n*S] */
+    int32_t nqanglib;   const double* qanglib;    /* [4n] fk theta0 ureyfk ureyr0 */
+    int32_t nqtors;     const int32_t* qtorsions; const int32_t* qtorsion_code; /* [4n], [n*S] */
+    int32_t nqtorlib;   const double* qtorlib;    /* [3n] fk rmult delta         */
+    int32_t nqimps;     const int32_t* qimpropers; const int32_t* qimproper_code; /* [4n], [n*S] */
+    int32_t nqimplib;   const double* qimplib;    /* [2n] fk phi0                */
+} qnb_bonded;
+
+/* Bonded energies of the last evaluation of every window: Eb[w*8 + k] =
+   E%p%bond, angle, torsion, improper, E%w%bond, angle, torsion, improper;
+   EQb[(w*nstates + s)*4 + k] = EQ(s)%q%bond, angle, torsion, improper. */
+int qnb_set_bonded(qnb_context* ctx, const qnb_bonded* b);
+int qnb_get_bonded_energies(qnb_context* ctx, double* Eb, double* EQb);
 
 /* ---- device-resident MD step (FP64) ----------------------------------------
    qdyn's leap-frog step for the spherical boundary with the Berendsen
@@ -376,10 +425,8 @@ int qnb_kernel_times(qnb_context* ctx, double* ms, int64_t* launches, int32_t n)
                           v = (x - xx) / dt for every atom;
      temperature          Ekin, Temp, Tfree and the Berendsen factors
                           sfact_g = sqrt(1 + dt/tau_T (Temp0/Tfree_g - 1)).
-   Bonded terms are outside this library: the step integrates the nonbonded,
-   Q-Q and solvent-boundary forces (constrain the solute's bonds, or add the
-   bonded gradient through the caller's own kernels on qnb_stream between
-   steps).  Units as qdyn: masses in amu, time in fs (converted with qdyn's
+   The step's forces are those of qnb_compute_dev: nonbonded, Q-Q, solvent
+   boundary and, once qnb_set_bonded was called, the bonded terms.  Units as qdyn: masses in amu, time in fs (converted with qdyn's
    0.020462 per fs, src/md.f90:207 and 231), velocities in A per internal
    time unit. */
 enum { QNB_MAX_TGROUPS = 4 };
@@ -423,10 +470,13 @@ int qnb_md_get_state(qnb_context* ctx, int32_t window, double* x, double* v);
 int qnb_md_prepare(qnb_context* ctx, int32_t stop_cm);
 /* nsteps steps of every window starting at step number istep0 (lists are
    rebuilt where istep % nbcycle == 0, watpol updates by istep).  rec (may be
-   NULL): [nsteps][nwin] records; EQ (may be NULL): [nsteps][nwin][nstates].
+   NULL): [nsteps][nwin] records; EQ (may be NULL): [nsteps][nwin][nstates];
+   Eb (may be NULL): [nsteps][nwin][8 + 4*nstates], the bonded energies as
+   qnb_get_bonded_energies orders them (classical, then Q per state).
    QNB_ERR_CONSTRAINT if SHAKE failed in any window (the coordinates are then
    those of the failed step). */
-int qnb_md_run(qnb_context* ctx, int32_t nsteps, int32_t istep0, qnb_md_record* rec, qnb_qenergies* EQ);
+int qnb_md_run(qnb_context* ctx, int32_t nsteps, int32_t istep0, qnb_md_record* rec, qnb_qenergies* EQ,
+               double* Eb);
 
 /* ---- allocation-free entry point (no counterpart in the reference) ------- */
 

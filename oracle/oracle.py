@@ -63,6 +63,7 @@ def lib():
         L.orc_md_velocity.argtypes = [I, P, P, P, D]
         L.orc_md_stop_cm.argtypes = [I, P, P]
         L.orc_md_temperature.argtypes = [I, P, P, P, I, P, P, P, P, D, D, D, D, D, D, P, P]
+        L.orc_bonded.argtypes = [P, P, P, I, P, P, P]
         L.orc_static_qq_size.restype = ctypes.c_long
         L.orc_static_qq_size.argtypes = [P, I, I]
         _lib = L
@@ -164,6 +165,19 @@ class Oracle:
         lib().orc_get_lrf(self.h, _p(out))
         return out
 
+    def bonded(self, x, bt, lam, d=None):
+        """pot_energy_bonds + the Q-atom bonded terms for BondedTerms bt:
+        returns (d, Eb[8], EQb[nstates][4])."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if d is None:
+            d = np.zeros_like(x)
+        st, keep = bt.to_struct(self.S)
+        Eb = np.zeros(8)
+        EQb = np.zeros((max(self.S, 1), 4))
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        lib().orc_bonded(_p(x), _p(d), ctypes.byref(st), self.S, _p(lam), _p(Eb), _p(EQb))
+        return d, Eb, EQb[: self.S]
+
     def evaluate(self, x, lam, cut=None, solvent=None, Tfree=300.0, istep=0, lists=True):
         """One full nonbonded evaluation in the reference's call order."""
         cut = cut or {}
@@ -214,8 +228,10 @@ class OracleMD:
     BOLTZ = 0.001986
     MAGIC = 0.020462
 
-    def __init__(self, oracle: Oracle, p, cons, sp=None, lam=None):
+    def __init__(self, oracle: Oracle, p, cons, sp=None, lam=None, bonded=None):
         self.o, self.p, self.cons, self.sp = oracle, p, cons, sp
+        self.bt = bonded
+        self.lam = None if lam is None else np.asarray(lam, dtype=np.float64)
         s = oracle.s
         self.n = s.natom
         self.mass = np.ascontiguousarray(s.mass[s.iac], dtype=np.float64)
@@ -275,6 +291,9 @@ class OracleMD:
         d, E, EQ = o.pot_energy_nonbonds(x, d)
         d, EQ = o.nonbond_qq(x, d, EQ)
         erst = [0.0, 0.0]
+        Eb = EQb = None
+        if self.bt is not None:
+            d, Eb, EQb = o.bonded(x, self.bt, self.lam, d)
         if self.sp is not None:
             erst[0] = o.restrain_solvent(x, d, self.tfree)
             if self.sp.wpol_restr:
@@ -287,4 +306,5 @@ class OracleMD:
             iters = self._shake(x, xx)
             lib().orc_md_velocity(self.n, _p(x), _p(xx), _p(v), self.dt)
         t = self.temperature(v)
-        return dict(E=E, EQ=EQ, erst=erst, ekin=t[0], temp=t[1], tfree=t[2], shake_iterations=iters)
+        return dict(E=E, EQ=EQ, erst=erst, Eb=Eb, EQb=EQb, ekin=t[0], temp=t[1], tfree=t[2],
+                    shake_iterations=iters)

@@ -1371,3 +1371,207 @@ void orc_md_temperature(int natom, const double* v, const double* mass, const ui
     }
     (void)natom;
 }
+
+/* ---- bonded terms (strict FP64) ------------------------------------------
+   bond_calc / angle_calc / torsion_calc / improper_calc src/bonded.f90:53-320;
+   bond, angle, urey_bradley, torsion, improper, improper2
+   src/bondene.f90:41-385, 689-762; qbond, qangle, qurey_bradley, qtorsion,
+   qimproper src/bondene.f90:387-688 (no Morse couplings). */
+static v3 vneg(v3 a) { v3 r = {-a.x, -a.y, -a.z}; return r; }
+static v3 vcrs(v3 a, v3 b) {
+    v3 r = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return r;
+}
+static v3 vdivs(v3 a, double s) { v3 r = {a.x / s, a.y / s, a.z / s}; return r; }
+static void gadd(double* d, int i, v3 g) { d[3 * i] += g.x; d[3 * i + 1] += g.y; d[3 * i + 2] += g.z; }
+#define QEPS 1e-10
+
+typedef struct { double angl; v3 a, b, c; } angval;
+static angval angle_calc(v3 a, v3 b, v3 c) {
+    v3 ab = vsub(a, b), bc = vsub(c, b);
+    double ab2 = vsq(ab); ab2 = 1.0 / ab2;
+    double bc2 = vsq(bc); bc2 = 1.0 / bc2;
+    double abd = sqrt(ab2), bcd = sqrt(bc2);
+    double scalar = vdot(ab, bc);
+    scalar = scalar * abd * bcd;
+    if (scalar > 1.0) scalar = 1.0;
+    if (scalar < -1.0) scalar = -1.0;
+    angval r;
+    r.angl = acos(scalar);
+    double inv = sin(r.angl);
+    if (fabs(inv) < QEPS) inv = QEPS;
+    inv = -1.0 / inv;
+    v3 af = vscale(vsub(vscale(vscale(bc, abd), bcd), vscale(ab, ab2 * scalar)), inv);
+    v3 cf = vscale(vsub(vscale(vscale(ab, abd), bcd), vscale(bc, bc2 * scalar)), inv);
+    r.a = af; r.b = vadd(af, cf); r.c = cf;
+    return r;
+}
+
+typedef struct { double angl; v3 a, b, c, d; } torval;
+static torval torsion_calc(v3 a, v3 b, v3 c, v3 d) {
+    v3 ab = vsub(a, b), bc = vsub(c, b), cd = vsub(d, c);
+    v3 cabc = vcrs(ab, bc), cbcd = vcrs(vneg(bc), cd);
+    double a2abc = vsq(cabc), a2bcd = vsq(cbcd);
+    double aabc = sqrt(a2abc), abcd = sqrt(a2bcd);
+    double scalar = vdot(cabc, cbcd);
+    scalar = scalar / (aabc * abcd);
+    if (scalar > 1.0) scalar = 1.0;
+    if (scalar < -1.0) scalar = -1.0;
+    torval r;
+    r.angl = acos(scalar);
+    v3 dc = vcrs(cabc, cbcd);
+    if (vdot(bc, dc) < 0.0) r.angl = -r.angl;
+    double inv = sin(r.angl);
+    if (fabs(inv) < QEPS) inv = QEPS;
+    inv = -1.0 / inv;
+    v3 v1 = vscale(vsub(vdivs(cbcd, aabc * abcd), vscale(vdivs(cabc, a2abc), scalar)), inv);
+    v3 v2 = vscale(vsub(vdivs(cabc, aabc * abcd), vscale(vdivs(cbcd, a2bcd), scalar)), inv);
+    v3 ca = vsub(ab, bc), db = vsub(vneg(bc), cd);
+    r.a = vcrs(bc, v1);
+    r.b = vadd(vcrs(ca, v1), vcrs(cd, v2));
+    r.c = vsub(vcrs(db, v2), vcrs(ab, v1));
+    r.d = vcrs(bc, v2);
+    return r;
+}
+
+/* Eb[8]: p bond angle torsion improper, w bond angle torsion improper (added);
+   EQb[4*S]: per state q bond angle torsion improper (added); d added. */
+void orc_bonded(const double* x, double* d, const qnb_bonded* b, int S, const double* lambda, double* Eb,
+                double* EQb) {
+    const double two_pi = 2.0 * (4.0 * atan(1.0));
+    for (int k = 0; k < b->nbonds; ++k) {
+        const int32_t* e = b->bonds + 3 * k;
+        if (e[2] < 0) continue;
+        double fk = b->bondlib[2 * e[2]], b0 = b->bondlib[2 * e[2] + 1];
+        v3 av = vsub(X(x, e[1]), X(x, e[0]));
+        double dist = sqrt(vsq(av));
+        double db = dist - b0;
+        Eb[k < b->nbonds_solute ? 0 : 4] += 0.5 * fk * db * db;
+        double dv = fk * db / dist;
+        gadd(d, e[0], vscale(av, -dv));
+        gadd(d, e[1], vscale(av, dv));
+    }
+    for (int k = 0; k < b->nangles; ++k) {
+        const int32_t* e = b->angles + 4 * k;
+        if (e[3] < 0) continue;
+        const double* L = b->anglib + 4 * e[3];
+        angval c = angle_calc(X(x, e[0]), X(x, e[1]), X(x, e[2]));
+        double da = c.angl - L[1];
+        int slot = k < b->nangles_solute ? 1 : 5;
+        Eb[slot] += 0.5 * L[0] * da * da;
+        double dv = L[0] * da;
+        gadd(d, e[0], vscale(c.a, dv));
+        gadd(d, e[1], vscale(c.b, -dv));
+        gadd(d, e[2], vscale(c.c, dv));
+        if (b->urey_bradley && L[2] > 0.0) {   /* urey_bradley: the reference's gradient signs */
+            v3 av = vsub(X(x, e[2]), X(x, e[0]));
+            double dist = sqrt(vsq(av));
+            double ru = dist - L[3];
+            Eb[slot] += L[2] * ru * ru;
+            double du = 2.0 * L[2] * ru / dist;
+            gadd(d, e[2], vscale(av, -du));
+            gadd(d, e[0], vscale(av, du));
+        }
+    }
+    for (int k = b->ntors - 1; k >= 0; --k) {
+        const int32_t* e = b->torsions + 5 * k;
+        if (e[4] < 0) continue;
+        const double* L = b->torlib + 4 * e[4];
+        torval c = torsion_calc(X(x, e[0]), X(x, e[1]), X(x, e[2]), X(x, e[3]));
+        double arg = L[1] * c.angl - L[2];
+        Eb[k < b->ntors_solute ? 2 : 6] += L[0] * (1.0 + cos(arg)) * L[3];
+        double dv = -L[1] * L[0] * sin(arg) * L[3];
+        gadd(d, e[0], vscale(c.a, dv)); gadd(d, e[1], vscale(c.b, dv));
+        gadd(d, e[2], vscale(c.c, dv)); gadd(d, e[3], vscale(c.d, dv));
+    }
+    for (int k = b->nimps - 1; k >= 0; --k) {
+        const int32_t* e = b->impropers + 5 * k;
+        if (e[4] < 0) continue;
+        const double* L = b->implib + 2 * e[4];
+        torval c = torsion_calc(X(x, e[0]), X(x, e[1]), X(x, e[2]), X(x, e[3]));
+        double ei, dv;
+        if (b->imp_type == 2) {
+            double arg = 2.0 * c.angl - L[1];
+            ei = L[0] * (1.0 + cos(arg));
+            dv = -2.0 * L[0] * sin(arg);
+        } else {
+            double arg = c.angl - L[1];
+            arg = arg - two_pi * round(arg / two_pi);
+            dv = L[0] * arg;
+            ei = 0.5 * dv * arg;
+        }
+        Eb[k < b->nimps_solute ? 3 : 7] += ei;
+        gadd(d, e[0], vscale(c.a, dv)); gadd(d, e[1], vscale(c.b, dv));
+        gadd(d, e[2], vscale(c.c, dv)); gadd(d, e[3], vscale(c.d, dv));
+    }
+    for (int st = 0; st < S; ++st) {
+        const double lam = lambda[st];
+        for (int k = 0; k < b->nqbonds; ++k) {
+            int code = b->qbond_code[k * S + st];
+            if (code < 0) continue;
+            const double* L = b->qbondlib + 4 * code;   /* Dmz amz r0 fk */
+            int i = b->qbonds[2 * k], j = b->qbonds[2 * k + 1];
+            v3 av = vsub(X(x, j), X(x, i));
+            double dist = sqrt(vsq(av));
+            double db = dist - L[2];
+            double fexp = exp(-L[1] * db);
+            EQb[4 * st] += L[0] * (fexp * fexp - 2.0 * fexp) + 0.5 * L[3] * db * db;
+            double dv = (2.0 * L[0] * L[1] * (fexp - fexp * fexp) + L[3] * db) * lam / dist;
+            gadd(d, i, vscale(av, -dv));
+            gadd(d, j, vscale(av, dv));
+        }
+        for (int k = 0; k < b->nqangles; ++k) {
+            int code = b->qangle_code[k * S + st];
+            if (code < 0) continue;
+            const double* L = b->qanglib + 4 * code;
+            const int32_t* e = b->qangles + 3 * k;
+            angval c = angle_calc(X(x, e[0]), X(x, e[1]), X(x, e[2]));
+            double da = c.angl - L[1];
+            EQb[4 * st + 1] += 0.5 * L[0] * da * da;
+            double dv = L[0] * da * lam;
+            gadd(d, e[0], vscale(c.a, dv));
+            gadd(d, e[1], vscale(c.b, -dv));
+            gadd(d, e[2], vscale(c.c, dv));
+        }
+        if (b->urey_bradley)
+            for (int k = 0; k < b->nqangles; ++k) {
+                int code = b->qangle_code[k * S + st];
+                if (code < 0 || b->qanglib[4 * code + 2] == 0.0) continue;
+                const double* L = b->qanglib + 4 * code;
+                const int32_t* e = b->qangles + 3 * k;
+                v3 av = vsub(X(x, e[2]), X(x, e[0]));
+                double dist = sqrt(vsq(av));
+                double ru = dist - L[3];
+                EQb[4 * st + 1] += L[2] * ru * ru;
+                double du = 2.0 * (L[2] * ru / dist) * lam;
+                gadd(d, e[0], vscale(av, -du));
+                gadd(d, e[2], vscale(av, du));
+            }
+        for (int k = 0; k < b->nqtors; ++k) {
+            int code = b->qtorsion_code[k * S + st];
+            if (code < 0) continue;
+            const double* L = b->qtorlib + 3 * code;
+            const int32_t* e = b->qtorsions + 4 * k;
+            torval c = torsion_calc(X(x, e[0]), X(x, e[1]), X(x, e[2]), X(x, e[3]));
+            double arg = L[1] * c.angl - L[2];
+            EQb[4 * st + 2] += L[0] * (1.0 + cos(arg));
+            double dv = -L[1] * L[0] * sin(arg) * lam;
+            gadd(d, e[0], vscale(c.a, dv)); gadd(d, e[1], vscale(c.b, dv));
+            gadd(d, e[2], vscale(c.c, dv)); gadd(d, e[3], vscale(c.d, dv));
+        }
+        for (int k = 0; k < b->nqimps; ++k) {
+            int code = b->qimproper_code[k * S + st];
+            if (code < 0) continue;
+            const double* L = b->qimplib + 2 * code;
+            const int32_t* e = b->qimpropers + 4 * k;
+            torval c = torsion_calc(X(x, e[0]), X(x, e[1]), X(x, e[2]), X(x, e[3]));
+            double arg = c.angl - L[1];
+            arg = arg - two_pi * round(arg / two_pi);
+            double dv = L[0] * arg;
+            EQb[4 * st + 3] += 0.5 * dv * arg;
+            dv = dv * lam;
+            gadd(d, e[0], vscale(c.a, dv)); gadd(d, e[1], vscale(c.b, dv));
+            gadd(d, e[2], vscale(c.c, dv)); gadd(d, e[3], vscale(c.d, dv));
+        }
+    }
+}

@@ -141,6 +141,10 @@ struct qnb_context {
     double* h_stage = nullptr;   // pinned staging for x / d (natom*3)
     double* h_e = nullptr;       // pinned energies (nwin x (kNumE doubles + kNumE fixed))
 
+    // bonded terms (qnb_set_bonded)
+    bool have_bonded = false;
+    BondedDev bonded{};
+    std::vector<void*> bonded_bufs;
     // device-resident MD (qnb_md_*)
     bool md_ready = false;         // qnb_md_init done
     bool md_prepared = false;      // qnb_md_prepare done since the last state change
@@ -1435,6 +1439,10 @@ int enqueue_compute(qnb_context* c, double Tfree, int istep) {
     TRY(compute_nonbond(c, 1, c->nwin));
     timed(c, K_QQ, [&] { launch_nonbond_qq(L, c->mixed); });
     c->launches++;
+    if (c->have_bonded) {
+        timed(c, K_BONDED, [&] { launch_bonded(L, c->bonded, c->mixed); });
+        c->launches++;
+    }
     if (c->have_solv) {
         timed(c, K_RESTRAIN, [&] { launch_restrain_solvent(L, c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv); });
         c->launches++;
@@ -1893,6 +1901,13 @@ constexpr double kMagicStepConv = 0.020462;   // fs -> internal time, src/global
 constexpr double kBoltz = 0.001986;           // src/globals.f90:46
 constexpr int kMdChunk = 256;                 // steps recorded on the device between read-backs
 
+// Eb[0..7] classical bonded, Eb[8 + 4s + k] Q bonded of state s
+void bonded_out(const qnb_context* c, const double* e, double* Eb) {
+    for (int k = 0; k < 8; ++k) Eb[k] = e[E_B0 + k];
+    for (int st = 0; st < c->S; ++st)
+        for (int k = 0; k < 4; ++k) Eb[8 + 4 * st + k] = e[qb_slot(st, k)];
+}
+
 int md_check(qnb_context* c) {
     if (!c) return fail(QNB_ERR_ARG, "null context");
     if (!c->md_ready) return fail(QNB_ERR_STATE, "qnb_md_init not called");
@@ -2045,7 +2060,8 @@ int qnb_md_prepare(qnb_context* c, int32_t stop_cm) {
     return QNB_OK;
 }
 
-int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* rec, qnb_qenergies* EQ) {
+int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* rec, qnb_qenergies* EQ,
+               double* Eb) {
     TRY(md_check(c));
     if (nsteps < 0 || istep0 < 0) return fail(QNB_ERR_ARG, "nsteps and istep0 must be >= 0");
     if (!c->md_prepared) return fail(QNB_ERR_STATE, "qnb_md_prepare not called since the last state change");
@@ -2066,15 +2082,17 @@ int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* re
             launch_md_clear_d(L, c->md);
             c->launches++;
             TRY(run_compute(c, -1.0, istep));   // Tfree < 0: restrain_solvent reads it on the device
-            launch_md_newvel(L, c->md);
-            launch_md_shake(L, c->md, 0);
-            if (c->md.nmol > 0) launch_md_velocity(L, c->md);
-            launch_md_temperature(L, c->md, c->m.excl);
-            launch_md_record(L, c->md, c->e_all, c->efix_all, c->md_rec + (size_t)k * W * kMdRec);
+            timed(c, K_MD, [&] {
+                launch_md_newvel(L, c->md);
+                launch_md_shake(L, c->md, 0);
+                if (c->md.nmol > 0) launch_md_velocity(L, c->md);
+                launch_md_temperature(L, c->md, c->m.excl);
+                launch_md_record(L, c->md, c->e_all, c->efix_all, c->md_rec + (size_t)k * W * kMdRec);
+            });
             c->launches += 4 + (c->md.nmol > 0 ? 1 : 0);
             TRY(check_launch());
         }
-        if (rec || EQ) {
+        if (rec || EQ || Eb) {
             CU(cudaMemcpyAsync(c->h_md_rec, c->md_rec, sizeof(double) * nk * W * kMdRec, cudaMemcpyDeviceToHost,
                                c->stream));
             CU(cudaStreamSynchronize(c->stream));
@@ -2100,9 +2118,149 @@ int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* re
                         for (int s = 0; s < c->S; ++s) EQ[idx * c->S + s] = qnb_qenergies{};
                         add_energies(e, nullptr, EQ + idx * c->S, c->S);
                     }
+                    if (Eb) bonded_out(c, e, Eb + idx * (8 + 4 * (size_t)c->S));
                 }
         }
         TRY(md_fail_check(c));
+    }
+    return QNB_OK;
+}
+
+}  // extern "C"
+
+// =============================================================================
+// Bonded terms (qnb_set_bonded)
+// =============================================================================
+extern "C" {
+
+int qnb_set_bonded(qnb_context* c, const qnb_bonded* b) {
+    if (!c || !b) return fail(QNB_ERR_ARG, "null argument");
+    const int n = c->natom, S = c->S;
+    auto atoms_ok = [&](const int32_t* v, int cnt, int stride, int na) -> bool {
+        for (int k = 0; k < cnt; ++k)
+            for (int a = 0; a < na; ++a)
+                if (v[stride * k + a] < 0 || v[stride * k + a] >= n) return false;
+        return true;
+    };
+    auto codes_ok = [&](const int32_t* v, int cnt, int stride, int off, int nlib) -> bool {
+        for (int k = 0; k < cnt; ++k)
+            if (v[stride * k + off] >= nlib) return false;
+        return true;
+    };
+    struct L { int cnt, sol; const int32_t* v; int lib; const double* libv; const char* name; };
+    const L cl[4] = {{b->nbonds, b->nbonds_solute, b->bonds, b->nbondlib, b->bondlib, "bond"},
+                     {b->nangles, b->nangles_solute, b->angles, b->nanglib, b->anglib, "angle"},
+                     {b->ntors, b->ntors_solute, b->torsions, b->ntorlib, b->torlib, "torsion"},
+                     {b->nimps, b->nimps_solute, b->impropers, b->nimplib, b->implib, "improper"}};
+    const int na[4] = {2, 3, 4, 4};
+    for (int k = 0; k < 4; ++k) {
+        if (cl[k].cnt < 0 || cl[k].sol < 0 || cl[k].sol > cl[k].cnt || cl[k].lib < 0 ||
+            (cl[k].cnt > 0 && !cl[k].v) || (cl[k].lib > 0 && !cl[k].libv))
+            return fail(QNB_ERR_ARG, "%s list: bad counts or null arrays", cl[k].name);
+        if (!atoms_ok(cl[k].v, cl[k].cnt, na[k] + 1, na[k]) || !codes_ok(cl[k].v, cl[k].cnt, na[k] + 1, na[k], cl[k].lib))
+            return fail(QNB_ERR_ARG, "%s list: atom or library code out of range", cl[k].name);
+    }
+    if (b->imp_type != 1 && b->imp_type != 2) return fail(QNB_ERR_ARG, "imp_type %d not 1 or 2", b->imp_type);
+    struct Q { int cnt; const int32_t* v; const int32_t* code; int lib; const double* libv; const char* name; };
+    const Q ql[4] = {{b->nqbonds, b->qbonds, b->qbond_code, b->nqbondlib, b->qbondlib, "Q bond"},
+                     {b->nqangles, b->qangles, b->qangle_code, b->nqanglib, b->qanglib, "Q angle"},
+                     {b->nqtors, b->qtorsions, b->qtorsion_code, b->nqtorlib, b->qtorlib, "Q torsion"},
+                     {b->nqimps, b->qimpropers, b->qimproper_code, b->nqimplib, b->qimplib, "Q improper"}};
+    for (int k = 0; k < 4; ++k) {
+        if (ql[k].cnt < 0 || ql[k].lib < 0 || (ql[k].cnt > 0 && (!ql[k].v || !ql[k].code || S == 0)) ||
+            (ql[k].lib > 0 && !ql[k].libv))
+            return fail(QNB_ERR_ARG, "%s list: bad counts or null arrays", ql[k].name);
+        if (!atoms_ok(ql[k].v, ql[k].cnt, na[k], na[k]) || !codes_ok(ql[k].code, ql[k].cnt * S, 1, 0, ql[k].lib))
+            return fail(QNB_ERR_ARG, "%s list: atom or library code out of range", ql[k].name);
+    }
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    for (void* p : c->bonded_bufs) c->release(p);
+    c->bonded_bufs.clear();
+    BondedDev d{};
+    auto up = [&](auto** dst, const auto& vec) -> int {
+        int rc = c->upload(dst, vec);
+        if (!rc) c->bonded_bufs.push_back((void*)*dst);
+        return rc;
+    };
+    std::vector<int4> bonds(b->nbonds), angles(b->nangles);
+    for (int k = 0; k < b->nbonds; ++k) bonds[k] = make_int4(b->bonds[3 * k], b->bonds[3 * k + 1], b->bonds[3 * k + 2], 0);
+    for (int k = 0; k < b->nangles; ++k)
+        angles[k] = make_int4(b->angles[4 * k], b->angles[4 * k + 1], b->angles[4 * k + 2], b->angles[4 * k + 3]);
+    std::vector<double2> bl(b->nbondlib), il(b->nimplib), qil(b->nqimplib);
+    for (int k = 0; k < b->nbondlib; ++k) bl[k] = make_double2(b->bondlib[2 * k], b->bondlib[2 * k + 1]);
+    for (int k = 0; k < b->nimplib; ++k) il[k] = make_double2(b->implib[2 * k], b->implib[2 * k + 1]);
+    for (int k = 0; k < b->nqimplib; ++k) qil[k] = make_double2(b->qimplib[2 * k], b->qimplib[2 * k + 1]);
+    auto d4 = [](const double* v, int cnt, int w) {
+        std::vector<double4> o(cnt);
+        for (int k = 0; k < cnt; ++k)
+            o[k] = make_double4(v[w * k], v[w * k + 1], w > 2 ? v[w * k + 2] : 0.0, w > 3 ? v[w * k + 3] : 0.0);
+        return o;
+    };
+    std::vector<double4> al = d4(b->anglib, b->nanglib, 4), tl = d4(b->torlib, b->ntorlib, 4),
+                         qbl = d4(b->qbondlib, b->nqbondlib, 4), qal = d4(b->qanglib, b->nqanglib, 4),
+                         qtl = d4(b->qtorlib, b->nqtorlib, 3);
+    std::vector<int> tors(b->torsions, b->torsions + 5 * (size_t)b->ntors),
+        imps(b->impropers, b->impropers + 5 * (size_t)b->nimps);
+    std::vector<int2> qb(b->nqbonds);
+    for (int k = 0; k < b->nqbonds; ++k) qb[k] = make_int2(b->qbonds[2 * k], b->qbonds[2 * k + 1]);
+    auto i4 = [](const int32_t* v, int cnt, int w) {
+        std::vector<int4> o(cnt);
+        for (int k = 0; k < cnt; ++k) o[k] = make_int4(v[w * k], v[w * k + 1], v[w * k + 2], w > 3 ? v[w * k + 3] : 0);
+        return o;
+    };
+    std::vector<int4> qa = i4(b->qangles, b->nqangles, 3), qt = i4(b->qtorsions, b->nqtors, 4),
+                      qi = i4(b->qimpropers, b->nqimps, 4);
+    std::vector<int> qbc(b->qbond_code, b->qbond_code + (size_t)b->nqbonds * S),
+        qac(b->qangle_code, b->qangle_code + (size_t)b->nqangles * S),
+        qtc(b->qtorsion_code, b->qtorsion_code + (size_t)b->nqtors * S),
+        qic(b->qimproper_code, b->qimproper_code + (size_t)b->nqimps * S);
+    TRY(up((int4**)&d.bonds, bonds));
+    TRY(up((double2**)&d.bondlib, bl));
+    TRY(up((int4**)&d.angles, angles));
+    TRY(up((double4**)&d.anglib, al));
+    TRY(up((int**)&d.tors, tors));
+    TRY(up((double4**)&d.torlib, tl));
+    TRY(up((int**)&d.imps, imps));
+    TRY(up((double2**)&d.implib, il));
+    TRY(up((int2**)&d.qbonds, qb));
+    TRY(up((int**)&d.qbond_code, qbc));
+    TRY(up((double4**)&d.qbondlib, qbl));
+    TRY(up((int4**)&d.qangles, qa));
+    TRY(up((int**)&d.qangle_code, qac));
+    TRY(up((double4**)&d.qanglib, qal));
+    TRY(up((int4**)&d.qtors, qt));
+    TRY(up((int**)&d.qtor_code, qtc));
+    TRY(up((double4**)&d.qtorlib, qtl));
+    TRY(up((int4**)&d.qimps, qi));
+    TRY(up((int**)&d.qimp_code, qic));
+    TRY(up((double2**)&d.qimplib, qil));
+    d.nb = b->nbonds; d.nb_sol = b->nbonds_solute;
+    d.na = b->nangles; d.na_sol = b->nangles_solute;
+    d.nt = b->ntors; d.nt_sol = b->ntors_solute;
+    d.ni = b->nimps; d.ni_sol = b->nimps_solute;
+    d.imp_type = b->imp_type;
+    d.urey = b->urey_bradley != 0;
+    d.nqb = b->nqbonds; d.nqa = b->nqangles; d.nqt = b->nqtors; d.nqi = b->nqimps;
+    d.nterms = d.nb + d.na + d.nt + d.ni + S * (d.nqb + d.nqa + d.nqt + d.nqi);
+    c->bonded = d;
+    c->have_bonded = d.nterms > 0;
+    ++c->epoch;   // captured graphs lack (or hold a stale) bonded launch
+    return QNB_OK;
+}
+
+int qnb_get_bonded_energies(qnb_context* c, double* Eb, double* EQb) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    std::vector<double> e((size_t)kNumE * c->nwin);
+    TRY(read_energies(c, c->nwin, e.data()));
+    for (int w = 0; w < c->nwin; ++w) {
+        double t[8 + 4 * kMaxStates];
+        bonded_out(c, e.data() + (size_t)w * kNumE, t);
+        if (Eb)
+            for (int k = 0; k < 8; ++k) Eb[8 * w + k] = t[k];
+        if (EQb)
+            for (int k = 0; k < 4 * c->S; ++k) EQb[(size_t)w * 4 * c->S + k] = t[8 + k];
     }
     return QNB_OK;
 }

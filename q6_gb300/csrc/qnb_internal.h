@@ -22,7 +22,12 @@ enum {
     E_RST_RAD, E_RST_POL, E_Q0
 };
 __host__ __device__ constexpr int eq_slot(int s, int k) { return E_Q0 + 6 * s + k; }
-constexpr int kNumE = E_Q0 + 6 * kMaxStates;
+// bonded: solute bond, angle, torsion, improper, then the same for solvent;
+// then per state the Q bond, angle, torsion, improper
+constexpr int E_B0 = E_Q0 + 6 * kMaxStates;
+constexpr int E_QB0 = E_B0 + 8;
+__host__ __device__ constexpr int qb_slot(int s, int k) { return E_QB0 + 4 * s + k; }
+constexpr int kNumE = E_QB0 + 4 * kMaxStates;
 
 // list counters (entries at list granularity, plus reference atom-pair counts)
 enum { C_WW = 0, C_PW, C_PP, C_QP, C_QW, C_PP14, C_PPG,
@@ -205,7 +210,7 @@ void launch_solvent_internal(const Launch& L, const int2* ij, const double* par,
 
 // kernel classes timed by the optional event profiler
 enum { K_WW = 0, K_QW, K_PW, K_PP, K_QP, K_LRF_TAYLOR, K_QQ, K_RESTRAIN, K_WATPOL, K_PACK, K_APPLY,
-       K_BUILD, K_LRF_BUILD, K_NUM };
+       K_BUILD, K_LRF_BUILD, K_BONDED, K_MD, K_NUM };
 
 struct SolventDev {
     double fk_wsphere, Dwmz, awmz, rwat, boltz, fkwpol, itdis;
@@ -223,6 +228,31 @@ void launch_q_adjoint(const Launch& L, int mixed);
 
 void launch_export_pairs(const Launch& L, int win, int kind, int32_t* di, int32_t* dj, int64_t cap,
                          int* dcount);
+
+// ---- bonded terms (FP64 in both forms) ---------------------------------------
+struct BondedDev {
+    int nb, nb_sol, na, na_sol, nt, nt_sol, ni, ni_sol;
+    const int4* bonds;      // i j code -
+    const double2* bondlib; // fk b0
+    const int4* angles;     // i j k code
+    const double4* anglib;  // fk theta0 ureyfk ureyr0
+    const int* tors;        // [5n] i j k l code
+    const double4* torlib;  // fk rmult delta 1/paths
+    const int* imps;        // [5n]
+    const double2* implib;  // fk phi0
+    int imp_type, urey;
+    int nqb, nqa, nqt, nqi;
+    const int2* qbonds; const int* qbond_code;   // [n], [n*S]
+    const double4* qbondlib;                     // Dmz amz r0 fk
+    const int4* qangles; const int* qangle_code; // i j k -
+    const double4* qanglib;
+    const int4* qtors; const int* qtor_code;
+    const double4* qtorlib;                      // fk rmult delta -
+    const int4* qimps; const int* qimp_code;
+    const double2* qimplib;
+    int nterms;             // classical terms + Q terms x states
+};
+void launch_bonded(const Launch& L, const BondedDev& b, int mixed);
 
 // ---- device-resident MD step (FP64) ----------------------------------------
 constexpr int kMaxTg = 4;          // temperature coupling groups

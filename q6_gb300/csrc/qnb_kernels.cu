@@ -2864,6 +2864,267 @@ void launch_row_sums(const Launch& L) {
     if (L.m.ncgp_solute + L.m.nwat == 0) return;
     k_row_sums<<<L.nwin, kRowSumBlock, 0, L.st>>>(L.m, L.ds);
 }
+// =============================================================================
+// Bonded terms (FP64 in both forms; the mixed form sums in fixed point)
+// =============================================================================
+struct V3 {
+    double x, y, z;
+};
+__device__ __forceinline__ V3 v3(const double* x, int i) { return V3{x[3 * i], x[3 * i + 1], x[3 * i + 2]}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a) { return V3{-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ V3 operator*(V3 a, double f) { return V3{a.x * f, a.y * f, a.z * f}; }
+__device__ __forceinline__ V3 operator/(V3 a, double f) { return V3{a.x / f, a.y / f, a.z / f}; }
+__device__ __forceinline__ double vdot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 vcross(V3 a, V3 b) {
+    return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+constexpr double kQrealEpsD = 1e-10;   // QREAL_EPS of the double-precision build
+constexpr double kPi = 3.14159265358979323846;   // 4 atan(1)
+
+// angle_calc, src/bonded.f90:78-118
+struct AngleVal {
+    double angl;
+    V3 a, b, c;
+};
+__device__ AngleVal angle_calc(V3 a, V3 b, V3 c) {
+    V3 ab = a - b, bc = c - b;
+    double ab2 = 1.0 / vdot(ab, ab), bc2 = 1.0 / vdot(bc, bc);
+    double abd = sqrt(ab2), bcd = sqrt(bc2);
+    double scalar = vdot(ab, bc) * abd * bcd;
+    scalar = fmin(1.0, fmax(-1.0, scalar));
+    AngleVal r;
+    r.angl = acos(scalar);
+    double inv = sin(r.angl);
+    if (fabs(inv) < kQrealEpsD) inv = kQrealEpsD;
+    inv = -1.0 / inv;
+    V3 af = ((bc * abd * bcd) - (ab * (ab2 * scalar))) * inv;
+    V3 cf = ((ab * abd * bcd) - (bc * (bc2 * scalar))) * inv;
+    r.a = af;
+    r.b = af + cf;
+    r.c = cf;
+    return r;
+}
+
+// torsion_calc / improper_calc (identical), src/bonded.f90:151-320
+struct TorsVal {
+    double angl;
+    V3 a, b, c, d;
+};
+__device__ TorsVal torsion_calc(V3 a, V3 b, V3 c, V3 d) {
+    V3 ab = a - b, bc = c - b, cd = d - c;
+    V3 cabc = vcross(ab, bc), cbcd = vcross(-bc, cd);
+    double a2abc = vdot(cabc, cabc), a2bcd = vdot(cbcd, cbcd);
+    double aabc = sqrt(a2abc), abcd = sqrt(a2bcd);
+    double scalar = vdot(cabc, cbcd) / (aabc * abcd);
+    scalar = fmin(1.0, fmax(-1.0, scalar));
+    TorsVal r;
+    r.angl = acos(scalar);
+    if (vdot(bc, vcross(cabc, cbcd)) < 0.0) r.angl = -r.angl;
+    double inv = sin(r.angl);
+    if (fabs(inv) < kQrealEpsD) inv = kQrealEpsD;
+    inv = -1.0 / inv;
+    V3 v1 = ((cbcd / (aabc * abcd)) - ((cabc / a2abc) * scalar)) * inv;
+    V3 v2 = ((cabc / (aabc * abcd)) - ((cbcd / a2bcd) * scalar)) * inv;
+    V3 ca = ab - bc, db = -bc - cd;
+    r.a = vcross(bc, v1);
+    r.b = vcross(ca, v1) + vcross(cd, v2);
+    r.c = vcross(db, v2) - vcross(ab, v1);
+    r.d = vcross(bc, v2);
+    return r;
+}
+
+template <bool MIX>
+struct BondedSink {
+    Acc<MIX> acc;
+    __device__ __forceinline__ void grad(int i, V3 g) const {
+        if constexpr (MIX) acc.gradd(i, g.x, g.y, g.z);
+        else acc.grad(i, g.x, g.y, g.z);
+    }
+    __device__ __forceinline__ void energy(int slot, double e) const {
+        if constexpr (MIX) acc.energy_fix(slot, to_fixd(e));
+        else acc.energy(slot, e);
+    }
+};
+
+// One thread per term: classical bonds, angles (+ Urey-Bradley), torsions,
+// impropers; then Q bonds, angles, torsions, impropers per state.
+template <bool MIX>
+__global__ void __launch_bounds__(128) k_bonded(DevModel m, const DevState* __restrict__ states, BondedDev b) {
+    const DevState& s = states[blockIdx.y];
+    const BondedSink<MIX> out{make_acc<MIX>(s)};
+    const double* __restrict__ x = s.x;
+    const int S = m.S;
+    const double two_pi = 2.0 * kPi;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < b.nterms; t += gridDim.x * blockDim.x) {
+        int u = t;
+        if (u < b.nb) {   // bond, src/bondene.f90:182-245
+            int4 e = b.bonds[u];
+            if (e.z < 0) continue;
+            double2 lib = b.bondlib[e.z];
+            V3 av = v3(x, e.y) - v3(x, e.x);
+            double dist = sqrt(vdot(av, av));
+            double db = dist - lib.y;
+            out.energy(E_B0 + (u < b.nb_sol ? 0 : 4), 0.5 * lib.x * db * db);
+            double dv = lib.x * db / dist;
+            out.grad(e.x, -(av * dv));
+            out.grad(e.y, av * dv);
+            continue;
+        }
+        u -= b.nb;
+        if (u < b.na) {   // angle, src/bondene.f90:41-113 (+ urey_bradley 115-180)
+            int4 e = b.angles[u];
+            if (e.w < 0) continue;
+            double4 lib = b.anglib[e.w];
+            const int slot = E_B0 + (u < b.na_sol ? 1 : 5);
+            AngleVal c = angle_calc(v3(x, e.x), v3(x, e.y), v3(x, e.z));
+            double da = c.angl - lib.y;
+            double ea = 0.5 * lib.x * da * da;
+            double dv = lib.x * da;
+            out.grad(e.x, c.a * dv);
+            out.grad(e.y, -(c.b * dv));
+            out.grad(e.z, c.c * dv);
+            if (b.urey && lib.z > 0.0) {
+                // the reference's solute/solvent Urey-Bradley adds the gradient
+                // with these signs (d(k) -= a du, d(i) += a du)
+                V3 av = v3(x, e.z) - v3(x, e.x);
+                double dist = sqrt(vdot(av, av));
+                double ru = dist - lib.w;
+                ea += lib.z * ru * ru;
+                double du = 2.0 * lib.z * ru / dist;
+                out.grad(e.z, -(av * du));
+                out.grad(e.x, av * du);
+            }
+            out.energy(slot, ea);
+            continue;
+        }
+        u -= b.na;
+        if (u < b.nt) {   // torsion, src/bondene.f90:689-762
+            const int* e = b.tors + 5 * u;
+            if (e[4] < 0) continue;
+            double4 lib = b.torlib[e[4]];
+            TorsVal c = torsion_calc(v3(x, e[0]), v3(x, e[1]), v3(x, e[2]), v3(x, e[3]));
+            double arg = lib.y * c.angl - lib.z;
+            out.energy(E_B0 + (u < b.nt_sol ? 2 : 6), lib.x * (1.0 + cos(arg)) * lib.w);
+            double dv = -lib.y * lib.x * sin(arg) * lib.w;
+            out.grad(e[0], c.a * dv);
+            out.grad(e[1], c.b * dv);
+            out.grad(e[2], c.c * dv);
+            out.grad(e[3], c.d * dv);
+            continue;
+        }
+        u -= b.nt;
+        if (u < b.ni) {   // improper (harmonic) / improper2 (periodic), src/bondene.f90:247-385
+            const int* e = b.imps + 5 * u;
+            if (e[4] < 0) continue;
+            double2 lib = b.implib[e[4]];
+            TorsVal c = torsion_calc(v3(x, e[0]), v3(x, e[1]), v3(x, e[2]), v3(x, e[3]));
+            double ei, dv;
+            if (b.imp_type == 2) {
+                double arg = 2.0 * c.angl - lib.y;
+                ei = lib.x * (1.0 + cos(arg));
+                dv = -2.0 * lib.x * sin(arg);
+            } else {
+                double arg = c.angl - lib.y;
+                arg = arg - two_pi * round(arg / two_pi);
+                dv = lib.x * arg;
+                ei = 0.5 * dv * arg;
+            }
+            out.energy(E_B0 + (u < b.ni_sol ? 3 : 7), ei);
+            out.grad(e[0], c.a * dv);
+            out.grad(e[1], c.b * dv);
+            out.grad(e[2], c.c * dv);
+            out.grad(e[3], c.d * dv);
+            continue;
+        }
+        u -= b.ni;
+        // Q terms: index = term * S + state
+        if (u < b.nqb * S) {   // qbond, src/bondene.f90:506-553
+            const int q = u / S, st = u % S, code = b.qbond_code[u];
+            if (code < 0) continue;
+            int2 e = b.qbonds[q];
+            double4 lib = b.qbondlib[code];   // Dmz amz r0 fk
+            V3 av = v3(x, e.y) - v3(x, e.x);
+            double dist = sqrt(vdot(av, av));
+            double db = dist - lib.z;
+            double fexp = exp(-lib.y * db);
+            out.energy(qb_slot(st, 0), lib.x * (fexp * fexp - 2.0 * fexp) + 0.5 * lib.w * db * db);
+            double dv = (2.0 * lib.x * lib.y * (fexp - fexp * fexp) + lib.w * db) * s.lambda[st] / dist;
+            out.grad(e.x, -(av * dv));
+            out.grad(e.y, av * dv);
+            continue;
+        }
+        u -= b.nqb * S;
+        if (u < b.nqa * S) {   // qangle (+ qurey_bradley), src/bondene.f90:387-504
+            const int q = u / S, st = u % S, code = b.qangle_code[u];
+            if (code < 0) continue;
+            int4 e = b.qangles[q];
+            double4 lib = b.qanglib[code];
+            const double lam = s.lambda[st];
+            AngleVal c = angle_calc(v3(x, e.x), v3(x, e.y), v3(x, e.z));
+            double da = c.angl - lib.y;
+            double ea = 0.5 * lib.x * da * da;
+            double dv = lib.x * da * lam;
+            out.grad(e.x, c.a * dv);
+            out.grad(e.y, -(c.b * dv));
+            out.grad(e.z, c.c * dv);
+            if (b.urey && lib.z != 0.0) {
+                V3 av = v3(x, e.z) - v3(x, e.x);
+                double dist = sqrt(vdot(av, av));
+                double ru = dist - lib.w;
+                ea += lib.z * ru * ru;
+                double du = 2.0 * (lib.z * ru / dist) * lam;
+                out.grad(e.x, -(av * du));
+                out.grad(e.z, av * du);
+            }
+            out.energy(qb_slot(st, 1), ea);
+            continue;
+        }
+        u -= b.nqa * S;
+        if (u < b.nqt * S) {   // qtorsion, src/bondene.f90:624-688
+            const int q = u / S, st = u % S, code = b.qtor_code[u];
+            if (code < 0) continue;
+            int4 e = b.qtors[q];
+            double4 lib = b.qtorlib[code];
+            TorsVal c = torsion_calc(v3(x, e.x), v3(x, e.y), v3(x, e.z), v3(x, e.w));
+            double arg = lib.y * c.angl - lib.z;
+            out.energy(qb_slot(st, 2), lib.x * (1.0 + cos(arg)));
+            double dv = -lib.y * lib.x * sin(arg) * s.lambda[st];
+            out.grad(e.x, c.a * dv);
+            out.grad(e.y, c.b * dv);
+            out.grad(e.z, c.c * dv);
+            out.grad(e.w, c.d * dv);
+            continue;
+        }
+        u -= b.nqt * S;
+        if (u < b.nqi * S) {   // qimproper (harmonic), src/bondene.f90:555-622
+            const int q = u / S, st = u % S, code = b.qimp_code[u];
+            if (code < 0) continue;
+            int4 e = b.qimps[q];
+            double2 lib = b.qimplib[code];
+            TorsVal c = torsion_calc(v3(x, e.x), v3(x, e.y), v3(x, e.z), v3(x, e.w));
+            double arg = c.angl - lib.y;
+            arg = arg - two_pi * round(arg / two_pi);
+            double dv = lib.x * arg;
+            out.energy(qb_slot(st, 3), 0.5 * dv * arg);
+            dv = dv * s.lambda[st];
+            out.grad(e.x, c.a * dv);
+            out.grad(e.y, c.b * dv);
+            out.grad(e.z, c.c * dv);
+            out.grad(e.w, c.d * dv);
+        }
+    }
+}
+
+void launch_bonded(const Launch& L, const BondedDev& b, int mixed) {
+    if (b.nterms == 0) return;
+    int blocks = std::min(256, (b.nterms + 127) / 128);
+    dim3 g(blocks, L.nwin);
+    if (mixed) k_bonded<true><<<g, 128, 0, L.st>>>(L.m, L.ds, b);
+    else k_bonded<false><<<g, 128, 0, L.st>>>(L.m, L.ds, b);
+}
+
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv) {
     if (L.m.nwat == 0) return;

@@ -40,11 +40,12 @@ EXPORTED = (
     "qnb_group_create", "qnb_group_compute", "qnb_group_destroy", "qnb_profile_collect",
     "qnb_profile_classes", "qnb_set_solvent_internal", "qnb_autotune", "qnb_get_tuning", "qnb_set_tuning",
     "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
+    "qnb_set_bonded", "qnb_get_bonded_energies",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
 KERNEL_CLASSES = ("ww", "qw", "pw", "pp", "qp", "lrf_taylor", "qq", "restrain", "watpol", "pack",
-                  "apply", "build", "lrf_build")
+                  "apply", "build", "lrf_build", "bonded", "md")
 
 
 class QnbError(RuntimeError):
@@ -93,7 +94,8 @@ def load_library(path: str = LIB_PATH):
         "qnb_set_solvent_internal": [P, I32, P, P, P, P],
         "qnb_autotune": [P, I32, P], "qnb_get_tuning": [P, P], "qnb_set_tuning": [P, P],
         "qnb_md_init": [P, P, P, I32, P, P, P], "qnb_md_set_velocities": [P, I32, P],
-        "qnb_md_get_state": [P, I32, P, P], "qnb_md_prepare": [P, I32], "qnb_md_run": [P, I32, I32, P, P],
+        "qnb_md_get_state": [P, I32, P, P], "qnb_md_prepare": [P, I32], "qnb_md_run": [P, I32, I32, P, P, P],
+        "qnb_set_bonded": [P, P], "qnb_get_bonded_energies": [P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -319,16 +321,31 @@ class NonbondedEngine:
 
     def md_run(self, nsteps, istep0=0, records=True):
         """nsteps MD steps of every window.  Returns (rec [nsteps][nwin]
-        structured as q6_gb300.md.MD_RECORD, EQ [nsteps][nwin][nstates][6])
-        or (None, None) without records."""
+        structured as q6_gb300.md.MD_RECORD, EQ [nsteps][nwin][nstates][6],
+        Eb [nsteps][nwin][8 + 4*nstates]) or (None, None, None) without
+        records."""
         from .md import MD_RECORD
         if not records:
-            self._check(self.lib.qnb_md_run(self.h, int(nsteps), int(istep0), None, None))
-            return None, None
+            self._check(self.lib.qnb_md_run(self.h, int(nsteps), int(istep0), None, None, None))
+            return None, None, None
         rec = np.zeros((nsteps, self.nwin), MD_RECORD)
         EQ = np.zeros((nsteps, self.nwin, max(self.S, 1), 6))
-        self._check(self.lib.qnb_md_run(self.h, int(nsteps), int(istep0), _p(rec), _p(EQ)))
-        return rec, EQ[:, :, : self.S]
+        Eb = np.zeros((nsteps, self.nwin, 8 + 4 * self.S))
+        self._check(self.lib.qnb_md_run(self.h, int(nsteps), int(istep0), _p(rec), _p(EQ), _p(Eb)))
+        return rec, EQ[:, :, : self.S], Eb
+
+    # ---- bonded terms ------------------------------------------------------
+    def set_bonded(self, bt):
+        """qnb_set_bonded from a q6_gb300.bonded.BondedTerms."""
+        st, keep = bt.to_struct(self.S)
+        self._check(self.lib.qnb_set_bonded(self.h, ctypes.byref(st)))
+
+    def bonded_energies(self):
+        """(Eb [nwin][8], EQb [nwin][nstates][4]) of the last evaluation."""
+        Eb = np.zeros((self.nwin, 8))
+        EQb = np.zeros((self.nwin, max(self.S, 1), 4))
+        self._check(self.lib.qnb_get_bonded_energies(self.h, _p(Eb), _p(EQb)))
+        return Eb, EQb[:, : self.S]
 
     def profile_classes(self, names):
         """Profile only the named kernel classes (KERNEL_CLASSES); [] stops."""

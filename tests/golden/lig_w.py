@@ -63,8 +63,44 @@ def load_lig_w() -> tuple[QSystem, dict]:
         qexpnb_pairs=np.zeros((0, 2), np.int32), xpcent=f["xpcent"], xwcent=f["xwcent"],
         rexcl_o=float(f["rexcl_o"]), rwat=float(f["rwat"]), mass=mass,
         iuse_switch_atom=int(f["iuse_switch_atom"]), name="lig_w")
-    golden = {k: float(f[k]) for k in ("golden_qsurr_el", "golden_qsurr_vdw", "golden_el", "golden_vdw")}
+    golden = {k: float(f[k]) for k in ("golden_qsurr_el", "golden_qsurr_vdw", "golden_el", "golden_vdw",
+                                       "golden_bnd", "golden_ang", "golden_tor", "golden_imp",
+                                       "golden_qbnd", "golden_qang", "golden_qtor", "golden_qimp")}
     golden["wbond_ij"] = f["wbond_ij"]
     golden["wbond_b0"] = f["wbond_b0"]
     golden["wbond_code"] = f["wbond_code"]
     return s, golden
+
+
+def lig_w_bonded(s):
+    """The bonded terms qdyn evaluates for lig_w: the topology lists with
+    the FEP-redefined terms and the SHAKE-constrained bonds removed
+    (defaults shake_solvent on, shake_solute off, shake_hydrogens on,
+    shake_heavy off), libraries converted as topology() does."""
+    from q6_gb300.bonded import DEG2RAD, BondedTerms, remove_redefined, remove_shaken
+    f = np.load(os.path.join(HERE, "lig_w.npz"))
+    anglib = f["anglib"].copy()
+    anglib[:, 1] *= DEG2RAD
+    torlib = f["torlib"].copy()
+    torlib[:, 2] *= DEG2RAD
+    torlib[:, 3] = 1.0 / torlib[:, 3]
+    implib = f["implib"].copy()
+    implib[:, 1] *= DEG2RAD
+    qanglib = f["fep_anglelib"].copy()
+    qanglib[:, 1] *= DEG2RAD
+    qtorlib = f["fep_torsionlib"].copy()
+    qtorlib[:, 2] *= DEG2RAD
+    qimplib = f["fep_improperlib"].copy()
+    qimplib[:, 1] *= DEG2RAD
+    bt = BondedTerms(
+        bonds=f["top_bonds"], nbonds_solute=int(f["nbonds_solute"]), bondlib=f["bondlib"],
+        angles=f["top_angles"], nangles_solute=int(f["nangles_solute"]), anglib=anglib,
+        torsions=f["top_torsions"], ntors_solute=int(f["ntors_solute"]), torlib=torlib,
+        impropers=f["top_impropers"], nimps_solute=int(f["nimps_solute"]), implib=implib,
+        imp_type=int(f["imp_type"]), urey_bradley=int(int(f["ff_type"]) == 3),
+        qbonds=f["fep_qbonds"], qbond_code=f["fep_qbond_code"], qbondlib=f["fep_bondlib"],
+        qangles=f["fep_qangles"], qangle_code=f["fep_qangle_code"], qanglib=qanglib,
+        qtorsions=f["fep_qtorsions"], qtorsion_code=f["fep_qtorsion_code"], qtorlib=qtorlib,
+        qimpropers=f["fep_qimpropers"], qimproper_code=f["fep_qimproper_code"], qimplib=qimplib)
+    bt = remove_redefined(bt)
+    return remove_shaken(bt, np.asarray(s.heavy).astype(bool), s.nat_solute)

@@ -9,8 +9,10 @@ the Q6 tree is not needed at test time.
 The step-0 energies that the Q6 regression test checks for this system
 (tests/basic_tests/eval_test.sh:99 and row 1 of
 SPH_leap-frog_berendsen_benchmark.en) are stored beside the arrays:
-Q-surr. el 3.12, vdW 139.43 (Q-atom state 1, lambda 1) and the sums of the
-solute, solvent and solute-solvent rows, EL -7.30, VdW -413.17.
+Q-surr. el 3.12, vdW 139.43 (Q-atom state 1, lambda 1), the sums of the
+solute, solvent and solute-solvent rows, EL -7.30, VdW -413.17, and the
+bonded columns of that row: solute bond 31.61, angle 30.69, torsion 6.28,
+improper 0.05; Q-atom bond -122.04, angle 0.68, torsion 2.17, improper 0.00.
 
 Usage: python tests/golden/make_lig_w_fixture.py [Q6_ROOT]
 """
@@ -86,8 +88,13 @@ class Reader:
 def read_top(path):
     r = Reader(path)
     assert r.line().strip() == "Q topology file"
-    while not r.line().strip().upper().startswith("END"):
-        pass
+    ff_type = 1   # FF_GROMOS unless the header names another (src/topo.f90:567)
+    while True:
+        ln = r.line().strip()
+        if ln.upper().startswith("END"):
+            break
+        if ln.upper().startswith("FF_TYPE"):
+            ff_type = int(ln.split()[1])
     nat_pro, nat_solute = r.head_ints(2)
     solv_atom = 3
     x = np.array(r.values(3 * nat_pro), dtype=np.float64).reshape(nat_pro, 3)
@@ -102,20 +109,23 @@ def read_top(path):
     na = r.head_ints(2)
     nangles = na[0]
     ang = np.array(r.values(4 * nangles, int), dtype=np.int64).reshape(nangles, 4)
+    nangles_solute = na[1] if len(na) > 1 else nangles
     nangcod = r.head_ints(1)[0]
-    anglib = [r.head_floats(3) for _ in range(nangcod)]
+    anglib = [(r.head_floats(5)[1:] + [0.0, 0.0])[:4] for _ in range(nangcod)]   # fk theta0 [ureyfk ureyr0]
     nt = r.head_ints(2)
     ntors = nt[0]
-    r.values(5 * ntors, int)
+    ntors_solute = nt[1] if len(nt) > 1 else ntors
+    tor = np.array(r.values(5 * ntors, int), dtype=np.int64).reshape(ntors, 5)
     ntorcod = r.head_ints(1)[0]
-    for _ in range(ntorcod):
-        r.line()
+    torlib = [r.head_floats(5)[1:5] for _ in range(ntorcod)]   # fk rmult deltor paths
     ni = r.head_ints(2)
     nimps = ni[0]
-    r.values(5 * nimps, int)
-    nimpcod = r.head_ints(2)[0]
-    for _ in range(nimpcod):
-        r.line()
+    nimps_solute = ni[1] if len(ni) > 1 else nimps
+    imp = np.array(r.values(5 * nimps, int), dtype=np.int64).reshape(nimps, 5)
+    nic = r.head_ints(2)
+    nimpcod = nic[0]
+    imp_type = nic[1] if len(nic) > 1 else 1
+    implib = [r.head_floats(3)[1:3] for _ in range(nimpcod)]   # fk imp0
     nq = r.head_ints(1)[0]
     crg = np.array(r.values(nq), dtype=np.float64)
     cg = r.head_ints(3)
@@ -185,7 +195,17 @@ def read_top(path):
         # SHAKE constraints qdyn applies at start-up (shake_solvent defaults on)
         wbond_ij=(bnd[nbonds_solute:, :2] - 1).astype(np.int32),
         wbond_b0=np.array([bondlib[int(c) - 1][2] for c in bnd[nbonds_solute:, 2]]),
-        wbond_code=bnd[nbonds_solute:, 2].astype(np.int32))
+        wbond_code=bnd[nbonds_solute:, 2].astype(np.int32),
+        # bonded lists (0-based atoms and codes) and libraries as the topology
+        # holds them (degrees, torsion paths not inverted)
+        ff_type=ff_type, top_bonds=(bnd - 1).astype(np.int32), nbonds_solute=nbonds_solute,
+        bondlib=np.array([b[1:3] for b in bondlib], np.float64),
+        top_angles=(ang - 1).astype(np.int32), nangles_solute=nangles_solute,
+        anglib=np.array(anglib, np.float64),
+        top_torsions=(tor - 1).astype(np.int32), ntors_solute=ntors_solute,
+        torlib=np.array(torlib, np.float64),
+        top_impropers=(imp - 1).astype(np.int32), nimps_solute=nimps_solute,
+        implib=np.array(implib, np.float64), imp_type=imp_type)
 
 
 def read_fep_atoms(path):
@@ -209,16 +229,64 @@ def read_fep_atoms(path):
     return states, np.array(atoms, np.int32)
 
 
+def read_fep_bonded(path, nstates):
+    """Q bonded sections of the FEP file as qatom_load_fep reads them
+    (src/qatom.f90:950-1510): [bond_types] id Dmz amz r0 (Morse) or id fk r0
+    (harmonic); [angle_types] id fk theta0 [ureyfk ureyr0]; [torsion_types]
+    id fk rmult deltor; [improper_types] id fk imp0; [change_*] atoms then one
+    type per state (0 = absent).  Comments after '!' are dropped."""
+    secs = {}
+    sec = None
+    with open(path) as f:
+        for ln in f:
+            t = ln.split("!")[0].strip()
+            if not t:
+                continue
+            if t.startswith("["):
+                sec = t.strip("[]").lower()
+                secs[sec] = []
+                continue
+            if sec:
+                secs[sec].append(t.split())
+    out = {}
+    bl = {}
+    for v in secs.get("bond_types", []):
+        if len(v) >= 4:
+            bl[int(v[0])] = (float(v[1]), float(v[2]), float(v[3]), 0.0)   # Dmz amz r0 fk
+        else:
+            bl[int(v[0])] = (0.0, 0.0, float(v[2]), float(v[1]))
+    al = {int(v[0]): (float(v[1]), float(v[2]), float(v[3]) if len(v) > 4 else 0.0,
+                      float(v[4]) if len(v) > 4 else 0.0) for v in secs.get("angle_types", [])}
+    tl = {int(v[0]): (float(v[1]), float(v[2]), float(v[3])) for v in secs.get("torsion_types", [])}
+    il = {int(v[0]): (float(v[1]), float(v[2])) for v in secs.get("improper_types", [])}
+    for name, lib, nat in (("bond", bl, 2), ("angle", al, 3), ("torsion", tl, 4), ("improper", il, 4)):
+        keys = sorted(lib)
+        index = {k: n for n, k in enumerate(keys)}
+        out["fep_%slib" % name] = np.array([lib[k] for k in keys], np.float64).reshape(len(keys), -1)
+        rows = secs.get("change_%ss" % name, [])
+        atoms = np.array([[int(a) - 1 for a in v[:nat]] for v in rows], np.int32).reshape(-1, nat)
+        codes = np.array([[index[int(c)] if int(c) > 0 else -1 for c in v[nat:nat + nstates]] for v in rows],
+                         np.int32).reshape(-1, nstates)
+        out["fep_q%ss" % name] = atoms
+        out["fep_q%s_code" % name] = codes
+    return out
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     d = os.path.join(root, "tests", "basic_tests", "prep_SPH")
     top = read_top(os.path.join(d, "lig_w.top"))
     nstates, iqseq = read_fep_atoms(os.path.join(d, "lig_w.fep"))
+    fepb = read_fep_bonded(os.path.join(d, "lig_w.fep"), nstates)
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lig_w.npz")
     np.savez_compressed(
-        out, **top, nstates=nstates, iqseq=iqseq,
+        out, **top, **fepb, nstates=nstates, iqseq=iqseq,
         golden_qsurr_el=3.12, golden_qsurr_vdw=139.43,
-        golden_el=-7.30, golden_vdw=-413.17)
+        golden_el=-7.30, golden_vdw=-413.17,
+        # row 1 of SPH_leap-frog_berendsen_benchmark.en: the solute row's
+        # bond, angle, torsion, improper and the Q-atom row's (state 1)
+        golden_bnd=31.61, golden_ang=30.69, golden_tor=6.28, golden_imp=0.05,
+        golden_qbnd=-122.04, golden_qang=0.68, golden_qtor=2.17, golden_qimp=0.00)
     print("wrote", out, "atoms", top["natom"], "solute", top["nat_solute"],
           "groups", len(top["cgp_first"]), "Q", len(iqseq))
 

@@ -58,6 +58,8 @@ def test_md_struct_offsets_match_c_compiler(tmp_path):
     import pytest
     if not shutil.which("gcc"):
         pytest.skip("no C compiler")
+    from q6_gb300.bonded import QnbBonded
+    bnames = [f[0] for f in QnbBonded._fields_]
     names = [f[0] for f in QnbMdParams._fields_]
     rec = list(MD_RECORD.names)
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "qnb.h"', "int main(void) {",
@@ -65,6 +67,8 @@ def test_md_struct_offsets_match_c_compiler(tmp_path):
     src += ['printf("%%zu\\n", offsetof(qnb_md_params, %s));' % n for n in names]
     src += ['printf("%zu\\n", sizeof(qnb_md_record));', 'printf("%zu\\n", offsetof(qnb_md_record, E));']
     src += ['printf("%%zu\\n", offsetof(qnb_md_record, %s));' % n for n in rec[1:]]
+    src += ['printf("%zu\\n", sizeof(qnb_bonded));']
+    src += ['printf("%%zu\\n", offsetof(qnb_bonded, %s));' % n for n in bnames]
     src += ["return 0; }"]
     c = tmp_path / "lay.c"
     c.write_text("\n".join(src))
@@ -75,7 +79,10 @@ def test_md_struct_offsets_match_c_compiler(tmp_path):
     assert out[1:1 + len(names)] == [getattr(QnbMdParams, n).offset for n in names]
     k = 1 + len(names)
     assert out[k] == MD_RECORD.itemsize
-    assert out[k + 1:] == [MD_RECORD.fields[n][1] for n in rec]
+    assert out[k + 1:k + 1 + len(rec)] == [MD_RECORD.fields[n][1] for n in rec]
+    k += 1 + len(rec)
+    assert out[k] == ctypes.sizeof(QnbBonded)
+    assert out[k + 1:] == [getattr(QnbBonded, n).offset for n in bnames]
 
 
 def test_create_fails_loudly_without_gpu_or_bad_args():

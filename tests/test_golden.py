@@ -10,7 +10,7 @@ src/bondene.f90:1025-1048) at the topology coordinates.
 import numpy as np
 
 from oracle.oracle import Oracle, shake
-from tests.golden.lig_w import load_lig_w
+from tests.golden.lig_w import lig_w_bonded, load_lig_w
 
 
 def _step0_coordinates(s, g):
@@ -46,3 +46,19 @@ def test_lig_w_without_shake_misses_golden():
     o = Oracle(s, use_lrf=True)
     d, E, EQ, _ = o.evaluate(s.x, [1.0])
     assert f"{EQ[0, 2] + EQ[0, 4]:.2f}" != f"{g['golden_qsurr_el']:.2f}"
+
+
+def test_lig_w_step0_bonded_energies_match_reference_strings():
+    """Row 1 of SPH_leap-frog_berendsen_benchmark.en: the solute row's bond,
+    angle, torsion, improper (31.61 30.69 6.28 0.05) and the Q-atom row's
+    (-122.04 0.68 2.17 0.00), with the FEP-redefined terms and the SHAKE-
+    constrained solvent bonds removed from the topology lists as qdyn does."""
+    s, g = load_lig_w()
+    x = _step0_coordinates(s, g)
+    o = Oracle(s, use_lrf=True)
+    _, Eb, EQb = o.bonded(x, lig_w_bonded(s), [1.0])
+    got = [Eb[0], Eb[1], Eb[2], Eb[3], EQb[0, 0], EQb[0, 1], EQb[0, 2], EQb[0, 3]]
+    want = [g[k] for k in ("golden_bnd", "golden_ang", "golden_tor", "golden_imp",
+                           "golden_qbnd", "golden_qang", "golden_qtor", "golden_qimp")]
+    for a, b in zip(got, want):
+        assert f"{a:.2f}" == f"{b:.2f}", (a, b)

@@ -27,7 +27,7 @@ def system():
     return make_system(R=14.0, n_solute=40, group_sizes=(3, 5), ntypes=6, nq=6, nstates=2, seed=5150)
 
 
-def device_run(s, prec, nsteps, lams, setup=SETUP, graphs=True, v0=None):
+def device_run(s, prec, nsteps, lams, setup=SETUP, graphs=True, v0=None, bonded=None, eb=None):
     W = len(lams)
     sp = default_solvent_params(s, itdis=4.0)
     with NonbondedEngine(s, precision=prec, windows=W) as e:
@@ -36,12 +36,16 @@ def device_run(s, prec, nsteps, lams, setup=SETUP, graphs=True, v0=None):
         for w in range(W):
             e.set_lambda(lams[w], window=w)
         e.set_coordinates_dev(np.stack([s.x] * W))
+        if bonded is not None:
+            e.set_bonded(bonded)
         e.md_init(setup)
         e.md_set_velocities(v0 if v0 is not None else np.stack([maxwell_velocities(s, 300.0, 11 + w)
                                                                  for w in range(W)]))
         e.md_prepare(stop_cm=True)
-        rec, EQ = e.md_run(nsteps)
+        rec, EQ, Eb = e.md_run(nsteps)
         st = [e.md_state(w) for w in range(W)]
+    if eb is not None:
+        eb.append(Eb)
     return rec, EQ, st
 
 
@@ -122,3 +126,27 @@ def test_shake_failure_is_reported(system):
         assert cons.ij[2].tolist() == [o + 1, o + 2]
         with pytest.raises(QnbError, match="SHAKE failed in window 0, molecule 0"):
             e.md_prepare()
+
+
+def test_fp64_md_with_bonded_terms_matches_oracle(system):
+    """The step with solute bonded and Q bonded terms (constraints on the
+    water only): 10 steps against the oracle's step with the same terms."""
+    from q6_gb300.bonded import synthetic_bonded
+    s = system
+    lam = [0.6, 0.4]
+    setup = dataclasses.replace(SETUP, shake_solute=False, stepsize=0.5)
+    bt = synthetic_bonded(s, seed=21)
+    eb = []
+    rec, EQ, st = device_run(s, PREC_FP64, 10, [lam], setup=setup, bonded=bt, eb=eb)
+    sp = default_solvent_params(s, itdis=4.0)
+    o = Oracle(s)
+    o.set_solvent_params(sp)
+    cons = build_constraints(s, setup)
+    md = OracleMD(o, md_params(s, setup, cons), cons, sp=sp, lam=lam, bonded=bt)
+    x, v = md.prepare(s.x, maxwell_velocities(s, 300.0, 11))
+    for k in range(10):
+        r = md.step(x, v, k, CUT)
+        assert np.allclose(eb[0][k, 0, :8], r["Eb"], rtol=1e-9, atol=1e-9), k
+        assert np.allclose(eb[0][k, 0, 8:].reshape(2, 4), r["EQb"], rtol=1e-9, atol=1e-9), k
+        assert abs(rec[k, 0]["temp"] - r["temp"]) <= 1e-10 * r["temp"], k
+    assert np.allclose(st[0][0], x, rtol=0, atol=1e-9)
