@@ -270,6 +270,8 @@ def run_ours(args, rank, world, local):
             out["cpu_baseline"] = cpu_baseline(s, sp, args)
         if args.replicas:
             out["replica_group"] = replica_group(args, local)
+        if args.md:
+            out["md_step"] = md_step(args, s, sp, lams, local, tuning)
         if args.fp64_compare:
             out["fp64_value"] = fp64_compare(args, s, sp, lams, local)
             out["mixed_over_fp64"] = round(out["value"] / out["fp64_value"], 3) if out["fp64_value"] else None
@@ -500,6 +502,71 @@ def replica_group(args, local):
                     "one CUDA graph launch per step"}
 
 
+def md_step(args, s, sp, lams, local, tuning=None):
+    """Device-resident MD steps (qnb_md_run) of the same 51 windows: the
+    evaluation above plus the solute and Q bonded terms of the generated
+    topology, leap-frog with Berendsen coupling (solute and solvent groups),
+    SHAKE of the waters and temperature(), lists every 25 steps, 1 fs steps
+    at 300 K.  Window-steps/s over the timed run; no host round trip inside
+    it (records read back after the run)."""
+    import numpy as np
+    import torch
+    from q6_gb300.bonded import synthetic_bonded
+    from q6_gb300.md import MdSetup, maxwell_velocities
+    from q6_gb300.qnb import PREC_MIXED, NonbondedEngine, QnbError
+    from q6_gb300.system import lambdas_for_window
+    nwin = args.windows
+    try:
+        e = NonbondedEngine(s, precision=PREC_MIXED, device=local, windows=nwin)
+        e.set_solvent_params(sp)
+        for w in range(nwin):
+            e.set_lambda(lambdas_for_window(lams[w], s.nstates), window=w)
+        if tuning:
+            e.set_tuning(tuning)
+        bt = synthetic_bonded(s, seed=21)
+        e.set_bonded(bt)
+        e.set_coordinates_dev(np.stack([s.x] * nwin))
+        setup = MdSetup(stepsize=1.0, temp0=300.0, tau_t=10.0, nbcycle=25, cut=dict(CUT))
+        e.md_init(setup)
+        # the generated start structure is strained (random solute tree, lattice
+        # water): Qmin-style steepest descent on the device first (untimed)
+        t_min = time.perf_counter()
+        maxf = e.md_minimize(args.md_minimize, initial_step=1e-4, force_cutoff=1.0, max_move=0.05)
+        t_min = time.perf_counter() - t_min
+        e.md_set_velocities(np.stack([maxwell_velocities(s, 300.0, 100 + w) for w in range(nwin)]))
+        e.md_prepare(stop_cm=True)
+        warm = 25
+        rec0, _, _ = e.md_run(warm, 0)
+        steps = max(50, min(4 * args.steps, 500))
+        steps -= steps % 25
+        stream = torch.cuda.ExternalStream(e.stream())
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        e.md_run(steps, warm, records=False)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        rec, _, Eb = e.md_run(1, warm + steps)
+        n = e.launches()
+        e.close()
+    except QnbError as ex:
+        return {"error": str(ex)}
+    return {"value": round(nwin * steps / (ms / 1e3), 1), "unit": "window-MD-steps/s",
+            "ms_per_step": round(ms / steps, 4), "steps": steps, "windows": nwin,
+            "list_builds": steps // 25, "bonded_terms": int(len(bt.bonds) + len(bt.angles) + len(bt.torsions) +
+                                                            len(bt.impropers)),
+            "q_bonded_terms": int(len(bt.qbonds) + len(bt.qangles) + len(bt.qtorsions) + len(bt.qimpropers)),
+            "tfree_start_end": [round(float(rec0[0]["tfree"].mean()), 2), round(float(rec[0]["tfree"].mean()), 2)],
+            "shake_iterations_per_step": round(float(rec[0]["shake_iterations"].mean()), 1),
+            "minimisation": {"steps": args.md_minimize, "max_force_after": round(float(maxf.max()), 1),
+                             "seconds": round(t_min, 2)},
+            "what": "mixed-form evaluation + bonded + leap-frog/Berendsen (tau_T 10 fs) + SHAKE + temperature, "
+                    "all windows on the device, after a steepest-descent relaxation of the generated start; timed "
+                    "with CUDA events around qnb_md_run (L2 not flushed between steps)"}
+
+
 def fp64_compare(args, s, sp, lams, local):
     """Plain FP64 form on the same workload (25 steps with one list build)."""
     import numpy as np
@@ -638,6 +705,10 @@ def main():
                     help="skip the 51-window + 16-replica graph group")
     ap.add_argument("--no-dg", dest="dg", action="store_false",
                     help="skip the mixed-vs-FP64 dG check")
+    ap.add_argument("--no-md", dest="md", action="store_false",
+                    help="skip the device-resident MD step measurement")
+    ap.add_argument("--md-minimize", type=int, default=3000,
+                    help="steepest-descent steps before the MD measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -468,6 +468,19 @@ int qnb_md_get_state(qnb_context* ctx, int32_t window, double* x, double* v);
    Required after qnb_md_init and after every qnb_md_set_velocities or
    coordinate upload before qnb_md_run. */
 int qnb_md_prepare(qnb_context* ctx, int32_t stop_cm);
+/* Qmin's steepest descent (src/minim.f90:891-935, 938-1160) on every
+   window's device coordinates: nsteps steps of pot_energy (Tfree 0), then
+   x -= d * scale with scale reset to initial_step whenever the largest atomic
+   force rose above the previous step's and grown by 1.2 otherwise; SHAKE
+   against the positions before the move; a window whose largest force is
+   below force_cutoff stops moving.  max_move > 0 (an addition to Qmin's
+   method, 0 = off) caps the largest atomic move of a step at max_move A,
+   for strained starting structures whose first moves would break SHAKE.
+   maxf (may be NULL) receives each window's largest force at the last step.
+   Lists are rebuilt every nbcycle steps.  Velocities are untouched; call
+   qnb_md_prepare before qnb_md_run. */
+int qnb_md_minimize(qnb_context* ctx, int32_t nsteps, double initial_step, double force_cutoff, double max_move,
+                    double* maxf);
 /* nsteps steps of every window starting at step number istep0 (lists are
    rebuilt where istep % nbcycle == 0, watpol updates by istep).  rec (may be
    NULL): [nsteps][nwin] records; EQ (may be NULL): [nsteps][nwin][nstates];

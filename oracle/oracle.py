@@ -283,6 +283,48 @@ class OracleMD:
         self.temperature(v)
         return x, v
 
+    def minimize(self, x, nsteps, cut, step0=1e-4, fcut=1.0, max_move=0.0):
+        """Qmin's steepest descent (src/minim.f90:891-935, 1056-1070) with
+        SHAKE against the positions before each move; returns (x, largest
+        force of the last step, potential energy per step)."""
+        x = np.ascontiguousarray(x, dtype=np.float64).copy()
+        o = self.o
+        oldmax, scale = 0.0, step0
+        epot, maxf = [], 0.0
+        for k in range(nsteps):
+            if k % self.p.nbcycle == 0:
+                o.make_pair_lists(x, **cut)
+            d = np.zeros_like(x)
+            d, E, EQ = o.pot_energy_nonbonds(x, d)
+            d, EQ = o.nonbond_qq(x, d, EQ)
+            e = sum(E.values()) + float(np.dot(self.lam, EQ.sum(1))) if self.lam is not None else sum(E.values())
+            if self.bt is not None:
+                d, Eb, EQb = o.bonded(x, self.bt, self.lam, d)
+                e += Eb.sum() + float(np.dot(self.lam, EQb.sum(1)))
+            if self.sp is not None:
+                e += o.restrain_solvent(x, d, 0.0)
+                if self.sp.wpol_restr:
+                    e += o.watpol(x, d, k, True)
+            epot.append(e)
+            maxf = float(np.sqrt((d * d).sum(1)).max())
+            rv = 1 if maxf > oldmax else 0
+            oldmax = maxf
+            if maxf < fcut:
+                rv = 2
+            if rv == 1:
+                scale = step0
+            elif rv == 0:
+                scale = scale * 1.20
+            xx = x.copy()
+            sc = 0.0 if rv == 2 else scale
+            if max_move > 0.0 and sc * maxf > max_move:
+                sc = max_move / maxf
+            if sc != 0.0:
+                x = x - d * sc
+            if self.nmol > 0:
+                self._shake(x, xx)
+        return x, maxf, np.array(epot)
+
     def step(self, x, v, istep, cut):
         o = self.o
         if istep % self.p.nbcycle == 0:

@@ -216,7 +216,9 @@ def synthetic_bonded(s, seed: int = 7, q_bonded: bool = True) -> BondedTerms:
     """Bonded terms for a generated system (q6_gb300.system.make_system): its
     solute bonds at their generated lengths, every angle and torsion of the
     bond graph, and one improper per branch atom, with seeded force
-    constants; equilibrium values at the generated geometry.  With q_bonded,
+    constants; bond lengths, angles and impropers at their generated values
+    and torsion phases that put the generated dihedrals at a minimum (the
+    Q terms get per-state offsets).  With q_bonded,
     the terms whose atoms are all Q atoms move to the Q lists with per-state
     force constants (redefining the topology terms).  Waters get harmonic
     O-H / H-H bonds and an H-O-H angle."""
@@ -235,14 +237,25 @@ def synthetic_bonded(s, seed: int = 7, q_bonded: bool = True) -> BondedTerms:
         a, b = x[i] - x[j], x[k] - x[j]
         return float(np.arccos(np.clip(a @ b / np.linalg.norm(a) / np.linalg.norm(b), -1, 1)))
 
+    def dihedral(i, j, k, l):   # torsion_calc's angle and sign convention
+        ab, bc, cd = x[i] - x[j], x[k] - x[j], x[l] - x[k]
+        c1, c2 = np.cross(ab, bc), np.cross(-bc, cd)
+        phi = float(np.arccos(np.clip(c1 @ c2 / np.linalg.norm(c1) / np.linalg.norm(c2), -1, 1)))
+        return -phi if bc @ np.cross(c1, c2) < 0 else phi
+
+    def tor_min(n, phi):   # delta putting the generated dihedral at the minimum of fk (1 + cos(n phi - delta))
+        return n * phi - np.pi
+
     bondlib = [(float(rng.uniform(300, 600)), dist(i, j)) for i, j in sb]
     bonds = [(i, j, k) for k, (i, j) in enumerate(sb)]
     anglib = [(float(rng.uniform(50, 120)), angle(i, j, k), 0.0, 0.0) for i, j, k in ang]
     angles = [(i, j, k, c) for c, (i, j, k) in enumerate(ang)]
-    torlib = [(float(rng.uniform(0.1, 2.0)), float(rng.choice([1.0, 2.0, 3.0])),
-               float(rng.choice([0.0, np.pi])), 1.0) for _ in tor]
+    torlib = []
+    for t in tor:
+        n = float(rng.choice([1.0, 2.0, 3.0]))
+        torlib.append((float(rng.uniform(0.1, 2.0)), n, tor_min(n, dihedral(*t)), 1.0))
     tors = [(i, j, k, l, c) for c, (i, j, k, l) in enumerate(tor)]
-    implib = [(float(rng.uniform(5, 20)), 0.0) for _ in imp]
+    implib = [(float(rng.uniform(5, 20)), dihedral(*t)) for t in imp]
     imps = [(i, j, k, l, c) for c, (i, j, k, l) in enumerate(imp)]
     # waters
     wb = len(bonds)
@@ -288,14 +301,14 @@ def synthetic_bonded(s, seed: int = 7, q_bonded: bool = True) -> BondedTerms:
         for t in qt:
             row = []
             for st in range(S):
-                qtl.append((float(rng.uniform(0.1, 2.0)), float(rng.choice([1.0, 2.0, 3.0])),
-                            float(rng.choice([0.0, np.pi]))))
+                n = float(rng.choice([1.0, 2.0, 3.0]))
+                qtl.append((float(rng.uniform(0.1, 2.0)), n, tor_min(n, dihedral(*t)) + float(rng.normal(0, 0.2))))
                 row.append(len(qtl) - 1)
             qtc.append(row)
         for t in qi:
             row = []
             for st in range(S):
-                qil.append((float(rng.uniform(5, 20)), float(rng.normal(0, 0.1))))
+                qil.append((float(rng.uniform(5, 20)), dihedral(*t) + float(rng.normal(0, 0.1))))
                 row.append(len(qil) - 1)
             qic.append(row)
         bt.qbonds, bt.qbond_code, bt.qbondlib = _i(qb, 2), _i(qbc, S), _f(qbl, 4)

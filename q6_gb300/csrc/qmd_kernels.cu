@@ -209,6 +209,53 @@ __global__ void __launch_bounds__(kTempBlock) k_md_stop_cm(MdDev md) {
         for (int c = 0; c < 3; ++c) v[3 * i + c] = __dsub_rn(v[3 * i + c], vcm[c]);
 }
 
+// Qmin's steepest descent step (src/minim.f90:891-935, 1056-1070), one
+// block per window: the largest atomic force; a rise above the previous
+// largest resets the scale to the initial step, otherwise it grows by 1.2;
+// below force_cutoff the window has converged and stays put.  xx keeps the
+// positions before the move (the SHAKE reference).
+__global__ void __launch_bounds__(kTempBlock) k_md_min_step(MdDev md, const DevState* __restrict__ states,
+                                                           double step0, double fcut, double max_move) {
+    const int w = blockIdx.x;
+    const size_t off = (size_t)w * 3 * md.natom;
+    double* __restrict__ x = states[w].x;
+    const double* __restrict__ d = states[w].d;
+    double* __restrict__ xx = md.xx + off;
+    MdWin& mw = md.win[w];
+    __shared__ double red[kTempBlock];
+    __shared__ double scale;
+    double mx = 0.0;
+    for (int i = threadIdx.x; i < md.natom; i += kTempBlock) {
+        const double fx = d[3 * i], fy = d[3 * i + 1], fz = d[3 * i + 2];
+        mx = fmax(mx, sqrt(fx * fx + fy * fy + fz * fz));
+    }
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int h = kTempBlock / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + h]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double maxf = red[0];
+        int rv = maxf > mw.min_oldmax ? 1 : 0;
+        mw.min_oldmax = maxf;
+        if (maxf < fcut) rv = 2;
+        if (rv == 1) mw.min_scale = step0;
+        else if (rv == 0) mw.min_scale = mw.min_scale * 1.20;
+        mw.min_state = rv;
+        mw.min_maxf = maxf;
+        double sc = rv == 2 ? 0.0 : mw.min_scale;
+        if (max_move > 0.0 && sc * maxf > max_move) sc = max_move / maxf;   // optional cap (not in Qmin)
+        scale = sc;
+    }
+    __syncthreads();
+    const double sc = scale;
+    for (int k = threadIdx.x; k < 3 * md.natom; k += kTempBlock) {
+        xx[k] = x[k];
+        if (sc != 0.0) x[k] = x[k] - d[k] * sc;
+    }
+}
+
 __global__ void k_md_record(MdDev md, int nwin, const double* __restrict__ e_all,
                             const unsigned long long* __restrict__ efix_all, double* __restrict__ rec) {
     const int w = blockIdx.x;
@@ -261,6 +308,9 @@ void launch_md_temperature(const Launch& L, const MdDev& md, const uint8_t* excl
 }
 void launch_md_stop_cm(const Launch& L, const MdDev& md) {
     k_md_stop_cm<<<L.nwin, kTempBlock, 0, L.st>>>(md);
+}
+void launch_md_min_step(const Launch& L, const MdDev& md, double step0, double fcut, double max_move) {
+    k_md_min_step<<<L.nwin, kTempBlock, 0, L.st>>>(md, L.ds, step0, fcut, max_move);
 }
 void launch_md_record(const Launch& L, const MdDev& md, const double* e_all, const unsigned long long* efix_all,
                       double* rec) {

@@ -2060,6 +2060,41 @@ int qnb_md_prepare(qnb_context* c, int32_t stop_cm) {
     return QNB_OK;
 }
 
+int qnb_md_minimize(qnb_context* c, int32_t nsteps, double initial_step, double force_cutoff, double max_move,
+                    double* maxf) {
+    TRY(md_check(c));
+    if (nsteps < 0 || !(initial_step > 0.0) || force_cutoff < 0.0 || max_move < 0.0)
+        return fail(QNB_ERR_ARG, "bad minimisation arguments");
+    CU(cudaSetDevice(c->device));
+    const qnb_md_params& p = c->mdp;
+    const int W = c->nwin;
+    CU(cudaMemsetAsync(c->md.fail, 0, sizeof(int) * W, c->stream));
+    std::vector<MdWin> mw(W);
+    CU(cudaMemcpy(mw.data(), c->md.win, sizeof(MdWin) * W, cudaMemcpyDeviceToHost));
+    for (auto& m : mw) m.min_oldmax = 0.0, m.min_scale = initial_step, m.min_state = 0;
+    CU(cudaMemcpy(c->md.win, mw.data(), sizeof(MdWin) * W, cudaMemcpyHostToDevice));
+    Cut cut{p.rcq * p.rcq, p.rclrf * p.rclrf, p.rcpp * p.rcpp, p.rcpw * p.rcpw, p.rcww * p.rcww};
+    for (int k = 0; k < nsteps; ++k) {
+        if (k % p.nbcycle == 0 || !c->lists_built) {
+            if (k > 0) TRY(md_fail_check(c));
+            TRY(build_lists(c, cut, W));
+        }
+        Launch L = c->all();
+        launch_md_clear_d(L, c->md);
+        TRY(run_compute(c, 0.0, k));
+        launch_md_min_step(L, c->md, initial_step, force_cutoff, max_move);
+        launch_md_shake(L, c->md, 0);
+        c->launches += 3;
+        TRY(check_launch());
+    }
+    TRY(md_fail_check(c));
+    CU(cudaMemcpy(mw.data(), c->md.win, sizeof(MdWin) * W, cudaMemcpyDeviceToHost));
+    if (maxf)
+        for (int w = 0; w < W; ++w) maxf[w] = mw[w].min_maxf;
+    c->md_prepared = false;
+    return QNB_OK;
+}
+
 int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* rec, qnb_qenergies* EQ,
                double* Eb) {
     TRY(md_check(c));

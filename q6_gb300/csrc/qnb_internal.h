@@ -262,6 +262,9 @@ struct MdWin {                     // per window, device
     double temp, tfree, ekin;      // last temperature()
     double tg_temp[kMaxTg], tg_tfree[kMaxTg], tg_texcl[kMaxTg];
     unsigned long long shake_iters;   // SHAKE iterations of the last step, summed over molecules
+    double min_oldmax, min_scale, min_maxf;   // steepest descent: previous largest force, scale, largest force
+    int min_state;                 // last minimisation step: 0 grown, 1 reset, 2 converged
+    int pad;
 };
 struct MdDev {
     int natom, ntg, nmol;
@@ -290,6 +293,7 @@ void launch_md_velocity(const Launch& L, const MdDev& md);
 void launch_md_copy_x(const Launch& L, const MdDev& md, int to_xx);   // xx = x (1) or the x - v dt of initial_constraint (2)
 void launch_md_temperature(const Launch& L, const MdDev& md, const uint8_t* excl);
 void launch_md_stop_cm(const Launch& L, const MdDev& md);
+void launch_md_min_step(const Launch& L, const MdDev& md, double step0, double fcut, double max_move);
 void launch_md_record(const Launch& L, const MdDev& md, const double* e_all, const unsigned long long* efix_all,
                       double* rec);
 void launch_md_clear_d(const Launch& L, const MdDev& md);   // d = 0, SHAKE count = 0

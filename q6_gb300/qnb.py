@@ -40,7 +40,7 @@ EXPORTED = (
     "qnb_group_create", "qnb_group_compute", "qnb_group_destroy", "qnb_profile_collect",
     "qnb_profile_classes", "qnb_set_solvent_internal", "qnb_autotune", "qnb_get_tuning", "qnb_set_tuning",
     "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
-    "qnb_set_bonded", "qnb_get_bonded_energies",
+    "qnb_set_bonded", "qnb_get_bonded_energies", "qnb_md_minimize",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -96,6 +96,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_md_init": [P, P, P, I32, P, P, P], "qnb_md_set_velocities": [P, I32, P],
         "qnb_md_get_state": [P, I32, P, P], "qnb_md_prepare": [P, I32], "qnb_md_run": [P, I32, I32, P, P, P],
         "qnb_set_bonded": [P, P], "qnb_get_bonded_energies": [P, P, P],
+        "qnb_md_minimize": [P, I32, D, D, D, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -315,6 +316,15 @@ class NonbondedEngine:
         v = np.zeros((self.s.natom, 3))
         self._check(self.lib.qnb_md_get_state(self.h, int(window), _p(x), _p(v)))
         return x, v
+
+    def md_minimize(self, nsteps, initial_step=1e-4, force_cutoff=1.0, max_move=0.0):
+        """Qmin-style steepest descent of every window (max_move > 0 caps
+        each step's largest atomic move); returns the largest atomic force
+        per window at the last step."""
+        maxf = np.zeros(self.nwin)
+        self._check(self.lib.qnb_md_minimize(self.h, int(nsteps), float(initial_step), float(force_cutoff),
+                                             float(max_move), _p(maxf)))
+        return maxf
 
     def md_prepare(self, stop_cm=True):
         self._check(self.lib.qnb_md_prepare(self.h, int(bool(stop_cm))))
