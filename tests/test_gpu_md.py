@@ -150,3 +150,30 @@ def test_fp64_md_with_bonded_terms_matches_oracle(system):
         assert np.allclose(eb[0][k, 0, 8:].reshape(2, 4), r["EQb"], rtol=1e-9, atol=1e-9), k
         assert abs(rec[k, 0]["temp"] - r["temp"]) <= 1e-10 * r["temp"], k
     assert np.allclose(st[0][0], x, rtol=0, atol=1e-9)
+
+
+def test_fp64_minimize_matches_oracle(system):
+    """qnb_md_minimize against the oracle's restatement of Qmin's steepest
+    descent (30 steps, move cap off and on): coordinates within 1e-9 A."""
+    from q6_gb300.bonded import synthetic_bonded
+    s = system
+    lam = [0.6, 0.4]
+    setup = dataclasses.replace(SETUP, shake_solute=False)
+    bt = synthetic_bonded(s, seed=22)
+    sp = default_solvent_params(s, itdis=4.0)
+    for cap in (0.0, 0.02):
+        with NonbondedEngine(s, precision=PREC_FP64) as e:
+            e.set_solvent_params(sp)
+            e.set_lambda(lam)
+            e.set_bonded(bt)
+            e.set_coordinates_dev(s.x[None])
+            e.md_init(setup)
+            maxf = e.md_minimize(30, initial_step=1e-4, force_cutoff=1.0, max_move=cap)
+            xd, _ = e.md_state(0)
+        o = Oracle(s)
+        o.set_solvent_params(sp)
+        cons = build_constraints(s, setup)
+        md = OracleMD(o, md_params(s, setup, cons), cons, sp=sp, lam=lam, bonded=bt)
+        xo, mfo, _ = md.minimize(s.x, 30, CUT, step0=1e-4, fcut=1.0, max_move=cap)
+        assert np.allclose(xd, xo, rtol=0, atol=1e-9), cap
+        assert abs(maxf[0] - mfo) <= 1e-6 * mfo, cap
