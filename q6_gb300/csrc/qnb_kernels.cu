@@ -2870,42 +2870,65 @@ void launch_row_sums(const Launch& L) {
     k_row_sums<<<L.nwin, kRowSumBlock, 0, L.st>>>(L.m, L.ds);
 }
 // =============================================================================
-// Bonded terms (FP64 in both forms; the mixed form sums in fixed point)
+// Bonded terms: FP64 in the plain form; FP32 arithmetic in the mixed form
+// (the reference's single-precision build, QREAL_EPS 1e-5), fixed-point sums
 // =============================================================================
+template <typename T>
 struct V3 {
-    double x, y, z;
+    T x, y, z;
 };
-__device__ __forceinline__ V3 v3(const double* x, int i) { return V3{x[3 * i], x[3 * i + 1], x[3 * i + 2]}; }
-__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ V3 operator-(V3 a) { return V3{-a.x, -a.y, -a.z}; }
-__device__ __forceinline__ V3 operator*(V3 a, double f) { return V3{a.x * f, a.y * f, a.z * f}; }
-__device__ __forceinline__ V3 operator/(V3 a, double f) { return V3{a.x / f, a.y / f, a.z / f}; }
-__device__ __forceinline__ double vdot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ V3 vcross(V3 a, V3 b) {
-    return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+template <typename T>
+__device__ __forceinline__ V3<T> operator-(V3<T> a, V3<T> b) { return V3<T>{a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <typename T>
+__device__ __forceinline__ V3<T> operator+(V3<T> a, V3<T> b) { return V3<T>{a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <typename T>
+__device__ __forceinline__ V3<T> operator-(V3<T> a) { return V3<T>{-a.x, -a.y, -a.z}; }
+template <typename T>
+__device__ __forceinline__ V3<T> operator*(V3<T> a, T f) { return V3<T>{a.x * f, a.y * f, a.z * f}; }
+template <typename T>
+__device__ __forceinline__ V3<T> operator/(V3<T> a, T f) { return V3<T>{a.x / f, a.y / f, a.z / f}; }
+template <typename T>
+__device__ __forceinline__ T vdot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename T>
+__device__ __forceinline__ V3<T> vcross(V3<T> a, V3<T> b) {
+    return V3<T>{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
-constexpr double kQrealEpsD = 1e-10;   // QREAL_EPS of the double-precision build
+// QREAL_EPS of the reference's double- and single-precision builds
+template <typename T>
+__device__ __forceinline__ constexpr T qreal_eps() { return std::is_same<T, float>::value ? T(1e-5) : T(1e-10); }
 constexpr double kPi = 3.14159265358979323846;   // 4 atan(1)
 
+// atom position: FP64 coordinates, or the mixed form's centred FP32 copy
+template <bool MIX>
+__device__ __forceinline__ V3<typename std::conditional<MIX, float, double>::type> atom_pos(const DevState& s, int i) {
+    if constexpr (MIX) {
+        float4 q = s.xq[i];
+        return V3<float>{q.x, q.y, q.z};
+    } else {
+        return V3<double>{s.x[3 * i], s.x[3 * i + 1], s.x[3 * i + 2]};
+    }
+}
+
 // angle_calc, src/bonded.f90:78-118
+template <typename T>
 struct AngleVal {
-    double angl;
-    V3 a, b, c;
+    T angl;
+    V3<T> a, b, c;
 };
-__device__ AngleVal angle_calc(V3 a, V3 b, V3 c) {
-    V3 ab = a - b, bc = c - b;
-    double ab2 = 1.0 / vdot(ab, ab), bc2 = 1.0 / vdot(bc, bc);
-    double abd = sqrt(ab2), bcd = sqrt(bc2);
-    double scalar = vdot(ab, bc) * abd * bcd;
-    scalar = fmin(1.0, fmax(-1.0, scalar));
-    AngleVal r;
+template <typename T>
+__device__ AngleVal<T> angle_calc(V3<T> a, V3<T> b, V3<T> c) {
+    V3<T> ab = a - b, bc = c - b;
+    T ab2 = T(1) / vdot(ab, ab), bc2 = T(1) / vdot(bc, bc);
+    T abd = sqrt(ab2), bcd = sqrt(bc2);
+    T scalar = vdot(ab, bc) * abd * bcd;
+    scalar = fmin(T(1), fmax(T(-1), scalar));
+    AngleVal<T> r;
     r.angl = acos(scalar);
-    double inv = sin(r.angl);
-    if (fabs(inv) < kQrealEpsD) inv = kQrealEpsD;
-    inv = -1.0 / inv;
-    V3 af = ((bc * abd * bcd) - (ab * (ab2 * scalar))) * inv;
-    V3 cf = ((ab * abd * bcd) - (bc * (bc2 * scalar))) * inv;
+    T inv = sin(r.angl);
+    if (fabs(inv) < qreal_eps<T>()) inv = qreal_eps<T>();
+    inv = T(-1) / inv;
+    V3<T> af = ((bc * abd * bcd) - (ab * (ab2 * scalar))) * inv;
+    V3<T> cf = ((ab * abd * bcd) - (bc * (bc2 * scalar))) * inv;
     r.a = af;
     r.b = af + cf;
     r.c = cf;
@@ -2913,26 +2936,28 @@ __device__ AngleVal angle_calc(V3 a, V3 b, V3 c) {
 }
 
 // torsion_calc / improper_calc (identical), src/bonded.f90:151-320
+template <typename T>
 struct TorsVal {
-    double angl;
-    V3 a, b, c, d;
+    T angl;
+    V3<T> a, b, c, d;
 };
-__device__ TorsVal torsion_calc(V3 a, V3 b, V3 c, V3 d) {
-    V3 ab = a - b, bc = c - b, cd = d - c;
-    V3 cabc = vcross(ab, bc), cbcd = vcross(-bc, cd);
-    double a2abc = vdot(cabc, cabc), a2bcd = vdot(cbcd, cbcd);
-    double aabc = sqrt(a2abc), abcd = sqrt(a2bcd);
-    double scalar = vdot(cabc, cbcd) / (aabc * abcd);
-    scalar = fmin(1.0, fmax(-1.0, scalar));
-    TorsVal r;
+template <typename T>
+__device__ TorsVal<T> torsion_calc(V3<T> a, V3<T> b, V3<T> c, V3<T> d) {
+    V3<T> ab = a - b, bc = c - b, cd = d - c;
+    V3<T> cabc = vcross(ab, bc), cbcd = vcross(-bc, cd);
+    T a2abc = vdot(cabc, cabc), a2bcd = vdot(cbcd, cbcd);
+    T aabc = sqrt(a2abc), abcd = sqrt(a2bcd);
+    T scalar = vdot(cabc, cbcd) / (aabc * abcd);
+    scalar = fmin(T(1), fmax(T(-1), scalar));
+    TorsVal<T> r;
     r.angl = acos(scalar);
-    if (vdot(bc, vcross(cabc, cbcd)) < 0.0) r.angl = -r.angl;
-    double inv = sin(r.angl);
-    if (fabs(inv) < kQrealEpsD) inv = kQrealEpsD;
-    inv = -1.0 / inv;
-    V3 v1 = ((cbcd / (aabc * abcd)) - ((cabc / a2abc) * scalar)) * inv;
-    V3 v2 = ((cabc / (aabc * abcd)) - ((cbcd / a2bcd) * scalar)) * inv;
-    V3 ca = ab - bc, db = -bc - cd;
+    if (vdot(bc, vcross(cabc, cbcd)) < T(0)) r.angl = -r.angl;
+    T inv = sin(r.angl);
+    if (fabs(inv) < qreal_eps<T>()) inv = qreal_eps<T>();
+    inv = T(-1) / inv;
+    V3<T> v1 = ((cbcd / (aabc * abcd)) - ((cabc / a2abc) * scalar)) * inv;
+    V3<T> v2 = ((cabc / (aabc * abcd)) - ((cbcd / a2bcd) * scalar)) * inv;
+    V3<T> ca = ab - bc, db = -bc - cd;
     r.a = vcross(bc, v1);
     r.b = vcross(ca, v1) + vcross(cd, v2);
     r.c = vcross(db, v2) - vcross(ab, v1);
@@ -2940,39 +2965,56 @@ __device__ TorsVal torsion_calc(V3 a, V3 b, V3 c, V3 d) {
     return r;
 }
 
+constexpr int kBondedSlots = 8 + 4 * kMaxStates;   // E_B0 .. qb_slot(kMaxStates - 1, 3)
+constexpr int kBondedBlock = 128;
+
 template <bool MIX>
 struct BondedSink {
+    typedef typename std::conditional<MIX, float, double>::type T;
+    typedef typename std::conditional<MIX, unsigned long long, double>::type ET;
     Acc<MIX> acc;
-    __device__ __forceinline__ void grad(int i, V3 g) const {
-        if constexpr (MIX) acc.gradd(i, g.x, g.y, g.z);
+    ET* red;   // shared per-block energy sums, slot - E_B0
+    __device__ __forceinline__ void grad(int i, V3<T> g) const {
+        if constexpr (MIX) acc.grad_alu(i, g.x, g.y, g.z);
         else acc.grad(i, g.x, g.y, g.z);
     }
-    __device__ __forceinline__ void energy(int slot, double e) const {
-        if constexpr (MIX) acc.energy_fix(slot, to_fixd(e));
-        else acc.energy(slot, e);
+    __device__ __forceinline__ void energy(int slot, T e) const {
+        if constexpr (MIX) atomicAdd(red + (slot - E_B0), to_fix_alu(e));
+        else atomicAdd(red + (slot - E_B0), e);
     }
 };
 
 // One thread per term: classical bonds, angles (+ Urey-Bradley), torsions,
-// impropers; then Q bonds, angles, torsions, impropers per state.
+// impropers; then Q bonds, angles, torsions, impropers per state.  Energies
+// are summed per block in shared memory and added once per block and slot.
 template <bool MIX>
-__global__ void __launch_bounds__(128) k_bonded(DevModel m, const DevState* __restrict__ states, BondedDev b) {
+__global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevState* __restrict__ states, BondedDev b) {
+    typedef typename std::conditional<MIX, float, double>::type T;
+    typedef typename BondedSink<MIX>::ET ET;
+    __shared__ ET red[kBondedSlots];
     const DevState& s = states[blockIdx.y];
-    const BondedSink<MIX> out{make_acc<MIX>(s)};
-    const double* __restrict__ x = s.x;
+    for (int k = threadIdx.x; k < kBondedSlots; k += blockDim.x) red[k] = ET(0);
+    __syncthreads();
+    const BondedSink<MIX> out{make_acc<MIX>(s), red};
     const int S = m.S;
-    const double two_pi = 2.0 * kPi;
+    const T two_pi = T(2.0 * kPi);
+    auto lam = [&](int st) -> T {
+        if constexpr (MIX) return s.lambdaf[st];
+        else return s.lambda[st];
+    };
+    auto P = [&](int i) { return atom_pos<MIX>(s, i); };
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < b.nterms; t += gridDim.x * blockDim.x) {
         int u = t;
         if (u < b.nb) {   // bond, src/bondene.f90:182-245
             int4 e = b.bonds[u];
             if (e.z < 0) continue;
             double2 lib = b.bondlib[e.z];
-            V3 av = v3(x, e.y) - v3(x, e.x);
-            double dist = sqrt(vdot(av, av));
-            double db = dist - lib.y;
-            out.energy(E_B0 + (u < b.nb_sol ? 0 : 4), 0.5 * lib.x * db * db);
-            double dv = lib.x * db / dist;
+            const T fk = (T)lib.x, b0 = (T)lib.y;
+            V3<T> av = P(e.y) - P(e.x);
+            T dist = sqrt(vdot(av, av));
+            T db = dist - b0;
+            out.energy(E_B0 + (u < b.nb_sol ? 0 : 4), T(0.5) * fk * db * db);
+            T dv = fk * db / dist;
             out.grad(e.x, -(av * dv));
             out.grad(e.y, av * dv);
             continue;
@@ -2982,22 +3024,23 @@ __global__ void __launch_bounds__(128) k_bonded(DevModel m, const DevState* __re
             int4 e = b.angles[u];
             if (e.w < 0) continue;
             double4 lib = b.anglib[e.w];
+            const T fk = (T)lib.x, th0 = (T)lib.y, ufk = (T)lib.z, ur0 = (T)lib.w;
             const int slot = E_B0 + (u < b.na_sol ? 1 : 5);
-            AngleVal c = angle_calc(v3(x, e.x), v3(x, e.y), v3(x, e.z));
-            double da = c.angl - lib.y;
-            double ea = 0.5 * lib.x * da * da;
-            double dv = lib.x * da;
+            AngleVal<T> c = angle_calc(P(e.x), P(e.y), P(e.z));
+            T da = c.angl - th0;
+            T ea = T(0.5) * fk * da * da;
+            T dv = fk * da;
             out.grad(e.x, c.a * dv);
             out.grad(e.y, -(c.b * dv));
             out.grad(e.z, c.c * dv);
-            if (b.urey && lib.z > 0.0) {
+            if (b.urey && ufk > T(0)) {
                 // the reference's solute/solvent Urey-Bradley adds the gradient
                 // with these signs (d(k) -= a du, d(i) += a du)
-                V3 av = v3(x, e.z) - v3(x, e.x);
-                double dist = sqrt(vdot(av, av));
-                double ru = dist - lib.w;
-                ea += lib.z * ru * ru;
-                double du = 2.0 * lib.z * ru / dist;
+                V3<T> av = P(e.z) - P(e.x);
+                T dist = sqrt(vdot(av, av));
+                T ru = dist - ur0;
+                ea += ufk * ru * ru;
+                T du = T(2) * ufk * ru / dist;
                 out.grad(e.z, -(av * du));
                 out.grad(e.x, av * du);
             }
@@ -3009,10 +3052,11 @@ __global__ void __launch_bounds__(128) k_bonded(DevModel m, const DevState* __re
             const int* e = b.tors + 5 * u;
             if (e[4] < 0) continue;
             double4 lib = b.torlib[e[4]];
-            TorsVal c = torsion_calc(v3(x, e[0]), v3(x, e[1]), v3(x, e[2]), v3(x, e[3]));
-            double arg = lib.y * c.angl - lib.z;
-            out.energy(E_B0 + (u < b.nt_sol ? 2 : 6), lib.x * (1.0 + cos(arg)) * lib.w);
-            double dv = -lib.y * lib.x * sin(arg) * lib.w;
+            const T fk = (T)lib.x, rm = (T)lib.y, dl = (T)lib.z, ip = (T)lib.w;
+            TorsVal<T> c = torsion_calc(P(e[0]), P(e[1]), P(e[2]), P(e[3]));
+            T arg = rm * c.angl - dl;
+            out.energy(E_B0 + (u < b.nt_sol ? 2 : 6), fk * (T(1) + cos(arg)) * ip);
+            T dv = -rm * fk * sin(arg) * ip;
             out.grad(e[0], c.a * dv);
             out.grad(e[1], c.b * dv);
             out.grad(e[2], c.c * dv);
@@ -3024,17 +3068,18 @@ __global__ void __launch_bounds__(128) k_bonded(DevModel m, const DevState* __re
             const int* e = b.imps + 5 * u;
             if (e[4] < 0) continue;
             double2 lib = b.implib[e[4]];
-            TorsVal c = torsion_calc(v3(x, e[0]), v3(x, e[1]), v3(x, e[2]), v3(x, e[3]));
-            double ei, dv;
+            const T fk = (T)lib.x, p0 = (T)lib.y;
+            TorsVal<T> c = torsion_calc(P(e[0]), P(e[1]), P(e[2]), P(e[3]));
+            T ei, dv;
             if (b.imp_type == 2) {
-                double arg = 2.0 * c.angl - lib.y;
-                ei = lib.x * (1.0 + cos(arg));
-                dv = -2.0 * lib.x * sin(arg);
+                T arg = T(2) * c.angl - p0;
+                ei = fk * (T(1) + cos(arg));
+                dv = T(-2) * fk * sin(arg);
             } else {
-                double arg = c.angl - lib.y;
+                T arg = c.angl - p0;
                 arg = arg - two_pi * round(arg / two_pi);
-                dv = lib.x * arg;
-                ei = 0.5 * dv * arg;
+                dv = fk * arg;
+                ei = T(0.5) * dv * arg;
             }
             out.energy(E_B0 + (u < b.ni_sol ? 3 : 7), ei);
             out.grad(e[0], c.a * dv);
@@ -3050,12 +3095,13 @@ __global__ void __launch_bounds__(128) k_bonded(DevModel m, const DevState* __re
             if (code < 0) continue;
             int2 e = b.qbonds[q];
             double4 lib = b.qbondlib[code];   // Dmz amz r0 fk
-            V3 av = v3(x, e.y) - v3(x, e.x);
-            double dist = sqrt(vdot(av, av));
-            double db = dist - lib.z;
-            double fexp = exp(-lib.y * db);
-            out.energy(qb_slot(st, 0), lib.x * (fexp * fexp - 2.0 * fexp) + 0.5 * lib.w * db * db);
-            double dv = (2.0 * lib.x * lib.y * (fexp - fexp * fexp) + lib.w * db) * s.lambda[st] / dist;
+            const T Dmz = (T)lib.x, amz = (T)lib.y, r0 = (T)lib.z, fk = (T)lib.w;
+            V3<T> av = P(e.y) - P(e.x);
+            T dist = sqrt(vdot(av, av));
+            T db = dist - r0;
+            T fexp = exp(-amz * db);
+            out.energy(qb_slot(st, 0), Dmz * (fexp * fexp - T(2) * fexp) + T(0.5) * fk * db * db);
+            T dv = (T(2) * Dmz * amz * (fexp - fexp * fexp) + fk * db) * lam(st) / dist;
             out.grad(e.x, -(av * dv));
             out.grad(e.y, av * dv);
             continue;
@@ -3066,20 +3112,21 @@ __global__ void __launch_bounds__(128) k_bonded(DevModel m, const DevState* __re
             if (code < 0) continue;
             int4 e = b.qangles[q];
             double4 lib = b.qanglib[code];
-            const double lam = s.lambda[st];
-            AngleVal c = angle_calc(v3(x, e.x), v3(x, e.y), v3(x, e.z));
-            double da = c.angl - lib.y;
-            double ea = 0.5 * lib.x * da * da;
-            double dv = lib.x * da * lam;
+            const T fk = (T)lib.x, th0 = (T)lib.y, ufk = (T)lib.z, ur0 = (T)lib.w;
+            const T l = lam(st);
+            AngleVal<T> c = angle_calc(P(e.x), P(e.y), P(e.z));
+            T da = c.angl - th0;
+            T ea = T(0.5) * fk * da * da;
+            T dv = fk * da * l;
             out.grad(e.x, c.a * dv);
             out.grad(e.y, -(c.b * dv));
             out.grad(e.z, c.c * dv);
-            if (b.urey && lib.z != 0.0) {
-                V3 av = v3(x, e.z) - v3(x, e.x);
-                double dist = sqrt(vdot(av, av));
-                double ru = dist - lib.w;
-                ea += lib.z * ru * ru;
-                double du = 2.0 * (lib.z * ru / dist) * lam;
+            if (b.urey && ufk != T(0)) {
+                V3<T> av = P(e.z) - P(e.x);
+                T dist = sqrt(vdot(av, av));
+                T ru = dist - ur0;
+                ea += ufk * ru * ru;
+                T du = T(2) * (ufk * ru / dist) * l;
                 out.grad(e.x, -(av * du));
                 out.grad(e.z, av * du);
             }
@@ -3092,10 +3139,11 @@ __global__ void __launch_bounds__(128) k_bonded(DevModel m, const DevState* __re
             if (code < 0) continue;
             int4 e = b.qtors[q];
             double4 lib = b.qtorlib[code];
-            TorsVal c = torsion_calc(v3(x, e.x), v3(x, e.y), v3(x, e.z), v3(x, e.w));
-            double arg = lib.y * c.angl - lib.z;
-            out.energy(qb_slot(st, 2), lib.x * (1.0 + cos(arg)));
-            double dv = -lib.y * lib.x * sin(arg) * s.lambda[st];
+            const T fk = (T)lib.x, rm = (T)lib.y, dl = (T)lib.z;
+            TorsVal<T> c = torsion_calc(P(e.x), P(e.y), P(e.z), P(e.w));
+            T arg = rm * c.angl - dl;
+            out.energy(qb_slot(st, 2), fk * (T(1) + cos(arg)));
+            T dv = -rm * fk * sin(arg) * lam(st);
             out.grad(e.x, c.a * dv);
             out.grad(e.y, c.b * dv);
             out.grad(e.z, c.c * dv);
@@ -3108,26 +3156,35 @@ __global__ void __launch_bounds__(128) k_bonded(DevModel m, const DevState* __re
             if (code < 0) continue;
             int4 e = b.qimps[q];
             double2 lib = b.qimplib[code];
-            TorsVal c = torsion_calc(v3(x, e.x), v3(x, e.y), v3(x, e.z), v3(x, e.w));
-            double arg = c.angl - lib.y;
+            const T fk = (T)lib.x, p0 = (T)lib.y;
+            TorsVal<T> c = torsion_calc(P(e.x), P(e.y), P(e.z), P(e.w));
+            T arg = c.angl - p0;
             arg = arg - two_pi * round(arg / two_pi);
-            double dv = lib.x * arg;
-            out.energy(qb_slot(st, 3), 0.5 * dv * arg);
-            dv = dv * s.lambda[st];
+            T dv = fk * arg;
+            out.energy(qb_slot(st, 3), T(0.5) * dv * arg);
+            dv = dv * lam(st);
             out.grad(e.x, c.a * dv);
             out.grad(e.y, c.b * dv);
             out.grad(e.z, c.c * dv);
             out.grad(e.w, c.d * dv);
         }
     }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kBondedSlots; k += blockDim.x) {
+        ET v = red[k];
+        if (v != ET(0)) {
+            if constexpr (MIX) out.acc.energy_fix(E_B0 + k, v);
+            else out.acc.energy(E_B0 + k, v);
+        }
+    }
 }
 
 void launch_bonded(const Launch& L, const BondedDev& b, int mixed) {
     if (b.nterms == 0) return;
-    int blocks = std::min(256, (b.nterms + 127) / 128);
+    int blocks = std::min(512, (b.nterms + kBondedBlock - 1) / kBondedBlock);
     dim3 g(blocks, L.nwin);
-    if (mixed) k_bonded<true><<<g, 128, 0, L.st>>>(L.m, L.ds, b);
-    else k_bonded<false><<<g, 128, 0, L.st>>>(L.m, L.ds, b);
+    if (mixed) k_bonded<true><<<g, kBondedBlock, 0, L.st>>>(L.m, L.ds, b);
+    else k_bonded<false><<<g, kBondedBlock, 0, L.st>>>(L.m, L.ds, b);
 }
 
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,

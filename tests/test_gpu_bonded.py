@@ -3,8 +3,8 @@
 lig_w: the reference's step-0 bonded columns (solute bond, angle, torsion,
 improper; Q-atom bond, angle, torsion, improper) reproduced on the device in
 both forms, and every energy and the gradient within 1e-9 (FP64 form) /
-1e-7 relative (mixed form: FP64 terms summed in 2^-32 fixed point) of the
-oracle.  A generated system with Q bonded terms in two states (Morse and
+2e-5 relative (mixed form: FP32 arithmetic per term, as the reference's
+single-precision build, summed in 2^-32 fixed point) of the oracle.  A generated system with Q bonded terms in two states (Morse and
 harmonic Q bonds): batched windows bit-equal to single contexts (mixed), and
 the FP64 form against the oracle with both improper forms."""
 import numpy as np
@@ -49,9 +49,10 @@ def test_lig_w_bonded_on_gpu(prec):
     o = Oracle(s)
     d0, _, _, _ = o.evaluate(x, [1.0], cut=CUT)
     d0, Eb0, EQb0 = o.bonded(x, bt, [1.0], d0)
-    tol = 1e-9 if prec == PREC_FP64 else 1e-7
-    assert np.allclose(Eb[0], Eb0, rtol=tol, atol=tol)
-    assert np.allclose(EQb[0], EQb0, rtol=tol, atol=tol)
+    # mixed form: FP32 arithmetic per term (the reference's single-precision build)
+    rtol, atol = (1e-9, 1e-9) if prec == PREC_FP64 else (2e-5, 2e-4)
+    assert np.allclose(Eb[0], Eb0, rtol=rtol, atol=atol)
+    assert np.allclose(EQb[0], EQb0, rtol=rtol, atol=atol)
     scale = np.maximum(np.abs(d0), np.median(np.abs(d0)))
     gtol = 1e-6 if prec == PREC_FP64 else 2e-3   # the nonbonded part dominates the mixed-form bar
     assert np.all(np.abs(D[0] - d0) <= gtol * scale + 1e-9)
