@@ -411,6 +411,18 @@ typedef struct qnb_bonded {
 int qnb_set_bonded(qnb_context* ctx, const qnb_bonded* b);
 int qnb_get_bonded_energies(qnb_context* ctx, double* Eb, double* EQb);
 
+/* fix_shell (src/potene.f90:386-423), evaluated inside qnb_compute_dev and
+   qnb_md_run once set: excluded atoms (the topology's excl flags) with
+   fk_fix and shell atoms (shell[i] != 0, as make_shell / make_shell2 mark
+   them, src/topo.f90:1426-1491) with fk_pshell are restrained harmonically
+   to xtop (natom x 3): E = 0.5 fk |x - xtop|^2 into E%restraint%fix / %shell.
+   xtop = NULL removes the restraint.  The freeze option is not supported. */
+int qnb_set_shell_restraint(qnb_context* ctx, const double* xtop, const uint8_t* shell, double fk_fix,
+                            double fk_pshell);
+/* Restraint energies of the last evaluation, Er[4w..4w+3] = fix, shell,
+   solvent_radial, water_pol of window w. */
+int qnb_get_restraint_energies(qnb_context* ctx, double* Er);
+
 /* ---- device-resident MD step (FP64) ----------------------------------------
    qdyn's leap-frog step for the spherical boundary with the Berendsen
    thermostat (md_run, src/md.f90:1687-1812), every window of the context on
@@ -451,6 +463,7 @@ typedef struct qnb_md_record {
     qnb_energies E;
     double solvent_radial, water_pol;
     double ekin, temp, tfree, shake_iterations;
+    double fix, shell;        /* E%restraint%fix, %shell (qnb_set_shell_restraint) */
 } qnb_md_record;
 
 /* mass[natom] (amu); the constraints of molecule m are

@@ -64,6 +64,7 @@ def lib():
         L.orc_md_stop_cm.argtypes = [I, P, P]
         L.orc_md_temperature.argtypes = [I, P, P, P, I, P, P, P, P, D, D, D, D, D, D, P, P]
         L.orc_bonded.argtypes = [P, P, P, I, P, P, P]
+        L.orc_fix_shell.argtypes = [I, P, P, P, P, P, D, D, P]
         L.orc_static_qq_size.restype = ctypes.c_long
         L.orc_static_qq_size.argtypes = [P, I, I]
         _lib = L
@@ -178,6 +179,19 @@ class Oracle:
         lib().orc_bonded(_p(x), _p(d), ctypes.byref(st), self.S, _p(lam), _p(Eb), _p(EQb))
         return d, Eb, EQb[: self.S]
 
+    def fix_shell(self, x, xtop, shell, fk_fix, fk_pshell, d=None):
+        """fix_shell: returns (d, [E_fix, E_shell])."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if d is None:
+            d = np.zeros_like(x)
+        E = np.zeros(2)
+        excl = np.ascontiguousarray(self.s.excl, dtype=np.uint8)
+        sh = np.ascontiguousarray(shell, dtype=np.uint8)
+        xt = np.ascontiguousarray(xtop, dtype=np.float64)
+        lib().orc_fix_shell(self.s.natom, _p(x), _p(d), _p(xt), _p(excl), _p(sh), float(fk_fix), float(fk_pshell),
+                            _p(E))
+        return d, E
+
     def evaluate(self, x, lam, cut=None, solvent=None, Tfree=300.0, istep=0, lists=True):
         """One full nonbonded evaluation in the reference's call order."""
         cut = cut or {}
@@ -228,9 +242,10 @@ class OracleMD:
     BOLTZ = 0.001986
     MAGIC = 0.020462
 
-    def __init__(self, oracle: Oracle, p, cons, sp=None, lam=None, bonded=None):
+    def __init__(self, oracle: Oracle, p, cons, sp=None, lam=None, bonded=None, shell=None):
         self.o, self.p, self.cons, self.sp = oracle, p, cons, sp
         self.bt = bonded
+        self.shell = shell   # (xtop, flags, fk_fix, fk_pshell) or None
         self.lam = None if lam is None else np.asarray(lam, dtype=np.float64)
         s = oracle.s
         self.n = s.natom
@@ -336,6 +351,9 @@ class OracleMD:
         Eb = EQb = None
         if self.bt is not None:
             d, Eb, EQb = o.bonded(x, self.bt, self.lam, d)
+        efs = [0.0, 0.0]
+        if self.shell is not None:
+            d, efs = o.fix_shell(x, *self.shell, d=d)
         if self.sp is not None:
             erst[0] = o.restrain_solvent(x, d, self.tfree)
             if self.sp.wpol_restr:
@@ -348,5 +366,5 @@ class OracleMD:
             iters = self._shake(x, xx)
             lib().orc_md_velocity(self.n, _p(x), _p(xx), _p(v), self.dt)
         t = self.temperature(v)
-        return dict(E=E, EQ=EQ, erst=erst, Eb=Eb, EQb=EQb, ekin=t[0], temp=t[1], tfree=t[2],
+        return dict(E=E, EQ=EQ, erst=erst, Eb=Eb, EQb=EQb, fix_shell=efs, ekin=t[0], temp=t[1], tfree=t[2],
                     shake_iterations=iters)

@@ -1575,3 +1575,18 @@ void orc_bonded(const double* x, double* d, const qnb_bonded* b, int S, const do
         }
     }
 }
+
+/* fix_shell, src/potene.f90:386-423: E[0] += fix, E[1] += shell */
+void orc_fix_shell(int natom, const double* x, double* d, const double* xtop, const uint8_t* excl,
+                   const uint8_t* shell, double fk_fix, double fk_pshell, double* E) {
+    for (int i = 0; i < natom; ++i) {
+        if (!excl[i] && !shell[i]) continue;
+        double fk = excl[i] ? fk_fix : fk_pshell;
+        v3 vec = vsub(X(x, i), X(xtop, i));
+        double r2 = vsq(vec);
+        double erst = 0.5 * fk * r2;
+        if (excl[i]) E[0] += erst;
+        if (shell[i]) E[1] += erst;
+        gadd(d, i, vscale(vec, fk));
+    }
+}

@@ -141,6 +141,11 @@ struct qnb_context {
     double* h_stage = nullptr;   // pinned staging for x / d (natom*3)
     double* h_e = nullptr;       // pinned energies (nwin x (kNumE doubles + kNumE fixed))
 
+    // fix_shell (qnb_set_shell_restraint)
+    bool have_shell = false;
+    uint8_t* d_shell_flags = nullptr;
+    double* d_xtop = nullptr;
+    double fk_fix = 0.0, fk_pshell = 0.0;
     // bonded terms (qnb_set_bonded)
     bool have_bonded = false;
     BondedDev bonded{};
@@ -1443,6 +1448,10 @@ int enqueue_compute(qnb_context* c, double Tfree, int istep) {
         timed(c, K_BONDED, [&] { launch_bonded(L, c->bonded, c->mixed); });
         c->launches++;
     }
+    if (c->have_shell) {
+        timed(c, K_RESTRAIN, [&] { launch_fix_shell(L, c->d_shell_flags, c->d_xtop, c->fk_fix, c->fk_pshell, c->mixed); });
+        c->launches++;
+    }
     if (c->have_solv) {
         timed(c, K_RESTRAIN, [&] { launch_restrain_solvent(L, c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv); });
         c->launches++;
@@ -2144,6 +2153,8 @@ int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* re
                         add_energies(e, &o.E, nullptr, c->S);
                         o.solvent_radial = e[E_RST_RAD];
                         o.water_pol = e[E_RST_POL];
+                        o.fix = e[E_RST_FIX];
+                        o.shell = e[E_RST_SHELL];
                         o.ekin = r[2 * kNumE];
                         o.temp = r[2 * kNumE + 1];
                         o.tfree = r[2 * kNumE + 2];
@@ -2296,6 +2307,53 @@ int qnb_get_bonded_energies(qnb_context* c, double* Eb, double* EQb) {
             for (int k = 0; k < 8; ++k) Eb[8 * w + k] = t[k];
         if (EQb)
             for (int k = 0; k < 4 * c->S; ++k) EQb[(size_t)w * 4 * c->S + k] = t[8 + k];
+    }
+    return QNB_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int qnb_set_shell_restraint(qnb_context* c, const double* xtop, const uint8_t* shell, double fk_fix, double fk_pshell) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    if (c->d_shell_flags) c->release(c->d_shell_flags), c->d_shell_flags = nullptr;
+    if (c->d_xtop) c->release(c->d_xtop), c->d_xtop = nullptr;
+    c->have_shell = false;
+    ++c->epoch;
+    if (!xtop) return QNB_OK;   // removes the restraint
+    if (!shell) return fail(QNB_ERR_ARG, "null shell flags");
+    if (!(fk_fix >= 0.0) || !(fk_pshell >= 0.0)) return fail(QNB_ERR_ARG, "negative force constant");
+    std::vector<uint8_t> excl(c->natom);
+    CU(cudaMemcpy(excl.data(), c->m.excl, c->natom, cudaMemcpyDeviceToHost));
+    std::vector<uint8_t> flags(c->natom);
+    int any = 0;
+    for (int i = 0; i < c->natom; ++i) {
+        flags[i] = (uint8_t)((excl[i] ? 1u : 0u) | (shell[i] ? 2u : 0u));
+        any |= flags[i];
+    }
+    std::vector<double> xt(xtop, xtop + 3 * (size_t)c->natom);
+    TRY(c->upload(&c->d_shell_flags, flags));
+    TRY(c->upload(&c->d_xtop, xt));
+    c->fk_fix = fk_fix;
+    c->fk_pshell = fk_pshell;
+    c->have_shell = any != 0;
+    return QNB_OK;
+}
+
+int qnb_get_restraint_energies(qnb_context* c, double* Er) {
+    if (!c || !Er) return fail(QNB_ERR_ARG, "null argument");
+    CU(cudaSetDevice(c->device));
+    std::vector<double> e((size_t)kNumE * c->nwin);
+    TRY(read_energies(c, c->nwin, e.data()));
+    for (int w = 0; w < c->nwin; ++w) {
+        const double* ew = e.data() + (size_t)w * kNumE;
+        Er[4 * w] = ew[E_RST_FIX];
+        Er[4 * w + 1] = ew[E_RST_SHELL];
+        Er[4 * w + 2] = ew[E_RST_RAD];
+        Er[4 * w + 3] = ew[E_RST_POL];
     }
     return QNB_OK;
 }

@@ -19,7 +19,7 @@ constexpr float kFixF = 4294967296.0f;
 // energy slots (doubles in FP64 mode, 2^-32 fixed point in mixed mode)
 enum {
     E_PP_EL = 0, E_PP_VDW, E_PW_EL, E_PW_VDW, E_WW_EL, E_WW_VDW, E_LRF,
-    E_RST_RAD, E_RST_POL, E_Q0
+    E_RST_RAD, E_RST_POL, E_RST_FIX, E_RST_SHELL, E_Q0
 };
 __host__ __device__ constexpr int eq_slot(int s, int k) { return E_Q0 + 6 * s + k; }
 // bonded: solute bond, angle, torsion, improper, then the same for solvent;
@@ -253,6 +253,9 @@ struct BondedDev {
     int nterms;             // classical terms + Q terms x states
 };
 void launch_bonded(const Launch& L, const BondedDev& b, int mixed);
+// fix_shell: flag bit 0 excluded (fk_fix), bit 1 shell (fk_pshell); xtop [natom*3]
+void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop, double fk_fix, double fk_pshell,
+                      int mixed);
 
 // ---- device-resident MD step (FP64) ----------------------------------------
 constexpr int kMaxTg = 4;          // temperature coupling groups

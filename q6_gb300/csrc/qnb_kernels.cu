@@ -3187,6 +3187,34 @@ void launch_bonded(const Launch& L, const BondedDev& b, int mixed) {
     else k_bonded<false><<<g, kBondedBlock, 0, L.st>>>(L.m, L.ds, b);
 }
 
+// fix_shell, src/potene.f90:386-423: excluded atoms (fk_fix) and shell atoms
+// (fk_pshell) restrained to their topology positions, FP64 in both forms
+template <bool MIX>
+__global__ void k_fix_shell(DevModel m, const DevState* __restrict__ states, const uint8_t* __restrict__ flags,
+                            const double* __restrict__ xtop, double fk_fix, double fk_pshell) {
+    const DevState& s = states[blockIdx.y];
+    Acc<MIX> acc = make_acc<MIX>(s);
+    ESum<MIX> efix, eshell;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.natom; i += gridDim.x * blockDim.x) {
+        const unsigned f = flags[i];
+        if (!f) continue;
+        const double fk = (f & 1u) ? fk_fix : fk_pshell;
+        double vx = s.x[3 * i] - xtop[3 * i], vy = s.x[3 * i + 1] - xtop[3 * i + 1], vz = s.x[3 * i + 2] - xtop[3 * i + 2];
+        double erst = 0.5 * fk * (vx * vx + vy * vy + vz * vz);
+        if (f & 1u) efix.add(erst);
+        if (f & 2u) eshell.add(erst);
+        if constexpr (MIX) acc.gradd(i, vx * fk, vy * fk, vz * fk);
+        else acc.grad(i, vx * fk, vy * fk, vz * fk);
+    }
+    efix.flush(acc, E_RST_FIX);
+    eshell.flush(acc, E_RST_SHELL);
+}
+void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop, double fk_fix, double fk_pshell,
+                      int mixed) {
+    dim3 g = grid_for(L.m.natom, 64, 8, L.nwin);
+    if (mixed) k_fix_shell<true><<<g, 64, 0, L.st>>>(L.m, L.ds, flags, xtop, fk_fix, fk_pshell);
+    else k_fix_shell<false><<<g, 64, 0, L.st>>>(L.m, L.ds, flags, xtop, fk_fix, fk_pshell);
+}
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv) {
     if (L.m.nwat == 0) return;

@@ -39,7 +39,8 @@ class QnbMdParams(ctypes.Structure):
 
 # qnb_md_record
 MD_RECORD = np.dtype([("E", "<f8", 7), ("solvent_radial", "<f8"), ("water_pol", "<f8"), ("ekin", "<f8"),
-                      ("temp", "<f8"), ("tfree", "<f8"), ("shake_iterations", "<f8")])
+                      ("temp", "<f8"), ("tfree", "<f8"), ("shake_iterations", "<f8"), ("fix", "<f8"),
+                      ("shell", "<f8")])
 
 
 @dataclass
@@ -51,8 +52,8 @@ class MdSetup:
     nbcycle: int = 25
     shake_solvent: bool = True
     shake_solute: bool = False
-    shake_hydrogens: bool = True    # with shake_solute: bonds to hydrogens
-    shake_heavy: bool = True        # with shake_solute: heavy-atom bonds
+    shake_hydrogens: bool = True    # bonds to hydrogens (qdyn's default on)
+    shake_heavy: bool = False       # heavy-atom bonds (qdyn's default off)
     cut: dict = field(default_factory=lambda: dict(Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0))
 
 
@@ -122,13 +123,16 @@ def build_constraints(s, setup: MdSetup) -> Constraints:
                     dist.append(d)
                 starts.append(len(ij))
     if setup.shake_solvent and s.nwat:
-        wb = water_bonds(s)
+        hv = np.asarray(s.mass)[np.asarray(s.iac)[s.nat_solute:s.nat_solute + s.solv_atom]] >= 4.0
+        wb = [(a, b, d) for a, b, d in water_bonds(s)
+              if (setup.shake_hydrogens if (not hv[a] or not hv[b]) else setup.shake_heavy)]
         for w in range(s.nwat):
             o = s.nat_solute + s.solv_atom * w
             for a, b, d in wb:
                 ij.append((o + a, o + b))
                 dist.append(d)
-            starts.append(len(ij))
+            if wb:
+                starts.append(len(ij))
     return Constraints(np.array(starts, np.int32), np.array(ij, np.int32).reshape(-1, 2),
                        np.array(dist, np.float64), np.zeros(MAX_TGROUPS))
 
@@ -190,3 +194,28 @@ def maxwell_velocities(s, temperature: float, seed: int):
     rng = np.random.default_rng(seed)
     m = s.mass[s.iac]
     return rng.normal(0.0, 1.0, (s.natom, 3)) * np.sqrt(BOLTZ * temperature / m)[:, None]
+
+
+def make_shell(s, rexcl_i: float, xtop=None):
+    """Shell atoms of fix_shell as make_shell (switch atoms, src/topo.f90:1426-1449)
+    or make_shell2 (group centres, 1455-1491) mark them: every atom of a solute
+    charge group whose (non-excluded, heavy) switch atom, or whose centre in
+    any-atom mode, lies beyond rexcl_i of xpcent in the topology coordinates.
+    rexcl_i <= 1 is a fraction of rexcl_o (src/simprep.f90:2670-2672)."""
+    xt = np.asarray(s.x if xtop is None else xtop, dtype=np.float64)
+    r = float(rexcl_i)
+    if r <= 1.0:
+        r = r * float(s.rexcl_o)
+    rin2 = r * r
+    shell = np.zeros(s.natom, np.uint8)
+    excl = np.asarray(s.excl).astype(bool)
+    heavy = np.asarray(s.heavy).astype(bool)
+    for g in range(s.ncgp_solute):
+        sw = int(s.cgp_iswitch[g])
+        if excl[sw] or not heavy[sw]:
+            continue
+        atoms = s.cgpatom[s.cgp_first[g]:s.cgp_last[g] + 1]
+        p = xt[sw] if s.iuse_switch_atom == 1 else xt[atoms].mean(0)
+        if float(((p - s.xpcent) ** 2).sum()) > rin2:
+            shell[atoms] = 1
+    return shell

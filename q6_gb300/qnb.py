@@ -40,7 +40,8 @@ EXPORTED = (
     "qnb_group_create", "qnb_group_compute", "qnb_group_destroy", "qnb_profile_collect",
     "qnb_profile_classes", "qnb_set_solvent_internal", "qnb_autotune", "qnb_get_tuning", "qnb_set_tuning",
     "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
-    "qnb_set_bonded", "qnb_get_bonded_energies", "qnb_md_minimize",
+    "qnb_set_bonded", "qnb_get_bonded_energies", "qnb_md_minimize", "qnb_set_shell_restraint",
+    "qnb_get_restraint_energies",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -97,6 +98,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_md_get_state": [P, I32, P, P], "qnb_md_prepare": [P, I32], "qnb_md_run": [P, I32, I32, P, P, P],
         "qnb_set_bonded": [P, P], "qnb_get_bonded_energies": [P, P, P],
         "qnb_md_minimize": [P, I32, D, D, D, P],
+        "qnb_set_shell_restraint": [P, P, P, D, D], "qnb_get_restraint_energies": [P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -343,6 +345,23 @@ class NonbondedEngine:
         Eb = np.zeros((nsteps, self.nwin, 8 + 4 * self.S))
         self._check(self.lib.qnb_md_run(self.h, int(nsteps), int(istep0), _p(rec), _p(EQ), _p(Eb)))
         return rec, EQ[:, :, : self.S], Eb
+
+    # ---- fix_shell ---------------------------------------------------------
+    def set_shell_restraint(self, xtop, shell, fk_fix=200.0, fk_pshell=10.0):
+        """fix_shell restraint to xtop (None removes it); shell: per-atom flags
+        (q6_gb300.md.make_shell).  Defaults: qdyn's fk_fix and fk_pshell."""
+        if xtop is None:
+            self._check(self.lib.qnb_set_shell_restraint(self.h, None, None, 0.0, 0.0))
+            return
+        xt = np.ascontiguousarray(xtop, dtype=np.float64)
+        sh = np.ascontiguousarray(shell, dtype=np.uint8)
+        self._check(self.lib.qnb_set_shell_restraint(self.h, _p(xt), _p(sh), float(fk_fix), float(fk_pshell)))
+
+    def restraint_energies(self):
+        """[nwin][4]: fix, shell, solvent_radial, water_pol of the last evaluation."""
+        Er = np.zeros((self.nwin, 4))
+        self._check(self.lib.qnb_get_restraint_energies(self.h, _p(Er)))
+        return Er
 
     # ---- bonded terms ------------------------------------------------------
     def set_bonded(self, bt):

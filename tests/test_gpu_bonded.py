@@ -91,3 +91,31 @@ def test_generated_bonded_batched_equals_single(sys_q):
         Eb1, EQb1, D1 = device_eval(s, bt, xs[w], [lams[w]], PREC_MIXED)[2:]
         assert np.array_equal(Eb3[w], Eb1[0]) and np.array_equal(EQb3[w], EQb1[0])
         assert np.array_equal(D3[w], D1[0])
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_MIXED])
+def test_fix_shell_on_gpu(prec):
+    """fix_shell inside qnb_compute_dev against the oracle: excluded atoms
+    (fk_fix 200) and shell atoms beyond 3 A of the solute centre (fk_pshell
+    10) restrained to the generated coordinates, evaluated at displaced ones."""
+    from q6_gb300.md import make_shell
+    s = make_system(R=12.0, n_solute=40, group_sizes=(3, 5), ntypes=6, nq=4, nstates=2, seed=13,
+                    excl_radius=10.0)
+    sh = make_shell(s, 3.0)
+    x = s.x + np.random.default_rng(2).normal(0, 0.05, s.x.shape)
+    with NonbondedEngine(s, precision=prec) as e:
+        e.set_lambda([0.5, 0.5])
+        e.set_shell_restraint(s.x, sh, 200.0, 10.0)
+        e.set_coordinates_dev(x[None])
+        e.make_pair_lists_dev(**CUT)
+        e.compute_dev(sync=True)
+        Er = e.restraint_energies()
+        D = e.gradient_dev()
+    o = Oracle(s)
+    d0, _, _, _ = o.evaluate(x, [0.5, 0.5], cut=CUT)
+    d0, E0 = o.fix_shell(x, s.x, sh, 200.0, 10.0, d0)
+    assert E0[0] > 0 and E0[1] > 0
+    assert np.allclose(Er[0, :2], E0, rtol=1e-9, atol=1e-9)
+    scale = np.maximum(np.abs(d0), np.median(np.abs(d0)))
+    gtol = 1e-6 if prec == PREC_FP64 else 2e-3
+    assert np.all(np.abs(D[0] - d0) <= gtol * scale + 1e-9)

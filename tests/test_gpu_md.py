@@ -19,7 +19,7 @@ from q6_gb300.system import default_solvent_params, lambdas_for_window, make_sys
 
 pytestmark = pytest.mark.gpu
 CUT = dict(Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
-SETUP = MdSetup(stepsize=1.0, temp0=300.0, tau_t=100.0, nbcycle=5, shake_solute=True, cut=CUT)
+SETUP = MdSetup(stepsize=1.0, temp0=300.0, tau_t=100.0, nbcycle=5, shake_solute=True, shake_heavy=True, cut=CUT)
 
 
 @pytest.fixture(scope="module")
@@ -27,7 +27,7 @@ def system():
     return make_system(R=14.0, n_solute=40, group_sizes=(3, 5), ntypes=6, nq=6, nstates=2, seed=5150)
 
 
-def device_run(s, prec, nsteps, lams, setup=SETUP, graphs=True, v0=None, bonded=None, eb=None):
+def device_run(s, prec, nsteps, lams, setup=SETUP, graphs=True, v0=None, bonded=None, eb=None, shell=None):
     W = len(lams)
     sp = default_solvent_params(s, itdis=4.0)
     with NonbondedEngine(s, precision=prec, windows=W) as e:
@@ -38,6 +38,8 @@ def device_run(s, prec, nsteps, lams, setup=SETUP, graphs=True, v0=None, bonded=
         e.set_coordinates_dev(np.stack([s.x] * W))
         if bonded is not None:
             e.set_bonded(bonded)
+        if shell is not None:
+            e.set_shell_restraint(*shell)
         e.md_init(setup)
         e.md_set_velocities(v0 if v0 is not None else np.stack([maxwell_velocities(s, 300.0, 11 + w)
                                                                  for w in range(W)]))
@@ -129,24 +131,28 @@ def test_shake_failure_is_reported(system):
 
 
 def test_fp64_md_with_bonded_terms_matches_oracle(system):
-    """The step with solute bonded and Q bonded terms (constraints on the
-    water only): 10 steps against the oracle's step with the same terms."""
+    """The step with solute bonded and Q bonded terms and fix_shell
+    (constraints on the water only): 10 steps against the oracle's step with
+    the same terms."""
     from q6_gb300.bonded import synthetic_bonded
     s = system
     lam = [0.6, 0.4]
     setup = dataclasses.replace(SETUP, shake_solute=False, stepsize=0.5)
+    from q6_gb300.md import make_shell
     bt = synthetic_bonded(s, seed=21)
+    shell = (s.x.copy(), make_shell(s, 3.0), 200.0, 10.0)
     eb = []
-    rec, EQ, st = device_run(s, PREC_FP64, 10, [lam], setup=setup, bonded=bt, eb=eb)
+    rec, EQ, st = device_run(s, PREC_FP64, 10, [lam], setup=setup, bonded=bt, eb=eb, shell=shell)
     sp = default_solvent_params(s, itdis=4.0)
     o = Oracle(s)
     o.set_solvent_params(sp)
     cons = build_constraints(s, setup)
-    md = OracleMD(o, md_params(s, setup, cons), cons, sp=sp, lam=lam, bonded=bt)
+    md = OracleMD(o, md_params(s, setup, cons), cons, sp=sp, lam=lam, bonded=bt, shell=shell)
     x, v = md.prepare(s.x, maxwell_velocities(s, 300.0, 11))
     for k in range(10):
         r = md.step(x, v, k, CUT)
         assert np.allclose(eb[0][k, 0, :8], r["Eb"], rtol=1e-9, atol=1e-9), k
+        assert np.allclose([rec[k, 0]["fix"], rec[k, 0]["shell"]], r["fix_shell"], rtol=1e-9, atol=1e-12), k
         assert np.allclose(eb[0][k, 0, 8:].reshape(2, 4), r["EQb"], rtol=1e-9, atol=1e-9), k
         assert abs(rec[k, 0]["temp"] - r["temp"]) <= 1e-10 * r["temp"], k
     assert np.allclose(st[0][0], x, rtol=0, atol=1e-9)

@@ -33,7 +33,7 @@ def run(s, setup, nsteps, T=300.0, seed=1):
 
 
 def test_constraints_hold_after_steps(small):
-    setup = MdSetup(stepsize=1.0, shake_solute=True, cut=CUT)
+    setup = MdSetup(stepsize=1.0, shake_solute=True, shake_heavy=True, cut=CUT)
     x, v, cons, _ = run(small, setup, 8)
     d = np.linalg.norm(x[cons.ij[:, 0]] - x[cons.ij[:, 1]], axis=1)
     # SHAKE marks a constraint done once |d0^2 - d^2| < 1e-4 d0^2 and does not
@@ -44,7 +44,7 @@ def test_constraints_hold_after_steps(small):
 
 
 def test_total_energy_conserved_without_thermostat(small):
-    setup = MdSetup(stepsize=0.25, tau_t=1e12, shake_solute=True, cut=CUT)
+    setup = MdSetup(stepsize=0.25, tau_t=1e12, shake_solute=True, shake_heavy=True, cut=CUT)
     _, _, _, out = run(small, setup, 40)
     etot = out[:, 0] + out[:, 1]
     # leap-frog kinetic energy is half a step off the potential: compare the
@@ -53,7 +53,7 @@ def test_total_energy_conserved_without_thermostat(small):
 
 
 def test_berendsen_pulls_temperature_to_target(small):
-    setup = MdSetup(stepsize=1.0, tau_t=10.0, temp0=150.0, shake_solute=True, cut=CUT)
+    setup = MdSetup(stepsize=1.0, tau_t=10.0, temp0=150.0, shake_solute=True, shake_heavy=True, cut=CUT)
     _, _, _, out = run(small, setup, 60, T=450.0)
     t = out[:, 3]
     assert abs(t[-10:].mean() - 150.0) < abs(t[:3].mean() - 150.0) / 2
