@@ -1873,7 +1873,8 @@ __device__ __forceinline__ int watpol_shell(const SolventDev& p, double rcd) {
 // instead of the reference's six divisions and an arc cosine; it orders like
 // theta), because swapping two waters' targets changes their forces by
 // fkwpol * dtheta0.  The unit vectors for the forces are FP32 from the same
-// FP64 differences, theta is FP64 (atan2, below), and the shell of every
+// FP64 differences, theta is an FP32 atan2 of the FP64 cross and dot products
+// (below), and the shell of every
 // water is decided exactly: the FP32 distance decides away from the shell
 // radii, the FP64 distance within 2e-4 of one.
 template <bool MIX>
@@ -1900,12 +1901,12 @@ __global__ void k_watpol_theta(DevModel m, const DevState* __restrict__ states, 
         float rm = sqrtf((float)uu), rc = sqrtf((float)rr);
         float rmx = (float)ux / rm, rmy = (float)uy / rm, rmz = (float)uz / rm;
         float rcx = (float)qx / rc, rcy = (float)qy / rc, rcz = (float)qz / rc;
-        // theta from atan2(|u x q|, u.q): well conditioned at 0 and pi, where
-        // the arc cosine of a rounded cosine is not (an FP32 cosine of 1 gives
-        // theta 0 for a water a few 1e-4 rad off the radius, and the force's
-        // 1/sin(theta) then meets an O(theta) vector difference)
+        // theta from atan2(|u x q|, u.q) of FP64 products: well conditioned at 0
+        // and pi, where the arc cosine of a rounded cosine is not (an FP32
+        // cosine of 1 gives theta 0 for a water a few 1e-5 rad off the radius,
+        // and the force's 1/sin(theta) then meets an O(theta) vector difference)
         double cx = uy * qz - uz * qy, cy = uz * qx - ux * qz, cz = ux * qy - uy * qx;
-        s.theta[w] = atan2(sqrt(cx * cx + cy * cy + cz * cz), ur);
+        s.theta[w] = (double)atan2f(sqrtf((float)(cx * cx + cy * cy + cz * cz)), (float)ur);
         v[0] = rmx; v[1] = rmy; v[2] = rmz; v[3] = rm;
         v[4] = rcx; v[5] = rcy; v[6] = rcz; v[7] = rc;
         bool near = false;
