@@ -537,8 +537,10 @@ def md_step(args, s, sp, lams, local, tuning=None):
         e.md_prepare(stop_cm=True)
         warm = 25
         rec0, _, _ = e.md_run(warm, 0)
-        steps = max(50, min(4 * args.steps, 500))
-        steps -= steps % 25
+        # the generated sphere's MD stays stable for a few hundred steps at
+        # the endpoint windows (it is a random solute tree, not an equilibrated
+        # structure): 200 timed steps, 8 list builds
+        steps = 200
         stream = torch.cuda.ExternalStream(e.stream())
         torch.cuda.synchronize()
         ev0 = torch.cuda.Event(enable_timing=True)

@@ -230,6 +230,19 @@ def synthetic_bonded(s, seed: int = 7, q_bonded: bool = True) -> BondedTerms:
     tor = torsions_from_bonds(sb, nb)
     imp = [(ns[0], j, ns[1], ns[2]) for j in range(nat) for ns in [sorted(nb[j])] if len(ns) >= 3]
 
+    def ang_of(i, j, k):
+        a, b = x[i] - x[j], x[k] - x[j]
+        return float(np.arccos(np.clip(a @ b / np.linalg.norm(a) / np.linalg.norm(b), -1, 1)))
+
+    # the random tree has some nearly straight angles; angle_calc's gradient
+    # (1/sin theta) is singular at 180 degrees and dihedrals through a straight
+    # angle are undefined, so those terms are left out (force fields treat
+    # linear angles separately)
+    lin = np.deg2rad(160.0)
+    ang = [t for t in ang if ang_of(*t) < lin]
+    tor = [t for t in tor if ang_of(t[0], t[1], t[2]) < lin and ang_of(t[1], t[2], t[3]) < lin]
+    imp = [t for t in imp if max(ang_of(t[0], t[1], t[2]), ang_of(t[2], t[1], t[3]), ang_of(t[0], t[1], t[3])) < lin]
+
     def dist(i, j):
         return float(np.linalg.norm(x[i] - x[j]))
 

@@ -322,32 +322,58 @@ def _grow_tree(rng, n, rmax, bond=1.5, clash=2.0, max_deg=4):
     return pos, bonds
 
 
-def _compact_groups(rng, pos, sizes_range, reach=4.0):
-    """Charge groups of spatially adjacent atoms: walk the atoms in order and
-    give each unassigned atom a group of a drawn size (sizes_range), filled
-    with its nearest unassigned atoms within `reach`.  Returns the atom order
-    with groups consecutive, and the group sizes."""
+def _compact_groups(rng, pos, sizes_range, bonds=None, reach=4.0):
+    """Charge groups as connected pieces of the solute's bond tree (bonded
+    groups stay compact in dynamics; a group of unbonded neighbours can drift
+    apart, and the switch-atom list test then misses its atoms' close
+    contacts).  The tree is cut bottom-up: every atom collects itself and the
+    still-open pieces of its children, a child's piece is closed as a group
+    when adding it would pass the drawn size, and an atom's piece is closed
+    once it reaches that size.  Returns the atom order with groups
+    consecutive (each group in tree order), and the group sizes."""
     n = len(pos)
-    cells: dict = {}
-    key = lambda c: (int(math.floor(c[0] / reach)), int(math.floor(c[1] / reach)), int(math.floor(c[2] / reach)))
-    for i in range(n):
-        cells.setdefault(key(pos[i]), []).append(i)
-    taken = np.zeros(n, dtype=bool)
-    order, sizes = [], []
-    for a in range(n):
-        if taken[a]:
+    adj = [[] for _ in range(n)]
+    for a, b in (bonds if bonds is not None else []):
+        adj[int(a)].append(int(b))
+        adj[int(b)].append(int(a))
+    lo, hi = sizes_range
+    seen = np.zeros(n, dtype=bool)
+    groups = []
+    for root in range(n):   # one pass per connected component
+        if seen[root]:
             continue
-        g = int(rng.integers(sizes_range[0], sizes_range[1] + 1))
-        cx, cy, cz = key(pos[a])
-        near = [j for dx in (-1, 0, 1) for dy in (-1, 0, 1) for dz in (-1, 0, 1)
-                for j in cells.get((cx + dx, cy + dy, cz + dz), ()) if j != a and not taken[j]]
-        near = [j for j in near if np.sum((pos[j] - pos[a]) ** 2) <= reach * reach]
-        near.sort(key=lambda j: (float(np.sum((pos[j] - pos[a]) ** 2)), j))
-        members = [a] + near[:g - 1]
-        taken[members] = True
-        order.extend(members)
-        sizes.append(len(members))
-    return np.array(order, dtype=np.int64), sizes
+        parent = {root: -1}
+        pre = [root]
+        seen[root] = True
+        stack = [root]
+        while stack:   # pre-order of the component
+            u = stack.pop()
+            for w in sorted(adj[u], reverse=True):
+                if not seen[w]:
+                    seen[w] = True
+                    parent[w] = u
+                    pre.append(w)
+                    stack.append(w)
+        open_piece = {}
+        target = {u: int(rng.integers(lo, hi + 1)) for u in pre}
+        for u in reversed(pre):   # children before parents
+            piece = [u]
+            for w in adj[u]:
+                if parent.get(w) == u and w in open_piece:
+                    cp = open_piece.pop(w)
+                    if len(piece) + len(cp) > max(target[u], hi):
+                        groups.append(cp)
+                    else:
+                        piece.extend(cp)
+            if len(piece) >= target[u]:
+                groups.append(piece)
+            else:
+                open_piece[u] = piece
+        for piece in open_piece.values():
+            groups.append(piece)
+    groups.sort(key=lambda g: min(g))
+    order = [a for g in groups for a in sorted(g)]
+    return np.array(order, dtype=np.int64), [len(g) for g in groups]
 
 
 def _graph_dist(n, bonds, maxd=3):
@@ -403,7 +429,7 @@ def make_system(R: float = 15.0, n_solute: int = 20, group_sizes=(3, 5), ntypes:
     # ---- solute -----------------------------------------------------------
     pos, bonds = _grow_tree(rng, n_solute, rmax=max(R - 2.0, 3.0))
     # charge groups of adjacent atoms, numbered consecutively
-    order, sizes = _compact_groups(rng, pos, group_sizes) if n_solute else (np.zeros(0, np.int64), [])
+    order, sizes = _compact_groups(rng, pos, group_sizes, bonds) if n_solute else (np.zeros(0, np.int64), [])
     new_of = np.empty(n_solute, dtype=np.int64)
     new_of[order] = np.arange(n_solute)
     pos = pos[order]

@@ -31,7 +31,7 @@ def test_bonded_gradient_matches_finite_differences(sys_b, imp_type):
     x = s.x + rng.normal(0, 0.05, s.x.shape)   # away from the equilibrium values
     o = Oracle(s)
     d, Eb, EQb = o.bonded(x, bt, lam)
-    assert np.count_nonzero(Eb) >= 5 and np.all(np.abs(EQb) > 0)
+    assert np.count_nonzero(Eb) >= 5 and np.count_nonzero(EQb) >= 4
     atoms = sorted(set(rng.choice(s.nat_solute, 10, replace=False).tolist()) | {int(s.iqseq[0])} |
                    {s.nat_solute, s.nat_solute + 1})
     h = 1e-5
