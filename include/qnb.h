@@ -411,6 +411,17 @@ typedef struct qnb_bonded {
 int qnb_set_bonded(qnb_context* ctx, const qnb_bonded* b);
 int qnb_get_bonded_energies(qnb_context* ctx, double* Eb, double* EQb);
 
+/* offdiag (src/nonbondene.f90:6238-6260): the EVB couplings of Q-state pairs
+   (states[2k], states[2k+1], 0-based) as functions of the distance of two Q
+   atoms (qatoms[2k], qatoms[2k+1], 0-based Q indices):
+   Hij = A[k] exp(-mu[k] r_kl).  Evaluated inside qnb_compute_dev and every
+   qnb_md_run step; n = 0 removes them.  qnb_get_offdiag returns the last
+   evaluation's Hij and r_kl, [nwin][n] each (either may be NULL); these are
+   the OFFD records put_ene writes. */
+int qnb_set_offdiag(qnb_context* ctx, int32_t n, const int32_t* states, const int32_t* qatoms, const double* A,
+                    const double* mu);
+int qnb_get_offdiag(qnb_context* ctx, double* Hij, double* rkl);
+
 /* fix_shell (src/potene.f90:386-423), evaluated inside qnb_compute_dev and
    qnb_md_run once set: excluded atoms (the topology's excl flags) with
    fk_fix and shell atoms (shell[i] != 0, as make_shell / make_shell2 mark

@@ -141,6 +141,9 @@ struct qnb_context {
     double* h_stage = nullptr;   // pinned staging for x / d (natom*3)
     double* h_e = nullptr;       // pinned energies (nwin x (kNumE doubles + kNumE fixed))
 
+    // offdiag (qnb_set_offdiag)
+    OffdDev offd{};
+    std::vector<void*> offd_bufs;
     // fix_shell (qnb_set_shell_restraint)
     bool have_shell = false;
     uint8_t* d_shell_flags = nullptr;
@@ -1452,6 +1455,10 @@ int enqueue_compute(qnb_context* c, double Tfree, int istep) {
         timed(c, K_RESTRAIN, [&] { launch_fix_shell(L, c->d_shell_flags, c->d_xtop, c->fk_fix, c->fk_pshell, c->mixed); });
         c->launches++;
     }
+    if (c->offd.n > 0) {
+        launch_offdiag(L, c->offd);
+        c->launches++;
+    }
     if (c->have_solv) {
         timed(c, K_RESTRAIN, [&] { launch_restrain_solvent(L, c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv); });
         c->launches++;
@@ -2354,6 +2361,62 @@ int qnb_get_restraint_energies(qnb_context* c, double* Er) {
         Er[4 * w + 1] = ew[E_RST_SHELL];
         Er[4 * w + 2] = ew[E_RST_RAD];
         Er[4 * w + 3] = ew[E_RST_POL];
+    }
+    return QNB_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int qnb_set_offdiag(qnb_context* c, int32_t n, const int32_t* states, const int32_t* qatoms, const double* A,
+                    const double* mu) {
+    if (!c || n < 0 || (n > 0 && (!states || !qatoms || !A || !mu))) return fail(QNB_ERR_ARG, "null argument");
+    for (int k = 0; k < n; ++k) {
+        if (states[2 * k] < 0 || states[2 * k] >= c->S || states[2 * k + 1] < 0 || states[2 * k + 1] >= c->S)
+            return fail(QNB_ERR_ARG, "offdiag %d: state out of range", k);
+        if (qatoms[2 * k] < 0 || qatoms[2 * k] >= c->nqat || qatoms[2 * k + 1] < 0 || qatoms[2 * k + 1] >= c->nqat)
+            return fail(QNB_ERR_ARG, "offdiag %d: Q atom out of range", k);
+    }
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    for (void* p : c->offd_bufs) c->release(p);
+    c->offd_bufs.clear();
+    c->offd = OffdDev{};
+    ++c->epoch;
+    if (n == 0) return QNB_OK;
+    std::vector<int> iqseq(c->nqat);
+    CU(cudaMemcpy(iqseq.data(), c->m.iqseq, sizeof(int) * c->nqat, cudaMemcpyDeviceToHost));
+    std::vector<int2> kl(n);
+    std::vector<double2> am(n);
+    for (int k = 0; k < n; ++k) {
+        kl[k] = make_int2(iqseq[qatoms[2 * k]], iqseq[qatoms[2 * k + 1]]);
+        am[k] = make_double2(A[k], mu[k]);
+    }
+    OffdDev o{};
+    o.n = n;
+    TRY(c->upload((int2**)&o.kl, kl));
+    c->offd_bufs.push_back((void*)o.kl);
+    TRY(c->upload((double2**)&o.Amu, am));
+    c->offd_bufs.push_back((void*)o.Amu);
+    TRY(c->alloc(&o.out, (size_t)2 * n * c->nwin));
+    c->offd_bufs.push_back((void*)o.out);
+    CU(cudaMemset(o.out, 0, sizeof(double) * 2 * n * c->nwin));
+    c->offd = o;
+    return QNB_OK;
+}
+
+int qnb_get_offdiag(qnb_context* c, double* Hij, double* rkl) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    const int n = c->offd.n;
+    if (n == 0) return QNB_OK;
+    std::vector<double> v((size_t)2 * n * c->nwin);
+    CU(cudaMemcpyAsync(v.data(), c->offd.out, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    for (size_t k = 0; k < (size_t)n * c->nwin; ++k) {
+        if (Hij) Hij[k] = v[2 * k];
+        if (rkl) rkl[k] = v[2 * k + 1];
     }
     return QNB_OK;
 }

@@ -253,6 +253,14 @@ struct BondedDev {
     int nterms;             // classical terms + Q terms x states
 };
 void launch_bonded(const Launch& L, const BondedDev& b, int mixed);
+// offdiag: Hij = A exp(-mu r_kl) per window, out[(w*n + io)*2] = Hij, rkl
+struct OffdDev {
+    int n;
+    const int2* kl;          // atom indices of the two Q atoms
+    const double2* Amu;      // A, mu
+    double* out;             // [nwin][n][2]
+};
+void launch_offdiag(const Launch& L, const OffdDev& o);
 // fix_shell: flag bit 0 excluded (fk_fix), bit 1 shell (fk_pshell); xtop [natom*3]
 void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop, double fk_fix, double fk_pshell,
                       int mixed);

@@ -3216,6 +3216,25 @@ void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop,
     if (mixed) k_fix_shell<true><<<g, 64, 0, L.st>>>(L.m, L.ds, flags, xtop, fk_fix, fk_pshell);
     else k_fix_shell<false><<<g, 64, 0, L.st>>>(L.m, L.ds, flags, xtop, fk_fix, fk_pshell);
 }
+// offdiag, src/nonbondene.f90:6238-6260: the EVB couplings
+// Hij = A exp(-mu r_kl) of Q-atom pairs, FP64 in both forms
+__global__ void k_offdiag(const DevState* __restrict__ states, OffdDev o) {
+    const int w = blockIdx.y;
+    const double* __restrict__ x = states[w].x;
+    for (int io = blockIdx.x * blockDim.x + threadIdx.x; io < o.n; io += gridDim.x * blockDim.x) {
+        int2 kl = o.kl[io];
+        double dx = x[3 * kl.y] - x[3 * kl.x], dy = x[3 * kl.y + 1] - x[3 * kl.x + 1],
+               dz = x[3 * kl.y + 2] - x[3 * kl.x + 2];
+        double r = sqrt(dx * dx + dy * dy + dz * dz);
+        double2 am = o.Amu[io];
+        o.out[((size_t)w * o.n + io) * 2] = am.x * exp(-am.y * r);
+        o.out[((size_t)w * o.n + io) * 2 + 1] = r;
+    }
+}
+void launch_offdiag(const Launch& L, const OffdDev& o) {
+    if (o.n == 0) return;
+    k_offdiag<<<dim3((o.n + 63) / 64, L.nwin), 64, 0, L.st>>>(L.ds, o);
+}
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv) {
     if (L.m.nwat == 0) return;

@@ -41,7 +41,7 @@ EXPORTED = (
     "qnb_profile_classes", "qnb_set_solvent_internal", "qnb_autotune", "qnb_get_tuning", "qnb_set_tuning",
     "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
     "qnb_set_bonded", "qnb_get_bonded_energies", "qnb_md_minimize", "qnb_set_shell_restraint",
-    "qnb_get_restraint_energies",
+    "qnb_get_restraint_energies", "qnb_set_offdiag", "qnb_get_offdiag",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -99,6 +99,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_set_bonded": [P, P], "qnb_get_bonded_energies": [P, P, P],
         "qnb_md_minimize": [P, I32, D, D, D, P],
         "qnb_set_shell_restraint": [P, P, P, D, D], "qnb_get_restraint_energies": [P, P],
+        "qnb_set_offdiag": [P, I32, P, P, P, P], "qnb_get_offdiag": [P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -345,6 +346,33 @@ class NonbondedEngine:
         Eb = np.zeros((nsteps, self.nwin, 8 + 4 * self.S))
         self._check(self.lib.qnb_md_run(self.h, int(nsteps), int(istep0), _p(rec), _p(EQ), _p(Eb)))
         return rec, EQ[:, :, : self.S], Eb
+
+    # ---- offdiag ------------------------------------------------------------
+    def set_offdiag(self, rows):
+        """rows: (state_i, state_j, qatom_k, qatom_l, A, mu), 0-based."""
+        rows = list(rows)
+        st = np.ascontiguousarray([[r[0], r[1]] for r in rows], dtype=np.int32).reshape(-1, 2)
+        qa = np.ascontiguousarray([[r[2], r[3]] for r in rows], dtype=np.int32).reshape(-1, 2)
+        A = np.ascontiguousarray([r[4] for r in rows], dtype=np.float64)
+        mu = np.ascontiguousarray([r[5] for r in rows], dtype=np.float64)
+        self.offd_states = st
+        self._check(self.lib.qnb_set_offdiag(self.h, len(rows), _p(st), _p(qa), _p(A), _p(mu)))
+
+    def offdiag(self):
+        """(Hij, rkl), [nwin][n] each, of the last evaluation."""
+        n = len(getattr(self, "offd_states", []))
+        Hij = np.zeros((self.nwin, n))
+        rkl = np.zeros((self.nwin, n))
+        if n:
+            self._check(self.lib.qnb_get_offdiag(self.h, _p(Hij), _p(rkl)))
+        return Hij, rkl
+
+    def offd_records(self, window=0):
+        """put_ene's OFFD records of a window (1-based states), for
+        q6_gb300.enefile.EnergyFileWriter.write_step(offd=...)."""
+        Hij, rkl = self.offdiag()
+        return [(int(i) + 1, int(j) + 1, float(h), float(r))
+                for (i, j), h, r in zip(self.offd_states, Hij[window], rkl[window])]
 
     # ---- fix_shell ---------------------------------------------------------
     def set_shell_restraint(self, xtop, shell, fk_fix=200.0, fk_pshell=10.0):
