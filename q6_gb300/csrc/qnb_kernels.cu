@@ -786,6 +786,102 @@ __global__ void __launch_bounds__(kLrfBlock) k_lrf_accumulate(DevModel m, const 
     }
 }
 
+// Mixed form, two target groups per warp: every lane applies the source atom
+// it loaded to both targets, so the shared-memory loads and the loop
+// overhead of a source atom are paid once for two targets (the kernel is
+// issue-bound: about 90 instructions per target and source with one target
+// per warp).  Sums and their order per target are those of k_lrf_accumulate.
+constexpr int kLrfPair = 2;
+__global__ void __launch_bounds__(kLrfBlock) k_lrf_accumulate2(DevModel m, const DevState* __restrict__ states, Cut c,
+                                                               const int* __restrict__ lrf_src) {
+    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
+    __shared__ float4 s_xs[kLrfBlock];
+    __shared__ int s_src[kLrfBlock];
+    __shared__ float4 s_xi[kLrfBlock];
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const float4* __restrict__ xq = s.xq;
+    double* __restrict__ lrf = s.lrf;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kLrfBlock / 32;
+    const int per_block = nw * kLrfPair;
+    for (int gbase = blockIdx.x * per_block; gbase < m.ncgp; gbase += gridDim.x * per_block) {   // block-uniform
+        int g2[kLrfPair], s2[kLrfPair];
+        bool act[kLrfPair];
+        Band rc_s[kLrfPair], rc_w[kLrfPair];
+        float4 x2[kLrfPair];
+        float ccx[kLrfPair], ccy[kLrfPair], ccz[kLrfPair];
+        float mom[kLrfPair][kLrfMom];
+#pragma unroll
+        for (int t = 0; t < kLrfPair; ++t) {
+            g2[t] = gbase + kLrfPair * warp + t;
+            s2[t] = 0;
+            act[t] = g2[t] < m.ncgp;
+            if (act[t]) {
+                s2[t] = group_dist_atom(m, g2[t]);
+                act[t] = !m.excl[s2[t]];
+            }
+            const bool sol2 = act[t] && g2[t] < m.ncgp_solute;
+            rc_s[t] = sol2 ? bpp : bpw;
+            rc_w[t] = sol2 ? bpw : bww;
+            double cx = 0.0, cy = 0.0, cz = 0.0;
+            x2[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (act[t]) {
+                const double* L = lrf + (size_t)g2[t] * kLrfLen;
+                cx = L[0]; cy = L[1]; cz = L[2];
+                x2[t] = xq[s2[t]];
+            }
+            ccx[t] = (float)(cx - m.xpcent[0]);
+            ccy[t] = (float)(cy - m.xpcent[1]);
+            ccz[t] = (float)(cz - m.xpcent[2]);
+#pragma unroll
+            for (int k = 0; k < kLrfMom; ++k) mom[t][k] = 0.f;
+        }
+        const bool any = act[0] || act[1];
+        for (int i0 = 0; i0 < m.natom; i0 += kLrfBlock) {
+            __syncthreads();
+            {
+                int i = i0 + threadIdx.x, t = threadIdx.x;
+                int src = i < m.natom ? lrf_src[i] : -1;
+                s_src[t] = src;
+                if (src >= 0) {
+                    s_xs[t] = xq[src & 0x3fffffff];
+                    s_xi[t] = xq[i];
+                }
+            }
+            __syncthreads();
+            if (!any) continue;
+            const int n = min(kLrfBlock, m.natom - i0);
+            for (int k = lane; k < n; k += kWarp) {
+                int src = s_src[k];   // distance atom of i's group | solute flag << 30
+                if (src < 0) continue;
+                const int s1 = src & 0x3fffffff;
+                const bool sol1 = (src >> 30) != 0;
+                const float4 xs = s_xs[k], xi = s_xi[k];
+#pragma unroll
+                for (int t = 0; t < kLrfPair; ++t) {
+                    if (!act[t] || s1 == s2[t]) continue;
+                    const Band& rc2 = sol1 ? rc_s[t] : rc_w[t];
+                    if (!lrf_pair(r2_f(x2[t], xs), rc2, blrf, x, s2[t], s1)) continue;
+                    lrf_terms<float>(xi.x - ccx[t], xi.y - ccy[t], xi.z - ccz[t], xi.w, mom[t]);
+                }
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < kLrfPair; ++t) {
+            if (!act[t]) continue;   // warp-uniform
+            double tot[kLrfMom];
+#pragma unroll
+            for (int k = 0; k < kLrfMom; ++k) {
+                float v = mom[t][k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+                tot[k] = (double)v;
+            }
+            if (lane == 0) lrf_expand(tot, lrf + (size_t)g2[t] * kLrfLen + 3);
+        }
+    }
+}
+
 // Unstaged variant: one warp per target group reads the source atoms straight
 // from global memory (lanes stride over the atoms, so loads are coalesced).
 template <bool MIX>
@@ -2761,8 +2857,14 @@ void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* 
 #ifndef QNB_LRF_FP64_STAGED
 #define QNB_LRF_FP64_STAGED 0
 #endif
+#ifndef QNB_LRF_PAIR
+#define QNB_LRF_PAIR 1   // mixed form: two target groups per warp (k_lrf_accumulate2)
+#endif
     dim3 g = grid_for((int64_t)L.m.ncgp * 32, kLrfBlock, L.tu.v[T_LRF], L.nwin);
-    if (mixed) k_lrf_accumulate<true><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
+    if (mixed && QNB_LRF_PAIR)
+        k_lrf_accumulate2<<<grid_for((int64_t)L.m.ncgp * 32 / kLrfPair, kLrfBlock, L.tu.v[T_LRF], L.nwin), kLrfBlock, 0,
+                            L.st>>>(L.m, L.ds, c, lrf_src);
+    else if (mixed) k_lrf_accumulate<true><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
     else if (QNB_LRF_FP64_STAGED) k_lrf_accumulate<false><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
     else k_lrf_accumulate_direct<false><<<grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
 }
