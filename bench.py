@@ -41,6 +41,25 @@ def window_lambdas(n):
     return [(w / (n - 1) if n > 1 else 0.5) for w in range(n)]
 
 
+def max_over_ranks(t_local, world, device="cpu"):
+    """The slowest rank's time (ms): every rank runs its own windows (replicas,
+    no exchange during the timed steps), so the job takes as long as its
+    slowest rank.  NCCL needs a device tensor, gloo a host tensor."""
+    if world <= 1:
+        return float(t_local)
+    import torch
+    t = torch.tensor([float(t_local)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
+def job_throughput(t_max_ms, world, nwin, steps):
+    """Window-steps per second of the whole job: world ranks x nwin windows
+    x steps, over the slowest rank's time."""
+    return world * nwin * steps / (t_max_ms / 1e3)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -179,14 +198,9 @@ def run_ours(args, rank, world, local):
         eng.profile_collect()
     ktimes = eng.kernel_times()
     eng.profile(False)
-    t_local = total_ms
-    if world > 1:
-        t = torch.tensor([t_local], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_local = float(t.item())
-        torch.distributed.barrier()
+    t_local = max_over_ranks(total_ms, world, device="cuda")
     ms_per_step = t_local / args.steps
-    value = world * nwin * args.steps / (t_local / 1e3)
+    value = job_throughput(t_local, world, nwin, args.steps)
     counts = {k: eng.list_size(i) for i, k in enumerate(("pp", "pw", "ww", "qp", "qw", "pp14"))}
 
     # ---- roofline of the dominant kernel class (live CUDA events) ---------
