@@ -2245,12 +2245,16 @@ int qnb_set_bonded(qnb_context* c, const qnb_bonded* b) {
     for (int k = 0; k < b->nimplib; ++k) il[k] = make_double2(b->implib[2 * k], b->implib[2 * k + 1]);
     for (int k = 0; k < b->nqimplib; ++k) qil[k] = make_double2(b->qimplib[2 * k], b->qimplib[2 * k + 1]);
     auto d4 = [](const double* v, int cnt, int w) {
-        std::vector<double4> o(cnt);
-        for (int k = 0; k < cnt; ++k)
-            o[k] = make_double4(v[w * k], v[w * k + 1], w > 2 ? v[w * k + 2] : 0.0, w > 3 ? v[w * k + 3] : 0.0);
+        std::vector<double4_16a> o(cnt);
+        for (int k = 0; k < cnt; ++k) {
+            o[k].x = v[w * k];
+            o[k].y = v[w * k + 1];
+            o[k].z = w > 2 ? v[w * k + 2] : 0.0;
+            o[k].w = w > 3 ? v[w * k + 3] : 0.0;
+        }
         return o;
     };
-    std::vector<double4> al = d4(b->anglib, b->nanglib, 4), tl = d4(b->torlib, b->ntorlib, 4),
+    std::vector<double4_16a> al = d4(b->anglib, b->nanglib, 4), tl = d4(b->torlib, b->ntorlib, 4),
                          qbl = d4(b->qbondlib, b->nqbondlib, 4), qal = d4(b->qanglib, b->nqanglib, 4),
                          qtl = d4(b->qtorlib, b->nqtorlib, 3);
     std::vector<int> tors(b->torsions, b->torsions + 5 * (size_t)b->ntors),
@@ -2271,20 +2275,20 @@ int qnb_set_bonded(qnb_context* c, const qnb_bonded* b) {
     TRY(up((int4**)&d.bonds, bonds));
     TRY(up((double2**)&d.bondlib, bl));
     TRY(up((int4**)&d.angles, angles));
-    TRY(up((double4**)&d.anglib, al));
+    TRY(up((double4_16a**)&d.anglib, al));
     TRY(up((int**)&d.tors, tors));
-    TRY(up((double4**)&d.torlib, tl));
+    TRY(up((double4_16a**)&d.torlib, tl));
     TRY(up((int**)&d.imps, imps));
     TRY(up((double2**)&d.implib, il));
     TRY(up((int2**)&d.qbonds, qb));
     TRY(up((int**)&d.qbond_code, qbc));
-    TRY(up((double4**)&d.qbondlib, qbl));
+    TRY(up((double4_16a**)&d.qbondlib, qbl));
     TRY(up((int4**)&d.qangles, qa));
     TRY(up((int**)&d.qangle_code, qac));
-    TRY(up((double4**)&d.qanglib, qal));
+    TRY(up((double4_16a**)&d.qanglib, qal));
     TRY(up((int4**)&d.qtors, qt));
     TRY(up((int**)&d.qtor_code, qtc));
-    TRY(up((double4**)&d.qtorlib, qtl));
+    TRY(up((double4_16a**)&d.qtorlib, qtl));
     TRY(up((int4**)&d.qimps, qi));
     TRY(up((int**)&d.qimp_code, qic));
     TRY(up((double2**)&d.qimplib, qil));

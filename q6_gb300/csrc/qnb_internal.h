@@ -235,19 +235,19 @@ struct BondedDev {
     const int4* bonds;      // i j code -
     const double2* bondlib; // fk b0
     const int4* angles;     // i j k code
-    const double4* anglib;  // fk theta0 ureyfk ureyr0
+    const double4_16a* anglib;  // fk theta0 ureyfk ureyr0
     const int* tors;        // [5n] i j k l code
-    const double4* torlib;  // fk rmult delta 1/paths
+    const double4_16a* torlib;  // fk rmult delta 1/paths
     const int* imps;        // [5n]
     const double2* implib;  // fk phi0
     int imp_type, urey;
     int nqb, nqa, nqt, nqi;
     const int2* qbonds; const int* qbond_code;   // [n], [n*S]
-    const double4* qbondlib;                     // Dmz amz r0 fk
+    const double4_16a* qbondlib;                     // Dmz amz r0 fk
     const int4* qangles; const int* qangle_code; // i j k -
-    const double4* qanglib;
+    const double4_16a* qanglib;
     const int4* qtors; const int* qtor_code;
-    const double4* qtorlib;                      // fk rmult delta -
+    const double4_16a* qtorlib;                      // fk rmult delta -
     const int4* qimps; const int* qimp_code;
     const double2* qimplib;
     int nterms;             // classical terms + Q terms x states

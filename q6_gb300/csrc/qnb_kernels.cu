@@ -3126,7 +3126,7 @@ __global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevSt
         if (u < b.na) {   // angle, src/bondene.f90:41-113 (+ urey_bradley 115-180)
             int4 e = b.angles[u];
             if (e.w < 0) continue;
-            double4 lib = b.anglib[e.w];
+            double4_16a lib = b.anglib[e.w];
             const T fk = (T)lib.x, th0 = (T)lib.y, ufk = (T)lib.z, ur0 = (T)lib.w;
             const int slot = E_B0 + (u < b.na_sol ? 1 : 5);
             AngleVal<T> c = angle_calc(P(e.x), P(e.y), P(e.z));
@@ -3154,7 +3154,7 @@ __global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevSt
         if (u < b.nt) {   // torsion, src/bondene.f90:689-762
             const int* e = b.tors + 5 * u;
             if (e[4] < 0) continue;
-            double4 lib = b.torlib[e[4]];
+            double4_16a lib = b.torlib[e[4]];
             const T fk = (T)lib.x, rm = (T)lib.y, dl = (T)lib.z, ip = (T)lib.w;
             TorsVal<T> c = torsion_calc(P(e[0]), P(e[1]), P(e[2]), P(e[3]));
             T arg = rm * c.angl - dl;
@@ -3197,7 +3197,7 @@ __global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevSt
             const int q = u / S, st = u % S, code = b.qbond_code[u];
             if (code < 0) continue;
             int2 e = b.qbonds[q];
-            double4 lib = b.qbondlib[code];   // Dmz amz r0 fk
+            double4_16a lib = b.qbondlib[code];   // Dmz amz r0 fk
             const T Dmz = (T)lib.x, amz = (T)lib.y, r0 = (T)lib.z, fk = (T)lib.w;
             V3<T> av = P(e.y) - P(e.x);
             T dist = sqrt(vdot(av, av));
@@ -3214,7 +3214,7 @@ __global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevSt
             const int q = u / S, st = u % S, code = b.qangle_code[u];
             if (code < 0) continue;
             int4 e = b.qangles[q];
-            double4 lib = b.qanglib[code];
+            double4_16a lib = b.qanglib[code];
             const T fk = (T)lib.x, th0 = (T)lib.y, ufk = (T)lib.z, ur0 = (T)lib.w;
             const T l = lam(st);
             AngleVal<T> c = angle_calc(P(e.x), P(e.y), P(e.z));
@@ -3241,7 +3241,7 @@ __global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevSt
             const int q = u / S, st = u % S, code = b.qtor_code[u];
             if (code < 0) continue;
             int4 e = b.qtors[q];
-            double4 lib = b.qtorlib[code];
+            double4_16a lib = b.qtorlib[code];
             const T fk = (T)lib.x, rm = (T)lib.y, dl = (T)lib.z;
             TorsVal<T> c = torsion_calc(P(e.x), P(e.y), P(e.z), P(e.w));
             T arg = rm * c.angl - dl;
