@@ -430,8 +430,38 @@ int qnb_get_offdiag(qnb_context* ctx, double* Hij, double* rkl);
    xtop = NULL removes the restraint.  The freeze option is not supported. */
 int qnb_set_shell_restraint(qnb_context* ctx, const double* xtop, const uint8_t* shell, double fk_fix,
                             double fk_pshell);
-/* Restraint energies of the last evaluation, Er[4w..4w+3] = fix, shell,
-   solvent_radial, water_pol of window w. */
+/* The input file's restraint sections, p_restrain (src/bondene.f90:764-1020),
+   evaluated inside qnb_compute_dev and qnb_md_run once set (FP64):
+     sequence  atoms seq_ij[2k]..seq_ij[2k+1] (heavy atoms, or all with
+               seq_ih[k] = 1) restrained to xtop with seq_fk[k]: each atom
+               (mode 0), their geometric centre (1; the reference's force on
+               each atom is dr fk m_i / 12.010) or mass centre (2) -> E%restraint%protein
+     position  atom pos_i[k] to pos_x[3k..] with per-axis pos_fk[3k..]
+     distance  atoms dist_ij[2k], [2k+1], flat bottom between dist_d[2k] and
+               dist_d[2k+1] (A), dist_fk[k]
+     angle     atoms ang_ijk[3k..] at ang_theta[k] (degrees), ang_fk[k]
+     wall      atoms wall_ij[2k]..[2k+1] (heavy, or all with wall_ih[k] = 1):
+               half-harmonic beyond wall_d[k] from xwcent (fk wall_fk[k]),
+               Morse inside (wall_aMorse, wall_dMorse) -> E%restraint%protein
+   State-dependent kinds (position, distance, angle) carry *_state[k]: -1 for
+   every state (the reference's 0: the energy goes to every state's
+   EQ(s)%restraint, the force is unweighted), else the 0-based state s whose
+   EQ(s)%restraint gets the energy and whose lambda weights the force.
+   Atom indices 0-based; xtop is natom x 3.  r = NULL removes the restraints.
+   The freeze option is not supported. */
+typedef struct qnb_restraints {
+    int32_t nseq;  const int32_t* seq_ij;  const double* seq_fk;  const int32_t* seq_ih;  const int32_t* seq_mode;
+    int32_t npos;  const int32_t* pos_i;   const int32_t* pos_state; const double* pos_x;  const double* pos_fk;
+    int32_t ndist; const int32_t* dist_ij; const int32_t* dist_state; const double* dist_d; const double* dist_fk;
+    int32_t nang;  const int32_t* ang_ijk; const int32_t* ang_state; const double* ang_theta; const double* ang_fk;
+    int32_t nwall; const int32_t* wall_ij; const double* wall_d;   const double* wall_fk;
+    const double* wall_aMorse; const double* wall_dMorse; const int32_t* wall_ih;
+} qnb_restraints;
+int qnb_set_restraints(qnb_context* ctx, const qnb_restraints* r, const double* xtop);
+
+/* Restraint energies of the last evaluation:
+   Er[w*(5 + nstates) + k] = fix, shell, solvent_radial, water_pol, protein,
+   then EQ(s)%restraint for every state s. */
 int qnb_get_restraint_energies(qnb_context* ctx, double* Er);
 
 /* ---- device-resident MD step (FP64) ----------------------------------------
@@ -475,6 +505,7 @@ typedef struct qnb_md_record {
     double solvent_radial, water_pol;
     double ekin, temp, tfree, shake_iterations;
     double fix, shell;        /* E%restraint%fix, %shell (qnb_set_shell_restraint) */
+    double protein;           /* E%restraint%protein (qnb_set_restraints)          */
 } qnb_md_record;
 
 /* mass[natom] (amu); the constraints of molecule m are

@@ -65,6 +65,7 @@ def lib():
         L.orc_md_temperature.argtypes = [I, P, P, P, I, P, P, P, P, D, D, D, D, D, D, P, P]
         L.orc_bonded.argtypes = [P, P, P, I, P, P, P]
         L.orc_fix_shell.argtypes = [I, P, P, P, P, P, D, D, P]
+        L.orc_p_restrain.argtypes = [P, P, P, P, P, P, P, I, P, P, P]
         L.orc_static_qq_size.restype = ctypes.c_long
         L.orc_static_qq_size.argtypes = [P, I, I]
         _lib = L
@@ -191,6 +192,24 @@ class Oracle:
         lib().orc_fix_shell(self.s.natom, _p(x), _p(d), _p(xt), _p(excl), _p(sh), float(fk_fix), float(fk_pshell),
                             _p(E))
         return d, E
+
+    def p_restrain(self, x, r, lam, xtop=None, d=None):
+        """p_restrain for a q6_gb300.restraints.Restraints: (d, E_protein,
+        EQ_restraint[nstates])."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if d is None:
+            d = np.zeros_like(x)
+        st, keep = r.to_struct()
+        xt = np.ascontiguousarray(self.s.x if xtop is None else xtop, dtype=np.float64)
+        heavy = np.ascontiguousarray(self.s.heavy, dtype=np.uint8)
+        mass = np.ascontiguousarray(self.s.mass[self.s.iac], dtype=np.float64)
+        xw = np.ascontiguousarray(self.s.xwcent, dtype=np.float64)
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        Ep = np.zeros(1)
+        EQr = np.zeros(max(self.S, 1))
+        lib().orc_p_restrain(_p(x), _p(d), ctypes.byref(st), _p(xt), _p(heavy), _p(mass), _p(xw), self.S, _p(lam),
+                             _p(Ep), _p(EQr))
+        return d, float(Ep[0]), EQr[: self.S]
 
     def evaluate(self, x, lam, cut=None, solvent=None, Tfree=300.0, istep=0, lists=True):
         """One full nonbonded evaluation in the reference's call order."""

@@ -1590,3 +1590,102 @@ void orc_fix_shell(int natom, const double* x, double* d, const double* xtop, co
         gadd(d, i, vscale(vec, fk));
     }
 }
+
+/* p_restrain, src/bondene.f90:764-1020 (no PBC, no freeze).  Eprot[0] +=
+   E%restraint%protein; EQr[s] += EQ(s)%restraint; xtop natom x 3; heavy and
+   mass per atom; xwcent the solvent centre.  States as qnb_restraints (-1:
+   every state). */
+static void rstate(int S, int st, double e, double* Eprot, double* EQr) {
+    if (st >= 0) EQr[st] += e;
+    else if (S == 0) Eprot[0] += e;
+    else for (int k = 0; k < S; ++k) EQr[k] += e;
+}
+void orc_p_restrain(const double* x, double* d, const qnb_restraints* r, const double* xtop, const uint8_t* heavy,
+                    const double* mass, const double* xwcent, int S, const double* lambda, double* Eprot,
+                    double* EQr) {
+    for (int k = 0; k < r->nseq; ++k) {
+        int a = r->seq_ij[2 * k], b = r->seq_ij[2 * k + 1], ih = r->seq_ih[k], mode = r->seq_mode[k];
+        double fk = r->seq_fk[k];
+        if (mode == 1 || mode == 2) {
+            v3 dr = {0.0, 0.0, 0.0};
+            double tot = 0.0;
+            for (int i = a; i <= b; ++i) {
+                if (!(heavy[i] || ih == 1)) continue;
+                double w = mode == 2 ? mass[i] : 1.0;
+                dr = vadd(dr, vscale(vsub(X(x, i), X(xtop, i)), w));
+                tot += w;
+            }
+            if (tot > 0.0) {
+                dr = vscale(dr, 1.0 / tot);
+                Eprot[0] += 0.5 * fk * vsq(dr);
+                for (int i = a; i <= b; ++i) {
+                    if (!(heavy[i] || ih == 1)) continue;
+                    gadd(d, i, vscale(dr, mode == 2 ? fk : fk * mass[i] / 12.010));
+                }
+            }
+        } else {
+            for (int i = a; i <= b; ++i) {
+                if (!(heavy[i] || ih == 1)) continue;
+                v3 dr = vsub(X(x, i), X(xtop, i));
+                Eprot[0] += 0.5 * fk * vsq(dr);
+                gadd(d, i, vscale(dr, fk));
+            }
+        }
+    }
+    for (int k = 0; k < r->npos; ++k) {
+        int i = r->pos_i[k], st = r->pos_state[k];
+        v3 x0 = {r->pos_x[3 * k], r->pos_x[3 * k + 1], r->pos_x[3 * k + 2]};
+        v3 fk = {r->pos_fk[3 * k], r->pos_fk[3 * k + 1], r->pos_fk[3 * k + 2]};
+        v3 dr = vsub(X(x, i), x0);
+        double wgt = st >= 0 ? lambda[st] : 1.0;
+        rstate(S, st, 0.5 * (fk.x * dr.x * dr.x + fk.y * dr.y * dr.y + fk.z * dr.z * dr.z), Eprot, EQr);
+        v3 g = {fk.x * dr.x * wgt, fk.y * dr.y * wgt, fk.z * dr.z * wgt};
+        gadd(d, i, g);
+    }
+    for (int k = 0; k < r->ndist; ++k) {
+        int i = r->dist_ij[2 * k], j = r->dist_ij[2 * k + 1], st = r->dist_state[k];
+        v3 av = vsub(X(x, j), X(x, i));
+        double dist = sqrt(vsq(av)), db;
+        if (dist < r->dist_d[2 * k]) db = dist - r->dist_d[2 * k];
+        else if (dist > r->dist_d[2 * k + 1]) db = dist - r->dist_d[2 * k + 1];
+        else continue;
+        double wgt = st >= 0 ? lambda[st] : 1.0;
+        rstate(S, st, 0.5 * r->dist_fk[k] * db * db, Eprot, EQr);
+        double dv = wgt * r->dist_fk[k] * db / dist;
+        gadd(d, i, vscale(av, -dv));
+        gadd(d, j, vscale(av, dv));
+    }
+    const double deg2rad = (4.0 * atan(1.0)) / 180.0;
+    for (int k = 0; k < r->nang; ++k) {
+        int i = r->ang_ijk[3 * k], j = r->ang_ijk[3 * k + 1], l = r->ang_ijk[3 * k + 2], st = r->ang_state[k];
+        angval c = angle_calc(X(x, i), X(x, j), X(x, l));
+        double db = c.angl - r->ang_theta[k] * deg2rad;
+        double wgt = st >= 0 ? lambda[st] : 1.0;
+        rstate(S, st, 0.5 * r->ang_fk[k] * db * db, Eprot, EQr);
+        double dv = wgt * r->ang_fk[k] * db;
+        gadd(d, i, vscale(c.a, dv));
+        gadd(d, j, vscale(c.b, -dv));
+        gadd(d, l, vscale(c.c, dv));
+    }
+    v3 xw = {xwcent[0], xwcent[1], xwcent[2]};
+    for (int k = 0; k < r->nwall; ++k) {
+        int a = r->wall_ij[2 * k], b = r->wall_ij[2 * k + 1], ih = r->wall_ih[k];
+        double fk = r->wall_fk[k], d0 = r->wall_d[k], aM = r->wall_aMorse[k], dM = r->wall_dMorse[k];
+        for (int i = a; i <= b; ++i) {
+            if (!(heavy[i] || ih == 1)) continue;
+            v3 av = vsub(X(x, i), xw);
+            double dist = sqrt(vsq(av));
+            double db = dist - d0, erst, dv;
+            if (db > 0.0) {
+                erst = 0.5 * fk * db * db - dM;
+                dv = fk * db / dist;
+            } else {
+                double fexp = exp(aM * db);
+                erst = dM * (fexp * fexp - 2.0 * fexp);
+                dv = -2.0 * dM * aM * (fexp - fexp * fexp) / dist;
+            }
+            Eprot[0] += erst;
+            gadd(d, i, vscale(av, dv));
+        }
+    }
+}

@@ -141,6 +141,11 @@ struct qnb_context {
     double* h_stage = nullptr;   // pinned staging for x / d (natom*3)
     double* h_e = nullptr;       // pinned energies (nwin x (kNumE doubles + kNumE fixed))
 
+    std::vector<uint8_t> h_heavy;  // topology heavy-atom flags
+    // p_restrain (qnb_set_restraints)
+    RestrDev restr{};
+    bool have_restr = false;
+    std::vector<void*> restr_bufs;
     // offdiag (qnb_set_offdiag)
     OffdDev offd{};
     std::vector<void*> offd_bufs;
@@ -464,6 +469,9 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     // solvent template: types and charges of the first molecule
     // (aLJ_solv/bLJ_solv/chg_solv, src/simprep.f90:3616-3621) and ww_precomp
     std::vector<uint8_t> heavy_solv(kMaxSolv, 0);
+    c->h_heavy.assign(t->natom, 1);
+    if (t->heavy)
+        for (int i = 0; i < t->natom; ++i) c->h_heavy[i] = t->heavy[i] ? 1 : 0;
     if (t->nwat > 0) {
         for (int a = 0; a < sa; ++a) {
             m.wtype[a] = t->iac[ns + a];
@@ -1459,6 +1467,10 @@ int enqueue_compute(qnb_context* c, double Tfree, int istep) {
         launch_offdiag(L, c->offd);
         c->launches++;
     }
+    if (c->have_restr) {
+        timed(c, K_RESTRAIN, [&] { launch_restraints(L, c->restr, c->mixed); });
+        c->launches++;
+    }
     if (c->have_solv) {
         timed(c, K_RESTRAIN, [&] { launch_restrain_solvent(L, c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv); });
         c->launches++;
@@ -2162,6 +2174,7 @@ int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* re
                         o.water_pol = e[E_RST_POL];
                         o.fix = e[E_RST_FIX];
                         o.shell = e[E_RST_SHELL];
+                        o.protein = e[E_RST_PROT];
                         o.ekin = r[2 * kNumE];
                         o.temp = r[2 * kNumE + 1];
                         o.tfree = r[2 * kNumE + 2];
@@ -2359,13 +2372,114 @@ int qnb_get_restraint_energies(qnb_context* c, double* Er) {
     CU(cudaSetDevice(c->device));
     std::vector<double> e((size_t)kNumE * c->nwin);
     TRY(read_energies(c, c->nwin, e.data()));
+    const size_t stride = 5 + (size_t)c->S;
     for (int w = 0; w < c->nwin; ++w) {
         const double* ew = e.data() + (size_t)w * kNumE;
-        Er[4 * w] = ew[E_RST_FIX];
-        Er[4 * w + 1] = ew[E_RST_SHELL];
-        Er[4 * w + 2] = ew[E_RST_RAD];
-        Er[4 * w + 3] = ew[E_RST_POL];
+        double* o = Er + stride * w;
+        o[0] = ew[E_RST_FIX];
+        o[1] = ew[E_RST_SHELL];
+        o[2] = ew[E_RST_RAD];
+        o[3] = ew[E_RST_POL];
+        o[4] = ew[E_RST_PROT];
+        for (int st = 0; st < c->S; ++st) o[5 + st] = ew[qr_slot(st)];
     }
+    return QNB_OK;
+}
+
+int qnb_set_restraints(qnb_context* c, const qnb_restraints* r, const double* xtop) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    for (void* p : c->restr_bufs) c->release(p);
+    c->restr_bufs.clear();
+    c->restr = RestrDev{};
+    c->have_restr = false;
+    ++c->epoch;
+    if (!r) return QNB_OK;
+    const int n = c->natom, S = c->S;
+    if (r->nseq < 0 || r->npos < 0 || r->ndist < 0 || r->nang < 0 || r->nwall < 0)
+        return fail(QNB_ERR_ARG, "negative restraint count");
+    if ((r->nseq > 0 && (!r->seq_ij || !r->seq_fk || !r->seq_ih || !r->seq_mode || !xtop)) ||
+        (r->npos > 0 && (!r->pos_i || !r->pos_state || !r->pos_x || !r->pos_fk)) ||
+        (r->ndist > 0 && (!r->dist_ij || !r->dist_state || !r->dist_d || !r->dist_fk)) ||
+        (r->nang > 0 && (!r->ang_ijk || !r->ang_state || !r->ang_theta || !r->ang_fk)) ||
+        (r->nwall > 0 && (!r->wall_ij || !r->wall_d || !r->wall_fk || !r->wall_aMorse || !r->wall_dMorse || !r->wall_ih)))
+        return fail(QNB_ERR_ARG, "null restraint array");
+    auto atom = [&](int i) { return i >= 0 && i < n; };
+    auto state = [&](int st) { return st >= -1 && st < S; };
+    std::vector<int4> seq(r->nseq), dist(r->ndist), ang(r->nang), wall(r->nwall);
+    std::vector<int2> pos(r->npos);
+    std::vector<double> sfk(r->seq_fk ? r->seq_fk : nullptr, r->seq_fk ? r->seq_fk + r->nseq : nullptr);
+    std::vector<double> pxf(6 * (size_t)r->npos), dp(3 * (size_t)r->ndist), ap(2 * (size_t)r->nang),
+        wp(4 * (size_t)r->nwall);
+    for (int k = 0; k < r->nseq; ++k) {
+        int a = r->seq_ij[2 * k], b = r->seq_ij[2 * k + 1], md = r->seq_mode[k];
+        if (!atom(a) || !atom(b) || a > b || md < 0 || md > 2) return fail(QNB_ERR_ARG, "sequence restraint %d", k);
+        seq[k] = make_int4(a, b, r->seq_ih[k], md);
+    }
+    for (int k = 0; k < r->npos; ++k) {
+        if (!atom(r->pos_i[k]) || !state(r->pos_state[k])) return fail(QNB_ERR_ARG, "position restraint %d", k);
+        pos[k] = make_int2(r->pos_i[k], r->pos_state[k]);
+        for (int cc = 0; cc < 3; ++cc) {
+            pxf[6 * k + cc] = r->pos_x[3 * k + cc];
+            pxf[6 * k + 3 + cc] = r->pos_fk[3 * k + cc];
+        }
+    }
+    for (int k = 0; k < r->ndist; ++k) {
+        int a = r->dist_ij[2 * k], b = r->dist_ij[2 * k + 1];
+        if (!atom(a) || !atom(b) || !state(r->dist_state[k])) return fail(QNB_ERR_ARG, "distance restraint %d", k);
+        dist[k] = make_int4(a, b, r->dist_state[k], 0);
+        dp[3 * k] = r->dist_d[2 * k];
+        dp[3 * k + 1] = r->dist_d[2 * k + 1];
+        dp[3 * k + 2] = r->dist_fk[k];
+    }
+    const double deg2rad = 3.14159265358979323846 / 180.0;
+    for (int k = 0; k < r->nang; ++k) {
+        int a = r->ang_ijk[3 * k], b = r->ang_ijk[3 * k + 1], d = r->ang_ijk[3 * k + 2];
+        if (!atom(a) || !atom(b) || !atom(d) || !state(r->ang_state[k])) return fail(QNB_ERR_ARG, "angle restraint %d", k);
+        ang[k] = make_int4(a, b, d, r->ang_state[k]);
+        ap[2 * k] = r->ang_theta[k] * deg2rad;
+        ap[2 * k + 1] = r->ang_fk[k];
+    }
+    for (int k = 0; k < r->nwall; ++k) {
+        int a = r->wall_ij[2 * k], b = r->wall_ij[2 * k + 1];
+        if (!atom(a) || !atom(b) || a > b) return fail(QNB_ERR_ARG, "wall restraint %d", k);
+        wall[k] = make_int4(a, b, r->wall_ih[k], 0);
+        wp[4 * k] = r->wall_d[k];
+        wp[4 * k + 1] = r->wall_fk[k];
+        wp[4 * k + 2] = r->wall_aMorse[k];
+        wp[4 * k + 3] = r->wall_dMorse[k];
+    }
+    RestrDev d{};
+    d.nseq = r->nseq; d.npos = r->npos; d.ndist = r->ndist; d.nang = r->nang; d.nwall = r->nwall;
+    auto up = [&](auto** dst, const auto& vec) -> int {
+        int rc = c->upload(dst, vec);
+        if (!rc) c->restr_bufs.push_back((void*)*dst);
+        return rc;
+    };
+    std::vector<double> xt(xtop ? xtop : nullptr, xtop ? xtop + 3 * (size_t)n : nullptr);
+    std::vector<double> mass(n, 0.0);
+    const std::vector<uint8_t>& heavy = c->h_heavy;
+    if (c->md_ready) CU(cudaMemcpy(mass.data(), c->md.mass, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < r->nseq; ++k)
+        if (seq[k].w == 1 || seq[k].w == 2)
+            for (int i = seq[k].x; i <= seq[k].y; ++i)
+                if (!(mass[i] > 0.0)) return fail(QNB_ERR_STATE, "centre restraints need the masses (qnb_md_init first)");
+    TRY(up((int4**)&d.seq, seq));
+    TRY(up((double**)&d.seq_fk, sfk));
+    TRY(up((int2**)&d.pos, pos));
+    TRY(up((double**)&d.pos_xfk, pxf));
+    TRY(up((int4**)&d.dist, dist));
+    TRY(up((double**)&d.dist_p, dp));
+    TRY(up((int4**)&d.ang, ang));
+    TRY(up((double**)&d.ang_p, ap));
+    TRY(up((int4**)&d.wall, wall));
+    TRY(up((double**)&d.wall_p, wp));
+    TRY(up((double**)&d.xtop, xt));
+    TRY(up((double**)&d.mass, mass));
+    TRY(up((uint8_t**)&d.heavy, heavy));
+    c->restr = d;
+    c->have_restr = (r->nseq + r->npos + r->ndist + r->nang + r->nwall) > 0;
     return QNB_OK;
 }
 

@@ -19,7 +19,7 @@ constexpr float kFixF = 4294967296.0f;
 // energy slots (doubles in FP64 mode, 2^-32 fixed point in mixed mode)
 enum {
     E_PP_EL = 0, E_PP_VDW, E_PW_EL, E_PW_VDW, E_WW_EL, E_WW_VDW, E_LRF,
-    E_RST_RAD, E_RST_POL, E_RST_FIX, E_RST_SHELL, E_Q0
+    E_RST_RAD, E_RST_POL, E_RST_FIX, E_RST_SHELL, E_RST_PROT, E_Q0
 };
 __host__ __device__ constexpr int eq_slot(int s, int k) { return E_Q0 + 6 * s + k; }
 // bonded: solute bond, angle, torsion, improper, then the same for solvent;
@@ -27,7 +27,9 @@ __host__ __device__ constexpr int eq_slot(int s, int k) { return E_Q0 + 6 * s + 
 constexpr int E_B0 = E_Q0 + 6 * kMaxStates;
 constexpr int E_QB0 = E_B0 + 8;
 __host__ __device__ constexpr int qb_slot(int s, int k) { return E_QB0 + 4 * s + k; }
-constexpr int kNumE = E_QB0 + 4 * kMaxStates;
+constexpr int E_QR0 = E_QB0 + 4 * kMaxStates;   // per state: EQ(s)%restraint
+__host__ __device__ constexpr int qr_slot(int s) { return E_QR0 + s; }
+constexpr int kNumE = E_QR0 + kMaxStates;
 
 // list counters (entries at list granularity, plus reference atom-pair counts)
 enum { C_WW = 0, C_PW, C_PP, C_QP, C_QW, C_PP14, C_PPG,
@@ -253,6 +255,24 @@ struct BondedDev {
     int nterms;             // classical terms + Q terms x states
 };
 void launch_bonded(const Launch& L, const BondedDev& b, int mixed);
+// p_restrain: the input's restraint sections
+struct RestrDev {
+    int nseq, npos, ndist, nang, nwall;
+    const int4* seq;        // first, last, include-hydrogens, mode
+    const double* seq_fk;
+    const int2* pos;        // atom, state (-1 all)
+    const double* pos_xfk;  // [6n] x0 y0 z0 fkx fky fkz
+    const int4* dist;       // i, j, state, -
+    const double* dist_p;   // [3n] d1 d2 fk
+    const int4* ang;        // i, j, k, state
+    const double* ang_p;    // [2n] theta0 (rad) fk
+    const int4* wall;       // first, last, include-hydrogens, -
+    const double* wall_p;   // [4n] d fk aMorse dMorse
+    const double* xtop;     // [natom*3]
+    const double* mass;     // [natom]
+    const uint8_t* heavy;   // [natom]
+};
+void launch_restraints(const Launch& L, const RestrDev& r, int mixed);
 // offdiag: Hij = A exp(-mu r_kl) per window, out[(w*n + io)*2] = Hij, rkl
 struct OffdDev {
     int n;

@@ -3337,6 +3337,161 @@ void launch_offdiag(const Launch& L, const OffdDev& o) {
     if (o.n == 0) return;
     k_offdiag<<<dim3((o.n + 63) / 64, L.nwin), 64, 0, L.st>>>(L.ds, o);
 }
+// p_restrain, src/bondene.f90:764-1020 (FP64 in both forms).  Blocks
+// [0, nseq) take one sequence restraint each (the centre modes sum their
+// atoms in a fixed-order tree), blocks [nseq, nseq + nwall) one wall
+// restraint each, the rest the position / distance / angle restraints.
+template <bool MIX>
+__device__ __forceinline__ void restr_energy(const Acc<MIX>& acc, int slot, double e) {
+    if constexpr (MIX) acc.energy_fix(slot, to_fixd(e));
+    else acc.energy(slot, e);
+}
+template <bool MIX>
+__device__ __forceinline__ void restr_grad(const Acc<MIX>& acc, int i, double gx, double gy, double gz) {
+    if constexpr (MIX) acc.gradd(i, gx, gy, gz);
+    else acc.grad(i, gx, gy, gz);
+}
+// a state-dependent restraint's energy: every state's EQ(s)%restraint for
+// state -1 (E%restraint%protein without states), else that state's
+template <bool MIX>
+__device__ __forceinline__ void restr_state_energy(const Acc<MIX>& acc, int S, int st, double e) {
+    if (st >= 0) restr_energy<MIX>(acc, qr_slot(st), e);
+    else if (S == 0) restr_energy<MIX>(acc, E_RST_PROT, e);
+    else
+        for (int k = 0; k < S; ++k) restr_energy<MIX>(acc, qr_slot(k), e);
+}
+constexpr int kRestrBlock = 128;
+template <bool MIX>
+__global__ void __launch_bounds__(kRestrBlock) k_restraints(DevModel m, const DevState* __restrict__ states, RestrDev r) {
+    const DevState& s = states[blockIdx.y];
+    const Acc<MIX> acc = make_acc<MIX>(s);
+    const double* __restrict__ x = s.x;
+    const int b = blockIdx.x;
+    if (b < r.nseq + r.nwall) {
+        const bool wall = b >= r.nseq;
+        const int4 q = wall ? r.wall[b - r.nseq] : r.seq[b];
+        const int first = q.x, last = q.y, ih = q.z, mode = wall ? 0 : q.w;
+        auto pick = [&](int i) { return r.heavy[i] || ih == 1; };
+        if (wall) {   // half-harmonic wall about xwcent, Morse inside
+            const double* p = r.wall_p + 4 * (b - r.nseq);
+            const double d0 = p[0], fk = p[1], aM = p[2], dM = p[3];
+            ESum<MIX> e;
+            for (int i = first + threadIdx.x; i <= last; i += kRestrBlock) {
+                if (!pick(i)) continue;
+                double vx = x[3 * i] - m.xwcent[0], vy = x[3 * i + 1] - m.xwcent[1], vz = x[3 * i + 2] - m.xwcent[2];
+                double dist = sqrt(vx * vx + vy * vy + vz * vz);
+                double db = dist - d0, erst, dv;
+                if (db > 0.0) {
+                    erst = 0.5 * fk * db * db - dM;
+                    dv = fk * db / dist;
+                } else {
+                    double fexp = exp(aM * db);
+                    erst = dM * (fexp * fexp - 2.0 * fexp);
+                    dv = -2.0 * dM * aM * (fexp - fexp * fexp) / dist;
+                }
+                e.add(erst);
+                restr_grad<MIX>(acc, i, vx * dv, vy * dv, vz * dv);
+            }
+            e.flush(acc, E_RST_PROT);
+            return;
+        }
+        const double fk = r.seq_fk[b];
+        if (mode == 0) {   // each atom to its topology position
+            ESum<MIX> e;
+            for (int i = first + threadIdx.x; i <= last; i += kRestrBlock) {
+                if (!pick(i)) continue;
+                double dx = x[3 * i] - r.xtop[3 * i], dy = x[3 * i + 1] - r.xtop[3 * i + 1],
+                       dz = x[3 * i + 2] - r.xtop[3 * i + 2];
+                e.add(0.5 * fk * (dx * dx + dy * dy + dz * dz));
+                restr_grad<MIX>(acc, i, dx * fk, dy * fk, dz * fk);
+            }
+            e.flush(acc, E_RST_PROT);
+            return;
+        }
+        // geometric (1) or mass (2) centre of the picked atoms
+        __shared__ double red[4][kRestrBlock];
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int i = first + threadIdx.x; i <= last; i += kRestrBlock) {
+            if (!pick(i)) continue;
+            const double w = mode == 2 ? r.mass[i] : 1.0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) a[c] += (x[3 * i + c] - r.xtop[3 * i + c]) * w;
+            a[3] += w;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = a[k];
+        __syncthreads();
+        for (int h = kRestrBlock / 2; h > 0; h >>= 1) {
+            if (threadIdx.x < h)
+#pragma unroll
+                for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+            __syncthreads();
+        }
+        const double tot = red[3][0];
+        if (tot <= 0.0) return;
+        const double drx = red[0][0] / tot, dry = red[1][0] / tot, drz = red[2][0] / tot;
+        if (threadIdx.x == 0) restr_energy<MIX>(acc, E_RST_PROT, 0.5 * fk * (drx * drx + dry * dry + drz * drz));
+        for (int i = first + threadIdx.x; i <= last; i += kRestrBlock) {
+            if (!pick(i)) continue;
+            const double f = mode == 2 ? fk : fk * r.mass[i] / 12.010;   // the reference's geometric-centre force
+            restr_grad<MIX>(acc, i, drx * f, dry * f, drz * f);
+        }
+        return;
+    }
+    const int nterm = r.npos + r.ndist + r.nang;
+    const int S = m.S;
+    for (int t = (b - r.nseq - r.nwall) * kRestrBlock + threadIdx.x; t < nterm;
+         t += (gridDim.x - r.nseq - r.nwall) * kRestrBlock) {
+        if (t < r.npos) {   // position restraint
+            int2 q = r.pos[t];
+            const double* p = r.pos_xfk + 6 * t;
+            const int i = q.x, st = q.y;
+            double dx = x[3 * i] - p[0], dy = x[3 * i + 1] - p[1], dz = x[3 * i + 2] - p[2];
+            const double wgt = st >= 0 ? s.lambda[st] : 1.0;
+            restr_state_energy<MIX>(acc, S, st, 0.5 * (p[3] * (dx * dx) + p[4] * (dy * dy) + p[5] * (dz * dz)));
+            restr_grad<MIX>(acc, i, p[3] * dx * wgt, p[4] * dy * wgt, p[5] * dz * wgt);
+            continue;
+        }
+        int u = t - r.npos;
+        if (u < r.ndist) {   // flat-bottom distance restraint
+            int4 q = r.dist[u];
+            const double* p = r.dist_p + 3 * u;
+            double vx = x[3 * q.y] - x[3 * q.x], vy = x[3 * q.y + 1] - x[3 * q.x + 1], vz = x[3 * q.y + 2] - x[3 * q.x + 2];
+            double dist = sqrt(vx * vx + vy * vy + vz * vz);
+            double db;
+            if (dist < p[0]) db = dist - p[0];
+            else if (dist > p[1]) db = dist - p[1];
+            else continue;
+            const double wgt = q.z >= 0 ? s.lambda[q.z] : 1.0;
+            restr_state_energy<MIX>(acc, S, q.z, 0.5 * p[2] * db * db);
+            double dv = wgt * p[2] * db / dist;
+            restr_grad<MIX>(acc, q.x, -vx * dv, -vy * dv, -vz * dv);
+            restr_grad<MIX>(acc, q.y, vx * dv, vy * dv, vz * dv);
+            continue;
+        }
+        u -= r.ndist;
+        {   // angle restraint
+            int4 q = r.ang[u];
+            const double* p = r.ang_p + 2 * u;
+            AngleVal<double> c = angle_calc(atom_pos<false>(s, q.x), atom_pos<false>(s, q.y), atom_pos<false>(s, q.z));
+            double db = c.angl - p[0];
+            const double wgt = q.w >= 0 ? s.lambda[q.w] : 1.0;
+            restr_state_energy<MIX>(acc, S, q.w, 0.5 * p[1] * db * db);
+            double dv = wgt * p[1] * db;
+            restr_grad<MIX>(acc, q.x, c.a.x * dv, c.a.y * dv, c.a.z * dv);
+            restr_grad<MIX>(acc, q.y, -c.b.x * dv, -c.b.y * dv, -c.b.z * dv);
+            restr_grad<MIX>(acc, q.z, c.c.x * dv, c.c.y * dv, c.c.z * dv);
+        }
+    }
+}
+void launch_restraints(const Launch& L, const RestrDev& r, int mixed) {
+    const int nterm = r.npos + r.ndist + r.nang;
+    const int nb = r.nseq + r.nwall + std::min(64, (nterm + kRestrBlock - 1) / kRestrBlock);
+    if (nb == 0) return;
+    dim3 g(nb, L.nwin);
+    if (mixed) k_restraints<true><<<g, kRestrBlock, 0, L.st>>>(L.m, L.ds, r);
+    else k_restraints<false><<<g, kRestrBlock, 0, L.st>>>(L.m, L.ds, r);
+}
 void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree, int mixed, const int* wsw,
                              const uint8_t* heavy_solv) {
     if (L.m.nwat == 0) return;

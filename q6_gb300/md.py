@@ -40,7 +40,7 @@ class QnbMdParams(ctypes.Structure):
 # qnb_md_record
 MD_RECORD = np.dtype([("E", "<f8", 7), ("solvent_radial", "<f8"), ("water_pol", "<f8"), ("ekin", "<f8"),
                       ("temp", "<f8"), ("tfree", "<f8"), ("shake_iterations", "<f8"), ("fix", "<f8"),
-                      ("shell", "<f8")])
+                      ("shell", "<f8"), ("protein", "<f8")])
 
 
 @dataclass

@@ -41,7 +41,7 @@ EXPORTED = (
     "qnb_profile_classes", "qnb_set_solvent_internal", "qnb_autotune", "qnb_get_tuning", "qnb_set_tuning",
     "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
     "qnb_set_bonded", "qnb_get_bonded_energies", "qnb_md_minimize", "qnb_set_shell_restraint",
-    "qnb_get_restraint_energies", "qnb_set_offdiag", "qnb_get_offdiag",
+    "qnb_get_restraint_energies", "qnb_set_offdiag", "qnb_get_offdiag", "qnb_set_restraints",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -99,7 +99,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_set_bonded": [P, P], "qnb_get_bonded_energies": [P, P, P],
         "qnb_md_minimize": [P, I32, D, D, D, P],
         "qnb_set_shell_restraint": [P, P, P, D, D], "qnb_get_restraint_energies": [P, P],
-        "qnb_set_offdiag": [P, I32, P, P, P, P], "qnb_get_offdiag": [P, P, P],
+        "qnb_set_offdiag": [P, I32, P, P, P, P], "qnb_get_offdiag": [P, P, P], "qnb_set_restraints": [P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -386,10 +386,21 @@ class NonbondedEngine:
         self._check(self.lib.qnb_set_shell_restraint(self.h, _p(xt), _p(sh), float(fk_fix), float(fk_pshell)))
 
     def restraint_energies(self):
-        """[nwin][4]: fix, shell, solvent_radial, water_pol of the last evaluation."""
-        Er = np.zeros((self.nwin, 4))
+        """[nwin][5 + nstates]: fix, shell, solvent_radial, water_pol, protein,
+        then EQ(s)%restraint, of the last evaluation."""
+        Er = np.zeros((self.nwin, 5 + self.S))
         self._check(self.lib.qnb_get_restraint_energies(self.h, _p(Er)))
         return Er
+
+    def set_restraints(self, r, xtop=None):
+        """qnb_set_restraints from a q6_gb300.restraints.Restraints (None
+        removes them); xtop defaults to the topology coordinates."""
+        if r is None:
+            self._check(self.lib.qnb_set_restraints(self.h, None, None))
+            return
+        st, keep = r.to_struct()
+        xt = np.ascontiguousarray(self.s.x if xtop is None else xtop, dtype=np.float64)
+        self._check(self.lib.qnb_set_restraints(self.h, ctypes.byref(st), _p(xt)))
 
     # ---- bonded terms ------------------------------------------------------
     def set_bonded(self, bt):

@@ -59,7 +59,9 @@ def test_md_struct_offsets_match_c_compiler(tmp_path):
     if not shutil.which("gcc"):
         pytest.skip("no C compiler")
     from q6_gb300.bonded import QnbBonded
+    from q6_gb300.restraints import QnbRestraints
     bnames = [f[0] for f in QnbBonded._fields_]
+    rnames = [f[0] for f in QnbRestraints._fields_]
     names = [f[0] for f in QnbMdParams._fields_]
     rec = list(MD_RECORD.names)
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "qnb.h"', "int main(void) {",
@@ -69,6 +71,8 @@ def test_md_struct_offsets_match_c_compiler(tmp_path):
     src += ['printf("%%zu\\n", offsetof(qnb_md_record, %s));' % n for n in rec[1:]]
     src += ['printf("%zu\\n", sizeof(qnb_bonded));']
     src += ['printf("%%zu\\n", offsetof(qnb_bonded, %s));' % n for n in bnames]
+    src += ['printf("%zu\\n", sizeof(qnb_restraints));']
+    src += ['printf("%%zu\\n", offsetof(qnb_restraints, %s));' % n for n in rnames]
     src += ["return 0; }"]
     c = tmp_path / "lay.c"
     c.write_text("\n".join(src))
@@ -82,7 +86,10 @@ def test_md_struct_offsets_match_c_compiler(tmp_path):
     assert out[k + 1:k + 1 + len(rec)] == [MD_RECORD.fields[n][1] for n in rec]
     k += 1 + len(rec)
     assert out[k] == ctypes.sizeof(QnbBonded)
-    assert out[k + 1:] == [getattr(QnbBonded, n).offset for n in bnames]
+    assert out[k + 1:k + 1 + len(bnames)] == [getattr(QnbBonded, n).offset for n in bnames]
+    k += 1 + len(bnames)
+    assert out[k] == ctypes.sizeof(QnbRestraints)
+    assert out[k + 1:] == [getattr(QnbRestraints, n).offset for n in rnames]
 
 
 def test_create_fails_loudly_without_gpu_or_bad_args():
