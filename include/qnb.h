@@ -422,6 +422,37 @@ int qnb_set_offdiag(qnb_context* ctx, int32_t n, const int32_t* states, const in
                     const double* mu);
 int qnb_get_offdiag(qnb_context* ctx, double* Hij, double* rkl);
 
+/* Monitor groups, the [nonbonded_monitor] input section: nbmonitorlist +
+   nonbond_monitor (src/nonbondene.f90:4517-4680).  ngroups atom groups of
+   solute atoms (group g = atoms[group_first[g] .. group_first[g+1]), 0-based)
+   and npairs pairs of them (pairs[2k], pairs[2k+1]).  Per pair and state the
+   Coulomb and LJ energies of every interacting atom pair between the two
+   groups, with the parameters the force loops use: Q-Q pairs the static
+   Q-Q entry (soft pairs, soft-core), Q-P pairs the q-p or Q-bonded-P values,
+   P-P pairs pp_precomp's (1-4 scaled, excluded pairs left out).  Evaluated
+   inside qnb_compute_dev and every qnb_md_run step (FP64); npairs = 0
+   removes them.  qnb_get_monitor_energies returns the last evaluation,
+   out[((w*npairs + k)*nstates + s)*2 + {0: Vel, 1: Vlj}].  Two index slips
+   of nbmonitorlist are not reproduced: its P-P branch indexes pp_map by the
+   loop counters and its Q-P branch qp_precomp with the arguments swapped;
+   both take the two atoms' own pair values here. */
+int qnb_set_monitor_groups(qnb_context* ctx, int32_t ngroups, const int32_t* group_first, const int32_t* atoms,
+                           int32_t npairs, const int32_t* pairs);
+int qnb_get_monitor_energies(qnb_context* ctx, double* out);
+
+/* Group contributions, the [group_contribution] input section: exc_assign +
+   calculate_exc (src/simprep.f90:2879-2945, src/nonbondene.f90:6825-6920).
+   mask[g*nat_solute + i] != 0 puts solute atom i in group g.  Per group and
+   state the energies of the interactions calculate_exc subtracts from EQ:
+   every Q-Q pair with an atom in the group, and every pair of a Q atom with
+   a non-Q solute atom of the group (Q-bonded-P pairs included), at any
+   distance.  out[((w*ngroups + g)*nstates + s)*4 + {0: qq el, 1: qq vdw,
+   2: qp el, 3: qp vdw}]; the energy file's array of the group holds EQ minus
+   these (el, vdw or both by the group's calculation type).  ngroups = 0
+   removes them. */
+int qnb_set_group_exclusions(qnb_context* ctx, int32_t ngroups, const uint8_t* mask);
+int qnb_get_group_exclusions(qnb_context* ctx, double* out);
+
 /* fix_shell (src/potene.f90:386-423), evaluated inside qnb_compute_dev and
    qnb_md_run once set: excluded atoms (the topology's excl flags) with
    fk_fix and shell atoms (shell[i] != 0, as make_shell / make_shell2 mark

@@ -149,6 +149,28 @@ struct qnb_context {
     // offdiag (qnb_set_offdiag)
     OffdDev offd{};
     std::vector<void*> offd_bufs;
+    // pair parameters kept from build_model for the listed pair sets
+    struct PairSrc {
+        std::vector<QQEntry> qq;        // the static Q-Q and Q-bonded-P entries (qq first, nqq_qq of them)
+        std::vector<QPar> qp;           // [nat_solute][nqat][S] (Q atoms with atoms not bonded/angled to Q)
+        std::vector<uint8_t> qp_set;    // same layout
+        std::vector<uint8_t> qnear;     // [natom] bonded/angled to a Q atom in some state
+        std::vector<int> iqatom;        // [natom] Q index or -1
+        std::vector<int> iqseq;         // [nqat] atom of each Q atom
+        std::vector<double> crg;        // [natom]
+        std::vector<int> iac;           // [natom]
+        std::vector<double2> lj;        // [3][nt][nt]
+        std::vector<uint8_t> ljcod;     // [nt][nt]
+        std::vector<std::pair<long long, int>> special;   // (i*natom + j, 1 excluded | 3 1-4), i < j, sorted
+        int nt = 0;
+        double el14 = 1.0;
+    } psrc;
+    // monitor groups and group contributions (one device list, monitor slots first)
+    std::vector<PairSetEntry> mon_e, exc_e;
+    std::vector<int> mon_first, exc_first;   // per slot entry counts turned into offsets
+    int mon_pairs = 0, exc_groups = 0;
+    PairSetDev psets{};
+    std::vector<void*> pset_bufs;
     // fix_shell (qnb_set_shell_restraint)
     bool have_shell = false;
     uint8_t* d_shell_flags = nullptr;
@@ -541,6 +563,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     };
     // qp_int_comp, src/simprep.f90:3112-3148 (atoms not bonded/angled to Q)
     std::vector<QPar> qp_tab((size_t)std::max(ns, 1) * std::max(nq, 1) * std::max(S, 1));
+    std::vector<uint8_t> qp_set(qp_tab.size(), 0);
     if (nq > 0)
         for (int ig = 0; ig < ns; ++ig) {
             if (qnear[ig]) continue;
@@ -550,6 +573,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                     if (QC(s, ig, jq) == 4) vdw = 3;   // kept for later states, as the reference does
                     int set;
                     qp_tab[((size_t)ig * nq + jq) * S + s] = qp_values(jq, ig, s, vdw, &set);
+                    qp_set[((size_t)ig * nq + jq) * S + s] = (uint8_t)set;
                 }
             }
         }
@@ -745,6 +769,23 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     }
     c->nqq = (int)qq.size();
     c->nqq_qq = nqq_qq;
+    {   // parameter sources of the listed pair sets (monitors, group contributions)
+        auto& ps = c->psrc;
+        ps.qq = qq;
+        ps.qp = qp_tab;
+        ps.qp_set = qp_set;
+        ps.qnear = qnear;
+        ps.iqatom = iqatom;
+        ps.iqseq.assign(t->iqseq, t->iqseq + nq);
+        ps.crg.assign(t->crg, t->crg + natom);
+        ps.iac.assign(t->iac, t->iac + natom);
+        ps.lj = lj;
+        ps.ljcod = ljcod;
+        ps.nt = nt;
+        ps.el14 = t->el14_scale;
+        ps.special.clear();
+        for (const Sp& q : sp) ps.special.emplace_back((long long)q.i * natom + q.j, q.k);
+    }
     TRY(c->upload(&c->st_qq, qq));
     std::vector<float4> qqf(qq.size());
     for (size_t k = 0; k < qq.size(); ++k)
@@ -1465,6 +1506,10 @@ int enqueue_compute(qnb_context* c, double Tfree, int istep) {
     }
     if (c->offd.n > 0) {
         launch_offdiag(L, c->offd);
+        c->launches++;
+    }
+    if (c->psets.nslots > 0) {
+        launch_pair_sets(L, c->psets);
         c->launches++;
     }
     if (c->have_restr) {
@@ -2537,6 +2582,217 @@ int qnb_get_offdiag(qnb_context* c, double* Hij, double* rkl) {
         if (rkl) rkl[k] = v[2 * k + 1];
     }
     return QNB_OK;
+}
+
+}  // extern "C"
+
+// ---- listed pair sets: monitor groups and group contributions --------------
+namespace {
+PairSetEntry pset_entry(int i, int j, int soft, double A, double B, double el, double sc) {
+    PairSetEntry e{};
+    e.i = i;
+    e.j = j;
+    e.soft = soft;
+    e.A = A;
+    e.B = B;
+    e.el = el;
+    e.sc = sc;
+    return e;
+}
+// the static Q-Q entry of Q atoms a < b (atom indices) in state s, or -1
+int find_qq(const qnb_context* c, int a, int b, int s) {
+    const auto& qq = c->psrc.qq;
+    for (int k = 0; k < c->nqq_qq; ++k)
+        if (qq[k].s == s && ((qq[k].i == a && qq[k].j == b) || (qq[k].i == b && qq[k].j == a))) return k;
+    return -1;
+}
+// the Q-bonded-P entry of Q atom qa and solute atom j in state s, or -1
+int find_qqp(const qnb_context* c, int qa, int j, int s) {
+    const auto& qq = c->psrc.qq;
+    for (int k = c->nqq_qq; k < (int)qq.size(); ++k)
+        if (qq[k].s == s && qq[k].i == qa && qq[k].j == j) return k;
+    return -1;
+}
+// Q atom (Q index iq) with non-Q solute atom j in state s: the Q-bonded-P
+// entry when j is bonded or angled to a Q atom, else the q-p table; false
+// when the pair does not interact (precompute's `set` off, or 1-2/1-3 to Q)
+bool q_pair(const qnb_context* c, int iq, int j, int s, PairSetEntry* e) {
+    const auto& ps = c->psrc;
+    const int nq = c->nqat, S = c->S;
+    const int qa = ps.iqseq[iq];
+    if (ps.qnear[j]) {
+        int k = find_qqp(c, qa, j, s);
+        if (k < 0) return false;
+        const QQEntry& q = ps.qq[k];
+        *e = pset_entry(qa, j, 0, q.A, q.B, q.el, q.sc);
+        return true;
+    }
+    size_t o = ((size_t)j * nq + iq) * S + s;
+    if (!ps.qp_set[o]) return false;
+    const QPar& p = ps.qp[o];
+    *e = pset_entry(qa, j, 0, p.A, p.B, p.el, p.sc);
+    return true;
+}
+// two non-Q solute atoms: pp_precomp's values (src/simprep.f90:3321-3351);
+// false for excluded pairs and pairs that do not interact
+bool p_pair(const qnb_context* c, int a, int b, PairSetEntry* e) {
+    const auto& ps = c->psrc;
+    int i = std::min(a, b), j = std::max(a, b);
+    long long key = (long long)i * c->natom + j;
+    auto it = std::lower_bound(ps.special.begin(), ps.special.end(), std::make_pair(key, 0));
+    int code = ps.ljcod[(size_t)ps.iac[i] * ps.nt + ps.iac[j]];
+    if (it != ps.special.end() && it->first == key) {
+        if (it->second == 1) return false;
+        code = 3;
+    }
+    double2 lj = ps.lj[((size_t)(code - 1) * ps.nt + ps.iac[i]) * ps.nt + ps.iac[j]];
+    double el = ps.crg[i] * ps.crg[j];
+    if (!(fabs(lj.x) > kQrealEps || fabs(lj.y) > kQrealEps || fabs(el) > kQrealEps)) return false;
+    if (code == 3) el *= ps.el14;
+    *e = pset_entry(i, j, 0, lj.x, lj.y, el, 0.0);
+    return true;
+}
+// concatenates the monitor and exclusion lists into the device list
+int upload_pair_sets(qnb_context* c) {
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    for (void* p : c->pset_bufs) c->release(p);
+    c->pset_bufs.clear();
+    c->psets = PairSetDev{};
+    ++c->epoch;
+    const int nslots = (int)(c->mon_first.size() + c->exc_first.size());
+    if (nslots == 0) return QNB_OK;
+    std::vector<PairSetEntry> e(c->mon_e);
+    e.insert(e.end(), c->exc_e.begin(), c->exc_e.end());
+    if (e.empty()) e.push_back(PairSetEntry{});   // keeps the buffer non-empty
+    std::vector<int> first(1, 0);
+    for (int n : c->mon_first) first.push_back(first.back() + n);
+    for (int n : c->exc_first) first.push_back(first.back() + n);
+    PairSetDev p{};
+    p.nslots = nslots;
+    TRY(c->upload((PairSetEntry**)&p.e, e));
+    c->pset_bufs.push_back((void*)p.e);
+    TRY(c->upload((int**)&p.slot_first, first));
+    c->pset_bufs.push_back((void*)p.slot_first);
+    TRY(c->alloc(&p.out, (size_t)2 * nslots * c->nwin));
+    c->pset_bufs.push_back((void*)p.out);
+    CU(cudaMemset(p.out, 0, sizeof(double) * 2 * nslots * c->nwin));
+    c->psets = p;
+    return QNB_OK;
+}
+int read_pair_sets(qnb_context* c, int first, int n, double* out) {
+    CU(cudaSetDevice(c->device));
+    if (n == 0 || c->psets.nslots == 0) return QNB_OK;
+    std::vector<double> v((size_t)2 * c->psets.nslots * c->nwin);
+    CU(cudaMemcpyAsync(v.data(), c->psets.out, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    for (int w = 0; w < c->nwin; ++w)
+        for (int k = 0; k < n; ++k) {
+            out[((size_t)w * n + k) * 2] = v[((size_t)w * c->psets.nslots + first + k) * 2];
+            out[((size_t)w * n + k) * 2 + 1] = v[((size_t)w * c->psets.nslots + first + k) * 2 + 1];
+        }
+    return QNB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int qnb_set_monitor_groups(qnb_context* c, int32_t ngroups, const int32_t* group_first, const int32_t* atoms,
+                           int32_t npairs, const int32_t* pairs) {
+    if (!c || ngroups < 0 || npairs < 0 || (npairs > 0 && (!group_first || !atoms || !pairs)))
+        return fail(QNB_ERR_ARG, "null argument");
+    for (int g = 0; npairs > 0 && g < ngroups; ++g) {
+        if (group_first[g] < 0 || group_first[g + 1] < group_first[g])
+            return fail(QNB_ERR_ARG, "monitor group %d: bad group_first", g);
+        for (int k = group_first[g]; k < group_first[g + 1]; ++k)
+            if (atoms[k] < 0 || atoms[k] >= c->nat_solute)
+                return fail(QNB_ERR_ARG, "monitor group %d: atom %d is not a solute atom", g, atoms[k]);
+    }
+    for (int p = 0; p < npairs; ++p)
+        if (pairs[2 * p] < 0 || pairs[2 * p] >= ngroups || pairs[2 * p + 1] < 0 || pairs[2 * p + 1] >= ngroups)
+            return fail(QNB_ERR_ARG, "monitor pair %d: group out of range", p);
+    const auto& ps = c->psrc;
+    const int S = c->S;
+    std::vector<PairSetEntry> ent;
+    std::vector<int> cnt;
+    // nbmonitorlist, src/nonbondene.f90:4517-4630: per pair and state, every
+    // interacting atom pair of the two groups
+    for (int p = 0; p < npairs; ++p) {
+        const int gi = pairs[2 * p], gj = pairs[2 * p + 1];
+        std::vector<std::vector<PairSetEntry>> per(S);
+        for (int a = group_first[gi]; a < group_first[gi + 1]; ++a)
+            for (int b = group_first[gj]; b < group_first[gj + 1]; ++b) {
+                const int i = atoms[a], j = atoms[b];
+                if (i == j) return fail(QNB_ERR_ARG, "two paired monitor atom groups contain the same atom %d", i);
+                const int qi = ps.iqatom[i], qj = ps.iqatom[j];
+                PairSetEntry e;
+                for (int s = 0; s < S; ++s) {
+                    if (qi >= 0 && qj >= 0) {
+                        int k = find_qq(c, std::min(i, j), std::max(i, j), s);
+                        if (k < 0) continue;
+                        const QQEntry& q = ps.qq[k];
+                        per[s].push_back(pset_entry(q.i, q.j, q.soft, q.A, q.B, q.el, q.sc));
+                    } else if (qi >= 0 || qj >= 0) {
+                        if (q_pair(c, qi >= 0 ? qi : qj, qi >= 0 ? j : i, s, &e)) per[s].push_back(e);
+                    } else if (p_pair(c, i, j, &e)) {
+                        per[s].push_back(e);
+                    }
+                }
+            }
+        for (int s = 0; s < S; ++s) {
+            cnt.push_back((int)per[s].size());
+            ent.insert(ent.end(), per[s].begin(), per[s].end());
+        }
+    }
+    c->mon_e.swap(ent);
+    c->mon_first.swap(cnt);
+    c->mon_pairs = npairs;
+    return upload_pair_sets(c);
+}
+
+int qnb_get_monitor_energies(qnb_context* c, double* out) {
+    if (!c || (!out && c->mon_pairs > 0)) return fail(QNB_ERR_ARG, "null argument");
+    return read_pair_sets(c, 0, c->mon_pairs * c->S, out);
+}
+
+int qnb_set_group_exclusions(qnb_context* c, int32_t ngroups, const uint8_t* mask) {
+    if (!c || ngroups < 0 || (ngroups > 0 && !mask)) return fail(QNB_ERR_ARG, "null argument");
+    const auto& ps = c->psrc;
+    const int S = c->S, nq = c->nqat, ns = c->nat_solute;
+    std::vector<PairSetEntry> ent;
+    std::vector<int> cnt;
+    // per group and state two slots: the Q-Q pairs with an atom in the group,
+    // then the Q-P pairs (Q-bonded-P and plain) whose solute atom is in it
+    for (int g = 0; g < ngroups; ++g) {
+        const uint8_t* mk = mask + (size_t)g * ns;
+        for (int s = 0; s < S; ++s) {
+            int n0 = (int)ent.size();
+            for (int k = 0; k < c->nqq_qq; ++k) {
+                const QQEntry& q = ps.qq[k];
+                if (q.s == s && (mk[q.i] || mk[q.j]))
+                    ent.push_back(pset_entry(q.i, q.j, q.soft, q.A, q.B, q.el, q.sc));
+            }
+            cnt.push_back((int)ent.size() - n0);
+            n0 = (int)ent.size();
+            for (int j = 0; j < ns; ++j) {
+                if (!mk[j] || ps.iqatom[j] >= 0) continue;
+                for (int iq = 0; iq < nq; ++iq) {
+                    PairSetEntry e;
+                    if (q_pair(c, iq, j, s, &e)) ent.push_back(e);
+                }
+            }
+            cnt.push_back((int)ent.size() - n0);
+        }
+    }
+    c->exc_e.swap(ent);
+    c->exc_first.swap(cnt);
+    c->exc_groups = ngroups;
+    return upload_pair_sets(c);
+}
+
+int qnb_get_group_exclusions(qnb_context* c, double* out) {
+    if (!c || (!out && c->exc_groups > 0)) return fail(QNB_ERR_ARG, "null argument");
+    return read_pair_sets(c, c->mon_pairs * c->S, c->exc_groups * c->S * 2, out);
 }
 
 }  // extern "C"

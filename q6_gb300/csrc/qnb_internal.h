@@ -281,6 +281,20 @@ struct OffdDev {
     double* out;             // [nwin][n][2]
 };
 void launch_offdiag(const Launch& L, const OffdDev& o);
+// listed pair energies (monitor groups, group-contribution exclusions): the
+// entries of slot k are [slot_first[k], slot_first[k+1]); each slot's Coulomb
+// and LJ sums are written to out[(w*nslots + k)*2 + {0,1}]
+struct alignas(16) PairSetEntry {
+    int i, j, soft, pad;
+    double A, B, el, sc;
+};
+struct PairSetDev {
+    int nslots;
+    const PairSetEntry* e;
+    const int* slot_first;   // [nslots+1]
+    double* out;             // [nwin][nslots][2]
+};
+void launch_pair_sets(const Launch& L, const PairSetDev& p);
 // fix_shell: flag bit 0 excluded (fk_fix), bit 1 shell (fk_pshell); xtop [natom*3]
 void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop, double fk_fix, double fk_pshell,
                       int mixed);

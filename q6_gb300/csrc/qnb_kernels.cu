@@ -3337,6 +3337,50 @@ void launch_offdiag(const Launch& L, const OffdDev& o) {
     if (o.n == 0) return;
     k_offdiag<<<dim3((o.n + 63) / 64, L.nwin), 64, 0, L.st>>>(L.ds, o);
 }
+// Listed pair energies with nbe_qq's arithmetic (src/nonbonded.f90:111-150;
+// nbe_qx, 200-222, is the same without the soft-pair branch): the energies of
+// monitor group pairs (nonbond_monitor, src/nonbondene.f90:4636-4680) and the
+// excluded interactions of group contributions (calculate_exc, 6825-6920).
+// FP64 in both forms; one block per (slot, window) sums its entries in a
+// fixed order, so the sums do not depend on the launch.
+constexpr int kPairSetBlock = 128;
+__global__ void __launch_bounds__(kPairSetBlock) k_pair_sets(const DevState* __restrict__ states, PairSetDev p) {
+    __shared__ double red[2][kPairSetBlock];
+    const int k = blockIdx.x, w = blockIdx.y;
+    const double* __restrict__ x = states[w].x;
+    double vel = 0.0, vlj = 0.0;
+    for (int q = p.slot_first[k] + threadIdx.x; q < p.slot_first[k + 1]; q += kPairSetBlock) {
+        PairSetEntry e = p.e[q];
+        double tx = x[3 * e.j] - x[3 * e.i], ty = x[3 * e.j + 1] - x[3 * e.i + 1], tz = x[3 * e.j + 2] - x[3 * e.i + 2];
+        double r2 = 1.0 / (tx * tx + ty * ty + tz * tz);
+        double r = sqrt(r2);
+        vel += e.el * r;
+        if (e.soft) {
+            vlj += e.A * exp(-e.B / r);
+        } else {
+            double r6 = 1.0 / (1.0 / (r2 * r2 * r2) + e.sc);
+            vlj += e.A * r6 * r6 - e.B * r6;
+        }
+    }
+    red[0][threadIdx.x] = vel;
+    red[1][threadIdx.x] = vlj;
+    __syncthreads();
+    for (int h = kPairSetBlock / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + h];
+            red[1][threadIdx.x] += red[1][threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        p.out[((size_t)w * p.nslots + k) * 2] = red[0][0];
+        p.out[((size_t)w * p.nslots + k) * 2 + 1] = red[1][0];
+    }
+}
+void launch_pair_sets(const Launch& L, const PairSetDev& p) {
+    if (p.nslots == 0) return;
+    k_pair_sets<<<dim3(p.nslots, L.nwin), kPairSetBlock, 0, L.st>>>(L.ds, p);
+}
 // p_restrain, src/bondene.f90:764-1020 (FP64 in both forms).  Blocks
 // [0, nseq) take one sequence restraint each (the centre modes sum their
 // atoms in a fixed-order tree), blocks [nseq, nseq + nwall) one wall
