@@ -72,6 +72,28 @@ class EnergyHeader:
         return _record(body)
 
 
+def group_contribution_header(groups, resid=None) -> EnergyHeader:
+    """The header of a run with [group_contribution] sections
+    (src/simprep.f90:3722-3808): array 1 is the whole system (NOGC), then one
+    array per group with its calculation type, three (FULL, ELECTRO, VDW) for
+    'all'; numres = the group's selection count, gcnum = the 1-based group,
+    resid = -1 for array 1 and then each selection's residue or atom number
+    (resid[g], a list per group, -1 when not given)."""
+    types, numres, gcnum, res = [NOGC], [1], [-1], [-1]
+    code = {"full": FULL, "electro": ELECTRO, "vdw": VDW}
+    for g, (count, caltype) in enumerate(groups):
+        kinds = [FULL, ELECTRO, VDW] if caltype == "all" else [code[caltype]]
+        for t in kinds:
+            types.append(t)
+            numres.append(int(count))
+            gcnum.append(g + 1)
+            ids = list(resid[g]) if resid is not None else [-1] * int(count)
+            res.extend(ids[:int(count)])
+    if len(types) == 1:
+        res = [-1, -1]
+    return EnergyHeader(len(types), types, numres, res, gcnum)
+
+
 def state_record(state: int, lam: float, qx_terms, q_bonded=None, restraint=None, arrays: int = 1) -> bytes:
     """One put_ene record of a state: qx_terms[arrays][6] = qq el, qq vdw,
     qp el, qp vdw, qw el, qw vdw (the engine's qnb_qenergies order);

@@ -42,6 +42,7 @@ EXPORTED = (
     "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
     "qnb_set_bonded", "qnb_get_bonded_energies", "qnb_md_minimize", "qnb_set_shell_restraint",
     "qnb_get_restraint_energies", "qnb_set_offdiag", "qnb_get_offdiag", "qnb_set_restraints",
+    "qnb_set_monitor_groups", "qnb_get_monitor_energies", "qnb_set_group_exclusions", "qnb_get_group_exclusions",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -100,6 +101,8 @@ def load_library(path: str = LIB_PATH):
         "qnb_md_minimize": [P, I32, D, D, D, P],
         "qnb_set_shell_restraint": [P, P, P, D, D], "qnb_get_restraint_energies": [P, P],
         "qnb_set_offdiag": [P, I32, P, P, P, P], "qnb_get_offdiag": [P, P, P], "qnb_set_restraints": [P, P, P],
+        "qnb_set_monitor_groups": [P, I32, P, P, I32, P], "qnb_get_monitor_energies": [P, P],
+        "qnb_set_group_exclusions": [P, I32, P], "qnb_get_group_exclusions": [P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -373,6 +376,79 @@ class NonbondedEngine:
         Hij, rkl = self.offdiag()
         return [(int(i) + 1, int(j) + 1, float(h), float(r))
                 for (i, j), h, r in zip(self.offd_states, Hij[window], rkl[window])]
+
+    # ---- monitor groups and group contributions ----------------------------
+    def set_monitor_groups(self, groups, pairs):
+        """[nonbonded_monitor]: groups = lists of 0-based solute atoms, pairs =
+        (group i, group j) to monitor; an empty pairs list removes them."""
+        first = np.zeros(len(groups) + 1, np.int32)
+        for g, a in enumerate(groups):
+            first[g + 1] = first[g] + len(a)
+        atoms = np.ascontiguousarray(np.concatenate([np.asarray(a, np.int32) for a in groups])
+                                     if groups else np.zeros(0, np.int32), dtype=np.int32)
+        pr = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        self.mon_npairs = len(pr)
+        self._check(self.lib.qnb_set_monitor_groups(self.h, len(groups), _p(first), _p(atoms), len(pr), _p(pr)))
+
+    def monitor_energies(self, lambdas=None):
+        """nonbond_monitor's output of the last evaluation: Vel and Vlj
+        [nwin][npairs][nstates]; with lambdas ([nwin][nstates] or [nstates])
+        also the lambda-weighted Vwel, Vwlj and Vwsum [nwin][npairs]."""
+        n = getattr(self, "mon_npairs", 0)
+        out = np.zeros((self.nwin, n, self.S, 2))
+        if n:
+            self._check(self.lib.qnb_get_monitor_energies(self.h, _p(out)))
+        r = {"Vel": out[..., 0], "Vlj": out[..., 1]}
+        if lambdas is not None:
+            lam = np.broadcast_to(np.asarray(lambdas, np.float64).reshape(-1, self.S), (self.nwin, self.S))
+            r["Vwel"] = np.einsum("wps,ws->wp", r["Vel"], lam)
+            r["Vwlj"] = np.einsum("wps,ws->wp", r["Vlj"], lam)
+            r["Vwsum"] = r["Vwel"] + r["Vwlj"]
+        return r
+
+    def set_group_contributions(self, groups):
+        """[group_contribution]: groups = (atoms, caltype) with 0-based solute
+        atoms and caltype 'full', 'electro', 'vdw' or 'all'; [] removes them.
+        The energy-file header for them is group_contribution_header(...)."""
+        mask = np.zeros((len(groups), self.s.nat_solute), np.uint8)
+        for g, (atoms, caltype) in enumerate(groups):
+            if caltype not in ("full", "electro", "vdw", "all"):
+                raise ValueError(f"group contribution {g}: unknown calculation type {caltype!r}")
+            mask[g, np.asarray(atoms, np.int64)] = 1
+        self.gc_groups = [(np.asarray(a), c) for a, c in groups]
+        self._check(self.lib.qnb_set_group_exclusions(self.h, len(groups), _p(np.ascontiguousarray(mask))))
+
+    def group_exclusions(self):
+        """The excluded interactions of every group, [nwin][ngroups][nstates][4]
+        = qq el, qq vdw, qp el, qp vdw, of the last evaluation."""
+        n = len(getattr(self, "gc_groups", []))
+        out = np.zeros((self.nwin, n, self.S, 4))
+        if n:
+            self._check(self.lib.qnb_get_group_exclusions(self.h, _p(out)))
+        return out
+
+    def group_contribution_EQ(self, EQ, window=0):
+        """calculate_exc (src/nonbondene.f90:6825-6920): the per-state Q
+        energies of every energy-file array, EQ [nstates][6] of the window
+        (array 1) followed by one array per group and calculation type with
+        the excluded interactions subtracted; [nstates][arrays*6] for
+        q6_gb300.enefile.EnergyFileWriter.write_step."""
+        from q6_gb300.enefile import ELECTRO, FULL, VDW, group_contribution_header
+        hdr = group_contribution_header([(len(a), c) for a, c in self.gc_groups])
+        exc = self.group_exclusions()[window]
+        EQ = np.asarray(EQ, np.float64).reshape(self.S, 6)
+        arrays = [EQ]
+        for a in range(1, hdr.arrays):
+            g, t = hdr.gcnum[a] - 1, hdr.types[a]
+            e = EQ.copy()
+            if t in (FULL, ELECTRO):
+                e[:, 0] -= exc[g, :, 0]
+                e[:, 2] -= exc[g, :, 2]
+            if t in (FULL, VDW):
+                e[:, 1] -= exc[g, :, 1]
+                e[:, 3] -= exc[g, :, 3]
+            arrays.append(e)
+        return np.concatenate(arrays, axis=1), hdr
 
     # ---- fix_shell ---------------------------------------------------------
     def set_shell_restraint(self, xtop, shell, fk_fix=200.0, fk_pshell=10.0):
