@@ -453,6 +453,24 @@ int qnb_get_monitor_energies(qnb_context* ctx, double* out);
 int qnb_set_group_exclusions(qnb_context* ctx, int32_t ngroups, const uint8_t* mask);
 int qnb_get_group_exclusions(qnb_context* ctx, double* out);
 
+/* Periodic boundary conditions (use_PBC): a rectangular box of edges
+   boxlength[3] (A) and the Q-list switching atom qswitch (0-based atom; the
+   FEP file's [PBC] switching_atom).  From the next qnb_make_pair_lists* call
+   the lists and energies follow the *_box routines: nbpplist_box,
+   nbpwlist_box, nbwwlist_box (switch atoms / first solvent atoms within the
+   cut-off in the minimum image, src/nonbondene.f90:1643-1775, 2730-2841,
+   4174-4273), nbqplist_box / nbqwlist_box (groups with any atom, waters with
+   the first atom, within Rcq of qswitch, 3747-3860, 3949-4026), and
+   nonbond_pp_box, _pw_box, _ww(_spc)_box, _qp_box, _qw(_spc)_box
+   (4763-6077), every pair at x_j + boxlength*nint((x_a - x_b)/boxlength) of
+   its units' reference atoms.  The static Q-Q lists keep plain distances, as
+   nonbond_qq does.  Cut-offs must not exceed half the shortest edge.
+   boxlength = NULL returns to the sphere.  Not supported with a box
+   (QNB_ERR_UNSUPPORTED): LRF, any-atom group cut-offs, excluded atoms,
+   solvent restraints and solvent internal pairs; constant pressure and
+   put_back_in_box are the caller's. */
+int qnb_set_box(qnb_context* ctx, const double* boxlength, int32_t qswitch);
+
 /* fix_shell (src/potene.f90:386-423), evaluated inside qnb_compute_dev and
    qnb_md_run once set: excluded atoms (the topology's excl flags) with
    fk_fix and shell atoms (shell[i] != 0, as make_shell / make_shell2 mark

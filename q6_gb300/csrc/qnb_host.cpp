@@ -991,6 +991,13 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
     Launch L = nw == 1 ? c->one() : c->all();
     bool do_qp = !(c->qp_done && cut.rcq2 > c->rexcl_o2);   // src/nonbondene.f90:3678
     bool do_qw = !(c->qw_done && cut.rcq2 > c->rexcl_o2);   // src/nonbondene.f90:3889
+    if (c->m.box) {
+        // the minimum image needs every cut-off within half the shortest box edge
+        double h = 0.5 * std::min(c->m.boxl[0], std::min(c->m.boxl[1], c->m.boxl[2]));
+        if (cut.rcpp2 > h * h || cut.rcpw2 > h * h || cut.rcww2 > h * h || cut.rcq2 > h * h)
+            return fail(QNB_ERR_ARG, "periodic box: cut-offs must not exceed half the box (%.3f A)", h);
+        do_qp = do_qw = true;
+    }
     for (int attempt = 0; attempt < 4; ++attempt) {
         unsigned keep = (do_qp ? 0u : 1u << C_QP) | (do_qw ? 0u : 1u << C_QW);   // everything else restarts
         launch_reset_counts(L, keep);
@@ -1009,16 +1016,20 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
             CU(cudaEventRecord(c->ev_join, c->stream2));
         }
         timed(c, K_BUILD, [&] {
-            if (c->mixed) {
+            if (c->m.box) {
+                launch_build_box(L, cut, c->d_qnear), nl += 3;
+            } else if (c->mixed) {
                 launch_build_rows(L, cut), ++nl;
             } else {
                 launch_build_pp(L, cut), nl += 2;
                 launch_build_pw(L, cut), ++nl;
                 launch_build_ww(L, cut), ++nl;
             }
-            if (do_qp) launch_build_qp(L, c->d_qnear, cut.rcq2), ++nl;
-            if (do_qw) launch_build_qw(L, cut), ++nl;
-            if (c->mixed && (do_qp || do_qw)) launch_clear_fq(L), ++nl;   // atoms may leave the Q lists
+            if (!c->m.box) {
+                if (do_qp) launch_build_qp(L, c->d_qnear, cut.rcq2), ++nl;
+                if (do_qw) launch_build_qw(L, cut), ++nl;
+                if (c->mixed && (do_qp || do_qw)) launch_clear_fq(L), ++nl;   // atoms may leave the Q lists
+            }
         });
         c->launches += nl + (c->use_lrf ? 1 : 0);
         if (c->use_lrf) CU(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
@@ -1052,6 +1063,12 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
     if (mx) {
         timed(c, K_PACK, [&] { launch_pack(L); });
         ++nl;
+    }
+    if (c->m.box) {   // periodic box: the *_box routines, src/potene.f90:326-343
+        int nb = 0;
+        timed(c, K_PP, [&] { nb = launch_box_nonbond(L, md, mx, c->d_iwhich, c->last_cut.rcq2); });
+        c->launches += nl + nb;
+        return check_launch();
     }
     // call order of pot_energy_nonbonds, src/potene.f90:340-379
     if (mx) {
@@ -1322,6 +1339,7 @@ int qnb_nonbond_qq(qnb_context* c, const double* x, double* d, qnb_qenergies* EQ
 }
 
 int qnb_set_solvent_params(qnb_context* c, const qnb_solvent_params* p) {
+    if (c && c->m.box) return fail(QNB_ERR_UNSUPPORTED, "solvent restraints are for the sphere, not a periodic box");
     if (!c || !p) return fail(QNB_ERR_ARG, "null argument");
     if (p->wpol_restr && (p->nwpolr_shell < 1 || p->nwpolr_shell > kMaxShell))
         return fail(QNB_ERR_ARG, "nwpolr_shell must be 1..%d", kMaxShell);
@@ -2793,6 +2811,38 @@ int qnb_set_group_exclusions(qnb_context* c, int32_t ngroups, const uint8_t* mas
 int qnb_get_group_exclusions(qnb_context* c, double* out) {
     if (!c || (!out && c->exc_groups > 0)) return fail(QNB_ERR_ARG, "null argument");
     return read_pair_sets(c, c->mon_pairs * c->S, c->exc_groups * c->S * 2, out);
+}
+
+int qnb_set_box(qnb_context* c, const double* boxlength, int32_t qswitch) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    if (!boxlength) {
+        c->m.box = 0;
+    } else {
+        for (int k = 0; k < 3; ++k)
+            if (!(boxlength[k] > 0.0)) return fail(QNB_ERR_ARG, "box length %d must be positive", k);
+        if (c->nqat > 0 && (qswitch < 0 || qswitch >= c->natom))
+            return fail(QNB_ERR_ARG, "switching atom %d out of range", qswitch);
+        if (c->use_lrf) return fail(QNB_ERR_UNSUPPORTED, "LRF with a periodic box is not supported");
+        if (c->m.any_atom) return fail(QNB_ERR_UNSUPPORTED, "a periodic box needs switch-atom cut-offs");
+        if (c->have_solv || c->nsi > 0)
+            return fail(QNB_ERR_UNSUPPORTED, "solvent restraints and solvent internal pairs are for the sphere");
+        std::vector<uint8_t> excl(c->natom);
+        CU(cudaMemcpy(excl.data(), c->m.excl, c->natom, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < c->natom; ++i)
+            if (excl[i]) return fail(QNB_ERR_UNSUPPORTED, "excluded atoms (atom %d) with a periodic box", i);
+        c->m.box = 1;
+        c->m.qswitch = qswitch;
+        for (int k = 0; k < 3; ++k) {
+            c->m.boxl[k] = boxlength[k];
+            c->m.inv_boxl[k] = 1.0 / boxlength[k];
+        }
+    }
+    c->lists_built = false;
+    c->qp_done = c->qw_done = false;
+    ++c->epoch;
+    return QNB_OK;
 }
 
 }  // extern "C"

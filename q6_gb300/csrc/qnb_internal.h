@@ -104,6 +104,11 @@ struct DevModel {
     double xpcent[3], xwcent[3];
     float wcoff[3];             // xpcent - xwcent in FP32: packed (xpcent-centred) coordinates to xwcent-centred
     double rexcl_o2;
+    // periodic box (qnb_set_box): rectangular box lengths, their inverses
+    // and the Q-list switching atom (FEP file [PBC] switching_atom)
+    int box;
+    int qswitch;
+    double boxl[3], inv_boxl[3];
     // FP32 copies are stored relative to xpcent, which bounds their magnitude
     // by the sphere size (FP32 cut-off prefilter and mixed-form pair math)
 };
@@ -295,6 +300,10 @@ struct PairSetDev {
     double* out;             // [nwin][nslots][2]
 };
 void launch_pair_sets(const Launch& L, const PairSetDev& p);
+// periodic box: list builds (pp, pw, ww, qp, qw) with minimum-image tests and
+// the box energy kernels (nonbond_*_box), FP64 arithmetic in both forms
+void launch_build_box(const Launch& L, const Cut& c, const uint8_t* qnear);
+int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, double rcq2);
 // fix_shell: flag bit 0 excluded (fk_fix), bit 1 shell (fk_pshell); xtop [natom*3]
 void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop, double fk_fix, double fk_pshell,
                       int mixed);

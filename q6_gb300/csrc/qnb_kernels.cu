@@ -3381,6 +3381,390 @@ void launch_pair_sets(const Launch& L, const PairSetDev& p) {
     if (p.nslots == 0) return;
     k_pair_sets<<<dim3(p.nslots, L.nwin), kPairSetBlock, 0, L.st>>>(L.ds, p);
 }
+
+// -----------------------------------------------------------------------------
+// Periodic box (use_PBC).  Every interaction is between two units (solute
+// charge group, water molecule, the Q region around qswitch) and uses one
+// lattice shift per unit pair, boxlength * nint((x_a - x_b) / boxlength) of
+// the units' reference atoms (q_nint, src/math.f90:566-574); the partner atom
+// is taken at x_j + shift.  FP64 arithmetic in both forms (the mixed form
+// accumulates in fixed point like its other FP64 terms).
+// -----------------------------------------------------------------------------
+__device__ __forceinline__ void box_shift(const DevModel& m, const double* __restrict__ x, int a, int b,
+                                          double& sx, double& sy, double& sz) {
+    sx = m.boxl[0] * round((x[3 * a] - x[3 * b]) * m.inv_boxl[0]);
+    sy = m.boxl[1] * round((x[3 * a + 1] - x[3 * b + 1]) * m.inv_boxl[1]);
+    sz = m.boxl[2] * round((x[3 * a + 2] - x[3 * b + 2]) * m.inv_boxl[2]);
+}
+// q_dist4(shift, boxlength*q_nint(shift*inv_boxl)) of atoms a and b
+__device__ __forceinline__ double box_d2(const DevModel& m, const double* __restrict__ x, int a, int b) {
+    double r2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        double d = x[3 * a + c] - x[3 * b + c];
+        double t = m.boxl[c] * round(d * m.inv_boxl[c]) - d;
+        r2 += t * t;
+    }
+    return r2;
+}
+template <bool MIX>
+__device__ __forceinline__ void box_grad(const Acc<MIX>& acc, int i, double gx, double gy, double gz) {
+    if constexpr (MIX) acc.gradd(i, gx, gy, gz);
+    else acc.grad(i, gx, gy, gz);
+}
+// one shifted pair: vec = shift - (x_i - x_j) (q_dist2(x(i)-x(j), shift))
+struct BoxPair {
+    double tx, ty, tz, r2, r;
+};
+__device__ __forceinline__ BoxPair box_pair(const double* __restrict__ x, int i, int j, double sx, double sy,
+                                            double sz) {
+    BoxPair p;
+    p.tx = sx - (x[3 * i] - x[3 * j]);
+    p.ty = sy - (x[3 * i + 1] - x[3 * j + 1]);
+    p.tz = sz - (x[3 * i + 2] - x[3 * j + 2]);
+    p.r2 = 1.0 / (p.tx * p.tx + p.ty * p.ty + p.tz * p.tz);
+    p.r = sqrt(p.r2);
+    return p;
+}
+
+// nbpplist_box, src/nonbondene.f90:1643-1775: solute group pairs whose switch
+// atoms are within Rcpp in the minimum image (each pair once, a group with
+// itself always); nbpwlist_box, 2730-2841: switch atom to the water's first
+// atom; nbwwlist_box, 4174-4273: first atoms of two waters.  The pair sets
+// are the reference's; the order inside a list is not.
+__global__ void k_build_box_groups(DevModel m, const DevState* __restrict__ states, double rcpp2, double rcpw2,
+                                   double rcww2) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const int G = m.ncgp_solute, W = m.nwat;
+    const int64_t npp = (int64_t)G * (G + 1) / 2, npw = (int64_t)G * W, nww = (int64_t)W * (W - 1) / 2;
+    const int64_t total = npp + npw + nww;
+    for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x; t0 < total; t0 += (int64_t)gridDim.x * blockDim.x) {
+        int64_t t = t0 + threadIdx.x;
+        int kind = -1, a = 0, b = 0;
+        if (t < npp) {   // (g1, g2), g1 <= g2, row-major over the upper triangle
+            // t = g1*(g1+1)/2 + g2 with g2 <= g1
+            int g1 = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+            while ((int64_t)(g1 + 1) * (g1 + 2) / 2 <= t) ++g1;
+            while ((int64_t)g1 * (g1 + 1) / 2 > t) --g1;
+            int g2 = (int)(t - (int64_t)g1 * (g1 + 1) / 2);
+            a = g2;
+            b = g1;
+            bool ok = (a == b) || box_d2(m, x, m.gsw[a], m.gsw[b]) <= rcpp2;
+            kind = ok ? 0 : -1;
+        } else if (t < npp + npw) {
+            int64_t u = t - npp;
+            a = (int)(u / W);
+            b = (int)(u % W);
+            bool ok = box_d2(m, x, m.gsw[a], m.nat_solute + m.sa * b) <= rcpw2;
+            kind = ok ? 1 : -1;
+        } else if (t < total) {
+            int64_t u = t - npp - npw;   // (i, j), i < j over the strict upper triangle
+            int j = (int)((sqrt(8.0 * (double)u + 1.0) + 1.0) * 0.5);
+            while ((int64_t)j * (j - 1) / 2 > u) --j;
+            while ((int64_t)(j + 1) * j / 2 <= u) ++j;
+            int i = (int)(u - (int64_t)j * (j - 1) / 2);
+            a = i;
+            b = j;
+            bool ok = box_d2(m, x, m.nat_solute + m.sa * a, m.nat_solute + m.sa * b) <= rcww2;
+            kind = ok ? 2 : -1;
+        }
+        // one append per kind and warp
+        for (int k = 0; k < 3; ++k) {
+            bool mine = kind == k;
+            int npairs = 0;
+            if (mine && k == 1) {
+                for (int q = m.gslot[a]; q < m.gslot[a + 1]; ++q) npairs += (m.iqatom[m.gatom[q]] < 0);
+                if (npairs == 0) mine = false;
+            }
+            if (!__any_sync(0xffffffffu, mine)) continue;
+            if (k == 0) {
+                int pos = warp_append(s.cnt + C_PPG, mine ? 1 : 0);
+                if (mine && pos < s.cap_ppg) s.ppg[pos] = make_int2(a, b);
+            } else if (k == 1) {
+                int pos = warp_append(s.cnt + C_PW, mine ? npairs : 0);
+                if (mine)
+                    for (int q = m.gslot[a]; q < m.gslot[a + 1]; ++q) {
+                        int i = m.gatom[q];
+                        if (m.iqatom[i] >= 0) continue;
+                        if (pos < s.cap_pw) s.pw[pos] = make_int2(i, b);
+                        ++pos;
+                    }
+            } else {
+                int pos = warp_append(s.cnt + C_WW, mine ? 1 : 0);
+                if (mine && pos < s.cap_ww) s.ww[pos] = make_int2(a, b);
+            }
+        }
+    }
+}
+
+// nbqplist_box / nbqplis2_box, src/nonbondene.f90:3747-3860, 3525-3644: solute
+// groups with any atom within Rcq of qswitch in the minimum image; their
+// atoms not bonded/angled to a Q atom.  nbqwlist_box, 3949-4026: waters whose
+// first atom is within Rcq of qswitch.  One block per window, appends in order.
+__global__ void __launch_bounds__(1024) k_build_box_q(DevModel m, const DevState* __restrict__ states,
+                                                      const uint8_t* __restrict__ qnear, double rcq2) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    int base = 0;
+    for (int g0 = 0; g0 < m.ncgp_solute; g0 += blockDim.x) {
+        int ig = g0 + threadIdx.x, na = 0;
+        if (ig < m.ncgp_solute) {
+            bool inside = false;
+            for (int a = m.gslot[ig]; a < m.gslot[ig + 1] && !inside; ++a)
+                inside = box_d2(m, x, m.gatom[a], m.qswitch) <= rcq2;
+            if (inside)
+                for (int a = m.gslot[ig]; a < m.gslot[ig + 1]; ++a) na += !qnear[m.gatom[a]];
+        }
+        int tot;
+        int pos = base + block_excl_scan(na, &tot);
+        if (na)
+            for (int a = m.gslot[ig]; a < m.gslot[ig + 1]; ++a) {
+                int i = m.gatom[a];
+                if (qnear[i]) continue;
+                if (pos < s.cap_qp) s.qp[pos] = i;
+                ++pos;
+            }
+        base += tot;
+    }
+    if (threadIdx.x == 0) s.cnt[C_QP] = base;
+    __syncthreads();
+    base = 0;
+    for (int w0 = 0; w0 < m.nwat; w0 += blockDim.x) {
+        int iw = w0 + threadIdx.x;
+        bool ok = iw < m.nwat && box_d2(m, x, m.nat_solute + m.sa * iw, m.qswitch) <= rcq2;
+        int tot;
+        int pos = base + block_excl_scan(ok ? 1 : 0, &tot);
+        if (ok && pos < s.cap_qw) s.qw[pos] = iw;
+        base += tot;
+    }
+    if (threadIdx.x == 0) s.cnt[C_QW] = base;
+}
+
+void launch_build_box(const Launch& L, const Cut& c, const uint8_t* qnear) {
+    const int64_t G = L.m.ncgp_solute, W = L.m.nwat;
+    const int64_t total = G * (G + 1) / 2 + G * W + W * (W - 1) / 2;
+    if (total > 0) {
+        k_build_box_groups<<<grid_for(total, 256, 8, L.nwin), 256, 0, L.st>>>(L.m, L.ds, c.rcpp2, c.rcpw2, c.rcww2);
+        if (G > 0) k_expand_pp<<<grid_for(L.s0.cap_ppg, 128, 8, L.nwin), 128, 0, L.st>>>(L.m, L.ds);
+    }
+    if (L.m.nqat > 0) k_build_box_q<<<dim3(1, L.nwin), 1024, 0, L.st>>>(L.m, L.ds, qnear, c.rcq2);
+}
+
+// nonbond_pp_box, src/nonbondene.f90:4763-4853 (nbe_b, src/nonbonded.f90:78-108)
+template <bool MIX>
+__global__ void __launch_bounds__(256) k_box_pp(DevModel m, const DevState* __restrict__ states,
+                                                const int* __restrict__ iwhich) {
+    const DevState& s = states[blockIdx.y];
+    Acc<MIX> acc = make_acc<MIX>(s);
+    ESum<MIX> eel, evdw;
+    const double* __restrict__ x = s.x;
+    int n = min((int64_t)s.cnt[C_PP], s.cap_pp);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        int2 e = s.pp[p];
+        int i = e.x, j = e.y & 0x0fffffff, code = e.y >> 28;
+        double sx, sy, sz;
+        box_shift(m, x, m.gsw[iwhich[i]], m.gsw[iwhich[j]], sx, sy, sz);
+        BoxPair q = box_pair(x, i, j, sx, sy, sz);
+        double2 ab = m.lj[((size_t)(code - 1) * m.natyps + m.iac[i]) * m.natyps + m.iac[j]];
+        double el = m.crg[i] * m.crg[j];
+        if (code == 3) el = el * m.el14;
+        double vel = el * q.r, r6 = q.r2 * q.r2 * q.r2;
+        double va = ab.x * r6 * r6, vb = ab.y * r6;
+        double dv = q.r2 * (-vel - 12.0 * va + 6.0 * vb);
+        box_grad<MIX>(acc, i, -q.tx * dv, -q.ty * dv, -q.tz * dv);
+        box_grad<MIX>(acc, j, q.tx * dv, q.ty * dv, q.tz * dv);
+        eel.add(vel);
+        evdw.add(va - vb);
+    }
+    eel.flush(acc, E_PP_EL);
+    evdw.flush(acc, E_PP_VDW);
+}
+
+// nonbond_pw_box, src/nonbondene.f90:4920-5009
+template <bool MIX>
+__global__ void __launch_bounds__(256) k_box_pw(DevModel m, const DevState* __restrict__ states,
+                                                const int* __restrict__ iwhich) {
+    const DevState& s = states[blockIdx.y];
+    Acc<MIX> acc = make_acc<MIX>(s);
+    ESum<MIX> eel, evdw;
+    const double* __restrict__ x = s.x;
+    int n = min((int64_t)s.cnt[C_PW], s.cap_pw);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        int2 e = s.pw[p];
+        int i = e.x, j0 = m.nat_solute + m.sa * e.y, ti = m.iac[i];
+        double sx, sy, sz;
+        box_shift(m, x, m.gsw[iwhich[i]], j0, sx, sy, sz);
+        double g[3] = {0, 0, 0};
+        for (int a = 0; a < m.sa; ++a) {
+            int tw = m.wtype[a];
+            int code = m.ljcod[ti * m.natyps + tw];
+            double2 ab = m.lj[((size_t)(code - 1) * m.natyps + ti) * m.natyps + tw];
+            BoxPair q = box_pair(x, i, j0 + a, sx, sy, sz);
+            double vel = m.crg[i] * m.wcrg[a] * q.r, r6 = q.r2 * q.r2 * q.r2;
+            double va = ab.x * r6 * r6, vb = ab.y * r6;
+            double dv = q.r2 * (-vel - 12.0 * va + 6.0 * vb);
+            g[0] -= q.tx * dv;
+            g[1] -= q.ty * dv;
+            g[2] -= q.tz * dv;
+            box_grad<MIX>(acc, j0 + a, q.tx * dv, q.ty * dv, q.tz * dv);
+            eel.add(vel);
+            evdw.add(va - vb);
+        }
+        box_grad<MIX>(acc, i, g[0], g[1], g[2]);
+    }
+    eel.flush(acc, E_PW_EL);
+    evdw.flush(acc, E_PW_VDW);
+}
+
+// nonbond_ww_spc_box / nonbond_ww_box, src/nonbondene.f90:5979-6077, 5576-5654
+// (nbe_spcb, src/nonbonded.f90:271-291): one shift per molecule pair from
+// the first atoms; SPC: LJ between the first atoms only
+template <bool MIX, bool SPC>
+__global__ void __launch_bounds__(256) k_box_ww(DevModel m, const DevState* __restrict__ states) {
+    const DevState& s = states[blockIdx.y];
+    Acc<MIX> acc = make_acc<MIX>(s);
+    ESum<MIX> eel, evdw;
+    const double* __restrict__ x = s.x;
+    int n = min((int64_t)s.cnt[C_WW], s.cap_ww);
+    const int sa = m.sa;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        int2 e = s.ww[p];
+        int i0 = m.nat_solute + sa * e.x, j0 = m.nat_solute + sa * e.y;
+        double sx, sy, sz;
+        box_shift(m, x, i0, j0, sx, sy, sz);
+        double gi[kMaxSolv][3] = {}, gj[kMaxSolv][3] = {};
+        for (int la = 0; la < sa; ++la)
+            for (int ka = 0; ka < sa; ++ka) {
+                bool lj = !SPC || (la == 0 && ka == 0);
+                int k = la * kMaxSolv + ka;
+                BoxPair q = box_pair(x, i0 + la, j0 + ka, sx, sy, sz);
+                double vel = m.wwE[k] * q.r, dv, vdw = 0.0;
+                if (lj) {
+                    double r6 = q.r2 * q.r2 * q.r2;
+                    double va = m.wwA[k] * r6 * r6, vb = m.wwB[k] * r6;
+                    dv = q.r2 * (-vel - 12.0 * va + 6.0 * vb);
+                    vdw = va - vb;
+                } else {
+                    dv = q.r2 * (-vel);
+                }
+                gi[la][0] -= q.tx * dv; gi[la][1] -= q.ty * dv; gi[la][2] -= q.tz * dv;
+                gj[ka][0] += q.tx * dv; gj[ka][1] += q.ty * dv; gj[ka][2] += q.tz * dv;
+                eel.add(vel);
+                evdw.add(vdw);
+            }
+        for (int a = 0; a < sa; ++a) {
+            box_grad<MIX>(acc, i0 + a, gi[a][0], gi[a][1], gi[a][2]);
+            box_grad<MIX>(acc, j0 + a, gj[a][0], gj[a][1], gj[a][2]);
+        }
+    }
+    eel.flush(acc, E_WW_EL);
+    evdw.flush(acc, E_WW_VDW);
+}
+
+// nonbond_qp_box, src/nonbondene.f90:5234-5335, and nonbond_qw_box /
+// nonbond_qw_spc_box, 5422-5505, 5771-5881 (nbe_qx, nbe_qspc): one thread per
+// (listed unit, Q atom); the unit's shift brings it next to qswitch, taken
+// from the first group atom inside Rcq (qp, nbqp_cgp) or the water's first
+// atom (qw).  Per-state energies are summed in registers.
+template <bool MIX, bool WATER, bool SPC>
+__global__ void __launch_bounds__(256) k_box_q(DevModel m, const DevState* __restrict__ states,
+                                               const int* __restrict__ iwhich, double rcq2) {
+    const DevState& s = states[blockIdx.y];
+    Acc<MIX> acc = make_acc<MIX>(s);
+    const double* __restrict__ x = s.x;
+    const int S = m.S, nq = m.nqat;
+    ESum<MIX> eel[kMaxStates], evdw[kMaxStates];
+    int n = WATER ? min((int64_t)s.cnt[C_QW], s.cap_qw) : min((int64_t)s.cnt[C_QP], s.cap_qp);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)n * nq;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        int u = (int)(t / nq), iq = (int)(t % nq);
+        int i = m.iqseq[iq];
+        double sx, sy, sz;
+        int j0, na;
+        if (WATER) {
+            j0 = m.nat_solute + m.sa * s.qw[u];
+            na = m.sa;
+            box_shift(m, x, m.qswitch, j0, sx, sy, sz);
+        } else {
+            j0 = s.qp[u];
+            na = 1;
+            int g = iwhich[j0], ref = m.gatom[m.gslot[g]];
+            for (int a = m.gslot[g]; a < m.gslot[g + 1]; ++a)
+                if (box_d2(m, x, m.gatom[a], m.qswitch) <= rcq2) {
+                    ref = m.gatom[a];
+                    break;
+                }
+            box_shift(m, x, m.qswitch, ref, sx, sy, sz);
+        }
+        double gi[3] = {0, 0, 0};
+        for (int a = 0; a < na; ++a) {
+            int j = j0 + a;
+            BoxPair q = box_pair(x, i, j, sx, sy, sz);
+            bool lj = !(WATER && SPC) || a == 0;
+            double dvs = 0.0;
+            double r6hc = 1.0 / (q.r2 * q.r2 * q.r2);
+            for (int st = 0; st < S; ++st) {
+                const QPar P = WATER ? m.qw_tab[((size_t)iq * m.sa + a) * S + st] : m.qp_tab[((size_t)j * nq + iq) * S + st];
+                double lam = s.lambda[st];
+                if (lj) {
+                    double vel, vdw, dv;
+                    nbe_qx_d(q.r2, q.r, r6hc, P.A, P.B, P.el, P.sc, lam, vel, vdw, dv);
+                    dvs += dv;
+                    eel[st].add(vel);
+                    evdw[st].add(vdw);
+                } else {   // nbe_qspc
+                    double vel = P.el * q.r;
+                    dvs += -q.r2 * vel * lam;
+                    eel[st].add(vel);
+                }
+            }
+            gi[0] -= q.tx * dvs;
+            gi[1] -= q.ty * dvs;
+            gi[2] -= q.tz * dvs;
+            box_grad<MIX>(acc, j, q.tx * dvs, q.ty * dvs, q.tz * dvs);
+        }
+        box_grad<MIX>(acc, i, gi[0], gi[1], gi[2]);
+    }
+    for (int st = 0; st < S; ++st) {
+        eel[st].flush(acc, eq_slot(st, WATER ? 4 : 2));
+        evdw[st].flush(acc, eq_slot(st, WATER ? 5 : 3));
+    }
+}
+
+int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, double rcq2) {
+    const DevModel& m = L.m;
+    int nl = 0;
+    auto grid = [&](int64_t n) { return grid_for(n > 1 ? n : 1, 256, 8, L.nwin); };
+    if (md && m.ncgp_solute > 0) {
+        if (mixed) k_box_pp<true><<<grid(L.s0.cap_pp), 256, 0, L.st>>>(m, L.ds, iwhich);
+        else k_box_pp<false><<<grid(L.s0.cap_pp), 256, 0, L.st>>>(m, L.ds, iwhich);
+        ++nl;
+    }
+    if (m.nwat > 0) {
+        if (md) {
+            if (mixed) k_box_pw<true><<<grid(L.s0.cap_pw), 256, 0, L.st>>>(m, L.ds, iwhich);
+            else k_box_pw<false><<<grid(L.s0.cap_pw), 256, 0, L.st>>>(m, L.ds, iwhich);
+            dim3 g = grid(L.s0.cap_ww);
+            if (mixed) { if (m.spc) k_box_ww<true, true><<<g, 256, 0, L.st>>>(m, L.ds); else k_box_ww<true, false><<<g, 256, 0, L.st>>>(m, L.ds); }
+            else { if (m.spc) k_box_ww<false, true><<<g, 256, 0, L.st>>>(m, L.ds); else k_box_ww<false, false><<<g, 256, 0, L.st>>>(m, L.ds); }
+            nl += 2;
+        }
+        if (m.nqat > 0) {
+            dim3 g = grid(L.s0.cap_qw * m.nqat);
+            if (mixed) { if (m.spc) k_box_q<true, true, true><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2); else k_box_q<true, true, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2); }
+            else { if (m.spc) k_box_q<false, true, true><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2); else k_box_q<false, true, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2); }
+            ++nl;
+        }
+    }
+    if (m.nqat > 0 && m.nat_solute > 0) {
+        dim3 g = grid(L.s0.cap_qp * m.nqat);
+        if (mixed) k_box_q<true, false, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2);
+        else k_box_q<false, false, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2);
+        ++nl;
+    }
+    return nl;
+}
 // p_restrain, src/bondene.f90:764-1020 (FP64 in both forms).  Blocks
 // [0, nseq) take one sequence restraint each (the centre modes sum their
 // atoms in a fixed-order tree), blocks [nseq, nseq + nwall) one wall

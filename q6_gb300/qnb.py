@@ -42,7 +42,7 @@ EXPORTED = (
     "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
     "qnb_set_bonded", "qnb_get_bonded_energies", "qnb_md_minimize", "qnb_set_shell_restraint",
     "qnb_get_restraint_energies", "qnb_set_offdiag", "qnb_get_offdiag", "qnb_set_restraints",
-    "qnb_set_monitor_groups", "qnb_get_monitor_energies", "qnb_set_group_exclusions", "qnb_get_group_exclusions",
+    "qnb_set_monitor_groups", "qnb_get_monitor_energies", "qnb_set_group_exclusions", "qnb_get_group_exclusions", "qnb_set_box",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -103,6 +103,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_set_offdiag": [P, I32, P, P, P, P], "qnb_get_offdiag": [P, P, P], "qnb_set_restraints": [P, P, P],
         "qnb_set_monitor_groups": [P, I32, P, P, I32, P], "qnb_get_monitor_energies": [P, P],
         "qnb_set_group_exclusions": [P, I32, P], "qnb_get_group_exclusions": [P, P],
+        "qnb_set_box": [P, P, I32],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -376,6 +377,18 @@ class NonbondedEngine:
         Hij, rkl = self.offdiag()
         return [(int(i) + 1, int(j) + 1, float(h), float(r))
                 for (i, j), h, r in zip(self.offd_states, Hij[window], rkl[window])]
+
+    # ---- periodic box --------------------------------------------------------
+    def set_box(self, boxlength, qswitch=None):
+        """Periodic boundary conditions (qnb_set_box): boxlength (3 edges, A)
+        or None for the sphere; qswitch: 0-based Q switching atom (default
+        the first Q atom)."""
+        if boxlength is None:
+            self._check(self.lib.qnb_set_box(self.h, None, 0))
+            return
+        L = np.ascontiguousarray(np.broadcast_to(np.asarray(boxlength, np.float64), (3,)))
+        qs = int(self.s.iqseq[0]) if qswitch is None and self.s.nqat else int(qswitch or 0)
+        self._check(self.lib.qnb_set_box(self.h, _p(L), qs))
 
     # ---- monitor groups and group contributions ----------------------------
     def set_monitor_groups(self, groups, pairs):
