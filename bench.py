@@ -286,6 +286,8 @@ def run_ours(args, rank, world, local):
             out["replica_group"] = replica_group(args, local)
         if args.md:
             out["md_step"] = md_step(args, s, sp, lams, local, tuning)
+        if args.box:
+            out["box_step"] = box_step(args, s, lams, local)
         if args.fp64_compare:
             out["fp64_value"] = fp64_compare(args, s, sp, lams, local)
             out["mixed_over_fp64"] = round(out["value"] / out["fp64_value"], 3) if out["fp64_value"] else None
@@ -583,6 +585,60 @@ def md_step(args, s, sp, lams, local, tuning=None):
                     "with CUDA events around qnb_md_run (L2 not flushed between steps)"}
 
 
+def box_step(args, s, lams, local):
+    """The periodic-box path (qnb_set_box; the *_box lists and energies) on the
+    same 6,060 atoms in a 53 A cubic box (2R + 3 A, so pairs wrap across the
+    faces), the sphere's excluded flags cleared and LRF off as the box path
+    requires: 51 windows, mixed form, lists every 25th step, Rcq 12 A.
+    Window-steps/s, L2 flushed before every timed step."""
+    import dataclasses
+
+    import numpy as np
+    import torch
+    from q6_gb300.qnb import PREC_MIXED, NonbondedEngine, QnbError
+    from q6_gb300.system import lambdas_for_window
+    nwin = args.windows
+    sb = dataclasses.replace(s, excl=np.zeros_like(np.asarray(s.excl)))
+    R = float(np.sqrt((np.asarray(s.x) ** 2).sum(1)).max())
+    L = 2.0 * round(R) + 3.0
+    cut = dict(Rcq=12.0, RcLRF=12.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
+    try:
+        e = NonbondedEngine(sb, precision=PREC_MIXED, use_lrf=False, device=local, windows=nwin)
+        e.set_box([L, L, L])
+        for w in range(nwin):
+            e.set_lambda(lambdas_for_window(lams[w], sb.nstates), window=w)
+        e.set_coordinates_dev(np.stack([sb.x] * nwin))
+        stream = torch.cuda.ExternalStream(e.stream())
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        for k in range(3):
+            e.make_pair_lists_dev(**cut)
+            e.compute_dev(istep=k, sync=True)
+        sizes = {k: int(e.list_size(v)) for k, v in (("pp", 0), ("pw", 1), ("ww", 2), ("qp", 3), ("qw", 4))}
+        steps = 50
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        tot = 0.0
+        for k in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ev0.record(stream)
+            if k % 25 == 0:
+                e.make_pair_lists_dev(**cut)
+            e.compute_dev(istep=k, sync=False)
+            ev1.record(stream)
+            ev1.synchronize()
+            tot += ev0.elapsed_time(ev1)
+        e.close()
+    except QnbError as ex:
+        return {"error": str(ex)}
+    return {"value": round(nwin * steps / (tot / 1e3), 1), "unit": "window-steps/s",
+            "ms_per_step": round(tot / steps, 4), "steps": steps, "windows": nwin, "box_A": L,
+            "list_sizes_window0": sizes,
+            "what": "periodic box: minimum-image lists every 25th step + pp/pw/ww/qp/qw box energies (FP32 pair "
+                    "arithmetic, fixed-point sums) + static Q-Q, all windows per launch"}
+
+
 def fp64_compare(args, s, sp, lams, local):
     """Plain FP64 form on the same workload (25 steps with one list build)."""
     import numpy as np
@@ -721,6 +777,8 @@ def main():
                     help="skip the 51-window + 16-replica graph group")
     ap.add_argument("--no-dg", dest="dg", action="store_false",
                     help="skip the mixed-vs-FP64 dG check")
+    ap.add_argument("--no-box", dest="box", action="store_false",
+                    help="skip the periodic-box line (box_step)")
     ap.add_argument("--no-md", dest="md", action="store_false",
                     help="skip the device-resident MD step measurement")
     ap.add_argument("--md-minimize", type=int, default=3000,

@@ -1132,7 +1132,8 @@ void add_energies(const double* e, qnb_energies* E, qnb_qenergies* EQ, int S) {
 // lists; they are built on demand from window 0's build coordinates with the
 // same exact selection as the rows
 int ensure_half_lists(qnb_context* c) {
-    if (!c->mixed || c->diag_valid || !c->lists_built) return QNB_OK;
+    // the box builders already write the half lists in both forms
+    if (!c->mixed || c->m.box || c->diag_valid || !c->lists_built) return QNB_OK;
     for (int attempt = 0; attempt < 4; ++attempt) {
         DevState tmp = c->st[0];
         tmp.x = c->st[0].x_build;

@@ -301,7 +301,8 @@ struct PairSetDev {
 };
 void launch_pair_sets(const Launch& L, const PairSetDev& p);
 // periodic box: list builds (pp, pw, ww, qp, qw) with minimum-image tests and
-// the box energy kernels (nonbond_*_box), FP64 arithmetic in both forms
+// the box energy kernels (nonbond_*_box); FP64 pair arithmetic in the FP64
+// form, FP32 in the mixed form
 void launch_build_box(const Launch& L, const Cut& c, const uint8_t* qnear);
 int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, double rcq2);
 // fix_shell: flag bit 0 excluded (fk_fix), bit 1 shell (fk_pshell); xtop [natom*3]

@@ -3387,8 +3387,10 @@ void launch_pair_sets(const Launch& L, const PairSetDev& p) {
 // charge group, water molecule, the Q region around qswitch) and uses one
 // lattice shift per unit pair, boxlength * nint((x_a - x_b) / boxlength) of
 // the units' reference atoms (q_nint, src/math.f90:566-574); the partner atom
-// is taken at x_j + shift.  FP64 arithmetic in both forms (the mixed form
-// accumulates in fixed point like its other FP64 terms).
+// is taken at x_j + shift.  The list decisions are FP64 in both forms; the
+// FP64 form computes the pairs in FP64, the mixed form in FP32 from the
+// packed coordinates with an FP32 shift (fixed-point sums), as its sphere
+// kernels do.
 // -----------------------------------------------------------------------------
 __device__ __forceinline__ void box_shift(const DevModel& m, const double* __restrict__ x, int a, int b,
                                           double& sx, double& sy, double& sz) {
@@ -3406,6 +3408,25 @@ __device__ __forceinline__ double box_d2(const DevModel& m, const double* __rest
         r2 += t * t;
     }
     return r2;
+}
+// the mixed form's FP32 pair geometry: packed coordinates (xpcent-centred)
+// and an FP32 shift; vec = shift - (x_i - x_j)
+__device__ __forceinline__ float3 box_shift_f(const DevModel& m, float4 a, float4 b) {
+    return make_float3((float)m.boxl[0] * roundf((a.x - b.x) * (float)m.inv_boxl[0]),
+                       (float)m.boxl[1] * roundf((a.y - b.y) * (float)m.inv_boxl[1]),
+                       (float)m.boxl[2] * roundf((a.z - b.z) * (float)m.inv_boxl[2]));
+}
+struct BoxPairF {
+    float tx, ty, tz, r2, r;
+};
+__device__ __forceinline__ BoxPairF box_pair_f(float4 a, float4 b, float3 sh) {
+    BoxPairF p;
+    p.tx = sh.x - (a.x - b.x);
+    p.ty = sh.y - (a.y - b.y);
+    p.tz = sh.z - (a.z - b.z);
+    p.r = rsqrtf(p.tx * p.tx + p.ty * p.ty + p.tz * p.tz);
+    p.r2 = p.r * p.r;
+    return p;
 }
 template <bool MIX>
 __device__ __forceinline__ void box_grad(const Acc<MIX>& acc, int i, double gx, double gy, double gz) {
@@ -3563,6 +3584,21 @@ __global__ void __launch_bounds__(256) k_box_pp(DevModel m, const DevState* __re
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         int2 e = s.pp[p];
         int i = e.x, j = e.y & 0x0fffffff, code = e.y >> 28;
+        if constexpr (MIX) {   // FP32 pair arithmetic as k_pp's mixed form
+            const float4 xi = s.xq[i], xj = s.xq[j];
+            BoxPairF q = box_pair_f(xi, xj, box_shift_f(m, s.xq[m.gsw[iwhich[i]]], s.xq[m.gsw[iwhich[j]]]));
+            float2 ab = m.ljf[((size_t)(code - 1) * m.natyps + m.iac[i]) * m.natyps + m.iac[j]];
+            float el = xi.w * xj.w;
+            if (code == 3) el *= m.el14f;
+            float vel = el * q.r, r6 = q.r2 * q.r2 * q.r2;
+            float va = ab.x * r6 * r6, vb = ab.y * r6;
+            float dv = q.r2 * (-vel - 12.0f * va + 6.0f * vb);
+            acc.grad(i, -q.tx * dv, -q.ty * dv, -q.tz * dv);
+            acc.grad(j, q.tx * dv, q.ty * dv, q.tz * dv);
+            eel.add(vel);
+            evdw.add(va - vb);
+            continue;
+        }
         double sx, sy, sz;
         box_shift(m, x, m.gsw[iwhich[i]], m.gsw[iwhich[j]], sx, sy, sz);
         BoxPair q = box_pair(x, i, j, sx, sy, sz);
@@ -3593,6 +3629,28 @@ __global__ void __launch_bounds__(256) k_box_pw(DevModel m, const DevState* __re
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         int2 e = s.pw[p];
         int i = e.x, j0 = m.nat_solute + m.sa * e.y, ti = m.iac[i];
+        if constexpr (MIX) {
+            const float4 xi = s.xq[i];
+            const float3 sh = box_shift_f(m, s.xq[m.gsw[iwhich[i]]], s.xq[j0]);
+            float g[3] = {0.f, 0.f, 0.f};
+            for (int a = 0; a < m.sa; ++a) {
+                int tw = m.wtype[a];
+                int code = m.ljcod[ti * m.natyps + tw];
+                float2 ab = m.ljf[((size_t)(code - 1) * m.natyps + ti) * m.natyps + tw];
+                BoxPairF q = box_pair_f(xi, s.xq[j0 + a], sh);
+                float vel = xi.w * m.wcrgf[a] * q.r, r6 = q.r2 * q.r2 * q.r2;
+                float va = ab.x * r6 * r6, vb = ab.y * r6;
+                float dv = q.r2 * (-vel - 12.0f * va + 6.0f * vb);
+                g[0] -= q.tx * dv;
+                g[1] -= q.ty * dv;
+                g[2] -= q.tz * dv;
+                acc.grad(j0 + a, q.tx * dv, q.ty * dv, q.tz * dv);
+                eel.add(vel);
+                evdw.add(va - vb);
+            }
+            acc.grad(i, g[0], g[1], g[2]);
+            continue;
+        }
         double sx, sy, sz;
         box_shift(m, x, m.gsw[iwhich[i]], j0, sx, sy, sz);
         double g[3] = {0, 0, 0};
@@ -3631,6 +3689,39 @@ __global__ void __launch_bounds__(256) k_box_ww(DevModel m, const DevState* __re
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         int2 e = s.ww[p];
         int i0 = m.nat_solute + sa * e.x, j0 = m.nat_solute + sa * e.y;
+        if constexpr (MIX) {
+            float4 xi[kMaxSolv], xj[kMaxSolv];
+            for (int a = 0; a < sa; ++a) {
+                xi[a] = s.xq[i0 + a];
+                xj[a] = s.xq[j0 + a];
+            }
+            const float3 sh = box_shift_f(m, xi[0], xj[0]);
+            float gi[kMaxSolv][3] = {}, gj[kMaxSolv][3] = {};
+            for (int la = 0; la < sa; ++la)
+                for (int ka = 0; ka < sa; ++ka) {
+                    bool lj = !SPC || (la == 0 && ka == 0);
+                    int k = la * kMaxSolv + ka;
+                    BoxPairF q = box_pair_f(xi[la], xj[ka], sh);
+                    float vel = m.wwEf[k] * q.r, dv, vdw = 0.0f;
+                    if (lj) {
+                        float r6 = q.r2 * q.r2 * q.r2;
+                        float va = m.wwAf[k] * r6 * r6, vb = m.wwBf[k] * r6;
+                        dv = q.r2 * (-vel - 12.0f * va + 6.0f * vb);
+                        vdw = va - vb;
+                    } else {
+                        dv = q.r2 * (-vel);
+                    }
+                    gi[la][0] -= q.tx * dv; gi[la][1] -= q.ty * dv; gi[la][2] -= q.tz * dv;
+                    gj[ka][0] += q.tx * dv; gj[ka][1] += q.ty * dv; gj[ka][2] += q.tz * dv;
+                    eel.add(vel);
+                    evdw.add(vdw);
+                }
+            for (int a = 0; a < sa; ++a) {
+                acc.grad(i0 + a, gi[a][0], gi[a][1], gi[a][2]);
+                acc.grad(j0 + a, gj[a][0], gj[a][1], gj[a][2]);
+            }
+            continue;
+        }
         double sx, sy, sz;
         box_shift(m, x, i0, j0, sx, sy, sz);
         double gi[kMaxSolv][3] = {}, gj[kMaxSolv][3] = {};
@@ -3680,6 +3771,61 @@ __global__ void __launch_bounds__(256) k_box_q(DevModel m, const DevState* __res
          t += (int64_t)gridDim.x * blockDim.x) {
         int u = (int)(t / nq), iq = (int)(t % nq);
         int i = m.iqseq[iq];
+        if constexpr (MIX) {   // FP32 pair arithmetic (QParF tables), as the mixed Q kernels
+            const float4 xi = s.xq[i], xs = s.xq[m.qswitch];
+            int j0, na;
+            float3 sh;
+            if (WATER) {
+                j0 = m.nat_solute + m.sa * s.qw[u];
+                na = m.sa;
+                sh = box_shift_f(m, xs, s.xq[j0]);
+            } else {
+                j0 = s.qp[u];
+                na = 1;
+                int g = iwhich[j0], ref = m.gatom[m.gslot[g]];
+                const float rq2 = (float)rcq2;
+                for (int a = m.gslot[g]; a < m.gslot[g + 1]; ++a) {
+                    float4 xa = s.xq[m.gatom[a]];
+                    float3 t3 = box_shift_f(m, xa, xs);
+                    float dx = t3.x - (xa.x - xs.x), dy = t3.y - (xa.y - xs.y), dz = t3.z - (xa.z - xs.z);
+                    if (dx * dx + dy * dy + dz * dz <= rq2) {
+                        ref = m.gatom[a];
+                        break;
+                    }
+                }
+                sh = box_shift_f(m, xs, s.xq[ref]);
+            }
+            float gi[3] = {0.f, 0.f, 0.f};
+            for (int a = 0; a < na; ++a) {
+                int j = j0 + a;
+                BoxPairF q = box_pair_f(xi, s.xq[j], sh);
+                bool lj = !(WATER && SPC) || a == 0;
+                float dvs = 0.0f;
+                float r6hc = __fdividef(1.0f, q.r2 * q.r2 * q.r2);
+                for (int st = 0; st < S; ++st) {
+                    const QParF P = WATER ? m.qw_tabf[((size_t)iq * m.sa + a) * S + st]
+                                          : m.qp_tabf[((size_t)j * nq + iq) * S + st];
+                    float lam = s.lambdaf[st];
+                    if (lj) {
+                        float vel, vdw, dv;
+                        nbe_qx_f(q.r2, q.r, r6hc, P.A, P.B, P.el, P.sc, lam, vel, vdw, dv);
+                        dvs += dv;
+                        eel[st].add(vel);
+                        evdw[st].add(vdw);
+                    } else {
+                        float vel = P.el * q.r;
+                        dvs += -q.r2 * vel * lam;
+                        eel[st].add(vel);
+                    }
+                }
+                gi[0] -= q.tx * dvs;
+                gi[1] -= q.ty * dvs;
+                gi[2] -= q.tz * dvs;
+                acc.grad(j, q.tx * dvs, q.ty * dvs, q.tz * dvs);
+            }
+            acc.grad(i, gi[0], gi[1], gi[2]);
+            continue;
+        }
         double sx, sy, sz;
         int j0, na;
         if (WATER) {

@@ -48,9 +48,8 @@ def device(s, prec, xs, lams):
     return d, E, EQ
 
 
-# the box kernels compute in FP64 in both forms; the mixed form's static Q-Q
-# and Q-bonded-P pairs (EQ and the gradient) keep their FP32 pair arithmetic
-@pytest.mark.parametrize("prec,tol,tolq", [(PREC_FP64, 1e-10, 1e-10), (PREC_MIXED, 1e-8, 1e-4)])
+# the mixed form computes its pairs in FP32 (box terms and static Q lists)
+@pytest.mark.parametrize("prec,tol,tolq", [(PREC_FP64, 1e-10, 1e-10), (PREC_MIXED, 1e-4, 1e-4)])
 def test_box_matches_oracle(sysb, prec, tol, tolq):
     s = sysb
     rng = np.random.default_rng(9)
