@@ -476,9 +476,15 @@ int qnb_set_box(qnb_context* ctx, const double* boxlength, int32_t qswitch);
    fk_fix and shell atoms (shell[i] != 0, as make_shell / make_shell2 mark
    them, src/topo.f90:1426-1491) with fk_pshell are restrained harmonically
    to xtop (natom x 3): E = 0.5 fk |x - xtop|^2 into E%restraint%fix / %shell.
-   xtop = NULL removes the restraint.  The freeze option is not supported. */
+   xtop = NULL removes the restraint.  The freeze option: qnb_set_freeze. */
 int qnb_set_shell_restraint(qnb_context* ctx, const double* xtop, const uint8_t* shell, double fk_fix,
                             double fk_pshell);
+/* excluded_freeze (src/potene.f90:401-405, src/bondene.f90:791-855): with
+   freeze != 0 every evaluation puts the excluded atoms back to xtop with zero
+   velocity (the MD velocities, once qnb_md_init ran) and zero fix_shell force
+   constant, and the restraint sections skip excluded atoms in their
+   `ih = 1` (all-atom) selections.  Needs qnb_set_shell_restraint's xtop. */
+int qnb_set_freeze(qnb_context* ctx, int32_t freeze);
 /* The input file's restraint sections, p_restrain (src/bondene.f90:764-1020),
    evaluated inside qnb_compute_dev and qnb_md_run once set (FP64):
      sequence  atoms seq_ij[2k]..seq_ij[2k+1] (heavy atoms, or all with
@@ -497,7 +503,7 @@ int qnb_set_shell_restraint(qnb_context* ctx, const double* xtop, const uint8_t*
    EQ(s)%restraint, the force is unweighted), else the 0-based state s whose
    EQ(s)%restraint gets the energy and whose lambda weights the force.
    Atom indices 0-based; xtop is natom x 3.  r = NULL removes the restraints.
-   The freeze option is not supported. */
+   With qnb_set_freeze on, excluded atoms leave the ih = 1 selections. */
 typedef struct qnb_restraints {
     int32_t nseq;  const int32_t* seq_ij;  const double* seq_fk;  const int32_t* seq_ih;  const int32_t* seq_mode;
     int32_t npos;  const int32_t* pos_i;   const int32_t* pos_state; const double* pos_x;  const double* pos_fk;

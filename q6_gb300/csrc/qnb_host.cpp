@@ -176,6 +176,7 @@ struct qnb_context {
     uint8_t* d_shell_flags = nullptr;
     double* d_xtop = nullptr;
     double fk_fix = 0.0, fk_pshell = 0.0;
+    int freeze = 0;                // excluded_freeze (qnb_set_freeze)
     // bonded terms (qnb_set_bonded)
     bool have_bonded = false;
     BondedDev bonded{};
@@ -1520,7 +1521,7 @@ int enqueue_compute(qnb_context* c, double Tfree, int istep) {
         c->launches++;
     }
     if (c->have_shell) {
-        timed(c, K_RESTRAIN, [&] { launch_fix_shell(L, c->d_shell_flags, c->d_xtop, c->fk_fix, c->fk_pshell, c->mixed); });
+        timed(c, K_RESTRAIN, [&] { launch_fix_shell(L, c->d_shell_flags, c->d_xtop, c->fk_fix, c->fk_pshell, c->mixed, c->freeze, c->md_ready ? c->md.v : nullptr); });
         c->launches++;
     }
     if (c->offd.n > 0) {
@@ -2450,6 +2451,39 @@ int qnb_get_restraint_energies(qnb_context* c, double* Er) {
     return QNB_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// per-atom codes of the restraint atom selection: bit 0 heavy, bit 1 an
+// excluded atom while excluded_freeze is on
+int restraint_atom_codes(qnb_context* c, std::vector<uint8_t>* out) {
+    out->assign(c->h_heavy.begin(), c->h_heavy.end());
+    if (c->freeze) {
+        std::vector<uint8_t> excl(c->natom);
+        CU(cudaMemcpy(excl.data(), c->m.excl, c->natom, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < c->natom; ++i)
+            if (excl[i]) (*out)[i] |= 2;
+    }
+    return QNB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int qnb_set_freeze(qnb_context* c, int32_t freeze) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    c->freeze = freeze ? 1 : 0;
+    if (c->have_restr && c->restr.heavy) {
+        std::vector<uint8_t> codes;
+        TRY(restraint_atom_codes(c, &codes));
+        CU(cudaMemcpy((void*)c->restr.heavy, codes.data(), codes.size(), cudaMemcpyHostToDevice));
+    }
+    ++c->epoch;
+    return QNB_OK;
+}
+
 int qnb_set_restraints(qnb_context* c, const qnb_restraints* r, const double* xtop) {
     if (!c) return fail(QNB_ERR_ARG, "null context");
     CU(cudaSetDevice(c->device));
@@ -2523,7 +2557,8 @@ int qnb_set_restraints(qnb_context* c, const qnb_restraints* r, const double* xt
     };
     std::vector<double> xt(xtop ? xtop : nullptr, xtop ? xtop + 3 * (size_t)n : nullptr);
     std::vector<double> mass(n, 0.0);
-    const std::vector<uint8_t>& heavy = c->h_heavy;
+    std::vector<uint8_t> heavy;
+    TRY(restraint_atom_codes(c, &heavy));
     if (c->md_ready) CU(cudaMemcpy(mass.data(), c->md.mass, sizeof(double) * n, cudaMemcpyDeviceToHost));
     for (int k = 0; k < r->nseq; ++k)
         if (seq[k].w == 1 || seq[k].w == 2)

@@ -307,7 +307,7 @@ void launch_build_box(const Launch& L, const Cut& c, const uint8_t* qnear);
 int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, double rcq2);
 // fix_shell: flag bit 0 excluded (fk_fix), bit 1 shell (fk_pshell); xtop [natom*3]
 void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop, double fk_fix, double fk_pshell,
-                      int mixed);
+                      int mixed, int freeze, double* v);
 
 // ---- device-resident MD step (FP64) ----------------------------------------
 constexpr int kMaxTg = 4;          // temperature coupling groups

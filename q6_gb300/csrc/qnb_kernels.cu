@@ -3292,15 +3292,26 @@ void launch_bonded(const Launch& L, const BondedDev& b, int mixed) {
 
 // fix_shell, src/potene.f90:386-423: excluded atoms (fk_fix) and shell atoms
 // (fk_pshell) restrained to their topology positions, FP64 in both forms
+// With freeze (excluded_freeze) an excluded atom is put back to xtop, its
+// velocity (v, the window's MD velocities, or null) zeroed, and its force
+// constant is zero (src/potene.f90:401-405).
 template <bool MIX>
 __global__ void k_fix_shell(DevModel m, const DevState* __restrict__ states, const uint8_t* __restrict__ flags,
-                            const double* __restrict__ xtop, double fk_fix, double fk_pshell) {
+                            const double* __restrict__ xtop, double fk_fix, double fk_pshell, int freeze,
+                            double* __restrict__ v) {
     const DevState& s = states[blockIdx.y];
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> efix, eshell;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.natom; i += gridDim.x * blockDim.x) {
         const unsigned f = flags[i];
         if (!f) continue;
+        if (freeze && (f & 1u)) {
+            for (int c = 0; c < 3; ++c) {
+                s.x[3 * i + c] = xtop[3 * i + c];
+                if (v) v[((size_t)blockIdx.y * m.natom + i) * 3 + c] = 0.0;
+            }
+            continue;
+        }
         const double fk = (f & 1u) ? fk_fix : fk_pshell;
         double vx = s.x[3 * i] - xtop[3 * i], vy = s.x[3 * i + 1] - xtop[3 * i + 1], vz = s.x[3 * i + 2] - xtop[3 * i + 2];
         double erst = 0.5 * fk * (vx * vx + vy * vy + vz * vz);
@@ -3313,10 +3324,10 @@ __global__ void k_fix_shell(DevModel m, const DevState* __restrict__ states, con
     eshell.flush(acc, E_RST_SHELL);
 }
 void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop, double fk_fix, double fk_pshell,
-                      int mixed) {
+                      int mixed, int freeze, double* v) {
     dim3 g = grid_for(L.m.natom, 64, 8, L.nwin);
-    if (mixed) k_fix_shell<true><<<g, 64, 0, L.st>>>(L.m, L.ds, flags, xtop, fk_fix, fk_pshell);
-    else k_fix_shell<false><<<g, 64, 0, L.st>>>(L.m, L.ds, flags, xtop, fk_fix, fk_pshell);
+    if (mixed) k_fix_shell<true><<<g, 64, 0, L.st>>>(L.m, L.ds, flags, xtop, fk_fix, fk_pshell, freeze, v);
+    else k_fix_shell<false><<<g, 64, 0, L.st>>>(L.m, L.ds, flags, xtop, fk_fix, fk_pshell, freeze, v);
 }
 // offdiag, src/nonbondene.f90:6238-6260: the EVB couplings
 // Hij = A exp(-mu r_kl) of Q-atom pairs, FP64 in both forms
@@ -3945,7 +3956,9 @@ __global__ void __launch_bounds__(kRestrBlock) k_restraints(DevModel m, const De
         const bool wall = b >= r.nseq;
         const int4 q = wall ? r.wall[b - r.nseq] : r.seq[b];
         const int first = q.x, last = q.y, ih = q.z, mode = wall ? 0 : q.w;
-        auto pick = [&](int i) { return r.heavy[i] || ih == 1; };
+        // heavy(i) .or. ih == 1 .and. .not.(excl(i) .and. freeze): bit 0 heavy,
+        // bit 1 an excluded atom frozen (qnb_set_freeze)
+        auto pick = [&](int i) { return (r.heavy[i] & 1) || (ih == 1 && !(r.heavy[i] & 2)); };
         if (wall) {   // half-harmonic wall about xwcent, Morse inside
             const double* p = r.wall_p + 4 * (b - r.nseq);
             const double d0 = p[0], fk = p[1], aM = p[2], dM = p[3];

@@ -42,7 +42,8 @@ EXPORTED = (
     "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
     "qnb_set_bonded", "qnb_get_bonded_energies", "qnb_md_minimize", "qnb_set_shell_restraint",
     "qnb_get_restraint_energies", "qnb_set_offdiag", "qnb_get_offdiag", "qnb_set_restraints",
-    "qnb_set_monitor_groups", "qnb_get_monitor_energies", "qnb_set_group_exclusions", "qnb_get_group_exclusions", "qnb_set_box",
+    "qnb_set_monitor_groups", "qnb_get_monitor_energies", "qnb_set_group_exclusions", "qnb_get_group_exclusions",
+    "qnb_set_box", "qnb_set_freeze",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -103,7 +104,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_set_offdiag": [P, I32, P, P, P, P], "qnb_get_offdiag": [P, P, P], "qnb_set_restraints": [P, P, P],
         "qnb_set_monitor_groups": [P, I32, P, P, I32, P], "qnb_get_monitor_energies": [P, P],
         "qnb_set_group_exclusions": [P, I32, P], "qnb_get_group_exclusions": [P, P],
-        "qnb_set_box": [P, P, I32],
+        "qnb_set_box": [P, P, I32], "qnb_set_freeze": [P, I32],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -464,6 +465,10 @@ class NonbondedEngine:
         return np.concatenate(arrays, axis=1), hdr
 
     # ---- fix_shell ---------------------------------------------------------
+    def set_freeze(self, freeze=True):
+        """excluded_freeze: excluded atoms held at xtop (qnb_set_freeze)."""
+        self._check(self.lib.qnb_set_freeze(self.h, int(bool(freeze))))
+
     def set_shell_restraint(self, xtop, shell, fk_fix=200.0, fk_pshell=10.0):
         """fix_shell restraint to xtop (None removes it); shell: per-atom flags
         (q6_gb300.md.make_shell).  Defaults: qdyn's fk_fix and fk_pshell."""
