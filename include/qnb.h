@@ -568,6 +568,14 @@ typedef struct qnb_md_record {
    k in [mol_first[m], mol_first[m+1]), m < nmol.  Velocities start at 0. */
 int qnb_md_init(qnb_context* ctx, const qnb_md_params* p, const double* mass, int32_t nmol,
                 const int32_t* mol_first, const int32_t* con_ij, const double* con_dist);
+/* Thermostat and integrator (the input's thermostat / integrator keys,
+   src/md.f90:244-301), after qnb_md_init: thermostat 0 Berendsen (default),
+   1 Nose-Hoover (nh_prop + newvel_nos, src/simprep.f90:2509-2550,
+   src/md.f90:1505-1521; nhchains 2..10, nhq <= 0 for the default
+   kbT/tau_T^2, the chain started as init_constraints does); integrator 0
+   leap-frog (default), 1 velocity Verlet (half-step force updates before and
+   after the move, as newvel_* do).  Langevin is not supported. */
+int qnb_md_set_thermostat(qnb_context* ctx, int32_t thermostat, int32_t integrator, int32_t nhchains, double nhq);
 int qnb_md_set_velocities(qnb_context* ctx, int32_t window, const double* v);
 /* x and/or v (natom x 3, either may be NULL) of one window. */
 int qnb_md_get_state(qnb_context* ctx, int32_t window, double* x, double* v);

@@ -7,6 +7,7 @@ baseline of the benchmark; the product package never imports this module.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import subprocess
 
@@ -60,6 +61,7 @@ def lib():
         L.orc_shake.restype = ctypes.c_long
         L.orc_shake.argtypes = [P, P, I, P, P, P, P, P]
         L.orc_md_newvel.argtypes = [I, P, P, P, P, P, D, I, P, P, P]
+        L.orc_md_newvel2.argtypes = [I, P, P, P, P, P, D, D, I, I, P, P, P]
         L.orc_md_velocity.argtypes = [I, P, P, P, D]
         L.orc_md_stop_cm.argtypes = [I, P, P]
         L.orc_md_temperature.argtypes = [I, P, P, P, I, P, P, P, P, D, D, D, D, D, D, P, P]
@@ -261,8 +263,12 @@ class OracleMD:
     BOLTZ = 0.001986
     MAGIC = 0.020462
 
-    def __init__(self, oracle: Oracle, p, cons, sp=None, lam=None, bonded=None, shell=None):
+    def __init__(self, oracle: Oracle, p, cons, sp=None, lam=None, bonded=None, shell=None,
+                 thermostat="berendsen", integrator="leap-frog", nhchains=10, nhq=0.0):
         self.o, self.p, self.cons, self.sp = oracle, p, cons, sp
+        self.nh = thermostat == "nose-hoover"
+        self.vv = integrator == "velocity-verlet"
+        self.nhchains = int(nhchains)
         self.bt = bonded
         self.shell = shell   # (xtop, flags, fk_fix, fk_pshell) or None
         self.lam = None if lam is None else np.asarray(lam, dtype=np.float64)
@@ -286,6 +292,43 @@ class OracleMD:
         if lam is not None:
             oracle.set_lambda(lam)
         self.tfree = 0.0
+        self.temp = 0.0
+        # Nose-Hoover chain, src/simprep.f90:2477-2485 (nhq default kbT/tau_T^2,
+        # src/md.f90:282-285)
+        self.nhq = nhq if nhq > 0.0 else self.BOLTZ * p.temp0 / (self.tau * self.tau)
+        self.qnh = np.full(self.nhchains, self.nhq)
+        self.qnh[0] = p.ndegf * self.nhq
+        self.vnh = np.zeros(self.nhchains)
+        self.xnh = np.zeros(self.nhchains)
+
+    def nh_prop(self):
+        """nh_prop, src/simprep.f90:2509-2550: returns the velocity scale."""
+        M, q, vn, xn = self.nhchains, self.qnh, self.vnh, self.xnh
+        dt2 = 0.5 * self.dt
+        dt4 = 0.5 * dt2
+        dt8 = 0.5 * dt4
+        kbT = self.BOLTZ * self.p.temp0
+        G = np.zeros(M)
+        G[0] = self.p.ndegf * self.BOLTZ * (self.temp - self.p.temp0) / q[0]
+        for i in range(1, M):
+            G[i] = (q[i - 1] * vn[i - 1] * vn[i - 1] - kbT) / q[i]
+        vn[M - 1] = vn[M - 1] + G[M - 1] * dt4
+        xn[M - 1] = xn[M - 1] + vn[M - 1] * dt2
+        ex = 1.0
+        for i in range(M - 2, -1, -1):
+            ex = math.exp(-dt8 * vn[i + 1])
+            vn[i] = (vn[i] * ex + G[i] * dt4) * ex
+            xn[i] = xn[i] + vn[i] * dt2
+        sc = math.exp(-vn[0] * dt2)
+        G[0] = self.p.ndegf * self.BOLTZ * (sc * sc * self.temp - self.p.temp0) / q[0]
+        vn[0] = (vn[0] * ex + G[0] * dt4) * ex
+        for i in range(1, M - 1):
+            ex = math.exp(-dt8 * vn[i + 1])
+            G[i] = (q[i - 1] * vn[i - 1] * vn[i - 1] - kbT) / q[i]
+            vn[i] = (vn[i] * ex + G[i] * dt4) * ex
+        G[M - 1] = (q[M - 2] * vn[M - 2] * vn[M - 2] - kbT) / q[M - 1]
+        vn[M - 1] = vn[M - 1] + G[M - 1] * dt4
+        return sc
 
     def _shake(self, x, ref):
         n = lib().orc_shake(_p(x), _p(ref), self.nmol, _p(self.cons.mol_first), _p(self.ci), _p(self.cj),
@@ -301,6 +344,7 @@ class OracleMD:
                                  self.p.ndegfree, self.p.temp0, self.dt, self.tau, self.BOLTZ, _p(self.sfact),
                                  _p(out))
         self.tfree = out[2]
+        self.temp = out[1]
         return out
 
     def prepare(self, x, v, stop_cm=True):
@@ -378,12 +422,18 @@ class OracleMD:
             if self.sp.wpol_restr:
                 erst[1] = o.watpol(x, d, istep, True)
         xx = np.zeros_like(x)
-        lib().orc_md_newvel(self.n, _p(x), _p(xx), _p(v), _p(d), _p(self.winv), self.dt, self.ntg,
-                            _p(self.first), _p(self.last), _p(self.sfact))
+        if self.nh:
+            v *= self.nh_prop()
+        sf = np.ones(self.ntg) if self.nh else self.sfact
+        lib().orc_md_newvel2(self.n, _p(x), _p(xx), _p(v), _p(d), _p(self.winv), self.dt,
+                             0.5 * self.dt if self.vv else self.dt, int(self.vv), self.ntg,
+                             _p(self.first), _p(self.last), _p(np.ascontiguousarray(sf)))
         iters = 0
         if self.nmol > 0:
             iters = self._shake(x, xx)
             lib().orc_md_velocity(self.n, _p(x), _p(xx), _p(v), self.dt)
+            if self.nh:
+                v *= self.nh_prop()
         t = self.temperature(v)
         return dict(E=E, EQ=EQ, erst=erst, Eb=Eb, EQb=EQb, fix_shell=efs, ekin=t[0], temp=t[1], tfree=t[2],
                     shake_iterations=iters)

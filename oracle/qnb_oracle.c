@@ -1324,6 +1324,24 @@ void orc_md_newvel(int natom, double* x, double* xx, double* v, const double* d,
     (void)natom;
 }
 
+/* newvel_ber / newvel_nos with the force step `step` (dt, or dt/2 for
+   velocity Verlet, which repeats the force half-step after the move),
+   src/md.f90:1451-1466, 1505-1521; sfact 1 for Nose-Hoover */
+void orc_md_newvel2(int natom, double* x, double* xx, double* v, const double* d, const double* winv, double dt,
+                    double step, int vv, int ntg, const int32_t* first, const int32_t* last, const double* sfact) {
+    for (int g = 0; g < ntg; ++g)
+        for (int i = first[g]; i <= last[g]; ++i)
+            for (int c = 0; c < 3; ++c) {
+                int k = 3 * i + c;
+                double vk = (v[k] - d[k] * winv[i] * step) * sfact[g];
+                xx[k] = x[k];
+                x[k] = x[k] + vk * dt;
+                if (vv) vk = (vk - d[k] * winv[i] * step) * sfact[g];
+                v[k] = vk;
+            }
+    (void)natom;
+}
+
 void orc_md_velocity(int natom, const double* x, const double* xx, double* v, double dt) {
     for (int k = 0; k < 3 * natom; ++k) v[k] = (x[k] - xx[k]) / dt;
 }

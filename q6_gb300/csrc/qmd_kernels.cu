@@ -22,7 +22,10 @@ __device__ __forceinline__ int tgroup_of(const MdDev& md, int i) {
     return -1;
 }
 
-// v = (v - d*winv*dt) * sfact;  xx = x;  x = x + v*dt
+// newvel_ber / newvel_nos, src/md.f90:1451-1466, 1505-1521:
+// v = (v - d*winv*step) * sfact;  xx = x;  x = x + v*dt; with velocity Verlet
+// step = dt/2 and the force half-step is applied again after the move.
+// Nose-Hoover scales in nh_prop instead (sfact 1 here).
 __global__ void k_md_newvel(MdDev md, const DevState* __restrict__ states) {
     const int w = blockIdx.y;
     const DevState& s = states[w];
@@ -33,16 +36,18 @@ __global__ void k_md_newvel(MdDev md, const DevState* __restrict__ states) {
     const double* __restrict__ d = s.d;
     const MdWin& mw = md.win[w];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < md.natom; i += gridDim.x * blockDim.x) {
-        int g = tgroup_of(md, i);
+        const int g = md.thermostat == 1 ? 0 : tgroup_of(md, i);
         if (g < 0) continue;
-        const double sf = mw.sfact[g], wi = md.winv[i];
+        const double sf = md.thermostat == 1 ? 1.0 : mw.sfact[g], wi = md.winv[i];
+        const double step = md.vv ? 0.5 * md.dt : md.dt;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const int k = 3 * i + c;
-            double vk = __dmul_rn(__dsub_rn(v[k], __dmul_rn(__dmul_rn(d[k], wi), md.dt)), sf);
-            v[k] = vk;
+            double vk = __dmul_rn(__dsub_rn(v[k], __dmul_rn(__dmul_rn(d[k], wi), step)), sf);
             xx[k] = x[k];
             x[k] = __dadd_rn(x[k], __dmul_rn(vk, md.dt));
+            if (md.vv) vk = __dmul_rn(__dsub_rn(vk, __dmul_rn(__dmul_rn(d[k], wi), step)), sf);
+            v[k] = vk;
         }
     }
 }
@@ -96,6 +101,50 @@ __global__ void k_md_shake(MdDev md, const DevState* __restrict__ states, int mo
         atomicAdd(&mw.shake_iters, (unsigned long long)nits);
         if (!ok) atomicCAS(md.fail + w, 0, m + 1);
     }
+}
+
+// nh_prop, src/simprep.f90:2509-2550, one thread per window: the chain's
+// half-step update around the velocity scale s = exp(-vnh(1) dt/2), driven
+// by the last temperature() (Temp, Ndegf); k_md_scale_v then applies s.
+__global__ void k_md_nh_prop(MdDev md, int nwin) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwin) return;
+    MdWin& mw = md.win[w];
+    const int M = md.nhchains;
+    double* q = mw.qnh;
+    double* vn = mw.vnh;
+    double* xn = mw.xnh;
+    const double dt2 = 0.5 * md.dt, dt4 = 0.5 * dt2, dt8 = 0.5 * dt4;
+    const double kbT = md.boltz * md.temp0;
+    double G[kMaxNh];
+    G[0] = md.ndegf * md.boltz * (mw.temp - md.temp0) / q[0];
+    for (int i = 1; i < M; ++i) G[i] = (q[i - 1] * vn[i - 1] * vn[i - 1] - kbT) / q[i];
+    vn[M - 1] = vn[M - 1] + G[M - 1] * dt4;
+    xn[M - 1] = xn[M - 1] + vn[M - 1] * dt2;
+    double ex = 1.0;
+    for (int i = M - 2; i >= 0; --i) {
+        ex = exp(-dt8 * vn[i + 1]);
+        vn[i] = (vn[i] * ex + G[i] * dt4) * ex;
+        xn[i] = xn[i] + vn[i] * dt2;
+    }
+    const double sc = exp(-vn[0] * dt2);
+    mw.nh_s = sc;
+    G[0] = md.ndegf * md.boltz * (sc * sc * mw.temp - md.temp0) / q[0];
+    vn[0] = (vn[0] * ex + G[0] * dt4) * ex;
+    for (int i = 1; i < M - 1; ++i) {
+        ex = exp(-dt8 * vn[i + 1]);
+        G[i] = (q[i - 1] * vn[i - 1] * vn[i - 1] - kbT) / q[i];
+        vn[i] = (vn[i] * ex + G[i] * dt4) * ex;
+    }
+    G[M - 1] = (q[M - 2] * vn[M - 2] * vn[M - 2] - kbT) / q[M - 1];
+    vn[M - 1] = vn[M - 1] + G[M - 1] * dt4;
+}
+__global__ void k_md_scale_v(MdDev md) {
+    const int w = blockIdx.y;
+    double* __restrict__ v = md.v + (size_t)w * 3 * md.natom;
+    const double sc = md.win[w].nh_s;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * md.natom; k += gridDim.x * blockDim.x)
+        v[k] = __dmul_rn(v[k], sc);
 }
 
 // v = (x - xx) / dt for every atom
@@ -290,6 +339,10 @@ dim3 atoms_grid(const Launch& L, int64_t n, int block) {
 
 }  // namespace
 
+void launch_md_nh(const Launch& L, const MdDev& md) {
+    k_md_nh_prop<<<(L.nwin + 31) / 32, 32, 0, L.st>>>(md, L.nwin);
+    k_md_scale_v<<<dim3((3 * md.natom + 255) / 256, L.nwin), 256, 0, L.st>>>(md);
+}
 void launch_md_newvel(const Launch& L, const MdDev& md) {
     k_md_newvel<<<atoms_grid(L, md.natom, 128), 128, 0, L.st>>>(md, L.ds);
 }

@@ -2112,6 +2112,37 @@ int qnb_md_init(qnb_context* c, const qnb_md_params* p, const double* mass, int3
     return QNB_OK;
 }
 
+int qnb_md_set_thermostat(qnb_context* c, int32_t thermostat, int32_t integrator, int32_t nhchains, double nhq) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    TRY(md_check(c));
+    if (thermostat < 0 || thermostat > 1) return fail(QNB_ERR_ARG, "thermostat %d (0 Berendsen, 1 Nose-Hoover)", thermostat);
+    if (integrator < 0 || integrator > 1) return fail(QNB_ERR_ARG, "integrator %d (0 leap-frog, 1 velocity Verlet)", integrator);
+    if (thermostat == 1 && (nhchains < 2 || nhchains > kMaxNh))
+        return fail(QNB_ERR_ARG, "nhchains %d (2..%d supported)", nhchains, kMaxNh);
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    c->md.thermostat = thermostat;
+    c->md.vv = integrator;
+    c->md.nhchains = thermostat == 1 ? nhchains : 0;
+    // nose-hoover_mass default kbT / tau_T^2 (src/md.f90:282-285), tau_T in internal units
+    c->md.nhq = nhq > 0.0 ? nhq : c->md.boltz * c->md.temp0 / (c->md.tau * c->md.tau);
+    // chain start, src/simprep.f90:2477-2485
+    std::vector<MdWin> win(c->nwin);
+    CU(cudaMemcpy(win.data(), c->md.win, sizeof(MdWin) * c->nwin, cudaMemcpyDeviceToHost));
+    for (auto& mw : win) {
+        for (int i = 0; i < kMaxNh; ++i) {
+            mw.qnh[i] = c->md.nhq;
+            mw.vnh[i] = 0.0;
+            mw.xnh[i] = 0.0;
+        }
+        mw.qnh[0] = c->md.ndegf * c->md.nhq;
+        mw.nh_s = 1.0;
+    }
+    CU(cudaMemcpy(c->md.win, win.data(), sizeof(MdWin) * c->nwin, cudaMemcpyHostToDevice));
+    ++c->epoch;
+    return QNB_OK;
+}
+
 int qnb_md_set_velocities(qnb_context* c, int32_t w, const double* v) {
     TRY(md_check(c));
     if (!v || w < 0 || w >= c->nwin) return fail(QNB_ERR_ARG, "bad window or null velocities");
@@ -2210,14 +2241,21 @@ int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* re
             launch_md_clear_d(L, c->md);
             c->launches++;
             TRY(run_compute(c, -1.0, istep));   // Tfree < 0: restrain_solvent reads it on the device
+            // md_run's step, src/md.f90:1768-1812: thermostat + move, SHAKE,
+            // v = (x - xx)/dt, Nose-Hoover again after SHAKE, temperature
+            const bool nh = c->md.thermostat == 1;
             timed(c, K_MD, [&] {
+                if (nh) launch_md_nh(L, c->md);
                 launch_md_newvel(L, c->md);
                 launch_md_shake(L, c->md, 0);
-                if (c->md.nmol > 0) launch_md_velocity(L, c->md);
+                if (c->md.nmol > 0) {
+                    launch_md_velocity(L, c->md);
+                    if (nh) launch_md_nh(L, c->md);
+                }
                 launch_md_temperature(L, c->md, c->m.excl);
                 launch_md_record(L, c->md, c->e_all, c->efix_all, c->md_rec + (size_t)k * W * kMdRec);
             });
-            c->launches += 4 + (c->md.nmol > 0 ? 1 : 0);
+            c->launches += 4 + (c->md.nmol > 0 ? 1 : 0) + (nh ? (c->md.nmol > 0 ? 4 : 2) : 0);
             TRY(check_launch());
         }
         if (rec || EQ || Eb) {

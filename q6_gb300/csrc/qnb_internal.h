@@ -312,8 +312,11 @@ void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop,
 // ---- device-resident MD step (FP64) ----------------------------------------
 constexpr int kMaxTg = 4;          // temperature coupling groups
 constexpr int kShakeMaxIter = 1000;   // CONST_MAX_ITER, src/globals.f90:520
+constexpr int kMaxNh = 10;         // Nose-Hoover chain length (qdyn's default numchain)
 struct MdWin {                     // per window, device
     double sfact[kMaxTg];          // Berendsen factors of the next newvel
+    double xnh[kMaxNh], vnh[kMaxNh], qnh[kMaxNh];   // Nose-Hoover chain (nh_prop)
+    double nh_s;                   // the last nh_prop's velocity scale
     double temp, tfree, ekin;      // last temperature()
     double tg_temp[kMaxTg], tg_tfree[kMaxTg], tg_texcl[kMaxTg];
     unsigned long long shake_iters;   // SHAKE iterations of the last step, summed over molecules
@@ -323,6 +326,10 @@ struct MdWin {                     // per window, device
 };
 struct MdDev {
     int natom, ntg, nmol;
+    int thermostat;                // 0 Berendsen, 1 Nose-Hoover (qnb_md_set_thermostat)
+    int vv;                        // velocity Verlet: half-step force updates before and after the move
+    int nhchains;
+    double nhq;                    // Nose-Hoover mass
     int tg_first[kMaxTg], tg_last[kMaxTg];
     double tg_ndegf[kMaxTg], tg_ndegfree[kMaxTg], ndegf, ndegfree;
     double dt, tau, temp0, boltz;
@@ -342,6 +349,8 @@ struct MdDev {
 // ekin, temp, tfree, SHAKE iterations
 constexpr int kMdRec = 2 * kNumE + 4;
 void launch_md_newvel(const Launch& L, const MdDev& md);
+// nh_prop (chain update, one thread per window) and v *= s of every atom
+void launch_md_nh(const Launch& L, const MdDev& md);
 // mode 0: constrain x against xx (the step); 1: constrain xx against x
 void launch_md_shake(const Launch& L, const MdDev& md, int mode);
 void launch_md_velocity(const Launch& L, const MdDev& md);

@@ -73,3 +73,43 @@ def test_degrees_of_freedom_rules(small):
     assert len(groups) == 2 and groups[1] == (s.nat_solute, s.natom - 1)
     one = temperature_groups(s, MdSetup(separate_scaling=False))
     assert one == [(0, s.natom - 1)]
+
+
+def test_nose_hoover_removes_heat(small):
+    # the generated structure heats up as its strain relaxes; the chain
+    # (Temp0 150 K) takes the heat out where the uncoupled run keeps it
+    s = small
+
+    def temps(thermostat, tau):
+        setup = MdSetup(stepsize=1.0, tau_t=tau, temp0=150.0, shake_solute=True, shake_heavy=True, cut=CUT)
+        cons = build_constraints(s, setup)
+        o = Oracle(s, use_lrf=False)
+        md = OracleMD(o, md_params(s, setup, cons), cons, lam=[0.7, 0.3], thermostat=thermostat, nhchains=4)
+        x, v = md.prepare(s.x, maxwell_velocities(s, 450.0, 1))
+        return np.array([md.step(x, v, k, CUT)["temp"] for k in range(200)])
+
+    nh = temps("nose-hoover", 10.0)
+    nve = temps("berendsen", 1e12)
+    assert nh[-30:].mean() < 0.9 * nve[-30:].mean()
+    assert nh[-30:].mean() < nh[20:50].mean()
+
+
+def test_velocity_verlet_half_steps(small):
+    # qdyn's velocity Verlet (newvel_*, src/md.f90:1451-1521): two force
+    # half-steps of the same gradient around the move, x += (v - F dt/2) dt
+    # and v -= F dt; without constraints SHAKE does not overwrite v
+    s = small
+    setup = MdSetup(stepsize=0.5, tau_t=1e12, shake_solvent=False, shake_solute=False, cut=CUT)
+    cons = build_constraints(s, setup)
+    o = Oracle(s, use_lrf=False)
+    md = OracleMD(o, md_params(s, setup, cons), cons, lam=[0.7, 0.3], integrator="velocity-verlet")
+    x, v = md.prepare(s.x, maxwell_velocities(s, 300.0, 1))
+    x0, v0 = x.copy(), v.copy()
+    o.make_pair_lists(x0, **CUT)
+    d, _, EQ = o.pot_energy_nonbonds(x0.copy(), np.zeros_like(x0))
+    d, _ = o.nonbond_qq(x0, d, EQ)
+    sf = md.sfact.copy()
+    md.step(x, v, 0, CUT)
+    a = d * md.winv[:, None] * (0.5 * md.dt)
+    np.testing.assert_allclose(x, x0 + (v0 - a) * sf[0] * md.dt, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(v, ((v0 - a) * sf[0] - a) * sf[0], rtol=1e-12, atol=1e-12)
