@@ -403,6 +403,17 @@ typedef struct qnb_bonded {
     int32_t nqtorlib;   const double* qtorlib;    /* [3n] fk rmult delta         */
     int32_t nqimps;     const int32_t* qimpropers; const int32_t* qimproper_code; /* [4n], [n*S] */
     int32_t nqimplib;   const double* qimplib;    /* [2n] fk phi0                */
+    /* [angle_couplings], [torsion_couplings], [improper_couplings]: rows
+       (Q term, Q bond, 1 to couple to bond breaking) with 0-based indices
+       into qangles / qtorsions / qimpropers and qbonds.  The term's energy
+       and force are scaled by gamma = EMorseD of the bond (1 - EMorseD when
+       breaking; 1 while the bond is shorter than r0), and the bond's atoms
+       get dMorse * (unscaled term energy), as qangle, qurey_bradley,
+       qtorsion and qimproper do (src/bondene.f90:387-688).  A coupled bond
+       absent in a state (code -1) gives gamma 1 there. */
+    int32_t nang_coupl; const int32_t* ang_coupl; /* [3n]                       */
+    int32_t ntor_coupl; const int32_t* tor_coupl; /* [3n]                       */
+    int32_t nimp_coupl; const int32_t* imp_coupl; /* [3n]                       */
 } qnb_bonded;
 
 /* Bonded energies of the last evaluation of every window: Eb[w*8 + k] =

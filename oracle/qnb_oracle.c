@@ -1522,8 +1522,48 @@ void orc_bonded(const double* x, double* d, const qnb_bonded* b, int S, const do
         gadd(d, e[0], vscale(c.a, dv)); gadd(d, e[1], vscale(c.b, dv));
         gadd(d, e[2], vscale(c.c, dv)); gadd(d, e[3], vscale(c.d, dv));
     }
+    /* EMorseD / dMorse of every Q bond in the current state (qbond,
+       src/bondene.f90:530-548); gamma 1 and no gradient for a bond absent in
+       the state or shorter than r0 */
+    double* emd = (double*)calloc((size_t)(b->nqbonds > 0 ? b->nqbonds : 1), sizeof(double));
+    v3* dmi = (v3*)calloc((size_t)(b->nqbonds > 0 ? b->nqbonds : 1), sizeof(v3));
     for (int st = 0; st < S; ++st) {
         const double lam = lambda[st];
+        for (int k = 0; k < b->nqbonds; ++k) {
+            int code = b->qbond_code[k * S + st];
+            emd[k] = 1.0;
+            dmi[k] = vscale(dmi[k], 0.0);
+            if (code < 0) continue;
+            const double* L = b->qbondlib + 4 * code;
+            int i = b->qbonds[2 * k], j = b->qbonds[2 * k + 1];
+            v3 av = vsub(X(x, j), X(x, i));
+            double dist = sqrt(vsq(av));
+            double db = dist - L[2];
+            double fexp = exp(-L[1] * db);
+            if (db > 0.0) {
+                emd[k] = -(fexp * fexp - 2.0 * fexp);
+                dmi[k] = vscale(av, 2.0 * L[1] * (fexp - fexp * fexp) * lam / dist);
+            }
+        }
+/* the coupling of term q in table (n, tab): sets gamma, returns the bond or -1 */
+#define COUPLING(n, tab, q, gamma)                                                  \
+    ({                                                                             \
+        int ib_ = -1;                                                              \
+        gamma = 1.0;                                                               \
+        for (int m_ = 0; m_ < (n); ++m_)                                           \
+            if ((tab)[3 * m_] == (q)) {                                            \
+                ib_ = (tab)[3 * m_ + 1];                                           \
+                gamma = emd[ib_];                                                  \
+                if ((tab)[3 * m_ + 2] == 1) gamma = 1.0 - gamma;                   \
+                break;                                                             \
+            }                                                                      \
+        ib_;                                                                       \
+    })
+#define COUPLED_GRAD(ib, e)                                                         \
+    if ((ib) >= 0) {                                                               \
+        gadd(d, b->qbonds[2 * (ib)], vscale(dmi[ib], (e)));                        \
+        gadd(d, b->qbonds[2 * (ib) + 1], vscale(dmi[ib], -(e)));                   \
+    }
         for (int k = 0; k < b->nqbonds; ++k) {
             int code = b->qbond_code[k * S + st];
             if (code < 0) continue;
@@ -1543,13 +1583,17 @@ void orc_bonded(const double* x, double* d, const qnb_bonded* b, int S, const do
             if (code < 0) continue;
             const double* L = b->qanglib + 4 * code;
             const int32_t* e = b->qangles + 3 * k;
+            double gamma;
+            int ib = COUPLING(b->nang_coupl, b->ang_coupl, k, gamma);
             angval c = angle_calc(X(x, e[0]), X(x, e[1]), X(x, e[2]));
             double da = c.angl - L[1];
-            EQb[4 * st + 1] += 0.5 * L[0] * da * da;
-            double dv = L[0] * da * lam;
+            double ae = 0.5 * L[0] * da * da;
+            EQb[4 * st + 1] += ae * gamma;
+            double dv = gamma * L[0] * da * lam;
             gadd(d, e[0], vscale(c.a, dv));
             gadd(d, e[1], vscale(c.b, -dv));
             gadd(d, e[2], vscale(c.c, dv));
+            COUPLED_GRAD(ib, ae)
         }
         if (b->urey_bradley)
             for (int k = 0; k < b->nqangles; ++k) {
@@ -1557,25 +1601,33 @@ void orc_bonded(const double* x, double* d, const qnb_bonded* b, int S, const do
                 if (code < 0 || b->qanglib[4 * code + 2] == 0.0) continue;
                 const double* L = b->qanglib + 4 * code;
                 const int32_t* e = b->qangles + 3 * k;
+                double gamma;
+                int ib = COUPLING(b->nang_coupl, b->ang_coupl, k, gamma);
                 v3 av = vsub(X(x, e[2]), X(x, e[0]));
                 double dist = sqrt(vsq(av));
                 double ru = dist - L[3];
-                EQb[4 * st + 1] += L[2] * ru * ru;
-                double du = 2.0 * (L[2] * ru / dist) * lam;
+                double eu = L[2] * ru * ru;
+                EQb[4 * st + 1] += eu * gamma;
+                double du = gamma * 2.0 * (L[2] * ru / dist) * lam;
                 gadd(d, e[0], vscale(av, -du));
                 gadd(d, e[2], vscale(av, du));
+                COUPLED_GRAD(ib, eu)
             }
         for (int k = 0; k < b->nqtors; ++k) {
             int code = b->qtorsion_code[k * S + st];
             if (code < 0) continue;
             const double* L = b->qtorlib + 3 * code;
             const int32_t* e = b->qtorsions + 4 * k;
+            double gamma;
+            int ib = COUPLING(b->ntor_coupl, b->tor_coupl, k, gamma);
             torval c = torsion_calc(X(x, e[0]), X(x, e[1]), X(x, e[2]), X(x, e[3]));
             double arg = L[1] * c.angl - L[2];
-            EQb[4 * st + 2] += L[0] * (1.0 + cos(arg));
-            double dv = -L[1] * L[0] * sin(arg) * lam;
+            double pe = L[0] * (1.0 + cos(arg));
+            EQb[4 * st + 2] += pe * gamma;
+            double dv = -L[1] * L[0] * sin(arg) * gamma * lam;
             gadd(d, e[0], vscale(c.a, dv)); gadd(d, e[1], vscale(c.b, dv));
             gadd(d, e[2], vscale(c.c, dv)); gadd(d, e[3], vscale(c.d, dv));
+            COUPLED_GRAD(ib, pe)
         }
         for (int k = 0; k < b->nqimps; ++k) {
             int code = b->qimproper_code[k * S + st];
@@ -1583,15 +1635,23 @@ void orc_bonded(const double* x, double* d, const qnb_bonded* b, int S, const do
             const double* L = b->qimplib + 2 * code;
             const int32_t* e = b->qimpropers + 4 * k;
             torval c = torsion_calc(X(x, e[0]), X(x, e[1]), X(x, e[2]), X(x, e[3]));
+            double gamma;
+            int ib = COUPLING(b->nimp_coupl, b->imp_coupl, k, gamma);
             double arg = c.angl - L[1];
             arg = arg - two_pi * round(arg / two_pi);
             double dv = L[0] * arg;
-            EQb[4 * st + 3] += 0.5 * dv * arg;
-            dv = dv * lam;
+            double pe = 0.5 * dv * arg;
+            EQb[4 * st + 3] += pe * gamma;
+            dv = dv * gamma * lam;
             gadd(d, e[0], vscale(c.a, dv)); gadd(d, e[1], vscale(c.b, dv));
             gadd(d, e[2], vscale(c.c, dv)); gadd(d, e[3], vscale(c.d, dv));
+            COUPLED_GRAD(ib, pe)
         }
     }
+#undef COUPLING
+#undef COUPLED_GRAD
+    free(emd);
+    free(dmi);
 }
 
 /* fix_shell, src/potene.f90:386-423: E[0] += fix, E[1] += shell */

@@ -43,6 +43,9 @@ class QnbBonded(ctypes.Structure):
         ("nqtorlib", ctypes.c_int32), ("qtorlib", F64P),
         ("nqimps", ctypes.c_int32), ("qimpropers", I32P), ("qimproper_code", I32P),
         ("nqimplib", ctypes.c_int32), ("qimplib", F64P),
+        ("nang_coupl", ctypes.c_int32), ("ang_coupl", I32P),
+        ("ntor_coupl", ctypes.c_int32), ("tor_coupl", I32P),
+        ("nimp_coupl", ctypes.c_int32), ("imp_coupl", I32P),
     ]
 
 
@@ -87,6 +90,10 @@ class BondedTerms:
     qimpropers: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.int32))
     qimproper_code: np.ndarray = field(default_factory=lambda: np.zeros((0, 1), np.int32))
     qimplib: np.ndarray = field(default_factory=lambda: np.zeros((0, 2)))
+    # Morse couplings: rows (Q term, Q bond, breaking flag), 0-based
+    ang_coupl: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
+    tor_coupl: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
+    imp_coupl: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
 
     def to_struct(self, nstates: int):
         """(QnbBonded, keep-alive list of arrays)."""
@@ -134,6 +141,9 @@ class BondedTerms:
         b.qimpropers, b.nqimps = ip(self.qimpropers, 4)
         b.qimproper_code = codes(self.qimproper_code, b.nqimps)
         b.qimplib, b.nqimplib = fp(self.qimplib, 2)
+        b.ang_coupl, b.nang_coupl = ip(self.ang_coupl, 3)
+        b.tor_coupl, b.ntor_coupl = ip(self.tor_coupl, 3)
+        b.imp_coupl, b.nimp_coupl = ip(self.imp_coupl, 3)
         return b, keep
 
 

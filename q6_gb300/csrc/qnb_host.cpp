@@ -2408,6 +2408,24 @@ int qnb_set_bonded(qnb_context* c, const qnb_bonded* b) {
     TRY(up((int4**)&d.qimps, qi));
     TRY(up((int**)&d.qimp_code, qic));
     TRY(up((double2**)&d.qimplib, qil));
+    // Morse couplings: per Q term the first matching row, bond | breaking << 30
+    auto couplings = [&](int nterm, int n, const int32_t* tab, const char* what, std::vector<int>* out) -> int {
+        out->assign(std::max(nterm, 1), -1);
+        for (int r = 0; r < n; ++r) {
+            int q = tab[3 * r], ib = tab[3 * r + 1], br = tab[3 * r + 2];
+            if (q < 0 || q >= nterm || ib < 0 || ib >= b->nqbonds || br < 0 || br > 1)
+                return fail(QNB_ERR_ARG, "%s coupling %d out of range", what, r);
+            if ((*out)[q] < 0) (*out)[q] = ib | (br << 30);
+        }
+        return QNB_OK;
+    };
+    std::vector<int> cpa, cpt, cpi;
+    TRY(couplings(b->nqangles, b->nang_coupl, b->ang_coupl, "angle", &cpa));
+    TRY(couplings(b->nqtors, b->ntor_coupl, b->tor_coupl, "torsion", &cpt));
+    TRY(couplings(b->nqimps, b->nimp_coupl, b->imp_coupl, "improper", &cpi));
+    TRY(up((int**)&d.qang_cpl, cpa));
+    TRY(up((int**)&d.qtor_cpl, cpt));
+    TRY(up((int**)&d.qimp_cpl, cpi));
     d.nb = b->nbonds; d.nb_sol = b->nbonds_solute;
     d.na = b->nangles; d.na_sol = b->nangles_solute;
     d.nt = b->ntors; d.nt_sol = b->ntors_solute;

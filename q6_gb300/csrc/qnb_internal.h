@@ -257,6 +257,8 @@ struct BondedDev {
     const double4_16a* qtorlib;                      // fk rmult delta -
     const int4* qimps; const int* qimp_code;
     const double2* qimplib;
+    // Morse couplings per Q angle / torsion / improper: -1, or the Q bond | breaking << 30
+    const int* qang_cpl; const int* qtor_cpl; const int* qimp_cpl;
     int nterms;             // classical terms + Q terms x states
 };
 void launch_bonded(const Launch& L, const BondedDev& b, int mixed);

@@ -3087,6 +3087,42 @@ struct BondedSink {
     }
 };
 
+// A Q term's Morse coupling in state st (qbond's EMorseD and dMorse,
+// src/bondene.f90:530-548): gamma and the bond's gradient direction
+// dMorse_i (dMorse_j = -dMorse_i); gamma 1 and no gradient when uncoupled,
+// when the bond is absent in the state or shorter than r0.
+template <typename T>
+struct Coupling {
+    int i = -1, j = -1;
+    T gamma = T(1);
+    V3<T> dmi{T(0), T(0), T(0)};
+};
+template <typename T, typename PF>
+__device__ __forceinline__ Coupling<T> morse_coupling(const BondedDev& b, int cpl, int st, int S, T lam, PF P) {
+    Coupling<T> c;
+    if (cpl < 0) return c;
+    const int ib = cpl & 0x3fffffff, brk = cpl >> 30;
+    const int code = b.qbond_code[ib * S + st];
+    T emd = T(1);
+    if (code >= 0) {
+        int2 e = b.qbonds[ib];
+        double4_16a lib = b.qbondlib[code];
+        const T amz = (T)lib.y, r0 = (T)lib.z;
+        V3<T> av = P(e.y) - P(e.x);
+        T dist = sqrt(vdot(av, av));
+        T db = dist - r0;
+        if (db > T(0)) {
+            T fexp = exp(-amz * db);
+            emd = -(fexp * fexp - T(2) * fexp);
+            c.dmi = av * (T(2) * amz * (fexp - fexp * fexp) * lam / dist);
+            c.i = e.x;
+            c.j = e.y;
+        }
+    }
+    c.gamma = brk ? T(1) - emd : emd;
+    return c;
+}
+
 // One thread per term: classical bonds, angles (+ Urey-Bradley), torsions,
 // impropers; then Q bonds, angles, torsions, impropers per state.  Energies
 // are summed per block in shared memory and added once per block and slot.
@@ -3217,10 +3253,11 @@ __global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevSt
             double4_16a lib = b.qanglib[code];
             const T fk = (T)lib.x, th0 = (T)lib.y, ufk = (T)lib.z, ur0 = (T)lib.w;
             const T l = lam(st);
+            const auto cp = morse_coupling<T>(b, b.qang_cpl[q], st, S, l, P);
             AngleVal<T> c = angle_calc(P(e.x), P(e.y), P(e.z));
             T da = c.angl - th0;
-            T ea = T(0.5) * fk * da * da;
-            T dv = fk * da * l;
+            T ea = T(0.5) * fk * da * da;   // the unscaled energy drives the coupled bond
+            T dv = cp.gamma * fk * da * l;
             out.grad(e.x, c.a * dv);
             out.grad(e.y, -(c.b * dv));
             out.grad(e.z, c.c * dv);
@@ -3229,11 +3266,15 @@ __global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevSt
                 T dist = sqrt(vdot(av, av));
                 T ru = dist - ur0;
                 ea += ufk * ru * ru;
-                T du = T(2) * (ufk * ru / dist) * l;
+                T du = cp.gamma * T(2) * (ufk * ru / dist) * l;
                 out.grad(e.x, -(av * du));
                 out.grad(e.z, av * du);
             }
-            out.energy(qb_slot(st, 1), ea);
+            out.energy(qb_slot(st, 1), ea * cp.gamma);
+            if (cp.i >= 0) {
+                out.grad(cp.i, cp.dmi * ea);
+                out.grad(cp.j, -(cp.dmi * ea));
+            }
             continue;
         }
         u -= b.nqa * S;
@@ -3243,14 +3284,20 @@ __global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevSt
             int4 e = b.qtors[q];
             double4_16a lib = b.qtorlib[code];
             const T fk = (T)lib.x, rm = (T)lib.y, dl = (T)lib.z;
+            const auto cp = morse_coupling<T>(b, b.qtor_cpl[q], st, S, lam(st), P);
             TorsVal<T> c = torsion_calc(P(e.x), P(e.y), P(e.z), P(e.w));
             T arg = rm * c.angl - dl;
-            out.energy(qb_slot(st, 2), fk * (T(1) + cos(arg)));
-            T dv = -rm * fk * sin(arg) * lam(st);
+            T pe = fk * (T(1) + cos(arg));
+            out.energy(qb_slot(st, 2), pe * cp.gamma);
+            T dv = -rm * fk * sin(arg) * cp.gamma * lam(st);
             out.grad(e.x, c.a * dv);
             out.grad(e.y, c.b * dv);
             out.grad(e.z, c.c * dv);
             out.grad(e.w, c.d * dv);
+            if (cp.i >= 0) {
+                out.grad(cp.i, cp.dmi * pe);
+                out.grad(cp.j, -(cp.dmi * pe));
+            }
             continue;
         }
         u -= b.nqt * S;
@@ -3260,16 +3307,22 @@ __global__ void __launch_bounds__(kBondedBlock) k_bonded(DevModel m, const DevSt
             int4 e = b.qimps[q];
             double2 lib = b.qimplib[code];
             const T fk = (T)lib.x, p0 = (T)lib.y;
+            const auto cp = morse_coupling<T>(b, b.qimp_cpl[q], st, S, lam(st), P);
             TorsVal<T> c = torsion_calc(P(e.x), P(e.y), P(e.z), P(e.w));
             T arg = c.angl - p0;
             arg = arg - two_pi * round(arg / two_pi);
             T dv = fk * arg;
-            out.energy(qb_slot(st, 3), T(0.5) * dv * arg);
-            dv = dv * lam(st);
+            T pe = T(0.5) * dv * arg;
+            out.energy(qb_slot(st, 3), pe * cp.gamma);
+            dv = dv * cp.gamma * lam(st);
             out.grad(e.x, c.a * dv);
             out.grad(e.y, c.b * dv);
             out.grad(e.z, c.c * dv);
             out.grad(e.w, c.d * dv);
+            if (cp.i >= 0) {
+                out.grad(cp.i, cp.dmi * pe);
+                out.grad(cp.j, -(cp.dmi * pe));
+            }
         }
     }
     __syncthreads();

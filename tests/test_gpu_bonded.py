@@ -119,3 +119,20 @@ def test_fix_shell_on_gpu(prec):
     scale = np.maximum(np.abs(d0), np.median(np.abs(d0)))
     gtol = 1e-6 if prec == PREC_FP64 else 2e-3
     assert np.all(np.abs(D[0] - d0) <= gtol * scale + 1e-9)
+
+
+@pytest.mark.parametrize("breaking", [0, 1])
+def test_morse_couplings_match_oracle(sys_q, breaking):
+    from tests.test_oracle_bonded import coupled_terms
+    s = sys_q
+    bt = coupled_terms(s, seed=9, breaking=breaking)
+    x = s.x + np.random.default_rng(2).normal(0, 0.03, s.x.shape)
+    lam = [0.35, 0.65]
+    o = Oracle(s)
+    d0, _, _, _ = o.evaluate(x, lam, cut=CUT)
+    d0, Eb0, EQb0 = o.bonded(x, bt, lam, d0)
+    scale = np.maximum(np.abs(d0), np.median(np.abs(d0)))
+    for prec, tol in ((PREC_FP64, 1e-9), (PREC_MIXED, 1e-4)):
+        E, EQ, Eb, EQb, D = device_eval(s, bt, x, [lam], prec)
+        assert np.allclose(EQb[0], EQb0, rtol=tol, atol=tol), prec
+        assert np.all(np.abs(D[0] - d0) <= (1e-6 if prec == PREC_FP64 else 1e-3) * scale + 1e-9), prec

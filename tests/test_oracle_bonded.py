@@ -82,3 +82,46 @@ def test_removal_rules():
     heavy = np.array([1, 1, 1, 1, 1, 0, 1], bool)
     sh = remove_shaken(r, heavy, nat_solute=5)
     assert sh.bonds[:, 2].tolist() == [0, -1, 0, -1]   # solvent bond with a hydrogen constrained
+
+
+def coupled_terms(s, seed, breaking=0):
+    """Generated bonded terms with Morse couplings ([angle_couplings] etc.):
+    the first Q angle, torsion and improper coupled to Q bonds whose r0 is
+    shortened so the bonds are stretched (EMorseD < 1)."""
+    bt = synthetic_bonded(s, seed=seed)
+    bt.qbondlib = np.array(bt.qbondlib, dtype=np.float64)
+    bt.qbondlib[:, 2] -= 0.15
+    nb = len(bt.qbonds)
+    assert nb >= 2 and len(bt.qangles) >= 2
+    bt.ang_coupl = np.array([[0, 0, breaking], [1, nb - 1, 0]], np.int32)
+    if len(bt.qtorsions):
+        bt.tor_coupl = np.array([[0, 1, breaking]], np.int32)
+    if len(bt.qimpropers):
+        bt.imp_coupl = np.array([[0, 0, 0]], np.int32)
+    return bt
+
+
+def test_morse_coupled_gradient_matches_finite_differences(sys_b):
+    s = sys_b
+    bt = coupled_terms(s, seed=3)
+    lam = np.array([0.3, 0.7])
+    x = s.x + np.random.default_rng(5).normal(0, 0.03, s.x.shape)
+    o = Oracle(s)
+    d, _, EQb = o.bonded(x, bt, lam)
+    _, _, EQu = o.bonded(x, _uncoupled(bt), lam)
+    assert not np.allclose(EQb[:, 1], EQu[:, 1])   # the coupling changes the angle energy
+    atoms = sorted({int(a) for a in np.concatenate([bt.qangles[:2].ravel(), bt.qbonds[[0, -1]].ravel()])})
+    h = 1e-5
+    for a in atoms:
+        for c in range(3):
+            xp, xm = x.copy(), x.copy()
+            xp[a, c] += h
+            xm[a, c] -= h
+            fd = (energy(o, xp, bt, lam) - energy(o, xm, bt, lam)) / (2 * h)
+            assert abs(fd - d[a, c]) <= 1e-5 * max(1.0, abs(fd)), (a, c, fd, d[a, c])
+
+
+def _uncoupled(bt):
+    import dataclasses
+    return dataclasses.replace(bt, ang_coupl=np.zeros((0, 3), np.int32), tor_coupl=np.zeros((0, 3), np.int32),
+                               imp_coupl=np.zeros((0, 3), np.int32))
