@@ -585,8 +585,14 @@ int qnb_md_init(qnb_context* ctx, const qnb_md_params* p, const double* mass, in
    src/md.f90:1505-1521; nhchains 2..10, nhq <= 0 for the default
    kbT/tau_T^2, the chain started as init_constraints does); integrator 0
    leap-frog (default), 1 velocity Verlet (half-step force updates before and
-   after the move, as newvel_* do).  Langevin is not supported. */
+   after the move, as newvel_* do).  Langevin: qnb_md_set_langevin. */
 int qnb_md_set_thermostat(qnb_context* ctx, int32_t thermostat, int32_t integrator, int32_t nhchains, double nhq);
+/* Langevin thermostat (newvel_lan with uniform random forces, the
+   default of src/md.f90:1468-1503, 1632-1648): friction <= 0 for 1/tau_T,
+   integrator as qnb_md_set_thermostat.  The random forces are uniform draws
+   from SplitMix64 keyed by (seed, window, step, atom component), not qdyn's
+   randm sequence: the same distribution, not the same numbers. */
+int qnb_md_set_langevin(qnb_context* ctx, int32_t integrator, double friction, uint64_t seed);
 int qnb_md_set_velocities(qnb_context* ctx, int32_t window, const double* v);
 /* x and/or v (natom x 3, either may be NULL) of one window. */
 int qnb_md_get_state(qnb_context* ctx, int32_t window, double* x, double* v);

@@ -62,6 +62,7 @@ def lib():
         L.orc_shake.argtypes = [P, P, I, P, P, P, P, P]
         L.orc_md_newvel.argtypes = [I, P, P, P, P, P, D, I, P, P, P]
         L.orc_md_newvel2.argtypes = [I, P, P, P, P, P, D, D, I, I, P, P, P]
+        L.orc_md_newvel_lan.argtypes = [I, P, P, P, P, P, D, D, I, D, D, ctypes.c_uint64, I, I]
         L.orc_md_velocity.argtypes = [I, P, P, P, D]
         L.orc_md_stop_cm.argtypes = [I, P, P]
         L.orc_md_temperature.argtypes = [I, P, P, P, I, P, P, P, P, D, D, D, D, D, D, P, P]
@@ -264,9 +265,11 @@ class OracleMD:
     MAGIC = 0.020462
 
     def __init__(self, oracle: Oracle, p, cons, sp=None, lam=None, bonded=None, shell=None,
-                 thermostat="berendsen", integrator="leap-frog", nhchains=10, nhq=0.0):
+                 thermostat="berendsen", integrator="leap-frog", nhchains=10, nhq=0.0, friction=0.0, seed=1):
         self.o, self.p, self.cons, self.sp = oracle, p, cons, sp
         self.nh = thermostat == "nose-hoover"
+        self.lan = thermostat == "langevin"
+        self.seed = int(seed)
         self.vv = integrator == "velocity-verlet"
         self.nhchains = int(nhchains)
         self.bt = bonded
@@ -300,6 +303,10 @@ class OracleMD:
         self.qnh[0] = p.ndegf * self.nhq
         self.vnh = np.zeros(self.nhchains)
         self.xnh = np.zeros(self.nhchains)
+        # Langevin, src/md.f90:250-253, 1632-1648 (uniform random forces)
+        self.friction = friction if friction > 0.0 else 1.0 / self.tau
+        step = 0.5 * self.dt if self.vv else self.dt
+        self.gkT = 24.0 * self.friction * self.BOLTZ * p.temp0 / step
 
     def nh_prop(self):
         """nh_prop, src/simprep.f90:2509-2550: returns the velocity scale."""
@@ -425,9 +432,13 @@ class OracleMD:
         if self.nh:
             v *= self.nh_prop()
         sf = np.ones(self.ntg) if self.nh else self.sfact
-        lib().orc_md_newvel2(self.n, _p(x), _p(xx), _p(v), _p(d), _p(self.winv), self.dt,
-                             0.5 * self.dt if self.vv else self.dt, int(self.vv), self.ntg,
-                             _p(self.first), _p(self.last), _p(np.ascontiguousarray(sf)))
+        step = 0.5 * self.dt if self.vv else self.dt
+        if self.lan:
+            lib().orc_md_newvel_lan(self.n, _p(x), _p(xx), _p(v), _p(d), _p(self.winv), self.dt, step,
+                                    int(self.vv), self.friction, self.gkT, self.seed, 0, int(istep))
+        else:
+            lib().orc_md_newvel2(self.n, _p(x), _p(xx), _p(v), _p(d), _p(self.winv), self.dt, step, int(self.vv),
+                                 self.ntg, _p(self.first), _p(self.last), _p(np.ascontiguousarray(sf)))
         iters = 0
         if self.nmol > 0:
             iters = self._shake(x, xx)

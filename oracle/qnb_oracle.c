@@ -1342,6 +1342,36 @@ void orc_md_newvel2(int natom, double* x, double* xx, double* v, const double* d
     (void)natom;
 }
 
+/* newvel_lan, src/md.f90:1468-1503, with the uniform random forces drawn
+   from SplitMix64 keyed by (seed, window, step, component) as the device
+   does (qdyn's own randm stream is sequential) */
+static uint64_t orc_splitmix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+void orc_md_newvel_lan(int natom, double* x, double* xx, double* v, const double* d, const double* winv, double dt,
+                       double step, int vv, double friction, double gkT, uint64_t seed, int window, int istep) {
+    const double lf = 1.0 - friction * step;
+    for (int i = 0; i < natom; ++i) {
+        const double rs = sqrt(gkT / winv[i]);
+        for (int c = 0; c < 3; ++c) {
+            int k = 3 * i + c;
+            uint64_t z = orc_splitmix64(orc_splitmix64(orc_splitmix64(seed + (uint64_t)window) + (uint64_t)(uint32_t)istep) +
+                                        (uint64_t)k);
+            double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+            double re = rs * (u - 0.5);
+            double fd = (d[k] - re) * winv[i] * step;
+            double vk = v[k] * lf - fd;
+            xx[k] = x[k];
+            x[k] = x[k] + vk * dt;
+            if (vv) vk = vk * lf - fd;
+            v[k] = vk;
+        }
+    }
+}
+
 void orc_md_velocity(int natom, const double* x, const double* xx, double* v, double dt) {
     for (int k = 0; k < 3 * natom; ++k) v[k] = (x[k] - xx[k]) / dt;
 }

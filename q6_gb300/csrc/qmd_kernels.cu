@@ -26,6 +26,22 @@ __device__ __forceinline__ int tgroup_of(const MdDev& md, int i) {
 // v = (v - d*winv*step) * sfact;  xx = x;  x = x + v*dt; with velocity Verlet
 // step = dt/2 and the force half-step is applied again after the move.
 // Nose-Hoover scales in nh_prop instead (sfact 1 here).
+// Langevin random forces: a uniform draw per (window, step, atom component)
+// from SplitMix64 (Steele, Lea and Flood 2014) chained over seed, window,
+// step and component; the reference draws from its own sequential randm
+// stream, which a parallel step cannot reproduce (same distribution).
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double lan_uniform(unsigned long long seed, int w, int istep, int k) {
+    unsigned long long z = splitmix64(splitmix64(splitmix64(seed + (unsigned long long)w) +
+                                                 (unsigned long long)(unsigned)istep) + (unsigned long long)k);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
 __global__ void k_md_newvel(MdDev md, const DevState* __restrict__ states) {
     const int w = blockIdx.y;
     const DevState& s = states[w];
@@ -36,6 +52,24 @@ __global__ void k_md_newvel(MdDev md, const DevState* __restrict__ states) {
     const double* __restrict__ d = s.d;
     const MdWin& mw = md.win[w];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < md.natom; i += gridDim.x * blockDim.x) {
+        if (md.thermostat == 2) {   // newvel_lan, src/md.f90:1468-1503 (uniform random forces)
+            const double wi = md.winv[i];
+            const double step = md.vv ? 0.5 * md.dt : md.dt;
+            const double lf = 1.0 - md.lan_friction * step;
+            const double rs = sqrt(__ddiv_rn(md.lan_gkT, wi));
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const int k = 3 * i + c;
+                const double re = __dmul_rn(rs, __dsub_rn(lan_uniform(md.lan_seed, w, md.istep, k), 0.5));
+                const double fd = __dmul_rn(__dmul_rn(__dsub_rn(d[k], re), wi), step);
+                double vk = __dsub_rn(__dmul_rn(v[k], lf), fd);
+                xx[k] = x[k];
+                x[k] = __dadd_rn(x[k], __dmul_rn(vk, md.dt));
+                if (md.vv) vk = __dsub_rn(__dmul_rn(vk, lf), fd);
+                v[k] = vk;
+            }
+            continue;
+        }
         const int g = md.thermostat == 1 ? 0 : tgroup_of(md, i);
         if (g < 0) continue;
         const double sf = md.thermostat == 1 ? 1.0 : mw.sfact[g], wi = md.winv[i];

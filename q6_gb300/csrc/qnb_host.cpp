@@ -2143,6 +2143,24 @@ int qnb_md_set_thermostat(qnb_context* c, int32_t thermostat, int32_t integrator
     return QNB_OK;
 }
 
+int qnb_md_set_langevin(qnb_context* c, int32_t integrator, double friction, uint64_t seed) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    TRY(md_check(c));
+    if (integrator < 0 || integrator > 1) return fail(QNB_ERR_ARG, "integrator %d (0 leap-frog, 1 velocity Verlet)", integrator);
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    c->md.thermostat = 2;
+    c->md.vv = integrator;
+    // langevin_friction default 1/tau_T (src/md.f90:250-253); gkT with
+    // uniform draws, src/md.f90:1637-1648
+    c->md.lan_friction = friction > 0.0 ? friction : 1.0 / c->md.tau;
+    const double step = integrator ? 0.5 * c->md.dt : c->md.dt;
+    c->md.lan_gkT = 24.0 * c->md.lan_friction * c->md.boltz * c->md.temp0 / step;
+    c->md.lan_seed = seed;
+    ++c->epoch;
+    return QNB_OK;
+}
+
 int qnb_md_set_velocities(qnb_context* c, int32_t w, const double* v) {
     TRY(md_check(c));
     if (!v || w < 0 || w >= c->nwin) return fail(QNB_ERR_ARG, "bad window or null velocities");
@@ -2244,6 +2262,7 @@ int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* re
             // md_run's step, src/md.f90:1768-1812: thermostat + move, SHAKE,
             // v = (x - xx)/dt, Nose-Hoover again after SHAKE, temperature
             const bool nh = c->md.thermostat == 1;
+            c->md.istep = istep;
             timed(c, K_MD, [&] {
                 if (nh) launch_md_nh(L, c->md);
                 launch_md_newvel(L, c->md);

@@ -328,10 +328,13 @@ struct MdWin {                     // per window, device
 };
 struct MdDev {
     int natom, ntg, nmol;
-    int thermostat;                // 0 Berendsen, 1 Nose-Hoover (qnb_md_set_thermostat)
+    int thermostat;                // 0 Berendsen, 1 Nose-Hoover, 2 Langevin (qnb_md_set_thermostat / _langevin)
     int vv;                        // velocity Verlet: half-step force updates before and after the move
     int nhchains;
     double nhq;                    // Nose-Hoover mass
+    double lan_friction, lan_gkT;  // Langevin: friction, 24 friction Boltz Temp0 / step (uniform draws)
+    unsigned long long lan_seed;
+    int istep;                     // the step newvel integrates (Langevin random-force counter)
     int tg_first[kMaxTg], tg_last[kMaxTg];
     double tg_ndegf[kMaxTg], tg_ndegfree[kMaxTg], ndegf, ndegfree;
     double dt, tau, temp0, boltz;

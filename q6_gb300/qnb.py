@@ -43,7 +43,7 @@ EXPORTED = (
     "qnb_set_bonded", "qnb_get_bonded_energies", "qnb_md_minimize", "qnb_set_shell_restraint",
     "qnb_get_restraint_energies", "qnb_set_offdiag", "qnb_get_offdiag", "qnb_set_restraints",
     "qnb_set_monitor_groups", "qnb_get_monitor_energies", "qnb_set_group_exclusions", "qnb_get_group_exclusions",
-    "qnb_set_box", "qnb_set_freeze", "qnb_md_set_thermostat",
+    "qnb_set_box", "qnb_set_freeze", "qnb_md_set_thermostat", "qnb_md_set_langevin",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -105,6 +105,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_set_monitor_groups": [P, I32, P, P, I32, P], "qnb_get_monitor_energies": [P, P],
         "qnb_set_group_exclusions": [P, I32, P], "qnb_get_group_exclusions": [P, P],
         "qnb_set_box": [P, P, I32], "qnb_set_freeze": [P, I32], "qnb_md_set_thermostat": [P, I32, I32, I32, D],
+        "qnb_md_set_langevin": [P, I32, D, ctypes.c_uint64],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -316,6 +317,11 @@ class NonbondedEngine:
         t = {"berendsen": 0, "nose-hoover": 1}[thermostat]
         g = {"leap-frog": 0, "velocity-verlet": 1}[integrator]
         self._check(self.lib.qnb_md_set_thermostat(self.h, t, g, int(nhchains), float(nhq)))
+
+    def md_set_langevin(self, integrator="leap-frog", friction=0.0, seed=1):
+        """Langevin thermostat (uniform random forces); friction <= 0 takes 1/tau_T."""
+        g = {"leap-frog": 0, "velocity-verlet": 1}[integrator]
+        self._check(self.lib.qnb_md_set_langevin(self.h, g, float(friction), int(seed)))
 
     def md_set_velocities(self, v, window=None):
         """v: [natom, 3] for one window (or every window if window is None),

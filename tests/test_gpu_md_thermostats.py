@@ -1,4 +1,6 @@
-"""Nose-Hoover thermostat and velocity Verlet on the device (qnb_md_set_thermostat;
+"""Nose-Hoover and Langevin thermostats and velocity Verlet on the device
+(qnb_md_set_thermostat, qnb_md_set_langevin; newvel_lan with the same
+SplitMix64 random forces as the oracle;
 nh_prop, src/simprep.f90:2509-2550; newvel_nos / newvel_ber with the
 velocity-Verlet half steps, src/md.f90:1451-1521, 1768-1812) against the
 oracle's MD step in the FP64 form: per-step energies, temperatures and the
@@ -23,7 +25,9 @@ def system():
 
 @pytest.mark.parametrize("thermostat,integrator,chains", [("nose-hoover", "leap-frog", 10),
                                                           ("nose-hoover", "velocity-verlet", 3),
-                                                          ("berendsen", "velocity-verlet", 10)])
+                                                          ("berendsen", "velocity-verlet", 10),
+                                                          ("langevin", "leap-frog", 0),
+                                                          ("langevin", "velocity-verlet", 0)])
 def test_fp64_matches_oracle(system, thermostat, integrator, chains):
     s = system
     lam = [0.6, 0.4]
@@ -35,7 +39,10 @@ def test_fp64_matches_oracle(system, thermostat, integrator, chains):
         e.set_lambda(lam)
         e.set_coordinates_dev(s.x[None])
         e.md_init(SETUP)
-        e.md_set_thermostat(thermostat, integrator, nhchains=chains)
+        if thermostat == "langevin":
+            e.md_set_langevin(integrator, seed=7)
+        else:
+            e.md_set_thermostat(thermostat, integrator, nhchains=chains)
         e.md_set_velocities(v0[None])
         e.md_prepare(stop_cm=True)
         rec, EQ, _ = e.md_run(n)
@@ -44,7 +51,7 @@ def test_fp64_matches_oracle(system, thermostat, integrator, chains):
     o.set_solvent_params(sp)
     cons = build_constraints(s, SETUP)
     md = OracleMD(o, md_params(s, SETUP, cons), cons, sp=sp, lam=lam, thermostat=thermostat,
-                  integrator=integrator, nhchains=chains)
+                  integrator=integrator, nhchains=max(chains, 2), seed=7)
     x, v = md.prepare(s.x, v0)
     for k in range(n):
         r = md.step(x, v, k, CUT)

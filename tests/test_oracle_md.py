@@ -113,3 +113,14 @@ def test_velocity_verlet_half_steps(small):
     a = d * md.winv[:, None] * (0.5 * md.dt)
     np.testing.assert_allclose(x, x0 + (v0 - a) * sf[0] * md.dt, rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(v, ((v0 - a) * sf[0] - a) * sf[0], rtol=1e-12, atol=1e-12)
+
+
+def test_langevin_pulls_temperature_to_target(small):
+    s = small
+    setup = MdSetup(stepsize=1.0, tau_t=10.0, temp0=150.0, shake_solute=True, shake_heavy=True, cut=CUT)
+    cons = build_constraints(s, setup)
+    o = Oracle(s, use_lrf=False)
+    md = OracleMD(o, md_params(s, setup, cons), cons, lam=[0.7, 0.3], thermostat="langevin", seed=7)
+    x, v = md.prepare(s.x, maxwell_velocities(s, 450.0, 1))
+    t = np.array([md.step(x, v, k, CUT)["temp"] for k in range(200)])
+    assert abs(t[-50:].mean() - 150.0) < 0.35 * 150.0
