@@ -478,8 +478,8 @@ int qnb_get_group_exclusions(qnb_context* ctx, double* out);
    nonbond_qq does.  Cut-offs must not exceed half the shortest edge.
    boxlength = NULL returns to the sphere.  Not supported with a box
    (QNB_ERR_UNSUPPORTED): LRF, any-atom group cut-offs, excluded atoms,
-   solvent restraints and solvent internal pairs; constant pressure and
-   put_back_in_box are the caller's. */
+   solvent restraints and solvent internal pairs.  Constant pressure is the
+   caller's; put_back_in_box: qnb_set_put_back_in_box. */
 int qnb_set_box(qnb_context* ctx, const double* boxlength, int32_t qswitch);
 
 /* fix_shell (src/potene.f90:386-423), evaluated inside qnb_compute_dev and
@@ -593,6 +593,19 @@ int qnb_md_set_thermostat(qnb_context* ctx, int32_t thermostat, int32_t integrat
    from SplitMix64 keyed by (seed, window, step, atom component), not qdyn's
    randm sequence: the same distribution, not the same numbers. */
 int qnb_md_set_langevin(qnb_context* ctx, int32_t integrator, double friction, uint64_t seed);
+/* put_back_in_box (src/simprep.f90:4177-4352) for a periodic box, after
+   qnb_md_init: molecule q is atoms[mol_first[q] .. mol_first[q+1]), the
+   first nmol_solute of them solute; put_solute / put_solvent select which
+   are wrapped (put_solute_back_in_box / put_solvent_back_in_box).  The box
+   centre is boxcentre (rigid_box_centre), or NULL for the mean of the solute
+   atoms (of all atoms without solute) at each call.  A molecule whose mass
+   centre lies beyond half a box edge from the centre moves by one edge on
+   that axis.  qnb_md_run calls it every NBcycle steps before the lists, as
+   md_run does; qnb_put_back_in_box calls it now and returns the centres
+   ([nwin][3], or NULL). */
+int qnb_set_put_back_in_box(qnb_context* ctx, int32_t nmol, const int32_t* mol_first, const int32_t* atoms,
+                            int32_t nmol_solute, int32_t put_solute, int32_t put_solvent, const double* boxcentre);
+int qnb_put_back_in_box(qnb_context* ctx, double* boxcentre);
 int qnb_md_set_velocities(qnb_context* ctx, int32_t window, const double* v);
 /* x and/or v (natom x 3, either may be NULL) of one window. */
 int qnb_md_get_state(qnb_context* ctx, int32_t window, double* x, double* v);

@@ -222,3 +222,27 @@ def box_energies(s, x, lam, L, qswitch, cut, lists=None):
                     EQ[st, 4] += vel
                     EQ[st, 5] += vdw
     return d, E, EQ
+
+
+def put_back_in_box(x, L, molecules, mass, nmol_solute, nat_solute, put_solute=True, put_solvent=True,
+                    boxcentre=None):
+    """put_back_in_box (src/simprep.f90:4177-4352): returns (x, centre)."""
+    x = np.array(x, dtype=np.float64)
+    L = np.asarray(L, np.float64)
+    if boxcentre is None:
+        n = nat_solute if nat_solute > 0 else len(x)
+        c = x[:n].mean(0)
+    else:
+        c = np.asarray(boxcentre, np.float64)
+    lo, hi = c - L / 2.0, c + L / 2.0
+    first = 0 if put_solute else nmol_solute
+    last = len(molecules) if put_solvent else nmol_solute
+    for mol in molecules[first:last]:
+        mol = np.asarray(mol)
+        cm = (x[mol] * mass[mol][:, None]).sum(0) * (1.0 / mass[mol].sum())
+        for k in range(3):
+            if cm[k] > hi[k]:
+                x[mol, k] -= L[k]
+            elif cm[k] < lo[k]:
+                x[mol, k] += L[k]
+    return x, c

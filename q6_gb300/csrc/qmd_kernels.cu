@@ -207,6 +207,54 @@ __global__ void k_md_copy_x(MdDev md, const DevState* __restrict__ states, int m
 // temperature(): one block per window; kinetic energies summed per group
 // (all, non-excluded, excluded) by a fixed-order tree
 constexpr int kTempBlock = 256;
+
+// put_back_in_box, src/simprep.f90:4177-4352: the box centre (boxcentre
+// fixed, or the plain mean of the solute atoms, else of all atoms), then every
+// selected molecule whose mass centre lies outside the box around it moves by
+// one box length per axis.  One block per window.
+__global__ void __launch_bounds__(kTempBlock) k_md_put_back(DevModel m, MdDev md, const DevState* __restrict__ states) {
+    __shared__ double red[3][kTempBlock];
+    const int w = blockIdx.x;
+    double* __restrict__ x = states[w].x;
+    double c[3] = {md.pb_centre[0], md.pb_centre[1], md.pb_centre[2]};
+    if (!md.pb_rigid) {
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int i = threadIdx.x; i < md.pb_nslu; i += kTempBlock) {
+            sx += x[3 * i];
+            sy += x[3 * i + 1];
+            sz += x[3 * i + 2];
+        }
+        red[0][threadIdx.x] = sx;
+        red[1][threadIdx.x] = sy;
+        red[2][threadIdx.x] = sz;
+        __syncthreads();
+        for (int h = kTempBlock / 2; h > 0; h >>= 1) {
+            if (threadIdx.x < h)
+                for (int k = 0; k < 3; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+            __syncthreads();
+        }
+        for (int k = 0; k < 3; ++k) c[k] = red[k][0] / (double)md.pb_nslu;
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; ++k) md.pb_boxc[3 * w + k] = c[k];
+    for (int mol = md.pb_first_mol + threadIdx.x; mol < md.pb_last_mol; mol += kTempBlock) {
+        double cm[3] = {0.0, 0.0, 0.0}, mt = 0.0;
+        for (int q = md.pb_mol_first[mol]; q < md.pb_mol_first[mol + 1]; ++q) {
+            const int a = md.pb_atoms[q];
+            const double ma = md.mass[a];
+            mt += ma;
+            for (int k = 0; k < 3; ++k) cm[k] += x[3 * a + k] * ma;
+        }
+        for (int k = 0; k < 3; ++k) {
+            const double cmk = cm[k] * (1.0 / mt);
+            const double hi = c[k] + m.boxl[k] / 2.0, lo = c[k] - m.boxl[k] / 2.0;
+            const double sh = cmk > hi ? -m.boxl[k] : (cmk < lo ? m.boxl[k] : 0.0);
+            if (sh != 0.0)
+                for (int q = md.pb_mol_first[mol]; q < md.pb_mol_first[mol + 1]; ++q) x[3 * md.pb_atoms[q] + k] += sh;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kTempBlock) k_md_temperature(MdDev md, const uint8_t* __restrict__ excl) {
     const int w = blockIdx.x;
     const size_t off = (size_t)w * 3 * md.natom;
@@ -373,6 +421,9 @@ dim3 atoms_grid(const Launch& L, int64_t n, int block) {
 
 }  // namespace
 
+void launch_md_put_back(const Launch& L, const MdDev& md) {
+    k_md_put_back<<<L.nwin, kTempBlock, 0, L.st>>>(L.m, md, L.ds);
+}
 void launch_md_nh(const Launch& L, const MdDev& md) {
     k_md_nh_prop<<<(L.nwin + 31) / 32, 32, 0, L.st>>>(md, L.nwin);
     k_md_scale_v<<<dim3((3 * md.natom + 255) / 256, L.nwin), 256, 0, L.st>>>(md);

@@ -2161,6 +2161,48 @@ int qnb_md_set_langevin(qnb_context* c, int32_t integrator, double friction, uin
     return QNB_OK;
 }
 
+int qnb_set_put_back_in_box(qnb_context* c, int32_t nmol, const int32_t* mol_first, const int32_t* atoms,
+                            int32_t nmol_solute, int32_t put_solute, int32_t put_solvent, const double* boxcentre) {
+    if (!c || nmol < 0 || (nmol > 0 && (!mol_first || !atoms))) return fail(QNB_ERR_ARG, "null argument");
+    TRY(md_check(c));
+    if (nmol_solute < 0 || nmol_solute > nmol) return fail(QNB_ERR_ARG, "nmol_solute out of range");
+    for (int q = 0; q < nmol; ++q)
+        if (mol_first[q] < 0 || mol_first[q + 1] <= mol_first[q]) return fail(QNB_ERR_ARG, "molecule %d empty", q);
+    for (int q = 0; nmol > 0 && q < mol_first[nmol]; ++q)
+        if (atoms[q] < 0 || atoms[q] >= c->natom) return fail(QNB_ERR_ARG, "molecule atom %d out of range", q);
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    MdDev& md = c->md;
+    md.pb_nmol = nmol;
+    md.pb_first_mol = put_solute ? 0 : nmol_solute;
+    md.pb_last_mol = put_solvent ? nmol : nmol_solute;
+    md.pb_rigid = boxcentre != nullptr;
+    md.pb_nslu = c->nat_solute > 0 ? c->nat_solute : c->natom;
+    for (int k = 0; k < 3; ++k) md.pb_centre[k] = boxcentre ? boxcentre[k] : 0.0;
+    if (nmol > 0) {
+        std::vector<int> first(mol_first, mol_first + nmol + 1), at(atoms, atoms + mol_first[nmol]);
+        TRY(c->upload((int**)&md.pb_mol_first, first));
+        TRY(c->upload((int**)&md.pb_atoms, at));
+        if (!md.pb_boxc) TRY(c->alloc(&md.pb_boxc, (size_t)3 * c->nwin));
+    }
+    ++c->epoch;
+    return QNB_OK;
+}
+
+int qnb_put_back_in_box(qnb_context* c, double* boxcentre) {
+    TRY(md_check(c));
+    if (!c->m.box) return fail(QNB_ERR_STATE, "no periodic box (qnb_set_box)");
+    if (c->md.pb_last_mol <= c->md.pb_first_mol) return QNB_OK;
+    CU(cudaSetDevice(c->device));
+    launch_md_put_back(c->all(), c->md);
+    c->launches++;
+    TRY(check_launch());
+    if (boxcentre)
+        CU(cudaMemcpyAsync(boxcentre, c->md.pb_boxc, sizeof(double) * 3 * c->nwin, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return QNB_OK;
+}
+
 int qnb_md_set_velocities(qnb_context* c, int32_t w, const double* v) {
     TRY(md_check(c));
     if (!v || w < 0 || w >= c->nwin) return fail(QNB_ERR_ARG, "bad window or null velocities");
@@ -2252,6 +2294,8 @@ int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* re
             const int istep = istep0 + k0 + k;
             if (istep % p.nbcycle == 0 || !c->lists_built) {
                 if (k0 + k > 0) TRY(md_fail_check(c));   // no list build on coordinates of a failed SHAKE
+                // every NBcycle steps, before the lists (src/md.f90:1663-1671)
+                if (c->m.box && c->md.pb_last_mol > c->md.pb_first_mol) launch_md_put_back(c->all(), c->md), c->launches++;
                 Cut cut{p.rcq * p.rcq, p.rclrf * p.rclrf, p.rcpp * p.rcpp, p.rcpw * p.rcpw, p.rcww * p.rcww};
                 TRY(build_lists(c, cut, W));
             }

@@ -335,6 +335,14 @@ struct MdDev {
     double lan_friction, lan_gkT;  // Langevin: friction, 24 friction Boltz Temp0 / step (uniform draws)
     unsigned long long lan_seed;
     int istep;                     // the step newvel integrates (Langevin random-force counter)
+    // put_back_in_box (qnb_set_put_back_in_box): molecules as atom lists
+    int pb_nmol, pb_first_mol, pb_last_mol;   // molecules [pb_first_mol, pb_last_mol) are wrapped
+    const int* pb_mol_first;       // [nmol+1]
+    const int* pb_atoms;
+    int pb_rigid;                  // rigid_box_centre: the centre stays at pb_centre
+    int pb_nslu;                   // atoms averaged for a floating centre (nat_solute, or natom)
+    double pb_centre[3];
+    double* pb_boxc;               // [nwin][3] the centre of the last call (boxcentre)
     int tg_first[kMaxTg], tg_last[kMaxTg];
     double tg_ndegf[kMaxTg], tg_ndegfree[kMaxTg], ndegf, ndegfree;
     double dt, tau, temp0, boltz;
@@ -356,6 +364,8 @@ constexpr int kMdRec = 2 * kNumE + 4;
 void launch_md_newvel(const Launch& L, const MdDev& md);
 // nh_prop (chain update, one thread per window) and v *= s of every atom
 void launch_md_nh(const Launch& L, const MdDev& md);
+// put_back_in_box, src/simprep.f90:4177-4352 (needs DevModel box lengths)
+void launch_md_put_back(const Launch& L, const MdDev& md);
 // mode 0: constrain x against xx (the step); 1: constrain xx against x
 void launch_md_shake(const Launch& L, const MdDev& md, int mode);
 void launch_md_velocity(const Launch& L, const MdDev& md);

@@ -44,6 +44,7 @@ EXPORTED = (
     "qnb_get_restraint_energies", "qnb_set_offdiag", "qnb_get_offdiag", "qnb_set_restraints",
     "qnb_set_monitor_groups", "qnb_get_monitor_energies", "qnb_set_group_exclusions", "qnb_get_group_exclusions",
     "qnb_set_box", "qnb_set_freeze", "qnb_md_set_thermostat", "qnb_md_set_langevin",
+    "qnb_set_put_back_in_box", "qnb_put_back_in_box",
 )
 TUNE_NAMES = ("rows_solute_blocks_per_sm", "rows_water_blocks_per_sm", "qp_blocks_per_sm", "qw_blocks_per_sm",
               "q_chunk_units", "lrf_taylor_blocks_per_sm", "lrf_build_blocks_per_sm", "row_build_blocks_per_sm")
@@ -106,6 +107,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_set_group_exclusions": [P, I32, P], "qnb_get_group_exclusions": [P, P],
         "qnb_set_box": [P, P, I32], "qnb_set_freeze": [P, I32], "qnb_md_set_thermostat": [P, I32, I32, I32, D],
         "qnb_md_set_langevin": [P, I32, D, ctypes.c_uint64],
+        "qnb_set_put_back_in_box": [P, I32, P, P, I32, I32, I32, P], "qnb_put_back_in_box": [P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -403,6 +405,35 @@ class NonbondedEngine:
         L = np.ascontiguousarray(np.broadcast_to(np.asarray(boxlength, np.float64), (3,)))
         qs = int(self.s.iqseq[0]) if qswitch is None and self.s.nqat else int(qswitch or 0)
         self._check(self.lib.qnb_set_box(self.h, _p(L), qs))
+
+    def set_put_back_in_box(self, molecules=None, put_solute=True, put_solvent=True, boxcentre=None):
+        """put_back_in_box for the MD runs of a periodic box (after md_init):
+        molecules = lists of atoms, solute molecules first (default: the
+        solute's bonded molecules, then each solvent molecule); boxcentre None
+        for a floating centre (the mean of the solute atoms)."""
+        from .md import solute_molecules
+        s = self.s
+        if molecules is None:
+            molecules = solute_molecules(s) + [list(range(s.nat_solute + s.solv_atom * w,
+                                                          s.nat_solute + s.solv_atom * (w + 1)))
+                                               for w in range(s.nwat)]
+            nslu = len(molecules) - s.nwat
+        else:
+            nslu = sum(1 for m in molecules if min(m) < s.nat_solute)
+        first = np.zeros(len(molecules) + 1, np.int32)
+        for q, mol in enumerate(molecules):
+            first[q + 1] = first[q] + len(mol)
+        atoms = np.ascontiguousarray(np.concatenate([np.asarray(m, np.int32) for m in molecules]), dtype=np.int32)
+        bc = None if boxcentre is None else np.ascontiguousarray(boxcentre, dtype=np.float64)
+        self._check(self.lib.qnb_set_put_back_in_box(self.h, len(molecules), _p(first), _p(atoms), nslu,
+                                                     int(put_solute), int(put_solvent),
+                                                     None if bc is None else _p(bc)))
+
+    def put_back_in_box(self):
+        """Wraps the molecules now; returns the box centres [nwin][3]."""
+        c = np.zeros((self.nwin, 3))
+        self._check(self.lib.qnb_put_back_in_box(self.h, _p(c)))
+        return c
 
     # ---- monitor groups and group contributions ----------------------------
     def set_monitor_groups(self, groups, pairs):

@@ -120,3 +120,34 @@ def test_box_rejects_unsupported(sysb):
         e.set_box(None)   # back to the sphere
         e.make_pair_lists_dev(**CUT)
         e.compute_dev(sync=True)
+
+
+def test_put_back_in_box(sysb):
+    from oracle.box import put_back_in_box
+    from q6_gb300.md import solute_molecules
+    s = sysb
+    L = np.asarray(BOX)
+    mols = solute_molecules(s) + [list(range(s.nat_solute + 3 * w, s.nat_solute + 3 * w + 3))
+                                  for w in range(s.nwat)]
+    rng = np.random.default_rng(4)
+    x = s.x.copy()
+    # every third water one box away on each axis (a call moves a molecule by
+    # at most one box length per axis, as the reference does)
+    for mol in mols[len(mols) - s.nwat:][::3]:
+        x[mol] += L * rng.integers(-1, 2, 3)
+    mass = np.asarray(s.mass)[np.asarray(s.iac)]
+    with NonbondedEngine(s, precision=PREC_FP64, use_lrf=False, windows=1) as e:
+        e.set_box(BOX)
+        e.set_coordinates_dev(x[None])
+        e.md_init(MdSetup(cut=CUT))
+        e.set_put_back_in_box()
+        c = e.put_back_in_box()
+        xd, _ = e.md_state(0)
+    xr, cr = put_back_in_box(x, L, mols, mass, len(mols) - s.nwat, s.nat_solute)
+    np.testing.assert_allclose(c[0], cr, rtol=1e-14, atol=1e-12)
+    np.testing.assert_array_equal(xd, xr)
+    assert np.abs(xd - x).max() > 0
+    # every wrapped molecule's mass centre lies within half a box of the centre
+    for mol in mols:
+        cm = (xd[mol] * mass[mol][:, None]).sum(0) / mass[mol].sum()
+        assert np.all(np.abs(cm - cr) <= L / 2 + 1e-9)
