@@ -476,8 +476,9 @@ int qnb_get_group_exclusions(qnb_context* ctx, double* out);
    (4763-6077), every pair at x_j + boxlength*nint((x_a - x_b)/boxlength) of
    its units' reference atoms.  The static Q-Q lists keep plain distances, as
    nonbond_qq does.  Cut-offs must not exceed half the shortest edge.
-   boxlength = NULL returns to the sphere.  Not supported with a box
-   (QNB_ERR_UNSUPPORTED): LRF, any-atom group cut-offs, excluded atoms,
+   With iuse_switch_atom = 0 the pp / pw lists are nbpplis2_box /
+   nbpwlis2_box's (any atom pair inside).  boxlength = NULL returns to the
+   sphere.  Not supported with a box (QNB_ERR_UNSUPPORTED): LRF, excluded atoms,
    solvent restraints and solvent internal pairs.  Constant pressure is the
    caller's; put_back_in_box: qnb_set_put_back_in_box. */
 int qnb_set_box(qnb_context* ctx, const double* boxlength, int32_t qswitch);

@@ -18,7 +18,10 @@ reference atoms (switch atoms, first solvent atoms, qswitch).  nonbond_qp_box
 as written takes the group shift with the opposite sign (x_a - x_qswitch
 against x_i - x_j) and reads a group index nbqplist_box never sets; the
 restatement uses the minimum image of the group's first atom inside Rcq, the
-shift nonbond_qw_spc_box uses for waters.
+shift nonbond_qw_spc_box uses for waters.  With any-atom group tests
+(nbpplis2_box, nbpwlis2_box) the reference shifts a group pair by its first
+atom pair inside the cut-off; the restatement keeps the switch atoms (the
+same shift unless a group spans half a box).
 """
 from __future__ import annotations
 
@@ -57,10 +60,16 @@ def box_lists(s, x, L, qswitch, cut):
     first = ns + sa * np.arange(W)
     pp = []
     G = len(groups)
+    any_atom = int(s.iuse_switch_atom) == 0   # nbpplis2_box / nbpwlis2_box: any atom pair
     for g1 in range(G):
         for g2 in range(g1, G):
-            if g1 != g2 and d2_min_image(L, x[sw[g1]], x[sw[g2]]) > cut["Rcpp"] ** 2:
-                continue
+            if g1 != g2:
+                if any_atom:
+                    d2 = d2_min_image(L, x[groups[g1]][:, None, :], x[groups[g2]][None, :, :])
+                    if (d2 > cut["Rcpp"] ** 2).all():
+                        continue
+                elif d2_min_image(L, x[sw[g1]], x[sw[g2]]) > cut["Rcpp"] ** 2:
+                    continue
             for i in groups[g1]:
                 if not nonq[i]:
                     continue
@@ -73,7 +82,11 @@ def box_lists(s, x, L, qswitch, cut):
     pw = []
     if W:
         for g in range(G):
-            inside = np.nonzero(d2_min_image(L, x[sw[g]][None, :], x[first]) <= cut["Rcpw"] ** 2)[0]
+            if any_atom:
+                d2 = d2_min_image(L, x[groups[g]][:, None, :], x[first][None, :, :])
+                inside = np.nonzero((d2 <= cut["Rcpw"] ** 2).any(0))[0]
+            else:
+                inside = np.nonzero(d2_min_image(L, x[sw[g]][None, :], x[first]) <= cut["Rcpw"] ** 2)[0]
             for i in groups[g]:
                 if nonq[i]:
                     pw.extend((int(i), int(w)) for w in inside)

@@ -2980,7 +2980,6 @@ int qnb_set_box(qnb_context* c, const double* boxlength, int32_t qswitch) {
         if (c->nqat > 0 && (qswitch < 0 || qswitch >= c->natom))
             return fail(QNB_ERR_ARG, "switching atom %d out of range", qswitch);
         if (c->use_lrf) return fail(QNB_ERR_UNSUPPORTED, "LRF with a periodic box is not supported");
-        if (c->m.any_atom) return fail(QNB_ERR_UNSUPPORTED, "a periodic box needs switch-atom cut-offs");
         if (c->have_solv || c->nsi > 0)
             return fail(QNB_ERR_UNSUPPORTED, "solvent restraints and solvent internal pairs are for the sphere");
         std::vector<uint8_t> excl(c->natom);

@@ -3535,13 +3535,26 @@ __global__ void k_build_box_groups(DevModel m, const DevState* __restrict__ stat
             int g2 = (int)(t - (int64_t)g1 * (g1 + 1) / 2);
             a = g2;
             b = g1;
-            bool ok = (a == b) || box_d2(m, x, m.gsw[a], m.gsw[b]) <= rcpp2;
+            bool ok = (a == b);
+            if (!ok && m.any_atom) {   // nbpplis2_box, src/nonbondene.f90:1091-1218: any atom pair
+                for (int p = m.gslot[a]; p < m.gslot[a + 1] && !ok; ++p)
+                    for (int q = m.gslot[b]; q < m.gslot[b + 1] && !ok; ++q)
+                        ok = box_d2(m, x, m.gatom[p], m.gatom[q]) <= rcpp2;
+            } else if (!ok) {
+                ok = box_d2(m, x, m.gsw[a], m.gsw[b]) <= rcpp2;
+            }
             kind = ok ? 0 : -1;
         } else if (t < npp + npw) {
             int64_t u = t - npp;
             a = (int)(u / W);
             b = (int)(u % W);
-            bool ok = box_d2(m, x, m.gsw[a], m.nat_solute + m.sa * b) <= rcpw2;
+            const int o = m.nat_solute + m.sa * b;
+            bool ok = false;
+            if (m.any_atom) {   // nbpwlis2_box, src/nonbondene.f90:2247-2357: any atom of the group
+                for (int p = m.gslot[a]; p < m.gslot[a + 1] && !ok; ++p) ok = box_d2(m, x, m.gatom[p], o) <= rcpw2;
+            } else {
+                ok = box_d2(m, x, m.gsw[a], o) <= rcpw2;
+            }
             kind = ok ? 1 : -1;
         } else if (t < total) {
             int64_t u = t - npp - npw;   // (i, j), i < j over the strict upper triangle

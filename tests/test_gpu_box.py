@@ -151,3 +151,22 @@ def test_put_back_in_box(sysb):
     for mol in mols:
         cm = (xd[mol] * mass[mol][:, None]).sum(0) / mass[mol].sum()
         assert np.all(np.abs(cm - cr) <= L / 2 + 1e-9)
+
+
+def test_any_atom_box_lists_match_oracle(sysb):
+    import dataclasses
+    s = dataclasses.replace(sysb, iuse_switch_atom=0)
+    rng = np.random.default_rng(12)
+    x = s.x + rng.normal(0, 0.03, s.x.shape)
+    lam = lambdas_for_window(0.5, 2)
+    d, E, EQ = device(s, PREC_FP64, [x], [lam])
+    dr, Er, EQr = reference(s, x, lam)
+    for k in Er:
+        assert E[0][k] == pytest.approx(Er[k], rel=1e-10, abs=1e-9), k
+    np.testing.assert_allclose(EQ[0], EQr, rtol=1e-10, atol=1e-9)
+    assert np.abs(d[0] - dr).max() < 1e-9 * np.abs(dr).max()
+    # more solute-water pairs than with switch atoms
+    from oracle.box import box_lists
+    n_any = len(box_lists(s, x, BOX, int(s.iqseq[0]), OCUT)["pw"])
+    n_sw = len(box_lists(sysb, x, BOX, int(s.iqseq[0]), OCUT)["pw"])
+    assert n_any > n_sw
