@@ -161,6 +161,9 @@ class NonbondedEngine:
     # ---- reference routines ---------------------------------------------
     def set_lambda(self, lam, window=None):
         lam = np.ascontiguousarray(lam, dtype=np.float64)
+        if not hasattr(self, "lambdas"):
+            self.lambdas = np.zeros((self.nwin, self.S))
+        self.lambdas[slice(None) if window is None else int(window)] = lam[: self.S]
         if window is None:
             self._check(self.lib.qnb_set_lambda(self.h, _p(lam)))
         else:
@@ -401,10 +404,12 @@ class NonbondedEngine:
         the first Q atom)."""
         if boxlength is None:
             self._check(self.lib.qnb_set_box(self.h, None, 0))
+            self.boxlength = None
             return
         L = np.ascontiguousarray(np.broadcast_to(np.asarray(boxlength, np.float64), (3,)))
         qs = int(self.s.iqseq[0]) if qswitch is None and self.s.nqat else int(qswitch or 0)
         self._check(self.lib.qnb_set_box(self.h, _p(L), qs))
+        self.boxlength, self.qswitch = L.copy(), qs
 
     def set_put_back_in_box(self, molecules=None, put_solute=True, put_solvent=True, boxcentre=None):
         """put_back_in_box for the MD runs of a periodic box (after md_init):
@@ -545,6 +550,7 @@ class NonbondedEngine:
         """qnb_set_bonded from a q6_gb300.bonded.BondedTerms."""
         st, keep = bt.to_struct(self.S)
         self._check(self.lib.qnb_set_bonded(self.h, ctypes.byref(st)))
+        self.bonded_terms = bt
 
     def bonded_energies(self):
         """(Eb [nwin][8], EQb [nwin][nstates][4]) of the last evaluation."""

@@ -170,3 +170,42 @@ def test_any_atom_box_lists_match_oracle(sysb):
     n_any = len(box_lists(s, x, BOX, int(s.iqseq[0]), OCUT)["pw"])
     n_sw = len(box_lists(sysb, x, BOX, int(s.iqseq[0]), OCUT)["pw"])
     assert n_any > n_sw
+
+
+def test_npt_volume_moves(sysb):
+    # qdyn's MC_volume around the device MD (q6_gb300.pressure.run_npt): the
+    # engine's potential energy equals the oracle's at the same box, and after
+    # the run the lists and energies follow the final box
+    from q6_gb300.pressure import PressureSetup, potential_energy, run_npt
+    s = sysb
+    lam = lambdas_for_window(0.5, 2)
+    with NonbondedEngine(s, precision=PREC_FP64, use_lrf=False, windows=1) as e:
+        e.set_box(BOX)
+        e.set_lambda(lam)
+        e.set_coordinates_dev(s.x[None])
+        e.make_pair_lists_dev(**CUT)
+        e.compute_dev(sync=True)
+        dr, Er, EQr = reference(s, s.x, lam)
+        u_ref = sum(Er.values()) + float(np.dot(lam, EQr.sum(1)))
+        assert potential_energy(e) == pytest.approx(u_ref, rel=1e-10)
+        e.md_init(MdSetup(stepsize=0.5, tau_t=100.0, nbcycle=5, cut=CUT))
+        e.md_set_velocities(maxwell_velocities(s, 300.0, 3)[None])
+        e.md_prepare(stop_cm=True)
+        setup = PressureSetup(max_volume_displ=150.0, pressure_bar=1.0, volume_change=10, seed=11)
+        rec, moves, L = run_npt(e, setup, 40, OCUT, 300.0)
+        assert len(rec) == 40 and len(moves) == 3 and np.isfinite(rec["E"]).all()
+        x, _ = e.md_state(0)
+        e.make_pair_lists_dev(**CUT)
+        e.compute_dev(sync=True)
+        u_dev = potential_energy(e)
+    assert np.allclose(L, e.boxlength)
+    for m in moves:
+        assert abs(m["dV"]) <= 150.0
+    qs = int(s.iqseq[0])
+    _, E1, EQ1 = box_energies(s, x, lam, L, qs, OCUT)
+    o = Oracle(s, use_lrf=False)
+    o.set_lambda(lam)
+    _, EQs = o.nonbond_qq(x)
+    o.close()
+    u1 = sum(E1.values()) + float(np.dot(lam, (EQ1 + EQs).sum(1)))
+    assert u_dev == pytest.approx(u1, rel=1e-9)
