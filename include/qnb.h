@@ -643,9 +643,11 @@ int qnb_md_run(qnb_context* ctx, int32_t nsteps, int32_t istep0, qnb_md_record* 
 /* ---- allocation-free entry point (no counterpart in the reference) ------- */
 
 /* Water-water SPC energies and gradient without any device allocation, for
-   callers that may not call cudaMalloc: a host that gives this library a
-   fixed memory budget, work recorded into a CUDA graph, or a process whose
-   own allocator owns the device.  It is the FP64 nbwwlist + nonbond_ww_spc
+   callers that may not call cudaMalloc: a program held to a fixed device-memory
+   budget by its scheduler or host application, a process whose own pool
+   allocator already holds the device's free memory, or a timed step loop in
+   which cudaMalloc/cudaFree would synchronise the device.  It is the FP64
+   nbwwlist + nonbond_ww_spc
    computation: water pairs whose O atoms lie within rc2 (neither O excluded)
    each contribute LJ + Coulomb for O-O and Coulomb for the other eight atom
    pairs.
@@ -665,8 +667,11 @@ int qnb_md_run(qnb_context* ctx, int32_t nsteps, int32_t istep0, qnb_md_record* 
    and calls that overlap on the GPU (different streams or threads) race.
    The first call on a device looks up the array's device address
    (cudaGetSymbolAddress) with that device current; make that first call
-   before any stream capture.  The call waits on `stream` once, after the
-   pair selection, to check the pair count. */
+   before any stream capture.  The address is kept for the life of the
+   process, so the entry point is not for use after a cudaDeviceReset.  The
+   call waits on `stream` once, after the pair selection, to check the pair
+   count.  The gradient and energies are added with FP64 atomics: repeated
+   calls agree to rounding, not bit for bit. */
 int qnb_ww_spc_noalloc(const double* x_dev, const uint8_t* excl_dev, int32_t first_water_atom, int32_t nwat,
                        double q_oxygen, double q_hydrogen, double A_oo, double B_oo, double rc2,
                        double* d_dev, double* e_dev, void* stream);

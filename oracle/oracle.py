@@ -16,28 +16,40 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
+LIB_TIMING = os.path.join(BUILD, "liboracle_timing.so")
 SRC = os.path.join(HERE, "qnb_oracle.c")
 
-# strict IEEE double: no FMA contraction, no fast-math
+# the checker: strict IEEE double, no FMA contraction, no fast-math
 CFLAGS = ["-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
           "-fno-associative-math", "-Wall", "-Wno-unused-function"]
+# the timed CPU baseline: the optimisation flags of the reference's own gcc
+# build (Q6 src/makefile, COMP=gcc: -Ofast -unroll -finline-limit=10000000);
+# no -march=native, so the same flags build on x86 and Arm hosts
+CFLAGS_TIMING = ["-Ofast", "-funroll-loops", "-finline-limit=10000000", "-std=c11", "-fPIC", "-shared",
+                 "-Wall", "-Wno-unused-function"]
+
+
+def _build_one(path, flags, force):
+    if force or not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(SRC):
+        subprocess.check_call(["gcc", *flags, "-o", path, SRC, "-lm"])
+    return path
 
 
 def build(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        subprocess.check_call(["gcc", *CFLAGS, "-o", LIB, SRC, "-lm"])
-    return LIB
+    _build_one(LIB_TIMING, CFLAGS_TIMING, force)
+    return _build_one(LIB, CFLAGS, force)
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(timing: bool = False):
+    """The checker library, or with timing=True the -Ofast build that the
+    CPU baseline times (never used as a checker)."""
+    if timing not in _libs:
         build()
-        L = ctypes.CDLL(LIB)
+        L = ctypes.CDLL(LIB_TIMING if timing else LIB)
         P = ctypes.c_void_p
         D = ctypes.c_double
         I = ctypes.c_int
@@ -71,8 +83,8 @@ def lib():
         L.orc_p_restrain.argtypes = [P, P, P, P, P, P, P, I, P, P, P]
         L.orc_static_qq_size.restype = ctypes.c_long
         L.orc_static_qq_size.argtypes = [P, I, I]
-        _lib = L
-    return _lib
+        _libs[timing] = L
+    return _libs[timing]
 
 
 def _p(a):
@@ -85,16 +97,17 @@ class Oracle:
     E_FIELDS = ("pp_el", "pp_vdw", "pw_el", "pw_vdw", "ww_el", "ww_vdw", "lrf")
     Q_FIELDS = ("qq_el", "qq_vdw", "qp_el", "qp_vdw", "qw_el", "qw_vdw")
 
-    def __init__(self, system, use_lrf: bool = True):
+    def __init__(self, system, use_lrf: bool = True, timing_build: bool = False):
         from q6_gb300.system import TopologyHandle
         self.s = system
         self.topo = TopologyHandle(system)
-        self.h = lib().orc_create(self.topo.ptr(), int(use_lrf))
+        self.L = lib(timing_build)
+        self.h = self.L.orc_create(self.topo.ptr(), int(use_lrf))
         self.S = system.nstates
 
     def close(self):
         if self.h:
-            lib().orc_destroy(self.h)
+            self.L.orc_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -105,11 +118,11 @@ class Oracle:
 
     def set_lambda(self, lam):
         lam = np.ascontiguousarray(lam, dtype=np.float64)
-        lib().orc_set_lambda(self.h, _p(lam))
+        self.L.orc_set_lambda(self.h, _p(lam))
 
     def make_pair_lists(self, x, Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0):
         x = np.ascontiguousarray(x, dtype=np.float64)
-        lib().orc_make_pair_lists(self.h, _p(x), Rcq, Rcq ** 2, RcLRF ** 2, Rcpp ** 2,
+        self.L.orc_make_pair_lists(self.h, _p(x), Rcq, Rcq ** 2, RcLRF ** 2, Rcpp ** 2,
                                   Rcpw ** 2, Rcww ** 2)
 
     def pot_energy_nonbonds(self, x, d=None, md=True):
@@ -118,7 +131,7 @@ class Oracle:
             d = np.zeros_like(x)
         E = np.zeros(7)
         EQ = np.zeros((self.S, 6))
-        lib().orc_pot_energy_nonbonds(self.h, _p(x), _p(d), _p(E), _p(EQ), int(md))
+        self.L.orc_pot_energy_nonbonds(self.h, _p(x), _p(d), _p(E), _p(EQ), int(md))
         return d, dict(zip(self.E_FIELDS, E)), EQ
 
     def nonbond_qq(self, x, d=None, EQ=None):
@@ -127,47 +140,47 @@ class Oracle:
             d = np.zeros_like(x)
         if EQ is None:
             EQ = np.zeros((self.S, 6))
-        lib().orc_nonbond_qq(self.h, _p(x), _p(d), _p(EQ))
+        self.L.orc_nonbond_qq(self.h, _p(x), _p(d), _p(EQ))
         return d, EQ
 
     def set_solvent_params(self, p):
-        lib().orc_set_solvent_params(self.h, ctypes.byref(p))
+        self.L.orc_set_solvent_params(self.h, ctypes.byref(p))
 
     def set_solvent_internal(self, pairs, A, B, el):
         """nonbnd_solv_int: (i, j) offsets inside a solvent molecule with their
         A, B, elec (applied to every molecule when md)."""
         ij = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
         a, b, e = (np.ascontiguousarray(np.asarray(v, dtype=np.float64)) for v in (A, B, el))
-        lib().orc_set_solvent_internal(self.h, len(a), _p(ij), _p(a), _p(b), _p(e))
+        self.L.orc_set_solvent_internal(self.h, len(a), _p(ij), _p(a), _p(b), _p(e))
 
     def restrain_solvent(self, x, d, Tfree):
         e = np.zeros(1)
-        lib().orc_restrain_solvent(self.h, _p(np.ascontiguousarray(x)), _p(d), Tfree, _p(e))
+        self.L.orc_restrain_solvent(self.h, _p(np.ascontiguousarray(x)), _p(d), Tfree, _p(e))
         return float(e[0])
 
     def watpol(self, x, d, istep, md=True):
         e = np.zeros(1)
-        lib().orc_watpol(self.h, _p(np.ascontiguousarray(x)), _p(d), int(istep), int(md), _p(e))
+        self.L.orc_watpol(self.h, _p(np.ascontiguousarray(x)), _p(d), int(istep), int(md), _p(e))
         return float(e[0])
 
     def watpol_state(self):
         a, b, c = np.zeros(16), np.zeros(16), np.zeros(16)
-        lib().orc_get_watpol_state(self.h, _p(a), _p(b), _p(c))
+        self.L.orc_get_watpol_state(self.h, _p(a), _p(b), _p(c))
         return a, b, c
 
     def list_size(self, kind):
-        return int(lib().orc_list_size(self.h, kind))
+        return int(self.L.orc_list_size(self.h, kind))
 
     def export_pairs(self, kind):
         n = self.list_size(kind)
         i = np.zeros(max(n, 1), np.int32)
         j = np.zeros(max(n, 1), np.int32)
-        m = lib().orc_export_pairs(self.h, kind, _p(i), _p(j))
+        m = self.L.orc_export_pairs(self.h, kind, _p(i), _p(j))
         return i[:m], j[:m]
 
     def lrf(self):
         out = np.zeros((self.s.ncgp, 43))
-        lib().orc_get_lrf(self.h, _p(out))
+        self.L.orc_get_lrf(self.h, _p(out))
         return out
 
     def bonded(self, x, bt, lam, d=None):
@@ -180,7 +193,7 @@ class Oracle:
         Eb = np.zeros(8)
         EQb = np.zeros((max(self.S, 1), 4))
         lam = np.ascontiguousarray(lam, dtype=np.float64)
-        lib().orc_bonded(_p(x), _p(d), ctypes.byref(st), self.S, _p(lam), _p(Eb), _p(EQb))
+        self.L.orc_bonded(_p(x), _p(d), ctypes.byref(st), self.S, _p(lam), _p(Eb), _p(EQb))
         return d, Eb, EQb[: self.S]
 
     def fix_shell(self, x, xtop, shell, fk_fix, fk_pshell, d=None):
@@ -192,7 +205,7 @@ class Oracle:
         excl = np.ascontiguousarray(self.s.excl, dtype=np.uint8)
         sh = np.ascontiguousarray(shell, dtype=np.uint8)
         xt = np.ascontiguousarray(xtop, dtype=np.float64)
-        lib().orc_fix_shell(self.s.natom, _p(x), _p(d), _p(xt), _p(excl), _p(sh), float(fk_fix), float(fk_pshell),
+        self.L.orc_fix_shell(self.s.natom, _p(x), _p(d), _p(xt), _p(excl), _p(sh), float(fk_fix), float(fk_pshell),
                             _p(E))
         return d, E
 
@@ -210,7 +223,7 @@ class Oracle:
         lam = np.ascontiguousarray(lam, dtype=np.float64)
         Ep = np.zeros(1)
         EQr = np.zeros(max(self.S, 1))
-        lib().orc_p_restrain(_p(x), _p(d), ctypes.byref(st), _p(xt), _p(heavy), _p(mass), _p(xw), self.S, _p(lam),
+        self.L.orc_p_restrain(_p(x), _p(d), ctypes.byref(st), _p(xt), _p(heavy), _p(mass), _p(xw), self.S, _p(lam),
                              _p(Ep), _p(EQr))
         return d, float(Ep[0]), EQr[: self.S]
 

@@ -1,14 +1,20 @@
 // Allocation-free variant of the FP64 solvent-solvent path.
 //
-// Some callers cannot allocate device memory during a run. Examples: a host
-// that hands this library a fixed memory budget and forbids cudaMalloc, an
-// application that records work into a CUDA graph, and a process whose other
-// allocator owns the device. qnb_ww_spc_noalloc serves them. It selects SPC
-// water pairs within the cut-off and evaluates their energies and gradient
-// (nbwwlist + nonbond_ww_spc, Q6 src/nonbondene.f90:4274-4395, 5886-5975)
-// without allocating. Its scratch, the water-pair list and its counter, is the
+// Some callers cannot allocate device memory while they run: a host program
+// that a job scheduler or an embedding application gives a fixed device-memory
+// budget, a process whose own pool allocator already holds the device's free
+// memory (a cudaMalloc there fails or fragments that pool), and a timed step
+// loop in which cudaMalloc/cudaFree would synchronise the whole device.
+// qnb_ww_spc_noalloc serves them. It selects SPC water pairs within the
+// cut-off and evaluates their energies and gradient (nbwwlist +
+// nonbond_ww_spc, Q6 src/nonbondene.f90:4274-4395, 5886-5975) without
+// allocating. Its scratch, the water-pair list and its counter, is the
 // file-scope array below. The array is part of the module image, so every GPU
 // that loads the library holds it until the process exits.
+//
+// Sums: the gradient and the two energies are added with FP64 atomics, so
+// their last bits depend on the order in which blocks finish (as in the FP64
+// form of the engine); repeated calls agree to rounding, not bit for bit.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -28,7 +34,9 @@ constexpr int kMaxDevices = 64;
 constexpr int kScratchHead = 32;
 static __device__ __align__(256) int2 g_noalloc_scratch[kScratchHead + kNoAllocMaxPairs];
 
-// device address of g_noalloc_scratch, looked up once per device
+// device address of g_noalloc_scratch, looked up once per device and kept for
+// the life of the process (a cudaDeviceReset invalidates it: this entry point
+// is not for use after a device reset)
 int2* g_scratch_ptr[kMaxDevices] = {nullptr};
 std::mutex g_scratch_mutex;
 

@@ -1,7 +1,7 @@
 """Build tests/golden/lig_w.npz from Q6's own regression-test inputs.
 
-Reads tests/basic_tests/prep_SPH/lig_w.top and lig_w.fep of the Q6 tree (path
-given on the command line, default /root/reference) with a reader written for
+Reads tests/basic_tests/prep_SPH/lig_w.top and lig_w.fep of the Q6 tree (its
+root directory is the required command-line argument) with a reader written for
 the Q topology text format as Q6 src/topo.f90:471-1115 parses it, and stores
 the arrays the nonbonded path needs.  The fixture is what the golden test uses;
 the Q6 tree is not needed at test time.
@@ -14,7 +14,7 @@ solute, solvent and solute-solvent rows, EL -7.30, VdW -413.17, and the
 bonded columns of that row: solute bond 31.61, angle 30.69, torsion 6.28,
 improper 0.05; Q-atom bond -122.04, angle 0.68, torsion 2.17, improper 0.00.
 
-Usage: python tests/golden/make_lig_w_fixture.py [Q6_ROOT]
+Usage: python tests/golden/make_lig_w_fixture.py Q6_ROOT
 """
 from __future__ import annotations
 
@@ -273,7 +273,9 @@ def read_fep_bonded(path, nstates):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_lig_w_fixture.py Q6_ROOT")
+    root = sys.argv[1]
     d = os.path.join(root, "tests", "basic_tests", "prep_SPH")
     top = read_top(os.path.join(d, "lig_w.top"))
     nstates, iqseq = read_fep_atoms(os.path.join(d, "lig_w.fep"))

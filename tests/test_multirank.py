@@ -48,3 +48,24 @@ def test_single_rank_needs_no_process_group():
     import bench
     assert bench.max_over_ranks(12.5, 1) == 12.5
     assert bench.job_throughput(500.0, 1, 51, 100) == 51 * 100 / 0.5
+
+
+def test_rebuild_cycle_amortisation_does_not_depend_on_the_step_count():
+    """The bench's step is the step of qdyn's cycle, one list rebuild every
+    25 steps, whatever --steps is: 20 timed steps (one rebuild) and 100 timed
+    steps (four rebuilds) of the same per-step costs give the same figure."""
+    import bench
+    assert bench.first_rebuild_step(5) == 25 and bench.first_rebuild_step(25) == 25
+    assert bench.first_rebuild_step(0) == 0 and bench.first_rebuild_step(26) == 50
+
+    def run(steps, istep0):
+        rb, pl = [], []
+        for k in range(istep0, istep0 + steps):
+            (rb if k % bench.NBCYCLE == 0 else pl).append(3.0 if k % bench.NBCYCLE == 0 else 0.5)
+        return rb, pl
+    a = bench.amortised_step_ms(*run(20, 25))
+    b = bench.amortised_step_ms(*run(100, 25))
+    assert a == b == (3.0 + 24 * 0.5) / 25
+    assert bench.amortised_step_ms([2.0], []) == 2.0
+    with pytest.raises(ValueError):
+        bench.amortised_step_ms([], [1.0])
