@@ -181,8 +181,12 @@ def remove_redefined(bt: BondedTerms) -> BondedTerms:
 def remove_shaken(bt: BondedTerms, heavy, nat_solute: int, shake_solvent=True, shake_solute=False,
                   shake_hydrogens=True, shake_heavy=False) -> BondedTerms:
     """Bonds SHAKE constrains get code -1 (src/simprep.f90:2300-2345); bonds
-    already removed (code -1) are not constrained."""
+    already removed (code -1) are not constrained.  Then, as init_constraints
+    does (src/simprep.f90:2461-2473), each constraint clears the first angle in
+    list order whose end atoms (i, k) are the constrained pair: the H-O-H angle
+    of a rigid water whose H-H distance is constrained contributes nothing."""
     bonds = bt.bonds.copy()
+    constrained = []
     for k, (i, j, c) in enumerate(bonds.tolist()):
         if c < 0:
             continue
@@ -190,8 +194,19 @@ def remove_shaken(bt: BondedTerms, heavy, nat_solute: int, shake_solvent=True, s
         pick = (shake_hydrogens if hyd else shake_heavy)
         if (shake_solute and i < nat_solute and pick) or (shake_solvent and i >= nat_solute and pick):
             bonds[k, 2] = -1
+            constrained.append((i, j))
+    angles = bt.angles.copy()
+    if len(angles) and constrained:
+        first = {}
+        for a, (i, _, k, _) in enumerate(angles.tolist()):
+            first.setdefault((min(i, k), max(i, k)), a)
+        for i, j in constrained:
+            a = first.get((min(i, j), max(i, j)))
+            if a is not None:
+                angles[a, 3] = -1
     out = BondedTerms(**{**bt.__dict__})
     out.bonds = bonds
+    out.angles = angles
     return out
 
 

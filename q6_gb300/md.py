@@ -98,10 +98,19 @@ def solute_molecules(s):
     return [comp[k] for k in sorted(comp)]
 
 
-def build_constraints(s, setup: MdSetup) -> Constraints:
+def build_constraints(s, setup: MdSetup, bonded=None) -> Constraints:
     """Constraint molecules in qdyn's order: solute molecules (bonds in
     topology order, hydrogen / heavy selection as init_constraints), then one
-    molecule per water."""
+    molecule per water.
+
+    With ``bonded`` (the topology's BondedTerms, redefined terms already
+    removed but shaken bonds not), the constrained bonds and their lengths
+    are the topology's own, as init_constraints takes them: every bond of a
+    non-removed code in topology order, of length bondlib(code) b0
+    (src/simprep.f90:2196-2345).  Without it, a generated system's bonds and
+    water geometry give them."""
+    if bonded is not None:
+        return _constraints_from_topology(s, setup, bonded)
     starts, ij, dist = [0], [], []
     if setup.shake_solute and s.nat_solute:
         mass = s.mass[s.iac]
@@ -133,6 +142,38 @@ def build_constraints(s, setup: MdSetup) -> Constraints:
                 dist.append(d)
             if wb:
                 starts.append(len(ij))
+    return Constraints(np.array(starts, np.int32), np.array(ij, np.int32).reshape(-1, 2),
+                       np.array(dist, np.float64), np.zeros(MAX_TGROUPS))
+
+
+def _constraints_from_topology(s, setup: MdSetup, bt) -> Constraints:
+    heavy = np.asarray(s.mass)[np.asarray(s.iac)] >= 4.0
+    mols = solute_molecules(s)
+    owner = {}
+    for m in mols:
+        for a in m:
+            owner[a] = min(m)
+    per_mol = {}
+    for i, j, c in np.asarray(bt.bonds).reshape(-1, 3).tolist():
+        if c < 0:
+            continue
+        hyd = not heavy[i] or not heavy[j]
+        pick = setup.shake_hydrogens if hyd else setup.shake_heavy
+        if i < s.nat_solute:
+            if not (setup.shake_solute and pick):
+                continue
+            key = (0, owner[i])
+        else:
+            if not (setup.shake_solvent and pick):
+                continue
+            key = (1, (i - s.nat_solute) // s.solv_atom)
+        per_mol.setdefault(key, []).append((i, j, float(bt.bondlib[c][1])))
+    starts, ij, dist = [0], [], []
+    for key in sorted(per_mol):
+        for i, j, b0 in per_mol[key]:
+            ij.append((i, j))
+            dist.append(b0)
+        starts.append(len(ij))
     return Constraints(np.array(starts, np.int32), np.array(ij, np.int32).reshape(-1, 2),
                        np.array(dist, np.float64), np.zeros(MAX_TGROUPS))
 

@@ -302,12 +302,14 @@ class NonbondedEngine:
         self._check(self.lib.qnb_set_tuning(self.h, _p(v)))
 
     # ---- device-resident MD step (qnb_md_*) -----------------------------
-    def md_init(self, setup=None):
+    def md_init(self, setup=None, bonded=None):
         """qnb_md_init from an MdSetup (q6_gb300.md): constraints, degrees of
-        freedom and temperature groups as qdyn derives them for this system."""
+        freedom and temperature groups as qdyn derives them for this system;
+        with ``bonded`` (the topology's BondedTerms before the shaken bonds
+        are removed) the constraint lengths are its bond library's."""
         from .md import MdSetup, build_constraints, md_params
         setup = setup or MdSetup()
-        cons = build_constraints(self.s, setup)
+        cons = build_constraints(self.s, setup, bonded)
         self.md_setup, self.md_constraints = setup, cons
         self.md_p = md_params(self.s, setup, cons)
         mass = np.ascontiguousarray(self.s.mass[self.s.iac], dtype=np.float64)

@@ -207,7 +207,9 @@ def default_solvent_params(s: QSystem, wpol: bool = True, fk_wsphere: float = 60
     """Boundary parameters as wat_sphere / wat_shells derive them
     (Q6 src/simprep.f90:4613-4891): Dwmz/awmz "magic" defaults from the
     solvent radius, shells of widths drout, 2 drout, ... from rwat inwards,
-    cstb from the Born term (zero total Q charge unless given)."""
+    cstb from the Born term.  crg_qtot is wat_sphere's crgQtot (born_charge;
+    0 turns the Born correction off) and mu_w its water dipole (water_dipole
+    from a topology; by default -q_O b0 cos(theta0/2) of SPC geometry)."""
     p = QnbSolventParams()
     rwat = s.rwat
     p.fk_wsphere = fk_wsphere
@@ -237,6 +239,33 @@ def default_solvent_params(s: QSystem, wpol: bool = True, fk_wsphere: float = 60
         p.theta_corr[i] = 0.0
         rout = rout - dr
     return p
+
+
+def born_charge(s: QSystem, lam, coulomb: float = 332.0) -> float:
+    """crgQtot of wat_sphere (Q6 src/simprep.f90:4638-4646): the Q atoms'
+    charges summed over states with the lambda weights, in elementary charges.
+    wat_sphere runs before prep_sim scales the charges by sqrt(coulomb)
+    (src/simprep.f90:3628-3631, 3714-3721), so the scaled charges held here
+    are divided back.  qdyn's Born correction (charge_correction, on by
+    default whenever polarisation is) uses it as default_solvent_params'
+    crg_qtot; with the correction off, crg_qtot is 0."""
+    lam = np.asarray(lam, dtype=np.float64)
+    q = np.asarray(s.qcrg, dtype=np.float64).reshape(s.nqat, s.nstates)
+    return float((q * lam[None, :]).sum() / math.sqrt(coulomb))
+
+
+def water_dipole(s: QSystem, bonded, coulomb: float = 332.0) -> float:
+    """mu_w of wat_shells (Q6 src/simprep.f90:4748-4751): minus the first
+    solvent atom's charge (elementary charges) times b0 of the bond code of
+    the topology's last bond times cos(theta0/2) of the angle code of its
+    last angle.  ``bonded`` is the topology's BondedTerms (anglib in radians)
+    before SHAKE removes any bond.  For a water topology whose last bond is
+    the H-H constraint, as Qprep writes SPC and TIP3P, b0 is the H-H distance
+    rather than O-H; this is the value qdyn's Born term uses."""
+    q1 = float(s.crg[s.nat_solute]) / math.sqrt(coulomb)
+    b_code = int(np.asarray(bonded.bonds)[-1][2])
+    a_code = int(np.asarray(bonded.angles)[-1][3])
+    return -q1 * float(bonded.bondlib[b_code][1]) * math.cos(float(bonded.anglib[a_code][1]) / 2.0)
 
 
 # --------------------------------------------------------------------------

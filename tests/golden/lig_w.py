@@ -66,6 +66,8 @@ def load_lig_w() -> tuple[QSystem, dict]:
     golden = {k: float(f[k]) for k in ("golden_qsurr_el", "golden_qsurr_vdw", "golden_el", "golden_vdw",
                                        "golden_bnd", "golden_ang", "golden_tor", "golden_imp",
                                        "golden_qbnd", "golden_qang", "golden_qtor", "golden_qimp")}
+    for k in ("golden_pot_band", "golden_kin_band", "golden_tot_band"):
+        golden[k] = tuple(float(v) for v in f[k])
     golden["wbond_ij"] = f["wbond_ij"]
     golden["wbond_b0"] = f["wbond_b0"]
     golden["wbond_code"] = f["wbond_code"]
@@ -76,8 +78,16 @@ def lig_w_bonded(s):
     """The bonded terms qdyn evaluates for lig_w: the topology lists with
     the FEP-redefined terms and the SHAKE-constrained bonds removed
     (defaults shake_solvent on, shake_solute off, shake_hydrogens on,
-    shake_heavy off), libraries converted as topology() does."""
-    from q6_gb300.bonded import DEG2RAD, BondedTerms, remove_redefined, remove_shaken
+    shake_heavy off) together with the angles those constraints clear,
+    libraries converted as topology() does."""
+    from q6_gb300.bonded import remove_shaken
+    return remove_shaken(lig_w_topology_terms(s), np.asarray(s.heavy).astype(bool), s.nat_solute)
+
+
+def lig_w_topology_terms(s):
+    """The topology's bonded terms with the FEP-redefined ones removed, before
+    SHAKE removes any bond: what init_constraints and wat_shells read."""
+    from q6_gb300.bonded import DEG2RAD, BondedTerms, remove_redefined
     f = np.load(os.path.join(HERE, "lig_w.npz"))
     anglib = f["anglib"].copy()
     anglib[:, 1] *= DEG2RAD
@@ -102,5 +112,24 @@ def lig_w_bonded(s):
         qangles=f["fep_qangles"], qangle_code=f["fep_qangle_code"], qanglib=qanglib,
         qtorsions=f["fep_qtorsions"], qtorsion_code=f["fep_qtorsion_code"], qtorlib=qtorlib,
         qimpropers=f["fep_qimpropers"], qimproper_code=f["fep_qimproper_code"], qimplib=qimplib)
-    bt = remove_redefined(bt)
-    return remove_shaken(bt, np.asarray(s.heavy).astype(bool), s.nat_solute)
+    return remove_redefined(bt)
+
+
+def lig_w_eq1_inputs(s):
+    """What qdyn derives from the regression run's first input (eq1.inp with
+    run_test.sh's sphere settings, tests/basic_tests/run_test.sh:172-179):
+    stepsize 0.1 fs, temperature 0.1 K, bath_coupling 1 fs, separate scaling,
+    non_bond 25, cut-offs 10 / q_atom 99 / lrf 99, LRF on; [solvent] with only
+    pol_update 100, so radial_force 60, polarisation on, polarisation_force 20
+    and charge_correction (the Born term) on by default (src/md.f90:730-790,
+    src/globals.f90:220-229), crgQtot of the ligand and mu_w from the
+    topology's last bond and angle codes (src/simprep.f90:4638-4646, 4748-4751).
+    Returns (MdSetup, QnbSolventParams, topology terms, evaluated bonded terms)."""
+    from q6_gb300.md import MdSetup
+    from q6_gb300.system import born_charge, default_solvent_params, water_dipole
+    top = lig_w_topology_terms(s)
+    cut = dict(Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
+    setup = MdSetup(stepsize=0.1, temp0=0.1, tau_t=1.0, separate_scaling=True, nbcycle=25, cut=cut)
+    sp = default_solvent_params(s, fk_wsphere=60.0, fkwpol=20.0, itdis=100.0,
+                                crg_qtot=born_charge(s, [1.0]), mu_w=water_dipole(s, top))
+    return setup, sp, top, lig_w_bonded(s)

@@ -13,6 +13,10 @@ Q-surr. el 3.12, vdW 139.43 (Q-atom state 1, lambda 1), the sums of the
 solute, solvent and solute-solvent rows, EL -7.30, VdW -413.17, and the
 bonded columns of that row: solute bond 31.61, angle 30.69, torsion 6.28,
 improper 0.05; Q-atom bond -122.04, angle 0.68, torsion 2.17, improper 0.00.
+The same row's last six columns, read from the file, are the reference's
+bands (mean -/+ one standard deviation over the 20 random seeds of its
+benchmark runs, run_test.sh:197-440) of the step-0 total, kinetic and
+potential energy: golden_tot_band, golden_kin_band, golden_pot_band.
 
 Usage: python tests/golden/make_lig_w_fixture.py Q6_ROOT
 """
@@ -272,6 +276,17 @@ def read_fep_bonded(path, nstates):
     return out
 
 
+def read_step0_bands(path):
+    """(TOT, KIN, POT) (lower, upper) bounds of the first data row of a
+    *_benchmark.en file (columns 26-31 after the step number)."""
+    for ln in open(path):
+        if ln.startswith("#") or not ln.strip():
+            continue
+        v = [float(t) for t in ln.split()[1:]]
+        return (v[24], v[25]), (v[26], v[27]), (v[28], v[29])
+    raise ValueError("no data row in " + path)
+
+
 def main():
     if len(sys.argv) != 2:
         sys.exit("usage: python tests/golden/make_lig_w_fixture.py Q6_ROOT")
@@ -280,9 +295,12 @@ def main():
     top = read_top(os.path.join(d, "lig_w.top"))
     nstates, iqseq = read_fep_atoms(os.path.join(d, "lig_w.fep"))
     fepb = read_fep_bonded(os.path.join(d, "lig_w.fep"), nstates)
+    tot, kin, pot = read_step0_bands(os.path.join(root, "tests", "basic_tests",
+                                                  "SPH_leap-frog_berendsen_benchmark.en"))
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lig_w.npz")
     np.savez_compressed(
         out, **top, **fepb, nstates=nstates, iqseq=iqseq,
+        golden_tot_band=np.array(tot), golden_kin_band=np.array(kin), golden_pot_band=np.array(pot),
         golden_qsurr_el=3.12, golden_qsurr_vdw=139.43,
         golden_el=-7.30, golden_vdw=-413.17,
         # row 1 of SPH_leap-frog_berendsen_benchmark.en: the solute row's

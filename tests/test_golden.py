@@ -62,3 +62,69 @@ def test_lig_w_step0_bonded_energies_match_reference_strings():
                            "golden_qbnd", "golden_qang", "golden_qtor", "golden_qimp")]
     for a, b in zip(got, want):
         assert f"{a:.2f}" == f"{b:.2f}", (a, b)
+
+
+def _step0_energies(s, seed, setup, sp, top, bt):
+    """qdyn's first MD step on the oracle: Maxwell velocities at the input's
+    0.1 K (numpy's generator in place of qdyn's random stream),
+    initial_constraint, stop_cm_translation and temperature(), then step 0
+    (pair lists, pot_energy, leap-frog with Berendsen, SHAKE, temperature).
+    Returns (POT, KIN, Tfree of the start)."""
+    from oracle.oracle import OracleMD
+    from q6_gb300.md import build_constraints, maxwell_velocities, md_params
+    cons = build_constraints(s, setup, top)
+    p = md_params(s, setup, cons)
+    o = Oracle(s, use_lrf=True)
+    o.set_solvent_params(sp)
+    omd = OracleMD(o, p, cons, sp=sp, lam=np.array([1.0]), bonded=bt)
+    x, v = omd.prepare(s.x, maxwell_velocities(s, setup.temp0, seed))
+    tfree0 = omd.tfree
+    r = omd.step(x, v, 0, setup.cut)
+    pot = (sum(r["E"].values()) + r["EQ"].sum() + r["erst"][0] + r["erst"][1] + r["Eb"][:6].sum()
+           + r["EQb"].sum())
+    o.close()
+    return pot, r["ekin"], tfree0
+
+
+def test_lig_w_step0_potential_and_kinetic_energy_match_reference_bands():
+    """Row 1 of SPH_leap-frog_berendsen_benchmark.en holds the reference's
+    step-0 POT, KIN and TOT as mean -/+ one standard deviation over the 20
+    random seeds of its benchmark.  POT covers every term of the path the
+    printed strings leave out (LRF, Q-Q, solvent radial restraint, water
+    polarisation) and KIN covers SHAKE and the Berendsen step.  Three qdyn
+    behaviours matter and are reproduced: the rigid-water angles are cleared
+    by init_constraints; the Born term is on with wat_shells' mu_w; and the
+    Tfree of restrain_solvent's shift comes from initial_constraint's SHAKE
+    of the start (about 35 K, not the 0.1 K of the Maxwell draw), since the
+    topology waters meet the constraints only to SHAKE's tolerance.  Over
+    20 seeds of our own the means must agree within three standard errors
+    plus the print rounding, and the spreads within a factor of two."""
+    from tests.golden.lig_w import lig_w_eq1_inputs
+    s, g = load_lig_w()
+    setup, sp, top, bt = lig_w_eq1_inputs(s)
+    res = np.array([_step0_energies(s, 1000 + k, setup, sp, top, bt) for k in range(20)])
+    pot, kin = res[:, 0], res[:, 1]
+    assert np.all(res[:, 2] > 20.0)            # the start's Tfree is set by SHAKE, not by 0.1 K
+    for ours, band in ((pot, g["golden_pot_band"]), (kin, g["golden_kin_band"]), (pot + kin, g["golden_tot_band"])):
+        ref_mean, ref_sd = 0.5 * (band[0] + band[1]), 0.5 * (band[1] - band[0])
+        sd = ours.std(ddof=1)
+        se = np.sqrt((sd ** 2 + ref_sd ** 2) / 20.0)
+        assert abs(ours.mean() - ref_mean) <= 3.0 * se + 0.005, (ours.mean(), ref_mean, se)
+        assert 0.5 <= sd / ref_sd <= 2.0, (sd, ref_sd)
+
+
+def test_lig_w_shaken_water_angles_are_cleared():
+    """init_constraints clears the first angle whose end atoms are a
+    constrained pair: each rigid water's H-O-H angle (6.33 kcal/mol at step
+    0 if it were kept)."""
+    from tests.golden.lig_w import lig_w_bonded, lig_w_topology_terms
+    s, g = load_lig_w()
+    top, bt = lig_w_topology_terms(s), lig_w_bonded(s)
+    water = np.arange(len(bt.angles)) >= bt.nangles_solute
+    assert np.all(bt.angles[water, 3] == -1) and np.all(top.angles[water, 3] >= 0)
+    assert np.all(bt.angles[~water, 3] == top.angles[~water, 3])
+    x = _step0_coordinates(s, g)
+    o = Oracle(s, use_lrf=True)
+    _, Eb, _ = o.bonded(x, bt, [1.0])
+    _, Eb_top, _ = o.bonded(x, top, [1.0])
+    assert Eb[5] == 0.0 and abs(Eb_top[5] - 6.33) < 0.01
