@@ -333,11 +333,16 @@ int qnb_group_destroy(qnb_group* group);
      dA[...]                          = dE_s/d qA(iq,s)
      dB[...]                          = dE_s/d qB(iq,s)
    E_s is the state's unweighted Q-atom nonbonded energy (qq + qp + qw).  qA,
-   qB are the Q atom's code-1 LJ factors (A_pair = qA * a_j, B_pair = qB * b_j;
-   qavdw(qiac(iq,s),1) with Q atom types, iaclib(iac)%avdw(1) otherwise);
-   1-4 and soft pairs use other factors and do not contribute to dA/dB.  The
-   gradient of the gap E2-E1 is dE2/dp(.,2) - dE1/dp(.,1).  Pair terms are
-   recomputed from the lists; geometric rule only (QNB_ERR_UNSUPPORTED else). */
+   qB are the Q atom's code-1 LJ factors (qavdw(qiac(iq,s),1) with Q atom
+   types, iaclib(iac)%avdw(1) otherwise), combined with the partner's as the
+   topology's rule does (src/simprep.f90:3326-3341): geometric A_pair = qA a_j,
+   B_pair = qB b_j; arithmetic A_pair = (qA + a_j)^12 qB b_j, B_pair =
+   2 (qA + a_j)^6 qB b_j.  1-4 and soft pairs use other factors and do not
+   contribute to dA/dB.  Each state's energy depends on that state's
+   parameters only, so the gradient of the gap E2-E1 is dE2/dp(.,2) for the
+   state-2 parameters and -dE1/dp(.,1) for the state-1 parameters.  Pair
+   terms are recomputed from the lists with FP64 geometry in both precision
+   forms; the sums use FP64 atomics (equal to rounding between calls). */
 int qnb_q_adjoint_dev(qnb_context* ctx, double* dq, double* dA, double* dB);
 
 /* Number of kernel launches the context issued since the last call. */

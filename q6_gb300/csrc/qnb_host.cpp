@@ -579,10 +579,29 @@ int build_model(qnb_context* c, const qnb_topology* t) {
             }
         }
     // adjoint factors of qp pairs: charge factor crg_j (x el14 for 1-4) and
-    // the environment LJ factors when the Q side uses its code-1 factor
-    m.adj_ok = t->ivdw_rule == 1 ? 1 : 0;
+    // the LJ chain factors when the Q side uses its code-1 factor
     auto q_side_code1 = [&](int vdw) { return t->qvdw_flag ? (vdw == 1 || vdw == 2) : (vdw == 1); };
-    std::vector<double4_16a> qp_adj(qp_tab.size());
+    // the Q atom's code-1 factors in state s
+    auto q_code1 = [&](int iq, int s2, double* qa, double* qb) {
+        if (t->qvdw_flag) {
+            *qa = t->qavdw[QIAC(iq, s2) * 3];
+            *qb = t->qbvdw[QIAC(iq, s2) * 3];
+        } else {
+            *qa = t->avdw[t->iac[t->iqseq[iq]] * 3];
+            *qb = t->bvdw[t->iac[t->iqseq[iq]] * 3];
+        }
+    };
+    // d/d(qa), d/d(qb) of A u^2 - B u for the Q side (qa, qb) against (ea, eb)
+    auto lj_chain = [&](double qa, double qb, double ea, double eb, QAdjF* f) {
+        if (t->ivdw_rule == 1) {
+            f->a2 = ea; f->a1 = 0.0; f->b2 = 0.0; f->b1 = -eb;
+        } else {
+            double S1 = qa + ea, S5 = S1 * S1 * S1 * S1 * S1, S6 = S5 * S1, tB = qb * eb;
+            f->a2 = 12.0 * S6 * S5 * tB; f->a1 = -12.0 * S5 * tB;
+            f->b2 = S6 * S6 * eb;        f->b1 = -2.0 * S6 * eb;
+        }
+    };
+    std::vector<QAdjF> qp_adj(qp_tab.size());
     if (nq > 0)
         for (int ig = 0; ig < ns; ++ig) {
             if (qnear[ig]) continue;
@@ -590,17 +609,18 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                 int vdw = t->ljcod[t->iac[ig] * nt + t->iac[t->iqseq[jq]]];
                 for (int s2 = 0; s2 < S; ++s2) {
                     if (QC(s2, ig, jq) == 4) vdw = 3;
-                    double4_16a f;
-                    f.x = t->qq_use_library_charges ? 0.0 : t->crg[ig] * (vdw == 3 ? t->el14_scale : 1.0);
-                    bool lj1 = q_side_code1(vdw);
-                    f.y = lj1 ? t->avdw[t->iac[ig] * 3 + vdw - 1] : 0.0;
-                    f.z = lj1 ? t->bvdw[t->iac[ig] * 3 + vdw - 1] : 0.0;
-                    f.w = 0.0;
+                    QAdjF f{};
+                    f.c = t->qq_use_library_charges ? 0.0 : t->crg[ig] * (vdw == 3 ? t->el14_scale : 1.0);
+                    if (q_side_code1(vdw)) {
+                        double qa, qb;
+                        q_code1(jq, s2, &qa, &qb);
+                        lj_chain(qa, qb, t->avdw[t->iac[ig] * 3 + vdw - 1], t->bvdw[t->iac[ig] * 3 + vdw - 1], &f);
+                    }
                     qp_adj[((size_t)ig * nq + jq) * S + s2] = f;
                 }
             }
         }
-    TRY(c->upload((double4_16a**)&m.qp_adj, qp_adj));
+    TRY(c->upload((QAdjF**)&m.qp_adj, qp_adj));
     std::vector<QParF> qp_tabf(qp_tab.size());
     for (size_t k = 0; k < qp_tab.size(); ++k)
         qp_tabf[k] = QParF{(float)qp_tab[k].A, (float)qp_tab[k].B, (float)qp_tab[k].el, (float)qp_tab[k].sc};
@@ -634,23 +654,24 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                     qw_tab[((size_t)iq * sa + a) * S + s] = p;
                 }
             }
-    std::vector<double4_16a> qw_adj(qw_tab.size());
+    std::vector<QAdjF> qw_adj(qw_tab.size());
     if (nq > 0 && t->nwat > 0)
         for (int iq = 0; iq < nq; ++iq)
             for (int a = 0; a < sa; ++a) {
                 int tw = t->iac[ns + a];
                 int vdw = t->ljcod[tw * nt + t->iac[t->iqseq[iq]]];
                 for (int s2 = 0; s2 < S; ++s2) {
-                    double4_16a f;
-                    f.x = t->qq_use_library_charges ? 0.0 : t->crg[ns + a];
-                    bool lj1 = q_side_code1(vdw);
-                    f.y = lj1 ? t->avdw[tw * 3 + vdw - 1] : 0.0;
-                    f.z = lj1 ? t->bvdw[tw * 3 + vdw - 1] : 0.0;
-                    f.w = 0.0;
+                    QAdjF f{};
+                    f.c = t->qq_use_library_charges ? 0.0 : t->crg[ns + a];
+                    if (q_side_code1(vdw)) {
+                        double qa, qb;
+                        q_code1(iq, s2, &qa, &qb);
+                        lj_chain(qa, qb, t->avdw[tw * 3 + vdw - 1], t->bvdw[tw * 3 + vdw - 1], &f);
+                    }
                     qw_adj[((size_t)iq * sa + a) * S + s2] = f;
                 }
             }
-    TRY(c->upload((double4_16a**)&m.qw_adj, qw_adj));
+    TRY(c->upload((QAdjF**)&m.qw_adj, qw_adj));
     std::vector<QParF> qw_tabf(qw_tab.size());
     for (size_t k = 0; k < qw_tab.size(); ++k)
         qw_tabf[k] = QParF{(float)qw_tab[k].A, (float)qw_tab[k].B, (float)qw_tab[k].el, (float)qw_tab[k].sc};
@@ -730,14 +751,17 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                 {
                     double f14 = vdw == 3 ? t->el14_scale : 1.0;
                     bool lib = t->qq_use_library_charges != 0;
-                    bool lj1 = vdw == 1;
-                    double fa_i = t->qvdw_flag ? t->qavdw[ti * 3] : t->avdw[t->iac[ia] * 3];
-                    double fa_j = t->qvdw_flag ? t->qavdw[tj * 3] : t->avdw[t->iac[ja] * 3];
-                    double fb_i = t->qvdw_flag ? t->qbvdw[ti * 3] : t->bvdw[t->iac[ia] * 3];
-                    double fb_j = t->qvdw_flag ? t->qbvdw[tj * 3] : t->bvdw[t->iac[ja] * 3];
-                    qadj.push_back(QQAdj{iq, jq, s, 0, lib ? 0.0 : QCRG(jq, s) * els * f14,
-                                         lib ? 0.0 : QCRG(iq, s) * els * f14, lj1 ? fa_j : 0.0, lj1 ? fa_i : 0.0,
-                                         lj1 ? fb_j : 0.0, lj1 ? fb_i : 0.0});
+                    QQAdj f{iq, jq, s, 0, QAdjF{}, QAdjF{}};
+                    f.fi.c = lib ? 0.0 : QCRG(jq, s) * els * f14;
+                    f.fj.c = lib ? 0.0 : QCRG(iq, s) * els * f14;
+                    if (vdw == 1) {   // both sides' code-1 factors
+                        double ai, bi, aj, bj;
+                        q_code1(iq, s, &ai, &bi);
+                        q_code1(jq, s, &aj, &bj);
+                        lj_chain(ai, bi, aj, bj, &f.fi);
+                        lj_chain(aj, bj, ai, bi, &f.fj);
+                    }
+                    qadj.push_back(f);
                 }
             }
         }
@@ -759,11 +783,14 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                 if (!set) continue;
                 qq.push_back(QQEntry{ia, ja, s, 0, p.A, p.B, p.el, p.sc});
                 {
-                    bool lj1 = q_side_code1(vdw);
-                    qadj.push_back(QQAdj{iq, -1, s, 0,
-                                         t->qq_use_library_charges ? 0.0 : t->crg[ja] * (vdw == 3 ? t->el14_scale : 1.0),
-                                         0.0, lj1 ? t->avdw[t->iac[ja] * 3 + vdw - 1] : 0.0, 0.0,
-                                         lj1 ? t->bvdw[t->iac[ja] * 3 + vdw - 1] : 0.0, 0.0});
+                    QQAdj f{iq, -1, s, 0, QAdjF{}, QAdjF{}};
+                    f.fi.c = t->qq_use_library_charges ? 0.0 : t->crg[ja] * (vdw == 3 ? t->el14_scale : 1.0);
+                    if (q_side_code1(vdw)) {
+                        double qa, qb;
+                        q_code1(iq, s, &qa, &qb);
+                        lj_chain(qa, qb, t->avdw[t->iac[ja] * 3 + vdw - 1], t->bvdw[t->iac[ja] * 3 + vdw - 1], &f.fi);
+                    }
+                    qadj.push_back(f);
                 }
             }
         }
@@ -1919,14 +1946,12 @@ int qnb_group_compute(qnb_group* g, double Tfree, int32_t istep) {
 
 int qnb_q_adjoint_dev(qnb_context* c, double* dq, double* dA, double* dB) {
     if (!c || !dq || !dA || !dB) return fail(QNB_ERR_ARG, "null argument");
-    if (!c->m.adj_ok) return fail(QNB_ERR_UNSUPPORTED, "parameter gradients need the geometric combination rule");
     if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built");
     CU(cudaSetDevice(c->device));
     const size_t n = (size_t)c->nqat * c->S;
     if (n == 0) return QNB_OK;
     for (int w = 0; w < c->nwin; ++w) CU(cudaMemsetAsync(c->st[w].adj, 0, sizeof(double) * 3 * n, c->stream));
-    if (c->mixed) launch_pack(c->all());
-    launch_q_adjoint(c->all(), c->mixed);
+    launch_q_adjoint(c->all());
     c->launches += 3;
     TRY(check_launch());
     std::vector<double> h(3 * n);

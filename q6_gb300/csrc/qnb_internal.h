@@ -46,13 +46,21 @@ struct alignas(16) QParF {
     float A, B, el, sc;
 };
 
-// Adjoint factors of a static Q pair: d(el)/d(qcrg), d(A)/d(qA), d(B)/d(qB)
-// for Q atom iq (c_i, a_i, b_i) and, for Q-Q pairs, for jq (c_j, a_j, b_j);
-// jq = -1 for a Q-bonded solute partner.  a/b are zero for pairs whose Q-side
-// LJ factor is not the code-1 factor (1-4 pairs, soft pairs).
+// Adjoint factors of one Q pair term E = el/r + A u^2 - B u, u = 1/(r^6 + alpha),
+// for the Q atom's charge and code-1 LJ factors a, b:
+//   dE/dq = c / r,  dE/da = a2 u^2 + a1 u,  dE/db = b2 u^2 + b1 u.
+// Geometric rule: a2 = a_other, b1 = -b_other, a1 = b2 = 0.  Arithmetic rule,
+// S = a + a_other: a2 = 12 S^11 b b_other, a1 = -12 S^5 b b_other,
+// b2 = S^12 b_other, b1 = -2 S^6 b_other.  The LJ factors are zero where the Q
+// side does not use its code-1 factor (1-4 pairs, soft pairs).
+struct alignas(16) QAdjF {
+    double c, a2, a1, b2, b1, pad;
+};
+// The same for a static Q pair: Q atom iq and, for Q-Q pairs, jq (jq = -1
+// for a Q-bonded solute partner).
 struct QQAdj {
     int iq, jq, s, pad;
-    double ci, cj, ai, aj, bi, bj;
+    QAdjF fi, fj;
 };
 
 // Static model on the device.  Passed by value to kernels.
@@ -96,11 +104,10 @@ struct DevModel {
     const QParF* qp_tabft;      // [nqat][nat_solute][S] (the transposed Q kernel's order)
     const QPar* qw_tab;         // [nqat][sa][S]
     const QParF* qw_tabf;
-    // adjoint factors (c, a, b, unused) with the layouts of qp_tab / qw_tab
-    const double4_16a* qp_adj;
-    const double4_16a* qw_adj;
+    // adjoint factors with the layouts of qp_tab / qw_tab
+    const QAdjF* qp_adj;
+    const QAdjF* qw_adj;
     const QQAdj* qq_adj;        // parallel to the static Q-Q / Q-bonded list
-    int adj_ok;                 // geometric rule: parameter gradients available
     double xpcent[3], xwcent[3];
     float wcoff[3];             // xpcent - xwcent in FP32: packed (xpcent-centred) coordinates to xwcent-centred
     double rexcl_o2;
@@ -231,7 +238,7 @@ void launch_restrain_solvent(const Launch& L, const SolventDev& p, double Tfree,
                              const uint8_t* heavy_solv);
 int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int mixed);
 
-void launch_q_adjoint(const Launch& L, int mixed);
+void launch_q_adjoint(const Launch& L);
 
 void launch_export_pairs(const Launch& L, int win, int kind, int32_t* di, int32_t* dj, int64_t cap,
                          int* dcount);

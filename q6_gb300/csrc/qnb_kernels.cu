@@ -1529,7 +1529,10 @@ __global__ void __launch_bounds__(kQBlock) k_qenv_lanes(DevModel m, const DevSta
     }
 }
 
-template <bool MIX, bool SPC, bool WATER, int SMAX>
+// Adjoint of the Q-environment terms in FP64 in both precision forms: the
+// adjoint is an occasional call for parameter fitting, and FP64 geometry keeps
+// its gradients to the FP64 reference's rounding.
+template <bool SPC, bool WATER, int SMAX>
 __global__ void __launch_bounds__(kQBlock) k_qadj_env(DevModel m, const DevState* __restrict__ states) {
     const DevState& s = states[blockIdx.y];
     double aq[2][SMAX] = {}, aa[2][SMAX] = {}, ab[2][SMAX] = {};
@@ -1546,32 +1549,22 @@ __global__ void __launch_bounds__(kQBlock) k_qadj_env(DevModel m, const DevState
                 int iq = k * 32 + lane;
                 if (iq >= m.nqat) break;
                 int i = m.iqseq[iq];
-                double r, r6;
-                if constexpr (MIX) {
-                    float4 xi = s.xq[i], xj = s.xq[j];
-                    float tx = xj.x - xi.x, ty = xj.y - xi.y, tz = xj.z - xi.z;
-                    float d2 = tx * tx + ty * ty + tz * tz;
-                    r = (double)rsqrtf(d2);
-                    r6 = (double)(d2 * d2 * d2);
-                } else {
-                    double tx = s.x[3 * j] - s.x[3 * i], ty = s.x[3 * j + 1] - s.x[3 * i + 1],
-                           tz = s.x[3 * j + 2] - s.x[3 * i + 2];
-                    double d2 = tx * tx + ty * ty + tz * tz;
-                    r = 1.0 / sqrt(d2);
-                    r6 = d2 * d2 * d2;
-                }
+                double tx = s.x[3 * j] - s.x[3 * i], ty = s.x[3 * j + 1] - s.x[3 * i + 1],
+                       tz = s.x[3 * j + 2] - s.x[3 * i + 2];
+                double d2 = tx * tx + ty * ty + tz * tz;
+                double r = 1.0 / sqrt(d2), r6 = d2 * d2 * d2;
                 size_t t0 = WATER ? (size_t)(iq * m.sa + a) * S : ((size_t)j * m.nqat + iq) * S;
-                const double4_16a* F = (WATER ? m.qw_adj : m.qp_adj) + t0;
+                const QAdjF* F = (WATER ? m.qw_adj : m.qp_adj) + t0;
                 const QPar* P = (WATER ? m.qw_tab : m.qp_tab) + t0;
 #pragma unroll
                 for (int st = 0; st < SMAX; ++st) {
                     if (st >= S) break;
-                    double4_16a f = F[st];
-                    aq[k][st] += f.x * r;
+                    const QAdjF& f = F[st];
+                    aq[k][st] += f.c * r;
                     if (lj) {
                         double u = 1.0 / (r6 + P[st].sc);
-                        aa[k][st] += f.y * u * u;
-                        ab[k][st] -= f.z * u;
+                        aa[k][st] += (f.a2 * u + f.a1) * u;
+                        ab[k][st] += (f.b2 * u + f.b1) * u;
                     }
                 }
             }
@@ -1613,17 +1606,17 @@ __global__ void k_qadj_qq(DevModel m, const DevState* __restrict__ states) {
     double u = 1.0 / (r6 + e.sc);
     int nqs = m.nqat * m.S;
     int oi = f.iq + m.nqat * f.s;
-    atomicAdd(s.adj + oi, f.ci * r);
+    atomicAdd(s.adj + oi, f.fi.c * r);
     if (!e.soft) {
-        atomicAdd(s.adj + nqs + oi, f.ai * u * u);
-        atomicAdd(s.adj + 2 * nqs + oi, -f.bi * u);
+        atomicAdd(s.adj + nqs + oi, (f.fi.a2 * u + f.fi.a1) * u);
+        atomicAdd(s.adj + 2 * nqs + oi, (f.fi.b2 * u + f.fi.b1) * u);
     }
     if (f.jq >= 0) {
         int oj = f.jq + m.nqat * f.s;
-        atomicAdd(s.adj + oj, f.cj * r);
+        atomicAdd(s.adj + oj, f.fj.c * r);
         if (!e.soft) {
-            atomicAdd(s.adj + nqs + oj, f.aj * u * u);
-            atomicAdd(s.adj + 2 * nqs + oj, -f.bj * u);
+            atomicAdd(s.adj + nqs + oj, (f.fj.a2 * u + f.fj.a1) * u);
+            atomicAdd(s.adj + 2 * nqs + oj, (f.fj.b2 * u + f.fj.b1) * u);
         }
     }
 }
@@ -4185,21 +4178,18 @@ int launch_watpol(const Launch& L, const SolventDev& p, int istep, int md, int m
     return nl;
 }
 
-void launch_q_adjoint(const Launch& L, int mixed) {
+void launch_q_adjoint(const Launch& L) {
     if (L.m.nqat == 0) return;
     bool spc = L.m.spc != 0, s4 = L.m.S <= 4;
-#define QA(MIX, SPC, W, SM) k_qadj_env<MIX, SPC, W, SM><<<g, kQBlock, 0, L.st>>>(L.m, L.ds)
+#define QA(SPC, W, SM) k_qadj_env<SPC, W, SM><<<g, kQBlock, 0, L.st>>>(L.m, L.ds)
     if (L.m.nwat > 0) {
         dim3 g = grid_for(L.s0.cap_qw * 32, kQBlock, 8, L.nwin);
-        if (mixed) { if (spc) { if (s4) QA(true, true, true, 4); else QA(true, true, true, kMaxStates); }
-                     else { if (s4) QA(true, false, true, 4); else QA(true, false, true, kMaxStates); } }
-        else { if (spc) { if (s4) QA(false, true, true, 4); else QA(false, true, true, kMaxStates); }
-               else { if (s4) QA(false, false, true, 4); else QA(false, false, true, kMaxStates); } }
+        if (spc) { if (s4) QA(true, true, 4); else QA(true, true, kMaxStates); }
+        else { if (s4) QA(false, true, 4); else QA(false, true, kMaxStates); }
     }
     if (L.m.nat_solute > 0) {
         dim3 g = grid_for(L.s0.cap_qp * 32, kQBlock, 8, L.nwin);
-        if (mixed) { if (s4) QA(true, true, false, 4); else QA(true, true, false, kMaxStates); }
-        else { if (s4) QA(false, true, false, 4); else QA(false, true, false, kMaxStates); }
+        if (s4) QA(true, false, 4); else QA(true, false, kMaxStates);
     }
 #undef QA
     if (L.s0.nqq > 0) k_qadj_qq<<<dim3((L.s0.nqq + 63) / 64, L.nwin), 64, 0, L.st>>>(L.m, L.ds);

@@ -1,6 +1,13 @@
-"""Adjoint of the Q-atom energies: dE_s/d(qcrg, qA, qB) from the GPU kernel
-against central finite differences of the FP64 oracle's energies (h = 1e-5
-relative), and the mixed-form adjoint against the FP64-form adjoint."""
+"""Adjoint of the Q-atom energies: dE_s/d(qcrg, qA, qB) from the GPU kernel.
+
+Config 4 as specified: 30 Q atoms in 4 states, every one of the 120 charges
+and 240 code-1 LJ factors, 200 seeded snapshots (one batched window each),
+against the FP64 reference gradient (oracle/adjoint.py, pinned to the C
+oracle's energies and central differences) and against central differences
+(h = 1e-5 relative) of the reference energies, within 1e-4 relative; the gap
+gradient d(E2 - E1) as its own assertion; the arithmetic combination rule.
+Also a system with soft pairs and electrostatic scaling against the C
+oracle's central differences, and the mixed form against the FP64 form."""
 import copy
 
 import numpy as np
@@ -30,6 +37,61 @@ def gpu_adjoint(s, prec):
         eng.make_pair_lists_dev(**CUT)
         dq, dA, dB = eng.q_adjoint_dev()
     return dq[0], dA[0], dB[0]
+
+
+def gpu_adjoint_snapshots(s, prec, xs):
+    """Adjoint of every snapshot, one batched window each: [n][nq][S] x 3."""
+    with NonbondedEngine(s, precision=prec, windows=len(xs)) as eng:
+        eng.set_coordinates_dev(np.stack(xs))
+        eng.make_pair_lists_dev(**CUT)
+        return eng.q_adjoint_dev()
+
+
+def close(g, ref, rel):
+    scale = np.abs(ref).max()
+    return bool(np.all(np.abs(g - ref) <= rel * np.maximum(np.abs(ref), 1e-3 * scale)))
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_MIXED])
+def test_config4_adjoint_200_snapshots(prec):
+    from oracle.adjoint import QEnergyReference
+    from q6_gb300.system import config_adjoint
+    s = config_adjoint()
+    rng = np.random.default_rng(4000)
+    xs = [s.x + rng.normal(0.0, 0.05, s.x.shape) for _ in range(200)]
+    dq, dA, dB = gpu_adjoint_snapshots(s, prec, xs)
+    ref = QEnergyReference(s)
+    assert dq.shape == (200, 30, 4) and dA.shape == (200, 30, 4)
+    for n, x in enumerate(xs):
+        _, gq, ga, gb = ref.evaluate(x)
+        fq, fa, fb = ref.finite_differences(x, h=1e-5)
+        for name, g, r, f in (("q", dq[n], gq, fq), ("A", dA[n], ga, fa), ("B", dB[n], gb, fb)):
+            assert close(g, r, 1e-9), (prec, n, name)          # the FP64 reference gradient
+            assert close(g, f, 1e-4), (prec, n, name)          # central differences
+            # the gap E2 - E1: +dE2/dp for state-2 parameters, -dE1/dp for state 1
+            gap = np.zeros_like(g)
+            gap[:, 1], gap[:, 0] = g[:, 1], -g[:, 0]
+            gap_fd = np.zeros_like(f)
+            gap_fd[:, 1], gap_fd[:, 0] = f[:, 1], -f[:, 0]
+            assert close(gap, gap_fd, 1e-4), (prec, n, name, "gap")
+
+
+def test_arithmetic_rule_adjoint():
+    from oracle.adjoint import QEnergyReference
+    from q6_gb300.system import config_adjoint
+    from tests.test_oracle_adjoint import arithmetic_variant
+    s = arithmetic_variant(config_adjoint())
+    rng = np.random.default_rng(4100)
+    xs = [s.x + rng.normal(0.0, 0.05, s.x.shape) for _ in range(20)]
+    ref = QEnergyReference(s)
+    for prec in (PREC_FP64, PREC_MIXED):
+        dq, dA, dB = gpu_adjoint_snapshots(s, prec, xs)
+        for n, x in enumerate(xs):
+            _, gq, ga, gb = ref.evaluate(x)
+            fq, fa, fb = ref.finite_differences(x, h=1e-5)
+            for name, g, r, f in (("q", dq[n], gq, fq), ("A", dA[n], ga, fa), ("B", dB[n], gb, fb)):
+                assert close(g, r, 1e-9), (prec, n, name)
+                assert close(g, f, 1e-4), (prec, n, name)
 
 
 @pytest.fixture(scope="module")
@@ -69,8 +131,8 @@ def test_adjoint_matches_finite_differences(evb4):
 
 
 def test_mixed_adjoint_matches_fp64_adjoint(evb4):
+    """Both forms recompute the pair terms in FP64: equal to rounding."""
     a64 = gpu_adjoint(evb4, PREC_FP64)
     a32 = gpu_adjoint(evb4, PREC_MIXED)
     for g64, g32 in zip(a64, a32):
-        scale = np.abs(g64).max()
-        assert np.all(np.abs(g32 - g64) <= 1e-3 * scale)
+        assert close(g32, g64, 1e-10)

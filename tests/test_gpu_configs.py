@@ -12,12 +12,14 @@ Bars: the FP64 form against the CPU oracle within 1e-6 kcal/mol per energy
 term (1e-9 relative for terms above 1,000 kcal/mol: the FP64 form sums with
 atomics, so its rounding follows the schedule) and 1e-6 relative per gradient
 component; the mixed form within 1e-3 relative; batched windows bit-equal to
-single-window contexts; list sizes equal."""
+single-window contexts; every pair list equal to the oracle's as a set
+(configs 1, 2, 4 and 5, both forms)."""
 import numpy as np
 import pytest
 
 from oracle.oracle import Oracle
-from q6_gb300.qnb import LIST_PP, LIST_PW, LIST_QP, LIST_QW, LIST_WW, PREC_FP64, PREC_MIXED, NonbondedEngine
+from q6_gb300.qnb import (LIST_PP, LIST_PP14, LIST_PW, LIST_QP, LIST_QW, LIST_WW, PREC_FP64, PREC_MIXED,
+                          NonbondedEngine)
 from q6_gb300.system import (config_adjoint, config_large, config_small, config_window, default_solvent_params,
                              lambdas_for_window, make_system)
 
@@ -36,6 +38,24 @@ def grad_ok(d, d0, rel):
     return bool(np.all(np.abs(d - d0) <= rel * scale + 1e-9))
 
 
+UNORDERED = {LIST_PP, LIST_PP14, LIST_WW}
+
+
+def assert_lists_equal_as_sets(eng, o, natom, label):
+    """Every pair list of the engine equals the oracle's as a set, compared
+    as sorted int64 keys (config 5 has ~10^7 entries)."""
+    for kind in (LIST_PP, LIST_PW, LIST_WW, LIST_QP, LIST_QW, LIST_PP14):
+        assert eng.list_size(kind) == o.list_size(kind), (label, kind)
+        keys = []
+        for i, j in (eng.export_pairs(kind), o.export_pairs(kind)):
+            i, j = i.astype(np.int64), j.astype(np.int64)
+            if kind in UNORDERED:
+                i, j = np.minimum(i, j), np.maximum(i, j)
+            keys.append(np.sort(i * natom + j))
+        assert np.array_equal(keys[0], keys[1]), (label, kind)
+        assert len(np.unique(keys[0])) == len(keys[0]), (label, kind)   # no pair listed twice
+
+
 def check_vs_oracle(s, cut, lam):
     sp = default_solvent_params(s)
     o = Oracle(s)
@@ -46,8 +66,7 @@ def check_vs_oracle(s, cut, lam):
         with NonbondedEngine(s, precision=prec) as eng:
             eng.set_solvent_params(sp)
             d, E, EQ, R = eng.evaluate(s.x, lam, cut=cut, solvent=sp)
-            for kind in (LIST_PP, LIST_PW, LIST_WW, LIST_QP, LIST_QW):
-                assert eng.list_size(kind) == o.list_size(kind), (prec, kind)
+            assert_lists_equal_as_sets(eng, o, s.natom, (s.name, prec))
         for k in E0:
             bar = fp64_bar(E0[k]) if prec == PREC_FP64 else tol * max(1.0, abs(E0[k]))
             assert abs(E[k] - E0[k]) <= bar, (prec, k, E[k], E0[k])
@@ -145,9 +164,14 @@ def test_config5_large_fp64_vs_oracle(large):
     o = Oracle(s)
     o.set_solvent_params(sp)
     d0, E0, EQ0, R0 = o.evaluate(s.x, lam, cut=CUT12, solvent=sp)
+    o.make_pair_lists(s.x, **CUT12)
     with NonbondedEngine(s, precision=PREC_FP64) as eng:
         eng.set_solvent_params(sp)
         d, E, EQ, R = eng.evaluate(s.x, lam, cut=CUT12, solvent=sp)
+        assert_lists_equal_as_sets(eng, o, s.natom, "config5 fp64")
+    with NonbondedEngine(s, precision=PREC_MIXED) as eng:
+        eng.make_pair_lists(s.x, **CUT12)
+        assert_lists_equal_as_sets(eng, o, s.natom, "config5 mixed")
     for k in E0:
         assert abs(E[k] - E0[k]) <= fp64_bar(E0[k]), (k, E[k], E0[k])
     assert np.all(np.abs(EQ - EQ0) <= 1e-6), (EQ, EQ0)
