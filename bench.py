@@ -405,20 +405,64 @@ def sgemm_fp32_peak(torch):
         return None
 
 
-def dg_check(s, sp, lams, local, nwin, frames=4):
-    """Per-window dG (Qfep exponential averaging) of the mixed form against
-    the FP64 form on identical frames: `frames` perturbed copies (0.05 A) of
-    each window's coordinates.  Every window's per-state energies go through
-    an energy file in qdyn's layout, and dG comes from the Qfep summary of
-    those files."""
+def fp64_md_frames(s, sp, lams, bt, local, nframes, every, equil, minimize_steps):
+    """Frames of each window's own FP64 trajectory: the device MD path in
+    the plain FP64 form (qnb_md_run: the evaluation, bonded terms, leap-frog
+    with Berendsen at 300 K, SHAKE, lists every 25 steps) at the window's
+    lambda, after a capped steepest descent of the generated start (in the
+    mixed form, set-up only) and `equil` steps.  Returns [nwin][nframes][natom][3]
+    and the number of MD steps run per window."""
     import numpy as np
+    from q6_gb300.md import MdSetup, maxwell_velocities
+    from q6_gb300.qnb import PREC_FP64, PREC_MIXED, NonbondedEngine
+    from q6_gb300.system import lambdas_for_window
+    nwin = len(lams)
+    setup = MdSetup(stepsize=1.0, temp0=300.0, tau_t=10.0, nbcycle=NBCYCLE, cut=dict(CUT))
+    with NonbondedEngine(s, precision=PREC_MIXED, device=local, windows=nwin) as e:
+        e.set_solvent_params(sp)
+        for w in range(nwin):
+            e.set_lambda(lambdas_for_window(lams[w], s.nstates), window=w)
+        e.set_bonded(bt)
+        e.set_coordinates_dev(np.stack([s.x] * nwin))
+        e.md_init(setup)
+        e.md_minimize(minimize_steps, initial_step=1e-4, force_cutoff=1.0, max_move=0.05)
+        x0 = np.stack([e.md_state(w)[0] for w in range(nwin)])
+    frames = np.zeros((nwin, nframes, s.natom, 3))
+    with NonbondedEngine(s, precision=PREC_FP64, device=local, windows=nwin) as e:
+        e.set_solvent_params(sp)
+        for w in range(nwin):
+            e.set_lambda(lambdas_for_window(lams[w], s.nstates), window=w)
+        e.set_bonded(bt)
+        e.set_coordinates_dev(x0)
+        e.md_init(setup)
+        e.md_set_velocities(np.stack([maxwell_velocities(s, 300.0, 300 + w) for w in range(nwin)]))
+        e.md_prepare(stop_cm=True)
+        e.md_run(equil, 0, records=False)
+        for k in range(nframes):
+            e.md_run(every, equil + k * every, records=False)
+            for w in range(nwin):
+                frames[w, k] = e.md_state(w)[0]
+    return frames, equil + nframes * every
+
+
+def dg_check(s, sp, lams, local, nwin, nframes=40, every=10, equil=100):
+    """Per-window dG (Qfep exponential averaging) of the mixed form against
+    the FP64 form on identical frames: `nframes` frames of each window's own
+    FP64 MD trajectory (fp64_md_frames), re-evaluated in both forms with the
+    lists rebuilt for every frame.  Every window's per-state energies (Q
+    nonbonded and Q bonded terms) go through an energy file in qdyn's layout,
+    and dG comes from the Qfep summary of those files."""
+    import numpy as np
+    from q6_gb300.bonded import remove_shaken, synthetic_bonded
     from q6_gb300.enefile import EnergyFileWriter, qfep_files
     from q6_gb300.fep import BOLTZ, window_increments
     from q6_gb300.qnb import PREC_FP64, PREC_MIXED, NonbondedEngine
     from q6_gb300.system import lambdas_for_window
-    rng = np.random.default_rng(99)
+    bt = remove_shaken(synthetic_bonded(s, seed=21), np.asarray(s.heavy).astype(bool), s.nat_solute)
+    t0 = time.perf_counter()
+    fr, nsteps = fp64_md_frames(s, sp, lams, bt, local, nframes, every, equil, 3000)
+    t_md = time.perf_counter() - t0
     lam = np.array([lambdas_for_window(l, s.nstates) for l in lams])
-    fr = np.stack([np.stack([s.x + rng.normal(0, 0.05, s.x.shape) for _ in range(frames)]) for _ in range(nwin)])
     out = {}
     tmp = tempfile.mkdtemp(prefix="qnb_dg_")
     for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
@@ -426,14 +470,16 @@ def dg_check(s, sp, lams, local, nwin, frames=4):
         files = [EnergyFileWriter(p, s.nstates) for p in paths]
         with NonbondedEngine(s, precision=prec, device=local, windows=nwin) as e:
             e.set_solvent_params(sp)
+            e.set_bonded(bt)
             for w in range(nwin):
                 e.set_lambda(lam[w], window=w)
-            for k in range(frames):
+            for k in range(nframes):
                 e.set_coordinates_dev(fr[:, k])
                 e.make_pair_lists_dev(**CUT)
                 _, EQ, _ = e.compute_dev(sync=True)
+                _, EQb = e.bonded_energies()
                 for w in range(nwin):
-                    files[w].write_step(lam[w], EQ[w])
+                    files[w].write_step(lam[w], EQ[w], q_bonded=EQb[w])
         for f in files:
             f.close()
         out[name] = window_increments(qfep_files(paths, s.nstates, rt=BOLTZ * 300.0)[3])
@@ -441,11 +487,15 @@ def dg_check(s, sp, lams, local, nwin, frames=4):
             os.remove(p)
     os.rmdir(tmp)
     err = np.abs(out["mixed"] - out["fp64"])
-    return {"windows": nwin, "frames_per_window": frames, "max_abs_err_kcal": round(float(err.max()), 6),
-            "mean_abs_err_kcal": round(float(err.mean()), 6), "tolerance_kcal": 0.02,
+    return {"windows": nwin, "frames_per_window": nframes, "max_abs_err_kcal": float("%.3g" % err.max()),
+            "mean_abs_err_kcal": float("%.3g" % err.mean()), "tolerance_kcal": 0.02,
             "total_dG_fp64": round(float(out["fp64"].sum()), 4), "total_dG_mixed": round(float(out["mixed"].sum()), 4),
-            "frames": "seeded 0.05 A perturbations of the window coordinates (no MD trajectory)",
-            "path": "per-window energy files in qdyn's put_ene layout -> Qfep FEP summary"}
+            "frames": f"FP64 MD trajectory of every window (device FP64 MD path at the window's lambda, 300 K, 1 fs): "
+                      f"{equil} steps to equilibrate, then a frame every {every} steps ({nsteps} steps per window), "
+                      f"after a capped steepest descent of the generated start",
+            "md_seconds": round(t_md, 1),
+            "path": "per-window energy files in qdyn's put_ene layout (Q nonbonded and Q bonded terms) -> Qfep "
+                    "FEP summary"}
 
 
 def read_traffic(kernel):
@@ -626,7 +676,7 @@ def md_step(args, s, sp, lams, local, tuning=None):
     it (records read back after the run)."""
     import numpy as np
     import torch
-    from q6_gb300.bonded import synthetic_bonded
+    from q6_gb300.bonded import remove_shaken, synthetic_bonded
     from q6_gb300.md import MdSetup, maxwell_velocities
     from q6_gb300.qnb import PREC_MIXED, NonbondedEngine, QnbError
     from q6_gb300.system import lambdas_for_window
@@ -638,7 +688,7 @@ def md_step(args, s, sp, lams, local, tuning=None):
             e.set_lambda(lambdas_for_window(lams[w], s.nstates), window=w)
         if tuning:
             e.set_tuning(tuning)
-        bt = synthetic_bonded(s, seed=21)
+        bt = remove_shaken(synthetic_bonded(s, seed=21), np.asarray(s.heavy).astype(bool), s.nat_solute)
         e.set_bonded(bt)
         e.set_coordinates_dev(np.stack([s.x] * nwin))
         setup = MdSetup(stepsize=1.0, temp0=300.0, tau_t=10.0, nbcycle=25, cut=dict(CUT))
@@ -672,8 +722,9 @@ def md_step(args, s, sp, lams, local, tuning=None):
         return {"error": str(ex)}
     return {"value": round(nwin * steps / (ms / 1e3), 1), "unit": "window-MD-steps/s",
             "ms_per_step": round(ms / steps, 4), "steps": steps, "windows": nwin,
-            "list_builds": steps // 25, "bonded_terms": int(len(bt.bonds) + len(bt.angles) + len(bt.torsions) +
-                                                            len(bt.impropers)),
+            "list_builds": steps // 25, "bonded_terms": int((bt.bonds[:, 2] >= 0).sum() + (bt.angles[:, 3] >= 0).sum() +
+                                                            (bt.torsions[:, 4] >= 0).sum() +
+                                                            (bt.impropers[:, 4] >= 0).sum()),
             "q_bonded_terms": int(len(bt.qbonds) + len(bt.qangles) + len(bt.qtorsions) + len(bt.qimpropers)),
             "tfree_start_end": [round(float(rec0[0]["tfree"].mean()), 2), round(float(rec[0]["tfree"].mean()), 2)],
             "shake_iterations_per_step": round(float(rec[0]["shake_iterations"].mean()), 1),

@@ -78,3 +78,62 @@ def test_dg_through_energy_files(tmp_path):
         assert np.allclose(dg, qfep_dg(v, lams, rt)[2], rtol=1e-12, atol=1e-10), name
         inc[name] = window_increments(dg)
     assert np.abs(inc["mixed"] - inc["fp64"]).max() <= 0.02
+
+
+def test_mixed_dg_on_fp64_md_frames():
+    """The primary check of the specification: frames of each window's own
+    FP64 trajectory (the device FP64 MD path at the window's lambda, 300 K,
+    bonded and Q bonded terms, SHAKE) re-evaluated in both forms; per-window
+    dG within 0.02 kcal/mol."""
+    from q6_gb300.bonded import remove_shaken, synthetic_bonded
+    from q6_gb300.md import MdSetup, maxwell_velocities
+    s = make_system(R=15.0, n_solute=40, group_sizes=(3, 5), ntypes=6, nq=8, nstates=2, q_sigma=0.4,
+                    seed=778)
+    W, K, every, equil = 11, 20, 10, 60
+    lams = np.array([lambdas_for_window(l, 2) for l in np.linspace(0.0, 1.0, W)])
+    sp = default_solvent_params(s)
+    bt = remove_shaken(synthetic_bonded(s, seed=5), np.asarray(s.heavy).astype(bool), s.nat_solute)
+    setup = MdSetup(stepsize=1.0, temp0=300.0, tau_t=10.0, nbcycle=25, cut=dict(CUT))
+    with NonbondedEngine(s, precision=PREC_MIXED, windows=W) as e:     # relax the generated start
+        e.set_solvent_params(sp)
+        for w in range(W):
+            e.set_lambda(lams[w], window=w)
+        e.set_bonded(bt)
+        e.set_coordinates_dev(np.stack([s.x] * W))
+        e.md_init(setup)
+        e.md_minimize(1500, initial_step=1e-4, force_cutoff=1.0, max_move=0.05)
+        x0 = np.stack([e.md_state(w)[0] for w in range(W)])
+    frames = np.zeros((W, K, s.natom, 3))
+    with NonbondedEngine(s, precision=PREC_FP64, windows=W) as e:
+        e.set_solvent_params(sp)
+        for w in range(W):
+            e.set_lambda(lams[w], window=w)
+        e.set_bonded(bt)
+        e.set_coordinates_dev(x0)
+        e.md_init(setup)
+        e.md_set_velocities(np.stack([maxwell_velocities(s, 300.0, 40 + w) for w in range(W)]))
+        e.md_prepare(stop_cm=True)
+        e.md_run(equil, 0, records=False)
+        for k in range(K):
+            e.md_run(every, equil + k * every, records=False)
+            for w in range(W):
+                frames[w, k] = e.md_state(w)[0]
+    assert np.all(np.isfinite(frames))
+    rt = BOLTZ * 300.0
+    inc = {}
+    for prec in (PREC_FP64, PREC_MIXED):
+        v = np.zeros((W, K, s.nstates))
+        with NonbondedEngine(s, precision=prec, windows=W) as e:
+            e.set_solvent_params(sp)
+            e.set_bonded(bt)
+            for w in range(W):
+                e.set_lambda(lams[w], window=w)
+            for k in range(K):
+                e.set_coordinates_dev(frames[:, k])
+                e.make_pair_lists_dev(**CUT)
+                _, EQ, _ = e.compute_dev(sync=True)
+                _, EQb = e.bonded_energies()
+                v[:, k, :] = state_energies(EQ) + EQb.sum(-1)
+        inc[prec] = window_increments(qfep_dg(v, lams, rt)[2])
+    err = np.abs(inc[PREC_MIXED] - inc[PREC_FP64])
+    assert err.max() <= 0.02, err
