@@ -396,6 +396,26 @@ int build_model(qnb_context* c, const qnb_topology* t) {
         lrf_src[i] = d | ((g < t->ncgp_solute ? 1 : 0) << 30);
     }
     TRY(c->upload(&c->d_lrf_src, lrf_src));
+    {   // the same sources grouped by charge group, in group order
+        std::vector<int> gmeta, goff{0}, gat;
+        for (int g = 0; g < t->ncgp; ++g) {
+            int n0 = (int)gat.size(), meta = -1;
+            for (int a = gslot[g]; a < gslot[g + 1]; ++a) {
+                int i = gatom[a];
+                if (lrf_src[i] < 0) continue;
+                meta = lrf_src[i];
+                gat.push_back(i);
+            }
+            if ((int)gat.size() > n0) {
+                gmeta.push_back(meta);
+                goff.push_back((int)gat.size());
+            }
+        }
+        m.nlrf_groups = (int)gmeta.size();
+        TRY(c->upload((int**)&m.lrf_gmeta, gmeta));
+        TRY(c->upload((int**)&m.lrf_goff, goff));
+        TRY(c->upload((int**)&m.lrf_gatom, gat));
+    }
     TRY(c->upload(&c->d_wsw, wsw));
 
     // special solute pairs: excluded (listex + listexlong) and 1-4 (list14 +
@@ -862,6 +882,8 @@ int alloc_state(qnb_context* c) {
         s.efix = c->efix_all + (size_t)kNumE * w;
         TRY(c->alloc(&s.lambda, (size_t)std::max(1, m.S)));
         TRY(c->alloc(&s.lrf, (size_t)std::max(1, m.ncgp) * kLrfLen));
+        if (c->mixed && c->use_lrf)
+            TRY(c->alloc(&s.lrf_part, (size_t)kLrfSplitMax * std::max(1, m.ncgp) * kLrfMoments));
         s.cnt = c->cnt_all + (size_t)C_NUM * w;
         TRY(c->alloc(&s.theta, (size_t)std::max(1, m.nwat)));
         TRY(c->alloc(&s.rkey, (size_t)std::max(1, m.nwat)));
@@ -1040,7 +1062,7 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
             CU(cudaEventRecord(c->ev_fork, c->stream));
             CU(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
             Launch L2{L.m, L.s0, L.ds, L.nwin, c->stream2, L.tu};
-            timed_on(c, c->stream2, K_LRF_BUILD, [&] { launch_lrf_accumulate(L2, cut, c->mixed, c->d_lrf_src); });
+            timed_on(c, c->stream2, K_LRF_BUILD, [&] { nl += launch_lrf_accumulate(L2, cut, c->mixed, c->d_lrf_src); });
             CU(cudaEventRecord(c->ev_join, c->stream2));
         }
         timed(c, K_BUILD, [&] {
@@ -1059,7 +1081,7 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
                 if (c->mixed && (do_qp || do_qw)) launch_clear_fq(L), ++nl;   // atoms may leave the Q lists
             }
         });
-        c->launches += nl + (c->use_lrf ? 1 : 0);
+        c->launches += nl;
         if (c->use_lrf) CU(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
         TRY(check_launch());
         CU(cudaMemcpyAsync(c->counts.data(), c->cnt_all, sizeof(int) * C_NUM * nw, cudaMemcpyDeviceToHost,
@@ -1324,7 +1346,7 @@ int qnb_make_pair_lists_dev(qnb_context* c, double Rq, double Rcq2, double RcLRF
     (void)Rq;
     if (!c) return fail(QNB_ERR_ARG, "null context");
     CU(cudaSetDevice(c->device));
-    Cut cut{Rcq2, RcLRF2, Rcpp2, Rcpw2, Rcww2};
+    Cut cut = make_cut(Rcq2, RcLRF2, Rcpp2, Rcpw2, Rcww2);
     return build_lists(c, cut, c->nwin);
 }
 
@@ -1334,7 +1356,7 @@ int qnb_make_pair_lists(qnb_context* c, const double* x, double Rq, double Rcq2,
     if (!c || !x) return fail(QNB_ERR_ARG, "null argument");
     CU(cudaSetDevice(c->device));
     TRY(stage_x(c, x));
-    Cut cut{Rcq2, RcLRF2, Rcpp2, Rcpw2, Rcww2};
+    Cut cut = make_cut(Rcq2, RcLRF2, Rcpp2, Rcpw2, Rcww2);
     return build_lists(c, cut, 1);
 }
 
@@ -2282,7 +2304,7 @@ int qnb_md_minimize(qnb_context* c, int32_t nsteps, double initial_step, double 
     CU(cudaMemcpy(mw.data(), c->md.win, sizeof(MdWin) * W, cudaMemcpyDeviceToHost));
     for (auto& m : mw) m.min_oldmax = 0.0, m.min_scale = initial_step, m.min_state = 0;
     CU(cudaMemcpy(c->md.win, mw.data(), sizeof(MdWin) * W, cudaMemcpyHostToDevice));
-    Cut cut{p.rcq * p.rcq, p.rclrf * p.rclrf, p.rcpp * p.rcpp, p.rcpw * p.rcpw, p.rcww * p.rcww};
+    Cut cut = make_cut(p.rcq * p.rcq, p.rclrf * p.rclrf, p.rcpp * p.rcpp, p.rcpw * p.rcpw, p.rcww * p.rcww);
     for (int k = 0; k < nsteps; ++k) {
         if (k % p.nbcycle == 0 || !c->lists_built) {
             if (k > 0) TRY(md_fail_check(c));
@@ -2321,7 +2343,7 @@ int qnb_md_run(qnb_context* c, int32_t nsteps, int32_t istep0, qnb_md_record* re
                 if (k0 + k > 0) TRY(md_fail_check(c));   // no list build on coordinates of a failed SHAKE
                 // every NBcycle steps, before the lists (src/md.f90:1663-1671)
                 if (c->m.box && c->md.pb_last_mol > c->md.pb_first_mol) launch_md_put_back(c->all(), c->md), c->launches++;
-                Cut cut{p.rcq * p.rcq, p.rclrf * p.rclrf, p.rcpp * p.rcpp, p.rcpw * p.rcpw, p.rcww * p.rcww};
+                Cut cut = make_cut(p.rcq * p.rcq, p.rclrf * p.rclrf, p.rcpp * p.rcpp, p.rcpw * p.rcpw, p.rcww * p.rcww);
                 TRY(build_lists(c, cut, W));
             }
             Launch L = c->all();

@@ -13,6 +13,8 @@ constexpr int kMaxSolv = 4;     // atoms per solvent molecule handled on device
 constexpr int kMaxStates = 8;   // FEP states
 constexpr int kMaxShell = 16;   // water polarisation shells
 constexpr int kLrfLen = 43;     // cgp_cent(3) phi0 phi1(3) phi2(9) phi3(27)
+constexpr int kLrfMoments = 24; // symmetric moments the LRF accumulation sums per target group
+constexpr int kLrfSplitMax = 8; // source ranges of the mixed form's LRF accumulation
 constexpr double kFix = 4294967296.0;   // 2^32: fixed-point quantum of forces/energies
 constexpr float kFixF = 4294967296.0f;
 
@@ -111,6 +113,14 @@ struct DevModel {
     double xpcent[3], xwcent[3];
     float wcoff[3];             // xpcent - xwcent in FP32: packed (xpcent-centred) coordinates to xwcent-centred
     double rexcl_o2;
+    // LRF sources grouped by charge group (mixed form's accumulation):
+    // groups with LRF-eligible atoms (non-Q atoms of groups whose distance
+    // atom is not excluded), their distance atom | solute flag << 30, and
+    // the offsets of their atoms in lrf_gatom (group-major)
+    int nlrf_groups;
+    const int* lrf_gmeta;       // [nlrf_groups]
+    const int* lrf_goff;        // [nlrf_groups + 1]
+    const int* lrf_gatom;       // [lrf_goff[nlrf_groups]]
     // periodic box (qnb_set_box): rectangular box lengths, their inverses
     // and the Q-list switching atom (FEP file [PBC] switching_atom)
     int box;
@@ -140,6 +150,7 @@ struct DevState {
     unsigned long long* efix;  // [kNumE] fixed-point energies (mixed form)
     double* lambda;      // [S]
     double* lrf;         // [ncgp*43]
+    double* lrf_part;    // mixed form: [kLrfSplitMax][ncgp][kLrfMoments] LRF moments per source range
     int* cnt;            // [C_NUM] list sizes (device-maintained)
     int2* ww; int64_t cap_ww;      // water pairs (iw, jw), iw < jw
     int2* pw; int64_t cap_pw;      // (solute atom, water)
@@ -173,9 +184,26 @@ struct DevState {
 };
 
 // ---- launch wrappers (qnb_kernels.cu) ---------------------------------------
+// FP32 decision band of a squared cut-off c: an FP32 distance below lo is
+// inside, above hi outside, in between the FP64 distance decides.  Computed
+// on the host: a double-to-float conversion in a kernel runs on GB300's
+// narrow FP64 pipe, and under register pressure the compiler may redo it
+// inside a loop.
+struct CutBand {
+    float lo, hi;
+};
+inline CutBand cut_band(double c) {
+    float f = (float)c;
+    return CutBand{f * 0.9998f, f * 1.0002f};
+}
 struct Cut {
     double rcq2, rlrf2, rcpp2, rcpw2, rcww2;
+    CutBand fq, flrf, fpp, fpw, fww;   // cut_band of each, filled by make_cut
 };
+inline Cut make_cut(double rcq2, double rlrf2, double rcpp2, double rcpw2, double rcww2) {
+    return Cut{rcq2, rlrf2, rcpp2, rcpw2, rcww2, cut_band(rcq2), cut_band(rlrf2), cut_band(rcpp2),
+               cut_band(rcpw2), cut_band(rcww2)};
+}
 
 // Every launch covers all nwin windows of a context (grid.y = window); s0 is
 // window 0's host-side state (capacities are equal across windows) and ds the
@@ -205,7 +233,7 @@ void launch_build_pw(const Launch& L, const Cut& c);
 void launch_build_pp(const Launch& L, const Cut& c);
 void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2);
 void launch_build_qw(const Launch& L, const Cut& c);
-void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src);
+int launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src);
 
 void launch_build_rows(const Launch& L, const Cut& c);
 void launch_rows_solute(const Launch& L, int maxg);

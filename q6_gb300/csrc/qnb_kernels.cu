@@ -40,6 +40,15 @@ __device__ __forceinline__ double dist2_exact(double ax, double ay, double az, d
     return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
+// The exact FP64 squared distance of two atoms, out of line: it serves the
+// rare candidates whose FP32 distance falls inside a cut-off's rounding band.
+// Inline, the compiler may evaluate it speculatively for every candidate, and
+// each of its FP64 operations then takes an issue slot of GB300's narrow FP64
+// pipe.
+__device__ __noinline__ double dist2_exact_atoms(const double* __restrict__ x, int a, int b) {
+    return dist2_exact(x[3 * a], x[3 * a + 1], x[3 * a + 2], x[3 * b], x[3 * b + 1], x[3 * b + 2]);
+}
+
 // warp-aggregated append: returns this lane's first slot (valid when n > 0)
 __device__ __forceinline__ int warp_append(int* counter, int n) {
     int lane = threadIdx.x & 31;
@@ -252,6 +261,7 @@ struct Band {
     float lo, hi;   // r2f < lo: inside; r2f > hi: outside
     double c;       // the FP64 threshold
 };
+__device__ __forceinline__ Band band(double c, CutBand b) { return Band{b.lo, b.hi, c}; }
 __device__ __forceinline__ Band band(double c) {
     float f = (float)c;
     return Band{f * 0.9998f, f * 1.0002f, c};
@@ -259,7 +269,7 @@ __device__ __forceinline__ Band band(double c) {
 __device__ __forceinline__ bool within(float r2f, const Band& rc, const double* __restrict__ x, int a, int b) {
     if (r2f < rc.lo) return true;
     if (r2f > rc.hi) return false;
-    return dist2_exact(x[3 * a], x[3 * a + 1], x[3 * a + 2], x[3 * b], x[3 * b + 1], x[3 * b + 2]) <= rc.c;
+    return dist2_exact_atoms(x, a, b) <= rc.c;
 }
 
 // Any-atom group tests (iuse_switch_atom = 0): nbpplis2(_lrf) and
@@ -611,7 +621,7 @@ __device__ __forceinline__ int group_dist_atom(const DevModel& m, int g) {
 //   m[21..23] U(c)    += f2 r2 dr_c
 // with f0 = q/r^3, f1 = 3 f0/r^2, f2 = -f1/r^2.  lrf_expand rebuilds the 40
 // reference coefficients, including its diagonal corrections of phi3.
-constexpr int kLrfMom = 24;
+constexpr int kLrfMom = kLrfMoments;
 template <typename T>
 __device__ __forceinline__ void lrf_terms(T dx, T dy, T dz, T q, T* m) {
     T r2 = dx * dx + dy * dy + dz * dz;
@@ -691,12 +701,55 @@ __device__ __forceinline__ void lrf_expand(const double* m, double* L) {
     P[24] -= U[0]; P[25] -= U[1]; P[26] -= 3.0 * U[2];
 }
 
+// The mixed form's LRF sums with 20 moments: the sums m[10] and m[21..23] of
+// lrf_terms follow from the others, F0 = tr S2 / 3 (f1 r2 = 3 f0) and
+// U(c) = (S3(xxc) + S3(yyc) + S3(zzc)) / 5 (dr_x^2 + dr_y^2 + dr_z^2 = r2), so
+// they are formed in FP64 from the totals instead of summed per atom.
+//   n[0] phi0, n[1..3] phi1, n[4..9] S2, n[10..19] S3 (the order of lrf_terms)
+constexpr int kLrfMom20 = 20;
+__device__ __forceinline__ void lrf_terms20(float dx, float dy, float dz, float q, float* n) {
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float ri = rsqrtf(r2), ri2 = ri * ri;
+    const float qri = q * ri;
+    const float f0 = qri * ri2;
+    const float f1 = 3.f * f0 * ri2;
+    const float g = -5.f * f1 * ri2;   // 5 f2
+    n[0] += qri;                        // f0 r2
+    n[1] -= dx * f0;
+    n[2] -= dy * f0;
+    n[3] -= dz * f0;
+    const float ax = dx * f1, ay = dy * f1, az = dz * f1;
+    n[4] += ax * dx; n[5] += ax * dy; n[6] += ax * dz;
+    n[7] += ay * dy; n[8] += ay * dz; n[9] += az * dz;
+    const float gx = g * dx, gy = g * dy, gz = g * dz;
+    const float gxx = gx * dx, gyy = gy * dy, gzz = gz * dz, gxy = gx * dy;
+    n[10] += gxx * dx;   // xxx
+    n[11] += gxx * dy;   // xxy
+    n[12] += gxx * dz;   // xxz
+    n[13] += gyy * dx;   // xyy
+    n[14] += gxy * dz;   // xyz
+    n[15] += gzz * dx;   // xzz
+    n[16] += gyy * dy;   // yyy
+    n[17] += gyy * dz;   // yyz
+    n[18] += gzz * dy;   // yzz
+    n[19] += gzz * dz;   // zzz
+}
+// the 24 moments of lrf_expand from the 20 (FP64)
+__device__ __forceinline__ void lrf_moments24(const double* n, double* m) {
+    for (int k = 0; k < 10; ++k) m[k] = n[k];
+    m[10] = (n[4] + n[7] + n[9]) / 3.0;
+    for (int k = 0; k < 10; ++k) m[11 + k] = n[10 + k];
+    m[21] = (n[10] + n[13] + n[15]) / 5.0;   // xxx + xyy + xzz
+    m[22] = (n[11] + n[16] + n[18]) / 5.0;   // xxy + yyy + yzz
+    m[23] = (n[12] + n[17] + n[19]) / 5.0;   // xxz + yyz + zzz
+}
+
 // LRF classification of a group pair: true when rc2 < r2 <= rlrf2 in FP64
 __device__ __forceinline__ bool lrf_pair(float r2f, const Band& rc, const Band& rl, const double* __restrict__ x,
                                          int a, int b) {
     if (r2f > rc.hi && r2f < rl.lo) return true;
     if (r2f < rc.lo || r2f > rl.hi) return false;
-    double r2 = dist2_exact(x[3 * a], x[3 * a + 1], x[3 * a + 2], x[3 * b], x[3 * b + 1], x[3 * b + 2]);
+    double r2 = dist2_exact_atoms(x, a, b);
     return r2 > rc.c && r2 <= rl.c;
 }
 
@@ -712,7 +765,8 @@ template <bool MIX>
 __global__ void __launch_bounds__(kLrfBlock) k_lrf_accumulate(DevModel m, const DevState* __restrict__ states, Cut c,
                                                               const int* __restrict__ lrf_src) {
     typedef typename std::conditional<MIX, float, double>::type T;
-    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
+    const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww),
+               blrf = band(c.rlrf2, c.flrf);
     __shared__ float4 s_xs[kLrfBlock];                  // distance atom of the source's group
     __shared__ int s_src[kLrfBlock];                    // lrf_src entry (-1: not a source)
     __shared__ T s_xi[4 * kLrfBlock];                   // source x, y, z (centred in FP32), charge
@@ -794,7 +848,8 @@ __global__ void __launch_bounds__(kLrfBlock) k_lrf_accumulate(DevModel m, const 
 constexpr int kLrfPair = 2;
 __global__ void __launch_bounds__(kLrfBlock) k_lrf_accumulate2(DevModel m, const DevState* __restrict__ states, Cut c,
                                                                const int* __restrict__ lrf_src) {
-    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
+    const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww),
+               blrf = band(c.rlrf2, c.flrf);
     __shared__ float4 s_xs[kLrfBlock];
     __shared__ int s_src[kLrfBlock];
     __shared__ float4 s_xi[kLrfBlock];
@@ -882,12 +937,133 @@ __global__ void __launch_bounds__(kLrfBlock) k_lrf_accumulate2(DevModel m, const
     }
 }
 
+// Mixed form, N-body layout: one thread per target group.  The blocks stage
+// the LRF source groups (the eligible atoms of each charge group, in group
+// order: lrf_gmeta / lrf_goff / lrf_gatom) in shared memory, kLrfGT groups
+// per tile, and every thread reads them as broadcasts.  The group-pair
+// classification runs once per (target, source group); the source group's
+// atoms then add their terms.  Each thread's 20 moment sums (lrf_terms20) run
+// in FP32 over at most kLrfFold source groups and are then folded into a
+// double-float accumulator with Knuth's TwoSum (s = a + b, bb = s - a,
+// e = (a - (s - bb)) + (b - bb)), so the FP32 rounding of the sums is kept
+// to short runs.  The source groups are split into nsplit ranges
+// (blockIdx.z, the split fixed by the topology) whose moments
+// k_lrf_combine adds in range order: each target's order of terms is fixed,
+// so its coefficients do not depend on the launch or the number of windows.
+constexpr int kLrfNB = 64;     // targets per block
+constexpr int kLrfGT = 64;     // source groups per staged tile
+constexpr int kLrfFold = 8;    // source groups per FP32 partial sum
+
+__device__ __forceinline__ void two_sum_fold(float& hi, float& lo, float& p) {
+    float s = __fadd_rn(hi, p);
+    float bb = __fsub_rn(s, hi);
+    float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+    p = 0.f;
+}
+
+__global__ void __launch_bounds__(kLrfNB, 10) k_lrf_nbody(DevModel m, const DevState* __restrict__ states, Cut c,
+                                                          int nsplit) {
+    const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww),
+               blrf = band(c.rlrf2, c.flrf);
+    __shared__ int s_meta[kLrfGT];
+    __shared__ int s_off[kLrfGT + 1];
+    __shared__ float4 s_xs[kLrfGT];
+    __shared__ float4 s_xi[kLrfGT * kMaxGroup];
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    const float4* __restrict__ xq = s.xq;
+    double* __restrict__ lrf = s.lrf;
+    const int g2 = blockIdx.x * kLrfNB + threadIdx.x;
+    int s2 = -1;
+    bool act = g2 < m.ncgp;
+    if (act) {
+        s2 = group_dist_atom(m, g2);
+        act = !m.excl[s2];
+    }
+    const bool sol2 = g2 < m.ncgp_solute;
+    const Band rc_s = sol2 ? bpp : bpw, rc_w = sol2 ? bpw : bww;
+    float ccx = 0.f, ccy = 0.f, ccz = 0.f;
+    float4 x2 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (act) {
+        const double* L = lrf + (size_t)g2 * kLrfLen;
+        ccx = (float)(L[0] - m.xpcent[0]);
+        ccy = (float)(L[1] - m.xpcent[1]);
+        ccz = (float)(L[2] - m.xpcent[2]);
+        x2 = xq[s2];
+    }
+    float part[kLrfMom20], hi[kLrfMom20], lo[kLrfMom20];
+#pragma unroll
+    for (int k = 0; k < kLrfMom20; ++k) part[k] = hi[k] = lo[k] = 0.f;
+    // this block's range of source groups (blockIdx.z of nsplit)
+    const int gbeg = (int)((int64_t)m.nlrf_groups * blockIdx.z / nsplit);
+    const int gend = (int)((int64_t)m.nlrf_groups * (blockIdx.z + 1) / nsplit);
+    for (int t0 = gbeg; t0 < gend; t0 += kLrfGT) {   // block-uniform
+        const int ng = min(kLrfGT, gend - t0);
+        const int a_base = m.lrf_goff[t0];
+        const int na = m.lrf_goff[t0 + ng] - a_base;   // <= kLrfGT * kMaxGroup
+        __syncthreads();   // the previous tile is consumed
+        for (int k = threadIdx.x; k < ng; k += kLrfNB) {
+            int meta = m.lrf_gmeta[t0 + k];
+            s_meta[k] = meta;
+            s_xs[k] = xq[meta & 0x3fffffff];
+            s_off[k] = m.lrf_goff[t0 + k] - a_base;
+        }
+        if (threadIdx.x == 0) s_off[ng] = na;
+        for (int k = threadIdx.x; k < na; k += kLrfNB) s_xi[k] = xq[m.lrf_gatom[a_base + k]];
+        __syncthreads();
+        if (!act) continue;
+        for (int gi = 0; gi < ng; ++gi) {
+            const int meta = s_meta[gi], s1 = meta & 0x3fffffff;
+            if (s1 != s2 && lrf_pair(r2_f(x2, s_xs[gi]), (meta >> 30) ? rc_s : rc_w, blrf, x, s2, s1)) {
+                const int k1 = s_off[gi + 1];
+                for (int k = s_off[gi]; k < k1; ++k) {
+                    const float4 xi = s_xi[k];
+                    lrf_terms20(xi.x - ccx, xi.y - ccy, xi.z - ccz, xi.w, part);
+                }
+            }
+            if ((gi + 1) % kLrfFold == 0 || gi == ng - 1) {
+#pragma unroll
+                for (int k = 0; k < kLrfMom20; ++k) two_sum_fold(hi[k], lo[k], part[k]);
+            }
+        }
+    }
+    if (!act) return;
+    double tot[kLrfMom20];
+#pragma unroll
+    for (int k = 0; k < kLrfMom20; ++k) tot[k] = (double)hi[k] + (double)lo[k];
+    double* out = s.lrf_part + ((size_t)blockIdx.z * m.ncgp + g2) * kLrfMom20;
+#pragma unroll
+    for (int k = 0; k < kLrfMom20; ++k) out[k] = tot[k];
+}
+
+// The source ranges' moments of each target summed in range order, then
+// expanded into the record.
+__global__ void k_lrf_combine(DevModel m, const DevState* __restrict__ states, int nsplit) {
+    const DevState& s = states[blockIdx.y];
+    const int g2 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g2 >= m.ncgp || m.excl[group_dist_atom(m, g2)]) return;
+    double tot[kLrfMom20];
+#pragma unroll
+    for (int k = 0; k < kLrfMom20; ++k) tot[k] = 0.0;
+    for (int z = 0; z < nsplit; ++z) {
+        const double* p = s.lrf_part + ((size_t)z * m.ncgp + g2) * kLrfMom20;
+#pragma unroll
+        for (int k = 0; k < kLrfMom20; ++k) tot[k] += p[k];
+    }
+    double m24[kLrfMom];
+    lrf_moments24(tot, m24);
+    lrf_expand(m24, s.lrf + (size_t)g2 * kLrfLen + 3);
+}
+
 // Unstaged variant: one warp per target group reads the source atoms straight
 // from global memory (lanes stride over the atoms, so loads are coalesced).
 template <bool MIX>
 __global__ void __launch_bounds__(128) k_lrf_accumulate_direct(DevModel m, const DevState* __restrict__ states, Cut c,
                                                          const int* __restrict__ lrf_src) {
-    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
+    const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww),
+               blrf = band(c.rlrf2, c.flrf);
     typedef typename std::conditional<MIX, float, double>::type T;
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
@@ -943,7 +1119,8 @@ __device__ __forceinline__ int group_last_atom(const DevModel& m, int g) {
 }
 template <bool MIX>
 __global__ void __launch_bounds__(128) k_lrf_accumulate_any(DevModel m, const DevState* __restrict__ states, Cut c) {
-    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
+    const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww),
+               blrf = band(c.rlrf2, c.flrf);
     typedef typename std::conditional<MIX, float, double>::type T;
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
@@ -2286,7 +2463,8 @@ __device__ __forceinline__ int row_append(int* __restrict__ row, int cap, int co
 // 2842-2955, 4274-4395) stored from both sides.  Rows 0..ncgp_solute-1 are
 // solute groups, the next nwat rows waters; one warp per row.
 __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cut c) {
-    const Band bpp = band(c.rcpp2), bpw = band(c.rcpw2), bww = band(c.rcww2), blrf = band(c.rlrf2);
+    const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww),
+               blrf = band(c.rlrf2, c.flrf);
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
     const float4* __restrict__ xq = s.xq;
@@ -2838,12 +3016,12 @@ void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2) {
     if (L.m.ncgp_solute == 0 || L.m.nqat == 0) return;
     k_build_qp<<<dim3(1, L.nwin), 1024, 0, L.st>>>(L.m, L.ds, qnear, rcq2);
 }
-void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src) {
+int launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src) {
     if (L.m.any_atom) {
         dim3 g = grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin);
         if (mixed) k_lrf_accumulate_any<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
         else k_lrf_accumulate_any<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
-        return;
+        return 1;
     }
 // FP64 form: the unstaged kernel measured faster (its FP64 terms, not the
 // loads, bound it, and the staged block holds more registers)
@@ -2853,13 +3031,27 @@ void launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* 
 #ifndef QNB_LRF_PAIR
 #define QNB_LRF_PAIR 1   // mixed form: two target groups per warp (k_lrf_accumulate2)
 #endif
+#ifndef QNB_LRF_NBODY
+#define QNB_LRF_NBODY 1  // mixed form: one thread per target group (k_lrf_nbody)
+#endif
     dim3 g = grid_for((int64_t)L.m.ncgp * 32, kLrfBlock, L.tu.v[T_LRF], L.nwin);
-    if (mixed && QNB_LRF_PAIR)
+    if (mixed && QNB_LRF_NBODY) {
+        // source ranges of at least one staged tile each; the split depends on
+        // the topology only, so a window's coefficients are the same in a
+        // batch of any size (51 windows of a 1,400-source-group system:
+        // 8 ranges, about 9 waves of resident target threads)
+        const int nsplit = std::min(kLrfSplitMax, std::max(1, L.m.nlrf_groups / kLrfGT));
+        dim3 g((L.m.ncgp + kLrfNB - 1) / kLrfNB, L.nwin, nsplit);
+        k_lrf_nbody<<<g, kLrfNB, 0, L.st>>>(L.m, L.ds, c, nsplit);
+        k_lrf_combine<<<dim3((L.m.ncgp + 127) / 128, L.nwin), 128, 0, L.st>>>(L.m, L.ds, nsplit);
+        return 2;
+    } else if (mixed && QNB_LRF_PAIR)
         k_lrf_accumulate2<<<grid_for((int64_t)L.m.ncgp * 32 / kLrfPair, kLrfBlock, L.tu.v[T_LRF], L.nwin), kLrfBlock, 0,
                             L.st>>>(L.m, L.ds, c, lrf_src);
     else if (mixed) k_lrf_accumulate<true><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
     else if (QNB_LRF_FP64_STAGED) k_lrf_accumulate<false><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
     else k_lrf_accumulate_direct<false><<<grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
+    return 1;
 }
 
 void launch_build_rows(const Launch& L, const Cut& c) {

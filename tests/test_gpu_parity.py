@@ -88,7 +88,9 @@ def test_lrf_records_match(name):
     o = Oracle(s)
     o.make_pair_lists(s.x, **CUT)
     L0 = o.lrf()
-    for prec, rel in ((PREC_FP64, 1e-10), (PREC_MIXED, 1e-3)):
+    # mixed form: FP32 terms, sums folded into double-float accumulators
+    # every few source groups (measured within 7e-6 of each coefficient's scale)
+    for prec, rel in ((PREC_FP64, 1e-10), (PREC_MIXED, 2e-5)):
         with NonbondedEngine(s, precision=prec) as eng:
             eng.make_pair_lists(s.x, **CUT)
             L = eng.lrf()
