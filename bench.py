@@ -33,8 +33,9 @@ sys.path.insert(0, ROOT)
 NBCYCLE = 25
 CUT = dict(Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
 METRIC = "MD steps/s summed over lambda windows (nonbonded hot path, mixed precision)"
-DTYPE_MIXED = ("f32 pair math; f64 cut-off decisions, group centres, LRF Taylor terms and energy records; "
-               "row-atom gradients f32 warp sums, shared-atom gradients and Q energies u64 fixed point")
+DTYPE_MIXED = ("f32 pair math; gradients accumulated in u64 fixed point (a row atom's f32 warp sum converted once "
+               "per atom and component); f64 cut-off decisions, group centres, LRF Taylor terms and energy records; "
+               "LRF coefficients from f32 terms in double-float sums")
 # algorithmic FP32 flops per unit (FMA = 2, rsqrt/rcp = 1)
 FLOPS = {"pp_atom_pair": 33, "ww_mol_pair": 209, "pw_atom_water": 77}
 

@@ -491,7 +491,12 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                         t->bvdw[b * 3 + k], &A, &B);
                 size_t o = ((size_t)k * nt + a) * nt + b;
                 lj[o] = make_double2(A, B);
-                ljf[o] = make_float2((float)A, (float)B);
+                // geometric rule: the FP32 product of the FP32 factors, which
+                // the plain partners of the solute rows form in the kernel
+                ljf[o] = t->ivdw_rule == 1
+                             ? make_float2((float)t->avdw[a * 3 + k] * (float)t->avdw[b * 3 + k],
+                                           (float)t->bvdw[a * 3 + k] * (float)t->bvdw[b * 3 + k])
+                             : make_float2((float)A, (float)B);
                 ljset[o] = (fabs(A) > kQrealEps || fabs(B) > kQrealEps) ? 1 : 0;
             }
     for (auto v : ljcod)
@@ -504,6 +509,27 @@ int build_model(qnb_context* c, const qnb_topology* t) {
             ljpair[(size_t)a * nt + b] = make_float4(p1.x, p1.y, p3.x, p3.y);
         }
     TRY(c->upload((float4**)&m.ljpair, ljpair));
+    {   // plain solute partners (see DevModel::gtmask)
+        m.geom = t->ivdw_rule == 1 ? 1 : 0;
+        std::vector<unsigned long long> gtm(std::max(1, t->ncgp_solute), 0ull);
+        for (int g = 0; g < t->ncgp_solute; ++g) {
+            if (nt > 64) {
+                gtm[g] = ~0ull;
+                continue;
+            }
+            for (int a = gslot[g]; a < gslot[g + 1]; ++a) {
+                int i = gatom[a];
+                if (iqatom[i] >= 0) continue;
+                for (int b = 0; b < nt; ++b)
+                    if (t->ljcod[t->iac[i] * nt + b] != 1) gtm[g] |= 1ull << b;
+            }
+        }
+        std::vector<float2> f1(std::max(1, natom));
+        for (int i = 0; i < natom; ++i)
+            f1[i] = make_float2((float)t->avdw[t->iac[i] * 3], (float)t->bvdw[t->iac[i] * 3]);
+        TRY(c->upload((unsigned long long**)&m.gtmask, gtm));
+        TRY(c->upload((float2**)&m.ljf1, f1));
+    }
     TRY(c->upload((double2**)&m.lj, lj));
     TRY(c->upload((float2**)&m.ljf, ljf));
     TRY(c->upload((uint8_t**)&m.ljset, ljset));
@@ -907,11 +933,14 @@ int alloc_state(qnb_context* c) {
         TRY(ensure_cap(c, &s.qp, &s.cap_qp, std::max<int64_t>(1024, (int64_t)m.nat_solute)));
         TRY(ensure_cap(c, &s.qw, &s.cap_qw, std::max<int64_t>(1024, (int64_t)m.nwat)));
         if (c->mixed) {
-            s.cap_gp = 1024;
+            s.cap_gp = 256;
+            s.cap_gf = 1024;
             s.cap_gw = 256;
             s.cap_rww = 256;
             s.cap_wg = 192;
             TRY(c->alloc(&s.row_gp, (size_t)std::max(1, m.ncgp_solute) * s.cap_gp));
+            TRY(c->alloc(&s.row_gf, (size_t)std::max(1, m.ncgp_solute) * s.cap_gf));
+            TRY(c->alloc(&s.cnt_gf, (size_t)std::max(1, m.ncgp_solute)));
             TRY(c->alloc(&s.row_gw, (size_t)std::max(1, m.ncgp_solute) * s.cap_gw));
             TRY(c->alloc(&s.row_ww, (size_t)std::max(1, m.nwat) * s.cap_rww));
             TRY(c->alloc(&s.row_wg, (size_t)std::max(1, m.nwat) * s.cap_wg));
@@ -1020,7 +1049,7 @@ int grow_lists(qnb_context* c, bool* grew, bool* do_qp, bool* do_qw) {
                 s.cap_gp = cap;
                 *grew = true;
             }
-            R rs[] = {{C_RGW, &s.cap_gw, &s.row_gw, c->ncgp_solute},
+            R rs[] = {{C_RGF, &s.cap_gf, &s.row_gf, c->ncgp_solute}, {C_RGW, &s.cap_gw, &s.row_gw, c->ncgp_solute},
                       {C_RWW, &s.cap_rww, &s.row_ww, c->nwat}, {C_RWG, &s.cap_wg, &s.row_wg, c->nwat}};
             for (auto& r : rs) {
                 if (need[r.k] <= *r.cap) continue;

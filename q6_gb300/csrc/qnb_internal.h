@@ -35,7 +35,7 @@ constexpr int kNumE = E_QR0 + kMaxStates;
 
 // list counters (entries at list granularity, plus reference atom-pair counts)
 enum { C_WW = 0, C_PW, C_PP, C_QP, C_QW, C_PP14, C_PPG,
-       C_RGP, C_RGW, C_RWW, C_RWG,   // longest row seen (mixed-form row lists)
+       C_RGP, C_RGW, C_RWW, C_RWG, C_RGF,   // longest row seen (mixed-form row lists)
        C_NUM };
 
 constexpr int kMaxGroup = 15;   // atoms per solute charge group handled on device
@@ -113,6 +113,14 @@ struct DevModel {
     double xpcent[3], xwcent[3];
     float wcoff[3];             // xpcent - xwcent in FP32: packed (xpcent-centred) coordinates to xwcent-centred
     double rexcl_o2;
+    // plain solute partners of the mixed form's solute rows: per solute group
+    // the partner types that need the general pair path (some non-Q atom of
+    // the group has LJ code 2 with them; all bits set when there are more
+    // than 64 types), and per atom its code-1 LJ factors in FP32 (geometric
+    // rule: A = a_i a_j, B = b_i b_j)
+    int geom;
+    const unsigned long long* gtmask;   // [ncgp_solute]
+    const float2* ljf1;                 // [natom]
     // LRF sources grouped by charge group (mixed form's accumulation):
     // groups with LRF-eligible atoms (non-Q atoms of groups whose distance
     // atom is not excluded), their distance atom | solute flag << 30, and
@@ -142,7 +150,7 @@ struct DevState {
     const double* md_tfree;   // Tfree of the window's last MD temperature() (null before qnb_md_init)
     double* d;           // [natom*3] gradient accumulator (FP64 mode target)
     float4* xq;          // [natom] FP32 (x,y,z,charge) for the mixed form
-    float* frow;         // [natom*3] mixed form: row-kernel gradient of each atom's own row (FP32)
+    float* frow;         // [natom*3] mixed form: row-kernel gradient of each atom's own row (FP32 warp sum)
     float4* erow;        // [ncgp_solute+nwat] mixed form: row energies (pp el, vdw, pw el, vdw | ww el, vdw)
     float* fq;           // [natom*3] mixed form: Q-environment gradient of each listed qp atom / qw water
     unsigned long long* fix;   // [natom*3] fixed-point gradient (mixed form)
@@ -160,7 +168,9 @@ struct DevState {
     int* qw;  int64_t cap_qw;      // waters interacting with all Q atoms
     // mixed form: gather rows (ELL, fixed capacity per row); row r of list X
     // holds partners at X[r*cap_X .. r*cap_X + cnt_X[r])
-    uint2* row_gp; int* cnt_gp; int cap_gp; // solute group -> solute atoms: {j | flags, 2-bit kind per row atom}
+    uint2* row_gp; int* cnt_gp; int cap_gp; // solute group -> solute atoms needing the general pair path:
+                                            // {j | flags, 2-bit kind per row atom}
+    int* row_gf; int* cnt_gf; int cap_gf;   // solute group -> plain solute partners (code 1 with every row atom)
     int* row_gw; int* cnt_gw; int cap_gw;   // solute group -> waters
     int* row_ww; int* cnt_ww; int cap_rww;  // water -> waters
     int* row_wg; int* cnt_wg; int cap_wg;   // water -> solute groups

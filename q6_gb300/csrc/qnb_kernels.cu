@@ -1954,8 +1954,12 @@ __global__ void k_apply_fixed(int n, const DevState* __restrict__ states, int ro
     double* __restrict__ d = states[blockIdx.y].d;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         long long v = (long long)fix[k];
+        // a row atom's gradient (its row's FP32 sum) is converted once to 64-bit
+        // fixed point and joins the atom's other fixed-point contributions as
+        // an integer (exact, order-free); the conversion is done here rather
+        // than in the row kernels, whose main loops it slowed by 15-24 %
+        if (rows) v += (long long)to_fix(frow[k]);
         double add = (double)v * (1.0 / kFix);
-        if (rows) add += (double)frow[k];
         if (qenv) add += (double)fq[k];
         if (add != 0.0) d[k] += add;
         if (v != 0) fix[k] = 0ull;
@@ -2473,40 +2477,58 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
     for (int r = warp_id_global(); r < nrows; r += warps_total()) {
         if (r < m.ncgp_solute) {
             int g = r, is = m.gsw[g];
-            int npp = 0, npw = 0;
+            int npp = 0, npf = 0, npw = 0;
             if (!m.excl[is]) {
                 int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
+                const unsigned long long tmask = m.gtmask[g];
                 uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
+                int* rf = s.row_gf + (size_t)g * s.cap_gf;
                 for (int j0 = 0; j0 < m.ncgp_solute; j0 += kWarp) {
                     int g2 = j0 + lane;
                     bool ok = false;
-                    int b0 = 0, n2 = 0, nq = 0;
+                    int b0 = 0, n2 = 0, ns = 0, nf = 0, sgi = -1;
                     if (g2 < m.ncgp_solute) {
                         int s2 = m.gsw[g2];
                         if (!m.excl[s2]) ok = (g2 == g) || gg_inside(m, x, xq, g, g2, bpp);
                         if (ok) {
                             b0 = m.gslot[g2];
                             n2 = m.gslot[g2 + 1] - b0;
-                            for (int b = 0; b < n2; ++b) nq += (m.iqatom[m.gatom[b0 + b]] < 0);
+                            sgi = m.nsg ? sg_find(m, g <= g2 ? (long long)g * m.ncgp_solute + g2
+                                                             : (long long)g2 * m.ncgp_solute + g) : -1;
+                            // the general path: the group itself, group pairs with
+                            // excluded / 1-4 atom pairs, and partner types with LJ
+                            // code 2 against a row atom; plain code-1 partners otherwise
+                            const bool all_special = g2 == g || sgi >= 0;
+                            for (int b = 0; b < n2; ++b) {
+                                int j = m.gatom[b0 + b];
+                                if (m.iqatom[j] >= 0) continue;
+                                if (all_special || ((tmask >> m.iac[j]) & 1ull)) ++ns;
+                                else ++nf;
+                            }
                         }
                     }
-                    // row-local offsets: inclusive warp scan of the emitted counts
-                    int incl = nq;
+                    // row-local offsets of both lists: one inclusive warp scan of the
+                    // packed counts (each below 2^15 per lane, at most 15 * 32 per warp)
+                    int incl = ns | (nf << 16);
 #pragma unroll
                     for (int o = 1; o < 32; o <<= 1) {
                         int v = __shfl_up_sync(kFull, incl, o);
                         if (lane >= o) incl += v;
                     }
                     int total = __shfl_sync(kFull, incl, 31);
-                    if (nq > 0) {
-                        int pos = npp + incl - nq;
-                        bool lower = g <= g2;
-                        int sgi = m.nsg ? sg_find(m, lower ? (long long)g * m.ncgp_solute + g2
-                                                           : (long long)g2 * m.ncgp_solute + g) : -1;
+                    if (ns + nf > 0) {
+                        int ps = npp + (incl & 0xffff) - ns, pf = npf + (incl >> 16) - nf;
+                        const bool lower = g <= g2;
+                        const bool all_special = g2 == g || sgi >= 0;
                         unsigned flags = (g < g2 ? 1u : 0u) | (g == g2 ? 2u : 0u);
                         for (int b = 0; b < n2; ++b) {
                             int j = m.gatom[b0 + b];
                             if (m.iqatom[j] >= 0) continue;
+                            if (!all_special && !((tmask >> m.iac[j]) & 1ull)) {
+                                if (pf < s.cap_gf) rf[pf] = j;
+                                ++pf;
+                                continue;
+                            }
                             unsigned mask = 0;
                             for (int a = 0; a < n1; ++a) {
                                 int i = m.gatom[a0 + a];
@@ -2519,11 +2541,12 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                                 mask |= (unsigned)kind << (2 * a);
                             }
                             if (m.type_in_entry) mask |= (unsigned)m.iac[j] << 16;
-                            if (pos < s.cap_gp) rp[pos] = make_uint2((unsigned)j | (flags << 28), mask);
-                            ++pos;
+                            if (ps < s.cap_gp) rp[ps] = make_uint2((unsigned)j | (flags << 28), mask);
+                            ++ps;
                         }
                     }
-                    npp += total;
+                    npp += total & 0xffff;
+                    npf += total >> 16;
                 }
                 int* rw = s.row_gw + (size_t)g * s.cap_gw;
                 for (int j0 = 0; j0 < m.nwat; j0 += kWarp) {
@@ -2538,8 +2561,10 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
             }
             if (lane == 0) {
                 s.cnt_gp[g] = min(npp, s.cap_gp);
+                s.cnt_gf[g] = min(npf, s.cap_gf);
                 s.cnt_gw[g] = min(npw, s.cap_gw);
                 atomicMax(s.cnt + C_RGP, npp);
+                atomicMax(s.cnt + C_RGF, npf);
                 atomicMax(s.cnt + C_RGW, npw);
             }
         } else {
@@ -2678,10 +2703,11 @@ template <int MAXG>
 constexpr int rows_min_blocks() {
     return QNB_ROWS_MIN_BLOCKS ? QNB_ROWS_MIN_BLOCKS : (MAXG <= 6 ? 6 : (MAXG <= 8 ? 4 : 1));
 }
-template <int MAXG>
+template <int MAXG, bool GEOM>
 __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(DevModel m, const DevState* __restrict__ states) {
     extern __shared__ float4 sh_lj[];   // natyps^2 type-pair table (dynamic: only its real size)
-    __shared__ __align__(16) uint2 sh_pp[4][2][kRowChunk];   // per warp: double-buffered pp entries
+    __shared__ __align__(16) uint2 sh_pp[4][2][kRowChunk];   // per warp: double-buffered special pp entries
+    __shared__ __align__(16) int sh_pf[4][2][kRowChunk];     // per warp: double-buffered plain pp entries
     __shared__ __align__(16) int sh_pw[4][kRowChunk];        // per warp: first chunk of pw entries
     constexpr bool kTypeInEntry = MAXG <= 8;
     const DevState& s = states[blockIdx.y];
@@ -2717,15 +2743,23 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
         // per-row FP32 energy sums of this lane, converted to fixed point once
         // per row (row contents do not depend on the grid, so neither do they)
         float rpel = 0.f, rpvdw = 0.f, rwel = 0.f, rwvdw = 0.f;
-        // ---- solute partner atoms (nonbond_pp, src/nonbondene.f90:4694-4760)
+        // ---- solute partner atoms (nonbond_pp, src/nonbondene.f90:4694-4760):
+        // the special entries (kinds, any LJ code) first, then the plain ones
         const uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
+        const int* rf = s.row_gf + (size_t)g * s.cap_gf;
         const int* rw = s.row_gw + (size_t)g * s.cap_gw;
-        const int nchunk = (npp + kRowChunk - 1) / kRowChunk;
+        const int npf = s.cnt_gf[g];
+        const int nchunk = (npp + kRowChunk - 1) / kRowChunk, nfchunk = (npf + kRowChunk - 1) / kRowChunk;
         auto fetch_pp = [&](int ch) {
             int e0 = ch * kRowChunk, units = (min(kRowChunk, npp - e0) + 1) >> 1;
             for (int u = lane; u < units; u += kWarp) cp_async16(&sh_pp[wib][ch & 1][2 * u], rp + e0 + 2 * u);
         };
+        auto fetch_pf = [&](int ch) {
+            int e0 = ch * kRowChunk, units = (min(kRowChunk, npf - e0) + 3) >> 2;
+            for (int u = lane; u < units; u += kWarp) cp_async16(&sh_pf[wib][ch & 1][4 * u], rf + e0 + 4 * u);
+        };
         if (nchunk > 0) fetch_pp(0);
+        if (nfchunk > 0) fetch_pf(0);
         for (int u = lane; u < (min(kRowChunk, npw) + 3) >> 2; u += kWarp) cp_async16(&sh_pw[wib][4 * u], rw + 4 * u);
         cp_async_commit();
         for (int ch = 0; ch < nchunk; ++ch) {
@@ -2766,6 +2800,56 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
         if (nchunk == 0) {
             cp_async_wait<0>();
             __syncwarp();
+        }
+        // plain partners: LJ code 1 with every row atom, no excluded or 1-4
+        // pair; with the geometric rule A and B are the products of the atoms'
+        // FP32 code-1 factors (the type table holds the same products)
+        {
+          float fa[MAXG], fb[MAXG];
+#pragma unroll
+          for (int a = 0; a < MAXG; ++a) {
+              float2 f1 = (GEOM && a < n1) ? m.ljf1[m.gatom[a0 + a]] : make_float2(0.f, 0.f);
+              fa[a] = f1.x;
+              fb[a] = f1.y;
+          }
+          for (int ch = 0; ch < nfchunk; ++ch) {
+            if (ch + 1 < nfchunk) {   // chunk 0 came with the first group
+                fetch_pf(ch + 1);
+                cp_async_commit();
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncwarp();
+            const int* buf = sh_pf[wib][ch & 1];
+            const int n = min(kRowChunk, npf - ch * kRowChunk);
+            for (int k = lane; k < n; k += kWarp) {
+              const int j = buf[k];
+              const float4 xb = xq[j];
+              float2 fj = make_float2(0.f, 0.f);
+              int tj = 0;
+              if constexpr (GEOM) fj = m.ljf1[j];
+              else tj = m.iac[j];
+#pragma unroll
+              for (int a = 0; a < MAXG; ++a) {
+                  if (qa[a]) continue;
+                  float A, B;
+                  if constexpr (GEOM) {
+                      A = fa[a] * fj.x;
+                      B = fb[a] * fj.y;
+                  } else {
+                      float4 p = lj(ta[a], tj);
+                      A = p.x;
+                      B = p.y;
+                  }
+                  float vel, vdw;
+                  pair_f(xa[a], xb, A, B, xa[a].w * xb.w, true, f[a][0], f[a][1], f[a][2], vel, vdw);
+                  rpel += vel;
+                  rpvdw += vdw;
+              }
+            }
+            __syncwarp();   // this buffer is refilled two chunks later
+          }
         }
         // ---- water partners (nonbond_pw, src/nonbondene.f90:4856-4916); energy counted here
         if (m.sa == 3 && m.wlj_mask == 1u) {   // SPC: O with LJ, two LJ-free H; the molecule loaded at once
@@ -2816,8 +2900,9 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
         }
         __syncwarp();   // sh_pw is refilled by the next row
         // The row owns its atoms' pp and pw gradient and its energies: FP32
-        // warp sums in a fixed shuffle order, stored without atomics or
-        // conversions (k_apply_fixed and k_row_sums add them in FP64)
+        // warp sums in a fixed shuffle order, stored without atomics
+        // (k_apply_fixed converts each atom's sum once to 64-bit fixed point
+        // and adds it as an integer; k_row_sums adds the energies in FP64)
         float e0 = warp_sum(0.5f * rpel), e1 = warp_sum(0.5f * rpvdw), e2 = warp_sum(rwel), e3 = warp_sum(rwvdw);
         if (lane == 0) s.erow[g] = make_float4(e0, e1, e2, e3);
 #pragma unroll
@@ -3066,10 +3151,14 @@ void launch_rows_solute(const Launch& L, int maxg) {
     if (L.m.ncgp_solute == 0) return;
     dim3 g = grid_for((int64_t)L.m.ncgp_solute * 32, 128, L.tu.v[T_ROWS_SOLUTE], L.nwin);
     int sm = lj_smem(L.m);
-    if (maxg <= 4) k_rows_solute<4><<<g, 128, sm, L.st>>>(L.m, L.ds);
-    else if (maxg <= 6) k_rows_solute<6><<<g, 128, sm, L.st>>>(L.m, L.ds);
-    else if (maxg <= 8) k_rows_solute<8><<<g, 128, sm, L.st>>>(L.m, L.ds);
-    else k_rows_solute<16><<<g, 128, sm, L.st>>>(L.m, L.ds);
+#define RS(MG, GE) k_rows_solute<MG, GE><<<g, 128, sm, L.st>>>(L.m, L.ds)
+    if (L.m.geom) {
+        if (maxg <= 4) RS(4, true); else if (maxg <= 6) RS(6, true); else if (maxg <= 8) RS(8, true); else RS(16, true);
+    } else {
+        if (maxg <= 4) RS(4, false); else if (maxg <= 6) RS(6, false); else if (maxg <= 8) RS(8, false);
+        else RS(16, false);
+    }
+#undef RS
 }
 void launch_solvent_internal(const Launch& L, const int2* ij, const double* par, int n, int mixed) {
     if (L.m.nwat == 0 || n == 0) return;
