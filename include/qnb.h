@@ -239,6 +239,23 @@ int qnb_list_size(qnb_context* ctx, int32_t kind, int64_t* n);
 int qnb_export_pairs(qnb_context* ctx, int32_t kind, int32_t* i, int32_t* j,
                      int64_t cap, int64_t* n);
 
+/* Gather rows of the mixed form's last list build (QNB_PREC_MIXED only).
+   Every listed solute group / water owns a row of partners, so each pair
+   within a cut-off appears in the rows of both sides:
+     QNB_ROWS_GP  solute group g -> solute atom j of a partner group (the
+                  group itself included; Q atoms left out)
+     QNB_ROWS_GW  solute group g -> water w     (nbpwlist selection)
+     QNB_ROWS_WW  water w -> water v            (nbwwlist selection)
+     QNB_ROWS_WG  water w -> solute group g     (nbpwlist selection)
+   Writes window win's (row, partner) entries into row/partner (capacity
+   cap); *n receives the count.  QNB_ERR_CAPACITY if cap < count.  Replaces
+   no reference interface: it exposes the rows the selections of
+   src/nonbondene.f90 (nbpplist 1777, nbpwlist 2842, nbwwlist 4274) are
+   stored in here, so tests can compare them with those lists as sets. */
+enum { QNB_ROWS_GP = 0, QNB_ROWS_GW = 1, QNB_ROWS_WW = 2, QNB_ROWS_WG = 3 };
+int qnb_export_rows(qnb_context* ctx, int32_t win, int32_t kind, int32_t* row,
+                    int32_t* partner, int64_t cap, int64_t* n);
+
 /* LRF records as 43 doubles per charge group in the order of LRF_TYPE
    (src/globals.f90:503-509): cgp_cent(3), phi0, phi1(3), phi2(9), phi3(27). */
 int qnb_get_lrf(qnb_context* ctx, double* lrf);

@@ -949,6 +949,14 @@ int alloc_state(qnb_context* c) {
             TRY(c->alloc(&s.cnt_ww, (size_t)std::max(1, m.nwat)));
             TRY(c->alloc(&s.cnt_wg, (size_t)std::max(1, m.nwat)));
             TRY(c->alloc(&s.x_build, n3));
+            if (!m.any_atom) {
+                s.cap_cells = kCellCap;
+                TRY(c->alloc(&s.grid, (size_t)1));
+                TRY(c->alloc(&s.cend_s, (size_t)s.cap_cells));
+                TRY(c->alloc(&s.cend_w, (size_t)s.cap_cells));
+                TRY(c->alloc(&s.bin_s, (size_t)std::max(1, m.ncgp_solute)));
+                TRY(c->alloc(&s.bin_w, (size_t)std::max(1, m.nwat)));
+            }
         }
         s.qq = c->st_qq;
         s.qqf = c->st_qqf;
@@ -1098,7 +1106,7 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
             if (c->m.box) {
                 launch_build_box(L, cut, c->d_qnear), nl += 3;
             } else if (c->mixed) {
-                launch_build_rows(L, cut), ++nl;
+                nl += launch_build_rows(L, cut);
             } else {
                 launch_build_pp(L, cut), nl += 2;
                 launch_build_pw(L, cut), ++nl;
@@ -1539,6 +1547,50 @@ int qnb_export_pairs(qnb_context* c, int32_t kind, int32_t* i, int32_t* j, int64
     cudaFree(dj);
     cudaFree(dc);
     return rc;
+}
+
+int qnb_export_rows(qnb_context* c, int32_t win, int32_t kind, int32_t* row, int32_t* partner, int64_t cap,
+                    int64_t* n) {
+    if (!c || !n) return fail(QNB_ERR_ARG, "null argument");
+    if (!c->mixed) return fail(QNB_ERR_ARG, "rows exist in the mixed form only");
+    if (win < 0 || win >= c->nwin) return fail(QNB_ERR_ARG, "window %d", win);
+    if (kind < QNB_ROWS_GP || kind > QNB_ROWS_WG) return fail(QNB_ERR_ARG, "row kind %d", kind);
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    const DevState& s = c->st[win];
+    const bool solute = kind == QNB_ROWS_GP || kind == QNB_ROWS_GW;
+    const int nrows = solute ? c->m.ncgp_solute : c->m.nwat;
+    // (count array, entry array, capacity, entry stride in ints, id mask) of each part
+    struct Part { const int* cnt; const int* rows; int cap; int stride; unsigned mask; };
+    std::vector<Part> parts;
+    if (kind == QNB_ROWS_GP) {
+        parts.push_back({s.cnt_gp, reinterpret_cast<const int*>(s.row_gp), s.cap_gp, 2, 0x0fffffffu});
+        parts.push_back({s.cnt_gf, s.row_gf, s.cap_gf, 1, 0xffffffffu});
+    } else if (kind == QNB_ROWS_GW) {
+        parts.push_back({s.cnt_gw, s.row_gw, s.cap_gw, 1, 0xffffffffu});
+    } else if (kind == QNB_ROWS_WW) {
+        parts.push_back({s.cnt_ww, s.row_ww, s.cap_rww, 1, 0xffffffffu});
+    } else {
+        parts.push_back({s.cnt_wg, s.row_wg, s.cap_wg, 1, 0xffffffffu});
+    }
+    std::vector<int32_t> ri, pj;
+    for (const Part& p : parts) {
+        if (nrows == 0 || !p.cnt || !p.rows) continue;
+        std::vector<int> cnt(nrows), ent((size_t)nrows * p.cap * p.stride);
+        CU(cudaMemcpy(cnt.data(), p.cnt, sizeof(int) * nrows, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(ent.data(), p.rows, sizeof(int) * ent.size(), cudaMemcpyDeviceToHost));
+        for (int r = 0; r < nrows; ++r)
+            for (int k = 0; k < cnt[r]; ++k) {
+                ri.push_back(r);
+                pj.push_back((int32_t)((unsigned)ent[((size_t)r * p.cap + k) * p.stride] & p.mask));
+            }
+    }
+    *n = (int64_t)ri.size();
+    if (*n > cap) return fail(QNB_ERR_CAPACITY, "export needs %lld entries", (long long)*n);
+    if (*n && (!row || !partner)) return fail(QNB_ERR_ARG, "null output");
+    std::copy(ri.begin(), ri.end(), row);
+    std::copy(pj.begin(), pj.end(), partner);
+    return QNB_OK;
 }
 
 int qnb_get_lrf(qnb_context* c, double* lrf) {

@@ -144,6 +144,16 @@ struct QQEntry {   // static Q-Q / Q-bonded-P pair of one state
 };
 
 
+// Geometry of a window's cell grid: cell (ix, iy, iz) of a point p holds
+// ix = clamp(trunc((p.x - lo.x) * inv_h), 0, nx - 1), likewise y and z; cell
+// index (iz * ny + iy) * nx + ix.  1 / inv_h is at least half the largest
+// cut-off plus a margin, so the partners of an atom lie within +-2 cells.
+struct CellGrid {
+    float lox, loy, loz, inv_h;
+    int nx, ny, nz, ncell;
+};
+constexpr int kCellCap = 32768;   // cells per window; a larger extent gets larger cells
+
 // Per-context device state of the lists, coordinates and accumulators.
 struct DevState {
     double* x;           // [natom*3] coordinates (FP64, as qdyn holds them)
@@ -174,6 +184,12 @@ struct DevState {
     int* row_gw; int* cnt_gw; int cap_gw;   // solute group -> waters
     int* row_ww; int* cnt_ww; int cap_rww;  // water -> waters
     int* row_wg; int* cnt_wg; int cap_wg;   // water -> solute groups
+    // mixed form, switch-atom cut-offs: the cell grid of the row build.  The
+    // non-excluded group switch atoms (bin_s) and water oxygens (bin_w) are
+    // binned on one uniform grid; cell c holds bin_X[c ? cend_X[c-1] : 0 ..
+    // cend_X[c]) in ascending index order, each entry the atom's FP32
+    // position with the group or water index in w
+    CellGrid* grid; int* cend_s; int* cend_w; float4* bin_s; float4* bin_w; int cap_cells;
     double* x_build;                        // coordinates of the last list build
     QQEntry* qq; int nqq;          // static qq + qqp entries (all states)
     const float4* qqf;   // the entries' (A, B, el, sc) in FP32 (mixed form)
@@ -245,7 +261,7 @@ void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2);
 void launch_build_qw(const Launch& L, const Cut& c);
 int launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src);
 
-void launch_build_rows(const Launch& L, const Cut& c);
+int launch_build_rows(const Launch& L, const Cut& c);
 void launch_rows_solute(const Launch& L, int maxg);
 void launch_rows_water(const Launch& L);
 void launch_ww(const Launch& L, int mixed);

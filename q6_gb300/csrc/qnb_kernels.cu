@@ -2463,33 +2463,213 @@ __device__ __forceinline__ int row_append(int* __restrict__ row, int cap, int co
     return count + __popc(b);
 }
 
+// ---- cell grid of the row build -------------------------------------------
+// The reference bins atoms for its neighbour search in populate_grids
+// (src/nonbondene.f90:6264-6460, under USE_GRID).  Here one block per window
+// bins the distance atoms of the switch-atom tests (each non-excluded solute
+// group's switch atom, each non-excluded water's oxygen) on a uniform grid:
+// cells of at least half the largest cut-off, counted with atomics, ranges
+// from a block scan, entries scattered and then sorted by index inside each
+// cell, so the grid's contents do not depend on the atomics' order.
+__device__ __forceinline__ int cell_coord(float p, float lo, float inv_h, int n) {
+    // clamped in FP32 first: a NaN or far-away coordinate lands in an edge cell
+    return (int)fminf(fmaxf((p - lo) * inv_h, 0.0f), (float)(n - 1));
+}
+__device__ __forceinline__ int3 cell_of(const CellGrid& G, float4 p) {
+    return make_int3(cell_coord(p.x, G.lox, G.inv_h, G.nx), cell_coord(p.y, G.loy, G.inv_h, G.ny),
+                     cell_coord(p.z, G.loz, G.inv_h, G.nz));
+}
+__device__ __forceinline__ int cell_index(const CellGrid& G, int3 c) { return (c.z * G.ny + c.y) * G.nx + c.x; }
+
+// distance atom of binned item t: solute groups first, then waters
+__device__ __forceinline__ int bin_atom(const DevModel& m, int t) {
+    return t < m.ncgp_solute ? m.gsw[t] : m.nat_solute + m.sa * (t - m.ncgp_solute);
+}
+
+__global__ void __launch_bounds__(1024) k_bin_cells(DevModel m, const DevState* __restrict__ states, float inv_h0) {
+    const DevState& s = states[blockIdx.x];
+    const float4* __restrict__ xq = s.xq;
+    const int ng = m.ncgp_solute, n = ng + m.nwat;
+    __shared__ float red[6][32];
+    __shared__ CellGrid G;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        int a = bin_atom(m, t);
+        if (m.excl[a]) continue;
+        float4 p = xq[a];
+        lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
+        hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(kFull, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(kFull, hi[k], o));
+        }
+    if (lane == 0)
+        for (int k = 0; k < 3; ++k) red[k][warp] = lo[k], red[3 + k][warp] = hi[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nw; ++w)
+            for (int k = 0; k < 3; ++k) red[k][0] = fminf(red[k][0], red[k][w]), red[3 + k][0] = fmaxf(red[3 + k][0], red[3 + k][w]);
+        float l[3], e[3];
+        for (int k = 0; k < 3; ++k) {
+            bool any = red[k][0] <= red[3 + k][0];   // false when nothing is binned (or NaN)
+            l[k] = any ? red[k][0] : 0.0f;
+            e[k] = any ? fminf(red[3 + k][0] - red[k][0], 1.0e6f) : 0.0f;
+        }
+        // larger cells keep the +-2 stencil sufficient: shrink inv_h until the grid fits
+        float ih = inv_h0;
+        int dim[3];
+        for (int it = 0; it < 256; ++it) {
+            for (int k = 0; k < 3; ++k) dim[k] = (int)(e[k] * ih) + 1;
+            if ((long long)dim[0] * dim[1] * dim[2] <= s.cap_cells) break;
+            ih *= 0.9f;
+        }
+        if ((long long)dim[0] * dim[1] * dim[2] > s.cap_cells) ih = 0.0f, dim[0] = dim[1] = dim[2] = 1;   // one cell
+        G = CellGrid{l[0], l[1], l[2], ih, dim[0], dim[1], dim[2], dim[0] * dim[1] * dim[2]};
+        *s.grid = G;
+    }
+    __syncthreads();
+    const CellGrid g = G;
+    for (int c = threadIdx.x; c < g.ncell; c += blockDim.x) s.cend_s[c] = 0, s.cend_w[c] = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        int a = bin_atom(m, t);
+        if (m.excl[a]) continue;
+        atomicAdd((t < ng ? s.cend_s : s.cend_w) + cell_index(g, cell_of(g, xq[a])), 1);
+    }
+    __syncthreads();
+    // exclusive scan of the counts, in place, both grids
+    int carry_s = 0, carry_w = 0;
+    for (int c0 = 0; c0 < g.ncell; c0 += blockDim.x) {
+        int c = c0 + threadIdx.x, tot;
+        int vs = c < g.ncell ? s.cend_s[c] : 0;
+        int es = block_excl_scan(vs, &tot);
+        if (c < g.ncell) s.cend_s[c] = carry_s + es;
+        carry_s += tot;
+        int vw = c < g.ncell ? s.cend_w[c] : 0;
+        int ew = block_excl_scan(vw, &tot);
+        if (c < g.ncell) s.cend_w[c] = carry_w + ew;
+        carry_w += tot;
+    }
+    __syncthreads();
+    // scatter: each append advances the cell's start to its end
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        int a = bin_atom(m, t);
+        if (m.excl[a]) continue;
+        float4 p = xq[a];
+        int c = cell_index(g, cell_of(g, p));
+        bool sol = t < ng;
+        int pos = atomicAdd((sol ? s.cend_s : s.cend_w) + c, 1);
+        p.w = __int_as_float(sol ? t : t - ng);
+        (sol ? s.bin_s : s.bin_w)[pos] = p;
+    }
+    __syncthreads();
+    // ascending index inside each cell (insertion sort; a cell holds a few entries)
+    for (int c = threadIdx.x; c < 2 * g.ncell; c += blockDim.x) {
+        bool sol = c < g.ncell;
+        int cc = sol ? c : c - g.ncell;
+        const int* ce = sol ? s.cend_s : s.cend_w;
+        float4* b = sol ? s.bin_s : s.bin_w;
+        int b0 = cc ? ce[cc - 1] : 0, b1 = ce[cc];
+        for (int i = b0 + 1; i < b1; ++i) {
+            float4 v = b[i];
+            int key = __float_as_int(v.w), j = i - 1;
+            while (j >= b0 && __float_as_int(b[j].w) > key) {
+                b[j + 1] = b[j];
+                --j;
+            }
+            b[j + 1] = v;
+        }
+    }
+}
+
+// The +-2 cell stencil of a row as 25 runs of consecutive cells along x
+// (one per (dy, dz)), each a contiguous range of the bin.  Lane r < 25 holds
+// run r's first entry (st) and the number of entries in runs before it
+// (pre); lanes 25..31 hold empty runs.  The warp then walks the runs as one
+// index space 0..total-1, 32 candidates at a time.
+struct Runs {
+    int st, pre, total;
+};
+__device__ __forceinline__ Runs stencil_runs(const int* __restrict__ cend, const CellGrid& G, int3 c) {
+    const int lane = threadIdx.x & 31;
+    int st = 0, len = 0;
+    if (lane < 25) {
+        int y = c.y + lane % 5 - 2, z = c.z + lane / 5 - 2;
+        if (y >= 0 && y < G.ny && z >= 0 && z < G.nz) {
+            int x0 = max(c.x - 2, 0), x1 = min(c.x + 2, G.nx - 1);
+            int c0 = (z * G.ny + y) * G.nx + x0;
+            st = c0 ? cend[c0 - 1] : 0;
+            len = cend[c0 + x1 - x0] - st;
+        }
+    }
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += v;
+    }
+    return Runs{st, incl - len, __shfl_sync(kFull, incl, 31)};
+}
+// bin position of candidate t (all lanes call it; t >= total gives an unused value)
+__device__ __forceinline__ int run_item(const Runs& R, int t) {
+    int r = 0;   // the last run with pre <= t; empty runs and lanes past 24 are skipped
+#pragma unroll
+    for (int step = 16; step; step >>= 1) {
+        int pv = __shfl_sync(kFull, R.pre, r + step);
+        if (pv <= t) r += step;
+    }
+    return __shfl_sync(kFull, R.st, r) + t - __shfl_sync(kFull, R.pre, r);
+}
+
 // nbpplist/nbpwlist/nbwwlist selections (src/nonbondene.f90:1777-1908,
 // 2842-2955, 4274-4395) stored from both sides.  Rows 0..ncgp_solute-1 are
-// solute groups, the next nwat rows waters; one warp per row.
+// solute groups, the next nwat rows waters; one warp per row.  CELLS: the
+// candidates are the entries of the row's +-2 cell stencil (switch-atom
+// tests); otherwise every group and water is a candidate (any-atom tests).
+// The inside tests are the same in both: the FP32 distance of the packed
+// positions, the FP64 distance within the decision band.
+template <bool CELLS>
 __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cut c) {
-    const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww),
-               blrf = band(c.rlrf2, c.flrf);
+    const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww);
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
     const float4* __restrict__ xq = s.xq;
     int nrows = m.ncgp_solute + m.nwat;
     int lane = threadIdx.x & 31;
+    CellGrid G;
+    if (CELLS) G = *s.grid;
     for (int r = warp_id_global(); r < nrows; r += warps_total()) {
         if (r < m.ncgp_solute) {
             int g = r, is = m.gsw[g];
             int npp = 0, npf = 0, npw = 0;
             if (!m.excl[is]) {
+                const float4 xs = xq[is];
+                Runs R{0, 0, 0};
+                if (CELLS) R = stencil_runs(s.cend_s, G, cell_of(G, xs));
+                const int ncand = CELLS ? R.total : m.ncgp_solute;
                 int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
                 const unsigned long long tmask = m.gtmask[g];
                 uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
                 int* rf = s.row_gf + (size_t)g * s.cap_gf;
-                for (int j0 = 0; j0 < m.ncgp_solute; j0 += kWarp) {
-                    int g2 = j0 + lane;
+                for (int j0 = 0; j0 < ncand; j0 += kWarp) {
+                    const int t = j0 + lane;
+                    const int bi = CELLS ? run_item(R, t) : 0;
                     bool ok = false;
-                    int b0 = 0, n2 = 0, ns = 0, nf = 0, sgi = -1;
-                    if (g2 < m.ncgp_solute) {
-                        int s2 = m.gsw[g2];
-                        if (!m.excl[s2]) ok = (g2 == g) || gg_inside(m, x, xq, g, g2, bpp);
+                    int g2 = -1, b0 = 0, n2 = 0, ns = 0, nf = 0, sgi = -1;
+                    if (t < ncand) {
+                        if (CELLS) {
+                            float4 it = s.bin_s[bi];
+                            g2 = __float_as_int(it.w);
+                            ok = g2 == g || within(r2_f(xs, it), bpp, x, is, m.gsw[g2]);
+                        } else {
+                            g2 = t;
+                            if (!m.excl[m.gsw[g2]]) ok = g2 == g || gg_inside(m, x, xq, g, g2, bpp);
+                        }
                         if (ok) {
                             b0 = m.gslot[g2];
                             n2 = m.gslot[g2 + 1] - b0;
@@ -2548,13 +2728,23 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                     npp += total & 0xffff;
                     npf += total >> 16;
                 }
+                if (CELLS) R = stencil_runs(s.cend_w, G, cell_of(G, xs));
+                const int ncw = CELLS ? R.total : m.nwat;
                 int* rw = s.row_gw + (size_t)g * s.cap_gw;
-                for (int j0 = 0; j0 < m.nwat; j0 += kWarp) {
-                    int jw = j0 + lane;
+                for (int j0 = 0; j0 < ncw; j0 += kWarp) {
+                    const int t = j0 + lane;
+                    const int bi = CELLS ? run_item(R, t) : 0;
                     bool ok = false;
-                    if (jw < m.nwat) {
-                        int jo = m.nat_solute + m.sa * jw;
-                        if (!m.excl[jo]) ok = gw_inside(m, x, xq, g, jo, bpw);
+                    int jw = t;
+                    if (t < ncw) {
+                        if (CELLS) {
+                            float4 it = s.bin_w[bi];
+                            jw = __float_as_int(it.w);
+                            ok = within(r2_f(xs, it), bpw, x, is, m.nat_solute + m.sa * jw);
+                        } else {
+                            int jo = m.nat_solute + m.sa * jw;
+                            if (!m.excl[jo]) ok = gw_inside(m, x, xq, g, jo, bpw);
+                        }
                     }
                     npw = row_append(rw, s.cap_gw, npw, ok, jw);
                 }
@@ -2571,25 +2761,45 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
             int w = r - m.ncgp_solute, io = m.nat_solute + m.sa * w;
             int nww = 0, nwg = 0;
             if (!m.excl[io]) {
-                float4 xi = xq[io];
+                const float4 xi = xq[io];
+                Runs R{0, 0, 0};
+                if (CELLS) R = stencil_runs(s.cend_w, G, cell_of(G, xi));
+                const int ncw = CELLS ? R.total : m.nwat;
                 int* rw = s.row_ww + (size_t)w * s.cap_rww;
-                for (int j0 = 0; j0 < m.nwat; j0 += kWarp) {
-                    int jw = j0 + lane;
+                for (int j0 = 0; j0 < ncw; j0 += kWarp) {
+                    const int t = j0 + lane;
+                    const int bi = CELLS ? run_item(R, t) : 0;
                     bool ok = false;
-                    if (jw < m.nwat && jw != w) {
-                        int jo = m.nat_solute + m.sa * jw;
-                        if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), bww, x, io, jo);
+                    int jw = t;
+                    if (t < ncw) {
+                        if (CELLS) {
+                            float4 it = s.bin_w[bi];
+                            jw = __float_as_int(it.w);
+                            ok = jw != w && within(r2_f(xi, it), bww, x, io, m.nat_solute + m.sa * jw);
+                        } else if (jw != w) {
+                            int jo = m.nat_solute + m.sa * jw;
+                            if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), bww, x, io, jo);
+                        }
                     }
                     nww = row_append(rw, s.cap_rww, nww, ok, jw);
                 }
+                if (CELLS) R = stencil_runs(s.cend_s, G, cell_of(G, xi));
+                const int ncg = CELLS ? R.total : m.ncgp_solute;
                 int* rg = s.row_wg + (size_t)w * s.cap_wg;
-                for (int j0 = 0; j0 < m.ncgp_solute; j0 += kWarp) {
-                    int g = j0 + lane;
+                for (int j0 = 0; j0 < ncg; j0 += kWarp) {
+                    const int t = j0 + lane;
+                    const int bi = CELLS ? run_item(R, t) : 0;
                     bool ok = false;
-                    if (g < m.ncgp_solute) {
-                        int s2 = m.gsw[g];
+                    int g = t;
+                    if (t < ncg) {
                         // the same test as from the group side
-                        if (!m.excl[s2]) ok = gw_inside(m, x, xq, g, io, bpw);
+                        if (CELLS) {
+                            float4 it = s.bin_s[bi];
+                            g = __float_as_int(it.w);
+                            ok = within(r2_f(it, xi), bpw, x, m.gsw[g], io);
+                        } else if (!m.excl[m.gsw[g]]) {
+                            ok = gw_inside(m, x, xq, g, io, bpw);
+                        }
                     }
                     nwg = row_append(rg, s.cap_wg, nwg, ok, g);
                 }
@@ -3139,10 +3349,21 @@ int launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* l
     return 1;
 }
 
-void launch_build_rows(const Launch& L, const Cut& c) {
+int launch_build_rows(const Launch& L, const Cut& c) {
     int nrows = L.m.ncgp_solute + L.m.nwat;
-    if (nrows == 0) return;
-    k_build_rows<<<grid_for((int64_t)nrows * 32, 128, L.tu.v[T_BUILD], L.nwin), 128, 0, L.st>>>(L.m, L.ds, c);
+    if (nrows == 0) return 0;
+    dim3 g = grid_for((int64_t)nrows * 32, 128, L.tu.v[T_BUILD], L.nwin);
+    if (L.m.any_atom) {   // any-atom group tests: every group and water is a candidate
+        k_build_rows<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+        return 1;
+    }
+    // cells of half the largest cut-off plus a margin far above the FP32
+    // rounding of the packed positions (a few 1e-6 A)
+    double rc = std::sqrt(std::max(c.rcpp2, std::max(c.rcpw2, c.rcww2)));
+    double h = 0.5 * (rc + std::max(0.01, 1e-4 * rc));
+    k_bin_cells<<<L.nwin, 1024, 0, L.st>>>(L.m, L.ds, (float)(1.0 / h));
+    k_build_rows<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+    return 2;
 }
 int lj_smem(const DevModel& m) {
     return m.natyps <= kMaxTypesShared ? (int)(m.natyps * m.natyps * sizeof(float4)) : 0;

@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libqnb.so")
 PREC_FP64 = 0
 PREC_MIXED = 1
 LIST_PP, LIST_PW, LIST_WW, LIST_QP, LIST_QW, LIST_PP14 = range(6)
+ROWS_GP, ROWS_GW, ROWS_WW, ROWS_WG = range(4)
 
 E_FIELDS = ("pp_el", "pp_vdw", "pw_el", "pw_vdw", "ww_el", "ww_vdw", "lrf")
 Q_FIELDS = ("qq_el", "qq_vdw", "qp_el", "qp_vdw", "qw_el", "qw_vdw")
@@ -32,7 +33,7 @@ EXPORTED = (
     "qnb_last_error", "qnb_version", "qnb_create", "qnb_destroy", "qnb_set_lambda",
     "qnb_make_pair_lists", "qnb_pot_energy_nonbonds", "qnb_nonbond_qq",
     "qnb_set_solvent_params", "qnb_restrain_solvent", "qnb_watpol", "qnb_get_watpol_state",
-    "qnb_list_size", "qnb_export_pairs", "qnb_get_lrf", "qnb_device_buffers", "qnb_stream",
+    "qnb_list_size", "qnb_export_pairs", "qnb_export_rows", "qnb_get_lrf", "qnb_device_buffers", "qnb_stream",
     "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_take_launch_count",
     "qnb_profile", "qnb_kernel_times", "qnb_create_batch", "qnb_window_count",
     "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
@@ -84,6 +85,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_restrain_solvent": [P, P, P, D, P], "qnb_watpol": [P, P, P, I32, I32, P],
         "qnb_get_watpol_state": [P, P, P, P], "qnb_list_size": [P, I32, P],
         "qnb_export_pairs": [P, I32, P, P, I64, P], "qnb_get_lrf": [P, P],
+        "qnb_export_rows": [P, I32, I32, P, P, I64, P],
         "qnb_device_buffers": [P, P, P], "qnb_stream": [P, P],
         "qnb_compute_dev": [P, D, I32, I32, P, P, P], "qnb_take_launch_count": [P, P],
         "qnb_profile": [P, I32], "qnb_kernel_times": [P, P, P, I32],
@@ -222,6 +224,17 @@ class NonbondedEngine:
         m = ctypes.c_int64()
         self._check(self.lib.qnb_export_pairs(self.h, kind, _p(i), _p(j), n, ctypes.byref(m)))
         return i[:m.value], j[:m.value]
+
+    def export_rows(self, kind, win=0):
+        """(row, partner) entries of the mixed form's gather rows of one
+        window (ROWS_GP / ROWS_GW / ROWS_WW / ROWS_WG)."""
+        m = ctypes.c_int64()
+        self.lib.qnb_export_rows(self.h, win, kind, None, None, 0, ctypes.byref(m))
+        n = int(m.value)
+        r = np.zeros(max(n, 1), np.int32)
+        p = np.zeros(max(n, 1), np.int32)
+        self._check(self.lib.qnb_export_rows(self.h, win, kind, _p(r), _p(p), n, ctypes.byref(m)))
+        return r[:m.value], p[:m.value]
 
     def lrf(self):
         out = np.zeros((self.s.ncgp, 43))
