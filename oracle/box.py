@@ -44,6 +44,28 @@ def d2_min_image(L, xa, xb):
     return (t * t).sum(-1)
 
 
+def _pairs_within_box(L, p, rc):
+    """(i, j), i < j, with minimum-image d2 <= rc^2 in FP64: a periodic k-d
+    tree proposes the pairs within rc + 0.01 A of the wrapped positions, the
+    d2 above decides (scipy; the all-pairs matrix when it is absent)."""
+    try:
+        from scipy.spatial import cKDTree
+    except ImportError:
+        cKDTree = None
+    if cKDTree is None or len(p) < 2:
+        d2 = d2_min_image(L, p[:, None, :], p[None, :, :])
+        return np.nonzero(np.triu(d2 <= rc * rc, 1))
+    w = np.mod(p, L)
+    w = np.where(w >= L, 0.0, w)   # mod may round up to L itself
+    cand = cKDTree(w, boxsize=L).query_pairs(rc + 0.01, output_type="ndarray")
+    if len(cand) == 0:
+        return np.zeros(0, np.int64), np.zeros(0, np.int64)
+    i, j = np.minimum(cand[:, 0], cand[:, 1]), np.maximum(cand[:, 0], cand[:, 1])
+    keep = d2_min_image(L, p[i], p[j]) <= rc * rc
+    o = np.lexsort((j[keep], i[keep]))
+    return i[keep][o], j[keep][o]
+
+
 def _groups(s):
     return [np.asarray(s.cgpatom[s.cgp_first[g]:s.cgp_last[g] + 1], np.int64) for g in range(s.ncgp_solute)]
 
@@ -92,8 +114,7 @@ def box_lists(s, x, L, qswitch, cut):
                     pw.extend((int(i), int(w)) for w in inside)
     ww = []
     if W:
-        d2 = d2_min_image(L, x[first][:, None, :], x[first][None, :, :])
-        iw, jw = np.nonzero(np.triu(d2 <= cut["Rcww"] ** 2, 1))
+        iw, jw = _pairs_within_box(L, x[first], cut["Rcww"])
         ww = list(zip(iw.tolist(), jw.tolist()))
     qp, qw = [], []
     if s.nqat:
@@ -171,24 +192,50 @@ def box_energies(s, x, lam, L, qswitch, cut, lists=None):
         E["pp_el"] += v[0]
         E["pp_vdw"] += v[1]
     wt = [int(s.iac[ns + a]) for a in range(sa)]
-    for i, w in lists["pw"]:
-        j0 = ns + sa * w
+
+    def pairs(i, j, sh, A, B, el, lj=True):
+        """pair() over arrays of pairs; returns the summed (el, vdw)."""
+        vec = sh - (x[i] - x[j])
+        r2 = 1.0 / (vec * vec).sum(1)
+        r = np.sqrt(r2)
+        vel = el * r
+        if lj:
+            r6 = r2 * r2 * r2
+            va, vb = A * r6 * r6, B * r6
+            dv = r2 * (-vel - 12.0 * va + 6.0 * vb)
+            vdw = float((va - vb).sum())
+        else:
+            dv, vdw = r2 * (-vel), 0.0
+        np.add.at(d, i, -vec * dv[:, None])
+        np.add.at(d, j, vec * dv[:, None])
+        return float(vel.sum()), vdw
+
+    if len(lists["pw"]):
+        P = np.asarray(lists["pw"], np.int64).reshape(-1, 2)
+        i, j0 = P[:, 0], ns + sa * P[:, 1]
         sh = shift_of(L, x[sw[iwhich[i]]], x[j0])
+        ti = np.asarray(s.iac, np.int64)[i]
         for a in range(sa):
-            code = int(s.ljcod[s.iac[i], wt[a]])
-            A, B = _lj_pair(s, int(s.iac[i]), wt[a], code)
-            v = pair(i, j0 + a, sh, A, B, s.crg[i] * s.crg[j0 + a])
+            code = np.asarray(s.ljcod, np.int64)[ti, wt[a]]
+            A = np.zeros(len(i))
+            B = np.zeros(len(i))
+            for t in np.unique(ti):
+                for c in np.unique(code[ti == t]):
+                    m = (ti == t) & (code == c)
+                    A[m], B[m] = _lj_pair(s, int(t), wt[a], int(c))
+            v = pairs(i, j0 + a, sh, A, B, s.crg[i] * s.crg[j0 + a])
             E["pw_el"] += v[0]
             E["pw_vdw"] += v[1]
-    for iw, jw in lists["ww"]:
-        i0, j0 = ns + sa * iw, ns + sa * jw
+    if len(lists["ww"]):
+        P = np.asarray(lists["ww"], np.int64).reshape(-1, 2)
+        i0, j0 = ns + sa * P[:, 0], ns + sa * P[:, 1]
         sh = shift_of(L, x[i0], x[j0])
         for la in range(sa):
             for ka in range(sa):
                 lj = (not spc) or (la == 0 and ka == 0)
                 code = int(s.ljcod[wt[la], wt[ka]])
                 A, B = _lj_pair(s, wt[la], wt[ka], code)
-                v = pair(i0 + la, j0 + ka, sh, A, B, s.crg[i0 + la] * s.crg[j0 + ka], lj)
+                v = pairs(i0 + la, j0 + ka, sh, A, B, s.crg[i0 + la] * s.crg[j0 + ka], lj)
                 E["ww_el"] += v[0]
                 E["ww_vdw"] += v[1]
 
@@ -224,17 +271,125 @@ def box_energies(s, x, lam, L, qswitch, cut, lists=None):
             for st, (vel, vdw) in enumerate(qpair(int(s.iqseq[iq]), j, sh, pars, True)):
                 EQ[st, 2] += vel
                 EQ[st, 3] += vdw
-    for w in lists["qw"]:
-        j0 = ns + sa * w
+    if len(lists["qw"]):
+        j0 = ns + sa * np.asarray(lists["qw"], np.int64)
         sh = shift_of(L, x[qswitch], x[j0])
         for iq in range(nq):
+            i = int(s.iqseq[iq])
             for a in range(sa):
-                pars = [_qw_values(s, iq, a, st) for st in range(S)]
                 lj = (not spc) or a == 0
-                for st, (vel, vdw) in enumerate(qpair(int(s.iqseq[iq]), j0 + a, sh, pars, lj)):
-                    EQ[st, 4] += vel
-                    EQ[st, 5] += vdw
+                vec = sh - (x[i] - x[j0 + a])
+                r2 = 1.0 / (vec * vec).sum(1)
+                r = np.sqrt(r2)
+                r6hc = 1.0 / (r2 * r2 * r2)
+                dvs = np.zeros(len(j0))
+                for st in range(S):
+                    A, B, el, sc = _qw_values(s, iq, a, st)
+                    vel = el * r
+                    if lj:
+                        r6 = 1.0 / (r6hc + sc)
+                        va, vb = A * r6 * r6, B * r6
+                        dvs += r2 * (-vel - (12.0 * va - 6.0 * vb) * r6 * r6hc) * lam[st]
+                        EQ[st, 5] += float((va - vb).sum())
+                    else:
+                        dvs += -r2 * vel * lam[st]
+                    EQ[st, 4] += float(vel.sum())
+                d[i] -= (vec * dvs[:, None]).sum(0)
+                np.add.at(d, j0 + a, vec * dvs[:, None])
     return d, E, EQ
+
+
+def _all_groups(s):
+    return [np.asarray(s.cgpatom[s.cgp_first[g]:s.cgp_last[g] + 1], np.int64) for g in range(s.ncgp)]
+
+
+def box_lrf(s, x, L, cut, batch=64):
+    """LRF records of the box lists (cgp_centers, then the LRF branch of
+    nbpplist_box_lrf 1910-2055, nbpwlist_box_lrf 2957-3085, nbwwlist_box_lrf
+    4397-4515 with lrf_update 628-725): every unit pair (solute group, water)
+    whose minimum-image switch-atom distance r2 satisfies Rc^2 < r2 <=
+    RcLRF^2 (Rc of the pair's kind) adds the non-Q atoms of each unit to the
+    other's Taylor moments about its group centre, the source shifted by
+    boxlength * nint((x_switch(source) - centre(target)) / boxlength).
+    Excluded atoms take part (the box lists do not test excl).  Returns
+    [ncgp][43]: centre(3), phi0, phi1(3), phi2(3x3 row-major), phi3(9x3)."""
+    x = np.asarray(x, np.float64)
+    L = np.asarray(L, np.float64)
+    groups = _all_groups(s)
+    G, Gs, ns, sa = s.ncgp, s.ncgp_solute, s.nat_solute, s.solv_atom
+    cent = np.array([x[a].mean(0) for a in groups])
+    sw = np.array([int(s.cgp_iswitch[g]) if g < Gs else int(groups[g][0]) for g in range(G)], np.int64)
+    isq = np.zeros(s.natom, bool)
+    isq[np.asarray(s.iqseq, np.int64)] = True
+    gof = np.zeros(s.natom, np.int64)
+    for g, a in enumerate(groups):
+        gof[a] = g
+    src = np.nonzero(~isq)[0]                 # LRF source atoms
+    sgrp = gof[src]
+    q = np.asarray(s.crg, np.float64)[src]
+    solute = np.arange(G) < Gs
+    rl2 = cut["RcLRF"] ** 2
+    out = np.zeros((G, 43))
+    out[:, :3] = cent
+    for b0 in range(0, G, batch):
+        tg = np.arange(b0, min(G, b0 + batch))
+        d2 = d2_min_image(L, x[sw][None, :, :], x[sw[tg]][:, None, :])          # [target][source group]
+        both = solute[tg][:, None] & solute[None, :]
+        none = ~solute[tg][:, None] & ~solute[None, :]
+        rc2 = np.where(both, cut["Rcpp"] ** 2, np.where(none, cut["Rcww"] ** 2, cut["Rcpw"] ** 2))
+        use = (d2 > rc2) & (d2 <= rl2)
+        use[np.arange(len(tg)), tg] = False
+        sh = L * nint((x[sw][None, :, :] - cent[tg][:, None, :]) / L)             # [target][source group][3]
+        dr = x[src][None, :, :] - cent[tg][:, None, :] - sh[:, sgrp, :]           # [target][atom][3]
+        w = use[:, sgrp]
+        r2 = (dr * dr).sum(2)
+        r2 = np.where(w, r2, 1.0)
+        f0 = np.where(w, q[None, :] / (r2 * np.sqrt(r2)), 0.0)
+        f1 = 3.0 * f0 / r2
+        f2 = -f1 / r2
+        out[tg, 3] = (f0 * r2).sum(1)
+        out[tg, 4:7] = -(dr * f0[:, :, None]).sum(1)
+        drT = dr.transpose(0, 2, 1)                                                # [t][3][a]
+        phi2 = (drT * f1[:, None, :]) @ dr                                         # sum_a f1 dr_k dr_l
+        phi2 -= f0.sum(1)[:, None, None] * np.eye(3)[None]
+        out[tg, 7:16] = phi2.reshape(len(tg), 9)
+        # phi3(n, j, c) = 5 f2 dr_n dr_j dr_c - f2 r2 (d_nj dr_c + d_nc dr_j + d_jc dr_n)
+        nj = (drT[:, :, None, :] * drT[:, None, :, :]).reshape(len(tg), 9, -1)   # [t][(n, j)][a]
+        phi3 = ((nj * (5.0 * f2)[:, None, :]) @ dr).reshape(len(tg), 3, 3, 3)
+        gs = ((f2 * r2)[:, :, None] * dr).sum(1)                                   # [t][3]
+        I = np.eye(3)
+        phi3 -= (I[None, :, :, None] * gs[:, None, None, :] + I[None, :, None, :] * gs[:, None, :, None]
+                 + I[None, None, :, :] * gs[:, :, None, None])
+        out[tg, 16:43] = phi3.reshape(len(tg), 27)
+    return out
+
+
+def box_lrf_taylor(s, x, lrf):
+    """lrf_taylor (src/nonbondene.f90:507-571) with use_PBC: every non-Q atom
+    (excluded atoms included) takes the Taylor potential and field of its own
+    group's record.  Returns (E_LRF, gradient)."""
+    x = np.asarray(x, np.float64)
+    groups = _all_groups(s)
+    isq = np.zeros(s.natom, bool)
+    isq[np.asarray(s.iqseq, np.int64)] = True
+    gof = np.zeros(s.natom, np.int64)
+    for g, a in enumerate(groups):
+        gof[a] = g
+    i = np.nonzero(~isq)[0]
+    R = lrf[gof[i]]
+    dr = R[:, :3] - x[i]
+    phi0, phi1 = R[:, 3], R[:, 4:7]
+    phi2 = R[:, 7:16].reshape(-1, 3, 3)
+    phi3 = R[:, 16:43].reshape(-1, 9, 3)
+    t2 = np.einsum("akl,al->ak", phi2, dr)                   # tmp_k = dr . phi2(k)
+    V = phi0 + (dr * phi1).sum(1) + 0.5 * (dr * t2).sum(1)
+    q = np.asarray(s.crg, np.float64)[i]
+    E = float((0.5 * q * V).sum())
+    t3 = np.einsum("amc,ac->am", phi3, dr).reshape(-1, 3, 3)   # [atom][k][j] = dr . phi3(3k + j)
+    df = phi1 + t2 + 0.5 * np.einsum("akj,aj->ak", t3, dr)
+    d = np.zeros_like(x)
+    d[i] -= df * q[:, None]
+    return E, d
 
 
 def put_back_in_box(x, L, molecules, mass, nmol_solute, nat_solute, put_solute=True, put_solvent=True,

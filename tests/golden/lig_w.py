@@ -18,8 +18,15 @@ from q6_gb300.system import QSystem
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def load_lig_w() -> tuple[QSystem, dict]:
-    f = np.load(os.path.join(HERE, "lig_w.npz"))
+FIXTURES = {"lig_w": "lig_w.npz", "lig_w_pbc": "lig_w_pbc.npz"}
+
+
+def load_lig_w(kind: str = "sph") -> tuple[QSystem, dict]:
+    """kind "sph": prep_SPH (the 20 A droplet); "pbc": prep_PBC (the same
+    solute in a 49.633 A periodic box; golden also holds boxlength, boxcentre
+    and the FEP file's switching atom qswitch, 0-based)."""
+    name = {"sph": "lig_w", "pbc": "lig_w_pbc"}[kind]
+    f = np.load(os.path.join(HERE, FIXTURES[name]))
     natom, nsol = int(f["natom"]), int(f["nat_solute"])
     sa = int(f["solv_atom"])
     scale = math.sqrt(float(f["coulomb"]))
@@ -62,7 +69,7 @@ def load_lig_w() -> tuple[QSystem, dict]:
         qconn=qconn, el_scale_pairs=np.zeros((0, 2), np.int32), el_scale=np.zeros((0, S)),
         qexpnb_pairs=np.zeros((0, 2), np.int32), xpcent=f["xpcent"], xwcent=f["xwcent"],
         rexcl_o=float(f["rexcl_o"]), rwat=float(f["rwat"]), mass=mass,
-        iuse_switch_atom=int(f["iuse_switch_atom"]), name="lig_w")
+        iuse_switch_atom=int(f["iuse_switch_atom"]), name=name)
     golden = {k: float(f[k]) for k in ("golden_qsurr_el", "golden_qsurr_vdw", "golden_el", "golden_vdw",
                                        "golden_bnd", "golden_ang", "golden_tor", "golden_imp",
                                        "golden_qbnd", "golden_qang", "golden_qtor", "golden_qimp")}
@@ -71,6 +78,10 @@ def load_lig_w() -> tuple[QSystem, dict]:
     golden["wbond_ij"] = f["wbond_ij"]
     golden["wbond_b0"] = f["wbond_b0"]
     golden["wbond_code"] = f["wbond_code"]
+    if "boxlength" in f.files:
+        golden["boxlength"] = f["boxlength"].copy()
+        golden["boxcentre"] = f["boxcentre"].copy()
+        golden["qswitch"] = int(f["qswitch"])
     return s, golden
 
 
@@ -88,7 +99,7 @@ def lig_w_topology_terms(s):
     """The topology's bonded terms with the FEP-redefined ones removed, before
     SHAKE removes any bond: what init_constraints and wat_shells read."""
     from q6_gb300.bonded import DEG2RAD, BondedTerms, remove_redefined
-    f = np.load(os.path.join(HERE, "lig_w.npz"))
+    f = np.load(os.path.join(HERE, FIXTURES[s.name]))
     anglib = f["anglib"].copy()
     anglib[:, 1] *= DEG2RAD
     torlib = f["torlib"].copy()
@@ -133,3 +144,27 @@ def lig_w_eq1_inputs(s):
     sp = default_solvent_params(s, fk_wsphere=60.0, fkwpol=20.0, itdis=100.0,
                                 crg_qtot=born_charge(s, [1.0]), mu_w=water_dipole(s, top))
     return setup, sp, top, lig_w_bonded(s)
+
+
+def lig_w_pbc_step0_coordinates(s, g):
+    """qdyn's step-0 coordinates of the box run: the start-up SHAKE of the
+    solvent bonds (initial_constraint, src/bondene.f90:1025-1048), then
+    put_back_in_box at the first list update (src/md.f90:1666-1671;
+    put_solvent_back_in_box on, put_solute_back_in_box off, the box centred on
+    the solute's mean position since rigid_box_centre defaults off)."""
+    from oracle.box import put_back_in_box
+    from oracle.oracle import shake
+    mols = {}
+    for (i, j), b0 in zip(g["wbond_ij"], g["wbond_b0"]):
+        mols.setdefault((int(i) - s.nat_solute) // s.solv_atom, []).append((int(i), int(j), float(b0)))
+    x = shake(s.x, [mols[k] for k in sorted(mols)], 1.0 / s.mass[s.iac])
+    molecules = [np.arange(s.nat_solute)] + [s.nat_solute + s.solv_atom * w + np.arange(s.solv_atom)
+                                             for w in range(s.nwat)]
+    x, _ = put_back_in_box(x, g["boxlength"], molecules, s.mass[s.iac], 1, s.nat_solute,
+                           put_solute=False, put_solvent=True)
+    return x
+
+
+# the box run's cut-offs (run_test.sh:173-176: q_atom 24, lrf 24; solute and
+# solvent cut-offs at their defaults of 10 A)
+PBC_CUT = dict(Rcq=24.0, RcLRF=24.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)

@@ -1,12 +1,15 @@
-"""Build tests/golden/lig_w.npz from Q6's own regression-test inputs.
+"""Build tests/golden/lig_w.npz and lig_w_pbc.npz from Q6's own regression-test
+inputs.
 
 Reads tests/basic_tests/prep_SPH/lig_w.top and lig_w.fep of the Q6 tree (its
 root directory is the required command-line argument) with a reader written for
 the Q topology text format as Q6 src/topo.f90:471-1115 parses it, and stores
-the arrays the nonbonded path needs.  The fixture is what the golden test uses;
-the Q6 tree is not needed at test time.
+the arrays the nonbonded path needs; likewise prep_PBC (the same solute in a
+49.633 A periodic box of 4,072 SPC waters, box size and centre from the
+topology, the FEP file's [PBC] switching_atom).  The fixtures are what the
+golden tests use; the Q6 tree is not needed at test time.
 
-The step-0 energies that the Q6 regression test checks for this system
+The step-0 energies that the Q6 regression test checks for the sphere
 (tests/basic_tests/eval_test.sh:99 and row 1 of
 SPH_leap-frog_berendsen_benchmark.en) are stored beside the arrays:
 Q-surr. el 3.12, vdW 139.43 (Q-atom state 1, lambda 1), the sums of the
@@ -16,7 +19,10 @@ improper 0.05; Q-atom bond -122.04, angle 0.68, torsion 2.17, improper 0.00.
 The same row's last six columns, read from the file, are the reference's
 bands (mean -/+ one standard deviation over the 20 random seeds of its
 benchmark runs, run_test.sh:197-440) of the step-0 total, kinetic and
-potential energy: golden_tot_band, golden_kin_band, golden_pot_band.
+potential energy: golden_tot_band, golden_kin_band, golden_pot_band.  For
+the box, row 1 of PBC_leap-frog_berendsen_benchmark.en (eval_test.sh:101:
+Q-surr. el -31.30, vdW 228.64; EL 380.33, VdW -1990.55; POT -1512.62 with a
+zero-width band; run with q_atom 24 and lrf 24, run_test.sh:173-176).
 
 Usage: python tests/golden/make_lig_w_fixture.py Q6_ROOT
 """
@@ -171,11 +177,20 @@ def read_top(path):
     while "solvent type" not in r.lines[r.k]:
         r.k += 1
     solvent_type = r.head_ints(1)[0]
-    rexcl_o, rwat = r.head_floats(2)
-    xpcent = np.array(r.head_floats(3))
-    xwcent = np.array(r.head_floats(3))
-    nexats, nexwat = r.head_ints(2)
-    excl = np.array(r.logicals(nat_pro), dtype=np.uint8)
+    boxl = boxc = None
+    if "PBC" in r.lines[r.k] and "boundary" in r.lines[r.k]:   # src/topo.f90: box size and centre, no exclusions
+        r.line()
+        boxl = np.array(r.head_floats(3))
+        boxc = np.array(r.head_floats(3))
+        rexcl_o = rwat = 0.0
+        xpcent = xwcent = boxc.copy()
+        excl = np.zeros(nat_pro, dtype=np.uint8)
+    else:
+        rexcl_o, rwat = r.head_floats(2)
+        xpcent = np.array(r.head_floats(3))
+        xwcent = np.array(r.head_floats(3))
+        nexats, nexwat = r.head_ints(2)
+        excl = np.array(r.logicals(nat_pro), dtype=np.uint8)
 
     pairs14 = [(i, i + o + 1) for i in range(nat_solute) for o in range(MAX_NBR_RANGE) if l14[i, o]]
     pairs14 += [(a - 1, b - 1) for a, b in p14long]
@@ -195,6 +210,7 @@ def read_top(path):
         el14_scale=el14_scale, pairs14=np.array(pairs14, np.int32).reshape(-1, 2),
         excl_pairs=np.array(expairs, np.int32).reshape(-1, 2), solvent_type=solvent_type,
         rexcl_o=rexcl_o, rwat=rwat, xpcent=xpcent, xwcent=xwcent, excl=excl,
+        **({} if boxl is None else dict(boxlength=boxl, boxcentre=boxc)),
         # solvent bonds in topology order with their equilibrium lengths: the
         # SHAKE constraints qdyn applies at start-up (shake_solvent defaults on)
         wbond_ij=(bnd[nbonds_solute:, :2] - 1).astype(np.int32),
@@ -287,28 +303,64 @@ def read_step0_bands(path):
     raise ValueError("no data row in " + path)
 
 
+def read_switching_atom(path):
+    """[PBC] switching_atom of an FEP file (src/qatom.f90:700-716), 0-based."""
+    sec = None
+    with open(path) as f:
+        for ln in f:
+            t = ln.split("!")[0].strip()
+            if t.startswith("["):
+                sec = t.strip("[]").lower()
+            elif sec == "pbc" and t.split() and t.split()[0] == "switching_atom":
+                return int(t.split()[1]) - 1
+    raise ValueError("no [PBC] switching_atom in " + path)
+
+
+def read_step0_row(path):
+    """Lower bounds of the first data row of a *_benchmark.en file in column
+    order (QEL QVdW EL VdW QBND QANG QTOR QIMP BND ANG TOR IMP TOT KIN POT)."""
+    for ln in open(path):
+        if ln.startswith("#") or not ln.strip():
+            continue
+        v = [float(t) for t in ln.split()[1:]]
+        return v[0::2]
+    raise ValueError("no data row in " + path)
+
+
+def build(root, kind):
+    bt = os.path.join(root, "tests", "basic_tests")
+    d = os.path.join(bt, "prep_" + kind)
+    top = read_top(os.path.join(d, "lig_w.top"))
+    fep = os.path.join(d, "lig_w.fep")
+    nstates, iqseq = read_fep_atoms(fep)
+    fepb = read_fep_bonded(fep, nstates)
+    en = os.path.join(bt, kind + "_leap-frog_berendsen_benchmark.en")
+    tot, kin, pot = read_step0_bands(en)
+    row = read_step0_row(en)
+    extra = {}
+    if kind == "PBC":
+        extra["qswitch"] = read_switching_atom(fep)
+    name = "lig_w.npz" if kind == "SPH" else "lig_w_pbc.npz"
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), name)
+    np.savez_compressed(
+        out, **top, **fepb, **extra, nstates=nstates, iqseq=iqseq,
+        golden_tot_band=np.array(tot), golden_kin_band=np.array(kin), golden_pot_band=np.array(pot),
+        # row 1 of <kind>_leap-frog_berendsen_benchmark.en (zero-width bands):
+        # Q-surr. el and vdW (the eval_test.sh line), the solute + solvent +
+        # solute-solvent EL and VdW, the solute row's bond, angle, torsion,
+        # improper and the Q-atom row's (state 1)
+        golden_qsurr_el=row[0], golden_qsurr_vdw=row[1], golden_el=row[2], golden_vdw=row[3],
+        golden_qbnd=row[4], golden_qang=row[5], golden_qtor=row[6], golden_qimp=row[7],
+        golden_bnd=row[8], golden_ang=row[9], golden_tor=row[10], golden_imp=row[11])
+    print("wrote", out, "atoms", top["natom"], "solute", top["nat_solute"],
+          "groups", len(top["cgp_first"]), "Q", len(iqseq), "row", row)
+
+
 def main():
     if len(sys.argv) != 2:
         sys.exit("usage: python tests/golden/make_lig_w_fixture.py Q6_ROOT")
-    root = sys.argv[1]
-    d = os.path.join(root, "tests", "basic_tests", "prep_SPH")
-    top = read_top(os.path.join(d, "lig_w.top"))
-    nstates, iqseq = read_fep_atoms(os.path.join(d, "lig_w.fep"))
-    fepb = read_fep_bonded(os.path.join(d, "lig_w.fep"), nstates)
-    tot, kin, pot = read_step0_bands(os.path.join(root, "tests", "basic_tests",
-                                                  "SPH_leap-frog_berendsen_benchmark.en"))
-    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lig_w.npz")
-    np.savez_compressed(
-        out, **top, **fepb, nstates=nstates, iqseq=iqseq,
-        golden_tot_band=np.array(tot), golden_kin_band=np.array(kin), golden_pot_band=np.array(pot),
-        golden_qsurr_el=3.12, golden_qsurr_vdw=139.43,
-        golden_el=-7.30, golden_vdw=-413.17,
-        # row 1 of SPH_leap-frog_berendsen_benchmark.en: the solute row's
-        # bond, angle, torsion, improper and the Q-atom row's (state 1)
-        golden_bnd=31.61, golden_ang=30.69, golden_tor=6.28, golden_imp=0.05,
-        golden_qbnd=-122.04, golden_qang=0.68, golden_qtor=2.17, golden_qimp=0.00)
-    print("wrote", out, "atoms", top["natom"], "solute", top["nat_solute"],
-          "groups", len(top["cgp_first"]), "Q", len(iqseq))
+    for kind in ("SPH", "PBC"):
+        build(sys.argv[1], kind)
 
 
 if __name__ == "__main__":
