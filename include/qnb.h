@@ -499,10 +499,18 @@ int qnb_get_group_exclusions(qnb_context* ctx, double* out);
    its units' reference atoms.  The static Q-Q lists keep plain distances, as
    nonbond_qq does.  Cut-offs must not exceed half the shortest edge.
    With iuse_switch_atom = 0 the pp / pw lists are nbpplis2_box /
-   nbpwlis2_box's (any atom pair inside).  boxlength = NULL returns to the
-   sphere.  Not supported with a box (QNB_ERR_UNSUPPORTED): LRF, excluded atoms,
-   solvent restraints and solvent internal pairs.  Constant pressure is the
-   caller's; put_back_in_box: qnb_set_put_back_in_box. */
+   nbpwlis2_box's (any atom pair inside).  With LRF on, unit pairs between
+   the cut-off and RcLRF in the minimum image feed the LRF moments as in
+   nbpplist_box_lrf / nbpwlist_box_lrf / nbwwlist_box_lrf (1910-2055,
+   2957-3085, 4397-4515), each source at x_i - boxlength*nint((x_switch -
+   centre)/boxlength) (lrf_update, 636-643), and lrf_taylor covers every
+   non-Q atom.  Excluded atoms take part like any other atom (the box lists,
+   lrf_taylor and temperature() test no exclusion under use_PBC); solvent
+   internal pairs use the minimum image (nonbond_solvent_internal_box,
+   6158-6228).  boxlength = NULL returns to the sphere (and its exclusions).
+   Not supported with a box (QNB_ERR_UNSUPPORTED): solvent restraints, and LRF
+   with iuse_switch_atom = 0 (nbpplis2_box_lrf / nbpwlis2_box_lrf).  Constant
+   pressure is the caller's; put_back_in_box: qnb_set_put_back_in_box. */
 int qnb_set_box(qnb_context* ctx, const double* boxlength, int32_t qswitch);
 
 /* fix_shell (src/potene.f90:386-423), evaluated inside qnb_compute_dev and

@@ -91,6 +91,20 @@ struct qnb_context {
     double* d_all = nullptr;       // [nwin][natom][3]
     int* d_iwhich = nullptr;
     int* d_lrf_src = nullptr;      // per atom: LRF source distance atom | solute flag << 30, or -1
+    // LRF source tables of the two boundaries: [0] the sphere's (groups whose
+    // distance atom is excluded are no source), [1] the box's (the box lists
+    // test no exclusion); qnb_set_box switches DevModel and d_lrf_src between them
+    struct LrfTables {
+        int* src = nullptr;
+        int* gmeta = nullptr;
+        int* goff = nullptr;
+        int* gatom = nullptr;
+        int n = 0;
+    } lrft[2];
+    // exclusion flags: the topology's, and all-clear for the box (excluded
+    // atoms take part in every box list, in lrf_taylor and in temperature())
+    uint8_t* d_excl_top = nullptr;
+    uint8_t* d_excl_none = nullptr;
     uint8_t* d_qnear = nullptr;
     int* d_wsw = nullptr;
     uint8_t* d_heavy_solv = nullptr;
@@ -296,6 +310,17 @@ int ensure_cap(qnb_context* c, T** buf, int64_t* cap, int64_t need) {
     return QNB_OK;
 }
 
+// points the model's LRF source tables (and the per-atom source array) at
+// the sphere's (0) or the box's (1)
+void use_lrf_tables(qnb_context* c, int tab) {
+    const auto& T = c->lrft[tab];
+    c->m.nlrf_groups = T.n;
+    c->m.lrf_gmeta = T.gmeta;
+    c->m.lrf_goff = T.goff;
+    c->m.lrf_gatom = T.gatom;
+    c->d_lrf_src = T.src;
+}
+
 int build_model(qnb_context* c, const qnb_topology* t) {
     const int natom = t->natom, ns = t->nat_solute, nt = t->natyps, nq = t->nqat, S = t->nstates;
     const int sa = t->solv_atom;
@@ -333,7 +358,9 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     }
     TRY(c->upload((int**)&m.iac, iac));
     TRY(c->upload((double**)&m.crg, crg));
-    TRY(c->upload((uint8_t**)&m.excl, excl));
+    TRY(c->upload(&c->d_excl_top, excl));
+    TRY(c->upload(&c->d_excl_none, std::vector<uint8_t>(natom, 0)));
+    m.excl = c->d_excl_top;
     TRY(c->upload((int**)&m.iqatom, iqatom));
     std::vector<int> iqseq(t->iqseq, t->iqseq + nq);
     TRY(c->upload((int**)&m.iqseq, iqseq));
@@ -385,18 +412,19 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     TRY(c->upload((int**)&m.gatom, gatom));
     TRY(c->upload((int**)&m.gsw, gsw));
     TRY(c->upload(&c->d_iwhich, iwhich));
-    // lrf_update sources: non-Q atoms of groups whose distance atom is not
-    // excluded (src/nonbondene.f90:658-660 and the list builders' excl skips)
-    std::vector<int> lrf_src(natom, -1);
-    for (int i = 0; i < natom; ++i) {
-        if (iqatom[i] >= 0) continue;
-        int g = iwhich[i];
-        int d = g < t->ncgp_solute ? t->cgp_iswitch[g] : ns + sa * (g - t->ncgp_solute);
-        if (t->excl[d]) continue;
-        lrf_src[i] = d | ((g < t->ncgp_solute ? 1 : 0) << 30);
-    }
-    TRY(c->upload(&c->d_lrf_src, lrf_src));
-    {   // the same sources grouped by charge group, in group order
+    // lrf_update sources: non-Q atoms (src/nonbondene.f90:658-660); in the
+    // sphere only of groups whose distance atom is not excluded (the list
+    // builders' excl skips), in the box of every group
+    for (int tab = 0; tab < 2; ++tab) {
+        std::vector<int> lrf_src(natom, -1);
+        for (int i = 0; i < natom; ++i) {
+            if (iqatom[i] >= 0) continue;
+            int g = iwhich[i];
+            int d = g < t->ncgp_solute ? t->cgp_iswitch[g] : ns + sa * (g - t->ncgp_solute);
+            if (tab == 0 && t->excl[d]) continue;
+            lrf_src[i] = d | ((g < t->ncgp_solute ? 1 : 0) << 30);
+        }
+        // the same sources grouped by charge group, in group order
         std::vector<int> gmeta, goff{0}, gat;
         for (int g = 0; g < t->ncgp; ++g) {
             int n0 = (int)gat.size(), meta = -1;
@@ -411,11 +439,14 @@ int build_model(qnb_context* c, const qnb_topology* t) {
                 goff.push_back((int)gat.size());
             }
         }
-        m.nlrf_groups = (int)gmeta.size();
-        TRY(c->upload((int**)&m.lrf_gmeta, gmeta));
-        TRY(c->upload((int**)&m.lrf_goff, goff));
-        TRY(c->upload((int**)&m.lrf_gatom, gat));
+        auto& T = c->lrft[tab];
+        T.n = (int)gmeta.size();
+        TRY(c->upload(&T.src, lrf_src));
+        TRY(c->upload(&T.gmeta, gmeta));
+        TRY(c->upload(&T.goff, goff));
+        TRY(c->upload(&T.gatom, gat));
     }
+    use_lrf_tables(c, 0);
     TRY(c->upload(&c->d_wsw, wsw));
 
     // special solute pairs: excluded (listex + listexlong) and 1-4 (list14 +
@@ -1154,6 +1185,9 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
     if (c->m.box) {   // periodic box: the *_box routines, src/potene.f90:326-343
         int nb = 0;
         timed(c, K_PP, [&] { nb = launch_box_nonbond(L, md, mx, c->d_iwhich, c->last_cut.rcq2); });
+        // src/potene.f90:326-339 and 373-377: solvent internal pairs, then the LRF Taylor terms
+        if (md && c->nsi) timed(c, K_WW, [&] { launch_solvent_internal(L, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
+        if (c->use_lrf && md) timed(c, K_LRF_TAYLOR, [&] { launch_lrf_taylor(L, c->d_iwhich, mx); }), ++nl;
         c->launches += nl + nb;
         return check_launch();
     }
@@ -2663,7 +2697,7 @@ int qnb_set_shell_restraint(qnb_context* c, const double* xtop, const uint8_t* s
     if (!shell) return fail(QNB_ERR_ARG, "null shell flags");
     if (!(fk_fix >= 0.0) || !(fk_pshell >= 0.0)) return fail(QNB_ERR_ARG, "negative force constant");
     std::vector<uint8_t> excl(c->natom);
-    CU(cudaMemcpy(excl.data(), c->m.excl, c->natom, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(excl.data(), c->d_excl_top, c->natom, cudaMemcpyDeviceToHost));
     std::vector<uint8_t> flags(c->natom);
     int any = 0;
     for (int i = 0; i < c->natom; ++i) {
@@ -2707,7 +2741,7 @@ int restraint_atom_codes(qnb_context* c, std::vector<uint8_t>* out) {
     out->assign(c->h_heavy.begin(), c->h_heavy.end());
     if (c->freeze) {
         std::vector<uint8_t> excl(c->natom);
-        CU(cudaMemcpy(excl.data(), c->m.excl, c->natom, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(excl.data(), c->d_excl_top, c->natom, cudaMemcpyDeviceToHost));
         for (int i = 0; i < c->natom; ++i)
             if (excl[i]) (*out)[i] |= 2;
     }
@@ -3102,23 +3136,25 @@ int qnb_set_box(qnb_context* c, const double* boxlength, int32_t qswitch) {
     CU(cudaStreamSynchronize(c->stream));
     if (!boxlength) {
         c->m.box = 0;
+        c->m.excl = c->d_excl_top;
+        use_lrf_tables(c, 0);
     } else {
         for (int k = 0; k < 3; ++k)
             if (!(boxlength[k] > 0.0)) return fail(QNB_ERR_ARG, "box length %d must be positive", k);
         if (c->nqat > 0 && (qswitch < 0 || qswitch >= c->natom))
             return fail(QNB_ERR_ARG, "switching atom %d out of range", qswitch);
-        if (c->use_lrf) return fail(QNB_ERR_UNSUPPORTED, "LRF with a periodic box is not supported");
-        if (c->have_solv || c->nsi > 0)
-            return fail(QNB_ERR_UNSUPPORTED, "solvent restraints and solvent internal pairs are for the sphere");
-        std::vector<uint8_t> excl(c->natom);
-        CU(cudaMemcpy(excl.data(), c->m.excl, c->natom, cudaMemcpyDeviceToHost));
-        for (int i = 0; i < c->natom; ++i)
-            if (excl[i]) return fail(QNB_ERR_UNSUPPORTED, "excluded atoms (atom %d) with a periodic box", i);
+        if (c->use_lrf && c->m.any_atom)
+            return fail(QNB_ERR_UNSUPPORTED, "LRF with a periodic box needs switch atoms (iuse_switch_atom 1)");
+        if (c->have_solv) return fail(QNB_ERR_UNSUPPORTED, "solvent restraints are for the sphere");
         c->m.box = 1;
+        c->m.excl = c->d_excl_none;   // the box lists, lrf_taylor and temperature() test no exclusion
+        use_lrf_tables(c, 1);
         c->m.qswitch = qswitch;
         for (int k = 0; k < 3; ++k) {
             c->m.boxl[k] = boxlength[k];
             c->m.inv_boxl[k] = 1.0 / boxlength[k];
+            c->m.boxlf[k] = (float)c->m.boxl[k];
+            c->m.inv_boxlf[k] = (float)c->m.inv_boxl[k];
         }
     }
     c->lists_built = false;

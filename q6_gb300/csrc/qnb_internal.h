@@ -134,6 +134,7 @@ struct DevModel {
     int box;
     int qswitch;
     double boxl[3], inv_boxl[3];
+    float boxlf[3], inv_boxlf[3];   // FP32 copies (set on the host)
     // FP32 copies are stored relative to xpcent, which bounds their magnitude
     // by the sphere size (FP32 cut-off prefilter and mixed-form pair math)
 };

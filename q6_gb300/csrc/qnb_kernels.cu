@@ -937,6 +937,71 @@ __global__ void __launch_bounds__(kLrfBlock) k_lrf_accumulate2(DevModel m, const
     }
 }
 
+// lattice shift and minimum-image distance of two atoms (periodic box)
+__device__ __forceinline__ void box_shift(const DevModel& m, const double* __restrict__ x, int a, int b,
+                                          double& sx, double& sy, double& sz) {
+    sx = m.boxl[0] * round((x[3 * a] - x[3 * b]) * m.inv_boxl[0]);
+    sy = m.boxl[1] * round((x[3 * a + 1] - x[3 * b + 1]) * m.inv_boxl[1]);
+    sz = m.boxl[2] * round((x[3 * a + 2] - x[3 * b + 2]) * m.inv_boxl[2]);
+}
+// q_dist4(shift, boxlength*q_nint(shift*inv_boxl)) of atoms a and b
+__device__ __forceinline__ double box_d2(const DevModel& m, const double* __restrict__ x, int a, int b) {
+    double r2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        double d = x[3 * a + c] - x[3 * b + c];
+        double t = m.boxl[c] * round(d * m.inv_boxl[c]) - d;
+        r2 += t * t;
+    }
+    return r2;
+}
+// ---- box LRF (the LRF branch of nbpplist_box_lrf, nbpwlist_box_lrf and
+// nbwwlist_box_lrf, src/nonbondene.f90:1910-2055, 2957-3085, 4397-4515, and
+// the shift of lrf_update, 636-643).  A unit pair is classified by the
+// minimum-image distance of its switch atoms; the source's atoms enter the
+// target's moments at x_i - shift, shift = boxlength * nint((x_switch(source)
+// - centre(target)) / boxlength).  In FP32 a lattice index whose fraction lies
+// within 1e-4 of one half (where FP32 and FP64 could round apart) is
+// recomputed in FP64 from the atoms, as are distances within the decision
+// bands.
+__device__ __forceinline__ bool near_half(float t) {
+    float a = fabsf(t);
+    return fabsf(a - truncf(a) - 0.5f) < 1e-4f;
+}
+__device__ __noinline__ bool lrf_pair_box_exact(const DevModel& m, const double* __restrict__ x, int a, int b,
+                                                double rc2, double rl2) {
+    const double r2 = box_d2(m, x, a, b);
+    return r2 > rc2 && r2 <= rl2;
+}
+// target switch atom a, source switch atom b (packed positions)
+__device__ __forceinline__ bool lrf_pair_box(const DevModel& m, float4 pa, float4 pb, const Band& rc, const Band& rl,
+                                             const double* __restrict__ x, int a, int b) {
+    const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+    const float tx = dx * m.inv_boxlf[0], ty = dy * m.inv_boxlf[1], tz = dz * m.inv_boxlf[2];
+    if (near_half(tx) || near_half(ty) || near_half(tz)) return lrf_pair_box_exact(m, x, a, b, rc.c, rl.c);
+    const float ex = m.boxlf[0] * roundf(tx) - dx, ey = m.boxlf[1] * roundf(ty) - dy, ez = m.boxlf[2] * roundf(tz) - dz;
+    const float r2f = ex * ex + ey * ey + ez * ez;
+    if (r2f > rc.hi && r2f < rl.lo) return true;
+    if (r2f < rc.lo || r2f > rl.hi) return false;
+    return lrf_pair_box_exact(m, x, a, b, rc.c, rl.c);
+}
+// lattice shift of source switch atom b against the target centre (FP64 centre
+// cd, packed FP32 centre cf)
+__device__ __noinline__ float3 lrf_shift_exact(const DevModel& m, const double* __restrict__ x, int b,
+                                                const double* __restrict__ cd) {
+    float3 r;
+    r.x = (float)(m.boxl[0] * round((x[3 * b] - cd[0]) * m.inv_boxl[0]));
+    r.y = (float)(m.boxl[1] * round((x[3 * b + 1] - cd[1]) * m.inv_boxl[1]));
+    r.z = (float)(m.boxl[2] * round((x[3 * b + 2] - cd[2]) * m.inv_boxl[2]));
+    return r;
+}
+__device__ __forceinline__ float3 lrf_shift(const DevModel& m, float4 pb, float cx, float cy, float cz,
+                                            const double* __restrict__ x, int b, const double* __restrict__ cd) {
+    const float tx = (pb.x - cx) * m.inv_boxlf[0], ty = (pb.y - cy) * m.inv_boxlf[1], tz = (pb.z - cz) * m.inv_boxlf[2];
+    if (near_half(tx) || near_half(ty) || near_half(tz)) return lrf_shift_exact(m, x, b, cd);
+    return make_float3(m.boxlf[0] * roundf(tx), m.boxlf[1] * roundf(ty), m.boxlf[2] * roundf(tz));
+}
+
 // Mixed form, N-body layout: one thread per target group.  The blocks stage
 // the LRF source groups (the eligible atoms of each charge group, in group
 // order: lrf_gmeta / lrf_goff / lrf_gatom) in shared memory, kLrfGT groups
@@ -963,6 +1028,7 @@ __device__ __forceinline__ void two_sum_fold(float& hi, float& lo, float& p) {
     p = 0.f;
 }
 
+template <bool BOX>
 __global__ void __launch_bounds__(kLrfNB, 10) k_lrf_nbody(DevModel m, const DevState* __restrict__ states, Cut c,
                                                           int nsplit) {
     const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww),
@@ -1016,7 +1082,18 @@ __global__ void __launch_bounds__(kLrfNB, 10) k_lrf_nbody(DevModel m, const DevS
         if (!act) continue;
         for (int gi = 0; gi < ng; ++gi) {
             const int meta = s_meta[gi], s1 = meta & 0x3fffffff;
-            if (s1 != s2 && lrf_pair(r2_f(x2, s_xs[gi]), (meta >> 30) ? rc_s : rc_w, blrf, x, s2, s1)) {
+            const Band& rc2 = (meta >> 30) ? rc_s : rc_w;
+            if (BOX) {
+                if (s1 != s2 && lrf_pair_box(m, x2, s_xs[gi], rc2, blrf, x, s2, s1)) {
+                    const float3 sh = lrf_shift(m, s_xs[gi], ccx, ccy, ccz, x, s1, lrf + (size_t)g2 * kLrfLen);
+                    const float ox = ccx + sh.x, oy = ccy + sh.y, oz = ccz + sh.z;
+                    const int k1 = s_off[gi + 1];
+                    for (int k = s_off[gi]; k < k1; ++k) {
+                        const float4 xi = s_xi[k];
+                        lrf_terms20(xi.x - ox, xi.y - oy, xi.z - oz, xi.w, part);
+                    }
+                }
+            } else if (s1 != s2 && lrf_pair(r2_f(x2, s_xs[gi]), rc2, blrf, x, s2, s1)) {
                 const int k1 = s_off[gi + 1];
                 for (int k = s_off[gi]; k < k1; ++k) {
                     const float4 xi = s_xi[k];
@@ -1059,7 +1136,7 @@ __global__ void k_lrf_combine(DevModel m, const DevState* __restrict__ states, i
 
 // Unstaged variant: one warp per target group reads the source atoms straight
 // from global memory (lanes stride over the atoms, so loads are coalesced).
-template <bool MIX>
+template <bool MIX, bool BOX>
 __global__ void __launch_bounds__(128) k_lrf_accumulate_direct(DevModel m, const DevState* __restrict__ states, Cut c,
                                                          const int* __restrict__ lrf_src) {
     const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww),
@@ -1088,6 +1165,15 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate_direct(DevModel m, const
             int s1 = src & 0x3fffffff;
             if (s1 == s2) continue;   // same group
             const Band& rc2 = (src >> 30) ? rc_s : rc_w;
+            if constexpr (BOX) {   // FP64 minimum image and lattice shift (the FP64 form)
+                static_assert(!MIX, "the mixed form's box LRF is k_lrf_nbody<true>");
+                if (!lrf_pair_box_exact(m, x, s2, s1, rc2.c, blrf.c)) continue;
+                double sx = m.boxl[0] * round((x[3 * s1] - cx) * m.inv_boxl[0]);
+                double sy = m.boxl[1] * round((x[3 * s1 + 1] - cy) * m.inv_boxl[1]);
+                double sz = m.boxl[2] * round((x[3 * s1 + 2] - cz) * m.inv_boxl[2]);
+                lrf_terms<double>(x[3 * i] - cx - sx, x[3 * i + 1] - cy - sy, x[3 * i + 2] - cz - sz, m.crg[i], mom);
+                continue;
+            }
             if (!lrf_pair(r2_f(x2, xq[s1]), rc2, blrf, x, s2, s1)) continue;
             if constexpr (MIX) {
                 float4 xi = xq[i];
@@ -2814,7 +2900,8 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
     }
 }
 
-// nonbond_solvent_internal, src/nonbondene.f90:6082-6154: the listed pairs
+// nonbond_solvent_internal, src/nonbondene.f90:6082-6154 (in a box
+// nonbond_solvent_internal_box, 6158-6228): the listed pairs
 // (offsets in a molecule, nonbnd_solv_int) inside every solvent molecule, for
 // solvents with torsions; q_dist2 and the reference's grouping of dv.  FP64
 // in both forms (a few pairs per molecule); the mixed form accumulates in
@@ -2831,6 +2918,11 @@ __global__ void k_solvent_internal(DevModel m, const DevState* __restrict__ stat
         for (int ip = 0; ip < n; ++ip) {
             int ia = is + ij[ip].x, ib = is + ij[ip].y;
             double tx = x[3 * ib] - x[3 * ia], ty = x[3 * ib + 1] - x[3 * ia + 1], tz = x[3 * ib + 2] - x[3 * ia + 2];
+            if (m.box) {   // nonbond_solvent_internal_box, src/nonbondene.f90:6158-6228: minimum image
+                double sx, sy, sz;
+                box_shift(m, x, ia, ib, sx, sy, sz);
+                tx += sx, ty += sy, tz += sz;
+            }
             double r2 = 1.0 / (tx * tx + ty * ty + tz * tz);
             double r = sqrt(r2);
             double r6 = r2 * r2 * r2;
@@ -3337,7 +3429,8 @@ int launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* l
         // 8 ranges, about 9 waves of resident target threads)
         const int nsplit = std::min(kLrfSplitMax, std::max(1, L.m.nlrf_groups / kLrfGT));
         dim3 g((L.m.ncgp + kLrfNB - 1) / kLrfNB, L.nwin, nsplit);
-        k_lrf_nbody<<<g, kLrfNB, 0, L.st>>>(L.m, L.ds, c, nsplit);
+        if (L.m.box) k_lrf_nbody<true><<<g, kLrfNB, 0, L.st>>>(L.m, L.ds, c, nsplit);
+        else k_lrf_nbody<false><<<g, kLrfNB, 0, L.st>>>(L.m, L.ds, c, nsplit);
         k_lrf_combine<<<dim3((L.m.ncgp + 127) / 128, L.nwin), 128, 0, L.st>>>(L.m, L.ds, nsplit);
         return 2;
     } else if (mixed && QNB_LRF_PAIR)
@@ -3345,7 +3438,10 @@ int launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* l
                             L.st>>>(L.m, L.ds, c, lrf_src);
     else if (mixed) k_lrf_accumulate<true><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
     else if (QNB_LRF_FP64_STAGED) k_lrf_accumulate<false><<<g, kLrfBlock, 0, L.st>>>(L.m, L.ds, c, lrf_src);
-    else k_lrf_accumulate_direct<false><<<grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
+    else if (L.m.box)
+        k_lrf_accumulate_direct<false, true><<<grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin), 128, 0, L.st>>>(
+            L.m, L.ds, c, lrf_src);
+    else k_lrf_accumulate_direct<false, false><<<grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c, lrf_src);
     return 1;
 }
 
@@ -3951,23 +4047,6 @@ void launch_pair_sets(const Launch& L, const PairSetDev& p) {
 // packed coordinates with an FP32 shift (fixed-point sums), as its sphere
 // kernels do.
 // -----------------------------------------------------------------------------
-__device__ __forceinline__ void box_shift(const DevModel& m, const double* __restrict__ x, int a, int b,
-                                          double& sx, double& sy, double& sz) {
-    sx = m.boxl[0] * round((x[3 * a] - x[3 * b]) * m.inv_boxl[0]);
-    sy = m.boxl[1] * round((x[3 * a + 1] - x[3 * b + 1]) * m.inv_boxl[1]);
-    sz = m.boxl[2] * round((x[3 * a + 2] - x[3 * b + 2]) * m.inv_boxl[2]);
-}
-// q_dist4(shift, boxlength*q_nint(shift*inv_boxl)) of atoms a and b
-__device__ __forceinline__ double box_d2(const DevModel& m, const double* __restrict__ x, int a, int b) {
-    double r2 = 0.0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        double d = x[3 * a + c] - x[3 * b + c];
-        double t = m.boxl[c] * round(d * m.inv_boxl[c]) - d;
-        r2 += t * t;
-    }
-    return r2;
-}
 // the mixed form's FP32 pair geometry: packed coordinates (xpcent-centred)
 // and an FP32 shift; vec = shift - (x_i - x_j)
 __device__ __forceinline__ float3 box_shift_f(const DevModel& m, float4 a, float4 b) {

@@ -168,3 +168,16 @@ def lig_w_pbc_step0_coordinates(s, g):
 # the box run's cut-offs (run_test.sh:173-176: q_atom 24, lrf 24; solute and
 # solvent cut-offs at their defaults of 10 A)
 PBC_CUT = dict(Rcq=24.0, RcLRF=24.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
+
+
+def lig_w_pbc_eq1_inputs(s):
+    """eq1.inp with run_test.sh's box settings (tests/basic_tests/run_test.sh:
+    172-176): [PBC] put_solvent_back_in_box on, put_solute_back_in_box off;
+    q_atom 24, lrf 24; otherwise as the sphere run (stepsize 0.1 fs,
+    temperature 0.1 K, bath_coupling 1 fs, separate scaling, non_bond 25); no
+    solvent restraints in a box.  Returns (MdSetup, topology terms, evaluated
+    bonded terms)."""
+    from q6_gb300.md import MdSetup
+    top = lig_w_topology_terms(s)
+    setup = MdSetup(stepsize=0.1, temp0=0.1, tau_t=1.0, separate_scaling=True, nbcycle=25, cut=PBC_CUT)
+    return setup, top, lig_w_bonded(s)

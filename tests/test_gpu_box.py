@@ -3,7 +3,9 @@ against the oracle restatement (oracle/box.py) plus the C oracle's static
 Q-Q lists, in a box small enough that pairs wrap: energies and gradient in
 both forms, several windows at once; moving whole charge groups and waters
 by lattice vectors changes nothing; a short MD run in the box; the
-unsupported combinations fail with QNB_ERR_UNSUPPORTED / QNB_ERR_ARG."""
+unsupported combinations fail with QNB_ERR_UNSUPPORTED / QNB_ERR_ARG.  The
+box LRF, excluded atoms and solvent internal pairs in a box are in
+test_gpu_box_lrf.py."""
 import numpy as np
 import pytest
 
@@ -106,8 +108,11 @@ def test_md_in_box(sysb):
 
 
 def test_box_rejects_unsupported(sysb):
+    import dataclasses
     s = sysb
-    with NonbondedEngine(s, precision=PREC_FP64, use_lrf=True, windows=1) as e:
+    # box LRF is the switch-atom form only (nbpplist_box_lrf, not nbpplis2_box_lrf)
+    with NonbondedEngine(dataclasses.replace(s, iuse_switch_atom=0), precision=PREC_FP64, use_lrf=True,
+                         windows=1) as e:
         with pytest.raises(QnbError):
             e.set_box(BOX)
     with NonbondedEngine(s, precision=PREC_FP64, use_lrf=False, windows=1) as e:
