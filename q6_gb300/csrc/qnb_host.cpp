@@ -509,6 +509,23 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     TRY(c->upload((long long**)&m.sg_key, sg_key));
     TRY(c->upload((int**)&m.sg_off, sg_off));
     TRY(c->upload((int**)&m.sg_ent, sg_ent));
+    {
+        std::vector<std::vector<int2>> per(std::max(1, t->ncgp_solute));
+        for (int k = 0; k < m.nsg; ++k) {
+            int gi = (int)(sg_key[k] / t->ncgp_solute), gj = (int)(sg_key[k] % t->ncgp_solute);
+            per[gi].push_back(make_int2(gj, k));
+            if (gj != gi) per[gj].push_back(make_int2(gi, k));
+        }
+        std::vector<int> off{0};
+        std::vector<int2> ent;
+        for (int g = 0; g < t->ncgp_solute; ++g) {
+            ent.insert(ent.end(), per[g].begin(), per[g].end());
+            off.push_back((int)ent.size());
+        }
+        if (ent.empty()) ent.push_back(make_int2(-1, -1));
+        TRY(c->upload((int**)&m.sgl_off, off));
+        TRY(c->upload((int2**)&m.sgl_ent, ent));
+    }
 
     // LJ tables per code (1..3) and type pair: precompute_set_values_pp's A/B
     std::vector<double2> lj(3 * (size_t)nt * nt);

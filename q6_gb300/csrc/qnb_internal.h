@@ -89,6 +89,10 @@ struct DevModel {
     const long long* sg_key;
     const int* sg_off;          // [nsg+1]
     const int* sg_ent;
+    // per solute group its special group pairs: sgl_ent[sgl_off[g] ..
+    // sgl_off[g+1]) = (partner group, sg index), the group itself included
+    const int* sgl_off;
+    const int2* sgl_ent;
     const double2* lj;          // [3][natyps][natyps] (A,B) per LJ code 1..3
     const float2* ljf;
     const float4* ljpair;       // [natyps][natyps]: (A,B) of ljcod code, (A,B) of code 3

@@ -1028,6 +1028,44 @@ __device__ __forceinline__ void two_sum_fold(float& hi, float& lo, float& p) {
     p = 0.f;
 }
 
+// The 20 moments of lrf_terms20 in packed FP32x2 arithmetic: the source
+// atom's (x, y) and (z, q) arrive as register pairs from the staged float4,
+// and the 20 sums are held as 10 pairs, so 10 FFMA2 replace 20 FFMA.  Each
+// sum gets the same products in the same order as in lrf_terms20.  Slots
+// (lrf_slot):
+// (n1,n2) (n3,n0) (n4,n5) (n6,n9) (n7,n8) (n10,n11) (n12,n19) (n13,n16)
+// (n14,n17) (n15,n18).
+__host__ __device__ constexpr int lrf_slot(int k) {
+    constexpr int t[kLrfMom20] = {1, 2, 3, 0, 4, 5, 6, 9, 7, 8, 10, 11, 12, 19, 13, 16, 14, 17, 15, 18};
+    return t[k];
+}
+__device__ __forceinline__ void lrf_terms20x2(float4 xi, float2 oxy, float2 ozq, float2* n) {
+    const float2 dxy = __fadd2_rn(make_float2(xi.x, xi.y), oxy);   // (dx, dy)
+    const float2 dzq = __fadd2_rn(make_float2(xi.z, xi.w), ozq);   // (dz, q)
+    const float dx = dxy.x, dy = dxy.y, dz = dzq.x, q = dzq.y;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float ri = rsqrtf(r2), ri2 = ri * ri;
+    const float qri = q * ri;
+    const float f0 = qri * ri2;
+    const float f1 = 3.f * f0 * ri2;
+    const float g = -5.f * f1 * ri2;
+    n[0] = __ffma2_rn(dxy, make_float2(-f0, -f0), n[0]);                 // n1 -= dx f0, n2 -= dy f0
+    n[1] = __ffma2_rn(dzq, make_float2(-f0, ri), n[1]);                  // n3 -= dz f0, n0 += q ri
+    const float2 axy = __fmul2_rn(dxy, make_float2(f1, f1));             // (ax, ay)
+    const float az = dz * f1;
+    n[2] = __ffma2_rn(make_float2(axy.x, axy.x), dxy, n[2]);            // n4 += ax dx, n5 += ax dy
+    n[3] = __ffma2_rn(make_float2(axy.x, az), make_float2(dz, dz), n[3]);  // n6 += ax dz, n9 += az dz
+    n[4] = __ffma2_rn(make_float2(axy.y, axy.y), make_float2(dy, dz), n[4]);   // n7 += ay dy, n8 += ay dz
+    const float2 gxy = __fmul2_rn(dxy, make_float2(g, g));               // (gx, gy)
+    const float gz = g * dz;
+    const float2 gxxyy = __fmul2_rn(gxy, dxy);                           // (gxx, gyy)
+    const float gzz = gz * dz, gxy_ = gxy.x * dy;
+    n[5] = __ffma2_rn(make_float2(gxxyy.x, gxxyy.x), dxy, n[5]);         // n10 += gxx dx, n11 += gxx dy
+    n[6] = __ffma2_rn(make_float2(gxxyy.x, gzz), make_float2(dz, dz), n[6]);   // n12 += gxx dz, n19 += gzz dz
+    n[7] = __ffma2_rn(make_float2(gxxyy.y, gxxyy.y), dxy, n[7]);         // n13 += gyy dx, n16 += gyy dy
+    n[8] = __ffma2_rn(make_float2(gxy_, gxxyy.y), make_float2(dz, dz), n[8]);  // n14 += gxy dz, n17 += gyy dz
+    n[9] = __ffma2_rn(make_float2(gzz, gzz), dxy, n[9]);                 // n15 += gzz dx, n18 += gzz dy
+}
 template <bool BOX>
 __global__ void __launch_bounds__(kLrfNB, 10) k_lrf_nbody(DevModel m, const DevState* __restrict__ states, Cut c,
                                                           int nsplit) {
@@ -1059,9 +1097,11 @@ __global__ void __launch_bounds__(kLrfNB, 10) k_lrf_nbody(DevModel m, const DevS
         ccz = (float)(L[2] - m.xpcent[2]);
         x2 = xq[s2];
     }
-    float part[kLrfMom20], hi[kLrfMom20], lo[kLrfMom20];
+    constexpr int NS = kLrfMom20 / 2;   // packed slots (lrf_slot)
+    float2 part[NS], hi[NS], lo[NS];
 #pragma unroll
-    for (int k = 0; k < kLrfMom20; ++k) part[k] = hi[k] = lo[k] = 0.f;
+    for (int k = 0; k < NS; ++k) part[k] = hi[k] = lo[k] = make_float2(0.f, 0.f);
+    const float2 oxy0 = make_float2(-ccx, -ccy), ozq0 = make_float2(-ccz, 0.f);
     // this block's range of source groups (blockIdx.z of nsplit)
     const int gbeg = (int)((int64_t)m.nlrf_groups * blockIdx.z / nsplit);
     const int gend = (int)((int64_t)m.nlrf_groups * (blockIdx.z + 1) / nsplit);
@@ -1086,30 +1126,30 @@ __global__ void __launch_bounds__(kLrfNB, 10) k_lrf_nbody(DevModel m, const DevS
             if (BOX) {
                 if (s1 != s2 && lrf_pair_box(m, x2, s_xs[gi], rc2, blrf, x, s2, s1)) {
                     const float3 sh = lrf_shift(m, s_xs[gi], ccx, ccy, ccz, x, s1, lrf + (size_t)g2 * kLrfLen);
-                    const float ox = ccx + sh.x, oy = ccy + sh.y, oz = ccz + sh.z;
+                    const float2 oxy = make_float2(-(ccx + sh.x), -(ccy + sh.y)), ozq = make_float2(-(ccz + sh.z), 0.f);
                     const int k1 = s_off[gi + 1];
-                    for (int k = s_off[gi]; k < k1; ++k) {
-                        const float4 xi = s_xi[k];
-                        lrf_terms20(xi.x - ox, xi.y - oy, xi.z - oz, xi.w, part);
-                    }
+                    for (int k = s_off[gi]; k < k1; ++k) lrf_terms20x2(s_xi[k], oxy, ozq, part);
                 }
             } else if (s1 != s2 && lrf_pair(r2_f(x2, s_xs[gi]), rc2, blrf, x, s2, s1)) {
                 const int k1 = s_off[gi + 1];
-                for (int k = s_off[gi]; k < k1; ++k) {
-                    const float4 xi = s_xi[k];
-                    lrf_terms20(xi.x - ccx, xi.y - ccy, xi.z - ccz, xi.w, part);
-                }
+                for (int k = s_off[gi]; k < k1; ++k) lrf_terms20x2(s_xi[k], oxy0, ozq0, part);
             }
             if ((gi + 1) % kLrfFold == 0 || gi == ng - 1) {
 #pragma unroll
-                for (int k = 0; k < kLrfMom20; ++k) two_sum_fold(hi[k], lo[k], part[k]);
+                for (int k = 0; k < NS; ++k) {
+                    two_sum_fold(hi[k].x, lo[k].x, part[k].x);
+                    two_sum_fold(hi[k].y, lo[k].y, part[k].y);
+                }
             }
         }
     }
     if (!act) return;
     double tot[kLrfMom20];
 #pragma unroll
-    for (int k = 0; k < kLrfMom20; ++k) tot[k] = (double)hi[k] + (double)lo[k];
+    for (int k = 0; k < NS; ++k) {
+        tot[lrf_slot(2 * k)] = (double)hi[k].x + (double)lo[k].x;
+        tot[lrf_slot(2 * k + 1)] = (double)hi[k].y + (double)lo[k].y;
+    }
     double* out = s.lrf_part + ((size_t)blockIdx.z * m.ncgp + g2) * kLrfMom20;
 #pragma unroll
     for (int k = 0; k < kLrfMom20; ++k) out[k] = tot[k];
@@ -2738,10 +2778,13 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                 Runs R{0, 0, 0};
                 if (CELLS) R = stencil_runs(s.cend_s, G, cell_of(G, xs));
                 const int ncand = CELLS ? R.total : m.ncgp_solute;
-                int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
                 const unsigned long long tmask = m.gtmask[g];
                 uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
                 int* rf = s.row_gf + (size_t)g * s.cap_gf;
+                // the row's special group pairs, one per lane (found by shuffles;
+                // a row with more than 32 falls back to the binary search)
+                const int sl0 = m.sgl_off[g], nsl = m.sgl_off[g + 1] - sl0;
+                const int2 my_sg = lane < nsl ? m.sgl_ent[sl0 + lane] : make_int2(-1, -1);
                 for (int j0 = 0; j0 < ncand; j0 += kWarp) {
                     const int t = j0 + lane;
                     const int bi = CELLS ? run_item(R, t) : 0;
@@ -2756,11 +2799,20 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                             g2 = t;
                             if (!m.excl[m.gsw[g2]]) ok = g2 == g || gg_inside(m, x, xq, g, g2, bpp);
                         }
+                    }
+                    if (nsl <= kWarp) {
+                        for (int c = 0; c < nsl; ++c) {   // warp-uniform
+                            const int eg = __shfl_sync(kFull, my_sg.x, c), es = __shfl_sync(kFull, my_sg.y, c);
+                            if (eg == g2) sgi = es;
+                        }
+                    }
+                    if (t < ncand) {
                         if (ok) {
                             b0 = m.gslot[g2];
                             n2 = m.gslot[g2 + 1] - b0;
-                            sgi = m.nsg ? sg_find(m, g <= g2 ? (long long)g * m.ncgp_solute + g2
-                                                             : (long long)g2 * m.ncgp_solute + g) : -1;
+                            if (nsl > kWarp)
+                                sgi = sg_find(m, g <= g2 ? (long long)g * m.ncgp_solute + g2
+                                                         : (long long)g2 * m.ncgp_solute + g);
                             // the general path: the group itself, group pairs with
                             // excluded / 1-4 atom pairs, and partner types with LJ
                             // code 2 against a row atom; plain code-1 partners otherwise
@@ -2795,16 +2847,19 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                                 ++pf;
                                 continue;
                             }
-                            unsigned mask = 0;
-                            for (int a = 0; a < n1; ++a) {
-                                int i = m.gatom[a0 + a];
-                                int kind = 0;
-                                if (i == j) kind = 1;
-                                else if (sgi >= 0) {
-                                    if (g == g2) kind = i < j ? sg_kind(m, sgi, a, b) : sg_kind(m, sgi, b, a);
-                                    else kind = lower ? sg_kind(m, sgi, a, b) : sg_kind(m, sgi, b, a);
+                            // 2-bit kind per row atom against partner atom b from one
+                            // pass over the group pair's entries (lower group's slot
+                            // sa, upper group's sb; a group's own pairs have i < j,
+                            // so an entry holds for both orders); the atom itself: 1
+                            unsigned mask = g == g2 ? 1u << (2 * b) : 0u;
+                            if (sgi >= 0) {
+                                for (int q = m.sg_off[sgi]; q < m.sg_off[sgi + 1]; ++q) {
+                                    const int e = m.sg_ent[q];
+                                    const int sa = e & 0xff, sb = (e >> 8) & 0xff;
+                                    const unsigned kind = (unsigned)(e >> 16);
+                                    if ((g == g2 || lower) && sb == b) mask |= kind << (2 * sa);
+                                    if ((g == g2 || !lower) && sa == b) mask |= kind << (2 * sb);
                                 }
-                                mask |= (unsigned)kind << (2 * a);
                             }
                             if (m.type_in_entry) mask |= (unsigned)m.iac[j] << 16;
                             if (ps < s.cap_gp) rp[ps] = make_uint2((unsigned)j | (flags << 28), mask);
@@ -2998,15 +3053,51 @@ constexpr int kRowChunk = 128;   // entries per prefetched chunk
 // Resident 128-thread blocks per SM asked of the register allocator: the
 // kernel waits mostly on its gathers, so occupancy pays more than the few
 // spilled registers (6 blocks = 80 registers for groups of up to 6 atoms).
+// Two row atoms against one partner in packed FP32x2 arithmetic (GB300's
+// FFMA2 / FMUL2 / FADD2; one rsqrt per atom on the SFU): the plain code-1
+// pair of the geometric rule, A = fa fj.x and B = fb fj.y.  The row kernels
+// are bound by the latency of each pair's dependent chain, and a packed
+// instruction advances two chains.  n* are the negated row positions, q the
+// row charges; adds the row atoms' gradient into g* and their energies into
+// pel / pvdw.
+__device__ __forceinline__ void pair2_plain(float2 nx, float2 ny, float2 nz, float2 q, float2 fa, float2 fb,
+                                            float2 bx, float2 by, float2 bz, float2 bq, float2 fjx, float2 fjy,
+                                            float2& gx, float2& gy, float2& gz, float2& pel, float2& pvdw) {
+    const float2 tx = __fadd2_rn(bx, nx), ty = __fadd2_rn(by, ny), tz = __fadd2_rn(bz, nz);
+    float2 rr = __fmul2_rn(tx, tx);
+    rr = __ffma2_rn(ty, ty, rr);
+    rr = __ffma2_rn(tz, tz, rr);
+    const float2 ri = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
+    const float2 r2 = __fmul2_rn(ri, ri);
+    const float2 vel = __fmul2_rn(__fmul2_rn(q, bq), ri);
+    const float2 r6 = __fmul2_rn(__fmul2_rn(r2, r2), r2);
+    const float2 va = __fmul2_rn(__fmul2_rn(__fmul2_rn(fa, fjx), r6), r6);
+    const float2 vb = __fmul2_rn(__fmul2_rn(fb, fjy), r6);
+    // -dv = r2 (vel + 12 va - 6 vb); the gradient of the row atom is -t dv
+    float2 t = __ffma2_rn(make_float2(12.f, 12.f), va, vel);
+    t = __ffma2_rn(make_float2(-6.f, -6.f), vb, t);
+    const float2 ndv = __fmul2_rn(r2, t);
+    gx = __ffma2_rn(tx, ndv, gx);
+    gy = __ffma2_rn(ty, ndv, gy);
+    gz = __ffma2_rn(tz, ndv, gz);
+    pel = __fadd2_rn(pel, vel);
+    pvdw = __fadd2_rn(pvdw, __ffma2_rn(make_float2(-1.f, -1.f), vb, va));
+}
+
 #ifndef QNB_ROWS_MIN_BLOCKS
 #define QNB_ROWS_MIN_BLOCKS 0   // 0: the per-size default below
 #endif
-template <int MAXG>
+// resident 128-thread blocks per SM the row kernel is compiled for: the
+// packed plain loop of the geometric rule holds twice the row-atom registers
+// and measured best at 5 (96 registers: 212 us per 51-window R25 step, 226 at
+// 6 blocks, where it spills inside the loop); the scalar loop at 6
+template <int MAXG, bool GEOM>
 constexpr int rows_min_blocks() {
-    return QNB_ROWS_MIN_BLOCKS ? QNB_ROWS_MIN_BLOCKS : (MAXG <= 6 ? 6 : (MAXG <= 8 ? 4 : 1));
+    return QNB_ROWS_MIN_BLOCKS ? QNB_ROWS_MIN_BLOCKS
+                               : (MAXG <= 6 ? (GEOM ? 5 : 6) : (MAXG <= 8 ? 4 : 1));
 }
 template <int MAXG, bool GEOM>
-__global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(DevModel m, const DevState* __restrict__ states) {
+__global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_solute(DevModel m, const DevState* __restrict__ states) {
     extern __shared__ float4 sh_lj[];   // natyps^2 type-pair table (dynamic: only its real size)
     __shared__ __align__(16) uint2 sh_pp[4][2][kRowChunk];   // per warp: double-buffered special pp entries
     __shared__ __align__(16) int sh_pf[4][2][kRowChunk];     // per warp: double-buffered plain pp entries
@@ -3046,7 +3137,9 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
         // per row (row contents do not depend on the grid, so neither do they)
         float rpel = 0.f, rpvdw = 0.f, rwel = 0.f, rwvdw = 0.f;
         // ---- solute partner atoms (nonbond_pp, src/nonbondene.f90:4694-4760):
-        // the special entries (kinds, any LJ code) first, then the plain ones
+        // the special entries (kinds, any LJ code) first, then the water
+        // partners, then the plain solute partners (the hot loop, last, so the
+        // type indices are no longer live in it)
         const uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
         const int* rf = s.row_gf + (size_t)g * s.cap_gf;
         const int* rw = s.row_gw + (size_t)g * s.cap_gw;
@@ -3103,56 +3196,6 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
             cp_async_wait<0>();
             __syncwarp();
         }
-        // plain partners: LJ code 1 with every row atom, no excluded or 1-4
-        // pair; with the geometric rule A and B are the products of the atoms'
-        // FP32 code-1 factors (the type table holds the same products)
-        {
-          float fa[MAXG], fb[MAXG];
-#pragma unroll
-          for (int a = 0; a < MAXG; ++a) {
-              float2 f1 = (GEOM && a < n1) ? m.ljf1[m.gatom[a0 + a]] : make_float2(0.f, 0.f);
-              fa[a] = f1.x;
-              fb[a] = f1.y;
-          }
-          for (int ch = 0; ch < nfchunk; ++ch) {
-            if (ch + 1 < nfchunk) {   // chunk 0 came with the first group
-                fetch_pf(ch + 1);
-                cp_async_commit();
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
-            __syncwarp();
-            const int* buf = sh_pf[wib][ch & 1];
-            const int n = min(kRowChunk, npf - ch * kRowChunk);
-            for (int k = lane; k < n; k += kWarp) {
-              const int j = buf[k];
-              const float4 xb = xq[j];
-              float2 fj = make_float2(0.f, 0.f);
-              int tj = 0;
-              if constexpr (GEOM) fj = m.ljf1[j];
-              else tj = m.iac[j];
-#pragma unroll
-              for (int a = 0; a < MAXG; ++a) {
-                  if (qa[a]) continue;
-                  float A, B;
-                  if constexpr (GEOM) {
-                      A = fa[a] * fj.x;
-                      B = fb[a] * fj.y;
-                  } else {
-                      float4 p = lj(ta[a], tj);
-                      A = p.x;
-                      B = p.y;
-                  }
-                  float vel, vdw;
-                  pair_f(xa[a], xb, A, B, xa[a].w * xb.w, true, f[a][0], f[a][1], f[a][2], vel, vdw);
-                  rpel += vel;
-                  rpvdw += vdw;
-              }
-            }
-            __syncwarp();   // this buffer is refilled two chunks later
-          }
-        }
         // ---- water partners (nonbond_pw, src/nonbondene.f90:4856-4916); energy counted here
         if (m.sa == 3 && m.wlj_mask == 1u) {   // SPC: O with LJ, two LJ-free H; the molecule loaded at once
           const float qo = m.wcrgf[0], qh1 = m.wcrgf[1], qh2 = m.wcrgf[2];
@@ -3199,6 +3242,110 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG>()) k_rows_solute(De
                 }
             }
         }
+        }
+        // plain partners: LJ code 1 with every row atom, no excluded or 1-4
+        // pair; with the geometric rule A and B are the products of the atoms'
+        // FP32 code-1 factors (the type table holds the same products)
+        {
+          // with the geometric rule a Q row atom gets zero charge and LJ
+          // factors here, so its terms are exact zeros (its row gradient is
+          // discarded) and the loop needs no per-atom test
+          float fa[MAXG], fb[MAXG];
+#pragma unroll
+          for (int a = 0; a < MAXG; ++a) {
+              float2 f1 = (GEOM && a < n1 && !qa[a]) ? m.ljf1[m.gatom[a0 + a]] : make_float2(0.f, 0.f);
+              fa[a] = f1.x;
+              fb[a] = f1.y;
+              if (GEOM && qa[a]) xa[a].w = 0.f;
+          }
+          for (int ch = 0; ch < nfchunk; ++ch) {
+            if (ch + 1 < nfchunk) {   // chunk 0 came with the first group
+                fetch_pf(ch + 1);
+                cp_async_commit();
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncwarp();
+            const int* buf = sh_pf[wib][ch & 1];
+            const int n = min(kRowChunk, npf - ch * kRowChunk);
+            // the next entry's partner data is loaded one iteration ahead
+            float4 xbn = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 fjn = make_float2(0.f, 0.f);
+            int tjn = 0;
+            if (lane < n) {
+                const int j = buf[lane];
+                xbn = xq[j];
+                if constexpr (GEOM) fjn = m.ljf1[j];
+                else tjn = m.iac[j];
+            }
+            if constexpr (GEOM) {
+              // row atoms in pairs (2p, 2p + 1); an odd group's last pair has a
+              // dummy atom far away with zero charge and factors
+              constexpr int NP = MAXG / 2;
+              float2 nx[NP], ny[NP], nz[NP], q2[NP], fa2[NP], fb2[NP], gx[NP], gy[NP], gz[NP];
+              float2 pel = make_float2(0.f, 0.f), pvdw = make_float2(0.f, 0.f);
+#pragma unroll
+              for (int p = 0; p < NP; ++p) {
+                  const int a = 2 * p, b = 2 * p + 1;
+                  const bool hb = b < n1;
+                  nx[p] = make_float2(-xa[a].x, hb ? -xa[b].x : -1.0e4f);
+                  ny[p] = make_float2(-xa[a].y, hb ? -xa[b].y : -1.0e4f);
+                  nz[p] = make_float2(-xa[a].z, hb ? -xa[b].z : -1.0e4f);
+                  q2[p] = make_float2(xa[a].w, hb ? xa[b].w : 0.f);
+                  fa2[p] = make_float2(fa[a], hb ? fa[b] : 0.f);
+                  fb2[p] = make_float2(fb[a], hb ? fb[b] : 0.f);
+                  gx[p] = make_float2(f[a][0], f[b][0]);   // the accumulators move into the pairs
+                  gy[p] = make_float2(f[a][1], f[b][1]);
+                  gz[p] = make_float2(f[a][2], f[b][2]);
+              }
+              for (int k = lane; k < n; k += kWarp) {
+                const float4 xb = xbn;
+                const float2 fj = fjn;
+                if (k + kWarp < n) {
+                    const int jn = buf[k + kWarp];
+                    xbn = xq[jn];
+                    fjn = m.ljf1[jn];
+                }
+                const float2 bx = make_float2(xb.x, xb.x), by = make_float2(xb.y, xb.y),
+                             bz = make_float2(xb.z, xb.z), bq = make_float2(xb.w, xb.w),
+                             fjx = make_float2(fj.x, fj.x), fjy = make_float2(fj.y, fj.y);
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    if (2 * p >= n1) break;   // warp-uniform
+                    pair2_plain(nx[p], ny[p], nz[p], q2[p], fa2[p], fb2[p], bx, by, bz, bq, fjx, fjy, gx[p], gy[p],
+                                gz[p], pel, pvdw);
+                }
+              }
+#pragma unroll
+              for (int p = 0; p < NP; ++p) {
+                  f[2 * p][0] = gx[p].x;
+                  f[2 * p][1] = gy[p].x;
+                  f[2 * p][2] = gz[p].x;
+                  f[2 * p + 1][0] = gx[p].y;
+                  f[2 * p + 1][1] = gy[p].y;
+                  f[2 * p + 1][2] = gz[p].y;
+              }
+              rpel += pel.x + pel.y;
+              rpvdw += pvdw.x + pvdw.y;
+            } else {
+              for (int k = lane; k < n; k += kWarp) {
+                const float4 xb = xbn;
+                const int tj = tjn;
+                if (k + kWarp < n) tjn = m.iac[buf[k + kWarp]], xbn = xq[buf[k + kWarp]];
+#pragma unroll
+                for (int a = 0; a < MAXG; ++a) {
+                    if (qa[a]) continue;   // warp-uniform
+                    float4 p = lj(ta[a], tj);
+                    float vel, vdw;
+                    pair_f(xa[a], xb, p.x, p.y, xa[a].w * xb.w, true, f[a][0], f[a][1], f[a][2], vel, vdw);
+                    rpel += vel;
+                    rpvdw += vdw;
+                }
+              }
+            }
+            __syncwarp();   // this buffer is refilled two chunks later
+          }
         }
         __syncwarp();   // sh_pw is refilled by the next row
         // The row owns its atoms' pp and pw gradient and its energies: FP32
