@@ -525,6 +525,32 @@ int build_model(qnb_context* c, const qnb_topology* t) {
         if (ent.empty()) ent.push_back(make_int2(-1, -1));
         TRY(c->upload((int**)&m.sgl_off, off));
         TRY(c->upload((int2**)&m.sgl_ent, ent));
+        // kind masks of both orientations (the entries hold (slot in gl,
+        // slot in gu); a group's own pairs are stored with i < j and hold for
+        // both orders)
+        std::vector<int> moff{0};
+        std::vector<unsigned> mk;
+        for (int k = 0; k < m.nsg; ++k) {
+            int gl = (int)(sg_key[k] / t->ncgp_solute), gu = (int)(sg_key[k] % t->ncgp_solute);
+            int nl = gslot[gl + 1] - gslot[gl], nu = gslot[gu + 1] - gslot[gu];
+            size_t base = mk.size();
+            mk.resize(base + nu + (gl == gu ? 0 : nl), 0u);
+            unsigned* lo = mk.data() + base;           // row gl, partner b of gu
+            unsigned* hi = lo + nu;                    // row gu, partner b of gl
+            if (gl == gu)
+                for (int b = 0; b < nu; ++b) lo[b] |= 1u << (2 * b);
+            for (int q = sg_off[k]; q < sg_off[k + 1]; ++q) {
+                int e = sg_ent[q], sa = e & 0xff, sb = (e >> 8) & 0xff;
+                unsigned kind = (unsigned)(e >> 16);
+                lo[sb] |= kind << (2 * sa);
+                if (gl == gu) lo[sa] |= kind << (2 * sb);
+                else hi[sa] |= kind << (2 * sb);
+            }
+            moff.push_back((int)mk.size());
+        }
+        if (mk.empty()) mk.push_back(0u);
+        TRY(c->upload((int**)&m.sgm_off, moff));
+        TRY(c->upload((unsigned**)&m.sgm, mk));
     }
 
     // LJ tables per code (1..3) and type pair: precompute_set_values_pp's A/B

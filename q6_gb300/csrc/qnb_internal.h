@@ -93,6 +93,12 @@ struct DevModel {
     // sgl_off[g+1]) = (partner group, sg index), the group itself included
     const int* sgl_off;
     const int2* sgl_ent;
+    // per special group pair (lower group gl, upper gu): the 2-bit kinds of
+    // every row atom against each partner atom, sgm[sgm_off[sg] + b] for row gl
+    // and partner b of gu (for gl == gu the atom itself is kind 1), then
+    // sgm[sgm_off[sg] + n(gu) + b] for row gu and partner b of gl
+    const int* sgm_off;
+    const unsigned* sgm;
     const double2* lj;          // [3][natyps][natyps] (A,B) per LJ code 1..3
     const float2* ljf;
     const float4* ljpair;       // [natyps][natyps]: (A,B) of ljcod code, (A,B) of code 3

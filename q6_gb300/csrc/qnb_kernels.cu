@@ -2779,6 +2779,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                 if (CELLS) R = stencil_runs(s.cend_s, G, cell_of(G, xs));
                 const int ncand = CELLS ? R.total : m.ncgp_solute;
                 const unsigned long long tmask = m.gtmask[g];
+                const int n1 = m.gslot[g + 1] - m.gslot[g];
                 uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
                 int* rf = s.row_gf + (size_t)g * s.cap_gf;
                 // the row's special group pairs, one per lane (found by shuffles;
@@ -2847,20 +2848,10 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                                 ++pf;
                                 continue;
                             }
-                            // 2-bit kind per row atom against partner atom b from one
-                            // pass over the group pair's entries (lower group's slot
-                            // sa, upper group's sb; a group's own pairs have i < j,
-                            // so an entry holds for both orders); the atom itself: 1
-                            unsigned mask = g == g2 ? 1u << (2 * b) : 0u;
-                            if (sgi >= 0) {
-                                for (int q = m.sg_off[sgi]; q < m.sg_off[sgi + 1]; ++q) {
-                                    const int e = m.sg_ent[q];
-                                    const int sa = e & 0xff, sb = (e >> 8) & 0xff;
-                                    const unsigned kind = (unsigned)(e >> 16);
-                                    if ((g == g2 || lower) && sb == b) mask |= kind << (2 * sa);
-                                    if ((g == g2 || !lower) && sa == b) mask |= kind << (2 * sb);
-                                }
-                            }
+                            // 2-bit kind per row atom against partner atom b (the
+                            // host's table of the group pair; none: every kind 0)
+                            unsigned mask = g == g2 ? 1u << (2 * b) : 0u;   // the atom itself
+                            if (sgi >= 0) mask = m.sgm[m.sgm_off[sgi] + (lower ? b : n1 + b)];
                             if (m.type_in_entry) mask |= (unsigned)m.iac[j] << 16;
                             if (ps < s.cap_gp) rp[ps] = make_uint2((unsigned)j | (flags << 28), mask);
                             ++ps;
