@@ -525,9 +525,12 @@ def run_e2e(args, s, sp, lams, prec, local, tuning=None):
     (qnb_download_gradient).
 
     Drop-in path (reported beside it): one context per window, as one qdyn
-    process per window holds, through the calls the Fortran shim makes
-    (make_pair_lists, pot_energy_nonbonds, nonbond_qq, restrain_solvent,
-    watpol), each copying x in and the gradient out."""
+    process per window holds, through the calls the Fortran shim makes:
+    make_pair_lists every 25th step and qnb_pot_energy_step (the nonbonded
+    side of pot_energy in one call, one copy of x in and of the gradient out);
+    beside it the same with the four separate entry points (pot_energy_nonbonds,
+    nonbond_qq, restrain_solvent, watpol), each copying x in and the gradient
+    out."""
     import numpy as np
     import torch
     from q6_gb300.qnb import NonbondedEngine
@@ -591,28 +594,44 @@ def run_e2e(args, s, sp, lams, prec, local, tuning=None):
             e.nonbond_qq(xs[w], d, EQ)
             e.restrain_solvent(xs[w], d, 300.0)
             e.watpol(xs[w], d, k)
-    rb1, pl1 = [], []
-    for k in range(k0, k0 + steps):
-        t0 = time.perf_counter()
-        for w, e1 in enumerate(engs):
-            x, d = xs[w], ds[w]
-            d[:] = 0.0
-            if k % NBCYCLE == 0:
-                e1.make_pair_lists(x, **CUT)
-            d, E, EQ = e1.pot_energy_nonbonds(x, d)
-            d, EQ = e1.nonbond_qq(x, d, EQ)
-            e1.restrain_solvent(x, d, 300.0)
-            e1.watpol(x, d, k)
-        (rb1 if k % NBCYCLE == 0 else pl1).append((time.perf_counter() - t0) * 1e3)
+    def drop_in_steps(fused):
+        rb1, pl1 = [], []
+        for k in range(k0, k0 + steps):
+            t0 = time.perf_counter()
+            for w, e1 in enumerate(engs):
+                x, d = xs[w], ds[w]
+                d[:] = 0.0
+                if k % NBCYCLE == 0:
+                    e1.make_pair_lists(x, **CUT)
+                if fused:
+                    e1.pot_energy_step(x, d, Tfree=300.0, istep=k)
+                else:
+                    d, E, EQ = e1.pot_energy_nonbonds(x, d)
+                    d, EQ = e1.nonbond_qq(x, d, EQ)
+                    e1.restrain_solvent(x, d, 300.0)
+                    e1.watpol(x, d, k)
+            (rb1 if k % NBCYCLE == 0 else pl1).append((time.perf_counter() - t0) * 1e3)
+        return rb1, pl1
+
+    rb1, pl1 = drop_in_steps(True)
+    rb2, pl2 = drop_in_steps(False)
     for e1 in engs:
         e1.close()
-    ms1 = amortised_step_ms(rb1, pl1)
+    ms1, ms2 = amortised_step_ms(rb1, pl1), amortised_step_ms(rb2, pl2)
     out["drop_in"] = {"value": round(nw1 / (ms1 / 1e3), 2), "unit": "steps/s", "windows": nw1,
                       "cycle": cycle_summary(rb1, pl1),
-                      "h2d_bytes_per_step": int(s.x.nbytes * (4 + 1.0 / NBCYCLE)),
-                      "d2h_bytes_per_step": int(s.x.nbytes * 4),
-                      "path": "qnb_make_pair_lists/qnb_pot_energy_nonbonds/qnb_nonbond_qq/qnb_restrain_solvent/"
-                              "qnb_watpol with host buffers, one context per window, windows in sequence"}
+                      "h2d_bytes_per_step": int(s.x.nbytes * (1 + 1.0 / NBCYCLE)),
+                      "d2h_bytes_per_step": int(s.x.nbytes),
+                      "path": "qnb_make_pair_lists every 25th step + qnb_pot_energy_step (the nonbonded side of "
+                              "pot_energy in one call) with host buffers, one context per window, windows in "
+                              "sequence",
+                      "separate_calls": {
+                          "value": round(nw1 / (ms2 / 1e3), 2), "unit": "steps/s",
+                          "cycle": cycle_summary(rb2, pl2),
+                          "h2d_bytes_per_step": int(s.x.nbytes * (4 + 1.0 / NBCYCLE)),
+                          "d2h_bytes_per_step": int(s.x.nbytes * 4),
+                          "path": "qnb_pot_energy_nonbonds/qnb_nonbond_qq/qnb_restrain_solvent/qnb_watpol, each "
+                                  "with its own copies and synchronisation"}}
     return out
 
 

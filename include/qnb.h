@@ -316,6 +316,21 @@ int qnb_autotune(qnb_context* ctx, int32_t reps, int32_t* values);
 int qnb_get_tuning(qnb_context* ctx, int32_t* values);
 int qnb_set_tuning(qnb_context* ctx, const int32_t* values);
 
+/* The nonbonded side of one pot_energy call of a single-window context
+   through host buffers, in one call: copies x (natom*3, the caller's memory)
+   in, evaluates what qnb_compute_dev evaluates (pot_energy_nonbonds(md=1),
+   nonbond_qq/qqp, restrain_solvent with Tfree and watpol at istep when
+   solvent parameters are set, and any bonded / restraint / offdiag terms
+   set on the context) as one graph replay, adds the gradient into d and the
+   energies into E, EQ[nstates] and Erst[2] (solvent_radial, water_pol; each
+   may be NULL).  One host synchronisation, where the separate entry points
+   (qnb_pot_energy_nonbonds, qnb_nonbond_qq, qnb_restrain_solvent,
+   qnb_watpol) take one each: src/potene.f90:140-170's nonbonded calls for a
+   shim that makes them back to back on the same coordinates.  Needs the
+   lists of a qnb_make_pair_lists* call; QNB_ERR_ARG for a batched context. */
+int qnb_pot_energy_step(qnb_context* ctx, const double* x, double* d, double Tfree, int32_t istep,
+                        qnb_energies* E, qnb_qenergies* EQ, double* Erst);
+
 /* Energies of the last qnb_compute_dev / qnb_group_compute evaluation of all
    windows, added into E[nwin], EQ[nwin*nstates], Erst[nwin*2] (waits for
    the context's stream). */

@@ -1864,6 +1864,34 @@ int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, q
     return QNB_OK;
 }
 
+int qnb_pot_energy_step(qnb_context* c, const double* x, double* d, double Tfree, int32_t istep, qnb_energies* E,
+                        qnb_qenergies* EQ, double* Erst) {
+    if (!c || !x || !d) return fail(QNB_ERR_ARG, "null argument");
+    if (c->nwin != 1) return fail(QNB_ERR_ARG, "single-window contexts only (batches: qnb_compute_dev)");
+    CU(cudaSetDevice(c->device));
+    if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built");
+    TRY(stage_x(c, x));
+    TRY(run_compute(c, Tfree, istep));   // gradient applied into window 0's FP64 accumulator
+    const size_t n = 3 * (size_t)c->natom;
+    // stream order: the coordinate copy out of h_stage precedes this copy into it
+    CU(cudaMemcpyAsync(c->h_stage, c->st[0].d, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemsetAsync(c->st[0].d, 0, n * sizeof(double), c->stream));
+    CU(cudaMemcpyAsync(c->h_e, c->e_all, sizeof(double) * kNumE, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(c->h_e + (size_t)kNumE * c->nwin, c->efix_all, sizeof(double) * kNumE,
+                       cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    for (size_t k = 0; k < n; ++k) d[k] += c->h_stage[k];
+    const long long* fx = (const long long*)(c->h_e + (size_t)kNumE * c->nwin);
+    double e[kNumE];
+    for (int k = 0; k < kNumE; ++k) e[k] = c->h_e[k] + (double)fx[k] * (1.0 / kFix);
+    add_energies(e, E, EQ, c->S);
+    if (Erst) {
+        Erst[0] += e[E_RST_RAD];
+        Erst[1] += e[E_RST_POL];
+    }
+    return QNB_OK;
+}
+
 int qnb_set_solvent_internal(qnb_context* c, int32_t n, const int32_t* ij, const double* A, const double* B,
                              const double* el) {
     if (!c || n < 0 || (n > 0 && (!ij || !A || !B || !el))) return fail(QNB_ERR_ARG, "null argument");

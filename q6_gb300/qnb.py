@@ -34,7 +34,7 @@ EXPORTED = (
     "qnb_make_pair_lists", "qnb_pot_energy_nonbonds", "qnb_nonbond_qq",
     "qnb_set_solvent_params", "qnb_restrain_solvent", "qnb_watpol", "qnb_get_watpol_state",
     "qnb_list_size", "qnb_export_pairs", "qnb_export_rows", "qnb_get_lrf", "qnb_device_buffers", "qnb_stream",
-    "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_take_launch_count",
+    "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_pot_energy_step", "qnb_take_launch_count",
     "qnb_profile", "qnb_kernel_times", "qnb_create_batch", "qnb_window_count",
     "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
     "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev", "qnb_get_energies_dev", "qnb_set_graphs",
@@ -88,6 +88,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_export_rows": [P, I32, I32, P, P, I64, P],
         "qnb_device_buffers": [P, P, P], "qnb_stream": [P, P],
         "qnb_compute_dev": [P, D, I32, I32, P, P, P], "qnb_take_launch_count": [P, P],
+        "qnb_pot_energy_step": [P, P, P, D, I32, P, P, P],
         "qnb_profile": [P, I32], "qnb_kernel_times": [P, P, P, I32],
         "qnb_create_batch": [P, P, I32, P], "qnb_window_count": [P, P],
         "qnb_set_lambda_window": [P, I32, P], "qnb_upload_coordinates": [P, P],
@@ -271,6 +272,18 @@ class NonbondedEngine:
     def make_pair_lists_dev(self, Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0):
         self._check(self.lib.qnb_make_pair_lists_dev(self.h, Rcq, Rcq ** 2, RcLRF ** 2, Rcpp ** 2,
                                                      Rcpw ** 2, Rcww ** 2))
+
+    def pot_energy_step(self, x, d=None, Tfree=300.0, istep=0):
+        """qnb_pot_energy_step (single-window context): the nonbonded side of
+        one pot_energy call through host buffers.  Returns (d, E, EQ, Erst)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if d is None:
+            d = np.zeros_like(x)
+        E = np.zeros(7)
+        EQ = np.zeros((max(self.S, 1), 6))
+        R = np.zeros(2)
+        self._check(self.lib.qnb_pot_energy_step(self.h, _p(x), _p(d), Tfree, int(istep), _p(E), _p(EQ), _p(R)))
+        return d, dict(zip(E_FIELDS, E)), EQ[: self.S], R
 
     def compute_dev(self, Tfree=300.0, istep=0, sync=True):
         """All windows; returns per-window energies (lists) when sync."""
