@@ -805,8 +805,9 @@ def box_step(args, s, lams, local):
     return {"value": round(nwin * steps / (tot / 1e3), 1), "unit": "window-steps/s",
             "ms_per_step": round(tot / steps, 4), "steps": steps, "windows": nwin, "box_A": L,
             "list_sizes_window0": sizes,
-            "what": "periodic box: minimum-image lists every 25th step + pp/pw/ww/qp/qw box energies (FP32 pair "
-                    "arithmetic, fixed-point sums) + static Q-Q, all windows per launch"}
+            "what": "periodic box: gather rows built every 25th step by periodic cell binning with minimum-image "
+                    "tests; pp/pw/ww on the rows at each unit pair's lattice image, qp/qw box energies, static Q-Q "
+                    "(FP32 pair arithmetic, fixed-point sums), all windows per launch"}
 
 
 def fp64_compare(args, s, sp, lams, local, xs):

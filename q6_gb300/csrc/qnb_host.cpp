@@ -412,6 +412,11 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     TRY(c->upload((int**)&m.gatom, gatom));
     TRY(c->upload((int**)&m.gsw, gsw));
     TRY(c->upload(&c->d_iwhich, iwhich));
+    {   // each atom's unit reference atom (the lattice shifts of the box rows)
+        std::vector<int> swat(natom);
+        for (int i = 0; i < natom; ++i) swat[i] = i < ns ? gsw[iwhich[i]] : ns + sa * ((i - ns) / sa);
+        TRY(c->upload((int**)&m.swat, swat));
+    }
     // lrf_update sources: non-Q atoms (src/nonbondene.f90:658-660); in the
     // sphere only of groups whose distance atom is not excluded (the list
     // builders' excl skips), in the box of every group
@@ -1178,7 +1183,10 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
         }
         timed(c, K_BUILD, [&] {
             if (c->m.box) {
-                launch_build_box(L, cut, c->d_qnear), nl += 3;
+                // the mixed form's box path builds the gather rows (switch
+                // atoms, minimum image); the Q lists keep the box builder
+                if (c->m.box_rows) nl += launch_build_rows(L, cut);
+                launch_build_box(L, cut, c->d_qnear, !c->m.box_rows), nl += c->m.box_rows ? 1 : 3;
             } else if (c->mixed) {
                 nl += launch_build_rows(L, cut);
             } else {
@@ -1227,7 +1235,16 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
     }
     if (c->m.box) {   // periodic box: the *_box routines, src/potene.f90:326-343
         int nb = 0;
-        timed(c, K_PP, [&] { nb = launch_box_nonbond(L, md, mx, c->d_iwhich, c->last_cut.rcq2); });
+        if (c->m.box_rows && md) {   // pp, pw, ww on the gather rows at each unit pair's image
+            if (c->m.natom > c->m.nat_solute) timed(c, K_WW, [&] { launch_rows_water(L); }), ++nl;
+            timed(c, K_PP, [&] {
+                launch_rows_solute(L, c->maxg);
+                launch_row_sums(L);
+            });
+            nl += 2;
+            c->rows_pending = true;
+        }
+        timed(c, K_QW, [&] { nb = launch_box_nonbond(L, md, mx, c->d_iwhich, c->last_cut.rcq2, !c->m.box_rows); });
         // src/potene.f90:326-339 and 373-377: solvent internal pairs, then the LRF Taylor terms
         if (md && c->nsi) timed(c, K_WW, [&] { launch_solvent_internal(L, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
         if (c->use_lrf && md) timed(c, K_LRF_TAYLOR, [&] { launch_lrf_taylor(L, c->d_iwhich, mx); }), ++nl;
@@ -1296,8 +1313,9 @@ void add_energies(const double* e, qnb_energies* E, qnb_qenergies* EQ, int S) {
 // lists; they are built on demand from window 0's build coordinates with the
 // same exact selection as the rows
 int ensure_half_lists(qnb_context* c) {
-    // the box builders already write the half lists in both forms
-    if (!c->mixed || c->m.box || c->diag_valid || !c->lists_built) return QNB_OK;
+    // the FP64 form's builders (and the box builders of the box path without
+    // rows) already write the half lists
+    if (!c->mixed || (c->m.box && !c->m.box_rows) || c->diag_valid || !c->lists_built) return QNB_OK;
     for (int attempt = 0; attempt < 4; ++attempt) {
         DevState tmp = c->st[0];
         tmp.x = c->st[0].x_build;
@@ -1306,9 +1324,13 @@ int ensure_half_lists(qnb_context* c) {
         unsigned keep = ~((1u << C_WW) | (1u << C_PW) | (1u << C_PP) | (1u << C_PP14) | (1u << C_PPG));
         launch_reset_counts(L, keep);
         launch_pack(L);
-        launch_build_pp(L, c->last_cut);
-        launch_build_pw(L, c->last_cut);
-        launch_build_ww(L, c->last_cut);
+        if (c->m.box) {
+            launch_build_box_pairs(L, c->last_cut);
+        } else {
+            launch_build_pp(L, c->last_cut);
+            launch_build_pw(L, c->last_cut);
+            launch_build_ww(L, c->last_cut);
+        }
         TRY(check_launch());
         CU(cudaMemcpyAsync(c->counts.data(), c->cnt_all, sizeof(int) * C_NUM, cudaMemcpyDeviceToHost, c->stream));
         CU(cudaStreamSynchronize(c->stream));
@@ -3207,6 +3229,7 @@ int qnb_set_box(qnb_context* c, const double* boxlength, int32_t qswitch) {
     CU(cudaStreamSynchronize(c->stream));
     if (!boxlength) {
         c->m.box = 0;
+        c->m.box_rows = 0;
         c->m.excl = c->d_excl_top;
         use_lrf_tables(c, 0);
     } else {
@@ -3218,6 +3241,7 @@ int qnb_set_box(qnb_context* c, const double* boxlength, int32_t qswitch) {
             return fail(QNB_ERR_UNSUPPORTED, "LRF with a periodic box needs switch atoms (iuse_switch_atom 1)");
         if (c->have_solv) return fail(QNB_ERR_UNSUPPORTED, "solvent restraints are for the sphere");
         c->m.box = 1;
+        c->m.box_rows = c->mixed && !c->m.any_atom ? 1 : 0;
         c->m.excl = c->d_excl_none;   // the box lists, lrf_taylor and temperature() test no exclusion
         use_lrf_tables(c, 1);
         c->m.qswitch = qswitch;

@@ -145,6 +145,8 @@ struct DevModel {
     int qswitch;
     double boxl[3], inv_boxl[3];
     float boxlf[3], inv_boxlf[3];   // FP32 copies (set on the host)
+    int box_rows;                   // 1: the mixed form's box path runs on the gather rows
+    const int* swat;                // [natom] the reference (switch) atom of the atom's unit
     // FP32 copies are stored relative to xpcent, which bounds their magnitude
     // by the sphere size (FP32 cut-off prefilter and mixed-form pair math)
 };
@@ -163,6 +165,9 @@ struct CellGrid {
     float lox, loy, loz, inv_h;
     int nx, ny, nz, ncell;
 };
+// In a periodic box the grid divides each box edge into n cells (n >= 5, so
+// the +-2 stencil never meets itself across the boundary): a point's cell is
+// trunc(frac(p / L) * n), and the stencil wraps modulo n.
 constexpr int kCellCap = 32768;   // cells per window; a larger extent gets larger cells
 
 // Per-context device state of the lists, coordinates and accumulators.
@@ -273,6 +278,11 @@ void launch_build_qw(const Launch& L, const Cut& c);
 int launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src);
 
 int launch_build_rows(const Launch& L, const Cut& c);
+// cells per box edge for the periodic row build (0: too few cells, the rows
+// take every candidate)
+int box_cells(const DevModel& m, const Cut& c, int* n);
+// the box half lists for inspection (pp group pairs expanded, pw, ww)
+void launch_build_box_pairs(const Launch& L, const Cut& c);
 void launch_rows_solute(const Launch& L, int maxg);
 void launch_rows_water(const Launch& L);
 void launch_ww(const Launch& L, int mixed);
@@ -377,8 +387,8 @@ void launch_pair_sets(const Launch& L, const PairSetDev& p);
 // periodic box: list builds (pp, pw, ww, qp, qw) with minimum-image tests and
 // the box energy kernels (nonbond_*_box); FP64 pair arithmetic in the FP64
 // form, FP32 in the mixed form
-void launch_build_box(const Launch& L, const Cut& c, const uint8_t* qnear);
-int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, double rcq2);
+void launch_build_box(const Launch& L, const Cut& c, const uint8_t* qnear, int pairs);
+int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, double rcq2, int pairs);
 // fix_shell: flag bit 0 excluded (fk_fix), bit 1 shell (fk_pshell); xtop [natom*3]
 void launch_fix_shell(const Launch& L, const uint8_t* flags, const double* xtop, double fk_fix, double fk_pshell,
                       int mixed, int freeze, double* v);

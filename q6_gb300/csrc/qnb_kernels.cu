@@ -2589,6 +2589,25 @@ __device__ __forceinline__ int row_append(int* __restrict__ row, int cap, int co
     return count + __popc(b);
 }
 
+// minimum-image test of a unit pair's reference atoms (a, b) against a
+// cut-off band: FP32 from the packed positions unless a lattice index lies
+// near one half or the distance inside the band, FP64 (box_d2) otherwise
+__device__ __noinline__ bool within_box_exact(const DevModel& m, const double* __restrict__ x, int a, int b,
+                                              double c) {
+    return box_d2(m, x, a, b) <= c;
+}
+__device__ __forceinline__ bool within_box(const DevModel& m, float4 pa, float4 pb, const Band& rc,
+                                           const double* __restrict__ x, int a, int b) {
+    const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+    const float tx = dx * m.inv_boxlf[0], ty = dy * m.inv_boxlf[1], tz = dz * m.inv_boxlf[2];
+    if (near_half(tx) || near_half(ty) || near_half(tz)) return within_box_exact(m, x, a, b, rc.c);
+    const float ex = m.boxlf[0] * roundf(tx) - dx, ey = m.boxlf[1] * roundf(ty) - dy, ez = m.boxlf[2] * roundf(tz) - dz;
+    const float r2f = ex * ex + ey * ey + ez * ez;
+    if (r2f < rc.lo) return true;
+    if (r2f > rc.hi) return false;
+    return within_box_exact(m, x, a, b, rc.c);
+}
+
 // ---- cell grid of the row build -------------------------------------------
 // The reference bins atoms for its neighbour search in populate_grids
 // (src/nonbondene.f90:6264-6460, under USE_GRID).  Here one block per window
@@ -2606,13 +2625,28 @@ __device__ __forceinline__ int3 cell_of(const CellGrid& G, float4 p) {
                      cell_coord(p.z, G.loz, G.inv_h, G.nz));
 }
 __device__ __forceinline__ int cell_index(const CellGrid& G, int3 c) { return (c.z * G.ny + c.y) * G.nx + c.x; }
+// periodic box: the cell of a point's fractional position (clamped in FP32: a
+// NaN lands in cell 0)
+__device__ __forceinline__ int pcell_coord(float p, float inv_l, int n) {
+    float f = p * inv_l;
+    f -= floorf(f);
+    return (int)fminf(fmaxf(f * (float)n, 0.0f), (float)(n - 1));
+}
+template <bool BOX>
+__device__ __forceinline__ int3 cell_at(const DevModel& m, const CellGrid& G, float4 p) {
+    if (BOX)
+        return make_int3(pcell_coord(p.x, m.inv_boxlf[0], G.nx), pcell_coord(p.y, m.inv_boxlf[1], G.ny),
+                         pcell_coord(p.z, m.inv_boxlf[2], G.nz));
+    return cell_of(G, p);
+}
 
 // distance atom of binned item t: solute groups first, then waters
 __device__ __forceinline__ int bin_atom(const DevModel& m, int t) {
     return t < m.ncgp_solute ? m.gsw[t] : m.nat_solute + m.sa * (t - m.ncgp_solute);
 }
 
-__global__ void __launch_bounds__(1024) k_bin_cells(DevModel m, const DevState* __restrict__ states, float inv_h0) {
+__global__ void __launch_bounds__(1024) k_bin_cells(DevModel m, const DevState* __restrict__ states, float inv_h0,
+                                                    int3 boxn) {
     const DevState& s = states[blockIdx.x];
     const float4* __restrict__ xq = s.xq;
     const int ng = m.ncgp_solute, n = ng + m.nwat;
@@ -2637,7 +2671,10 @@ __global__ void __launch_bounds__(1024) k_bin_cells(DevModel m, const DevState* 
     if (lane == 0)
         for (int k = 0; k < 3; ++k) red[k][warp] = lo[k], red[3 + k][warp] = hi[k];
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && boxn.x > 0) {   // periodic box: n cells per edge, set on the host
+        G = CellGrid{0.f, 0.f, 0.f, 0.f, boxn.x, boxn.y, boxn.z, boxn.x * boxn.y * boxn.z};
+        *s.grid = G;
+    } else if (threadIdx.x == 0) {
         for (int w = 1; w < nw; ++w)
             for (int k = 0; k < 3; ++k) red[k][0] = fminf(red[k][0], red[k][w]), red[3 + k][0] = fmaxf(red[3 + k][0], red[3 + k][w]);
         float l[3], e[3];
@@ -2665,7 +2702,8 @@ __global__ void __launch_bounds__(1024) k_bin_cells(DevModel m, const DevState* 
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
         int a = bin_atom(m, t);
         if (m.excl[a]) continue;
-        atomicAdd((t < ng ? s.cend_s : s.cend_w) + cell_index(g, cell_of(g, xq[a])), 1);
+        const int3 cc = boxn.x > 0 ? cell_at<true>(m, g, xq[a]) : cell_of(g, xq[a]);
+        atomicAdd((t < ng ? s.cend_s : s.cend_w) + cell_index(g, cc), 1);
     }
     __syncthreads();
     // exclusive scan of the counts, in place, both grids
@@ -2687,7 +2725,7 @@ __global__ void __launch_bounds__(1024) k_bin_cells(DevModel m, const DevState* 
         int a = bin_atom(m, t);
         if (m.excl[a]) continue;
         float4 p = xq[a];
-        int c = cell_index(g, cell_of(g, p));
+        int c = cell_index(g, boxn.x > 0 ? cell_at<true>(m, g, p) : cell_of(g, p));
         bool sol = t < ng;
         int pos = atomicAdd((sol ? s.cend_s : s.cend_w) + c, 1);
         p.w = __int_as_float(sol ? t : t - ng);
@@ -2721,13 +2759,26 @@ __global__ void __launch_bounds__(1024) k_bin_cells(DevModel m, const DevState* 
 struct Runs {
     int st, pre, total;
 };
-__device__ __forceinline__ Runs stencil_runs(const int* __restrict__ cend, const CellGrid& G, int3 c) {
+// In a periodic box y and z wrap modulo n, and an x-run that crosses the
+// boundary is split: seg 0 holds the part inside [0, nx), seg 1 the part
+// wrapped to the other side (empty for runs that do not cross).
+template <bool BOX>
+__device__ __forceinline__ Runs stencil_runs(const int* __restrict__ cend, const CellGrid& G, int3 c, int seg = 0) {
     const int lane = threadIdx.x & 31;
     int st = 0, len = 0;
     if (lane < 25) {
         int y = c.y + lane % 5 - 2, z = c.z + lane / 5 - 2;
-        if (y >= 0 && y < G.ny && z >= 0 && z < G.nz) {
-            int x0 = max(c.x - 2, 0), x1 = min(c.x + 2, G.nx - 1);
+        int x0 = max(c.x - 2, 0), x1 = min(c.x + 2, G.nx - 1);
+        if (BOX) {
+            y = (y + G.ny) % G.ny;
+            z = (z + G.nz) % G.nz;
+            if (seg == 1) {   // the wrapped part, if any (nx >= 5: at most one side wraps)
+                if (c.x - 2 < 0) x0 = c.x - 2 + G.nx, x1 = G.nx - 1;
+                else if (c.x + 2 >= G.nx) x0 = 0, x1 = c.x + 2 - G.nx;
+                else x0 = 1, x1 = 0;   // empty
+            }
+        }
+        if (y >= 0 && y < G.ny && z >= 0 && z < G.nz && x0 <= x1) {
             int c0 = (z * G.ny + y) * G.nx + x0;
             st = c0 ? cend[c0 - 1] : 0;
             len = cend[c0 + x1 - x0] - st;
@@ -2759,8 +2810,9 @@ __device__ __forceinline__ int run_item(const Runs& R, int t) {
 // tests); otherwise every group and water is a candidate (any-atom tests).
 // The inside tests are the same in both: the FP32 distance of the packed
 // positions, the FP64 distance within the decision band.
-template <bool CELLS>
+template <bool CELLS, bool BOX>
 __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cut c) {
+    constexpr int NSEG = CELLS && BOX ? 2 : 1;   // a periodic stencil's wrapped x-runs come second
     const Band bpp = band(c.rcpp2, c.fpp), bpw = band(c.rcpw2, c.fpw), bww = band(c.rcww2, c.fww);
     const DevState& s = states[blockIdx.y];
     const double* __restrict__ x = s.x;
@@ -2776,8 +2828,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
             if (!m.excl[is]) {
                 const float4 xs = xq[is];
                 Runs R{0, 0, 0};
-                if (CELLS) R = stencil_runs(s.cend_s, G, cell_of(G, xs));
-                const int ncand = CELLS ? R.total : m.ncgp_solute;
+                const int3 cs = CELLS ? cell_at<BOX>(m, G, xs) : make_int3(0, 0, 0);
                 const unsigned long long tmask = m.gtmask[g];
                 const int n1 = m.gslot[g + 1] - m.gslot[g];
                 uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
@@ -2786,6 +2837,9 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                 // a row with more than 32 falls back to the binary search)
                 const int sl0 = m.sgl_off[g], nsl = m.sgl_off[g + 1] - sl0;
                 const int2 my_sg = lane < nsl ? m.sgl_ent[sl0 + lane] : make_int2(-1, -1);
+                for (int seg = 0; seg < NSEG; ++seg) {
+                if (CELLS) R = stencil_runs<BOX>(s.cend_s, G, cs, seg);
+                const int ncand = CELLS ? R.total : m.ncgp_solute;
                 for (int j0 = 0; j0 < ncand; j0 += kWarp) {
                     const int t = j0 + lane;
                     const int bi = CELLS ? run_item(R, t) : 0;
@@ -2795,7 +2849,11 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                         if (CELLS) {
                             float4 it = s.bin_s[bi];
                             g2 = __float_as_int(it.w);
-                            ok = g2 == g || within(r2_f(xs, it), bpp, x, is, m.gsw[g2]);
+                            ok = g2 == g || (BOX ? within_box(m, xs, it, bpp, x, is, m.gsw[g2])
+                                                 : within(r2_f(xs, it), bpp, x, is, m.gsw[g2]));
+                        } else if (BOX) {
+                            g2 = t;
+                            ok = g2 == g || within_box(m, xs, xq[m.gsw[g2]], bpp, x, is, m.gsw[g2]);
                         } else {
                             g2 = t;
                             if (!m.excl[m.gsw[g2]]) ok = g2 == g || gg_inside(m, x, xq, g, g2, bpp);
@@ -2860,9 +2918,11 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                     npp += total & 0xffff;
                     npf += total >> 16;
                 }
-                if (CELLS) R = stencil_runs(s.cend_w, G, cell_of(G, xs));
-                const int ncw = CELLS ? R.total : m.nwat;
+                }
                 int* rw = s.row_gw + (size_t)g * s.cap_gw;
+                for (int seg = 0; seg < NSEG; ++seg) {
+                if (CELLS) R = stencil_runs<BOX>(s.cend_w, G, cs, seg);
+                const int ncw = CELLS ? R.total : m.nwat;
                 for (int j0 = 0; j0 < ncw; j0 += kWarp) {
                     const int t = j0 + lane;
                     const int bi = CELLS ? run_item(R, t) : 0;
@@ -2872,13 +2932,18 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                         if (CELLS) {
                             float4 it = s.bin_w[bi];
                             jw = __float_as_int(it.w);
-                            ok = within(r2_f(xs, it), bpw, x, is, m.nat_solute + m.sa * jw);
+                            const int jo = m.nat_solute + m.sa * jw;
+                            ok = BOX ? within_box(m, xs, it, bpw, x, is, jo) : within(r2_f(xs, it), bpw, x, is, jo);
+                        } else if (BOX) {
+                            const int jo = m.nat_solute + m.sa * jw;
+                            ok = within_box(m, xs, xq[jo], bpw, x, is, jo);
                         } else {
                             int jo = m.nat_solute + m.sa * jw;
                             if (!m.excl[jo]) ok = gw_inside(m, x, xq, g, jo, bpw);
                         }
                     }
                     npw = row_append(rw, s.cap_gw, npw, ok, jw);
+                }
                 }
             }
             if (lane == 0) {
@@ -2895,9 +2960,11 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
             if (!m.excl[io]) {
                 const float4 xi = xq[io];
                 Runs R{0, 0, 0};
-                if (CELLS) R = stencil_runs(s.cend_w, G, cell_of(G, xi));
-                const int ncw = CELLS ? R.total : m.nwat;
+                const int3 ci = CELLS ? cell_at<BOX>(m, G, xi) : make_int3(0, 0, 0);
                 int* rw = s.row_ww + (size_t)w * s.cap_rww;
+                for (int seg = 0; seg < NSEG; ++seg) {
+                if (CELLS) R = stencil_runs<BOX>(s.cend_w, G, ci, seg);
+                const int ncw = CELLS ? R.total : m.nwat;
                 for (int j0 = 0; j0 < ncw; j0 += kWarp) {
                     const int t = j0 + lane;
                     const int bi = CELLS ? run_item(R, t) : 0;
@@ -2907,17 +2974,22 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                         if (CELLS) {
                             float4 it = s.bin_w[bi];
                             jw = __float_as_int(it.w);
-                            ok = jw != w && within(r2_f(xi, it), bww, x, io, m.nat_solute + m.sa * jw);
+                            const int jo = m.nat_solute + m.sa * jw;
+                            ok = jw != w && (BOX ? within_box(m, xi, it, bww, x, io, jo)
+                                                 : within(r2_f(xi, it), bww, x, io, jo));
                         } else if (jw != w) {
                             int jo = m.nat_solute + m.sa * jw;
-                            if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), bww, x, io, jo);
+                            if (BOX) ok = within_box(m, xi, xq[jo], bww, x, io, jo);
+                            else if (!m.excl[jo]) ok = within(r2_f(xi, xq[jo]), bww, x, io, jo);
                         }
                     }
                     nww = row_append(rw, s.cap_rww, nww, ok, jw);
                 }
-                if (CELLS) R = stencil_runs(s.cend_s, G, cell_of(G, xi));
-                const int ncg = CELLS ? R.total : m.ncgp_solute;
+                }
                 int* rg = s.row_wg + (size_t)w * s.cap_wg;
+                for (int seg = 0; seg < NSEG; ++seg) {
+                if (CELLS) R = stencil_runs<BOX>(s.cend_s, G, ci, seg);
+                const int ncg = CELLS ? R.total : m.ncgp_solute;
                 for (int j0 = 0; j0 < ncg; j0 += kWarp) {
                     const int t = j0 + lane;
                     const int bi = CELLS ? run_item(R, t) : 0;
@@ -2928,12 +3000,16 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                         if (CELLS) {
                             float4 it = s.bin_s[bi];
                             g = __float_as_int(it.w);
-                            ok = within(r2_f(it, xi), bpw, x, m.gsw[g], io);
+                            ok = BOX ? within_box(m, it, xi, bpw, x, m.gsw[g], io)
+                                     : within(r2_f(it, xi), bpw, x, m.gsw[g], io);
+                        } else if (BOX) {
+                            ok = within_box(m, xq[m.gsw[g]], xi, bpw, x, m.gsw[g], io);
                         } else if (!m.excl[m.gsw[g]]) {
                             ok = gw_inside(m, x, xq, g, io, bpw);
                         }
                     }
                     nwg = row_append(rg, s.cap_wg, nwg, ok, g);
+                }
                 }
             }
             if (lane == 0) {
@@ -3075,6 +3151,18 @@ __device__ __forceinline__ void pair2_plain(float2 nx, float2 ny, float2 nz, flo
     pvdw = __fadd2_rn(pvdw, __ffma2_rn(make_float2(-1.f, -1.f), vb, va));
 }
 
+// periodic box: partner position p at the image of its unit's reference
+// atom ref_p nearest the row's reference atom ref_row, p + boxlength *
+// nint((ref_row - ref_p) / boxlength) in FP32 (the unit pair's shift of the
+// *_box energy routines; for a listed pair the lattice index is never near a
+// half, since the reference atoms are within a cut-off below half a box)
+__device__ __forceinline__ float4 at_image(const DevModel& m, float4 p, float4 ref_row, float4 ref_p) {
+    p.x += m.boxlf[0] * roundf((ref_row.x - ref_p.x) * m.inv_boxlf[0]);
+    p.y += m.boxlf[1] * roundf((ref_row.y - ref_p.y) * m.inv_boxlf[1]);
+    p.z += m.boxlf[2] * roundf((ref_row.z - ref_p.z) * m.inv_boxlf[2]);
+    return p;
+}
+
 #ifndef QNB_ROWS_MIN_BLOCKS
 #define QNB_ROWS_MIN_BLOCKS 0   // 0: the per-size default below
 #endif
@@ -3087,7 +3175,7 @@ constexpr int rows_min_blocks() {
     return QNB_ROWS_MIN_BLOCKS ? QNB_ROWS_MIN_BLOCKS
                                : (MAXG <= 6 ? (GEOM ? 5 : 6) : (MAXG <= 8 ? 4 : 1));
 }
-template <int MAXG, bool GEOM>
+template <int MAXG, bool GEOM, bool BOX>
 __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_solute(DevModel m, const DevState* __restrict__ states) {
     extern __shared__ float4 sh_lj[];   // natyps^2 type-pair table (dynamic: only its real size)
     __shared__ __align__(16) uint2 sh_pp[4][2][kRowChunk];   // per warp: double-buffered special pp entries
@@ -3106,6 +3194,8 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
     for (int g = warp_id_global(); g < m.ncgp_solute; g += warps_total()) {
         int npp = s.cnt_gp[g], npw = s.cnt_gw[g];   // an empty row still writes its zeros
         int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
+        // periodic box: the row group's reference atom (its lattice shifts)
+        const float4 xsw = BOX ? xq[m.gsw[g]] : make_float4(0.f, 0.f, 0.f, 0.f);
         int ta[MAXG];
         float4 xa[MAXG];
         bool qa[MAXG];
@@ -3163,6 +3253,7 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
             uint2 e = buf[k];
             int j = (int)(e.x & 0x0fffffffu);
             float4 xb = xq[j];
+            if (BOX) xb = at_image(m, xb, xsw, xq[m.swat[j]]);
             int tj = kTypeInEntry ? (int)(e.y >> 16) : m.iac[j];
             const unsigned kinds = kTypeInEntry ? (e.y & 0xffffu) : e.y;
 #pragma unroll
@@ -3194,6 +3285,10 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
           for (int k = lane; k < npw; k += kWarp) {
             int j0 = m.nat_solute + 3 * (k < kRowChunk ? sh_pw[wib][k] : rw[k]);
             float4 xo = xq[j0], xh1 = xq[j0 + 1], xh2 = xq[j0 + 2];
+            if (BOX) {
+                const float4 xr = xo;
+                xo = at_image(m, xo, xsw, xr), xh1 = at_image(m, xh1, xsw, xr), xh2 = at_image(m, xh2, xsw, xr);
+            }
 #pragma unroll
             for (int a = 0; a < MAXG; ++a) {
                 if (qa[a]) continue;
@@ -3209,8 +3304,10 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
         } else {
         for (int k = lane; k < npw; k += kWarp) {
             int j0 = m.nat_solute + m.sa * (k < kRowChunk ? sh_pw[wib][k] : rw[k]);
+            const float4 xr = BOX ? xq[j0] : make_float4(0.f, 0.f, 0.f, 0.f);
             for (int b = 0; b < m.sa; ++b) {
                 float4 xb = xq[j0 + b];
+                if (BOX) xb = at_image(m, xb, xsw, xr);
                 int tw = m.wtype[b];
                 if ((m.wlj_mask >> b) & 1u) {
 #pragma unroll
@@ -3267,6 +3364,7 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
             if (lane < n) {
                 const int j = buf[lane];
                 xbn = xq[j];
+                if (BOX) xbn = at_image(m, xbn, xsw, xq[m.swat[j]]);
                 if constexpr (GEOM) fjn = m.ljf1[j];
                 else tjn = m.iac[j];
             }
@@ -3296,6 +3394,7 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
                 if (k + kWarp < n) {
                     const int jn = buf[k + kWarp];
                     xbn = xq[jn];
+                    if (BOX) xbn = at_image(m, xbn, xsw, xq[m.swat[jn]]);
                     fjn = m.ljf1[jn];
                 }
                 const float2 bx = make_float2(xb.x, xb.x), by = make_float2(xb.y, xb.y),
@@ -3323,7 +3422,12 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
               for (int k = lane; k < n; k += kWarp) {
                 const float4 xb = xbn;
                 const int tj = tjn;
-                if (k + kWarp < n) tjn = m.iac[buf[k + kWarp]], xbn = xq[buf[k + kWarp]];
+                if (k + kWarp < n) {
+                    const int jn = buf[k + kWarp];
+                    tjn = m.iac[jn];
+                    xbn = xq[jn];
+                    if (BOX) xbn = at_image(m, xbn, xsw, xq[m.swat[jn]]);
+                }
 #pragma unroll
                 for (int a = 0; a < MAXG; ++a) {
                     if (qa[a]) continue;   // warp-uniform
@@ -3362,7 +3466,7 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
 
 // water rows: ww (waters, SPC fast path as nonbond_ww_spc) and wp (solute
 // groups) gradient of the water's atoms
-template <bool SPC>
+template <bool SPC, bool BOX>
 __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevState* __restrict__ states) {
     extern __shared__ float4 sh_lj[];   // natyps^2 type-pair table (dynamic: only its real size)
     __shared__ __align__(16) int sh_ww[4][2][kRowChunk];   // per warp: double-buffered ww entries
@@ -3409,10 +3513,12 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
             int w2 = buf[k];
             int j0 = m.nat_solute + sa * w2;
             float pel = 0.f, pvdw = 0.f;
+            const float4 xr = BOX ? xq[j0] : make_float4(0.f, 0.f, 0.f, 0.f);   // partner's first atom
 #pragma unroll
             for (int b = 0; b < kMaxSolv; ++b) {
                 if (b >= sa) break;
                 float4 xb = xq[j0 + b];
+                if (BOX) xb = at_image(m, xb, xa[0], xr);
 #pragma unroll
                 for (int a = 0; a < kMaxSolv; ++a) {
                     if (a >= sa) break;
@@ -3437,10 +3543,12 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
         }
         for (int k = lane; k < nwg; k += kWarp) {
             int g = k < kRowChunk ? sh_wg[wib][k] : rg[k];
+            const float4 xr = BOX ? xq[m.gsw[g]] : make_float4(0.f, 0.f, 0.f, 0.f);   // group's switch atom
             for (int bb = m.gslot[g]; bb < m.gslot[g + 1]; ++bb) {
                 int j = m.gatom[bb];
                 if (m.iqatom[j] >= 0) continue;
                 float4 xb = xq[j];
+                if (BOX) xb = at_image(m, xb, xa[0], xr);
                 int tj = m.iac[j];
 #pragma unroll
                 for (int a = 0; a < kMaxSolv; ++a) {
@@ -3583,20 +3691,41 @@ int launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* l
     return 1;
 }
 
+// cells of half the largest cut-off plus a margin far above the FP32 rounding
+// of the packed positions (a few 1e-6 A)
+static double cell_edge(const Cut& c) {
+    double rc = std::sqrt(std::max(c.rcpp2, std::max(c.rcpw2, c.rcww2)));
+    return 0.5 * (rc + std::max(0.01, 1e-4 * rc));
+}
+int box_cells(const DevModel& m, const Cut& c, int* n) {
+    const double h = cell_edge(c);
+    for (int k = 0; k < 3; ++k) n[k] = (int)std::min(1.0e6, m.boxl[k] / h);
+    while ((int64_t)n[0] * n[1] * n[2] > kCellCap) {   // fewer, larger cells
+        int k = n[0] >= n[1] && n[0] >= n[2] ? 0 : (n[1] >= n[2] ? 1 : 2);
+        --n[k];
+    }
+    return n[0] >= 5 && n[1] >= 5 && n[2] >= 5;
+}
 int launch_build_rows(const Launch& L, const Cut& c) {
     int nrows = L.m.ncgp_solute + L.m.nwat;
     if (nrows == 0) return 0;
     dim3 g = grid_for((int64_t)nrows * 32, 128, L.tu.v[T_BUILD], L.nwin);
+    if (L.m.box) {   // periodic box (switch atoms): minimum-image tests, wrapped stencil
+        int n[3];
+        if (!box_cells(L.m, c, n)) {   // fewer than 5 cells per edge: every unit is a candidate
+            k_build_rows<false, true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+            return 1;
+        }
+        k_bin_cells<<<L.nwin, 1024, 0, L.st>>>(L.m, L.ds, 0.f, make_int3(n[0], n[1], n[2]));
+        k_build_rows<true, true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+        return 2;
+    }
     if (L.m.any_atom) {   // any-atom group tests: every group and water is a candidate
-        k_build_rows<false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+        k_build_rows<false, false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
         return 1;
     }
-    // cells of half the largest cut-off plus a margin far above the FP32
-    // rounding of the packed positions (a few 1e-6 A)
-    double rc = std::sqrt(std::max(c.rcpp2, std::max(c.rcpw2, c.rcww2)));
-    double h = 0.5 * (rc + std::max(0.01, 1e-4 * rc));
-    k_bin_cells<<<L.nwin, 1024, 0, L.st>>>(L.m, L.ds, (float)(1.0 / h));
-    k_build_rows<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
+    k_bin_cells<<<L.nwin, 1024, 0, L.st>>>(L.m, L.ds, (float)(1.0 / cell_edge(c)), make_int3(0, 0, 0));
+    k_build_rows<true, false><<<g, 128, 0, L.st>>>(L.m, L.ds, c);
     return 2;
 }
 int lj_smem(const DevModel& m) {
@@ -3606,13 +3735,15 @@ void launch_rows_solute(const Launch& L, int maxg) {
     if (L.m.ncgp_solute == 0) return;
     dim3 g = grid_for((int64_t)L.m.ncgp_solute * 32, 128, L.tu.v[T_ROWS_SOLUTE], L.nwin);
     int sm = lj_smem(L.m);
-#define RS(MG, GE) k_rows_solute<MG, GE><<<g, 128, sm, L.st>>>(L.m, L.ds)
+#define RS(MG, GE, BX) k_rows_solute<MG, GE, BX><<<g, 128, sm, L.st>>>(L.m, L.ds)
+#define RSB(MG, GE) do { if (L.m.box) RS(MG, GE, true); else RS(MG, GE, false); } while (0)
     if (L.m.geom) {
-        if (maxg <= 4) RS(4, true); else if (maxg <= 6) RS(6, true); else if (maxg <= 8) RS(8, true); else RS(16, true);
+        if (maxg <= 4) RSB(4, true); else if (maxg <= 6) RSB(6, true); else if (maxg <= 8) RSB(8, true); else RSB(16, true);
     } else {
-        if (maxg <= 4) RS(4, false); else if (maxg <= 6) RS(6, false); else if (maxg <= 8) RS(8, false);
-        else RS(16, false);
+        if (maxg <= 4) RSB(4, false); else if (maxg <= 6) RSB(6, false); else if (maxg <= 8) RSB(8, false);
+        else RSB(16, false);
     }
+#undef RSB
 #undef RS
 }
 void launch_solvent_internal(const Launch& L, const int2* ij, const double* par, int n, int mixed) {
@@ -3625,8 +3756,11 @@ void launch_rows_water(const Launch& L) {
     if (L.m.nwat == 0) return;
     dim3 g = grid_for((int64_t)L.m.nwat * 32, 128, L.tu.v[T_ROWS_WATER], L.nwin);
     int sm = lj_smem(L.m);
-    if (L.m.spc) k_rows_water<true><<<g, 128, sm, L.st>>>(L.m, L.ds);
-    else k_rows_water<false><<<g, 128, sm, L.st>>>(L.m, L.ds);
+    if (L.m.box) {
+        if (L.m.spc) k_rows_water<true, true><<<g, 128, sm, L.st>>>(L.m, L.ds);
+        else k_rows_water<false, true><<<g, 128, sm, L.st>>>(L.m, L.ds);
+    } else if (L.m.spc) k_rows_water<true, false><<<g, 128, sm, L.st>>>(L.m, L.ds);
+    else k_rows_water<false, false><<<g, 128, sm, L.st>>>(L.m, L.ds);
 }
 void launch_ww(const Launch& L, int mixed) {
     if (L.m.nwat == 0) return;
@@ -4351,13 +4485,16 @@ __global__ void __launch_bounds__(1024) k_build_box_q(DevModel m, const DevState
     if (threadIdx.x == 0) s.cnt[C_QW] = base;
 }
 
-void launch_build_box(const Launch& L, const Cut& c, const uint8_t* qnear) {
+void launch_build_box_pairs(const Launch& L, const Cut& c) {
     const int64_t G = L.m.ncgp_solute, W = L.m.nwat;
     const int64_t total = G * (G + 1) / 2 + G * W + W * (W - 1) / 2;
     if (total > 0) {
         k_build_box_groups<<<grid_for(total, 256, 8, L.nwin), 256, 0, L.st>>>(L.m, L.ds, c.rcpp2, c.rcpw2, c.rcww2);
         if (G > 0) k_expand_pp<<<grid_for(L.s0.cap_ppg, 128, 8, L.nwin), 128, 0, L.st>>>(L.m, L.ds);
     }
+}
+void launch_build_box(const Launch& L, const Cut& c, const uint8_t* qnear, int pairs) {
+    if (pairs) launch_build_box_pairs(L, c);
     if (L.m.nqat > 0) k_build_box_q<<<dim3(1, L.nwin), 1024, 0, L.st>>>(L.m, L.ds, qnear, c.rcq2);
 }
 
@@ -4667,10 +4804,11 @@ __global__ void __launch_bounds__(256) k_box_q(DevModel m, const DevState* __res
     }
 }
 
-int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, double rcq2) {
+int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, double rcq2, int pairs) {
     const DevModel& m = L.m;
     int nl = 0;
     auto grid = [&](int64_t n) { return grid_for(n > 1 ? n : 1, 256, 8, L.nwin); };
+    if (!pairs) md = 0;   // the gather rows evaluate pp, pw and ww (the mixed form's box rows)
     if (md && m.ncgp_solute > 0) {
         if (mixed) k_box_pp<true><<<grid(L.s0.cap_pp), 256, 0, L.st>>>(m, L.ds, iwhich);
         else k_box_pp<false><<<grid(L.s0.cap_pp), 256, 0, L.st>>>(m, L.ds, iwhich);

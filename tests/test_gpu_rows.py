@@ -16,7 +16,8 @@ Cases: the benchmark droplets (R15, R25 with a 3,000-atom solute), excluded
 atoms outside 13 A, a 2 A cut-off on the R25 sphere (the grid would need
 more than 32,768 cells, so the cells grow), water only, unequal cut-offs
 (the cells follow the largest), and a batch of three windows with different
-coordinates."""
+coordinates; and in a periodic box (minimum image, wrapped stencil, or
+every unit a candidate when a box edge holds fewer than 5 cells)."""
 import numpy as np
 import pytest
 
@@ -28,32 +29,41 @@ pytestmark = pytest.mark.gpu
 CUT10 = dict(Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
 
 
-def _pairs_within(a, b, rc):
-    """(i, k) with |a_i - b_k|^2 <= rc^2 in FP64 (dx*dx + dy*dy + dz*dz)."""
+def _pairs_within(a, b, rc, box=None):
+    """(i, k) with |a_i - b_k|^2 <= rc^2 in FP64 (dx*dx + dy*dy + dz*dz); in a
+    periodic box the minimum image (L nint(d / L) - d, as the box lists)."""
     from scipy.spatial import cKDTree
     if len(a) == 0 or len(b) == 0:
         return np.zeros((0, 2), np.int64)
-    lists = cKDTree(b).query_ball_point(a, rc + 0.01)
+    if box is None:
+        lists = cKDTree(b).query_ball_point(a, rc + 0.01)
+    else:
+        L = np.asarray(box, np.float64)
+        lists = cKDTree(np.mod(b, L) % L, boxsize=L).query_ball_point(np.mod(a, L) % L, rc + 0.01)
     ii = np.repeat(np.arange(len(a)), [len(v) for v in lists])
     kk = np.concatenate([np.asarray(v, np.int64) for v in lists]) if len(ii) else np.zeros(0, np.int64)
     d = a[ii] - b[kk]
+    if box is not None:
+        d = L * (np.sign(d / L) * np.floor(np.abs(d / L) + 0.5)) - d
     r2 = d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2]
     keep = r2 <= rc * rc
     return np.stack([ii[keep], kk[keep]], 1)
 
 
-def expected_rows(s, x, Rcpp, Rcpw, Rcww):
-    """Sets of (row, partner) keys of the four row kinds, in FP64."""
+def expected_rows(s, x, Rcpp, Rcpw, Rcww, box=None):
+    """Sets of (row, partner) keys of the four row kinds, in FP64 (in a box
+    no atom is excluded: the box lists test no exclusion)."""
     ng, sa = s.ncgp_solute, s.solv_atom
     sw = s.cgp_iswitch[:ng].astype(np.int64)
-    gin = np.nonzero(s.excl[sw] == 0)[0]
+    excl = np.zeros_like(s.excl) if box is not None else s.excl
+    gin = np.nonzero(excl[sw] == 0)[0]
     oat = s.nat_solute + sa * np.arange(s.nwat)
-    win = np.nonzero(s.excl[oat] == 0)[0]
+    win = np.nonzero(excl[oat] == 0)[0]
     isq = np.zeros(s.natom, bool)
     isq[np.asarray(s.iqseq, np.int64)] = True
     out = {}
     # GP: group pairs by switch atoms (the group itself included), expanded to non-Q partner atoms
-    gg = _pairs_within(x[sw[gin]], x[sw[gin]], Rcpp)
+    gg = _pairs_within(x[sw[gin]], x[sw[gin]], Rcpp, box)
     keys = []
     for a, b in gg:
         g, g2 = gin[a], gin[b]
@@ -61,10 +71,10 @@ def expected_rows(s, x, Rcpp, Rcpw, Rcww):
         atoms = atoms[~isq[atoms]]
         keys.append(g * s.natom + atoms.astype(np.int64))
     out[ROWS_GP] = np.sort(np.concatenate(keys)) if keys else np.zeros(0, np.int64)
-    gw = _pairs_within(x[sw[gin]], x[oat[win]], Rcpw)
+    gw = _pairs_within(x[sw[gin]], x[oat[win]], Rcpw, box)
     out[ROWS_GW] = np.sort(gin[gw[:, 0]] * s.natom + win[gw[:, 1]])
     out[ROWS_WG] = np.sort(win[gw[:, 1]] * s.natom + gin[gw[:, 0]])
-    ww = _pairs_within(x[oat[win]], x[oat[win]], Rcww)
+    ww = _pairs_within(x[oat[win]], x[oat[win]], Rcww, box)
     ww = ww[ww[:, 0] != ww[:, 1]]
     out[ROWS_WW] = np.sort(win[ww[:, 0]] * s.natom + win[ww[:, 1]])
     return out
@@ -80,17 +90,19 @@ def device_rows(eng, s, win=0):
     return out
 
 
-def check_rows(s, cut, xs=None):
+def check_rows(s, cut, xs=None, box=None):
     xs = s.x[None] if xs is None else xs
     W = len(xs)
-    with NonbondedEngine(s, precision=PREC_MIXED, windows=W) as eng:
+    with NonbondedEngine(s, precision=PREC_MIXED, windows=W, use_lrf=box is None) as eng:
+        if box is not None:
+            eng.set_box(box)
         for w in range(W):
             eng.set_lambda([0.5] * s.nstates, window=w)
         eng.set_coordinates_dev(xs)
         eng.make_pair_lists_dev(**cut)
         got = [device_rows(eng, s, w) for w in range(W)]
     for w in range(W):
-        exp = expected_rows(s, xs[w], cut["Rcpp"], cut["Rcpw"], cut["Rcww"])
+        exp = expected_rows(s, xs[w], cut["Rcpp"], cut["Rcpw"], cut["Rcww"], box)
         for kind in exp:
             assert np.array_equal(got[w][kind], exp[kind]), (s.name, w, kind, len(got[w][kind]), len(exp[kind]))
     return got
@@ -140,3 +152,20 @@ def test_rows_batch_of_windows_with_different_coordinates():
     xs = np.stack([s.x + rng.normal(0.0, 0.3, s.x.shape) for _ in range(3)])
     got = check_rows(s, CUT10, xs)
     assert not np.array_equal(got[0][ROWS_WW], got[1][ROWS_WW])
+
+
+def test_rows_periodic_box_cells_and_all_candidates():
+    """The box rows (switch atoms, minimum image): the R25 sphere's atoms in a
+    55 A box, with cells (10 per edge) and with the excluded flags set (the
+    box ignores them); and a 25 A box where 10 A cut-offs leave fewer than 5
+    cells per edge, so every unit is a candidate; pairs wrap across the faces
+    in both."""
+    import dataclasses
+    cut = dict(Rcq=12.0, RcLRF=12.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
+    s = config_window()
+    check_rows(s, cut, box=[55.0] * 3)
+    r = np.linalg.norm(s.x - s.x.mean(0), axis=1)
+    se = dataclasses.replace(s, excl=(r > 20.0).astype(np.uint8))
+    check_rows(se, cut, box=[55.0] * 3)
+    small = make_system(R=11.0, n_solute=60, group_sizes=(3, 5), ntypes=5, nq=3, nstates=2, seed=404)
+    check_rows(small, cut, box=[25.0] * 3)
