@@ -13,6 +13,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -70,6 +71,11 @@ struct qnb_context {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;   // list build: the LRF accumulation runs beside the row build
+    // mixed form's evaluation: after the coordinate pack the rows run on the
+    // main stream, the Q-environment / LRF Taylor kernels on stream2 and the
+    // rest of the step's terms on stream3, joined before the gradient apply
+    cudaStream_t stream3 = nullptr;
+    cudaEvent_t ev_pk = nullptr, ev_jb = nullptr, ev_jc = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int mixed = 0;
     int use_lrf = 1;
@@ -1225,13 +1231,55 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
     return fail(QNB_ERR_CAPACITY, "pair lists kept overflowing");
 }
 
-int compute_nonbond(qnb_context* c, int md, int nw) {
+// side: the caller's further terms of the step (qq, bonded, restraints,
+// watpol), enqueued on the Launch it is given
+using SideWork = std::function<int(const Launch&)>;
+
+int compute_nonbond(qnb_context* c, int md, int nw, const SideWork& side = SideWork()) {
     if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built");
     Launch L = nw == 1 ? c->one() : c->all();
     int mx = c->mixed, nl = 0;
     if (mx) {
         timed(c, K_PACK, [&] { launch_pack(L); });
         ++nl;
+    }
+    if (mx && !c->m.box) {
+        // three branches after the pack (every sum is fixed point, so the
+        // result does not depend on their interleaving); src/potene.f90:340-379
+        // for the nonbonded terms' meaning
+        CU(cudaEventRecord(c->ev_pk, c->stream));
+        CU(cudaStreamWaitEvent(c->stream2, c->ev_pk, 0));
+        CU(cudaStreamWaitEvent(c->stream3, c->ev_pk, 0));
+        Launch LB = L, LC = L;
+        LB.st = c->stream2;
+        LC.st = c->stream3;
+        // rows: ww + the water side of pw; pp + the solute side of pw
+        if (md) {
+            if (c->m.natom > c->m.nat_solute) timed(c, K_WW, [&] { launch_rows_water(L); }), ++nl;
+            timed(c, K_PP, [&] {
+                launch_rows_solute(L, c->maxg);
+                launch_row_sums(L);
+            });
+            nl += 2;
+            c->rows_pending = true;   // frow holds this evaluation's row gradients
+        }
+        // Q environment, solvent internal pairs, LRF Taylor terms
+        if (c->m.natom > c->m.nat_solute) {
+            timed_on(c, LB.st, K_QW, [&] { launch_qw(LB, mx); }), ++nl;
+            if (md && c->nsi) timed_on(c, LB.st, K_WW, [&] { launch_solvent_internal(LB, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
+        }
+        timed_on(c, LB.st, K_QP, [&] { launch_qp(LB, mx); }), ++nl;
+        c->qenv_pending = true;   // fq holds this evaluation's Q-environment gradients
+        if (c->use_lrf && md) timed_on(c, LB.st, K_LRF_TAYLOR, [&] { launch_lrf_taylor(LB, c->d_iwhich, mx); }), ++nl;
+        // the caller's further terms
+        int rc = side ? side(LC) : QNB_OK;
+        CU(cudaEventRecord(c->ev_jb, c->stream2));
+        CU(cudaEventRecord(c->ev_jc, c->stream3));
+        CU(cudaStreamWaitEvent(c->stream, c->ev_jb, 0));
+        CU(cudaStreamWaitEvent(c->stream, c->ev_jc, 0));
+        c->launches += nl;
+        TRY(rc);
+        return check_launch();
     }
     if (c->m.box) {   // periodic box: the *_box routines, src/potene.f90:326-343
         int nb = 0;
@@ -1249,6 +1297,7 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
         if (md && c->nsi) timed(c, K_WW, [&] { launch_solvent_internal(L, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
         if (c->use_lrf && md) timed(c, K_LRF_TAYLOR, [&] { launch_lrf_taylor(L, c->d_iwhich, mx); }), ++nl;
         c->launches += nl + nb;
+        if (side) TRY(side(L));
         return check_launch();
     }
     // call order of pot_energy_nonbonds, src/potene.f90:340-379
@@ -1285,6 +1334,7 @@ int compute_nonbond(qnb_context* c, int md, int nw) {
         ++nl;
     }
     c->launches += nl;
+    if (side) TRY(side(L));
     return check_launch();
 }
 
@@ -1403,6 +1453,10 @@ int qnb_create_batch(const qnb_topology* t, const qnb_options* opt, int32_t nwin
     int rc = QNB_OK;
     if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream3, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_pk, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_jb, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_jc, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
         rc = fail(QNB_ERR_CUDA, "stream creation failed");
@@ -1443,6 +1497,10 @@ int qnb_destroy(qnb_context* c) {
     if (c->h_e) cudaFreeHost(c->h_e);
     if (c->h_md_rec) cudaFreeHost(c->h_md_rec);
     if (c->stream2) cudaStreamSynchronize(c->stream2), cudaStreamDestroy(c->stream2);
+    if (c->stream3) cudaStreamSynchronize(c->stream3), cudaStreamDestroy(c->stream3);
+    if (c->ev_pk) cudaEventDestroy(c->ev_pk);
+    if (c->ev_jb) cudaEventDestroy(c->ev_jb);
+    if (c->ev_jc) cudaEventDestroy(c->ev_jc);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1742,36 +1800,42 @@ namespace {
 int enqueue_compute(qnb_context* c, double Tfree, int istep) {
     Launch L = c->all();
     TRY(zero_acc(c, c->nwin));
-    TRY(compute_nonbond(c, 1, c->nwin));
-    timed(c, K_QQ, [&] { launch_nonbond_qq(L, c->mixed); });
-    c->launches++;
-    if (c->have_bonded) {
-        timed(c, K_BONDED, [&] { launch_bonded(L, c->bonded, c->mixed); });
+    // the step's terms beside the nonbonded ones (their own branch in the
+    // mixed form: none reads what the pair kernels write)
+    auto side = [&](const Launch& S) -> int {
+        const cudaStream_t st = S.st;
+        timed_on(c, st, K_QQ, [&] { launch_nonbond_qq(S, c->mixed); });
         c->launches++;
-    }
-    if (c->have_shell) {
-        timed(c, K_RESTRAIN, [&] { launch_fix_shell(L, c->d_shell_flags, c->d_xtop, c->fk_fix, c->fk_pshell, c->mixed, c->freeze, c->md_ready ? c->md.v : nullptr); });
-        c->launches++;
-    }
-    if (c->offd.n > 0) {
-        launch_offdiag(L, c->offd);
-        c->launches++;
-    }
-    if (c->psets.nslots > 0) {
-        launch_pair_sets(L, c->psets);
-        c->launches++;
-    }
-    if (c->have_restr) {
-        timed(c, K_RESTRAIN, [&] { launch_restraints(L, c->restr, c->mixed); });
-        c->launches++;
-    }
-    if (c->have_solv) {
-        timed(c, K_RESTRAIN, [&] { launch_restrain_solvent(L, c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv); });
-        c->launches++;
-        int nl = 0;
-        timed(c, K_WATPOL, [&] { nl = launch_watpol(L, c->solv, istep, 1, c->mixed); });
-        c->launches += nl;
-    }
+        if (c->have_bonded) {
+            timed_on(c, st, K_BONDED, [&] { launch_bonded(S, c->bonded, c->mixed); });
+            c->launches++;
+        }
+        if (c->have_shell) {
+            timed_on(c, st, K_RESTRAIN, [&] { launch_fix_shell(S, c->d_shell_flags, c->d_xtop, c->fk_fix, c->fk_pshell, c->mixed, c->freeze, c->md_ready ? c->md.v : nullptr); });
+            c->launches++;
+        }
+        if (c->offd.n > 0) {
+            launch_offdiag(S, c->offd);
+            c->launches++;
+        }
+        if (c->psets.nslots > 0) {
+            launch_pair_sets(S, c->psets);
+            c->launches++;
+        }
+        if (c->have_restr) {
+            timed_on(c, st, K_RESTRAIN, [&] { launch_restraints(S, c->restr, c->mixed); });
+            c->launches++;
+        }
+        if (c->have_solv) {
+            timed_on(c, st, K_RESTRAIN, [&] { launch_restrain_solvent(S, c->solv, Tfree, c->mixed, c->d_wsw, c->d_heavy_solv); });
+            c->launches++;
+            int nl = 0;
+            timed_on(c, st, K_WATPOL, [&] { nl = launch_watpol(S, c->solv, istep, 1, c->mixed); });
+            c->launches += nl;
+        }
+        return check_launch();
+    };
+    TRY(compute_nonbond(c, 1, c->nwin, side));
     if (c->mixed) {
         timed(c, K_APPLY, [&] { launch_apply_fixed(L, c->rows_pending ? 1 : 0, c->qenv_pending ? 1 : 0); });
         c->rows_pending = c->qenv_pending = false;
