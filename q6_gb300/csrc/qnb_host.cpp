@@ -75,7 +75,7 @@ struct qnb_context {
     // main stream, the Q-environment / LRF Taylor kernels on stream2 and the
     // rest of the step's terms on stream3, joined before the gradient apply
     cudaStream_t stream3 = nullptr;
-    cudaEvent_t ev_pk = nullptr, ev_jb = nullptr, ev_jc = nullptr;
+    cudaEvent_t ev_pk = nullptr, ev_jb = nullptr, ev_jc = nullptr, ev_rw = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int mixed = 0;
     int use_lrf = 1;
@@ -1253,13 +1253,18 @@ int compute_nonbond(qnb_context* c, int md, int nw, const SideWork& side = SideW
         Launch LB = L, LC = L;
         LB.st = c->stream2;
         LC.st = c->stream3;
-        // rows: ww + the water side of pw; pp + the solute side of pw
+        // rows: pp + the solute side of pw on the main stream, ww + the water
+        // side of pw first on the third branch; the row energies' sum waits
+        // for both
         if (md) {
-            if (c->m.natom > c->m.nat_solute) timed(c, K_WW, [&] { launch_rows_water(L); }), ++nl;
-            timed(c, K_PP, [&] {
-                launch_rows_solute(L, c->maxg);
-                launch_row_sums(L);
-            });
+            const bool wrows = c->m.natom > c->m.nat_solute;
+            if (wrows) {
+                timed_on(c, LC.st, K_WW, [&] { launch_rows_water(LC); }), ++nl;
+                CU(cudaEventRecord(c->ev_rw, LC.st));
+            }
+            timed(c, K_PP, [&] { launch_rows_solute(L, c->maxg); });   // the class times the solute rows alone
+            if (wrows) CU(cudaStreamWaitEvent(c->stream, c->ev_rw, 0));
+            launch_row_sums(L);
             nl += 2;
             c->rows_pending = true;   // frow holds this evaluation's row gradients
         }
@@ -1457,6 +1462,7 @@ int qnb_create_batch(const qnb_topology* t, const qnb_options* opt, int32_t nwin
         cudaEventCreateWithFlags(&c->ev_pk, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_jb, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_jc, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_rw, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
         rc = fail(QNB_ERR_CUDA, "stream creation failed");
@@ -1501,6 +1507,7 @@ int qnb_destroy(qnb_context* c) {
     if (c->ev_pk) cudaEventDestroy(c->ev_pk);
     if (c->ev_jb) cudaEventDestroy(c->ev_jb);
     if (c->ev_jc) cudaEventDestroy(c->ev_jc);
+    if (c->ev_rw) cudaEventDestroy(c->ev_rw);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->stream) cudaStreamDestroy(c->stream);
