@@ -346,6 +346,15 @@ int qnb_get_energies_dev(qnb_context* ctx, qnb_energies* E, qnb_qenergies* EQ, d
 int qnb_set_graphs(qnb_context* ctx, int32_t enable);
 int qnb_profile_collect(qnb_context* ctx);
 
+/* Branches of the mixed form's evaluation (on by default): after the
+   coordinate pack the solute rows run on the context's stream, the water
+   rows and the step's further terms (qq, bonded, restraints, watpol) on a
+   second stream, the Q-environment and LRF Taylor kernels on a third, all
+   joined before the fixed-point gradient apply.  Every sum is fixed point,
+   so results are the same with enable = 0, which runs them in one stream
+   (each kernel then has the device to itself, e.g. for per-kernel timing). */
+int qnb_set_concurrency(qnb_context* ctx, int32_t enable);
+
 /* A group of contexts (systems of different sizes, e.g. replicas of uneven
    sphere radii, on one device) evaluated as ONE CUDA graph launch: each
    context's kernel sequence is an independent branch of the graph, so the

@@ -126,6 +126,7 @@ struct qnb_context {
     // variant (watpol theta_corr update step or not), valid while its key
     // (launch-geometry epoch, Tfree) matches
     bool use_graphs = true;
+    bool branches = true;            // mixed form: the evaluation's parallel branches (qnb_set_concurrency)
     uint64_t epoch = 1;            // bumped whenever launch parameters change
     struct Pending {
         int k;
@@ -1243,16 +1244,20 @@ int compute_nonbond(qnb_context* c, int md, int nw, const SideWork& side = SideW
         timed(c, K_PACK, [&] { launch_pack(L); });
         ++nl;
     }
-    if (mx && !c->m.box) {
+    if (mx && (!c->m.box || c->m.box_rows)) {
+        const bool br = c->branches;
         // three branches after the pack (every sum is fixed point, so the
         // result does not depend on their interleaving); src/potene.f90:340-379
-        // for the nonbonded terms' meaning
-        CU(cudaEventRecord(c->ev_pk, c->stream));
-        CU(cudaStreamWaitEvent(c->stream2, c->ev_pk, 0));
-        CU(cudaStreamWaitEvent(c->stream3, c->ev_pk, 0));
+        // for the nonbonded terms' meaning (in a box 326-343: the rows at each
+        // unit pair's image, the box Q kernels)
         Launch LB = L, LC = L;
-        LB.st = c->stream2;
-        LC.st = c->stream3;
+        if (br) {
+            CU(cudaEventRecord(c->ev_pk, c->stream));
+            CU(cudaStreamWaitEvent(c->stream2, c->ev_pk, 0));
+            CU(cudaStreamWaitEvent(c->stream3, c->ev_pk, 0));
+            LB.st = c->stream2;
+            LC.st = c->stream3;
+        }
         // rows: pp + the solute side of pw on the main stream, ww + the water
         // side of pw first on the third branch; the row energies' sum waits
         // for both
@@ -1260,44 +1265,44 @@ int compute_nonbond(qnb_context* c, int md, int nw, const SideWork& side = SideW
             const bool wrows = c->m.natom > c->m.nat_solute;
             if (wrows) {
                 timed_on(c, LC.st, K_WW, [&] { launch_rows_water(LC); }), ++nl;
-                CU(cudaEventRecord(c->ev_rw, LC.st));
+                if (br) CU(cudaEventRecord(c->ev_rw, LC.st));
             }
             timed(c, K_PP, [&] { launch_rows_solute(L, c->maxg); });   // the class times the solute rows alone
-            if (wrows) CU(cudaStreamWaitEvent(c->stream, c->ev_rw, 0));
+            if (wrows && br) CU(cudaStreamWaitEvent(c->stream, c->ev_rw, 0));
             launch_row_sums(L);
             nl += 2;
             c->rows_pending = true;   // frow holds this evaluation's row gradients
         }
         // Q environment, solvent internal pairs, LRF Taylor terms
-        if (c->m.natom > c->m.nat_solute) {
-            timed_on(c, LB.st, K_QW, [&] { launch_qw(LB, mx); }), ++nl;
+        if (c->m.box) {
+            int nb = 0;
+            timed_on(c, LB.st, K_QW, [&] { nb = launch_box_nonbond(LB, md, mx, c->d_iwhich, c->last_cut.rcq2, 0); });
+            nl += nb;
             if (md && c->nsi) timed_on(c, LB.st, K_WW, [&] { launch_solvent_internal(LB, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
+        } else {
+            if (c->m.natom > c->m.nat_solute) {
+                timed_on(c, LB.st, K_QW, [&] { launch_qw(LB, mx); }), ++nl;
+                if (md && c->nsi) timed_on(c, LB.st, K_WW, [&] { launch_solvent_internal(LB, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
+            }
+            timed_on(c, LB.st, K_QP, [&] { launch_qp(LB, mx); }), ++nl;
+            c->qenv_pending = true;   // fq holds this evaluation's Q-environment gradients
         }
-        timed_on(c, LB.st, K_QP, [&] { launch_qp(LB, mx); }), ++nl;
-        c->qenv_pending = true;   // fq holds this evaluation's Q-environment gradients
         if (c->use_lrf && md) timed_on(c, LB.st, K_LRF_TAYLOR, [&] { launch_lrf_taylor(LB, c->d_iwhich, mx); }), ++nl;
         // the caller's further terms
         int rc = side ? side(LC) : QNB_OK;
-        CU(cudaEventRecord(c->ev_jb, c->stream2));
-        CU(cudaEventRecord(c->ev_jc, c->stream3));
-        CU(cudaStreamWaitEvent(c->stream, c->ev_jb, 0));
-        CU(cudaStreamWaitEvent(c->stream, c->ev_jc, 0));
+        if (br) {
+            CU(cudaEventRecord(c->ev_jb, c->stream2));
+            CU(cudaEventRecord(c->ev_jc, c->stream3));
+            CU(cudaStreamWaitEvent(c->stream, c->ev_jb, 0));
+            CU(cudaStreamWaitEvent(c->stream, c->ev_jc, 0));
+        }
         c->launches += nl;
         TRY(rc);
         return check_launch();
     }
     if (c->m.box) {   // periodic box: the *_box routines, src/potene.f90:326-343
         int nb = 0;
-        if (c->m.box_rows && md) {   // pp, pw, ww on the gather rows at each unit pair's image
-            if (c->m.natom > c->m.nat_solute) timed(c, K_WW, [&] { launch_rows_water(L); }), ++nl;
-            timed(c, K_PP, [&] {
-                launch_rows_solute(L, c->maxg);
-                launch_row_sums(L);
-            });
-            nl += 2;
-            c->rows_pending = true;
-        }
-        timed(c, K_QW, [&] { nb = launch_box_nonbond(L, md, mx, c->d_iwhich, c->last_cut.rcq2, !c->m.box_rows); });
+        timed(c, K_PP, [&] { nb = launch_box_nonbond(L, md, mx, c->d_iwhich, c->last_cut.rcq2, 1); });
         // src/potene.f90:326-339 and 373-377: solvent internal pairs, then the LRF Taylor terms
         if (md && c->nsi) timed(c, K_WW, [&] { launch_solvent_internal(L, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
         if (c->use_lrf && md) timed(c, K_LRF_TAYLOR, [&] { launch_lrf_taylor(L, c->d_iwhich, mx); }), ++nl;
@@ -2133,6 +2138,15 @@ int qnb_get_energies_dev(qnb_context* c, qnb_energies* E, qnb_qenergies* EQ, dou
 int qnb_set_graphs(qnb_context* c, int32_t enable) {
     if (!c) return fail(QNB_ERR_ARG, "null context");
     c->use_graphs = enable != 0;
+    return QNB_OK;
+}
+
+int qnb_set_concurrency(qnb_context* c, int32_t enable) {
+    if (!c) return fail(QNB_ERR_ARG, "null context");
+    if (c->branches != (enable != 0)) {
+        c->branches = enable != 0;
+        ++c->epoch;   // the captured graphs hold the old structure
+    }
     return QNB_OK;
 }
 

@@ -37,7 +37,7 @@ EXPORTED = (
     "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_pot_energy_step", "qnb_take_launch_count",
     "qnb_profile", "qnb_kernel_times", "qnb_create_batch", "qnb_window_count",
     "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
-    "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev", "qnb_get_energies_dev", "qnb_set_graphs",
+    "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev", "qnb_get_energies_dev", "qnb_set_graphs", "qnb_set_concurrency",
     "qnb_group_create", "qnb_group_compute", "qnb_group_destroy", "qnb_profile_collect",
     "qnb_profile_classes", "qnb_set_solvent_internal", "qnb_autotune", "qnb_get_tuning", "qnb_set_tuning",
     "qnb_md_init", "qnb_md_set_velocities", "qnb_md_get_state", "qnb_md_prepare", "qnb_md_run",
@@ -95,7 +95,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_download_gradient": [P, P, I32],
         "qnb_ww_spc_noalloc": [P, P, I32, I32, D, D, D, D, D, P, P, P],
         "qnb_q_adjoint_dev": [P, P, P, P],
-        "qnb_get_energies_dev": [P, P, P, P], "qnb_set_graphs": [P, I32],
+        "qnb_get_energies_dev": [P, P, P, P], "qnb_set_graphs": [P, I32], "qnb_set_concurrency": [P, I32],
         "qnb_group_create": [P, I32, P], "qnb_group_compute": [P, D, I32], "qnb_group_destroy": [P],
         "qnb_profile_collect": [P], "qnb_profile_classes": [P, ctypes.c_uint32],
         "qnb_set_solvent_internal": [P, I32, P, P, P, P],
@@ -601,6 +601,10 @@ class NonbondedEngine:
     def set_graphs(self, enable: bool):
         """CUDA-graph replay of compute_dev (on by default)."""
         self._check(self.lib.qnb_set_graphs(self.h, int(bool(enable))))
+
+    def set_concurrency(self, enable: bool):
+        """The mixed form's parallel evaluation branches (on by default)."""
+        self._check(self.lib.qnb_set_concurrency(self.h, int(bool(enable))))
 
     def q_adjoint_dev(self):
         """dE_s/dqcrg, dE_s/dqA, dE_s/dqB per window: arrays [nwin][nqat][nstates]."""
