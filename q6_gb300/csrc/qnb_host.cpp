@@ -373,7 +373,9 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     TRY(c->upload((int**)&m.iqseq, iqseq));
 
     // charge groups: slot ranges must be consecutive (as the topology stores them)
-    std::vector<int> gslot(t->ncgp + 1), gsw(t->ncgp), iwhich(natom, 0);
+    // iwhich: an atom's charge group, -1 for atoms in none (a sphere topology
+    // leaves excluded atoms out of the groups)
+    std::vector<int> gslot(t->ncgp + 1), gsw(t->ncgp), iwhich(natom, -1);
     for (int g = 0; g < t->ncgp; ++g) {
         if (t->cgp_first[g] != (g ? t->cgp_last[g - 1] + 1 : 0))
             return fail(QNB_ERR_ARG, "charge group %d: slots not consecutive", g);
@@ -421,7 +423,8 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     TRY(c->upload(&c->d_iwhich, iwhich));
     {   // each atom's unit reference atom (the lattice shifts of the box rows)
         std::vector<int> swat(natom);
-        for (int i = 0; i < natom; ++i) swat[i] = i < ns ? gsw[iwhich[i]] : ns + sa * ((i - ns) / sa);
+        for (int i = 0; i < natom; ++i)
+            swat[i] = i >= ns ? ns + sa * ((i - ns) / sa) : (iwhich[i] >= 0 ? gsw[iwhich[i]] : i);
         TRY(c->upload((int**)&m.swat, swat));
     }
     // lrf_update sources: non-Q atoms (src/nonbondene.f90:658-660); in the
@@ -430,7 +433,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     for (int tab = 0; tab < 2; ++tab) {
         std::vector<int> lrf_src(natom, -1);
         for (int i = 0; i < natom; ++i) {
-            if (iqatom[i] >= 0) continue;
+            if (iqatom[i] >= 0 || iwhich[i] < 0) continue;
             int g = iwhich[i];
             int d = g < t->ncgp_solute ? t->cgp_iswitch[g] : ns + sa * (g - t->ncgp_solute);
             if (tab == 0 && t->excl[d]) continue;
@@ -480,13 +483,20 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     });
     // per solute group pair: the special atom pairs, keyed g1*ncgp_solute+g2
     std::vector<int> slot_of(natom, -1);
+    // a group of Q atoms only has no pair rows (Q atoms take no part in the
+    // pp / pw lists or as LRF sources), so its size is not bounded
+    std::vector<uint8_t> gallq(std::max(1, t->ncgp_solute), 0);
     for (int g = 0; g < t->ncgp_solute; ++g) {
-        if (gslot[g + 1] - gslot[g] > kMaxGroup)
-            return fail(QNB_ERR_UNSUPPORTED, "solute charge group %d has %d atoms (max %d)", g,
+        int nonq = 0;
+        for (int a = gslot[g]; a < gslot[g + 1]; ++a) nonq += iqatom[gatom[a]] < 0 ? 1 : 0;
+        gallq[g] = nonq == 0 ? 1 : 0;
+        if (gslot[g + 1] - gslot[g] > kMaxGroup && !gallq[g])
+            return fail(QNB_ERR_UNSUPPORTED, "solute charge group %d has %d atoms (max %d unless all are Q atoms)", g,
                         gslot[g + 1] - gslot[g], kMaxGroup);
         for (int a = gslot[g]; a < gslot[g + 1]; ++a) slot_of[gatom[a]] = a - gslot[g];
-        c->maxg = std::max(c->maxg, gslot[g + 1] - gslot[g]);
+        if (!gallq[g]) c->maxg = std::max(c->maxg, gslot[g + 1] - gslot[g]);
     }
+    TRY(c->upload((uint8_t**)&m.gallq, gallq));
     // must agree with k_rows_solute's template choice (MAXG <= 8)
     m.type_in_entry = (c->maxg <= 8 && t->natyps <= 0xffff) ? 1 : 0;
     struct SG {
@@ -499,6 +509,7 @@ int build_model(qnb_context* c, const qnb_topology* t) {
         if (sp[k].i < 0 || sp[k].j >= ns) return fail(QNB_ERR_ARG, "special pair outside the solute");
         int i = sp[k].i, j = sp[k].j;   // i < j
         int gi = iwhich[i], gj = iwhich[j];
+        if (gi < 0 || gj < 0) continue;   // an atom in no charge group is in no pair list
         int si = slot_of[i], sj = slot_of[j];
         if (gi > gj) {
             std::swap(gi, gj);
@@ -547,6 +558,10 @@ int build_model(qnb_context* c, const qnb_topology* t) {
             int nl = gslot[gl + 1] - gslot[gl], nu = gslot[gu + 1] - gslot[gu];
             size_t base = mk.size();
             mk.resize(base + nu + (gl == gu ? 0 : nl), 0u);
+            if (gallq[gl] || gallq[gu]) {   // no row of a Q-only group; the other row skips its (Q) atoms
+                moff.push_back((int)mk.size());
+                continue;
+            }
             unsigned* lo = mk.data() + base;           // row gl, partner b of gu
             unsigned* hi = lo + nu;                    // row gu, partner b of gl
             if (gl == gu)

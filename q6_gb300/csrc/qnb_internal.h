@@ -130,6 +130,7 @@ struct DevModel {
     // rule: A = a_i a_j, B = b_i b_j)
     int geom;
     const unsigned long long* gtmask;   // [ncgp_solute]
+    const uint8_t* gallq;               // [ncgp_solute] 1: every atom of the group is a Q atom (no pair row)
     const float2* ljf1;                 // [natom]
     // LRF sources grouped by charge group (mixed form's accumulation):
     // groups with LRF-eligible atoms (non-Q atoms of groups whose distance

@@ -2040,7 +2040,7 @@ __global__ void __launch_bounds__(256) k_lrf_taylor(DevModel m, const DevState* 
     Acc<MIX> acc = make_acc<MIX>(s);
     ESum<MIX> elrf;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.natom; i += gridDim.x * blockDim.x) {
-        if (m.excl[i] || m.iqatom[i] >= 0) continue;
+        if (m.excl[i] || m.iqatom[i] >= 0 || iwhich[i] < 0) continue;   // (an atom in no group: no record)
         const double* L = s.lrf + (size_t)iwhich[i] * kLrfLen;
         double dx = L[0] - s.x[3 * i], dy = L[1] - s.x[3 * i + 1], dz = L[2] - s.x[3 * i + 2];
         const double* p1 = L + 4;
@@ -2608,6 +2608,13 @@ __device__ __forceinline__ bool within_box(const DevModel& m, float4 pa, float4 
     return within_box_exact(m, x, a, b, rc.c);
 }
 
+// partner atom j needs the general pair path against some row atom (its LJ
+// code with a row atom's type is not 1); with more than 64 atom types the
+// 64-bit row mask cannot hold them, and every partner takes the general path
+__device__ __forceinline__ bool type_special(const DevModel& m, unsigned long long tmask, int j) {
+    return m.natyps > 64 || ((tmask >> m.iac[j]) & 1ull);
+}
+
 // ---- cell grid of the row build -------------------------------------------
 // The reference bins atoms for its neighbour search in populate_grids
 // (src/nonbondene.f90:6264-6460, under USE_GRID).  Here one block per window
@@ -2825,7 +2832,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
         if (r < m.ncgp_solute) {
             int g = r, is = m.gsw[g];
             int npp = 0, npf = 0, npw = 0;
-            if (!m.excl[is]) {
+            if (!m.excl[is] && !m.gallq[g]) {   // a Q-only group's row stays empty
                 const float4 xs = xq[is];
                 Runs R{0, 0, 0};
                 const int3 cs = CELLS ? cell_at<BOX>(m, G, xs) : make_int3(0, 0, 0);
@@ -2879,7 +2886,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                             for (int b = 0; b < n2; ++b) {
                                 int j = m.gatom[b0 + b];
                                 if (m.iqatom[j] >= 0) continue;
-                                if (all_special || ((tmask >> m.iac[j]) & 1ull)) ++ns;
+                                if (all_special || type_special(m, tmask, j)) ++ns;
                                 else ++nf;
                             }
                         }
@@ -2901,7 +2908,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                         for (int b = 0; b < n2; ++b) {
                             int j = m.gatom[b0 + b];
                             if (m.iqatom[j] >= 0) continue;
-                            if (!all_special && !((tmask >> m.iac[j]) & 1ull)) {
+                            if (!all_special && !type_special(m, tmask, j)) {
                                 if (pf < s.cap_gf) rf[pf] = j;
                                 ++pf;
                                 continue;
@@ -3194,6 +3201,11 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
     for (int g = warp_id_global(); g < m.ncgp_solute; g += warps_total()) {
         int npp = s.cnt_gp[g], npw = s.cnt_gw[g];   // an empty row still writes its zeros
         int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
+        if (n1 > MAXG) {   // a Q-only group larger than the rows handle: empty row, zero gradient
+            for (int a = lane; a < 3 * n1; a += kWarp) s.frow[3 * m.gatom[a0 + a / 3] + a % 3] = 0.f;
+            if (lane == 0) s.erow[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+            continue;
+        }
         // periodic box: the row group's reference atom (its lattice shifts)
         const float4 xsw = BOX ? xq[m.gsw[g]] : make_float4(0.f, 0.f, 0.f, 0.f);
         int ta[MAXG];

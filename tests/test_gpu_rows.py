@@ -7,7 +7,8 @@ nbpwlist (2842-2955) a group and a water when the switch atom and the
 oxygen are within Rcpw, nbwwlist (4274-4395) two waters when their oxygens
 are within Rcww; excluded switch atoms / oxygens take part in none.  The
 rows hold each selected pair from both sides (a group's row also holds the
-group itself), Q atoms left out of the solute partners.  Expected sets are
+group itself), Q atoms left out of the solute partners, and a group of Q
+atoms only has an empty row (its atoms' pairs are the Q lists').  Expected sets are
 computed here in FP64 from the coordinates (a k-d tree proposes pairs within
 the cut-off plus 0.01 A, the FP64 squared distance decides); the water-water
 set is also anchored to the CPU oracle's nbww list.
@@ -61,18 +62,22 @@ def expected_rows(s, x, Rcpp, Rcpw, Rcww, box=None):
     win = np.nonzero(excl[oat] == 0)[0]
     isq = np.zeros(s.natom, bool)
     isq[np.asarray(s.iqseq, np.int64)] = True
+    # a group of Q atoms only has an empty row (its atoms' pairs are Q lists)
+    allq = np.array([isq[s.cgpatom[s.cgp_first[g]:s.cgp_last[g] + 1]].all() for g in range(ng)], bool)
+    rows_g = np.nonzero((excl[sw] == 0) & ~allq)[0]
     out = {}
     # GP: group pairs by switch atoms (the group itself included), expanded to non-Q partner atoms
-    gg = _pairs_within(x[sw[gin]], x[sw[gin]], Rcpp, box)
+    gg = _pairs_within(x[sw[rows_g]], x[sw[gin]], Rcpp, box)
     keys = []
     for a, b in gg:
-        g, g2 = gin[a], gin[b]
+        g, g2 = rows_g[a], gin[b]
         atoms = s.cgpatom[s.cgp_first[g2]: s.cgp_last[g2] + 1]
         atoms = atoms[~isq[atoms]]
         keys.append(g * s.natom + atoms.astype(np.int64))
     out[ROWS_GP] = np.sort(np.concatenate(keys)) if keys else np.zeros(0, np.int64)
     gw = _pairs_within(x[sw[gin]], x[oat[win]], Rcpw, box)
-    out[ROWS_GW] = np.sort(gin[gw[:, 0]] * s.natom + win[gw[:, 1]])
+    keep = ~allq[gin[gw[:, 0]]]
+    out[ROWS_GW] = np.sort(gin[gw[keep, 0]] * s.natom + win[gw[keep, 1]])
     out[ROWS_WG] = np.sort(win[gw[:, 1]] * s.natom + gin[gw[:, 0]])
     ww = _pairs_within(x[oat[win]], x[oat[win]], Rcww, box)
     ww = ww[ww[:, 0] != ww[:, 1]]
