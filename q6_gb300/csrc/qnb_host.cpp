@@ -612,23 +612,26 @@ int build_model(qnb_context* c, const qnb_topology* t) {
     TRY(c->upload((float4**)&m.ljpair, ljpair));
     {   // plain solute partners (see DevModel::gtmask)
         m.geom = t->ivdw_rule == 1 ? 1 : 0;
-        std::vector<unsigned long long> gtm(std::max(1, t->ncgp_solute), 0ull);
+        std::vector<ulonglong2> gtm(std::max(1, t->ncgp_solute), make_ulonglong2(0ull, 0ull));
         for (int g = 0; g < t->ncgp_solute; ++g) {
-            if (nt > 64) {
-                gtm[g] = ~0ull;
+            if (nt > 128) {   // every partner takes the general path
+                gtm[g] = make_ulonglong2(~0ull, ~0ull);
                 continue;
             }
             for (int a = gslot[g]; a < gslot[g + 1]; ++a) {
                 int i = gatom[a];
                 if (iqatom[i] >= 0) continue;
                 for (int b = 0; b < nt; ++b)
-                    if (t->ljcod[t->iac[i] * nt + b] != 1) gtm[g] |= 1ull << b;
+                    if (t->ljcod[t->iac[i] * nt + b] != 1) {
+                        if (b < 64) gtm[g].x |= 1ull << b;
+                        else gtm[g].y |= 1ull << (b - 64);
+                    }
             }
         }
         std::vector<float2> f1(std::max(1, natom));
         for (int i = 0; i < natom; ++i)
             f1[i] = make_float2((float)t->avdw[t->iac[i] * 3], (float)t->bvdw[t->iac[i] * 3]);
-        TRY(c->upload((unsigned long long**)&m.gtmask, gtm));
+        TRY(c->upload((ulonglong2**)&m.gtmask, gtm));
         TRY(c->upload((float2**)&m.ljf1, f1));
     }
     TRY(c->upload((double2**)&m.lj, lj));

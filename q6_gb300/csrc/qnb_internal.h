@@ -126,10 +126,10 @@ struct DevModel {
     // plain solute partners of the mixed form's solute rows: per solute group
     // the partner types that need the general pair path (some non-Q atom of
     // the group has LJ code 2 with them; all bits set when there are more
-    // than 64 types), and per atom its code-1 LJ factors in FP32 (geometric
+    // than 128 types), and per atom its code-1 LJ factors in FP32 (geometric
     // rule: A = a_i a_j, B = b_i b_j)
     int geom;
-    const unsigned long long* gtmask;   // [ncgp_solute]
+    const ulonglong2* gtmask;           // [ncgp_solute] types 0-63 (x) and 64-127 (y)
     const uint8_t* gallq;               // [ncgp_solute] 1: every atom of the group is a Q atom (no pair row)
     const float2* ljf1;                 // [natom]
     // LRF sources grouped by charge group (mixed form's accumulation):

@@ -2609,10 +2609,12 @@ __device__ __forceinline__ bool within_box(const DevModel& m, float4 pa, float4 
 }
 
 // partner atom j needs the general pair path against some row atom (its LJ
-// code with a row atom's type is not 1); with more than 64 atom types the
-// 64-bit row mask cannot hold them, and every partner takes the general path
-__device__ __forceinline__ bool type_special(const DevModel& m, unsigned long long tmask, int j) {
-    return m.natyps > 64 || ((tmask >> m.iac[j]) & 1ull);
+// code with a row atom's type is not 1); the row mask covers 128 types, and
+// with more every partner takes the general path
+__device__ __forceinline__ bool type_special(const DevModel& m, ulonglong2 tmask, int j) {
+    if (m.natyps > 128) return true;
+    const int t = m.iac[j];
+    return t < 64 ? ((tmask.x >> t) & 1ull) : ((tmask.y >> (t - 64)) & 1ull);
 }
 
 // ---- cell grid of the row build -------------------------------------------
@@ -2836,7 +2838,7 @@ __global__ void k_build_rows(DevModel m, const DevState* __restrict__ states, Cu
                 const float4 xs = xq[is];
                 Runs R{0, 0, 0};
                 const int3 cs = CELLS ? cell_at<BOX>(m, G, xs) : make_int3(0, 0, 0);
-                const unsigned long long tmask = m.gtmask[g];
+                const ulonglong2 tmask = m.gtmask[g];
                 const int n1 = m.gslot[g + 1] - m.gslot[g];
                 uint2* rp = s.row_gp + (size_t)g * s.cap_gp;
                 int* rf = s.row_gf + (size_t)g * s.cap_gf;

@@ -87,6 +87,20 @@ def test_config4_four_state_evb():
     check_vs_oracle(config_adjoint(), CUT10, [0.4, 0.3, 0.2, 0.1])
 
 
+@pytest.mark.parametrize("ntypes,pairs", [(100, ((0, 1), (70, 90), (5, 99), (64, 63))),
+                                           (140, ((0, 1), (130, 135), (3, 100)))])
+def test_many_atom_types(ntypes, pairs):
+    """Type-2 LJ pairs among more than 64 atom types: the mixed form's rows
+    mark per group which partner types need the general pair path in a
+    128-type mask (types 64 and above in its second word); with more than
+    128 types every partner takes the general path."""
+    s = make_system(R=16.0, n_solute=400, group_sizes=(3, 6), ntypes=ntypes, nq=6, nstates=2,
+                    seed=77 + ntypes, type2_pairs=pairs)
+    hi = s.iac[: s.nat_solute]
+    assert (hi >= 64).any() and any((hi == a).any() and (hi == b).any() for a, b in pairs if a >= 64 or b >= 64)
+    check_vs_oracle(s, CUT10, [0.5, 0.5])
+
+
 def batched_vs_single(s, cut, lams, check_windows, prec=PREC_MIXED):
     W = len(lams)
     sp = default_solvent_params(s)
