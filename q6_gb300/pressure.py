@@ -105,15 +105,47 @@ def default_molecules(s):
                                   for w in range(s.nwat)]
 
 
-def run_npt(engine, setup: PressureSetup, nsteps, cut, temp0, istep0=0, molecules=None, boxcentre=None):
+_CUT_DEFAULTS = dict(Rcq=99.0, RcLRF=99.0, Rcpp=10.0, Rcpw=10.0, Rcww=10.0)
+
+
+def npt_cutoffs(engine, setup: PressureSetup, cut=None):
+    """The cut-offs of the trial energies: those the MD run builds its lists
+    with (the engine's MD set-up), so that a trial compares energies under the
+    same lists.  A cut dict that is passed must agree with them.  qdyn tries a
+    volume move only inside the list-update block of the step loop
+    (src/md.f90:1661, 1724-1731), so volume_change must be a multiple of
+    nbcycle."""
+    md = getattr(engine, "md_setup", None)
+    if md is None:
+        raise ValueError("constant pressure needs an initialised MD state (md_init)")
+    if setup.volume_change <= 0 or setup.volume_change % md.nbcycle != 0:
+        raise ValueError(f"volume_change {setup.volume_change} is not a multiple of nbcycle {md.nbcycle}")
+    mdcut = {k: md.cut.get(k, v) for k, v in _CUT_DEFAULTS.items()}
+    if cut is not None:
+        keys = [k for k in _CUT_DEFAULTS if k != "RcLRF" or getattr(engine, "use_lrf", True)]
+        for k in keys:
+            if k in cut and float(cut[k]) != float(mdcut[k]):
+                raise ValueError(f"{k} = {cut[k]} differs from the MD run's {mdcut[k]}")
+    return mdcut
+
+
+def run_npt(engine, setup: PressureSetup, nsteps, cut=None, temp0=300.0, istep0=0, molecules=None,
+            boxcentre=None):
     """Device MD (qnb_md_run) with an MC volume move every volume_change
     steps, before that step's evaluation as md_run does.  The engine holds
-    one window, a periodic box (set_box) and an initialised MD state.
+    one window, a periodic box (set_box) and an initialised MD state.  The
+    trial energies use the MD run's cut-offs (npt_cutoffs); molecules scale
+    about boxcentre, by default the rigid box centre given to
+    set_put_back_in_box, else the mean of the solute atoms at the move (the
+    floating centre put_back_in_box uses).
     Returns (records, per-move info dicts, final box edges)."""
     if engine.nwin != 1:
         raise ValueError("constant pressure needs a single-window engine (one box per context)")
     if getattr(engine, "boxlength", None) is None:
         raise ValueError("constant pressure needs a periodic box (set_box)")
+    cut = npt_cutoffs(engine, setup, cut)
+    if boxcentre is None:
+        boxcentre = getattr(engine, "pb_boxcentre", None)
     s = engine.s
     molecules = molecules if molecules is not None else default_molecules(s)
     mass = np.asarray(s.mass, np.float64)[np.asarray(s.iac)]

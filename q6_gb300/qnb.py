@@ -133,6 +133,7 @@ class NonbondedEngine:
         self.s = system
         self.S = system.nstates
         self.nwin = int(windows)
+        self.use_lrf = bool(use_lrf)
         self.topo = TopologyHandle(system)
         opt = QnbOptions(precision, int(use_lrf), device, 0)
         h = ctypes.c_void_p()
@@ -458,6 +459,7 @@ class NonbondedEngine:
             first[q + 1] = first[q] + len(mol)
         atoms = np.ascontiguousarray(np.concatenate([np.asarray(m, np.int32) for m in molecules]), dtype=np.int32)
         bc = None if boxcentre is None else np.ascontiguousarray(boxcentre, dtype=np.float64)
+        self.pb_boxcentre = None if bc is None else bc.copy()
         self._check(self.lib.qnb_set_put_back_in_box(self.h, len(molecules), _p(first), _p(atoms), nslu,
                                                      int(put_solute), int(put_solvent),
                                                      None if bc is None else _p(bc)))

@@ -97,3 +97,59 @@ def test_moves_with_the_box_oracle(sysp):
     with pytest.raises(ValueError):
         mc_volume_move(energy, x, np.array([18.0] * 3), mols, mass, np.zeros(3), setup, 300.0,
                        Draws([0.0, 0.5]), CUT)
+
+
+class FakeNptEngine:
+    """The host side of an engine as run_npt sees it: one window, a box, an
+    MD set-up; md_run returns empty records and md_state the coordinates."""
+
+    def __init__(self, s, nbcycle, cut, boxcentre=None):
+        from q6_gb300.md import MdSetup
+        self.s, self.nwin, self.use_lrf, self.qswitch = s, 1, False, int(s.iqseq[0])
+        self.boxlength = np.array([23.5] * 3)
+        self.md_setup = MdSetup(nbcycle=nbcycle, cut=cut)
+        self.pb_boxcentre = None if boxcentre is None else np.asarray(boxcentre, np.float64)
+
+    def md_run(self, n, istep):
+        return np.zeros(n), None, None
+
+    def md_state(self, w):
+        return self.s.x.copy(), np.zeros_like(self.s.x)
+
+    def set_box(self, L, qs):
+        self.boxlength = np.array(L, np.float64)
+
+    def set_coordinates_dev(self, x):
+        pass
+
+
+def test_npt_takes_the_md_cutoffs_nbcycle_multiple_and_rigid_centre(sysp, monkeypatch):
+    """run_npt's trial energies use the MD run's cut-offs (a cut dict that
+    differs is refused), volume moves come only on list-update steps
+    (volume_change a multiple of nbcycle, src/md.f90:1661, 1724-1731), and the
+    molecules scale about the rigid box centre given to put_back_in_box."""
+    import q6_gb300.pressure as pr
+    s = sysp
+    mdcut = dict(Rcq=11.0, RcLRF=11.0, Rcpp=9.0, Rcpw=9.0, Rcww=9.0)
+    setup = PressureSetup(max_volume_displ=100.0, volume_change=10)
+    eng = FakeNptEngine(s, 5, mdcut, boxcentre=(1.0, 2.0, 3.0))
+    assert pr.npt_cutoffs(eng, setup) == mdcut
+    assert pr.npt_cutoffs(eng, setup, CUT) == mdcut          # RcLRF is not compared with LRF off
+    with pytest.raises(ValueError, match="Rcpp"):
+        pr.npt_cutoffs(eng, setup, dict(CUT, Rcpp=10.0))
+    with pytest.raises(ValueError, match="nbcycle"):
+        pr.npt_cutoffs(FakeNptEngine(s, 25, mdcut), setup)
+    seen = []
+
+    def fake_move(energy, x, L, molecules, mass, centre, setup_, temp0, rng, cut, E_old=None):
+        seen.append((np.array(centre), dict(cut)))
+        return False, x, L, 0.0, {}
+
+    monkeypatch.setattr(pr, "mc_volume_move", fake_move)
+    rec, moves, L = pr.run_npt(eng, setup, 30, temp0=300.0)
+    assert len(rec) == 30 and len(moves) == 2
+    for c, cut in seen:
+        assert np.array_equal(c, [1.0, 2.0, 3.0]) and cut == mdcut
+    seen.clear()
+    pr.run_npt(FakeNptEngine(s, 5, mdcut), setup, 20, temp0=300.0)   # floating centre: the solute mean
+    assert np.allclose(seen[0][0], s.x[:s.nat_solute].mean(0))
