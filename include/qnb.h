@@ -720,8 +720,7 @@ int qnb_md_run(qnb_context* ctx, int32_t nsteps, int32_t istep0, qnb_md_record* 
    calls on a device share the array: each call clears its counter first,
    and calls that overlap on the GPU (different streams or threads) race.
    The first call on a device looks up the array's device address
-   (cudaGetSymbolAddress) with that device current; make that first call
-   before any stream capture.  The address is kept for the life of the
+   (cudaGetSymbolAddress) with that device current.  The address is kept for the life of the
    process, so the entry point is not for use after a cudaDeviceReset.  The
    call waits on `stream` once, after the pair selection, to check the pair
    count.  The gradient and energies are added with FP64 atomics: repeated
