@@ -538,11 +538,11 @@ def run_e2e(args, s, sp, lams, prec, local, tuning=None):
     """Same metric end to end through the public C ABI with host buffers.
 
     Batched path (the headline): one context holds every window, as a driver
-    running all lambda windows in one process would; each step copies all
-    windows' coordinates in from pinned host memory (qnb_upload_coordinates),
-    rebuilds the lists every 25th step, evaluates (qnb_compute_dev, energies
-    read back) and copies all gradients out to pinned memory
-    (qnb_download_gradient).
+    running all lambda windows in one process would; each step is one
+    qnb_step_host call: all windows' coordinates in from pinned host memory,
+    the lists rebuilt every 25th step, the evaluation, all gradients out to
+    pinned memory and the energies read back, with one host synchronisation
+    (two on a rebuild step, whose list counts are checked).
 
     Drop-in path (reported beside it): one context per window, as one qdyn
     process per window holds, through the calls the Fortran shim makes:
@@ -569,13 +569,11 @@ def run_e2e(args, s, sp, lams, prec, local, tuning=None):
     rng = np.random.default_rng(77)
     x_pin[:] = np.stack([s.x + rng.normal(0.0, 0.01, size=s.x.shape) for _ in range(nwin)])
 
-    def step(k):
-        eng.set_coordinates_dev(x_pin)                    # H2D, all windows
-        if k % NBCYCLE == 0:
-            eng.make_pair_lists_dev(**CUT)
-        eng.compute_dev(Tfree=300.0, istep=k, sync=True)  # energies D2H
-        eng.gradient_dev(out=d_pin)                       # gradients D2H
+    def step(k):   # coordinates H2D, lists every 25th step, evaluation, gradients + energies D2H
+        eng.step_host(x_pin, out=d_pin, Tfree=300.0, istep=k, rebuild_lists=k % NBCYCLE == 0)
 
+    eng.set_coordinates_dev(x_pin)
+    eng.make_pair_lists_dev(**CUT)   # the cut-offs every later rebuild uses
     warm = max(3, args.warmup)
     for k in range(warm):
         step(k)
@@ -592,9 +590,9 @@ def run_e2e(args, s, sp, lams, prec, local, tuning=None):
     out = {"value": round(nwin / (ms / 1e3), 2), "unit": "steps/s", "ms_per_step": round(ms, 4),
            "h2d_bytes_per_step": int(nbytes), "d2h_bytes_per_step": int(nbytes + ebytes), "windows": nwin,
            "steps": steps, "cycle": cycle_summary(rb, pl),
-           "path": "qnb_upload_coordinates (pinned) + qnb_make_pair_lists_dev every 25th step + "
-                   "qnb_compute_dev(sync) + qnb_download_gradient (pinned), one context holding all windows; "
-                   "host clock around each step"}
+           "path": "qnb_step_host: coordinates in from pinned memory, lists rebuilt every 25th step, "
+                   "evaluation, gradients out to pinned memory and energies back in one call, one context "
+                   "holding all windows; host clock around each step"}
 
     # drop-in path: one single-window context per window
     nw1 = min(nwin, 8)

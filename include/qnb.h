@@ -331,6 +331,22 @@ int qnb_set_tuning(qnb_context* ctx, const int32_t* values);
 int qnb_pot_energy_step(qnb_context* ctx, const double* x, double* d, double Tfree, int32_t istep,
                         qnb_energies* E, qnb_qenergies* EQ, double* Erst);
 
+/* One step of every window of a (batched) context through host buffers, in
+   one call with one host synchronisation: copies the coordinates of all
+   windows (x_all, nwin x natom x 3; pinned memory makes the copy
+   asynchronous) into HBM, rebuilds the pair lists with the cut-offs of the
+   last qnb_make_pair_lists* call when rebuild_lists != 0 (qdyn's list update
+   every NBcycle steps, src/md.f90:1661-1690, on this step's coordinates),
+   evaluates what qnb_compute_dev evaluates, writes the gradient of all
+   windows into d_all (nwin x natom x 3, overwritten; the device
+   accumulators are cleared) and adds the energies into E[nwin],
+   EQ[nwin*nstates] and Erst[nwin*2] (each may be NULL).  The same work as
+   qnb_upload_coordinates + qnb_make_pair_lists_dev + qnb_compute_dev(sync)
+   + qnb_download_gradient(clear), which wait on the device three or four
+   times.  Needs lists built once (QNB_ERR_STATE otherwise). */
+int qnb_step_host(qnb_context* ctx, const double* x_all, double* d_all, double Tfree, int32_t istep,
+                  int32_t rebuild_lists, qnb_energies* E, qnb_qenergies* EQ, double* Erst);
+
 /* Energies of the last qnb_compute_dev / qnb_group_compute evaluation of all
    windows, added into E[nwin], EQ[nwin*nstates], Erst[nwin*2] (waits for
    the context's stream). */

@@ -1083,13 +1083,22 @@ int zero_acc(qnb_context* c, int nw) {
 }
 
 // energies of the first nw windows: out[w*kNumE + k] (FP64 slots + fixed-point slots)
-int read_energies(qnb_context* c, int nw, double* out) {
+// the energy records of nw windows copied to the pinned h_e (enqueued)
+int enqueue_energies(qnb_context* c, int nw) {
     CU(cudaMemcpyAsync(c->h_e, c->e_all, sizeof(double) * kNumE * nw, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaMemcpyAsync(c->h_e + (size_t)kNumE * c->nwin, c->efix_all, sizeof(double) * kNumE * nw,
                        cudaMemcpyDeviceToHost, c->stream));
-    CU(cudaStreamSynchronize(c->stream));
+    return QNB_OK;
+}
+// after the copies have landed: FP64 part + fixed-point part per slot
+void finish_energies(const qnb_context* c, int nw, double* out) {
     const long long* fx = (const long long*)(c->h_e + (size_t)kNumE * c->nwin);
     for (int k = 0; k < kNumE * nw; ++k) out[k] = c->h_e[k] + (double)fx[k] * (1.0 / kFix);
+}
+int read_energies(qnb_context* c, int nw, double* out) {
+    TRY(enqueue_energies(c, nw));
+    CU(cudaStreamSynchronize(c->stream));
+    finish_energies(c, nw, out);
     return QNB_OK;
 }
 
@@ -1953,16 +1962,21 @@ int run_compute(qnb_context* c, double Tfree, int istep) {
     return QNB_OK;
 }
 
-int energies_out(qnb_context* c, qnb_energies* E, qnb_qenergies* EQ, double* Erst) {
-    std::vector<double> e((size_t)kNumE * c->nwin);
-    TRY(read_energies(c, c->nwin, e.data()));
+// adds the energies of every window, as read into e, into E / EQ / Erst
+void add_window_energies(const qnb_context* c, const double* e, qnb_energies* E, qnb_qenergies* EQ, double* Erst) {
     for (int w = 0; w < c->nwin; ++w) {
-        add_energies(e.data() + (size_t)w * kNumE, E ? E + w : nullptr, EQ ? EQ + (size_t)w * c->S : nullptr, c->S);
+        add_energies(e + (size_t)w * kNumE, E ? E + w : nullptr, EQ ? EQ + (size_t)w * c->S : nullptr, c->S);
         if (Erst) {
             Erst[2 * w] += e[(size_t)w * kNumE + E_RST_RAD];
             Erst[2 * w + 1] += e[(size_t)w * kNumE + E_RST_POL];
         }
     }
+}
+
+int energies_out(qnb_context* c, qnb_energies* E, qnb_qenergies* EQ, double* Erst) {
+    std::vector<double> e((size_t)kNumE * c->nwin);
+    TRY(read_energies(c, c->nwin, e.data()));
+    add_window_energies(c, e.data(), E, EQ, Erst);
     return QNB_OK;
 }
 
@@ -1977,6 +1991,28 @@ int qnb_compute_dev(qnb_context* c, double Tfree, int32_t istep, int32_t sync, q
     if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built");
     TRY(run_compute(c, Tfree, istep));
     if (sync) TRY(energies_out(c, E, EQ, Erst));
+    return QNB_OK;
+}
+
+int qnb_step_host(qnb_context* c, const double* x_all, double* d_all, double Tfree, int32_t istep,
+                  int32_t rebuild_lists, qnb_energies* E, qnb_qenergies* EQ, double* Erst) {
+    if (!c || !x_all || !d_all) return fail(QNB_ERR_ARG, "null argument");
+    CU(cudaSetDevice(c->device));
+    if (!c->lists_built) return fail(QNB_ERR_STATE, "pair lists not built (build them once with qnb_make_pair_lists_dev)");
+    const size_t n = 3 * (size_t)c->natom * c->nwin;
+    CU(cudaMemcpyAsync(c->x_all, x_all, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    if (rebuild_lists) {   // waits for its list counts
+        const Cut cut = c->last_cut;
+        TRY(build_lists(c, cut, c->nwin));
+    }
+    TRY(run_compute(c, Tfree, istep));
+    CU(cudaMemcpyAsync(d_all, c->d_all, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemsetAsync(c->d_all, 0, sizeof(double) * n, c->stream));
+    TRY(enqueue_energies(c, c->nwin));
+    CU(cudaStreamSynchronize(c->stream));
+    std::vector<double> e((size_t)kNumE * c->nwin);
+    finish_energies(c, c->nwin, e.data());
+    add_window_energies(c, e.data(), E, EQ, Erst);
     return QNB_OK;
 }
 

@@ -34,7 +34,7 @@ EXPORTED = (
     "qnb_make_pair_lists", "qnb_pot_energy_nonbonds", "qnb_nonbond_qq",
     "qnb_set_solvent_params", "qnb_restrain_solvent", "qnb_watpol", "qnb_get_watpol_state",
     "qnb_list_size", "qnb_export_pairs", "qnb_export_rows", "qnb_get_lrf", "qnb_device_buffers", "qnb_stream",
-    "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_pot_energy_step", "qnb_take_launch_count",
+    "qnb_make_pair_lists_dev", "qnb_compute_dev", "qnb_pot_energy_step", "qnb_step_host", "qnb_take_launch_count",
     "qnb_profile", "qnb_kernel_times", "qnb_create_batch", "qnb_window_count",
     "qnb_set_lambda_window", "qnb_upload_coordinates", "qnb_download_gradient",
     "qnb_ww_spc_noalloc", "qnb_q_adjoint_dev", "qnb_get_energies_dev", "qnb_set_graphs", "qnb_set_concurrency",
@@ -89,6 +89,7 @@ def load_library(path: str = LIB_PATH):
         "qnb_device_buffers": [P, P, P], "qnb_stream": [P, P],
         "qnb_compute_dev": [P, D, I32, I32, P, P, P], "qnb_take_launch_count": [P, P],
         "qnb_pot_energy_step": [P, P, P, D, I32, P, P, P],
+        "qnb_step_host": [P, P, P, D, I32, I32, P, P, P],
         "qnb_profile": [P, I32], "qnb_kernel_times": [P, P, P, I32],
         "qnb_create_batch": [P, P, I32, P], "qnb_window_count": [P, P],
         "qnb_set_lambda_window": [P, I32, P], "qnb_upload_coordinates": [P, P],
@@ -287,13 +288,40 @@ class NonbondedEngine:
         return d, dict(zip(E_FIELDS, E)), EQ[: self.S], R
 
     def compute_dev(self, Tfree=300.0, istep=0, sync=True):
-        """All windows; returns per-window energies (lists) when sync."""
+        """All windows; returns per-window energies (lists) when sync, else
+        None at once (the evaluation is only enqueued)."""
+        if not sync:
+            self._check(self.lib.qnb_compute_dev(self.h, Tfree, int(istep), 0, None, None, None))
+            return None
         W = self.nwin
         E = np.zeros((W, 7))
         EQ = np.zeros((W, max(self.S, 1), 6))
         R = np.zeros((W, 2))
-        self._check(self.lib.qnb_compute_dev(self.h, Tfree, int(istep), int(sync), _p(E), _p(EQ), _p(R)))
+        self._check(self.lib.qnb_compute_dev(self.h, Tfree, int(istep), 1, _p(E), _p(EQ), _p(R)))
         return [dict(zip(E_FIELDS, e)) for e in E], EQ[:, : self.S], R
+
+    def step_host(self, x_all, out=None, Tfree=300.0, istep=0, rebuild_lists=False):
+        """One step of every window through host buffers with one host
+        synchronisation (qnb_step_host): coordinates of all windows in (nwin x
+        natom x 3; pinned memory for an asynchronous copy), lists rebuilt with
+        the last cut-offs when rebuild_lists, the evaluation of compute_dev,
+        the gradient of all windows written into `out` (a C-contiguous
+        float64 array, e.g. a view of pinned memory; allocated if None).
+        Returns (gradient, E [nwin][7] with columns E_FIELDS, EQ
+        [nwin][nstates][6], restraints [nwin][2]) as arrays: per-window dicts
+        cost more host time than the call itself at 51 windows."""
+        W = self.nwin
+        xa = np.ascontiguousarray(x_all, dtype=np.float64)
+        assert xa.size == W * self.s.natom * 3
+        if out is None:
+            out = np.zeros((W, self.s.natom, 3))
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == xa.size
+        E = np.zeros((W, 7))
+        EQ = np.zeros((W, max(self.S, 1), 6))
+        R = np.zeros((W, 2))
+        self._check(self.lib.qnb_step_host(self.h, _p(xa), _p(out), Tfree, int(istep), int(bool(rebuild_lists)),
+                                           _p(E), _p(EQ), _p(R)))
+        return out, E, EQ[:, : self.S], R
 
     def energies_dev(self):
         """Energies of the last evaluation of every window (waits for it):
