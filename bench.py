@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the qdyn nonbonded hot path on GB300.
 
-Metric: MD steps/s summed over lambda windows (BASELINE metric), mixed form.
+Metric: MD steps/s summed over lambda windows (the headline metric of the reference workflow), mixed form.
 Workload: 51 lambda windows (lambda = 0, 0.02, ..., 1) of the seeded 25 A,
 2-state sphere (3,000-atom synthetic solute in 3-6-atom charge groups, 12 LJ
 types, 20 Q atoms, SPC water filling the sphere), 10 A cut-offs, Rcq 99,
@@ -537,7 +537,7 @@ def read_traffic(kernel):
 def run_e2e(args, s, sp, lams, prec, local, tuning=None):
     """Same metric end to end through the public C ABI with host buffers.
 
-    Batched path (the headline): one context holds every window, as a driver
+    Batched path (the headline): one context holds every window, as a program
     running all lambda windows in one process would; each step is one
     qnb_step_host call: all windows' coordinates in from pinned host memory,
     the lists rebuilt every 25th step, the evaluation, all gradients out to

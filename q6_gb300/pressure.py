@@ -12,7 +12,7 @@ energy in the new box and accepts with the Metropolis rule on
 (P in kcal/(mol A^3): the input's bar times 1.43836e-5).  The uniform draws
 come from numpy's seeded generator, not qdyn's randm stream.  The reference's
 atom_based_scaling option (scaling every atom, then SHAKE) is not supported.
-One box per context: the driver wants a single-window engine.
+One box per context: run_npt wants a single-window engine.
 """
 from __future__ import annotations
 
