@@ -15,6 +15,11 @@ waters, 20 Q atoms; 10 A cut-offs), where the CPU oracle would take minutes:
 * Translation invariance: moving every atom and both sphere centres by the
   same vector leaves the energies and the gradient unchanged up to the
   rounding of the moved coordinates.
+* Permutation invariance: relabelling the water molecules (every water has
+  the same parameters) maps the water-water rows onto the relabelled ones as
+  sets, exactly (the cut-off decisions are FP64 on unchanged coordinates),
+  and permutes the gradient, with the energies unchanged up to the order of
+  the sums.
 """
 import dataclasses
 
@@ -76,3 +81,33 @@ def test_translation_invariance_full_size(sphere, prec, etol, gtol):
     np.testing.assert_allclose(EQ1, EQ0, rtol=etol, atol=etol)
     scale = np.maximum(np.abs(d0), np.median(np.abs(d0)))
     assert np.all(np.abs(d1 - d0) <= gtol * scale)
+
+
+@pytest.mark.parametrize("prec,etol,gtol", [(PREC_FP64, 1e-9, 1e-9), (PREC_MIXED, 2e-5, 2e-3)])
+def test_water_relabelling_full_size(sphere, prec, etol, gtol):
+    from q6_gb300.qnb import ROWS_WW
+    s = sphere
+    ns, sa, W = s.nat_solute, s.solv_atom, s.nwat
+    perm = np.random.default_rng(4).permutation(W)          # new water k holds old water perm[k]
+    atom_map = np.arange(s.natom)
+    atom_map[ns:] = (ns + sa * perm[:, None] + np.arange(sa)).reshape(-1)   # new atom -> old atom
+    moved = dataclasses.replace(s, x=s.x[atom_map], excl=s.excl[atom_map])
+    out = []
+    for sysm in (s, moved):
+        with NonbondedEngine(sysm, precision=prec, use_lrf=False) as e:
+            d, E, EQ, _ = e.evaluate(sysm.x, [0.5, 0.5], cut=CUT)
+            rows = None
+            if prec == PREC_MIXED:
+                r, p = e.export_rows(ROWS_WW, 0)
+                rows = (r.astype(np.int64), p.astype(np.int64))
+        out.append((d, E, EQ, rows))
+    (d0, E0, EQ0, rows0), (d1, E1, EQ1, rows1) = out
+    for k in E0:
+        assert abs(E1[k] - E0[k]) <= etol * max(1.0, abs(E0[k])), (k, E1[k], E0[k])
+    np.testing.assert_allclose(EQ1, EQ0, rtol=etol, atol=etol)
+    scale = np.maximum(np.abs(d0), np.median(np.abs(d0)))
+    assert np.all(np.abs(d1 - d0[atom_map]) <= gtol * scale[atom_map])
+    if rows0 is not None:
+        key0 = np.sort(rows0[0] * W + rows0[1])
+        key1 = np.sort(perm[rows1[0]] * W + perm[rows1[1]])   # relabelled rows in the old numbering
+        assert len(key0) > 0 and np.array_equal(key0, key1)
