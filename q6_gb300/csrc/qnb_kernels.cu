@@ -1745,16 +1745,20 @@ __global__ void __launch_bounds__(kQBlock, 3) k_qenv(DevModel m, const DevState*
 // once.  The sums do not depend on the grid.  qw's parameters are the same
 // for all lanes (broadcast); qp's come from the [Q atom][solute atom] table,
 // so lanes holding consecutive solute atoms read consecutive entries.
-// Sums each of 16 values over the 32 lanes of a warp at once: a butterfly
-// whose step with lane bit o halves the vector, every lane keeping the half
-// its bit o selects and adding the partner's copy of it; after the steps 16,
-// 8, 4, 2 and a last exchange with lane ^ 1, lanes 2v and 2v + 1 hold the sum
-// of value v.  Each sum pairs the lanes as warp_sum does (lane i with i + 16,
-// then with i + 8, ...), so it is the same FP32 value warp_sum gives, for 30
-// shuffles and 15 additions fewer per 16 values than 16 warp_sum calls.
-__device__ __forceinline__ float reduce16_scatter(float (&g)[16], int lane) {
+// Sums each of N (16 or 32) values over the 32 lanes of a warp at once: a
+// butterfly whose step with lane bit o halves the vector, every lane keeping
+// the half its bit o selects and adding the partner's copy of it, until one
+// value is left; the remaining lane bits are summed as in warp_sum.  With
+// N = 32 lane v ends with the sum of value v, with N = 16 lanes 2v and 2v + 1
+// do.  Each sum pairs the lanes as warp_sum does (lane i with i + 16, then
+// with i + 8, ...), so it is the same FP32 value warp_sum gives, for N - 1
+// shuffles and additions instead of 5 N.
+template <int N>
+__device__ __forceinline__ float reduce_scatter(float (&g)[N], int lane) {
+    static_assert(N == 16 || N == 32, "16 or 32 values");
+    int o = 16;
 #pragma unroll
-    for (int o = 16, len = 16; o > 1; o >>= 1, len >>= 1) {
+    for (int len = N; len > 1; o >>= 1, len >>= 1) {
         const bool up = lane & o;
 #pragma unroll
         for (int i = 0; i < len / 2; ++i) {
@@ -1763,7 +1767,10 @@ __device__ __forceinline__ float reduce16_scatter(float (&g)[16], int lane) {
             g[i] = keep + __shfl_xor_sync(kFull, send, o);
         }
     }
-    return g[0] + __shfl_xor_sync(kFull, g[0], 1);
+    float v = g[0];
+#pragma unroll
+    for (; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
 }
 constexpr int kQRed = 5;   // Q atoms per transposed reduction (15 of its 16 values)
 
@@ -1799,7 +1806,7 @@ __global__ void __launch_bounds__(kQBlock) k_qenv_lanes(DevModel m, const DevSta
 #pragma unroll
         for (int st = 0; st < SMAX; ++st) pel[st] = pvdw[st] = 0.f;
         // Q atoms in blocks of kQRed: their 3 kQRed gradient components are
-        // summed over the warp in one transposed butterfly (reduce16_scatter)
+        // summed over the warp in one transposed butterfly (reduce_scatter)
         for (int q0 = 0; q0 < nq; q0 += kQRed) {
             float g[16];
 #pragma unroll
@@ -1828,7 +1835,7 @@ __global__ void __launch_bounds__(kQBlock) k_qenv_lanes(DevModel m, const DevSta
                 g[3 * b + 1] = gy;
                 g[3 * b + 2] = gz;
             }
-            const float v = reduce16_scatter(g, lane);
+            const float v = reduce_scatter<16>(g, lane);
             const int idx = lane >> 1;   // the component this lane pair holds
             if (!(lane & 1) && idx < 3 * kQRed && 3 * q0 + idx < 3 * nq) atomicAdd(&red[3 * q0 + idx], to_fix_alu(v));
         }
@@ -3491,18 +3498,38 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
         // warp sums in a fixed shuffle order, stored without atomics
         // (k_apply_fixed converts each atom's sum once to 64-bit fixed point
         // and adds it as an integer; k_row_sums adds the energies in FP64)
-        float e0 = warp_sum(0.5f * rpel), e1 = warp_sum(0.5f * rpvdw), e2 = warp_sum(rwel), e3 = warp_sum(rwvdw);
-        if (lane == 0) s.erow[g] = make_float4(e0, e1, e2, e3);
+        if constexpr (MAXG <= 8) {
+            // the row atoms' 3 x 8 gradient components and the 4 energies in
+            // one transposed warp sum: lane v ends with value v
+            float gv[32];
 #pragma unroll
-        for (int a = 0; a < MAXG; ++a) {
-            if (a >= n1) break;   // warp-uniform
-            float v0 = warp_sum(f[a][0]), v1 = warp_sum(f[a][1]), v2 = warp_sum(f[a][2]);
-            if (lane == 0) {
-                int i = m.gatom[a0 + a];
-                float* fr = s.frow + 3 * i;
-                fr[0] = qa[a] ? 0.f : v0;
-                fr[1] = qa[a] ? 0.f : v1;
-                fr[2] = qa[a] ? 0.f : v2;
+            for (int a = 0; a < 8; ++a) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) gv[3 * a + c] = a < MAXG ? f[a < MAXG ? a : 0][c] : 0.f;
+            }
+            gv[24] = 0.5f * rpel, gv[25] = 0.5f * rpvdw, gv[26] = rwel, gv[27] = rwvdw;
+            gv[28] = gv[29] = gv[30] = gv[31] = 0.f;
+            const float v = reduce_scatter<32>(gv, lane);
+            if (lane < 3 * n1) {
+                const int i = m.gatom[a0 + lane / 3];
+                s.frow[3 * i + lane % 3] = m.iqatom[i] >= 0 ? 0.f : v;
+            } else if (lane >= 24 && lane < 28) {
+                reinterpret_cast<float*>(s.erow + g)[lane - 24] = v;
+            }
+        } else {
+            float e0 = warp_sum(0.5f * rpel), e1 = warp_sum(0.5f * rpvdw), e2 = warp_sum(rwel), e3 = warp_sum(rwvdw);
+            if (lane == 0) s.erow[g] = make_float4(e0, e1, e2, e3);
+#pragma unroll
+            for (int a = 0; a < MAXG; ++a) {
+                if (a >= n1) break;   // warp-uniform
+                float v0 = warp_sum(f[a][0]), v1 = warp_sum(f[a][1]), v2 = warp_sum(f[a][2]);
+                if (lane == 0) {
+                    int i = m.gatom[a0 + a];
+                    float* fr = s.frow + 3 * i;
+                    fr[0] = qa[a] ? 0.f : v0;
+                    fr[1] = qa[a] ? 0.f : v1;
+                    fr[2] = qa[a] ? 0.f : v2;
+                }
             }
         }
     }
