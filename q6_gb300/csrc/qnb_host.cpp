@@ -1231,8 +1231,8 @@ int build_lists(qnb_context* c, const Cut& cut, int nw) {
             if (!c->m.box) {
                 if (do_qp) launch_build_qp(L, c->d_qnear, cut.rcq2), ++nl;
                 if (do_qw) launch_build_qw(L, cut), ++nl;
-                if (c->mixed && (do_qp || do_qw)) launch_clear_fq(L), ++nl;   // atoms may leave the Q lists
             }
+            if (c->mixed && (do_qp || do_qw)) launch_clear_fq(L), ++nl;   // atoms may leave the Q lists
         });
         c->launches += nl;
         if (c->use_lrf) CU(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
@@ -1305,6 +1305,7 @@ int compute_nonbond(qnb_context* c, int md, int nw, const SideWork& side = SideW
             int nb = 0;
             timed_on(c, LB.st, K_QW, [&] { nb = launch_box_nonbond(LB, md, mx, c->d_iwhich, c->last_cut.rcq2, 0); });
             nl += nb;
+            c->qenv_pending = true;   // the box Q terms store the environment atoms' gradients in fq
             if (md && c->nsi) timed_on(c, LB.st, K_WW, [&] { launch_solvent_internal(LB, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
         } else {
             if (c->m.natom > c->m.nat_solute) {
@@ -1330,6 +1331,7 @@ int compute_nonbond(qnb_context* c, int md, int nw, const SideWork& side = SideW
     if (c->m.box) {   // periodic box: the *_box routines, src/potene.f90:326-343
         int nb = 0;
         timed(c, K_PP, [&] { nb = launch_box_nonbond(L, md, mx, c->d_iwhich, c->last_cut.rcq2, 1); });
+        if (mx) c->qenv_pending = true;   // the box Q terms store the environment atoms' gradients in fq
         // src/potene.f90:326-339 and 373-377: solvent internal pairs, then the LRF Taylor terms
         if (md && c->nsi) timed(c, K_WW, [&] { launch_solvent_internal(L, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
         if (c->use_lrf && md) timed(c, K_LRF_TAYLOR, [&] { launch_lrf_taylor(L, c->d_iwhich, mx); }), ++nl;

@@ -1745,6 +1745,15 @@ __global__ void __launch_bounds__(kQBlock, 3) k_qenv(DevModel m, const DevState*
 // once.  The sums do not depend on the grid.  qw's parameters are the same
 // for all lanes (broadcast); qp's come from the [Q atom][solute atom] table,
 // so lanes holding consecutive solute atoms read consecutive entries.
+// periodic box, mixed form's FP32 pair geometry: packed coordinates
+// (xpcent-centred) and an FP32 lattice shift of a against b (boxlength *
+// nint((a - b) / boxlength)); a pair vector is shift - (x_i - x_j)
+__device__ __forceinline__ float3 box_shift_f(const DevModel& m, float4 a, float4 b) {
+    return make_float3((float)m.boxl[0] * roundf((a.x - b.x) * (float)m.inv_boxl[0]),
+                       (float)m.boxl[1] * roundf((a.y - b.y) * (float)m.inv_boxl[1]),
+                       (float)m.boxl[2] * roundf((a.z - b.z) * (float)m.inv_boxl[2]));
+}
+
 // Sums each of N (16 or 32) values over the 32 lanes of a warp at once: a
 // butterfly whose step with lane bit o halves the vector, every lane keeping
 // the half its bit o selects and adding the partner's copy of it, until one
@@ -1774,8 +1783,16 @@ __device__ __forceinline__ float reduce_scatter(float (&g)[N], int lane) {
 }
 constexpr int kQRed = 5;   // Q atoms per transposed reduction (15 of its 16 values)
 
-template <bool SPC, bool WATER, int SMAX>
-__global__ void __launch_bounds__(kQBlock) k_qenv_lanes(DevModel m, const DevState* __restrict__ states) {
+//
+// BOX (nonbond_qp_box, src/nonbondene.f90:5234-5335; nonbond_qw_box /
+// nonbond_qw_spc_box, 5422-5505, 5771-5881): each unit is taken at the image
+// next to qswitch, shifted by the lattice vector of qswitch against the
+// water's first atom (qw) or against the first atom of the solute atom's
+// group within Rcq of qswitch (qp, nbqp_cgp; iwhich, rq2); the pair vector
+// is shift - (x_q - x_j).
+template <bool SPC, bool WATER, int SMAX, bool BOX = false>
+__global__ void __launch_bounds__(kQBlock) k_qenv_lanes(DevModel m, const DevState* __restrict__ states,
+                                                        const int* __restrict__ iwhich = nullptr, float rq2 = 0.f) {
     const DevState& s = states[blockIdx.y];
     __shared__ unsigned long long red[3 * kMaxQ];
     __shared__ float4 sq[kMaxQ];
@@ -1802,6 +1819,26 @@ __global__ void __launch_bounds__(kQBlock) k_qenv_lanes(DevModel m, const DevSta
             gj[a][0] = gj[a][1] = gj[a][2] = 0.f;
             xj[a] = (act && a < na) ? s.xq[j0 + a] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
+        float3 sh = make_float3(0.f, 0.f, 0.f);   // the unit's lattice shift (BOX)
+        if (BOX && act) {
+            const float4 xs = s.xq[m.qswitch];
+            if (WATER) {
+                sh = box_shift_f(m, xs, xj[0]);
+            } else {
+                const int grp = iwhich[j0];
+                int ref = m.gatom[m.gslot[grp]];
+                for (int b = m.gslot[grp]; b < m.gslot[grp + 1]; ++b) {
+                    const float4 xb = s.xq[m.gatom[b]];
+                    const float3 t3 = box_shift_f(m, xb, xs);
+                    const float dx = t3.x - (xb.x - xs.x), dy = t3.y - (xb.y - xs.y), dz = t3.z - (xb.z - xs.z);
+                    if (dx * dx + dy * dy + dz * dz <= rq2) {
+                        ref = m.gatom[b];
+                        break;
+                    }
+                }
+                sh = box_shift_f(m, xs, s.xq[ref]);
+            }
+        }
         float pel[SMAX], pvdw[SMAX];
 #pragma unroll
         for (int st = 0; st < SMAX; ++st) pel[st] = pvdw[st] = 0.f;
@@ -1822,7 +1859,12 @@ __global__ void __launch_bounds__(kQBlock) k_qenv_lanes(DevModel m, const DevSta
                     for (int a = 0; a < NA; ++a) {
                         if (a >= na) break;
                         const bool lj = !WATER || !SPC || a == 0;
-                        float tx = xj[a].x - xi.x, ty = xj[a].y - xi.y, tz = xj[a].z - xi.z;
+                        float tx, ty, tz;
+                        if (BOX) {
+                            tx = sh.x - (xi.x - xj[a].x), ty = sh.y - (xi.y - xj[a].y), tz = sh.z - (xi.z - xj[a].z);
+                        } else {
+                            tx = xj[a].x - xi.x, ty = xj[a].y - xi.y, tz = xj[a].z - xi.z;
+                        }
                         float r = rsqrtf(tx * tx + ty * ty + tz * tz), r2 = r * r;
                         const QParF* P = WATER ? m.qw_tabf + (iq * m.sa + a) * S
                                                : m.qp_tabft + ((size_t)iq * m.nat_solute + j0) * S;
@@ -4390,13 +4432,7 @@ void launch_pair_sets(const Launch& L, const PairSetDev& p) {
 // packed coordinates with an FP32 shift (fixed-point sums), as its sphere
 // kernels do.
 // -----------------------------------------------------------------------------
-// the mixed form's FP32 pair geometry: packed coordinates (xpcent-centred)
-// and an FP32 shift; vec = shift - (x_i - x_j)
-__device__ __forceinline__ float3 box_shift_f(const DevModel& m, float4 a, float4 b) {
-    return make_float3((float)m.boxl[0] * roundf((a.x - b.x) * (float)m.inv_boxl[0]),
-                       (float)m.boxl[1] * roundf((a.y - b.y) * (float)m.inv_boxl[1]),
-                       (float)m.boxl[2] * roundf((a.z - b.z) * (float)m.inv_boxl[2]));
-}
+// (the mixed form's lattice shift box_shift_f is defined with the Q kernels)
 struct BoxPairF {
     float tx, ty, tz, r2, r;
 };
@@ -4751,10 +4787,11 @@ __global__ void __launch_bounds__(256) k_box_ww(DevModel m, const DevState* __re
 }
 
 // nonbond_qp_box, src/nonbondene.f90:5234-5335, and nonbond_qw_box /
-// nonbond_qw_spc_box, 5422-5505, 5771-5881 (nbe_qx, nbe_qspc): one thread per
-// (listed unit, Q atom); the unit's shift brings it next to qswitch, taken
-// from the first group atom inside Rcq (qp, nbqp_cgp) or the water's first
-// atom (qw).  Per-state energies are summed in registers.
+// nonbond_qw_spc_box, 5422-5505, 5771-5881 (nbe_qx, nbe_qspc), FP64 form
+// (the mixed form runs k_qenv_lanes<..., BOX>): one thread per (listed unit,
+// Q atom); the unit's shift brings it next to qswitch, taken from the first
+// group atom inside Rcq (qp, nbqp_cgp) or the water's first atom (qw).
+// Per-state energies are summed in registers.
 template <bool MIX, bool WATER, bool SPC>
 __global__ void __launch_bounds__(256) k_box_q(DevModel m, const DevState* __restrict__ states,
                                                const int* __restrict__ iwhich, double rcq2) {
@@ -4768,61 +4805,6 @@ __global__ void __launch_bounds__(256) k_box_q(DevModel m, const DevState* __res
          t += (int64_t)gridDim.x * blockDim.x) {
         int u = (int)(t / nq), iq = (int)(t % nq);
         int i = m.iqseq[iq];
-        if constexpr (MIX) {   // FP32 pair arithmetic (QParF tables), as the mixed Q kernels
-            const float4 xi = s.xq[i], xs = s.xq[m.qswitch];
-            int j0, na;
-            float3 sh;
-            if (WATER) {
-                j0 = m.nat_solute + m.sa * s.qw[u];
-                na = m.sa;
-                sh = box_shift_f(m, xs, s.xq[j0]);
-            } else {
-                j0 = s.qp[u];
-                na = 1;
-                int g = iwhich[j0], ref = m.gatom[m.gslot[g]];
-                const float rq2 = (float)rcq2;
-                for (int a = m.gslot[g]; a < m.gslot[g + 1]; ++a) {
-                    float4 xa = s.xq[m.gatom[a]];
-                    float3 t3 = box_shift_f(m, xa, xs);
-                    float dx = t3.x - (xa.x - xs.x), dy = t3.y - (xa.y - xs.y), dz = t3.z - (xa.z - xs.z);
-                    if (dx * dx + dy * dy + dz * dz <= rq2) {
-                        ref = m.gatom[a];
-                        break;
-                    }
-                }
-                sh = box_shift_f(m, xs, s.xq[ref]);
-            }
-            float gi[3] = {0.f, 0.f, 0.f};
-            for (int a = 0; a < na; ++a) {
-                int j = j0 + a;
-                BoxPairF q = box_pair_f(xi, s.xq[j], sh);
-                bool lj = !(WATER && SPC) || a == 0;
-                float dvs = 0.0f;
-                float r6hc = __fdividef(1.0f, q.r2 * q.r2 * q.r2);
-                for (int st = 0; st < S; ++st) {
-                    const QParF P = WATER ? m.qw_tabf[((size_t)iq * m.sa + a) * S + st]
-                                          : m.qp_tabf[((size_t)j * nq + iq) * S + st];
-                    float lam = s.lambdaf[st];
-                    if (lj) {
-                        float vel, vdw, dv;
-                        nbe_qx_f(q.r2, q.r, r6hc, P.A, P.B, P.el, P.sc, lam, vel, vdw, dv);
-                        dvs += dv;
-                        eel[st].add(vel);
-                        evdw[st].add(vdw);
-                    } else {
-                        float vel = P.el * q.r;
-                        dvs += -q.r2 * vel * lam;
-                        eel[st].add(vel);
-                    }
-                }
-                gi[0] -= q.tx * dvs;
-                gi[1] -= q.ty * dvs;
-                gi[2] -= q.tz * dvs;
-                acc.grad(j, q.tx * dvs, q.ty * dvs, q.tz * dvs);
-            }
-            acc.grad(i, gi[0], gi[1], gi[2]);
-            continue;
-        }
         double sx, sy, sz;
         int j0, na;
         if (WATER) {
@@ -4875,6 +4857,16 @@ __global__ void __launch_bounds__(256) k_box_q(DevModel m, const DevState* __res
     }
 }
 
+// the mixed form's box Q terms (k_qenv_lanes<..., BOX>)
+template <bool WATER>
+void launch_box_qenv(const Launch& L, const int* iwhich, double rcq2, dim3 g) {
+    const bool spc = L.m.spc != 0, s4 = L.m.S <= 4;
+    const float rq2 = (float)rcq2;
+#define QB(SPC, SM) k_qenv_lanes<SPC, WATER, SM, true><<<g, kQBlock, 0, L.st>>>(L.m, L.ds, iwhich, rq2)
+    if (spc) { if (s4) QB(true, 4); else QB(true, kMaxStates); }
+    else { if (s4) QB(false, 4); else QB(false, kMaxStates); }
+#undef QB
+}
 int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, double rcq2, int pairs) {
     const DevModel& m = L.m;
     int nl = 0;
@@ -4895,16 +4887,22 @@ int launch_box_nonbond(const Launch& L, int md, int mixed, const int* iwhich, do
             nl += 2;
         }
         if (m.nqat > 0) {
-            dim3 g = grid(L.s0.cap_qw * m.nqat);
-            if (mixed) { if (m.spc) k_box_q<true, true, true><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2); else k_box_q<true, true, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2); }
-            else { if (m.spc) k_box_q<false, true, true><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2); else k_box_q<false, true, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2); }
+            if (mixed) {   // lane = water, Q atoms looped (k_qenv_lanes' box form); environment gradient into fq
+                launch_box_qenv<true>(L, iwhich, rcq2, grid_for(L.s0.cap_qw * 32, kQBlock, L.tu.v[T_QW], L.nwin));
+            } else {
+                dim3 g = grid(L.s0.cap_qw * m.nqat);
+                if (m.spc) k_box_q<false, true, true><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2); else k_box_q<false, true, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2);
+            }
             ++nl;
         }
     }
     if (m.nqat > 0 && m.nat_solute > 0) {
-        dim3 g = grid(L.s0.cap_qp * m.nqat);
-        if (mixed) k_box_q<true, false, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2);
-        else k_box_q<false, false, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2);
+        if (mixed) {
+            launch_box_qenv<false>(L, iwhich, rcq2, grid_for(L.s0.cap_qp * 32, kQBlock, L.tu.v[T_QP], L.nwin));
+        } else {
+            dim3 g = grid(L.s0.cap_qp * m.nqat);
+            k_box_q<false, false, false><<<g, 256, 0, L.st>>>(m, L.ds, iwhich, rcq2);
+        }
         ++nl;
     }
     return nl;
