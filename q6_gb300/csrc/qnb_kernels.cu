@@ -3590,13 +3590,17 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
     const float4* __restrict__ xq = s.xq;
     int lane = threadIdx.x & 31;
     const int sa = m.sa;
+    // SPC rows: 3-atom molecules (the launcher's choice), so the row's atom
+    // arrays hold 3 entries and a partner's atoms are loaded one iteration
+    // ahead
+    constexpr int NA = SPC ? 3 : kMaxSolv;
     for (int w = warp_id_global(); w < m.nwat; w += warps_total()) {
         int nww = s.cnt_ww[w], nwg = s.cnt_wg[w];   // an empty row still writes its zeros
         int i0 = m.nat_solute + sa * w;
-        float4 xa[kMaxSolv];
-        float f[kMaxSolv][3];
+        float4 xa[NA];
+        float f[NA][3];
 #pragma unroll
-        for (int a = 0; a < kMaxSolv; ++a) {
+        for (int a = 0; a < NA; ++a) {
             f[a][0] = f[a][1] = f[a][2] = 0.f;
             xa[a] = a < sa ? xq[i0 + a] : make_float4(0, 0, 0, 0);
         }
@@ -3622,6 +3626,43 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
           __syncwarp();
           const int* buf = sh_ww[wib][ch & 1];
           const int n = min(kRowChunk, nww - ch * kRowChunk);
+          if constexpr (SPC) {
+            float4 nx0 = make_float4(0.f, 0.f, 0.f, 0.f), nx1 = nx0, nx2 = nx0;
+            int nw2 = 0;
+            if (lane < n) {
+                nw2 = buf[lane];
+                const int j = m.nat_solute + 3 * nw2;
+                nx0 = xq[j], nx1 = xq[j + 1], nx2 = xq[j + 2];
+            }
+            for (int k = lane; k < n; k += kWarp) {
+              const int w2 = nw2;
+              const float4 xp[3] = {nx0, nx1, nx2};
+              if (k + kWarp < n) {   // the next partner, one iteration ahead
+                  nw2 = buf[k + kWarp];
+                  const int j = m.nat_solute + 3 * nw2;
+                  nx0 = xq[j], nx1 = xq[j + 1], nx2 = xq[j + 2];
+              }
+              float pel = 0.f, pvdw = 0.f;
+#pragma unroll
+              for (int b = 0; b < 3; ++b) {
+                  float4 xb = xp[b];
+                  if (BOX) xb = at_image(m, xb, xa[0], xp[0]);
+#pragma unroll
+                  for (int a = 0; a < 3; ++a) {
+                      const int kk = a * kMaxSolv + b;
+                      const bool lj = a == 0 && b == 0;
+                      float vel, vdw;
+                      pair_f(xa[a], xb, m.wwAf[kk], m.wwBf[kk], m.wwEf[kk], lj, f[a][0], f[a][1], f[a][2], vel, vdw);
+                      pel += vel;
+                      if (lj) pvdw += vdw;
+                  }
+              }
+              if (w < w2) {   // each molecule pair's energy once
+                  rel += pel;
+                  rvdw += pvdw;
+              }
+            }
+          } else {
           for (int k = lane; k < n; k += kWarp) {
             int w2 = buf[k];
             int j0 = m.nat_solute + sa * w2;
@@ -3633,20 +3674,20 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
                 float4 xb = xq[j0 + b];
                 if (BOX) xb = at_image(m, xb, xa[0], xr);
 #pragma unroll
-                for (int a = 0; a < kMaxSolv; ++a) {
+                for (int a = 0; a < NA; ++a) {
                     if (a >= sa) break;
                     int kk = a * kMaxSolv + b;
-                    bool lj = !SPC || (a == 0 && b == 0);
                     float vel, vdw;
-                    pair_f(xa[a], xb, m.wwAf[kk], m.wwBf[kk], m.wwEf[kk], lj, f[a][0], f[a][1], f[a][2], vel, vdw);
+                    pair_f(xa[a], xb, m.wwAf[kk], m.wwBf[kk], m.wwEf[kk], true, f[a][0], f[a][1], f[a][2], vel, vdw);
                     pel += vel;
-                    if (lj) pvdw += vdw;
+                    pvdw += vdw;
                 }
             }
             if (w < w2) {   // each molecule pair's energy once
                 rel += pel;
                 rvdw += pvdw;
             }
+          }
           }
           __syncwarp();   // this buffer is refilled two chunks later
         }
@@ -3664,7 +3705,7 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
                 if (BOX) xb = at_image(m, xb, xa[0], xr);
                 int tj = m.iac[j];
 #pragma unroll
-                for (int a = 0; a < kMaxSolv; ++a) {
+                for (int a = 0; a < NA; ++a) {
                     if (a >= sa) break;
                     bool ljw = (m.wlj_mask >> a) & 1u;
                     float4 p = ljw ? lj(tj, m.wtype[a]) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -3678,7 +3719,7 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
         float e0 = warp_sum(rel), e1 = warp_sum(rvdw);
         if (lane == 0) s.erow[m.ncgp_solute + w] = make_float4(e0, e1, 0.f, 0.f);
 #pragma unroll
-        for (int a = 0; a < kMaxSolv; ++a) {
+        for (int a = 0; a < NA; ++a) {
             if (a >= sa) break;
             float v0 = warp_sum(f[a][0]), v1 = warp_sum(f[a][1]), v2 = warp_sum(f[a][2]);
             if (lane == 0) {
@@ -3869,10 +3910,11 @@ void launch_rows_water(const Launch& L) {
     if (L.m.nwat == 0) return;
     dim3 g = grid_for((int64_t)L.m.nwat * 32, 128, L.tu.v[T_ROWS_WATER], L.nwin);
     int sm = lj_smem(L.m);
+    const bool spc = L.m.spc && L.m.sa == 3;   // the SPC rows assume 3-atom molecules
     if (L.m.box) {
-        if (L.m.spc) k_rows_water<true, true><<<g, 128, sm, L.st>>>(L.m, L.ds);
+        if (spc) k_rows_water<true, true><<<g, 128, sm, L.st>>>(L.m, L.ds);
         else k_rows_water<false, true><<<g, 128, sm, L.st>>>(L.m, L.ds);
-    } else if (L.m.spc) k_rows_water<true, false><<<g, 128, sm, L.st>>>(L.m, L.ds);
+    } else if (spc) k_rows_water<true, false><<<g, 128, sm, L.st>>>(L.m, L.ds);
     else k_rows_water<false, false><<<g, 128, sm, L.st>>>(L.m, L.ds);
 }
 void launch_ww(const Launch& L, int mixed) {
