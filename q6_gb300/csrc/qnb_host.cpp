@@ -75,7 +75,7 @@ struct qnb_context {
     // main stream, the Q-environment / LRF Taylor kernels on stream2 and the
     // rest of the step's terms on stream3, joined before the gradient apply
     cudaStream_t stream3 = nullptr;
-    cudaEvent_t ev_pk = nullptr, ev_jb = nullptr, ev_jc = nullptr, ev_rw = nullptr;
+    cudaEvent_t ev_pk = nullptr, ev_jb = nullptr, ev_jc = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int mixed = 0;
     int use_lrf = 1;
@@ -1006,7 +1006,6 @@ int alloc_state(qnb_context* c) {
         CU(cudaMemset(s.frow, 0, sizeof(float) * 3 * m.natom));   // atoms outside every row stay 0
         TRY(c->alloc(&s.fq, (size_t)3 * m.natom));
         CU(cudaMemset(s.fq, 0, sizeof(float) * 3 * m.natom));     // atoms outside the Q lists stay 0
-        TRY(c->alloc(&s.erow, (size_t)std::max(1, m.ncgp_solute + m.nwat)));
         TRY(c->alloc(&s.fix, n3));
         s.e = c->e_all + (size_t)kNumE * w;
         s.efix = c->efix_all + (size_t)kNumE * w;
@@ -1286,18 +1285,12 @@ int compute_nonbond(qnb_context* c, int md, int nw, const SideWork& side = SideW
             LC.st = c->stream3;
         }
         // rows: pp + the solute side of pw on the main stream, ww + the water
-        // side of pw first on the third branch; the row energies' sum waits
-        // for both
+        // side of pw first on the third branch (each row adds its energies to
+        // the window's fixed-point slots itself)
         if (md) {
-            const bool wrows = c->m.natom > c->m.nat_solute;
-            if (wrows) {
-                timed_on(c, LC.st, K_WW, [&] { launch_rows_water(LC); }), ++nl;
-                if (br) CU(cudaEventRecord(c->ev_rw, LC.st));
-            }
+            if (c->m.natom > c->m.nat_solute) timed_on(c, LC.st, K_WW, [&] { launch_rows_water(LC); }), ++nl;
             timed(c, K_PP, [&] { launch_rows_solute(L, c->maxg); });   // the class times the solute rows alone
-            if (wrows && br) CU(cudaStreamWaitEvent(c->stream, c->ev_rw, 0));
-            launch_row_sums(L);
-            nl += 2;
+            ++nl;
             c->rows_pending = true;   // frow holds this evaluation's row gradients
         }
         // Q environment, solvent internal pairs, LRF Taylor terms
@@ -1350,11 +1343,8 @@ int compute_nonbond(qnb_context* c, int md, int nw, const SideWork& side = SideW
             if (md && c->nsi) timed(c, K_WW, [&] { launch_solvent_internal(L, c->d_si, c->d_sip, c->nsi, mx); }), ++nl;
         }
         if (md) {
-            timed(c, K_PP, [&] {
-                launch_rows_solute(L, c->maxg);
-                launch_row_sums(L);
-            });
-            nl += 2;
+            timed(c, K_PP, [&] { launch_rows_solute(L, c->maxg); });
+            ++nl;
             c->rows_pending = true;   // frow holds this evaluation's row gradients
         }
     } else {
@@ -1496,7 +1486,6 @@ int qnb_create_batch(const qnb_topology* t, const qnb_options* opt, int32_t nwin
         cudaEventCreateWithFlags(&c->ev_pk, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_jb, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_jc, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_rw, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
         rc = fail(QNB_ERR_CUDA, "stream creation failed");
@@ -1541,7 +1530,6 @@ int qnb_destroy(qnb_context* c) {
     if (c->ev_pk) cudaEventDestroy(c->ev_pk);
     if (c->ev_jb) cudaEventDestroy(c->ev_jb);
     if (c->ev_jc) cudaEventDestroy(c->ev_jc);
-    if (c->ev_rw) cudaEventDestroy(c->ev_rw);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->stream) cudaStreamDestroy(c->stream);

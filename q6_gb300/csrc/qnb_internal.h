@@ -178,7 +178,6 @@ struct DevState {
     double* d;           // [natom*3] gradient accumulator (FP64 mode target)
     float4* xq;          // [natom] FP32 (x,y,z,charge) for the mixed form
     float* frow;         // [natom*3] mixed form: row-kernel gradient of each atom's own row (FP32 warp sum)
-    float4* erow;        // [ncgp_solute+nwat] mixed form: row energies (pp el, vdw, pw el, vdw | ww el, vdw)
     float* fq;           // [natom*3] mixed form: Q-environment gradient of each listed qp atom / qw water
     unsigned long long* fix;   // [natom*3] fixed-point gradient (mixed form)
     double* e;           // [kNumE] FP64 energies
@@ -295,7 +294,6 @@ void launch_nonbond_qq(const Launch& L, int mixed);
 void launch_lrf_taylor(const Launch& L, const int* iwhich, int mixed);
 void launch_apply_fixed(const Launch& L, int rows, int qenv);
 void launch_clear_fq(const Launch& L);
-void launch_row_sums(const Launch& L);
 void launch_solvent_internal(const Launch& L, const int2* ij, const double* par, int n, int mixed);
 
 // kernel classes timed by the optional event profiler

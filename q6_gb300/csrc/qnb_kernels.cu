@@ -2171,46 +2171,6 @@ __global__ void k_apply_fixed(int n, const DevState* __restrict__ states, int ro
     }
 }
 
-// Row energies of the mixed form summed in FP64 (one block per window, a
-// fixed reduction tree): the pp/pw/ww energy slots.
-constexpr int kRowSumBlock = 512;
-__global__ void __launch_bounds__(kRowSumBlock) k_row_sums(DevModel m, const DevState* __restrict__ states) {
-    const DevState& s = states[blockIdx.x];
-    __shared__ double red[kRowSumBlock / 32][6];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    const int nrows = m.ncgp_solute + m.nwat;
-    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
-        float4 e = s.erow[r];
-        if (r < m.ncgp_solute) {
-            a[0] += e.x; a[1] += e.y; a[2] += e.z; a[3] += e.w;
-        } else {
-            a[4] += e.x; a[5] += e.y;
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < 6; ++k) a[k] = warp_sum(a[k]);
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < 6; ++k) red[warp][k] = a[k];
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            double v = lane < kRowSumBlock / 32 ? red[lane][k] : 0.0;
-            a[k] = warp_sum(v);
-        }
-        if (lane == 0) {   // the only writer of these slots in the mixed form
-            s.e[E_PP_EL] += a[0];
-            s.e[E_PP_VDW] += a[1];
-            s.e[E_PW_EL] += a[2];
-            s.e[E_PW_VDW] += a[3];
-            s.e[E_WW_EL] += a[4];
-            s.e[E_WW_VDW] += a[5];
-        }
-    }
-}
-
 // =============================================================================
 // Spherical-boundary solvent terms (FP64 in both forms)
 // =============================================================================
@@ -3284,7 +3244,6 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
         int a0 = m.gslot[g], n1 = m.gslot[g + 1] - a0;
         if (n1 > MAXG) {   // a Q-only group larger than the rows handle: empty row, zero gradient
             for (int a = lane; a < 3 * n1; a += kWarp) s.frow[3 * m.gatom[a0 + a / 3] + a % 3] = 0.f;
-            if (lane == 0) s.erow[g] = make_float4(0.f, 0.f, 0.f, 0.f);
             continue;
         }
         // periodic box: the row group's reference atom (its lattice shifts)
@@ -3539,7 +3498,9 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
         // The row owns its atoms' pp and pw gradient and its energies: FP32
         // warp sums in a fixed shuffle order, stored without atomics
         // (k_apply_fixed converts each atom's sum once to 64-bit fixed point
-        // and adds it as an integer; k_row_sums adds the energies in FP64)
+        // and adds it as an integer); the row's four energies are converted
+        // to fixed point once and added to the window's energy slots as
+        // integers (order-free, so the step needs no separate energy sum)
         if constexpr (MAXG <= 8) {
             // the row atoms' 3 x 8 gradient components and the 4 energies in
             // one transposed warp sum: lane v ends with value v
@@ -3555,12 +3516,17 @@ __global__ void __launch_bounds__(128, rows_min_blocks<MAXG, GEOM>()) k_rows_sol
             if (lane < 3 * n1) {
                 const int i = m.gatom[a0 + lane / 3];
                 s.frow[3 * i + lane % 3] = m.iqatom[i] >= 0 ? 0.f : v;
-            } else if (lane >= 24 && lane < 28) {
-                reinterpret_cast<float*>(s.erow + g)[lane - 24] = v;
+            } else if (lane >= 24 && lane < 28 && v != 0.f) {   // E_PP_EL, E_PP_VDW, E_PW_EL, E_PW_VDW
+                atomicAdd(s.efix + E_PP_EL + (lane - 24), to_fix(v));
             }
         } else {
             float e0 = warp_sum(0.5f * rpel), e1 = warp_sum(0.5f * rpvdw), e2 = warp_sum(rwel), e3 = warp_sum(rwvdw);
-            if (lane == 0) s.erow[g] = make_float4(e0, e1, e2, e3);
+            if (lane == 0) {
+                const float ev[4] = {e0, e1, e2, e3};
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (ev[k] != 0.f) atomicAdd(s.efix + E_PP_EL + k, to_fix(ev[k]));
+            }
 #pragma unroll
             for (int a = 0; a < MAXG; ++a) {
                 if (a >= n1) break;   // warp-uniform
@@ -3717,7 +3683,10 @@ __global__ void __launch_bounds__(128, 8) k_rows_water(DevModel m, const DevStat
         __syncwarp();   // sh_wg is refilled by the next row
         // row gradient and energies stored as in k_rows_solute
         float e0 = warp_sum(rel), e1 = warp_sum(rvdw);
-        if (lane == 0) s.erow[m.ncgp_solute + w] = make_float4(e0, e1, 0.f, 0.f);
+        if (lane == 0) {
+            if (e0 != 0.f) atomicAdd(s.efix + E_WW_EL, to_fix(e0));
+            if (e1 != 0.f) atomicAdd(s.efix + E_WW_VDW, to_fix(e1));
+        }
 #pragma unroll
         for (int a = 0; a < NA; ++a) {
             if (a >= sa) break;
@@ -3985,10 +3954,6 @@ __global__ void k_clear_fq(int n, const DevState* __restrict__ states) {
 void launch_clear_fq(const Launch& L) {
     int n = 3 * L.m.natom;
     k_clear_fq<<<grid_for(n, 256, 4, L.nwin), 256, 0, L.st>>>(n, L.ds);
-}
-void launch_row_sums(const Launch& L) {
-    if (L.m.ncgp_solute + L.m.nwat == 0) return;
-    k_row_sums<<<L.nwin, kRowSumBlock, 0, L.st>>>(L.m, L.ds);
 }
 // =============================================================================
 // Bonded terms: FP64 in the plain form; FP32 arithmetic in the mixed form
