@@ -236,16 +236,36 @@ def run_ours(args, rank, world, local):
         eng.compute_dev(Tfree=300.0, istep=istep, sync=False)
 
     snap = energy_snapshot(eng)      # mixed-form energies for the per-term error against FP64
-    # warm-up, every kernel class bracketed with events: picks the dominant
-    # per-step class for the roofline
+    # the dominant per-step class for the roofline: two steps with every class
+    # bracketed and the evaluation's branches off, so each class is timed alone
+    # (beside the other branches a small kernel's span includes its wait for
+    # block slots)
+    eng.set_concurrency(False)
     eng.profile(True)
-    for i in range(args.warmup):
+    for i in range(2):
         step(i)
         eng.profile_collect()
     torch.cuda.synchronize()
     kt_warm = eng.kernel_times()
+    eng.profile(False)
+    eng.set_concurrency(True)
     per_step = [c for c in KERNEL_CLASSES if c not in ("build", "lrf_build") and kt_warm[c][1] > 0]
     dom = max(per_step, key=lambda c: kt_warm[c][0])
+    # warm-up in the timed configuration (branches on, the dominant class
+    # bracketed): every step graph the timed steps replay is captured here,
+    # the watpol-update step's too (every itdis steps)
+    istep0 = first_rebuild_step(args.warmup)
+    eng.profile_classes([dom])
+    for i in range(args.warmup):
+        step(i)
+        eng.profile_collect()
+    itdis = int(round(sp.itdis))
+    upd = [k for k in range(istep0, istep0 + args.steps) if itdis > 0 and k > 0 and k % itdis == 0]
+    if upd:
+        eng.compute_dev(Tfree=300.0, istep=upd[0], sync=False)
+        eng.profile_collect()
+    torch.cuda.synchronize()
+    eng.kernel_times()               # the class totals restart with the timed region
     eng.launches()
     if world > 1:
         torch.distributed.barrier()
@@ -254,8 +274,6 @@ def run_ours(args, rank, world, local):
     # timed region: exactly --steps steps as a user runs them (graph replay),
     # starting at a list rebuild, with only the dominant class bracketed by
     # events (two event-record nodes per step)
-    istep0 = first_rebuild_step(args.warmup)
-    eng.profile_classes([dom])
     rb, pl = timed_steps(torch, stream, flush, args.steps, istep0, step, after=eng.profile_collect)
     torch.cuda.synchronize()
     if world > 1:

@@ -300,8 +300,9 @@ int qnb_set_solvent_internal(qnb_context* ctx, int32_t n, const int32_t* ij, con
                              const double* el);
 
 /* Launch-geometry autotuner (no counterpart in the reference).  Times, with
-   CUDA events over `reps` evaluations of the current lists and coordinates,
-   the candidate blocks-per-SM of each per-step kernel class and of the list
+   CUDA events over `reps` evaluations of the current lists and coordinates
+   (the evaluation's parallel branches off, so each class runs alone), the
+   candidate blocks-per-SM of each per-step kernel class and of the list
    build, one parameter at a time, and keeps the fastest.  Results are
    independent of these choices.  The Q chunk (units per fixed-point
    conversion of the Q energies, default 8) is kept: it sets the grouping of

@@ -2099,8 +2099,11 @@ int qnb_autotune(qnb_context* c, int32_t reps, int32_t* values) {
                            c->stream));
     CU(cudaStreamSynchronize(c->stream));
     collect_profile(c);
-    const bool prof0 = c->profiling, graphs0 = c->use_graphs;
+    // each candidate is timed with the evaluation's branches off: beside the
+    // other branches a kernel's span includes its wait for block slots
+    const bool prof0 = c->profiling, graphs0 = c->use_graphs, branches0 = c->branches;
     const unsigned mask0 = c->prof_mask;
+    c->branches = false;
     double ms0[K_NUM];
     int64_t n0[K_NUM];
     for (int k = 0; k < K_NUM; ++k) ms0[k] = c->prof_ms[k], n0[k] = c->prof_n[k];
@@ -2160,6 +2163,7 @@ int qnb_autotune(qnb_context* c, int32_t reps, int32_t* values) {
     c->profiling = prof0;
     c->prof_mask = mask0;
     c->use_graphs = graphs0;
+    c->branches = branches0;
     for (int k = 0; k < K_NUM; ++k) c->prof_ms[k] = ms0[k], c->prof_n[k] = n0[k];
     for (int w = 0; w < c->nwin; ++w)
         CU(cudaMemcpyAsync(c->st[w].wstate, ws.data() + wsn * w, sizeof(double) * wsn, cudaMemcpyHostToDevice,
