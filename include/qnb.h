@@ -549,9 +549,13 @@ int qnb_get_group_exclusions(qnb_context* ctx, double* out);
    lrf_taylor and temperature() test no exclusion under use_PBC); solvent
    internal pairs use the minimum image (nonbond_solvent_internal_box,
    6158-6228).  boxlength = NULL returns to the sphere (and its exclusions).
-   Not supported with a box (QNB_ERR_UNSUPPORTED): solvent restraints, and LRF
-   with iuse_switch_atom = 0 (nbpplis2_box_lrf / nbpwlis2_box_lrf).  Constant
-   pressure is the caller's; put_back_in_box: qnb_set_put_back_in_box. */
+   With iuse_switch_atom = 0 and LRF on, a unit pair with a solute group
+   feeds the LRF moments when none of its minimum-image atom pairs (a water
+   by its first atom) lies within the cut-off and one lies within RcLRF
+   (nbpplis2_box_lrf / nbpwlis2_box_lrf, 1220-1367, 2359-2491; FP64 terms in
+   both precision forms).  Not supported with a box (QNB_ERR_UNSUPPORTED):
+   solvent restraints.  Constant pressure is the caller's; put_back_in_box:
+   qnb_set_put_back_in_box. */
 int qnb_set_box(qnb_context* ctx, const double* boxlength, int32_t qswitch);
 
 /* fix_shell (src/potene.f90:386-423), evaluated inside qnb_compute_dev and

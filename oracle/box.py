@@ -303,6 +303,16 @@ def _all_groups(s):
     return [np.asarray(s.cgpatom[s.cgp_first[g]:s.cgp_last[g] + 1], np.int64) for g in range(s.ncgp)]
 
 
+def _unit_min_d2(L, x, tests):
+    """[G][G] minimum-image d2 minimised over the atom pairs of two units'
+    test atoms (tests[g]: the atoms unit g is tested by)."""
+    T = np.concatenate(tests)
+    starts = np.cumsum([0] + [len(t) for t in tests[:-1]])
+    D = d2_min_image(L, x[T][:, None, :], x[T][None, :, :])
+    D = np.minimum.reduceat(D, starts, axis=0)
+    return np.minimum.reduceat(D, starts, axis=1)
+
+
 def box_lrf(s, x, L, cut, batch=64):
     """LRF records of the box lists (cgp_centers, then the LRF branch of
     nbpplist_box_lrf 1910-2055, nbpwlist_box_lrf 2957-3085, nbwwlist_box_lrf
@@ -311,6 +321,11 @@ def box_lrf(s, x, L, cut, batch=64):
     RcLRF^2 (Rc of the pair's kind) adds the non-Q atoms of each unit to the
     other's Taylor moments about its group centre, the source shifted by
     boxlength * nint((x_switch(source) - centre(target)) / boxlength).
+    With the topology's switch-atom flag off (nbpplis2_box_lrf 1220-1367,
+    nbpwlis2_box_lrf 2359-2491) a pair with a solute group is LRF when no
+    atom pair of the two units (a water by its first atom) lies within Rc
+    and some atom pair within RcLRF; water pairs keep the first-atom test,
+    and lrf_update still shifts by the source's switch atom.
     Excluded atoms take part (the box lists do not test excl).  Returns
     [ncgp][43]: centre(3), phi0, phi1(3), phi2(3x3 row-major), phi3(9x3)."""
     x = np.asarray(x, np.float64)
@@ -319,6 +334,10 @@ def box_lrf(s, x, L, cut, batch=64):
     G, Gs, ns, sa = s.ncgp, s.ncgp_solute, s.nat_solute, s.solv_atom
     cent = np.array([x[a].mean(0) for a in groups])
     sw = np.array([int(s.cgp_iswitch[g]) if g < Gs else int(groups[g][0]) for g in range(G)], np.int64)
+    if int(s.iuse_switch_atom) == 0:   # any-atom unit tests
+        dmin = _unit_min_d2(L, x, [groups[g] if g < Gs else np.array([ns + sa * (g - Gs)]) for g in range(G)])
+    else:
+        dmin = None
     isq = np.zeros(s.natom, bool)
     isq[np.asarray(s.iqseq, np.int64)] = True
     gof = np.zeros(s.natom, np.int64)
@@ -333,7 +352,10 @@ def box_lrf(s, x, L, cut, batch=64):
     out[:, :3] = cent
     for b0 in range(0, G, batch):
         tg = np.arange(b0, min(G, b0 + batch))
-        d2 = d2_min_image(L, x[sw][None, :, :], x[sw[tg]][:, None, :])          # [target][source group]
+        if dmin is None:
+            d2 = d2_min_image(L, x[sw][None, :, :], x[sw[tg]][:, None, :])      # [target][source group]
+        else:
+            d2 = dmin[tg]
         both = solute[tg][:, None] & solute[None, :]
         none = ~solute[tg][:, None] & ~solute[None, :]
         rc2 = np.where(both, cut["Rcpp"] ** 2, np.where(none, cut["Rcww"] ** 2, cut["Rcpw"] ** 2))

@@ -3370,8 +3370,6 @@ int qnb_set_box(qnb_context* c, const double* boxlength, int32_t qswitch) {
             if (!(boxlength[k] > 0.0)) return fail(QNB_ERR_ARG, "box length %d must be positive", k);
         if (c->nqat > 0 && (qswitch < 0 || qswitch >= c->natom))
             return fail(QNB_ERR_ARG, "switching atom %d out of range", qswitch);
-        if (c->use_lrf && c->m.any_atom)
-            return fail(QNB_ERR_UNSUPPORTED, "LRF with a periodic box needs switch atoms (iuse_switch_atom 1)");
         if (c->have_solv) return fail(QNB_ERR_UNSUPPORTED, "solvent restraints are for the sphere");
         c->m.box = 1;
         c->m.box_rows = c->mixed && !c->m.any_atom ? 1 : 0;

@@ -1305,6 +1305,74 @@ __global__ void __launch_bounds__(128) k_lrf_accumulate_any(DevModel m, const De
     }
 }
 
+// Periodic box with the switch-atom flag off (nbpplis2_box_lrf /
+// nbpwlis2_box_lrf, src/nonbondene.f90:1220-1367, 2359-2491; water pairs
+// nbwwlist_box_lrf 4397-4515): a unit pair with a solute group is "LRF" when
+// none of its minimum-image atom pairs (a water by its first atom; Q and
+// excluded atoms included) lies within the pair's cut-off and one lies within
+// RcLRF; water pairs take the first-atom test.  lrf_update (628-725) shifts
+// the source by boxlength * nint((x_switch(source) - centre(target)) /
+// boxlength).  FP64 geometry and terms in both forms (this topology option
+// is off the benchmark path).  One warp per target group, lanes over the
+// source groups; the moments are summed in a fixed lane order.
+__device__ __forceinline__ void unit_pair_min_box(const DevModel& m, const double* __restrict__ x, int g1, int g2,
+                                                  double rc2, double rl2, bool& inside, bool& lrf) {
+    // a water is tested by its molecule's first atom
+    const bool w1 = g1 >= m.ncgp_solute, w2 = g2 >= m.ncgp_solute;
+    const int a0 = w1 ? 0 : m.gslot[g1], a1 = w1 ? 1 : m.gslot[g1 + 1];
+    const int b0 = w2 ? 0 : m.gslot[g2], b1 = w2 ? 1 : m.gslot[g2 + 1];
+    inside = lrf = false;
+    for (int a = a0; a < a1 && !inside; ++a) {
+        const int i = w1 ? group_dist_atom(m, g1) : m.gatom[a];
+        for (int b = b0; b < b1 && !inside; ++b) {
+            const double r2 = box_d2(m, x, i, w2 ? group_dist_atom(m, g2) : m.gatom[b]);
+            if (r2 <= rc2) inside = true;
+            else if (r2 <= rl2) lrf = true;
+        }
+    }
+}
+__global__ void __launch_bounds__(128) k_lrf_accumulate_any_box(DevModel m, const DevState* __restrict__ states,
+                                                               Cut c) {
+    const DevState& s = states[blockIdx.y];
+    const double* __restrict__ x = s.x;
+    double* __restrict__ lrf = s.lrf;
+    const int lane = threadIdx.x & 31;
+    for (int g2 = warp_id_global(); g2 < m.ncgp; g2 += warps_total()) {
+        const bool sol2 = g2 < m.ncgp_solute;
+        double* L = lrf + (size_t)g2 * kLrfLen;
+        const double cx = L[0], cy = L[1], cz = L[2];
+        double mom[kLrfMom];
+#pragma unroll
+        for (int k = 0; k < kLrfMom; ++k) mom[k] = 0.0;
+        for (int g1 = lane; g1 < m.ncgp; g1 += kWarp) {
+            if (g1 == g2) continue;
+            const bool sol1 = g1 < m.ncgp_solute;
+            const double rc2 = sol1 && sol2 ? c.rcpp2 : (sol1 || sol2 ? c.rcpw2 : c.rcww2);
+            bool inside, far;
+            unit_pair_min_box(m, x, g1, g2, rc2, c.rlrf2, inside, far);
+            if (inside || !far) continue;
+            const int s1 = group_dist_atom(m, g1);
+            const double sx = m.boxl[0] * round((x[3 * s1] - cx) * m.inv_boxl[0]);
+            const double sy = m.boxl[1] * round((x[3 * s1 + 1] - cy) * m.inv_boxl[1]);
+            const double sz = m.boxl[2] * round((x[3 * s1 + 2] - cz) * m.inv_boxl[2]);
+            for (int a = m.gslot[g1]; a < m.gslot[g1 + 1]; ++a) {
+                const int i = m.gatom[a];
+                if (m.iqatom[i] >= 0) continue;
+                lrf_terms<double>(x[3 * i] - cx - sx, x[3 * i + 1] - cy - sy, x[3 * i + 2] - cz - sz, m.crg[i], mom);
+            }
+        }
+        double tot[kLrfMom];
+#pragma unroll
+        for (int k = 0; k < kLrfMom; ++k) {
+            double v = mom[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+            tot[k] = v;
+        }
+        if (lane == 0) lrf_expand(tot, L + 3);
+    }
+}
+
 // =============================================================================
 // Force / energy kernels
 // =============================================================================
@@ -3773,6 +3841,10 @@ void launch_build_qp(const Launch& L, const uint8_t* qnear, double rcq2) {
     k_build_qp<<<dim3(1, L.nwin), 1024, 0, L.st>>>(L.m, L.ds, qnear, rcq2);
 }
 int launch_lrf_accumulate(const Launch& L, const Cut& c, int mixed, const int* lrf_src) {
+    if (L.m.any_atom && L.m.box) {
+        k_lrf_accumulate_any_box<<<grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin), 128, 0, L.st>>>(L.m, L.ds, c);
+        return 1;
+    }
     if (L.m.any_atom) {
         dim3 g = grid_for((int64_t)L.m.ncgp * 32, 128, 16, L.nwin);
         if (mixed) k_lrf_accumulate_any<true><<<g, 128, 0, L.st>>>(L.m, L.ds, c);

@@ -110,11 +110,6 @@ def test_md_in_box(sysb):
 def test_box_rejects_unsupported(sysb):
     import dataclasses
     s = sysb
-    # box LRF is the switch-atom form only (nbpplist_box_lrf, not nbpplis2_box_lrf)
-    with NonbondedEngine(dataclasses.replace(s, iuse_switch_atom=0), precision=PREC_FP64, use_lrf=True,
-                         windows=1) as e:
-        with pytest.raises(QnbError):
-            e.set_box(BOX)
     with NonbondedEngine(s, precision=PREC_FP64, use_lrf=False, windows=1) as e:
         e.set_box(BOX)
         e.set_coordinates_dev(s.x[None])

@@ -10,7 +10,9 @@ sums) within 2e-5; energies and gradient as the other box tests.  Moving
 whole groups and waters by lattice vectors leaves the LRF energy unchanged.
 Excluded atoms take part in a box like any other atom (the box lists,
 lrf_taylor under use_PBC and temperature() test no exclusion).  Solvent
-internal pairs use the minimum image (nonbond_solvent_internal_box)."""
+internal pairs use the minimum image (nonbond_solvent_internal_box).  With
+the switch-atom flag off the any-atom selection (nbpplis2_box_lrf /
+nbpwlis2_box_lrf) feeds the moments."""
 import dataclasses
 
 import numpy as np
@@ -80,6 +82,30 @@ def test_box_lrf_matches_oracle(sysb, prec, rtol, etol):
     err = np.abs(rec[:, 3:] - recr[:, 3:]) / record_scale(recr)
     assert err.max() <= rtol, (prec, err.max())
     assert abs(Er["lrf"]) > 1.0
+    for k in Er:
+        assert E[0][k] == pytest.approx(Er[k], rel=etol, abs=etol * 10), k
+    np.testing.assert_allclose(EQ[0], EQr, rtol=etol, atol=etol * 10)
+    scale = np.abs(dr).max()
+    assert np.abs(d[0] - dr).max() < etol * 10 * scale
+
+
+@pytest.mark.parametrize("prec,etol", [(PREC_FP64, 1e-10), (PREC_MIXED, 1e-4)])
+def test_any_atom_box_lrf_matches_oracle(sysb, prec, etol):
+    """Switch-atom flag off (nbpplis2_box_lrf / nbpwlis2_box_lrf): a unit pair
+    feeds the LRF moments when no minimum-image atom pair is within the
+    cut-off and one is within RcLRF.  The records are FP64 in both forms
+    (1e-10 of each coefficient's scale); they differ from the switch-atom
+    selection's on this system."""
+    s = dataclasses.replace(sysb, iuse_switch_atom=0)
+    rng = np.random.default_rng(23)
+    x = s.x + rng.normal(0, 0.03, s.x.shape)
+    lam = lambdas_for_window(0.75, 2)
+    d, E, EQ, rec = device(s, prec, [x], [lam])
+    dr, Er, EQr, recr = reference(s, x, lam)
+    np.testing.assert_allclose(rec[:, :3], recr[:, :3], rtol=0, atol=1e-12)
+    err = np.abs(rec[:, 3:] - recr[:, 3:]) / record_scale(recr)
+    assert err.max() <= 1e-10, (prec, err.max())
+    assert np.abs(box_lrf(sysb, x, BOX, OCUT)[:, 3:] - recr[:, 3:]).max() > 1e-6
     for k in Er:
         assert E[0][k] == pytest.approx(Er[k], rel=etol, abs=etol * 10), k
     np.testing.assert_allclose(EQ[0], EQr, rtol=etol, atol=etol * 10)
